@@ -1,0 +1,187 @@
+/* sphgpu.h — C ABI of the GB300 (sm_103a) implementation of OpenSPH's per-step hot path.
+ *
+ * One handle owns the particle state of one simulation, resident in HBM, and one CUDA stream. The entry
+ * points below replace the reference's per-step C++ interfaces; the reference-side adaptor classes that
+ * forward to them are shown in INTEGRATION.md. Every function returns an sphgpu_status (0 = success); no
+ * C++ exception crosses this boundary. Handles are not re-entrant: one host thread per handle at a time,
+ * as the reference calls ISolver/ITimeStepping from one thread (core/timestepping/ISolver.h:22-31).
+ *
+ * Units and conventions follow the reference: SI units, Vector quantities are 4 doubles {x, y, z, h}
+ * (core/objects/geometry/Vector.h), symmetric traceless tensors are 5 doubles {xx, yy, xy, xz, yz}
+ * (core/objects/geometry/TracelessTensor.h), symmetric tensors are 6 doubles {xx, yy, zz, xy, xz, yz}
+ * (core/objects/geometry/SymmetricTensor.h), index quantities are uint32 (Size).
+ */
+#ifndef SPHGPU_H
+#define SPHGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPHGPU_ABI_VERSION 1
+
+typedef enum {
+    SPHGPU_OK = 0,
+    SPHGPU_ERR_ARGUMENT = 1,    /* null pointer, size mismatch, unknown quantity, invalid setting */
+    SPHGPU_ERR_ALLOCATION = 2,  /* device or pinned-host allocation failed */
+    SPHGPU_ERR_CAPACITY = 3,    /* a device work list overflowed; sphgpu_required_capacity() says how much */
+    SPHGPU_ERR_NONFINITE = 4,   /* the device NaN/Inf scan found a non-finite value in the state */
+    SPHGPU_ERR_CUDA = 5,        /* a CUDA runtime call failed; see sphgpu_last_error() */
+    SPHGPU_ERR_STATE = 6,       /* call out of order (e.g. gravity eval before build) */
+    SPHGPU_ERR_UNSUPPORTED = 7  /* a setting the GPU path does not implement */
+} sphgpu_status;
+
+/* Quantity identifiers: the numeric values of the reference's QuantityId (core/quantities/QuantityIds.h). */
+enum {
+    SPHGPU_Q_POSITION = 0,             /* Vector; order 0 = r, 1 = v, 2 = dv/dt */
+    SPHGPU_Q_MASS = 1,                 /* double */
+    SPHGPU_Q_PRESSURE = 2,             /* double */
+    SPHGPU_Q_DENSITY = 3,              /* double; order 0, 1 */
+    SPHGPU_Q_ENERGY = 4,               /* double; order 0, 1 */
+    SPHGPU_Q_SOUND_SPEED = 5,          /* double */
+    SPHGPU_Q_DEVIATORIC_STRESS = 6,    /* traceless tensor; order 0, 1 */
+    SPHGPU_Q_DAMAGE = 10,              /* double; order 0, 1 */
+    SPHGPU_Q_EPS_MIN = 11,             /* double */
+    SPHGPU_Q_M_ZERO = 12,              /* double */
+    SPHGPU_Q_EXPLICIT_GROWTH = 13,     /* double */
+    SPHGPU_Q_N_FLAWS = 14,             /* uint32 */
+    SPHGPU_Q_STRESS_REDUCING = 16,     /* double */
+    SPHGPU_Q_VELOCITY_GRADIENT = 26,   /* symmetric tensor */
+    SPHGPU_Q_VELOCITY_DIVERGENCE = 27, /* double */
+    SPHGPU_Q_NEIGHBOR_CNT = 38,        /* uint32 */
+    SPHGPU_Q_FLAG = 42,                /* uint32 */
+    SPHGPU_Q_MATERIAL_ID = 43          /* uint32, index into sphgpu_config.materials */
+};
+
+/* Force flags: the reference's ForceEnum (core/system/Settings.h) bits used by this path. */
+enum {
+    SPHGPU_FORCE_PRESSURE = 1 << 0,
+    SPHGPU_FORCE_SOLID_STRESS = 1 << 1,
+    SPHGPU_FORCE_SELF_GRAVITY = 1 << 5
+};
+
+enum { SPHGPU_EOS_TILLOTSON = 0, SPHGPU_EOS_IDEAL_GAS = 1 };
+enum { SPHGPU_YIELDING_NONE = 0, SPHGPU_YIELDING_VON_MISES = 1 };
+enum { SPHGPU_DAMAGE_NONE = 0, SPHGPU_DAMAGE_SCALAR_GRADY_KIPP = 1 };
+enum { SPHGPU_INTEGRATOR_PREDICTOR_CORRECTOR = 0, SPHGPU_INTEGRATOR_LEAP_FROG = 1 };
+enum {
+    SPHGPU_PRECISION_FP64 = 0, /* every operation in FP64; pair terms IEEE-identical to the reference */
+    SPHGPU_PRECISION_MIXED = 1 /* FP32 cell-relative pair sums and walk, FP64 state/integrator/totals */
+};
+
+/* One material (the reference's BodySettings entries read by EosMaterial/SolidMaterial, core/sph/Materials.cpp,
+ * core/physics/Eos.cpp:198-238, core/physics/Rheology.cpp:36-83, core/physics/Damage.cpp:128-170) plus the
+ * clamping ranges of IMaterial::range (core/quantities/IMaterial.h:172). */
+typedef struct {
+    int32_t eos;
+    int32_t yielding;
+    int32_t damage;
+    int32_t reserved;
+    double density;               /* rho0 */
+    double bulk_modulus;          /* A */
+    double tillotson_nonlinear_b; /* B */
+    double tillotson_small_a;
+    double tillotson_small_b;
+    double tillotson_alpha;
+    double tillotson_beta;
+    double tillotson_sublimation; /* u0 */
+    double tillotson_energy_iv;
+    double tillotson_energy_cv;
+    double adiabatic_index;       /* ideal gas gamma */
+    double shear_modulus;
+    double elasticity_limit;
+    double melt_energy;
+    double young_modulus;
+    double density_range[2];
+    double energy_range[2];
+    double damage_range[2];
+} sphgpu_material;
+
+/* Run settings (the reference's RunSettingsId entries of the path). */
+typedef struct {
+    uint32_t particle_count;
+    uint32_t material_count;
+    const sphgpu_material* materials;
+    uint32_t forces;                   /* SPHGPU_FORCE_* */
+    int32_t adaptive_smoothing_length; /* AdaptiveSmoothingLength (1) or ConstSmoothingLength (0) */
+    double smoothing_length_range[2];
+    double av_alpha;
+    double av_beta;
+    int32_t sum_only_undamaged;
+    int32_t gravity_multipole_order;   /* 0 (monopole), 2 (quadrupole) or 3 (octupole) */
+    double gravity_constant;
+    double gravity_opening_angle;
+    uint32_t gravity_leaf_size;
+    int32_t integrator;                /* SPHGPU_INTEGRATOR_* */
+    double courant_number;
+    double max_timestep;
+    double initial_timestep;
+    int32_t precision;                 /* SPHGPU_PRECISION_* */
+    int32_t device;                    /* CUDA device ordinal */
+} sphgpu_config;
+
+typedef struct sphgpu_handle sphgpu_handle;
+
+/* Library / handle lifetime. */
+int sphgpu_abi_version(void);
+/* Replaces Factory::getSolver + ISolver::create (core/system/Factory.cpp:324, core/timestepping/ISolver.h:50):
+ * validates the settings and allocates the device state for config->particle_count particles. */
+sphgpu_status sphgpu_create(const sphgpu_config* config, sphgpu_handle** out);
+sphgpu_status sphgpu_destroy(sphgpu_handle* h);
+/* Text of the last error on this handle (or of the last failed sphgpu_create when h is NULL). */
+const char* sphgpu_last_error(const sphgpu_handle* h);
+/* The cudaStream_t all work of this handle is queued on (for callers that time or overlap it). */
+void* sphgpu_stream(sphgpu_handle* h);
+sphgpu_status sphgpu_synchronize(sphgpu_handle* h);
+
+/* State transfer: Storage::getValue/getDt/getD2t (core/quantities/Storage.h:242) across the boundary.
+ * `order` is 0 (value), 1 (first derivative) or 2 (second derivative); `count` is the particle count. */
+sphgpu_status sphgpu_set_quantity(sphgpu_handle* h, int32_t id, int32_t order, const void* src, uint64_t count);
+sphgpu_status sphgpu_get_quantity(sphgpu_handle* h, int32_t id, int32_t order, void* dst, uint64_t count);
+
+/* ISymmetricFinder::build (core/objects/finders/NeighborFinder.h:101-133) on the current positions. */
+sphgpu_status sphgpu_build_neighbors(sphgpu_handle* h);
+/* The unordered interacting-pair set {i<j : |r_i-r_j|^2 < (2*(h_i+h_j)/2)^2} of SymmetricSolver::loop
+ * (core/sph/solvers/SymmetricSolver.cpp:118-131); pairs are written as (i, j) with i < j, sorted.
+ * If *npairs on return exceeds capacity, nothing beyond capacity was written (SPHGPU_ERR_CAPACITY). */
+sphgpu_status sphgpu_get_pairs(sphgpu_handle* h, uint32_t* pair_i, uint32_t* pair_j, uint64_t capacity,
+    uint64_t* npairs);
+
+/* IGravity::build + evalSelfGravity (core/gravity/IGravity.h:16-62, core/gravity/BarnesHut.cpp:50-99):
+ * builds the k-d tree and multipole moments, then adds the self-gravity acceleration of every particle to
+ * dv (host array of 4*count doubles, may be NULL to only update the internal acceleration buffer). */
+sphgpu_status sphgpu_gravity_build(sphgpu_handle* h);
+sphgpu_status sphgpu_gravity_eval(sphgpu_handle* h, double* dv, uint64_t count);
+/* IGravity::evalAcceleration (core/gravity/BarnesHut.cpp:118-160) at npoints host points (4 doubles each). */
+sphgpu_status sphgpu_gravity_eval_points(sphgpu_handle* h, const double* points, uint64_t npoints, double* acc);
+/* StatisticsId::GRAVITY_NODES_APPROX / GRAVITY_NODES_EXACT / GRAVITY_NODE_COUNT of the last evaluation. */
+sphgpu_status sphgpu_gravity_stats(sphgpu_handle* h, uint64_t out[3]);
+
+/* ISolver::integrate (core/sph/solvers/SymmetricSolver.cpp:58-95 wrapped by GravitySolver::loop,
+ * core/sph/solvers/GravitySolver.cpp:64-91): materials initialize, gravity, pair loop, finalize. The
+ * highest derivatives are overwritten (the caller's zeroHighestDerivatives is implied). */
+sphgpu_status sphgpu_integrate(sphgpu_handle* h);
+
+/* ITimeStepping::step x nsteps (core/timestepping/TimeStepping.cpp:34-75, PredictorCorrector :272-346,
+ * LeapFrog :352-391) followed each step by the Courant criterion (core/timestepping/TimeStepCriterion.cpp:
+ * 315-356). Runs asynchronously on the handle's stream; the time step stays on the device. */
+sphgpu_status sphgpu_step(sphgpu_handle* h, uint32_t nsteps);
+sphgpu_status sphgpu_get_timestep(sphgpu_handle* h, double* dt);
+sphgpu_status sphgpu_set_timestep(sphgpu_handle* h, double dt);
+
+/* Conserved totals (core/physics/Integrals.h:62-148) as compensated FP64 device reductions:
+ * out[0..2] momentum, out[3..5] angular momentum about the origin, out[6] kinetic energy,
+ * out[7] internal energy, out[8] total mass. */
+sphgpu_status sphgpu_totals(sphgpu_handle* h, double out[9]);
+
+/* Device NaN/Inf scan of the integrated state; SPHGPU_ERR_NONFINITE with the first bad particle index. */
+sphgpu_status sphgpu_check_finite(sphgpu_handle* h, uint64_t* first_bad);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPHGPU_H */

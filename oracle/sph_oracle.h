@@ -1,0 +1,85 @@
+/* sph_oracle.h — CPU oracle of OpenSPH's per-step hot path (TEST INFRASTRUCTURE, NOT THE PRODUCT).
+ *
+ * A plain C++ restatement of the reference algorithms, used only by tests/, by __graft_entry__.smoke() and
+ * by bench.py's CPU-baseline leg to check and time the GPU library. Its settings and state layouts are the
+ * public structs of include/sphgpu.h so both sides read the same inputs. Its results are pinned against
+ * golden vectors produced by the reference itself (tests/golden/, made by tests/golden/make_golden.py from
+ * oracle/ref_driver.cpp).
+ */
+#ifndef SPH_ORACLE_H
+#define SPH_ORACLE_H
+
+#include "../include/sphgpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Host particle state. Arrays are owned by the caller; optional arrays may be NULL when the physics of the
+ * run does not use them (solid arrays without SOLID_STRESS, damage arrays without a fracture model). */
+typedef struct {
+    uint32_t n;
+    double* r;       /* 4n: x, y, z, h */
+    double* v;       /* 4n */
+    double* dv;      /* 4n */
+    double* m;
+    double* rho;
+    double* drho;
+    double* u;
+    double* du;
+    double* p;
+    double* cs;
+    double* divv;
+    uint32_t* ncnt;
+    uint32_t* flag;
+    uint32_t* mat;
+    double* S;       /* 5n: xx, yy, xy, xz, yz */
+    double* dS;      /* 5n */
+    double* gradv;   /* 6n: xx, yy, zz, xy, xz, yz */
+    double* reduce;
+    double* D;
+    double* dD;
+    double* eps_min;
+    double* m_zero;
+    double* growth;
+    uint32_t* n_flaws;
+} ora_state;
+
+/* Number of worker threads used by the parallel loops (0 = hardware concurrency). */
+void ora_set_threads(int threads);
+
+/* LUT kernels (core/sph/kernel/Kernel.h:51-188, core/sph/kernel/GravityKernel.h:35-120). */
+double ora_sph_kernel_value(double qsqr);
+double ora_sph_kernel_grad(double qsqr);
+double ora_gravity_kernel_grad(double qsqr);
+
+/* EosMaterial::initialize for one material (core/sph/Materials.cpp:47-58). */
+int ora_eos(const sphgpu_material* mat, uint64_t n, const double* rho, const double* u, double* p, double* cs);
+
+/* Interacting pair set of SymmetricSolver::loop (i < j, sorted by (i, j)). */
+int ora_pairs(uint64_t n, const double* r, uint32_t* pi, uint32_t* pj, uint64_t capacity, uint64_t* npairs);
+
+/* BarnesHut::build + evalSelfGravity, adding into dv (4n). kernel_radius 0 selects point masses (the
+ * default-constructed kernel), 2 the SPH gravity kernel of the cubic spline. stats: approx, exact, nodes. */
+int ora_gravity_bh(uint64_t n, const double* r, const double* m, double G, double theta, int order,
+    uint32_t leaf_size, int kernel_radius, double* dv, uint64_t* stats);
+/* BarnesHut::evalAcceleration at npoints points after building on the n particles. */
+int ora_gravity_points(uint64_t n, const double* r, const double* m, double G, double theta, int order,
+    uint32_t leaf_size, int kernel_radius, uint64_t npoints, const double* points, double* acc);
+/* BruteForceGravity::evalSelfGravity restricted to the targets listed in idx (all if idx is NULL). */
+int ora_gravity_direct(uint64_t n, const double* r, const double* m, double G, int kernel_radius,
+    uint64_t ntargets, const uint32_t* idx, double* acc);
+
+/* ISolver::integrate on the state (highest derivatives are overwritten). */
+int ora_integrate(const sphgpu_config* cfg, ora_state* s);
+/* nsteps of ITimeStepping::step with the Courant criterion; *dt is the step to use first and receives the
+ * next one; dts (nsteps entries, may be NULL) receives the step used by each step. */
+int ora_run(const sphgpu_config* cfg, ora_state* s, uint32_t nsteps, double* dt, double* dts);
+/* Conserved totals, same layout as sphgpu_totals. */
+int ora_totals(const ora_state* s, double out[9]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,91 @@
+"""Shared test cases: settings and initial states rebuilt from the golden fixtures of tests/golden/.
+
+Each fixture holds the reference's own initial state (after InitialConditions and ISolver::create), its
+derivatives after one ISolver::integrate ("d0_"), the state after the first step ("s1_") and after the last
+("sN_"), and the time-step sequence ("dts").
+"""
+import os
+
+import numpy as np
+
+from opensph_gb300 import abi
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+STATE_FIELDS = ["r", "v", "dv", "m", "rho", "drho", "u", "du", "p", "cs", "divv", "ncnt", "flag",
+                "S", "dS", "gradv", "reduce", "D", "dD", "eps_min", "m_zero", "growth", "n_flaws"]
+
+
+def load(name):
+    with np.load(os.path.join(GOLDEN, name + ".npz")) as f:
+        return {k: f[k] for k in f.files}
+
+
+def kind(fx):
+    return str(fx["driver_args"]).split()[0]
+
+
+def materials_of(fx):
+    k = kind(fx)
+    ranges = fx["mat_ranges"].reshape(-1, 6)
+    mats = []
+    for i, rg in enumerate(ranges):
+        if k == "sphere":
+            m = abi.basalt(yielding=abi.YIELDING_NONE, damage=abi.DAMAGE_NONE)
+        elif k == "impact":
+            m = abi.basalt()
+        elif k == "gas":
+            m = abi.ideal_gas(gamma=5.0 / 3.0, density=1.0)
+        else:
+            raise ValueError(k)
+        m.density_range[:] = rg[0:2]
+        m.energy_range[:] = rg[2:4]
+        m.damage_range[:] = rg[4:6]
+        m.young_modulus = float(fx["mat_young"][i])
+        mats.append(m)
+    return mats
+
+
+def config_of(fx, precision=abi.PRECISION_FP64):
+    k = kind(fx)
+    n = len(fx["s0_m"])
+    mats = materials_of(fx)
+    if k == "sphere":
+        return abi.make_config(n, mats, forces=abi.FORCE_PRESSURE | abi.FORCE_SELF_GRAVITY,
+                               gravity_constant=float(fx["G"][0]), precision=precision)
+    if k == "impact":
+        return abi.make_config(n, mats, forces=abi.FORCE_PRESSURE | abi.FORCE_SOLID_STRESS | abi.FORCE_SELF_GRAVITY,
+                               adaptive_h=True, gravity_constant=float(fx["G"][0]), precision=precision)
+    if k == "gas":
+        return abi.make_config(n, mats, forces=abi.FORCE_PRESSURE, integrator=abi.INTEGRATOR_LEAP_FROG,
+                               initial_timestep=1e-3, precision=precision)
+    raise ValueError(k)
+
+
+def state_of(fx, prefix="s0_"):
+    st = {}
+    for f in STATE_FIELDS:
+        key = prefix + f
+        if key in fx:
+            st[f] = fx[key].copy()
+    st["mat"] = fx["mat"].copy()
+    n = len(st["m"])
+    for f in ("divv", "ncnt"):
+        if f not in st:
+            st[f] = np.zeros(n, dtype="u4" if f == "ncnt" else "f8")
+    if "S" in st and "gradv" not in st:
+        st["gradv"] = np.zeros(6 * n)
+    return st
+
+
+def scale_err(a, b):
+    """max |a - b| / max |b| : error relative to the magnitude of the quantity over all particles."""
+    a = np.asarray(a, dtype="f8")
+    b = np.asarray(b, dtype="f8")
+    s = np.max(np.abs(b)) if b.size else 0.0
+    d = np.max(np.abs(a - b)) if b.size else 0.0
+    return d / s if s > 0 else d
+
+
+def vec3(a):
+    return np.asarray(a).reshape(-1, 4)[:, :3]

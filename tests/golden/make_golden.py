@@ -1,0 +1,61 @@
+"""Regenerates the golden fixtures of tests/golden/ from the REFERENCE implementation.
+
+Builds oracle/_ref/refdriver from the reference's own core/*.cpp sources (oracle/Makefile, target `ref`;
+needs the reference tree, by default /root/reference) and runs it in each mode below. Every fixture stores
+the reference's inputs and outputs, so the tests never need the reference itself.
+
+    python tests/golden/make_golden.py [--ref /root/reference]
+"""
+import argparse
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, HERE)
+from refbin import read_refbin  # noqa: E402
+
+# name -> refdriver arguments (mode + mode arguments)
+FIXTURES = {
+    # basalt sphere: Tillotson, Continuity + Pressure + StandardAV, BH theta 0.5 octupole, PC, Courant
+    "sphere_n1000": ["sphere", "1000", "1e4", "4", "1"],
+    # solid impact: + SolidStress (Hooke), von Mises, Grady-Kipp damage, adaptive h
+    "impact_n1200": ["impact", "1200", "5e4", "80", "5e3", "4", "5e3", "45"],
+    # ideal gas sphere + Mach-3 impactor, leap-frog, no gravity
+    "gas_n1500": ["gas", "1500", "80", "4"],
+    # gravity only: Plummer sphere, BH theta 0.5 octupole vs brute force
+    "gravity_n3000": ["gravity", "3000", "0.5", "7", "1e-3"],
+    "gravity_n3000_t07": ["gravity", "3000", "0.7", "11", "1e-2"],
+    # symmetric finder pair set (KdTree findLowerRank + SymmetricSolver filter), variable h
+    "pairs_n1500": ["pairs", "1500", "3"],
+    # Tillotson EOS values on a (rho, u) grid
+    "eos_tillotson": ["eos"],
+}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only", nargs="*")
+    args = ap.parse_args()
+    subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref", f"REF={args.ref}",
+                    f"-j{os.cpu_count() or 4}"], check=True)
+    driver = os.path.join(REPO, "oracle", "_ref", "refdriver")
+    for name, argv in FIXTURES.items():
+        if args.only and name not in args.only:
+            continue
+        with tempfile.TemporaryDirectory() as tmp:
+            out = os.path.join(tmp, "out.bin")
+            subprocess.run([driver, out] + argv, check=True)
+            data = read_refbin(out)
+        data["driver_args"] = np.array(" ".join(argv))
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **data)
+        print(name, sum(v.nbytes for v in data.values()), "bytes")
+
+
+if __name__ == "__main__":
+    main()

@@ -27,7 +27,7 @@ typedef enum {
     SPHGPU_OK = 0,
     SPHGPU_ERR_ARGUMENT = 1,    /* null pointer, size mismatch, unknown quantity, invalid setting */
     SPHGPU_ERR_ALLOCATION = 2,  /* device or pinned-host allocation failed */
-    SPHGPU_ERR_CAPACITY = 3,    /* a device work list overflowed; sphgpu_required_capacity() says how much */
+    SPHGPU_ERR_CAPACITY = 3,    /* a device work list or caller buffer was too small (see sphgpu_last_error) */
     SPHGPU_ERR_NONFINITE = 4,   /* the device NaN/Inf scan found a non-finite value in the state */
     SPHGPU_ERR_CUDA = 5,        /* a CUDA runtime call failed; see sphgpu_last_error() */
     SPHGPU_ERR_STATE = 6,       /* call out of order (e.g. gravity eval before build) */
@@ -67,6 +67,8 @@ enum { SPHGPU_EOS_TILLOTSON = 0, SPHGPU_EOS_IDEAL_GAS = 1 };
 enum { SPHGPU_YIELDING_NONE = 0, SPHGPU_YIELDING_VON_MISES = 1 };
 enum { SPHGPU_DAMAGE_NONE = 0, SPHGPU_DAMAGE_SCALAR_GRADY_KIPP = 1 };
 enum { SPHGPU_INTEGRATOR_PREDICTOR_CORRECTOR = 0, SPHGPU_INTEGRATOR_LEAP_FROG = 1 };
+/* GravityKernelEnum (core/system/Settings.h): point masses or the gravity kernel of the SPH kernel */
+enum { SPHGPU_GRAVITY_KERNEL_POINT_PARTICLES = 0, SPHGPU_GRAVITY_KERNEL_SPH_KERNEL = 1 };
 enum {
     SPHGPU_PRECISION_FP64 = 0, /* every operation in FP64; pair terms IEEE-identical to the reference */
     SPHGPU_PRECISION_MIXED = 1 /* FP32 cell-relative pair sums and walk, FP64 state/integrator/totals */
@@ -112,6 +114,8 @@ typedef struct {
     double av_beta;
     int32_t sum_only_undamaged;
     int32_t gravity_multipole_order;   /* 0 (monopole), 2 (quadrupole) or 3 (octupole) */
+    int32_t gravity_kernel;            /* SPHGPU_GRAVITY_KERNEL_* */
+    int32_t reserved0;
     double gravity_constant;
     double gravity_opening_angle;
     uint32_t gravity_leaf_size;
@@ -179,6 +183,23 @@ sphgpu_status sphgpu_totals(sphgpu_handle* h, double out[9]);
 
 /* Device NaN/Inf scan of the integrated state; SPHGPU_ERR_NONFINITE with the first bad particle index. */
 sphgpu_status sphgpu_check_finite(sphgpu_handle* h, uint64_t* first_bad);
+
+/* Phases of a step, timed with CUDA events when profiling is on; the GPU counterparts of the reference's
+ * StatisticsId::GRAVITY_BUILD_TIME, GRAVITY_EVAL_TIME and SPH_EVAL_TIME (core/system/Statistics.h:108-160,
+ * set at core/sph/solvers/GravitySolver.cpp:71-90). */
+enum {
+    SPHGPU_PHASE_PREDICT = 0,       /* predictor (or leap-frog drift) + EOS / rheology initialize */
+    SPHGPU_PHASE_GRAVITY_BUILD = 1, /* k-d tree + multipole moments */
+    SPHGPU_PHASE_GRAVITY_EVAL = 2,  /* tree walk */
+    SPHGPU_PHASE_NEIGHBORS = 3,     /* neighbour grid build + cell-sorted copies */
+    SPHGPU_PHASE_SPH_EVAL = 4,      /* pair loop + finalize + fracture model */
+    SPHGPU_PHASE_CORRECT = 5,       /* corrector (or leap-frog kick) + Courant criterion */
+    SPHGPU_PHASE_COUNT = 6
+};
+sphgpu_status sphgpu_set_profiling(sphgpu_handle* h, int32_t enabled);
+/* Device milliseconds per phase and the number of this library's kernel launches since the last call
+ * (synchronizes the stream; resets the accumulators). Either output may be NULL. */
+sphgpu_status sphgpu_phase_times(sphgpu_handle* h, double out[SPHGPU_PHASE_COUNT], uint64_t* launches);
 
 #ifdef __cplusplus
 }

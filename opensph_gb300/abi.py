@@ -48,6 +48,8 @@ DAMAGE_NONE = 0
 DAMAGE_SCALAR_GRADY_KIPP = 1
 INTEGRATOR_PREDICTOR_CORRECTOR = 0
 INTEGRATOR_LEAP_FROG = 1
+GRAVITY_KERNEL_POINT_PARTICLES = 0
+GRAVITY_KERNEL_SPH_KERNEL = 1
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
 
@@ -113,6 +115,8 @@ class Config(ctypes.Structure):
         ("av_beta", ctypes.c_double),
         ("sum_only_undamaged", ctypes.c_int32),
         ("gravity_multipole_order", ctypes.c_int32),
+        ("gravity_kernel", ctypes.c_int32),
+        ("reserved0", ctypes.c_int32),
         ("gravity_constant", ctypes.c_double),
         ("gravity_opening_angle", ctypes.c_double),
         ("gravity_leaf_size", ctypes.c_uint32),
@@ -189,6 +193,7 @@ def make_config(n, materials, forces=FORCE_PRESSURE | FORCE_SELF_GRAVITY, adapti
     c.av_beta = 3.0
     c.sum_only_undamaged = 1
     c.gravity_multipole_order = 3
+    c.gravity_kernel = GRAVITY_KERNEL_SPH_KERNEL
     c.gravity_constant = GRAVITY_CONSTANT
     c.gravity_opening_angle = 0.5
     c.gravity_leaf_size = 25

@@ -1,0 +1,968 @@
+// abi.cu — the C ABI of libsphgpu (include/sphgpu.h): handle lifetime, state transfer and the per-step
+// orchestration of the kernels (the GB300 replacement of ITimeStepping::step -> ISolver::integrate ->
+// GravitySolver::loop -> SymmetricSolver::loop, core/timestepping/TimeStepping.cpp:34-391,
+// core/sph/solvers/GravitySolver.cpp:64-91, core/sph/solvers/SymmetricSolver.cpp:58-141).
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "state.h"
+
+using namespace sphgpu;
+
+struct sphgpu_handle {
+    sphgpu_config cfg;
+    std::vector<sphgpu_material> materials;
+    Physics ph;
+    DState s;
+    Grid grid;
+    Tree tree;
+    MaterialD* d_mats = nullptr;
+    double* d_lut_sph = nullptr;   // LutKernel<3>(CubicSpline<3>) gradient table
+    double* d_lut_grav = nullptr;  // LutKernel<3>(GravityKernel<CubicSpline<3>>) gradient table
+    float* d_lut_sph_f = nullptr;
+    double* d_dt = nullptr;
+    double* d_dt_min = nullptr;
+    uint32_t* d_err = nullptr;
+    double* d_tot_partial = nullptr;
+    double* d_tot = nullptr;
+    unsigned long long* d_count = nullptr;
+    unsigned long long* h_pinned = nullptr; // small pinned scratch for device->host scalars
+    cudaStream_t stream = nullptr;
+    std::vector<void*> allocations;
+    std::string error;
+    bool gravity_current = false;
+    // profiling: device time per phase (CUDA events on the handle's stream) and own kernel launches
+    bool profiling = false;
+    std::vector<cudaEvent_t> event_pool;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> marks;
+    double phase_ms[SPHGPU_PHASE_COUNT] = { 0 };
+    unsigned long long launches = 0;
+};
+
+namespace {
+
+thread_local std::string gCreateError;
+
+sphgpu_status fail(sphgpu_handle* h, sphgpu_status code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (h) {
+        h->error = buf;
+    } else {
+        gCreateError = buf;
+    }
+    return code;
+}
+
+sphgpu_status cudaFail(sphgpu_handle* h, cudaError_t e, const char* where) {
+    return fail(h, SPHGPU_ERR_CUDA, "%s: %s", where, cudaGetErrorString(e));
+}
+
+cudaEvent_t takeEvent(sphgpu_handle* h) {
+    if (!h->event_pool.empty()) {
+        cudaEvent_t e = h->event_pool.back();
+        h->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// Scoped phase timer: records a start/end event pair on the stream when profiling is on.
+struct Phase {
+    sphgpu_handle* h;
+    int id;
+    cudaEvent_t start = nullptr;
+    Phase(sphgpu_handle* hh, int phase) : h(hh), id(phase) {
+        if (h->profiling) {
+            start = takeEvent(h);
+            cudaEventRecord(start, h->stream);
+        }
+    }
+    ~Phase() {
+        if (h->profiling && start) {
+            cudaEvent_t end = takeEvent(h);
+            cudaEventRecord(end, h->stream);
+            h->marks.push_back({ id, { start, end } });
+        }
+    }
+};
+
+#define CUDA_TRY(h, call)                                                                                        \
+    do {                                                                                                         \
+        cudaError_t e_ = (call);                                                                                 \
+        if (e_ != cudaSuccess) {                                                                                 \
+            return cudaFail(h, e_, #call);                                                                       \
+        }                                                                                                        \
+    } while (0)
+
+// ---- LUT tables: the reference's LutKernel construction (core/sph/kernel/Kernel.h:51-100) ----------------
+
+const double kPi = 3.14159265358979323846264338327950288419716939937510;
+
+double cubicGrad(double qSqr) {
+    const double norm = 1. / kPi;
+    const double q = std::sqrt(qSqr);
+    if (q == 0.) {
+        return -3. * norm;
+    }
+    if (q < 1.) {
+        const double a = 2. - q, b = 1. - q;
+        return (1. / q) * norm * (-0.75 * (a * a) + 3. * (b * b));
+    }
+    if (q < 2.) {
+        const double a = 2. - q;
+        return (1. / q) * norm * (-0.75 * (a * a));
+    }
+    return 0.;
+}
+
+double gravGrad(double qSqr) {
+    const double q = std::sqrt(qSqr);
+    if (q == 0.) {
+        return 4. / 3.;
+    }
+    if (q < 1.) {
+        return 1. / q * (4. / 3. * q - 6. / 5. * (q * q * q) + 1. / 2. * (qSqr * qSqr));
+    }
+    return 1. / q *
+           (8. / 3. * q - 3. * qSqr + 6. / 5. * (q * q * q) - 1. / 6. * (qSqr * qSqr) - 1. / (15. * qSqr));
+}
+
+template <typename F>
+std::vector<double> makeLut(F f) {
+    const double rad = 2.;
+    const double radInvSqr = 1. / (rad * rad);
+    const double qSqrToIdx = double(LUT_ENTRIES) * radInvSqr;
+    std::vector<double> out(LUT_ENTRIES + 1);
+    for (int i = 0; i < LUT_ENTRIES + 1; ++i) {
+        out[i] = f(double(i) / qSqrToIdx);
+    }
+    return out;
+}
+
+MaterialD toDevice(const sphgpu_material& m) {
+    MaterialD d;
+    d.eos = m.eos;
+    d.yielding = m.yielding;
+    d.damage = m.damage;
+    d.pad = 0;
+    d.rho0 = m.density;
+    d.A = m.bulk_modulus;
+    d.B = m.tillotson_nonlinear_b;
+    d.a = m.tillotson_small_a;
+    d.b = m.tillotson_small_b;
+    d.alpha = m.tillotson_alpha;
+    d.beta = m.tillotson_beta;
+    d.u0 = m.tillotson_sublimation;
+    d.uiv = m.tillotson_energy_iv;
+    d.ucv = m.tillotson_energy_cv;
+    d.gamma = m.adiabatic_index;
+    d.mu = m.shear_modulus;
+    d.limit = m.elasticity_limit;
+    d.u_melt = m.melt_energy;
+    d.young = m.young_modulus;
+    d.rho_lo = m.density_range[0];
+    d.rho_hi = m.density_range[1];
+    d.u_lo = m.energy_range[0];
+    d.u_hi = m.energy_range[1];
+    d.d_lo = m.damage_range[0];
+    d.d_hi = m.damage_range[1];
+    return d;
+}
+
+template <typename T>
+cudaError_t devAlloc(sphgpu_handle* h, T** p, size_t count) {
+    void* ptr = nullptr;
+    cudaError_t e = cudaMalloc(&ptr, std::max<size_t>(count * sizeof(T), 16));
+    if (e == cudaSuccess) {
+        cudaMemset(ptr, 0, std::max<size_t>(count * sizeof(T), 16));
+        h->allocations.push_back(ptr);
+        *p = static_cast<T*>(ptr);
+    }
+    return e;
+}
+
+struct QuantitySlot {
+    void* dev;     // device base pointer
+    int comps;     // components per particle
+    int bytes;     // bytes per component
+    bool soa;      // component-major on the device
+};
+
+// Maps (quantity, order) to the device buffer; dev == nullptr if the handle does not hold it.
+bool slotOf(sphgpu_handle* h, int id, int order, QuantitySlot& q) {
+    DState& s = h->s;
+    q = QuantitySlot{ nullptr, 1, 8, false };
+    switch (id) {
+    case SPHGPU_Q_POSITION:
+        q.comps = 4;
+        q.dev = order == 0 ? (void*)s.r : (order == 1 ? (void*)s.v : (order == 2 ? (void*)s.dv : nullptr));
+        return order >= 0 && order <= 2;
+    case SPHGPU_Q_MASS:
+        q.dev = s.m;
+        return order == 0;
+    case SPHGPU_Q_PRESSURE:
+        q.dev = s.p;
+        return order == 0;
+    case SPHGPU_Q_DENSITY:
+        q.dev = order == 0 ? (void*)s.rho : (void*)s.drho;
+        return order == 0 || order == 1;
+    case SPHGPU_Q_ENERGY:
+        q.dev = order == 0 ? (void*)s.u : (void*)s.du;
+        return order == 0 || order == 1;
+    case SPHGPU_Q_SOUND_SPEED:
+        q.dev = s.cs;
+        return order == 0;
+    case SPHGPU_Q_DEVIATORIC_STRESS:
+        q.comps = 5;
+        q.soa = true;
+        q.dev = order == 0 ? (void*)s.S : (void*)s.dS;
+        return order == 0 || order == 1;
+    case SPHGPU_Q_DAMAGE:
+        q.dev = order == 0 ? (void*)s.D : (void*)s.dD;
+        return order == 0 || order == 1;
+    case SPHGPU_Q_EPS_MIN:
+        q.dev = s.eps_min;
+        return order == 0;
+    case SPHGPU_Q_M_ZERO:
+        q.dev = s.m_zero;
+        return order == 0;
+    case SPHGPU_Q_EXPLICIT_GROWTH:
+        q.dev = s.growth;
+        return order == 0;
+    case SPHGPU_Q_N_FLAWS:
+        q.bytes = 4;
+        q.dev = s.n_flaws;
+        return order == 0;
+    case SPHGPU_Q_STRESS_REDUCING:
+        q.dev = s.reduce;
+        return order == 0;
+    case SPHGPU_Q_VELOCITY_GRADIENT:
+        q.comps = 6;
+        q.soa = true;
+        q.dev = s.gradv;
+        return order == 0;
+    case SPHGPU_Q_VELOCITY_DIVERGENCE:
+        q.dev = s.divv;
+        return order == 0;
+    case SPHGPU_Q_NEIGHBOR_CNT:
+        q.bytes = 4;
+        q.dev = s.ncnt;
+        return order == 0;
+    case SPHGPU_Q_FLAG:
+        q.bytes = 4;
+        q.dev = s.flag;
+        return order == 0;
+    case SPHGPU_Q_MATERIAL_ID:
+        q.bytes = 4;
+        q.dev = s.mat;
+        return order == 0;
+    default:
+        return false;
+    }
+}
+
+sphgpu_status checkDeviceError(sphgpu_handle* h) {
+    cudaError_t e = cudaMemcpyAsync(h->h_pinned, h->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) {
+        e = cudaStreamSynchronize(h->stream);
+    }
+    if (e != cudaSuccess) {
+        return cudaFail(h, e, "device error check");
+    }
+    const uint32_t err = *reinterpret_cast<uint32_t*>(h->h_pinned);
+    if (err) {
+        cudaMemsetAsync(h->d_err, 0, sizeof(uint32_t), h->stream);
+        cudaStreamSynchronize(h->stream);
+        return fail(h, SPHGPU_ERR_CAPACITY, "device work list overflow (error bits 0x%x)", err);
+    }
+    return SPHGPU_OK;
+}
+
+// gravity build + walk into s.agrav (GravitySolver::loop, first half)
+sphgpu_status evalGravity(sphgpu_handle* h) {
+    {
+        Phase ph(h, SPHGPU_PHASE_GRAVITY_BUILD);
+        cudaError_t e = treeBuild(h->s, h->tree, h->ph, h->d_err, h->stream);
+        if (e != cudaSuccess) {
+            return cudaFail(h, e, "gravity build");
+        }
+        h->launches += h->tree.launches;
+    }
+    {
+        Phase ph(h, SPHGPU_PHASE_GRAVITY_EVAL);
+        launchGravityWalk(h->s, h->tree, h->ph, h->d_lut_grav, h->d_err, h->stream);
+        h->launches += 1;
+    }
+    h->gravity_current = true;
+    return SPHGPU_OK;
+}
+
+// the derivative evaluation of ISolver::integrate after the materials were initialized
+sphgpu_status evalDerivatives(sphgpu_handle* h) {
+    if (h->ph.gravity) {
+        const sphgpu_status st = evalGravity(h);
+        if (st != SPHGPU_OK) {
+            return st;
+        }
+    }
+    {
+        Phase ph(h, SPHGPU_PHASE_NEIGHBORS);
+        launchGridBuild(h->s, h->grid, h->ph, h->stream);
+        h->launches += h->grid.launches;
+        launchGatherSorted(h->s, h->grid, h->ph, h->stream);
+        h->launches += h->grid.launches;
+    }
+    {
+        Phase ph(h, SPHGPU_PHASE_SPH_EVAL);
+        if (h->ph.precision == SPHGPU_PRECISION_MIXED) {
+            launchPairSumMixed(h->s, h->grid, h->ph, h->d_mats, h->d_lut_sph_f, h->stream);
+        } else {
+            launchPairSum64(h->s, h->grid, h->ph, h->d_mats, h->d_lut_sph, h->stream);
+        }
+        h->launches += 1;
+    }
+    return SPHGPU_OK;
+}
+
+void swapPredictions(sphgpu_handle* h) {
+    DState& s = h->s;
+    std::swap(s.dv, s.pdv);
+    std::swap(s.drho, s.pdrho);
+    std::swap(s.du, s.pdu);
+    std::swap(s.dS, s.pdS);
+    std::swap(s.dD, s.pdD);
+}
+
+sphgpu_status validate(const sphgpu_config* c) {
+    if (!c) {
+        return fail(nullptr, SPHGPU_ERR_ARGUMENT, "config is NULL");
+    }
+    if (c->material_count == 0 || !c->materials) {
+        return fail(nullptr, SPHGPU_ERR_ARGUMENT, "at least one material is required");
+    }
+    if (c->gravity_leaf_size == 0 || c->gravity_leaf_size > 32) {
+        return fail(nullptr, SPHGPU_ERR_UNSUPPORTED, "gravity_leaf_size must be in [1, 32] (got %u)",
+            c->gravity_leaf_size);
+    }
+    if ((c->forces & SPHGPU_FORCE_SELF_GRAVITY) && !(c->gravity_opening_angle > 0.)) {
+        return fail(nullptr, SPHGPU_ERR_ARGUMENT, "gravity_opening_angle must be positive");
+    }
+    if (c->gravity_multipole_order != 0 && c->gravity_multipole_order != 2 && c->gravity_multipole_order != 3) {
+        return fail(nullptr, SPHGPU_ERR_UNSUPPORTED, "gravity_multipole_order must be 0, 2 or 3");
+    }
+    if (c->integrator != SPHGPU_INTEGRATOR_PREDICTOR_CORRECTOR && c->integrator != SPHGPU_INTEGRATOR_LEAP_FROG) {
+        return fail(nullptr, SPHGPU_ERR_UNSUPPORTED, "unknown integrator %d", c->integrator);
+    }
+    if (c->precision != SPHGPU_PRECISION_FP64 && c->precision != SPHGPU_PRECISION_MIXED) {
+        return fail(nullptr, SPHGPU_ERR_UNSUPPORTED, "unknown precision %d", c->precision);
+    }
+    if (!(c->forces & SPHGPU_FORCE_PRESSURE)) {
+        return fail(nullptr, SPHGPU_ERR_UNSUPPORTED, "the pressure force is required");
+    }
+    for (uint32_t k = 0; k < c->material_count; ++k) {
+        const sphgpu_material& m = c->materials[k];
+        if (m.eos != SPHGPU_EOS_TILLOTSON && m.eos != SPHGPU_EOS_IDEAL_GAS) {
+            return fail(nullptr, SPHGPU_ERR_UNSUPPORTED, "material %u: unknown EOS %d", k, m.eos);
+        }
+        if (!(m.density > 0.)) {
+            return fail(nullptr, SPHGPU_ERR_ARGUMENT, "material %u: density must be positive", k);
+        }
+    }
+    return SPHGPU_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int sphgpu_abi_version(void) {
+    return SPHGPU_ABI_VERSION;
+}
+
+const char* sphgpu_last_error(const sphgpu_handle* h) {
+    return h ? h->error.c_str() : gCreateError.c_str();
+}
+
+sphgpu_status sphgpu_create(const sphgpu_config* config, sphgpu_handle** out) {
+    if (!out) {
+        return fail(nullptr, SPHGPU_ERR_ARGUMENT, "out is NULL");
+    }
+    *out = nullptr;
+    sphgpu_status st = validate(config);
+    if (st != SPHGPU_OK) {
+        return st;
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        return fail(nullptr, SPHGPU_ERR_CUDA, "no CUDA device available");
+    }
+    if (config->device < 0 || config->device >= ndev) {
+        return fail(nullptr, SPHGPU_ERR_ARGUMENT, "device %d out of range", config->device);
+    }
+    if (cudaSetDevice(config->device) != cudaSuccess) {
+        return fail(nullptr, SPHGPU_ERR_CUDA, "cudaSetDevice failed");
+    }
+    sphgpu_handle* h = new (std::nothrow) sphgpu_handle();
+    if (!h) {
+        return fail(nullptr, SPHGPU_ERR_ALLOCATION, "host allocation failed");
+    }
+    h->cfg = *config;
+    h->materials.assign(config->materials, config->materials + config->material_count);
+    h->cfg.materials = h->materials.data();
+    const uint32_t n = config->particle_count;
+
+    Physics& ph = h->ph;
+    std::memset(&ph, 0, sizeof(ph));
+    bool anyRheology = false, anyDamage = false;
+    for (const sphgpu_material& m : h->materials) {
+        anyRheology = anyRheology || m.yielding != SPHGPU_YIELDING_NONE;
+        anyDamage = anyDamage || (m.yielding != SPHGPU_YIELDING_NONE && m.damage != SPHGPU_DAMAGE_NONE);
+    }
+    ph.solid = (config->forces & SPHGPU_FORCE_SOLID_STRESS) ? 1 : 0;
+    ph.damage = ph.solid && anyDamage ? 1 : 0;
+    ph.gravity = (config->forces & SPHGPU_FORCE_SELF_GRAVITY) ? 1 : 0;
+    ph.adaptive_h = config->adaptive_smoothing_length ? 1 : 0;
+    ph.sum_only_undamaged = config->sum_only_undamaged ? 1 : 0;
+    ph.integrator = config->integrator;
+    ph.precision = config->precision;
+    ph.multipole_order = config->gravity_multipole_order;
+    ph.kernel_radius = config->gravity_kernel == SPHGPU_GRAVITY_KERNEL_POINT_PARTICLES ? 0 : 2;
+    ph.leaf_size = config->gravity_leaf_size;
+    ph.nmat = config->material_count;
+    ph.h_lo = config->smoothing_length_range[0];
+    ph.h_hi = config->smoothing_length_range[1];
+    ph.av_alpha = config->av_alpha;
+    ph.av_beta = config->av_beta;
+    ph.G = config->gravity_constant;
+    ph.theta_inv = config->gravity_opening_angle > 0. ? 1. / config->gravity_opening_angle : 2.;
+    ph.courant = config->courant_number;
+    ph.max_dt = config->max_timestep;
+    (void)anyRheology;
+
+    cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    DState& s = h->s;
+    s.n = n;
+    const size_t nn = std::max<uint32_t>(n, 1);
+    auto A = [&](auto** p, size_t count) {
+        if (e == cudaSuccess) {
+            e = devAlloc(h, p, count);
+        }
+    };
+    A(&s.r, nn);
+    A(&s.v, nn);
+    A(&s.dv, nn);
+    A(&s.pdv, nn);
+    A(&s.agrav, nn);
+    A(&s.m, nn);
+    A(&s.rho, nn);
+    A(&s.drho, nn);
+    A(&s.pdrho, nn);
+    A(&s.u, nn);
+    A(&s.du, nn);
+    A(&s.pdu, nn);
+    A(&s.p, nn);
+    A(&s.cs, nn);
+    A(&s.divv, nn);
+    A(&s.ncnt, nn);
+    A(&s.flag, nn);
+    A(&s.mat, nn);
+    if (ph.solid) {
+        A(&s.S, 5 * nn);
+        A(&s.dS, 5 * nn);
+        A(&s.pdS, 5 * nn);
+        A(&s.gradv, 6 * nn);
+        A(&s.reduce, nn);
+    }
+    if (ph.damage) {
+        A(&s.D, nn);
+        A(&s.dD, nn);
+        A(&s.pdD, nn);
+        A(&s.eps_min, nn);
+        A(&s.m_zero, nn);
+        A(&s.growth, nn);
+        A(&s.n_flaws, nn);
+    }
+    A(&h->d_mats, h->materials.size());
+    A(&h->d_lut_sph, LUT_ENTRIES + 1);
+    A(&h->d_lut_grav, LUT_ENTRIES + 1);
+    A(&h->d_lut_sph_f, LUT_ENTRIES + 1);
+    A(&h->d_dt, 1);
+    A(&h->d_dt_min, 1);
+    A(&h->d_err, 1);
+    A(&h->d_tot_partial, 256 * 9);
+    A(&h->d_tot, 9);
+    A(&h->d_count, 2);
+    if (e == cudaSuccess) {
+        e = cudaMallocHost((void**)&h->h_pinned, 64 * sizeof(unsigned long long));
+    }
+    if (e == cudaSuccess) {
+        e = gridAllocate(h->grid, n, ph.solid != 0);
+    }
+    if (e == cudaSuccess && ph.gravity) {
+        e = treeAllocate(h->tree, n, ph.leaf_size);
+    }
+    if (e != cudaSuccess) {
+        const std::string msg = std::string("device allocation failed: ") + cudaGetErrorString(e);
+        sphgpu_destroy(h);
+        cudaGetLastError();
+        return fail(nullptr, SPHGPU_ERR_ALLOCATION, "%s", msg.c_str());
+    }
+    std::vector<MaterialD> md;
+    for (const sphgpu_material& m : h->materials) {
+        md.push_back(toDevice(m));
+    }
+    const std::vector<double> lutS = makeLut(cubicGrad);
+    const std::vector<double> lutG = makeLut(gravGrad);
+    std::vector<float> lutSf(lutS.begin(), lutS.end());
+    const double dt0 = config->initial_timestep;
+    const double big = 1.7976931348623157e308;
+    e = cudaMemcpy(h->d_mats, md.data(), md.size() * sizeof(MaterialD), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        e = cudaMemcpy(h->d_lut_sph, lutS.data(), lutS.size() * sizeof(double), cudaMemcpyHostToDevice);
+    }
+    if (e == cudaSuccess) {
+        e = cudaMemcpy(h->d_lut_grav, lutG.data(), lutG.size() * sizeof(double), cudaMemcpyHostToDevice);
+    }
+    if (e == cudaSuccess) {
+        e = cudaMemcpy(h->d_lut_sph_f, lutSf.data(), lutSf.size() * sizeof(float), cudaMemcpyHostToDevice);
+    }
+    if (e == cudaSuccess) {
+        e = cudaMemcpy(h->d_dt, &dt0, sizeof(double), cudaMemcpyHostToDevice);
+    }
+    if (e == cudaSuccess) {
+        e = cudaMemcpy(h->d_dt_min, &big, sizeof(double), cudaMemcpyHostToDevice);
+    }
+    if (e == cudaSuccess) {
+        // reference defaults: every particle has STRESS_REDUCING = 1 (VonMisesRheology::create)
+        if (s.reduce) {
+            std::vector<double> ones(nn, 1.);
+            e = cudaMemcpy(s.reduce, ones.data(), nn * sizeof(double), cudaMemcpyHostToDevice);
+        }
+    }
+    if (e == cudaSuccess) {
+        e = cudaDeviceSynchronize();
+    }
+    if (e != cudaSuccess) {
+        const std::string msg = cudaGetErrorString(e);
+        sphgpu_destroy(h);
+        return fail(nullptr, SPHGPU_ERR_CUDA, "initialisation failed: %s", msg.c_str());
+    }
+    *out = h;
+    return SPHGPU_OK;
+}
+
+sphgpu_status sphgpu_destroy(sphgpu_handle* h) {
+    if (!h) {
+        return SPHGPU_OK;
+    }
+    if (h->stream) {
+        cudaStreamSynchronize(h->stream);
+    }
+    for (void* p : h->allocations) {
+        cudaFree(p);
+    }
+    for (auto& m : h->marks) {
+        cudaEventDestroy(m.second.first);
+        cudaEventDestroy(m.second.second);
+    }
+    for (cudaEvent_t e : h->event_pool) {
+        cudaEventDestroy(e);
+    }
+    gridFree(h->grid);
+    treeFree(h->tree);
+    if (h->h_pinned) {
+        cudaFreeHost(h->h_pinned);
+    }
+    if (h->stream) {
+        cudaStreamDestroy(h->stream);
+    }
+    delete h;
+    return SPHGPU_OK;
+}
+
+void* sphgpu_stream(sphgpu_handle* h) {
+    return h ? (void*)h->stream : nullptr;
+}
+
+sphgpu_status sphgpu_synchronize(sphgpu_handle* h) {
+    if (!h) {
+        return SPHGPU_ERR_ARGUMENT;
+    }
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return SPHGPU_OK;
+}
+
+sphgpu_status sphgpu_set_quantity(sphgpu_handle* h, int32_t id, int32_t order, const void* src, uint64_t count) {
+    if (!h || !src) {
+        return h ? fail(h, SPHGPU_ERR_ARGUMENT, "NULL source") : SPHGPU_ERR_ARGUMENT;
+    }
+    QuantitySlot q;
+    if (!slotOf(h, id, order, q)) {
+        return fail(h, SPHGPU_ERR_ARGUMENT, "unknown quantity %d (order %d)", id, order);
+    }
+    if (!q.dev) {
+        return fail(h, SPHGPU_ERR_ARGUMENT, "quantity %d is not used by the configured physics", id);
+    }
+    if (count != h->s.n) {
+        return fail(h, SPHGPU_ERR_ARGUMENT, "quantity %d: %llu values given for %u particles", id,
+            (unsigned long long)count, h->s.n);
+    }
+    const size_t n = count;
+    if (q.soa) {
+        const double* a = static_cast<const double*>(src);
+        std::vector<double> t(n * q.comps);
+        for (size_t i = 0; i < n; ++i) {
+            for (int c = 0; c < q.comps; ++c) {
+                t[c * n + i] = a[i * q.comps + c];
+            }
+        }
+        CUDA_TRY(h, cudaMemcpyAsync(q.dev, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    } else {
+        CUDA_TRY(h, cudaMemcpyAsync(q.dev, src, n * q.comps * q.bytes, cudaMemcpyHostToDevice, h->stream));
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    }
+    h->gravity_current = false;
+    return SPHGPU_OK;
+}
+
+sphgpu_status sphgpu_get_quantity(sphgpu_handle* h, int32_t id, int32_t order, void* dst, uint64_t count) {
+    if (!h || !dst) {
+        return h ? fail(h, SPHGPU_ERR_ARGUMENT, "NULL destination") : SPHGPU_ERR_ARGUMENT;
+    }
+    QuantitySlot q;
+    if (!slotOf(h, id, order, q) || !q.dev) {
+        return fail(h, SPHGPU_ERR_ARGUMENT, "quantity %d (order %d) is not held by this handle", id, order);
+    }
+    if (count != h->s.n) {
+        return fail(h, SPHGPU_ERR_ARGUMENT, "quantity %d: room for %llu values, %u particles", id,
+            (unsigned long long)count, h->s.n);
+    }
+    const size_t n = count;
+    if (q.soa) {
+        std::vector<double> t(n * q.comps);
+        CUDA_TRY(h, cudaMemcpyAsync(t.data(), q.dev, t.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        double* a = static_cast<double*>(dst);
+        for (size_t i = 0; i < n; ++i) {
+            for (int c = 0; c < q.comps; ++c) {
+                a[i * q.comps + c] = t[c * n + i];
+            }
+        }
+    } else {
+        CUDA_TRY(h, cudaMemcpyAsync(dst, q.dev, n * q.comps * q.bytes, cudaMemcpyDeviceToHost, h->stream));
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    }
+    return SPHGPU_OK;
+}
+
+sphgpu_status sphgpu_build_neighbors(sphgpu_handle* h) {
+    if (!h) {
+        return SPHGPU_ERR_ARGUMENT;
+    }
+    launchGridBuild(h->s, h->grid, h->ph, h->stream);
+    launchGatherSorted(h->s, h->grid, h->ph, h->stream);
+    CUDA_TRY(h, cudaGetLastError());
+    return SPHGPU_OK;
+}
+
+sphgpu_status sphgpu_get_pairs(sphgpu_handle* h, uint32_t* pair_i, uint32_t* pair_j, uint64_t capacity,
+    uint64_t* npairs) {
+    if (!h || !npairs || (capacity && (!pair_i || !pair_j))) {
+        return h ? fail(h, SPHGPU_ERR_ARGUMENT, "invalid pair buffers") : SPHGPU_ERR_ARGUMENT;
+    }
+    const sphgpu_status st = sphgpu_build_neighbors(h);
+    if (st != SPHGPU_OK) {
+        return st;
+    }
+    launchCountPairs(h->s, h->grid, h->d_count, h->stream);
+    CUDA_TRY(h, cudaMemcpyAsync(h->h_pinned, h->d_count, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+        h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    const unsigned long long total = h->h_pinned[0];
+    *npairs = total;
+    if (total > capacity) {
+        return fail(h, SPHGPU_ERR_CAPACITY, "%llu pairs, capacity %llu", total, (unsigned long long)capacity);
+    }
+    if (total == 0) {
+        return SPHGPU_OK;
+    }
+    uint32_t* dpi = nullptr;
+    uint32_t* dpj = nullptr;
+    CUDA_TRY(h, cudaMalloc(&dpi, total * sizeof(uint32_t)));
+    cudaError_t e = cudaMalloc(&dpj, total * sizeof(uint32_t));
+    if (e != cudaSuccess) {
+        cudaFree(dpi);
+        return cudaFail(h, e, "pair buffer");
+    }
+    launchListPairs(h->s, h->grid, dpi, dpj, h->d_count, total, h->stream);
+    std::vector<uint32_t> a(total), b(total);
+    e = cudaMemcpyAsync(a.data(), dpi, total * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) {
+        e = cudaMemcpyAsync(b.data(), dpj, total * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream);
+    }
+    if (e == cudaSuccess) {
+        e = cudaStreamSynchronize(h->stream);
+    }
+    cudaFree(dpi);
+    cudaFree(dpj);
+    if (e != cudaSuccess) {
+        return cudaFail(h, e, "pair list");
+    }
+    std::vector<uint64_t> key(total);
+    for (size_t k = 0; k < total; ++k) {
+        key[k] = (uint64_t(a[k]) << 32) | b[k];
+    }
+    std::sort(key.begin(), key.end());
+    for (size_t k = 0; k < total; ++k) {
+        pair_i[k] = uint32_t(key[k] >> 32);
+        pair_j[k] = uint32_t(key[k] & 0xffffffffu);
+    }
+    return SPHGPU_OK;
+}
+
+sphgpu_status sphgpu_gravity_build(sphgpu_handle* h) {
+    if (!h) {
+        return SPHGPU_ERR_ARGUMENT;
+    }
+    if (!h->ph.gravity) {
+        return fail(h, SPHGPU_ERR_STATE, "self-gravity is not enabled in the configuration");
+    }
+    cudaError_t e = treeBuild(h->s, h->tree, h->ph, h->d_err, h->stream);
+    if (e != cudaSuccess) {
+        return cudaFail(h, e, "gravity build");
+    }
+    return checkDeviceError(h);
+}
+
+sphgpu_status sphgpu_gravity_eval(sphgpu_handle* h, double* dv, uint64_t count) {
+    if (!h) {
+        return SPHGPU_ERR_ARGUMENT;
+    }
+    if (!h->ph.gravity || !h->tree.built) {
+        return fail(h, SPHGPU_ERR_STATE, "gravity_eval before gravity_build");
+    }
+    if (dv && count != h->s.n) {
+        return fail(h, SPHGPU_ERR_ARGUMENT, "dv holds %llu particles, state has %u", (unsigned long long)count,
+            h->s.n);
+    }
+    launchGravityWalk(h->s, h->tree, h->ph, h->d_lut_grav, h->d_err, h->stream);
+    CUDA_TRY(h, cudaGetLastError());
+    const sphgpu_status st = checkDeviceError(h);
+    if (st != SPHGPU_OK) {
+        return st;
+    }
+    if (dv) {
+        std::vector<double> a(size_t(h->s.n) * 4);
+        CUDA_TRY(h, cudaMemcpyAsync(a.data(), h->s.agrav, a.size() * sizeof(double), cudaMemcpyDeviceToHost,
+            h->stream));
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        for (size_t i = 0; i < size_t(h->s.n); ++i) {
+            for (int c = 0; c < 3; ++c) {
+                dv[4 * i + c] += a[4 * i + c];
+            }
+        }
+    }
+    return SPHGPU_OK;
+}
+
+sphgpu_status sphgpu_gravity_eval_points(sphgpu_handle* h, const double* points, uint64_t npoints, double* acc) {
+    if (!h || (npoints && (!points || !acc))) {
+        return h ? fail(h, SPHGPU_ERR_ARGUMENT, "invalid point buffers") : SPHGPU_ERR_ARGUMENT;
+    }
+    if (!h->ph.gravity || !h->tree.built) {
+        return fail(h, SPHGPU_ERR_STATE, "gravity_eval_points before gravity_build");
+    }
+    if (npoints == 0) {
+        return SPHGPU_OK;
+    }
+    dbl4* dp = nullptr;
+    dbl4* da = nullptr;
+    CUDA_TRY(h, cudaMalloc(&dp, npoints * sizeof(dbl4)));
+    cudaError_t e = cudaMalloc(&da, npoints * sizeof(dbl4));
+    if (e == cudaSuccess) {
+        e = cudaMemcpyAsync(dp, points, npoints * sizeof(dbl4), cudaMemcpyHostToDevice, h->stream);
+    }
+    if (e == cudaSuccess) {
+        launchGravityPoints(h->s, h->tree, h->ph, h->d_lut_grav, dp, da, uint32_t(npoints), h->stream);
+        e = cudaMemcpyAsync(acc, da, npoints * sizeof(dbl4), cudaMemcpyDeviceToHost, h->stream);
+    }
+    if (e == cudaSuccess) {
+        e = cudaStreamSynchronize(h->stream);
+    }
+    cudaFree(dp);
+    if (da) {
+        cudaFree(da);
+    }
+    if (e != cudaSuccess) {
+        return cudaFail(h, e, "gravity points");
+    }
+    return SPHGPU_OK;
+}
+
+sphgpu_status sphgpu_gravity_stats(sphgpu_handle* h, uint64_t out[3]) {
+    if (!h || !out) {
+        return SPHGPU_ERR_ARGUMENT;
+    }
+    if (!h->ph.gravity) {
+        return fail(h, SPHGPU_ERR_STATE, "self-gravity is not enabled");
+    }
+    CUDA_TRY(h, cudaMemcpyAsync(h->h_pinned, h->tree.stats, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+        h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    out[0] = h->h_pinned[0];
+    out[1] = h->h_pinned[1];
+    out[2] = h->tree.node_count;
+    return SPHGPU_OK;
+}
+
+sphgpu_status sphgpu_integrate(sphgpu_handle* h) {
+    if (!h) {
+        return SPHGPU_ERR_ARGUMENT;
+    }
+    {
+        Phase ph(h, SPHGPU_PHASE_PREDICT);
+        launchMaterialsInit(h->s, h->ph, h->d_mats, h->stream);
+        h->launches += 1;
+    }
+    sphgpu_status st = evalDerivatives(h);
+    if (st != SPHGPU_OK) {
+        return st;
+    }
+    CUDA_TRY(h, cudaGetLastError());
+    return checkDeviceError(h);
+}
+
+sphgpu_status sphgpu_step(sphgpu_handle* h, uint32_t nsteps) {
+    if (!h) {
+        return SPHGPU_ERR_ARGUMENT;
+    }
+    for (uint32_t k = 0; k < nsteps; ++k) {
+        const bool lf = h->ph.integrator == SPHGPU_INTEGRATOR_LEAP_FROG;
+        {
+            Phase ph(h, SPHGPU_PHASE_PREDICT);
+            if (lf) {
+                launchLeapFrogDriftInit(h->s, h->ph, h->d_mats, h->d_dt, h->stream);
+            } else {
+                launchPredict(h->s, h->ph, h->d_mats, h->d_dt, h->stream);
+                swapPredictions(h);
+            }
+            h->launches += 1;
+        }
+        sphgpu_status st = evalDerivatives(h);
+        if (st != SPHGPU_OK) {
+            return st;
+        }
+        {
+            Phase ph(h, SPHGPU_PHASE_CORRECT);
+            if (lf) {
+                launchLeapFrogKick(h->s, h->ph, h->d_mats, h->d_dt, h->d_dt_min, h->stream);
+            } else {
+                launchCorrect(h->s, h->ph, h->d_mats, h->d_dt, h->d_dt_min, h->stream);
+            }
+            launchCourantFinish(h->d_dt, h->d_dt_min, h->ph.max_dt, h->stream);
+            h->launches += 2;
+        }
+        CUDA_TRY(h, cudaGetLastError());
+    }
+    return checkDeviceError(h);
+}
+
+sphgpu_status sphgpu_get_timestep(sphgpu_handle* h, double* dt) {
+    if (!h || !dt) {
+        return SPHGPU_ERR_ARGUMENT;
+    }
+    CUDA_TRY(h, cudaMemcpyAsync(dt, h->d_dt, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return SPHGPU_OK;
+}
+
+sphgpu_status sphgpu_set_timestep(sphgpu_handle* h, double dt) {
+    if (!h || !(dt > 0.)) {
+        return h ? fail(h, SPHGPU_ERR_ARGUMENT, "time step must be positive") : SPHGPU_ERR_ARGUMENT;
+    }
+    CUDA_TRY(h, cudaMemcpyAsync(h->d_dt, &dt, sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return SPHGPU_OK;
+}
+
+sphgpu_status sphgpu_totals(sphgpu_handle* h, double out[9]) {
+    if (!h || !out) {
+        return SPHGPU_ERR_ARGUMENT;
+    }
+    launchTotals(h->s, h->d_tot_partial, h->d_tot, h->stream);
+    CUDA_TRY(h, cudaMemcpyAsync(out, h->d_tot, 9 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return SPHGPU_OK;
+}
+
+sphgpu_status sphgpu_check_finite(sphgpu_handle* h, uint64_t* first_bad) {
+    if (!h) {
+        return SPHGPU_ERR_ARGUMENT;
+    }
+    const unsigned long long none = ~0ull;
+    CUDA_TRY(h, cudaMemcpyAsync(h->d_count, &none, sizeof(none), cudaMemcpyHostToDevice, h->stream));
+    launchCheckFinite(h->s, h->d_count, h->stream);
+    CUDA_TRY(h, cudaMemcpyAsync(h->h_pinned, h->d_count, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+        h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    const unsigned long long bad = h->h_pinned[0];
+    if (first_bad) {
+        *first_bad = bad;
+    }
+    if (bad != none) {
+        return fail(h, SPHGPU_ERR_NONFINITE, "non-finite value at particle %llu", bad);
+    }
+    return SPHGPU_OK;
+}
+
+sphgpu_status sphgpu_set_profiling(sphgpu_handle* h, int32_t enabled) {
+    if (!h) {
+        return SPHGPU_ERR_ARGUMENT;
+    }
+    h->profiling = enabled != 0;
+    return SPHGPU_OK;
+}
+
+sphgpu_status sphgpu_phase_times(sphgpu_handle* h, double out[SPHGPU_PHASE_COUNT], uint64_t* launches) {
+    if (!h) {
+        return SPHGPU_ERR_ARGUMENT;
+    }
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    for (auto& m : h->marks) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, m.second.first, m.second.second);
+        h->phase_ms[m.first] += ms;
+        h->event_pool.push_back(m.second.first);
+        h->event_pool.push_back(m.second.second);
+    }
+    h->marks.clear();
+    if (out) {
+        for (int k = 0; k < SPHGPU_PHASE_COUNT; ++k) {
+            out[k] = h->phase_ms[k];
+        }
+    }
+    if (launches) {
+        *launches = h->launches;
+    }
+    for (int k = 0; k < SPHGPU_PHASE_COUNT; ++k) {
+        h->phase_ms[k] = 0.;
+    }
+    h->launches = 0;
+    return SPHGPU_OK;
+}
+
+} // extern "C"

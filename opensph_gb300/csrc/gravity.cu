@@ -1,0 +1,1207 @@
+// gravity.cu — Barnes-Hut self-gravity in FP64 (compiled with -fmad=false).
+//
+// Replaces BarnesHut::build / evalSelfGravity / evalAcceleration (core/gravity/BarnesHut.cpp:50-175,
+// 212-489) with the k-d tree of KdTree::buildTree (core/objects/finders/KdTree.inl.h:44-160) and the
+// moments of core/gravity/Moments.h.
+//
+// Build: level-synchronous. Every segment (tree node still to split) of a level is processed by one CTA,
+// which reproduces the reference partition exactly: the two-pointer partition of the reference around the
+// box centre is equivalent to pairing the k-th element above the split (from the left) with the k-th
+// element below it (from the right) while they are out of order, which a CTA computes with block scans;
+// the sliding-midpoint steps (single extreme element moved to one side) are arg-min/arg-max reductions
+// with the reference's first-occurrence tie rule; after more than five consecutive slides the reference's
+// std::nth_element is replayed by one thread (libstdc++ introselect). Leaf membership and the order of the
+// particles inside each leaf are therefore identical to the reference's, and so are the leaf boxes and
+// centres of mass. Moments are then formed bottom-up, one launch per level.
+//
+// Walk: one warp per leaf replays the reference's dual walk along the leaf's root path: at each ancestor
+// the pending check-list entries are classified against that ancestor's box with the reference's
+// sphere-box test (core/objects/geometry/Sphere.h:70-116), so every leaf receives exactly the reference's
+// particle list and node list. Each lane owns one particle of the leaf (leaf size <= 32) and evaluates the
+// exact softened pair terms and octupole expansions as soon as the warp classifies them.
+
+#include "state.h"
+
+namespace sphgpu {
+
+namespace {
+
+constexpr int BUILD_THREADS = 256;
+constexpr int MAX_PATH = 512;
+
+struct PosView {
+    const dbl4* r;
+    __device__ __forceinline__ double val(uint32_t i, int dim) const {
+        const dbl4 p = r[i];
+        return dim == 0 ? p.x : (dim == 1 ? p.y : p.z);
+    }
+};
+
+__device__ __forceinline__ int argMax3(const double s[3]) {
+    int m = 0;
+    if (s[1] > s[m]) {
+        m = 1;
+    }
+    if (s[2] > s[m]) {
+        m = 2;
+    }
+    return m;
+}
+
+// ---------------------------------------------------------------------------------------------------------
+// libstdc++ introselect, replayed for the rare nth_element split of KdTree::buildTree (single thread)
+// ---------------------------------------------------------------------------------------------------------
+
+struct NthCtx {
+    uint32_t* a;
+    PosView pv;
+    int dim;
+    __device__ __forceinline__ bool less(uint32_t x, uint32_t y) const {
+        return pv.val(x, dim) < pv.val(y, dim);
+    }
+};
+
+__device__ void pushHeap(NthCtx& c, long first, long hole, long top, uint32_t value) {
+    long parent = (hole - 1) / 2;
+    while (hole > top && c.less(c.a[first + parent], value)) {
+        c.a[first + hole] = c.a[first + parent];
+        hole = parent;
+        parent = (hole - 1) / 2;
+    }
+    c.a[first + hole] = value;
+}
+
+__device__ void adjustHeap(NthCtx& c, long first, long hole, long len, uint32_t value) {
+    const long top = hole;
+    long second = hole;
+    while (second < (len - 1) / 2) {
+        second = 2 * (second + 1);
+        if (c.less(c.a[first + second], c.a[first + second - 1])) {
+            second--;
+        }
+        c.a[first + hole] = c.a[first + second];
+        hole = second;
+    }
+    if ((len & 1) == 0 && second == (len - 2) / 2) {
+        second = 2 * (second + 1);
+        c.a[first + hole] = c.a[first + second - 1];
+        hole = second - 1;
+    }
+    pushHeap(c, first, hole, top, value);
+}
+
+__device__ void heapSelect(NthCtx& c, long first, long middle, long last) {
+    const long len = middle - first;
+    if (len >= 2) {
+        long parent = (len - 2) / 2;
+        while (true) {
+            adjustHeap(c, first, parent, len, c.a[first + parent]);
+            if (parent == 0) {
+                break;
+            }
+            parent--;
+        }
+    }
+    for (long i = middle; i < last; ++i) {
+        if (c.less(c.a[i], c.a[first])) {
+            const uint32_t value = c.a[i];
+            c.a[i] = c.a[first];
+            adjustHeap(c, first, 0, len, value);
+        }
+    }
+}
+
+__device__ __forceinline__ void iterSwap(uint32_t* a, long x, long y) {
+    const uint32_t t = a[x];
+    a[x] = a[y];
+    a[y] = t;
+}
+
+__device__ void moveMedianToFirst(NthCtx& c, long result, long x, long y, long z) {
+    if (c.less(c.a[x], c.a[y])) {
+        if (c.less(c.a[y], c.a[z])) {
+            iterSwap(c.a, result, y);
+        } else if (c.less(c.a[x], c.a[z])) {
+            iterSwap(c.a, result, z);
+        } else {
+            iterSwap(c.a, result, x);
+        }
+    } else if (c.less(c.a[x], c.a[z])) {
+        iterSwap(c.a, result, x);
+    } else if (c.less(c.a[y], c.a[z])) {
+        iterSwap(c.a, result, z);
+    } else {
+        iterSwap(c.a, result, y);
+    }
+}
+
+__device__ long unguardedPartition(NthCtx& c, long first, long last, long pivot) {
+    while (true) {
+        while (c.less(c.a[first], c.a[pivot])) {
+            ++first;
+        }
+        --last;
+        while (c.less(c.a[pivot], c.a[last])) {
+            --last;
+        }
+        if (!(first < last)) {
+            return first;
+        }
+        iterSwap(c.a, first, last);
+        ++first;
+    }
+}
+
+__device__ void insertionSort(NthCtx& c, long first, long last) {
+    if (first == last) {
+        return;
+    }
+    for (long i = first + 1; i != last; ++i) {
+        if (c.less(c.a[i], c.a[first])) {
+            const uint32_t val = c.a[i];
+            for (long k = i; k > first; --k) {
+                c.a[k] = c.a[k - 1];
+            }
+            c.a[first] = val;
+        } else {
+            const uint32_t val = c.a[i];
+            long last2 = i, next = i - 1;
+            while (c.less(val, c.a[next])) {
+                c.a[last2] = c.a[next];
+                last2 = next;
+                --next;
+            }
+            c.a[last2] = val;
+        }
+    }
+}
+
+__device__ void nthElement(NthCtx& c, long first, long nth, long last) {
+    if (first == last || nth == last) {
+        return;
+    }
+    long n = last - first;
+    int lg = 0;
+    while (n > 1) {
+        n >>= 1;
+        ++lg;
+    }
+    int depth = 2 * lg;
+    while (last - first > 3) {
+        if (depth == 0) {
+            heapSelect(c, first, nth + 1, last);
+            iterSwap(c.a, first, nth);
+            return;
+        }
+        --depth;
+        const long mid = first + (last - first) / 2;
+        moveMedianToFirst(c, first, first + 1, mid, last - 1);
+        const long cut = unguardedPartition(c, first + 1, last, first);
+        if (cut <= nth) {
+            first = cut;
+        } else {
+            last = cut;
+        }
+    }
+    insertionSort(c, first, last);
+}
+
+// ---------------------------------------------------------------------------------------------------------
+// build
+// ---------------------------------------------------------------------------------------------------------
+
+__global__ void initRootKernel(uint32_t n, uint32_t* idx, BhSegment* seg, BhNodeGeom* geom, uint32_t* counters,
+    const unsigned long long* bounds) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        idx[i] = i;
+    }
+    if (i == 0) {
+        BhSegment s;
+        s.from = 0;
+        s.to = n;
+        s.node = 0;
+        s.sliding = 0;
+        for (int k = 0; k < 3; ++k) {
+            s.lo[k] = doubleUnflip(bounds[k]);
+            s.hi[k] = doubleUnflip(bounds[3 + k]);
+        }
+        seg[0] = s;
+        geom[0].parent = -1;
+        geom[0].level = 0;
+        counters[0] = 1;
+        counters[1] = 0;
+        counters[2] = 0;
+    }
+}
+
+__global__ void boundsOnlyKernel(const dbl4* __restrict__ r, uint32_t n, unsigned long long* b) {
+    unsigned long long mn[3] = { ~0ull, ~0ull, ~0ull }, mx[3] = { 0, 0, 0 };
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const dbl4 p = r[i];
+        const unsigned long long f[3] = { doubleFlip(p.x), doubleFlip(p.y), doubleFlip(p.z) };
+        for (int k = 0; k < 3; ++k) {
+            mn[k] = min(mn[k], f[k]);
+            mx[k] = max(mx[k], f[k]);
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        for (int k = 0; k < 3; ++k) {
+            mn[k] = min(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], off));
+            mx[k] = max(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], off));
+        }
+    }
+    if ((threadIdx.x & 31) == 0) {
+        for (int k = 0; k < 3; ++k) {
+            atomicMin(&b[k], mn[k]);
+            atomicMax(&b[3 + k], mx[k]);
+        }
+    }
+}
+
+__global__ void resetBounds6(unsigned long long* b) {
+    if (threadIdx.x < 3) {
+        b[threadIdx.x] = ~0ull;
+        b[3 + threadIdx.x] = 0ull;
+    }
+}
+
+// block-wide helpers (BUILD_THREADS threads)
+__device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t& total, uint32_t* sh) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
+        if (lane >= off) {
+            x += y;
+        }
+    }
+    if (lane == 31) {
+        sh[warp] = x;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < (BUILD_THREADS / 32) ? sh[lane] : 0;
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, w, off);
+            if (lane >= off) {
+                w += y;
+            }
+        }
+        if (lane < (BUILD_THREADS / 32)) {
+            sh[lane] = w;
+        }
+    }
+    __syncthreads();
+    const uint32_t warpOffset = warp > 0 ? sh[warp - 1] : 0;
+    total = sh[BUILD_THREADS / 32 - 1];
+    __syncthreads();
+    return warpOffset + x - v;
+}
+
+__device__ __forceinline__ uint32_t blockSum(uint32_t v, uint32_t* sh) {
+    uint32_t total;
+    blockExclusiveScan(v, total, sh);
+    return total;
+}
+
+__device__ __forceinline__ bool blockAny(bool v, int* sh) {
+    const int r = __syncthreads_or(v ? 1 : 0);
+    (void)sh;
+    return r != 0;
+}
+
+// (value, position) lexicographic minimum across the block; dir = +1 for min, -1 for max
+__device__ void blockArgExtreme(double& val, uint32_t& pos, bool isMax, double* shv, uint32_t* shp) {
+    for (int off = 16; off > 0; off >>= 1) {
+        const double ov = __shfl_xor_sync(0xffffffffu, val, off);
+        const uint32_t op = __shfl_xor_sync(0xffffffffu, pos, off);
+        const bool better = isMax ? (ov > val || (ov == val && op < pos)) : (ov < val || (ov == val && op < pos));
+        if (better) {
+            val = ov;
+            pos = op;
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        shv[warp] = val;
+        shp[warp] = pos;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < BUILD_THREADS / 32; ++w) {
+            const double ov = shv[w];
+            const uint32_t op = shp[w];
+            const bool better =
+                isMax ? (ov > shv[0] || (ov == shv[0] && op < shp[0])) : (ov < shv[0] || (ov == shv[0] && op < shp[0]));
+            if (better) {
+                shv[0] = ov;
+                shp[0] = op;
+            }
+        }
+    }
+    __syncthreads();
+    val = shv[0];
+    pos = shp[0];
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(BUILD_THREADS) splitLevelKernel(PosView pv, uint32_t* idx, uint32_t* posB,
+    uint32_t* posS, const BhSegment* segIn, uint32_t nIn, BhSegment* segOut, BhNodeGeom* geom, uint32_t* counters,
+    uint32_t* leaves, uint32_t leafSize, uint32_t nodeCapacity, uint32_t segCapacity, uint32_t* devError) {
+    __shared__ uint32_t shScan[32];
+    __shared__ double shV[32];
+    __shared__ uint32_t shP[32];
+    __shared__ int shAny[4];
+    __shared__ uint32_t shNode[2];
+    for (uint32_t sidx = blockIdx.x; sidx < nIn; sidx += gridDim.x) {
+        const BhSegment sg = segIn[sidx];
+        const uint32_t from = sg.from, to = sg.to;
+        const int node = sg.node;
+        if (to - from <= leafSize) {
+            // KdTree::addLeaf: tight box of the leaf's points
+            double lo[3] = { DBL_MAX, DBL_MAX, DBL_MAX }, hi[3] = { -DBL_MAX, -DBL_MAX, -DBL_MAX };
+            if (threadIdx.x == 0) {
+                for (uint32_t k = from; k < to; ++k) {
+                    const uint32_t i = idx[k];
+                    for (int d = 0; d < 3; ++d) {
+                        const double x = pv.val(i, d);
+                        lo[d] = fmin(lo[d], x);
+                        hi[d] = fmax(hi[d], x);
+                    }
+                }
+                BhNodeGeom& g = geom[node];
+                for (int d = 0; d < 3; ++d) {
+                    g.lo[d] = lo[d];
+                    g.hi[d] = hi[d];
+                }
+                g.left = -1;
+                g.right = -1;
+                g.from = from;
+                g.to = to;
+                const uint32_t slot = atomicAdd(&counters[2], 1u);
+                leaves[slot] = uint32_t(node);
+            }
+            __syncthreads();
+            continue;
+        }
+        // split by the dimension of largest extent of the (split) box
+        double boxSize[3];
+        for (int d = 0; d < 3; ++d) {
+            boxSize[d] = sg.hi[d] - sg.lo[d];
+        }
+        int splitIdx = argMax3(boxSize);
+        // singularity of each dimension: all values equal to the last one
+        bool diff[3] = { false, false, false };
+        for (uint32_t k = from + threadIdx.x; k < to; k += BUILD_THREADS) {
+            const uint32_t i = idx[k];
+            const uint32_t il = idx[to - 1];
+            for (int d = 0; d < 3; ++d) {
+                diff[d] = diff[d] || (pv.val(i, d) != pv.val(il, d));
+            }
+        }
+        bool nonSingular[3];
+        for (int d = 0; d < 3; ++d) {
+            nonSingular[d] = blockAny(diff[d], shAny);
+        }
+        bool degenerated = false;
+        for (int dim = 0; dim < 3; ++dim) {
+            if (!nonSingular[splitIdx]) {
+                boxSize[splitIdx] = 0.;
+                splitIdx = argMax3(boxSize);
+                if (boxSize[0] == 0. && boxSize[1] == 0. && boxSize[2] == 0.) {
+                    degenerated = true;
+                    break;
+                }
+            } else {
+                break;
+            }
+        }
+        double splitPosition = 0.5 * (sg.lo[splitIdx] + sg.hi[splitIdx]);
+        uint32_t n1;
+        bool sliding = false;
+        double lo1[3], hi1[3], lo2[3], hi2[3];
+        for (int d = 0; d < 3; ++d) {
+            lo1[d] = lo2[d] = sg.lo[d];
+            hi1[d] = hi2[d] = sg.hi[d];
+        }
+        if (sg.sliding <= 5 && !degenerated) {
+            // ranks of the elements above (B) and below (S) the split position, left to right
+            uint32_t baseB = 0, baseS = 0;
+            for (uint32_t k0 = from; k0 < to; k0 += BUILD_THREADS) {
+                const uint32_t k = k0 + threadIdx.x;
+                bool isB = false, isS = false;
+                if (k < to) {
+                    const double x = pv.val(idx[k], splitIdx);
+                    isB = x > splitPosition;
+                    isS = x < splitPosition;
+                }
+                uint32_t totB, totS;
+                const uint32_t rb = blockExclusiveScan(isB ? 1u : 0u, totB, shScan);
+                const uint32_t rs = blockExclusiveScan(isS ? 1u : 0u, totS, shScan);
+                if (isB) {
+                    posB[from + baseB + rb] = k;
+                }
+                if (isS) {
+                    posS[from + baseS + rs] = k;
+                }
+                baseB += totB;
+                baseS += totS;
+            }
+            __syncthreads();
+            const uint32_t nB = baseB, nS = baseS;
+            // K = number of (k-th B from the left, k-th S from the right) pairs that are out of order
+            const uint32_t m = min(nB, nS);
+            uint32_t cntLocal = 0;
+            for (uint32_t k = threadIdx.x; k < m; k += BUILD_THREADS) {
+                cntLocal += (posB[from + k] < posS[from + nS - 1 - k]) ? 1u : 0u;
+            }
+            const uint32_t K = blockSum(cntLocal, shScan);
+            // the two-pointer partition swaps exactly these pairs
+            for (uint32_t k = threadIdx.x; k < K; k += BUILD_THREADS) {
+                const uint32_t a = posB[from + k], b = posS[from + nS - 1 - k];
+                const uint32_t t = idx[a];
+                idx[a] = idx[b];
+                idx[b] = t;
+            }
+            __syncthreads();
+            uint32_t n1b = K < nB ? posB[from + K] : to;
+            if (K >= 1) {
+                n1b = min(n1b, posS[from + nS - K]);
+            }
+            n1 = n1b;
+            if (n1 == from || n1 == to) {
+                // sliding midpoint: move the extreme element (first occurrence) to the empty side
+                const bool isMax = (n1 == to);
+                double val = isMax ? -DBL_MAX : DBL_MAX;
+                uint32_t pos = 0xffffffffu;
+                for (uint32_t k = from + threadIdx.x; k < to; k += BUILD_THREADS) {
+                    const double x = pv.val(idx[k], splitIdx);
+                    const bool better = isMax ? (x > val || (x == val && k < pos)) : (x < val || (x == val && k < pos));
+                    if (better) {
+                        val = x;
+                        pos = k;
+                    }
+                }
+                blockArgExtreme(val, pos, isMax, shV, shP);
+                if (threadIdx.x == 0) {
+                    const uint32_t dst = isMax ? to - 1 : from;
+                    const uint32_t t = idx[dst];
+                    idx[dst] = idx[pos];
+                    idx[pos] = t;
+                }
+                __syncthreads();
+                splitPosition = val;
+                n1 = isMax ? to - 1 : from + 1;
+                sliding = true;
+            }
+            hi1[splitIdx] = splitPosition;
+            lo2[splitIdx] = splitPosition;
+        } else {
+            n1 = (from + to) >> 1;
+            if (!degenerated && threadIdx.x == 0) {
+                NthCtx c{ idx, pv, splitIdx };
+                nthElement(c, long(from), long(n1), long(to));
+            }
+            __syncthreads();
+            const double x = pv.val(idx[n1], splitIdx);
+            hi1[splitIdx] = x;
+            lo2[splitIdx] = x;
+        }
+        // inner node with two children; allocate ids and push the child segments of the next level
+        if (threadIdx.x == 0) {
+            uint32_t child = atomicAdd(&counters[0], 2u);
+            uint32_t slot = atomicAdd(&counters[1], 2u);
+            if (child + 2 > nodeCapacity || slot + 2 > segCapacity) {
+                atomicOr(devError, child + 2 > nodeCapacity ? uint32_t(DEV_ERR_NODE_CAPACITY)
+                                                            : uint32_t(DEV_ERR_SEGMENT_CAPACITY));
+                child = 0xffffffffu;
+            }
+            shNode[0] = child;
+            shNode[1] = slot;
+        }
+        __syncthreads();
+        const uint32_t child = shNode[0], slot = shNode[1];
+        if (threadIdx.x == 0 && child != 0xffffffffu) {
+            BhNodeGeom& g = geom[node];
+            g.left = int32_t(child);
+            g.right = int32_t(child + 1);
+            g.from = from;
+            g.to = to;
+            const int lvl = g.level;
+            geom[child].parent = node;
+            geom[child].level = lvl + 1;
+            geom[child + 1].parent = node;
+            geom[child + 1].level = lvl + 1;
+            const uint32_t next = sliding ? sg.sliding + 1 : 0;
+            BhSegment l, r;
+            l.from = from;
+            l.to = n1;
+            l.node = int32_t(child);
+            l.sliding = next;
+            r.from = n1;
+            r.to = to;
+            r.node = int32_t(child + 1);
+            r.sliding = next;
+            for (int d = 0; d < 3; ++d) {
+                l.lo[d] = lo1[d];
+                l.hi[d] = hi1[d];
+                r.lo[d] = lo2[d];
+                r.hi[d] = hi2[d];
+            }
+            segOut[slot] = l;
+            segOut[slot + 1] = r;
+        }
+        __syncthreads();
+    }
+}
+
+// symmetric tensor index helpers: rank 2 {xx xy xz yy yz zz}, rank 3 {xxx xxy xxz xyy xyz xzz yyy yyz yzz zzz}
+__device__ __forceinline__ int i2(int a, int b) {
+    const int lo = min(a, b), hi = max(a, b);
+    return lo == 0 ? hi : (lo == 1 ? 2 + hi : 5);
+}
+__device__ __forceinline__ int i3(int a, int b, int c) {
+    int x = a, y = b, z = c, t;
+    if (x > y) {
+        t = x;
+        x = y;
+        y = t;
+    }
+    if (y > z) {
+        t = y;
+        y = z;
+        z = t;
+    }
+    if (x > y) {
+        t = x;
+        x = y;
+        y = t;
+    }
+    // index of the sorted triple in {000 001 002 011 012 022 111 112 122 222}
+    if (x == 0) {
+        return y == 0 ? z : (y == 1 ? 2 + z : 5);
+    }
+    if (x == 1) {
+        return y == 1 ? 5 + z : 8;
+    }
+    return 9;
+}
+
+// BarnesHut::buildLeaf (core/gravity/BarnesHut.cpp:376-437), one thread per leaf
+__device__ void buildLeaf(const dbl4* __restrict__ r, const double* __restrict__ m, double G,
+    const uint32_t* __restrict__ idx, double thetaInv, BhNodeGeom& g, BhNodeMoments& mo) {
+    const uint32_t cnt = g.to - g.from;
+    for (int k = 0; k < 6; ++k) {
+        mo.q2[k] = 0.;
+    }
+    for (int k = 0; k < 10; ++k) {
+        mo.q3[k] = 0.;
+    }
+    if (cnt == 1) {
+        const uint32_t i = idx[g.from];
+        const dbl4 p = r[i];
+        g.com[0] = p.x;
+        g.com[1] = p.y;
+        g.com[2] = p.z;
+        mo.m0 = G * m[i];
+        g.r_open = 0.;
+        return;
+    }
+    double cx = 0., cy = 0., cz = 0., mLeaf = 0.;
+    for (uint32_t k = g.from; k < g.to; ++k) {
+        const uint32_t i = idx[k];
+        const dbl4 p = r[i];
+        const double mi = G * m[i];
+        cx += mi * p.x;
+        cy += mi * p.y;
+        cz += mi * p.z;
+        mLeaf += mi;
+    }
+    cx /= mLeaf;
+    cy /= mLeaf;
+    cz /= mLeaf;
+    g.com[0] = cx;
+    g.com[1] = cy;
+    g.com[2] = cz;
+    const double rmx = fmax(cx - g.lo[0], g.hi[0] - cx), rmy = fmax(cy - g.lo[1], g.hi[1] - cy),
+                 rmz = fmax(cz - g.lo[2], g.hi[2] - cz);
+    g.r_open = 2. / sqrt(3.) * thetaInv * sqrt(rmx * rmx + rmy * rmy + rmz * rmz);
+    double M2[6] = { 0, 0, 0, 0, 0, 0 }, M3[10] = { 0, 0, 0, 0, 0, 0, 0, 0, 0, 0 };
+    for (uint32_t k = g.from; k < g.to; ++k) {
+        const uint32_t i = idx[k];
+        const dbl4 p = r[i];
+        const double mi = G * m[i];
+        const double d[3] = { p.x - cx, p.y - cy, p.z - cz };
+        for (int a = 0; a < 3; ++a) {
+            for (int b = a; b < 3; ++b) {
+                M2[i2(a, b)] += (d[a] * d[b]) * mi;
+                for (int c = b; c < 3; ++c) {
+                    M3[i3(a, b, c)] += (d[a] * d[b] * d[c]) * mi;
+                }
+            }
+        }
+    }
+    const double tr = M2[0] + M2[3] + M2[5];
+    for (int a = 0; a < 3; ++a) {
+        for (int b = a; b < 3; ++b) {
+            mo.q2[i2(a, b)] = M2[i2(a, b)] + (a == b ? tr : 0.) * (-1. / 3.);
+        }
+    }
+    double T1[3];
+    for (int k = 0; k < 3; ++k) {
+        T1[k] = M3[i3(0, 0, k)] + M3[i3(1, 1, k)] + M3[i3(2, 2, k)];
+    }
+    for (int a = 0; a < 3; ++a) {
+        for (int b = a; b < 3; ++b) {
+            for (int c = b; c < 3; ++c) {
+                const double perm = (a == b ? T1[c] : 0.) + (b == c ? T1[a] : 0.) + (c == a ? T1[b] : 0.);
+                mo.q3[i3(a, b, c)] = M3[i3(a, b, c)] + perm * (-1. / 5.);
+            }
+        }
+    }
+    mo.m0 = mLeaf;
+}
+
+// parallelAxisTheorem for orders 2 and 3 (core/gravity/Moments.h:182-295), accumulated into (q2, q3)
+__device__ void shiftAdd(const BhNodeMoments& c, const double d[3], double q2[6], double q3[10]) {
+    const double Q = c.m0;
+    const double dd = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    double Qd[3];
+    for (int k = 0; k < 3; ++k) {
+        Qd[k] = c.q2[i2(k, 0)] * d[0] + c.q2[i2(k, 1)] * d[1] + c.q2[i2(k, 2)] * d[2];
+    }
+    for (int a = 0; a < 3; ++a) {
+        for (int b = a; b < 3; ++b) {
+            const double f2 = d[a] * d[b] + (a == b ? dd : 0.) * (-1. / 3.);
+            q2[i2(a, b)] += c.q2[i2(a, b)] + f2 * Q;
+            for (int cc = b; cc < 3; ++cc) {
+                const double perm = (a == b ? d[cc] : 0.) + (b == cc ? d[a] : 0.) + (cc == a ? d[b] : 0.);
+                const double f3 = d[a] * d[b] * d[cc] + perm * dd * (-1. / 5.);
+                const double pq = c.q2[i2(a, b)] * d[cc] + c.q2[i2(b, cc)] * d[a] + c.q2[i2(cc, a)] * d[b];
+                const double t2 = (a == b ? Qd[cc] : 0.) + (a == cc ? Qd[b] : 0.) + (b == cc ? Qd[a] : 0.);
+                q3[i3(a, b, cc)] += c.q3[i3(a, b, cc)] + f3 * Q + pq + (-2. / 5.) * t2;
+            }
+        }
+    }
+}
+
+__global__ void momentsLevelKernel(const dbl4* __restrict__ r, const double* __restrict__ m, double G,
+    const uint32_t* __restrict__ idx, double thetaInv, BhNodeGeom* geom, BhNodeMoments* mom, uint32_t first,
+    uint32_t last) {
+    const uint32_t id = first + blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= last) {
+        return;
+    }
+    BhNodeGeom g = geom[id];
+    BhNodeMoments mo;
+    if (g.left < 0) {
+        buildLeaf(r, m, G, idx, thetaInv, g, mo);
+    } else {
+        // BarnesHut::buildInner (core/gravity/BarnesHut.cpp:439-489)
+        const BhNodeGeom& gl = geom[g.left];
+        const BhNodeGeom& gr = geom[g.right];
+        for (int d = 0; d < 3; ++d) {
+            g.lo[d] = fmin(gl.lo[d], gr.lo[d]);
+            g.hi[d] = fmax(gl.hi[d], gr.hi[d]);
+        }
+        const BhNodeMoments& ml = mom[g.left];
+        const BhNodeMoments& mr = mom[g.right];
+        const double mt = ml.m0 + mr.m0;
+        for (int k = 0; k < 6; ++k) {
+            mo.q2[k] = 0.;
+        }
+        for (int k = 0; k < 10; ++k) {
+            mo.q3[k] = 0.;
+        }
+        if (mt == 0.) {
+            mo.m0 = 0.;
+            g.com[0] = g.com[1] = g.com[2] = 0.;
+            g.r_open = 0.;
+        } else {
+            for (int d = 0; d < 3; ++d) {
+                g.com[d] = (ml.m0 * gl.com[d] + mr.m0 * gr.com[d]) / mt;
+            }
+            const double rmx = fmax(g.com[0] - g.lo[0], g.hi[0] - g.com[0]);
+            const double rmy = fmax(g.com[1] - g.lo[1], g.hi[1] - g.com[1]);
+            const double rmz = fmax(g.com[2] - g.lo[2], g.hi[2] - g.com[2]);
+            g.r_open = 2. / sqrt(3.) * thetaInv * sqrt(rmx * rmx + rmy * rmy + rmz * rmz);
+            mo.m0 = mt;
+            const double dl[3] = { gl.com[0] - g.com[0], gl.com[1] - g.com[1], gl.com[2] - g.com[2] };
+            shiftAdd(ml, dl, mo.q2, mo.q3);
+            const double dr[3] = { gr.com[0] - g.com[0], gr.com[1] - g.com[1], gr.com[2] - g.com[2] };
+            shiftAdd(mr, dr, mo.q2, mo.q3);
+        }
+    }
+    geom[id] = g;
+    mom[id] = mo;
+}
+
+// ---------------------------------------------------------------------------------------------------------
+// evaluation helpers
+// ---------------------------------------------------------------------------------------------------------
+
+// GravityLutKernel::grad (core/sph/kernel/GravityKernel.h:69-80) of LutKernel<3>(GravityKernel<CubicSpline>)
+__device__ __forceinline__ void gravGrad(double rx, double ry, double rz, double h, const double* __restrict__ lut,
+    int kernelRadius, double& gx, double& gy, double& gz) {
+    const double hInv = 1. / h;
+    const double sx = rx * hInv, sy = ry * hInv, sz = rz * hInv;
+    const double qSqr = sx * sx + sy * sy + sz * sz;
+    const double rad = double(kernelRadius);
+    if (qSqr + SPH_EPS >= rad * rad) {
+        const double len = sqrt(rx * rx + ry * ry + rz * rz);
+        const double l3 = len * len * len;
+        gx = rx / l3;
+        gy = ry / l3;
+        gz = rz / l3;
+        return;
+    }
+    const double floatIdx = (double(LUT_ENTRIES) * (1. / (2. * 2.))) * qSqr;
+    const int idx1 = int(floatIdx);
+    const double ratio = floatIdx - double(idx1);
+    const double g = __ldg(lut + idx1) * (1. - ratio) + __ldg(lut + idx1 + 1) * ratio;
+    const double h3 = hInv * hInv * hInv;
+    gx = (h3 * rx) * g;
+    gy = (h3 * ry) * g;
+    gz = (h3 * rz) * g;
+}
+
+// evaluateGravity (core/gravity/Moments.h:336-360) at dr = r_i - com, accumulated into a
+__device__ __forceinline__ void evalMultipole(double drx, double dry, double drz, const BhNodeMoments& mo, int order,
+    double& ax, double& ay, double& az) {
+    const double invDistSqr = 1. / (drx * drx + dry * dry + drz * drz);
+    double gamma[5];
+    gamma[0] = -sqrt(invDistSqr);
+    for (int i = 1; i < 5; ++i) {
+        gamma[i] = -(2. * i - 1.) * invDistSqr * gamma[i - 1];
+    }
+    const double x[3] = { -drx, -dry, -drz };
+    double a[3] = { 0., 0., 0. };
+    if (order >= 3) {
+        double Q1[3], Q0 = 0.;
+        for (int i = 0; i < 3; ++i) {
+            double s = 0.;
+            for (int j = 0; j < 3; ++j) {
+                for (int k = 0; k < 3; ++k) {
+                    s += mo.q3[i3(i, j, k)] * x[j] * x[k];
+                }
+            }
+            Q1[i] = s * 0.5;
+            Q0 += s * x[i];
+        }
+        Q0 *= 1. / 6.;
+        for (int i = 0; i < 3; ++i) {
+            a[i] += gamma[4] * x[i] * Q0 + gamma[3] * Q1[i];
+        }
+    }
+    if (order >= 2) {
+        double Q1[3], Q0 = 0.;
+        for (int i = 0; i < 3; ++i) {
+            Q1[i] = mo.q2[i2(i, 0)] * x[0] + mo.q2[i2(i, 1)] * x[1] + mo.q2[i2(i, 2)] * x[2];
+            Q0 += Q1[i] * x[i];
+        }
+        Q0 *= 0.5;
+        for (int i = 0; i < 3; ++i) {
+            a[i] += gamma[3] * x[i] * Q0 + gamma[2] * Q1[i];
+        }
+    }
+    for (int i = 0; i < 3; ++i) {
+        a[i] += gamma[1] * x[i] * mo.m0;
+    }
+    ax += a[0];
+    ay += a[1];
+    az += a[2];
+}
+
+// Sphere::intersectsBox: 0 box outside, 1 intersection, 2 box inside the sphere
+__device__ int intersectsBox(const double p[3], double rad, const double lo[3], const double hi[3]) {
+    double l2 = 0., r2 = 0.;
+    for (int d = 0; d < 3; ++d) {
+        const double lft = fmax(lo[d] - p[d], 0.);
+        const double rgt = fmax(p[d] - hi[d], 0.);
+        l2 = d == 0 ? lft * lft : l2 + lft * lft;
+        r2 = d == 0 ? rgt * rgt : r2 + rgt * rgt;
+    }
+    const double rSqr = rad * rad;
+    const double distSqr = rSqr - l2 - r2;
+    if (!(distSqr > 0.)) {
+        return 0;
+    }
+    const double sx = hi[0] - lo[0], sy = hi[1] - lo[1], sz = hi[2] - lo[2];
+    const double vx[8] = { lo[0], lo[0] + sx, lo[0] + 0., lo[0] + 0., hi[0], hi[0] - sx, hi[0] - 0., hi[0] - 0. };
+    const double vy[8] = { lo[1], lo[1] + 0., lo[1] + sy, lo[1] + 0., hi[1], hi[1] - 0., hi[1] - sy, hi[1] - 0. };
+    const double vz[8] = { lo[2], lo[2] + 0., lo[2] + 0., lo[2] + sz, hi[2], hi[2] - 0., hi[2] - 0., hi[2] - sz };
+    for (int k = 0; k < 8; ++k) {
+        const double dx = vx[k] - p[0], dy = vy[k] - p[1], dz = vz[k] - p[2];
+        if (!(dx * dx + dy * dy + dz * dz < rSqr)) {
+            return 1;
+        }
+    }
+    return 2;
+}
+
+enum : int { CL_KEEP = 0, CL_PARTICLES = 1, CL_NODE = 2, CL_OPEN = 3 };
+
+// ---------------------------------------------------------------------------------------------------------
+// walk: one warp per leaf
+// ---------------------------------------------------------------------------------------------------------
+
+constexpr int WALK_THREADS = 128;
+
+__global__ void __launch_bounds__(WALK_THREADS) walkKernel(const dbl4* __restrict__ r,
+    const double* __restrict__ m, double G, const uint32_t* __restrict__ idx, const BhNodeGeom* __restrict__ geom,
+    const BhNodeMoments* __restrict__ mom, const uint32_t* __restrict__ leaves, uint32_t nLeaves,
+    const double* __restrict__ lut, int kernelRadius, int order, int32_t* scratch, uint32_t listCap,
+    dbl4* agrav, unsigned long long* stats, uint32_t* devError) {
+    __shared__ int32_t pathSh[WALK_THREADS / 32][MAX_PATH];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const uint32_t warpGlobal = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nWarps = (gridDim.x * blockDim.x) >> 5;
+    int32_t* listA = scratch + size_t(warpGlobal) * 2 * listCap;
+    int32_t* listB = listA + listCap;
+    int32_t* path = pathSh[wib];
+    unsigned long long nApprox = 0, nExact = 0;
+
+    for (uint32_t li = warpGlobal; li < nLeaves; li += nWarps) {
+        const int leaf = int(leaves[li]);
+        const BhNodeGeom lg = geom[leaf];
+        const uint32_t cnt = lg.to - lg.from;
+        // root path (path[0] = root ... path[depth] = leaf)
+        int depth = 0;
+        if (lane == 0) {
+            int d = 0, nd = leaf;
+            while (geom[nd].parent >= 0 && d < MAX_PATH - 1) {
+                nd = geom[nd].parent;
+                ++d;
+            }
+            depth = d;
+            nd = leaf;
+            for (int k = d; k >= 0; --k) {
+                path[k] = nd;
+                nd = geom[nd].parent;
+            }
+            if (d >= MAX_PATH - 1) {
+                atomicOr(devError, uint32_t(DEV_ERR_WALK_CAPACITY));
+            }
+        }
+        depth = __shfl_sync(0xffffffffu, depth, 0);
+        __syncwarp();
+        const bool active = uint32_t(lane) < cnt;
+        uint32_t pi = 0;
+        dbl4 ri = mkd4(0., 0., 0., 1.);
+        if (active) {
+            pi = idx[lg.from + lane];
+            ri = r[pi];
+        }
+        double ax = 0., ay = 0., az = 0.;
+        int32_t* cur = listA;
+        int32_t* nxt = listB;
+        uint32_t ncur = 0, nnxt = 0;
+        bool overflow = false;
+        for (int k = 1; k <= depth && !overflow; ++k) {
+            const int ev = path[k];
+            const int par = path[k - 1];
+            const BhNodeGeom& pg = geom[par];
+            const int sib = pg.left == ev ? pg.right : pg.left;
+            const bool evLeaf = (k == depth);
+            double elo[3], ehi[3];
+            for (int d = 0; d < 3; ++d) {
+                elo[d] = geom[ev].lo[d];
+                ehi[d] = geom[ev].hi[d];
+            }
+            if (lane == 0) {
+                cur[ncur] = sib;
+            }
+            ncur += 1;
+            __syncwarp();
+            uint32_t pos = 0;
+            while (pos < ncur) {
+                const uint32_t batch = min(32u, ncur - pos);
+                const uint32_t e = pos + lane;
+                int node = -1, cls = CL_KEEP;
+                if (uint32_t(lane) < batch) {
+                    node = cur[e];
+                    const BhNodeGeom& ng = geom[node];
+                    if (ng.r_open == 0.) {
+                        cls = CL_PARTICLES;
+                    } else {
+                        const int res = intersectsBox(ng.com, ng.r_open, elo, ehi);
+                        if (res == 2 || (evLeaf && res != 0)) {
+                            cls = ng.left < 0 ? CL_PARTICLES : CL_OPEN;
+                        } else if (res == 0) {
+                            cls = CL_NODE;
+                        } else {
+                            cls = CL_KEEP;
+                        }
+                    }
+                }
+                const unsigned mKeep = __ballot_sync(0xffffffffu, uint32_t(lane) < batch && cls == CL_KEEP);
+                const unsigned mOpen = __ballot_sync(0xffffffffu, cls == CL_OPEN);
+                const unsigned mPart = __ballot_sync(0xffffffffu, cls == CL_PARTICLES);
+                const unsigned mNode = __ballot_sync(0xffffffffu, cls == CL_NODE);
+                const unsigned below = (1u << lane) - 1u;
+                const uint32_t nOpen = __popc(mOpen), nKeep = __popc(mKeep);
+                if (ncur + 2 * nOpen > listCap || nnxt + nKeep > listCap) {
+                    overflow = true;
+                    break;
+                }
+                if (cls == CL_KEEP && uint32_t(lane) < batch) {
+                    nxt[nnxt + __popc(mKeep & below)] = node;
+                }
+                if (cls == CL_OPEN) {
+                    const uint32_t slot = ncur + 2 * __popc(mOpen & below);
+                    cur[slot] = geom[node].left;
+                    cur[slot + 1] = geom[node].right;
+                }
+                pos += batch;
+                ncur += 2 * nOpen;
+                nnxt += nKeep;
+                __syncwarp();
+                // exact pair terms with every particle of the listed leaves
+                unsigned mp = mPart;
+                while (mp) {
+                    const int src = __ffs(mp) - 1;
+                    mp &= mp - 1;
+                    const int pn = __shfl_sync(0xffffffffu, node, src);
+                    const uint32_t f0 = geom[pn].from, f1 = geom[pn].to;
+                    nExact += 1;
+                    for (uint32_t t = f0; t < f1; ++t) {
+                        const uint32_t j = idx[t];
+                        const dbl4 rj = r[j];
+                        const double mj = G * m[j];
+                        if (active) {
+                            double gx, gy, gz;
+                            gravGrad(rj.x - ri.x, rj.y - ri.y, rj.z - ri.z, 0.5 * (rj.w + ri.w), lut, kernelRadius,
+                                gx, gy, gz);
+                            ax += mj * gx;
+                            ay += mj * gy;
+                            az += mj * gz;
+                        }
+                    }
+                }
+                // multipole expansions
+                unsigned mn = mNode;
+                while (mn) {
+                    const int src = __ffs(mn) - 1;
+                    mn &= mn - 1;
+                    const int nn = __shfl_sync(0xffffffffu, node, src);
+                    nApprox += 1;
+                    if (active) {
+                        const BhNodeGeom& ng = geom[nn];
+                        evalMultipole(ri.x - ng.com[0], ri.y - ng.com[1], ri.z - ng.com[2], mom[nn], order, ax, ay, az);
+                    }
+                }
+            }
+            // the kept entries are the check list of the next ancestor
+            int32_t* t = cur;
+            cur = nxt;
+            nxt = t;
+            ncur = nnxt;
+            nnxt = 0;
+        }
+        if (overflow) {
+            if (lane == 0) {
+                atomicOr(devError, uint32_t(DEV_ERR_WALK_CAPACITY));
+            }
+            continue;
+        }
+        // intra-leaf pairs
+        for (uint32_t t = lg.from; t < lg.to; ++t) {
+            const uint32_t j = idx[t];
+            const dbl4 rj = r[j];
+            const double mj = G * m[j];
+            if (active && j != pi) {
+                double gx, gy, gz;
+                gravGrad(rj.x - ri.x, rj.y - ri.y, rj.z - ri.z, 0.5 * (rj.w + ri.w), lut, kernelRadius, gx, gy, gz);
+                ax += mj * gx;
+                ay += mj * gy;
+                az += mj * gz;
+            }
+        }
+        if (active) {
+            agrav[pi] = mkd4(ax, ay, az, 0.);
+        }
+    }
+    if (lane == 0) {
+        atomicAdd(&stats[0], nApprox);
+        atomicAdd(&stats[1], nExact);
+    }
+}
+
+// BarnesHut::evalImpl / evalExact (core/gravity/BarnesHut.cpp:118-175, 364-374): one thread per point
+__global__ void pointsKernel(const dbl4* __restrict__ r, const double* __restrict__ m, double G,
+    const uint32_t* __restrict__ idx, const BhNodeGeom* __restrict__ geom, const BhNodeMoments* __restrict__ mom,
+    const double* __restrict__ lut, int kernelRadius, int order, double thetaInv, const dbl4* pts, dbl4* acc,
+    uint32_t np) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= np) {
+        return;
+    }
+    const dbl4 p = pts[k];
+    const double thetaSqr = 1. / (thetaInv * thetaInv);
+    double ax = 0., ay = 0., az = 0.;
+    int stack[128];
+    int sp = 0;
+    stack[sp++] = 0;
+    while (sp > 0) {
+        const int id = stack[--sp];
+        const BhNodeGeom& g = geom[id];
+        const double sx = g.hi[0] - g.lo[0], sy = g.hi[1] - g.lo[1], sz = g.hi[2] - g.lo[2];
+        const double boxSizeSqr = sx * sx + sy * sy + sz * sz;
+        const double cx = 0.5 * (g.lo[0] + g.hi[0]) - p.x, cy = 0.5 * (g.lo[1] + g.hi[1]) - p.y,
+                     cz = 0.5 * (g.lo[2] + g.hi[2]) - p.z;
+        const double boxDistSqr = cx * cx + cy * cy + cz * cz;
+        const bool contains = !(p.x < g.lo[0] || p.x > g.hi[0] || p.y < g.lo[1] || p.y > g.hi[1] || p.z < g.lo[2] ||
+                                p.z > g.hi[2]);
+        if (!contains && boxSizeSqr > 0. && boxSizeSqr / (boxDistSqr + SPH_EPS) < thetaSqr) {
+            evalMultipole(p.x - g.com[0], p.y - g.com[1], p.z - g.com[2], mom[id], order, ax, ay, az);
+        } else if (g.left < 0) {
+            for (uint32_t t = g.from; t < g.to; ++t) {
+                const uint32_t i = idx[t];
+                const dbl4 ri = r[i];
+                double gx, gy, gz;
+                gravGrad(ri.x - p.x, ri.y - p.y, ri.z - p.z, ri.w, lut, kernelRadius, gx, gy, gz);
+                const double mi = G * m[i];
+                ax += mi * gx;
+                ay += mi * gy;
+                az += mi * gz;
+            }
+        } else if (sp + 2 <= 128) {
+            stack[sp++] = g.right;
+            stack[sp++] = g.left;
+        }
+    }
+    acc[k] = mkd4(ax, ay, az, 0.);
+}
+
+} // namespace
+
+cudaError_t treeAllocate(Tree& t, uint32_t n, uint32_t leafSize) {
+    const uint32_t nn = n > 0 ? n : 1;
+    t.node_capacity = 2 * nn + 8;
+    t.seg_capacity = nn + 8;
+    t.walk_warps = 152 * 8 * (WALK_THREADS / 32);
+    t.walk_capacity = 4096;
+    (void)leafSize;
+    cudaError_t e = cudaSuccess;
+    auto alloc = [&](void** p, size_t bytes) {
+        if (e == cudaSuccess) {
+            e = cudaMalloc(p, bytes > 0 ? bytes : 16);
+        }
+    };
+    alloc((void**)&t.idx, nn * sizeof(uint32_t));
+    alloc((void**)&t.scratch_b, nn * sizeof(uint32_t));
+    alloc((void**)&t.scratch_s, nn * sizeof(uint32_t));
+    alloc((void**)&t.geom, size_t(t.node_capacity) * sizeof(BhNodeGeom));
+    alloc((void**)&t.mom, size_t(t.node_capacity) * sizeof(BhNodeMoments));
+    alloc((void**)&t.seg[0], size_t(t.seg_capacity) * sizeof(BhSegment));
+    alloc((void**)&t.seg[1], size_t(t.seg_capacity) * sizeof(BhSegment));
+    alloc((void**)&t.counters, 8 * sizeof(uint32_t));
+    alloc((void**)&t.leaves, nn * sizeof(uint32_t));
+    alloc((void**)&t.walk_scratch, size_t(t.walk_warps) * 2 * t.walk_capacity * sizeof(int32_t));
+    alloc((void**)&t.stats, 4 * sizeof(unsigned long long));
+    alloc((void**)&t.bbox, 8 * sizeof(unsigned long long));
+    if (e == cudaSuccess) {
+        e = cudaMallocHost((void**)&t.counters_host, 8 * sizeof(uint32_t));
+    }
+    return e;
+}
+
+void treeFree(Tree& t) {
+    void* ptrs[] = { t.idx, t.scratch_b, t.scratch_s, t.geom, t.mom, t.seg[0], t.seg[1], t.counters, t.leaves,
+        t.walk_scratch, t.stats, t.bbox };
+    for (void* p : ptrs) {
+        if (p) {
+            cudaFree(p);
+        }
+    }
+    if (t.counters_host) {
+        cudaFreeHost(t.counters_host);
+    }
+    t = Tree();
+}
+
+cudaError_t treeBuild(const DState& s, Tree& t, const Physics& ph, uint32_t* devError, cudaStream_t st) {
+    const uint32_t n = s.n;
+    t.built = false;
+    t.level_start.clear();
+    if (n == 0) {
+        t.node_count = 0;
+        t.leaf_count = 0;
+        t.built = true;
+        return cudaSuccess;
+    }
+    // root box = bounding box of all points (KdTree::buildImpl)
+    t.launches = 3;
+    resetBounds6<<<1, 32, 0, st>>>(t.bbox);
+    boundsOnlyKernel<<<min(ceilDiv(n, 256), 152 * 8), 256, 0, st>>>(s.r, n, t.bbox);
+    initRootKernel<<<ceilDiv(n, 256), 256, 0, st>>>(n, t.idx, t.seg[0], t.geom, t.counters, t.bbox);
+    const PosView pv{ s.r };
+    uint32_t nIn = 1;
+    int cur = 0;
+    t.level_start.push_back(0);
+    t.level_start.push_back(1);
+    for (int level = 0; nIn > 0; ++level) {
+        const int grid = int(min(nIn, 152u * 16u));
+        t.launches++;
+        splitLevelKernel<<<grid, BUILD_THREADS, 0, st>>>(pv, t.idx, t.scratch_b, t.scratch_s, t.seg[cur], nIn,
+            t.seg[1 - cur], t.geom, t.counters, t.leaves, ph.leaf_size, t.node_capacity, t.seg_capacity, devError);
+        cudaMemcpyAsync(t.counters_host, t.counters, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+        cudaMemsetAsync(t.counters + 1, 0, sizeof(uint32_t), st);
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            return e;
+        }
+        nIn = t.counters_host[1];
+        t.node_count = t.counters_host[0];
+        t.leaf_count = t.counters_host[2];
+        if (nIn > 0) {
+            t.level_start.push_back(t.node_count);
+        }
+        cur = 1 - cur;
+        if (level > 100000) {
+            break;
+        }
+    }
+    // bottom-up moments, deepest level first
+    const double G = ph.G;
+    for (int L = int(t.level_start.size()) - 2; L >= 0; --L) {
+        const uint32_t first = t.level_start[L], last = t.level_start[L + 1];
+        if (last > first) {
+            t.launches++;
+            momentsLevelKernel<<<ceilDiv(last - first, 128), 128, 0, st>>>(s.r, s.m, G, t.idx, ph.theta_inv, t.geom,
+                t.mom, first, last);
+        }
+    }
+    t.built = true;
+    return cudaGetLastError();
+}
+
+void launchGravityWalk(const DState& s, Tree& t, const Physics& ph, const double* lut, uint32_t* devError,
+    cudaStream_t st) {
+    cudaMemsetAsync(t.stats, 0, 2 * sizeof(unsigned long long), st);
+    if (s.n == 0) {
+        return;
+    }
+    cudaMemsetAsync(s.agrav, 0, size_t(s.n) * sizeof(dbl4), st);
+    if (ph.leaf_size > 32) {
+        // one warp owns a leaf: larger leaves are not supported by this walk
+        return;
+    }
+    const int blocks = int(t.walk_warps / (WALK_THREADS / 32));
+    walkKernel<<<blocks, WALK_THREADS, 0, st>>>(s.r, s.m, ph.G, t.idx, t.geom, t.mom, t.leaves, t.leaf_count, lut,
+        ph.kernel_radius,
+        ph.multipole_order, t.walk_scratch, t.walk_capacity, s.agrav, t.stats, devError);
+}
+
+void launchGravityPoints(const DState& s, const Tree& t, const Physics& ph, const double* lut, const dbl4* points,
+    dbl4* acc, uint32_t npoints, cudaStream_t st) {
+    if (npoints == 0 || s.n == 0) {
+        return;
+    }
+    pointsKernel<<<ceilDiv(npoints, 128), 128, 0, st>>>(s.r, s.m, ph.G, t.idx, t.geom, t.mom, lut, ph.kernel_radius,
+        ph.multipole_order, ph.theta_inv, points, acc, npoints);
+}
+
+} // namespace sphgpu

@@ -1,0 +1,191 @@
+// sph32.cu — mixed-precision SPH pair loop (FP32 pair terms, compensated accumulation, FP64 finalize).
+//
+// Same derivative set as sph64.cu (SymmetricSolver::loop with VelocityDivergence, VelocityGradient,
+// PressureGradient, StressDivergence, StandardAV and NeighborCountTerm, core/sph/solvers/SymmetricSolver.cpp:
+// 109-141), evaluated with FP32 arithmetic on inputs prepared so that no large absolute value enters a
+// difference: positions are stored relative to the origin of their own grid cell (the pair separation is
+// then rel_i - rel_j - offset * cell, exact to FP32 rounding of a cell-sized quantity), velocities as
+// unevaluated float pairs hi + lo (the separation of two nearby velocities is exact in the hi part by the
+// Sterbenz lemma, so the FP32 difference keeps ~1e-14 relative accuracy of the FP64 inputs). Sums over
+// neighbours use Kahan compensation. Material updates, finalize and integrator stay FP64.
+
+#include "physics.cuh"
+
+namespace sphgpu {
+
+namespace {
+
+struct Kahan {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        const float y = x - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const {
+        return double(s) - double(c);
+    }
+};
+
+__device__ __forceinline__ float lutGradF(const float* __restrict__ lut, float qSqr) {
+    if (qSqr >= 4.f) {
+        return 0.f;
+    }
+    const float floatIdx = float(LUT_ENTRIES / 4) * qSqr;
+    const int idx1 = min(int(floatIdx), LUT_ENTRIES - 1);
+    const float ratio = floatIdx - float(idx1);
+    const float g0 = __ldg(lut + idx1), g1 = __ldg(lut + idx1 + 1);
+    return g0 + (g1 - g0) * ratio;
+}
+
+template <bool Solid>
+__global__ void __launch_bounds__(128) pairSumMixedKernel(DState s, Grid g, Physics ph,
+    const MaterialD* __restrict__ mats, const float* __restrict__ lut) {
+    const uint32_t n = s.n;
+    const uint32_t si = blockIdx.x * blockDim.x + threadIdx.x;
+    if (si >= n) {
+        return;
+    }
+    const GridInfo* gi = g.info;
+    const uint32_t i = g.perm[si];
+    const float4 pi0 = g.mx0[si], pi1 = g.mx1[si], pi2 = g.mx2[si], pi3 = g.mx3[si];
+    const float cellf = float(gi->cell);
+    float Sif[5] = { 0, 0, 0, 0, 0 };
+    if (Solid) {
+        for (int c = 0; c < 5; ++c) {
+            Sif[c] = g.mxS[c * n + si];
+        }
+    }
+    const float rhoiInv = 1.f / pi2.w;
+    const float alpha = float(ph.av_alpha), beta = float(ph.av_beta);
+    Kahan ax, ay, az, du, divv;
+    float gv[6] = { 0, 0, 0, 0, 0, 0 };
+    uint32_t cnt = 0;
+    const int dxc = gi->dims[0], dyc = gi->dims[1], dzc = gi->dims[2];
+    const uint32_t key = g.keys_sorted[si];
+    const int cx = int(key % uint32_t(dxc)), cy = int((key / uint32_t(dxc)) % uint32_t(dyc)),
+              cz = int(key / (uint32_t(dxc) * uint32_t(dyc)));
+    for (int oz = -1; oz <= 1; ++oz) {
+        const int z = cz + oz;
+        if (z < 0 || z >= dzc) {
+            continue;
+        }
+        for (int oy = -1; oy <= 1; ++oy) {
+            const int y = cy + oy;
+            if (y < 0 || y >= dyc) {
+                continue;
+            }
+            for (int ox = -1; ox <= 1; ++ox) {
+                const int x = cx + ox;
+                if (x < 0 || x >= dxc) {
+                    continue;
+                }
+                const uint32_t c = (uint32_t(z) * uint32_t(dyc) + uint32_t(y)) * uint32_t(dxc) + uint32_t(x);
+                const uint32_t tEnd = g.cell_end[c];
+                const float sx = float(ox) * cellf, sy = float(oy) * cellf, sz = float(oz) * cellf;
+                for (uint32_t t = g.cell_start[c]; t < tEnd; ++t) {
+                    if (t == si) {
+                        continue;
+                    }
+                    const float4 pj0 = g.mx0[t];
+                    const float drx = (pi0.x - pj0.x) - sx, dry = (pi0.y - pj0.y) - sy, drz = (pi0.z - pj0.z) - sz;
+                    const float d2 = drx * drx + dry * dry + drz * drz;
+                    const float hbar = 0.5f * (pi0.w + pj0.w);
+                    const float rad = 2.f * hbar;
+                    if (!(d2 < rad * rad)) {
+                        continue;
+                    }
+                    const float4 pj1 = g.mx1[t], pj2 = g.mx2[t], pj3 = g.mx3[t];
+                    const float hInv = 1.f / hbar;
+                    const float h2 = hInv * hInv;
+                    const float gl = lutGradF(lut, d2 * h2) * (h2 * h2 * hInv);
+                    const float gx = drx * gl, gy = dry * gl, gz = drz * gl;
+                    cnt++;
+                    const float mj = pj1.w, rhoj = pj2.w;
+                    const float dvx = (pj1.x - pi1.x) + (pj2.x - pi2.x);
+                    const float dvy = (pj1.y - pi1.y) + (pj2.y - pi2.y);
+                    const float dvz = (pj1.z - pi1.z) + (pj2.z - pi2.z);
+                    const float mr = mj * rhoiInv;
+                    divv.add(mr * (dvx * gx + dvy * gy + dvz * gz));
+                    float fx = -(pi3.x + pj3.x), fy = fx, fz = fx;
+                    fx *= gx;
+                    fy *= gy;
+                    fz *= gz;
+                    const float dvdr = -(dvx * drx + dvy * dry + dvz * drz);
+                    if (dvdr < 0.f) {
+                        const float rhobar = 0.5f * (pi2.w + rhoj);
+                        const float csbar = 0.5f * (pi3.y + pj3.y);
+                        const float mu = hbar * dvdr / (d2 + 1.e-2f * (hbar * hbar));
+                        const float av = (-alpha * csbar * mu + beta * (mu * mu)) / rhobar;
+                        fx -= av * gx;
+                        fy -= av * gy;
+                        fz -= av * gz;
+                        du.add(mj * (0.5f * av * -(dvx * gx + dvy * gy + dvz * gz)));
+                    }
+                    if (Solid) {
+                        const bool undamaged = !ph.sum_only_undamaged ||
+                                               (__float_as_uint(pi3.w) == __float_as_uint(pj3.w) && pi3.z != 0.f &&
+                                                   pj3.z != 0.f);
+                        if (undamaged) {
+                            gv[0] += mr * (dvx * gx);
+                            gv[1] += mr * (dvy * gy);
+                            gv[2] += mr * (dvz * gz);
+                            gv[3] += mr * (0.5f * (dvx * gy + dvy * gx));
+                            gv[4] += mr * (0.5f * (dvx * gz + dvz * gx));
+                            gv[5] += mr * (0.5f * (dvy * gz + dvz * gy));
+                            float tt[5];
+                            for (int k = 0; k < 5; ++k) {
+                                tt[k] = Sif[k] + g.mxS[k * n + t];
+                            }
+                            const float tzz = -tt[0] - tt[1];
+                            fx += tt[0] * gx + tt[2] * gy + tt[3] * gz;
+                            fy += tt[2] * gx + tt[1] * gy + tt[4] * gz;
+                            fz += tt[3] * gx + tt[4] * gy + tzz * gz;
+                        }
+                    }
+                    ax.add(mj * fx);
+                    ay.add(mj * fy);
+                    az.add(mj * fz);
+                }
+            }
+        }
+    }
+    double gax = 0., gay = 0., gaz = 0.;
+    if (ph.gravity) {
+        const dbl4 a = s.agrav[i];
+        gax = a.x;
+        gay = a.y;
+        gaz = a.z;
+    }
+    const dbl4 ri = g.rs[si];
+    const double rhoi = g.rhos[si], pri = g.ps[si];
+    double Si[5] = { 0, 0, 0, 0, 0 };
+    double gvd[6];
+    for (int c = 0; c < 6; ++c) {
+        gvd[c] = gv[c];
+    }
+    if (Solid) {
+        for (int c = 0; c < 5; ++c) {
+            Si[c] = g.Ss[c * n + si];
+        }
+    }
+    finalizeParticle<Solid>(s, ph, mats, i, ri, rhoi, pri, Si, gax + ax.value(), gay + ay.value(), gaz + az.value(),
+        du.value(), divv.value(), gvd, cnt);
+}
+
+} // namespace
+
+void launchPairSumMixed(const DState& s, const Grid& g, const Physics& ph, const MaterialD* mats, const float* lut,
+    cudaStream_t st) {
+    if (!s.n) {
+        return;
+    }
+    if (ph.solid) {
+        pairSumMixedKernel<true><<<ceilDiv(s.n, 128), 128, 0, st>>>(s, g, ph, mats, lut);
+    } else {
+        pairSumMixedKernel<false><<<ceilDiv(s.n, 128), 128, 0, st>>>(s, g, ph, mats, lut);
+    }
+}
+
+} // namespace sphgpu

@@ -1,0 +1,520 @@
+// sph64.cu — FP64 SPH derivative loop, material models and integrators (compiled with -fmad=false).
+//
+// Replaces, for one GPU:
+//   SymmetricSolver::loop + DerivativeHolder::evalSymmetric (core/sph/solvers/SymmetricSolver.cpp:109-141)
+//     with its terms: VelocityDivergence / VelocityGradient (core/sph/equations/DerivativeHelpers.h:292-361),
+//     PressureGradient, StressDivergence (core/sph/equations/EquationTerm.cpp:12-140), StandardAV
+//     (core/sph/equations/av/Standard.h:63-83), NeighborCountTerm (core/sph/equations/HelperTerms.h:16-63)
+//   EquationHolder::finalize (EquationTerm.cpp:90-99, 177-203, 289-316, 366-391, 427-434)
+//   EosMaterial / SolidMaterial initialize + finalize (core/sph/Materials.cpp:47-81): TillotsonEos,
+//     IdealGasEos (core/physics/Eos.cpp:42-45, 198-238), VonMisesRheology (core/physics/Rheology.cpp:36-83),
+//     ScalarGradyKippModel::integrate (core/physics/Damage.cpp:128-170)
+//   PredictorCorrector / LeapFrog (core/timestepping/TimeStepping.cpp:82-391), CourantCriterion
+//     (core/timestepping/TimeStepCriterion.cpp:315-356)
+//
+// The pair loop is a gather: one thread per particle (in cell-sorted order) sums the contributions of all
+// of its neighbours. Each per-pair term is the same IEEE expression the reference evaluates for that pair
+// (this file is compiled without FMA contraction), so results differ from the reference's sequential
+// scatter only by the order of the sums. No atomics: the results are bit-reproducible run to run.
+
+#include "physics.cuh"
+
+namespace sphgpu {
+
+namespace {
+
+// ------------------------------------------------------------------------------------------------------
+// kernels
+// ------------------------------------------------------------------------------------------------------
+
+__global__ void materialsInitKernel(DState s, Physics ph, const MaterialD* __restrict__ mats) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < s.n) {
+        materialInit(s, ph, mats, i);
+    }
+}
+
+// LutKernel<3>::gradImpl (core/sph/kernel/Kernel.h:129-144)
+__device__ __forceinline__ double lutGrad(const double* __restrict__ lut, double qSqr) {
+    if (qSqr >= 4.) {
+        return 0.;
+    }
+    const double floatIdx = (double(LUT_ENTRIES) * (1. / (2. * 2.))) * qSqr;
+    const int idx1 = int(floatIdx);
+    const double ratio = floatIdx - double(idx1);
+    return __ldg(lut + idx1) * (1. - ratio) + __ldg(lut + idx1 + 1) * ratio;
+}
+
+__device__ __forceinline__ bool interacts64(const dbl4& a, const dbl4& b) {
+    const double dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+    const double d2 = dx * dx + dy * dy + dz * dz;
+    const double rad = 2. * (0.5 * (a.w + b.w));
+    return d2 < rad * rad;
+}
+
+template <bool Solid>
+__global__ void __launch_bounds__(128) pairSum64Kernel(DState s, Grid g, Physics ph,
+    const MaterialD* __restrict__ mats, const double* __restrict__ lut) {
+    const uint32_t n = s.n;
+    const uint32_t si = blockIdx.x * blockDim.x + threadIdx.x;
+    if (si >= n) {
+        return;
+    }
+    const GridInfo* gi = g.info;
+    const uint32_t i = g.perm[si];
+    const dbl4 ri = g.rs[si];
+    const dbl4 vi = g.vs[si];
+    const double rhoi = g.rhos[si], pri = g.ps[si], csi = g.css[si];
+    double Si[5] = { 0, 0, 0, 0, 0 };
+    double redi = 0.;
+    uint32_t flagi = 0;
+    if (Solid) {
+        for (int c = 0; c < 5; ++c) {
+            Si[c] = g.Ss[c * n + si];
+        }
+        redi = g.reduces[si];
+        flagi = g.flags[si];
+    }
+    double ax = 0., ay = 0., az = 0.;
+    if (ph.gravity) {
+        const dbl4 a = s.agrav[i];
+        ax = a.x;
+        ay = a.y;
+        az = a.z;
+    }
+    double du = 0., divv = 0.;
+    double gv[6] = { 0, 0, 0, 0, 0, 0 };
+    uint32_t cnt = 0;
+    const double alpha = ph.av_alpha, beta = ph.av_beta;
+    const int dxc = gi->dims[0], dyc = gi->dims[1], dzc = gi->dims[2];
+    const uint32_t key = g.keys_sorted[si];
+    const int cx = int(key % uint32_t(dxc)), cy = int((key / uint32_t(dxc)) % uint32_t(dyc)),
+              cz = int(key / (uint32_t(dxc) * uint32_t(dyc)));
+    const double rhoi2 = rhoi * rhoi;
+    for (int z = max(cz - 1, 0); z <= min(cz + 1, dzc - 1); ++z) {
+        for (int y = max(cy - 1, 0); y <= min(cy + 1, dyc - 1); ++y) {
+            const uint32_t rowBase = (uint32_t(z) * uint32_t(dyc) + uint32_t(y)) * uint32_t(dxc);
+            const uint32_t c0 = rowBase + uint32_t(max(cx - 1, 0));
+            const uint32_t c1 = rowBase + uint32_t(min(cx + 1, dxc - 1));
+            // the cells of one x-row have consecutive keys, so their particles form one contiguous range
+            // of the cell-sorted order
+            uint32_t tb = 0xffffffffu, tEnd = 0;
+            for (uint32_t c = c0; c <= c1; ++c) {
+                const uint32_t cs0 = g.cell_start[c], ce0 = g.cell_end[c];
+                if (ce0 > cs0) {
+                    tb = min(tb, cs0);
+                    tEnd = max(tEnd, ce0);
+                }
+            }
+            for (uint32_t t = tb; t < tEnd; ++t) {
+                if (t == si) {
+                    continue;
+                }
+                const dbl4 rj = g.rs[t];
+                if (!interacts64(ri, rj)) {
+                    continue;
+                }
+                const dbl4 vj = g.vs[t];
+                const double mj = g.ms[t], rhoj = g.rhos[t];
+                // symmetrized kernel gradient at hbar (core/sph/kernel/Kernel.h:32-36, 640-644)
+                const double hbar = 0.5 * (ri.w + rj.w);
+                const double drx = ri.x - rj.x, dry = ri.y - rj.y, drz = ri.z - rj.z;
+                const double hInv = 1. / hbar;
+                const double h2 = hInv * hInv;
+                const double h5 = (h2 * h2) * hInv;
+                const double gl = lutGrad(lut, (drx * drx + dry * dry + drz * drz) * (hInv * hInv));
+                const double gx = (drx * h5) * gl, gy = (dry * h5) * gl, gz = (drz * h5) * gl;
+                cnt++;
+                // velocity divergence (CenterDensityDiscr)
+                const double dvx = vj.x - vi.x, dvy = vj.y - vi.y, dvz = vj.z - vi.z;
+                divv += mj / rhoi * (dvx * gx + dvy * gy + dvz * gz);
+                // pressure gradient (StandardForceDiscr)
+                {
+                    const double pr = pri / rhoi2 + g.ps[t] / (rhoj * rhoj);
+                    ax += mj * -(pr * gx);
+                    ay += mj * -(pr * gy);
+                    az += mj * -(pr * gz);
+                }
+                // standard artificial viscosity
+                {
+                    const double ux = vi.x - vj.x, uy = vi.y - vj.y, uz = vi.z - vj.z;
+                    const double dvdr = ux * drx + uy * dry + uz * drz;
+                    if (!(dvdr >= 0.)) {
+                        const double rhobar = 0.5 * (rhoi + rhoj);
+                        const double csbar = 0.5 * (csi + g.css[t]);
+                        const double mu =
+                            hbar * dvdr / ((drx * drx + dry * dry + drz * drz) + 1.e-2 * (hbar * hbar));
+                        const double av = 1. / rhobar * (-alpha * csbar * mu + beta * (mu * mu));
+                        ax += mj * -(av * gx);
+                        ay += mj * -(av * gy);
+                        az += mj * -(av * gz);
+                        du += mj * (0.5 * av * (ux * gx + uy * gy + uz * gz));
+                    }
+                }
+                if (Solid) {
+                    const bool undamaged =
+                        !ph.sum_only_undamaged || (flagi == g.flags[t] && redi != 0. && g.reduces[t] != 0.);
+                    if (undamaged) {
+                        const double f = mj / rhoi;
+                        gv[0] += f * (dvx * gx);
+                        gv[1] += f * (dvy * gy);
+                        gv[2] += f * (dvz * gz);
+                        gv[3] += f * (0.5 * (dvx * gy + dvy * gx));
+                        gv[4] += f * (0.5 * (dvx * gz + dvz * gx));
+                        gv[5] += f * (0.5 * (dvy * gz + dvz * gy));
+                        const double rhoj2 = rhoj * rhoj;
+                        double tt[5];
+                        for (int c = 0; c < 5; ++c) {
+                            tt[c] = Si[c] / rhoi2 + g.Ss[c * n + t] / rhoj2;
+                        }
+                        const double tzz = -tt[0] - tt[1];
+                        ax += mj * (tt[0] * gx + tt[2] * gy + tt[3] * gz);
+                        ay += mj * (tt[2] * gx + tt[1] * gy + tt[4] * gz);
+                        az += mj * (tt[3] * gx + tt[4] * gy + tzz * gz);
+                    }
+                }
+            }
+        }
+    }
+    finalizeParticle<Solid>(s, ph, mats, i, ri, rhoi, pri, Si, ax, ay, az, du, divv, gv, cnt);
+}
+
+// PredictorCorrector::makePredictions (TimeStepping.cpp:286-300) + materials initialize at the prediction
+__global__ void predictKernel(DState s, Physics ph, const MaterialD* __restrict__ mats, const double* __restrict__ dtp) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = s.n;
+    if (i >= n) {
+        return;
+    }
+    const double dt = *dtp;
+    const double dt2 = 0.5 * (dt * dt);
+    dbl4 r = s.r[i], v = s.v[i];
+    const dbl4 a = s.dv[i];
+    r.x += v.x * dt + a.x * dt2;
+    r.y += v.y * dt + a.y * dt2;
+    r.z += v.z * dt + a.z * dt2;
+    r.w += v.w * dt + a.w * dt2;
+    v.x += a.x * dt;
+    v.y += a.y * dt;
+    v.z += a.z * dt;
+    v.w += a.w * dt;
+    s.r[i] = r;
+    s.v[i] = v;
+    const MaterialD& mt = mats[ph.nmat > 1 ? s.mat[i] : 0];
+    double rho = s.rho[i], drho = s.drho[i];
+    rho += drho * dt;
+    clampDeriv(rho, drho, mt.rho_lo, mt.rho_hi);
+    s.rho[i] = rho;
+    s.drho[i] = drho;
+    double u = s.u[i], du = s.du[i];
+    u += du * dt;
+    clampDeriv(u, du, mt.u_lo, mt.u_hi);
+    s.u[i] = u;
+    s.du[i] = du;
+    if (ph.solid) {
+        for (int c = 0; c < 5; ++c) {
+            s.S[c * n + i] += s.dS[c * n + i] * dt;
+        }
+        if (ph.damage) {
+            double D = s.D[i], dD = s.dD[i];
+            D += dD * dt;
+            clampDeriv(D, dD, mt.d_lo, mt.d_hi);
+            s.D[i] = D;
+            s.dD[i] = dD;
+        }
+    }
+    materialInit(s, ph, mats, i);
+}
+
+__device__ __forceinline__ void blockMinToGlobal(double local, double* out) {
+    __shared__ double red[32];
+    for (int off = 16; off > 0; off >>= 1) {
+        local = fmin(local, __shfl_xor_sync(0xffffffffu, local, off));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        red[threadIdx.x >> 5] = local;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : DBL_MAX;
+        for (int off = 16; off > 0; off >>= 1) {
+            v = fmin(v, __shfl_xor_sync(0xffffffffu, v, off));
+        }
+        if (threadIdx.x == 0 && v < DBL_MAX) {
+            atomicMinPos(out, v);
+        }
+    }
+}
+
+// PredictorCorrector::makeCorrections (TimeStepping.cpp:302-322) + CourantCriterion partial minimum
+__global__ void correctKernel(DState s, Physics ph, const MaterialD* __restrict__ mats, const double* __restrict__ dtp,
+    double* dtMin) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = s.n;
+    double local = DBL_MAX;
+    if (i < n) {
+        const double dt = *dtp;
+        const double dt2 = 0.5 * (dt * dt);
+        const double ca = 1. / 3., cb = 0.5;
+        dbl4 r = s.r[i], v = s.v[i];
+        const dbl4 pa = s.pdv[i], a = s.dv[i];
+        r.x -= ca * (pa.x - a.x) * dt2;
+        r.y -= ca * (pa.y - a.y) * dt2;
+        r.z -= ca * (pa.z - a.z) * dt2;
+        r.w -= ca * (pa.w - a.w) * dt2;
+        v.x -= cb * (pa.x - a.x) * dt;
+        v.y -= cb * (pa.y - a.y) * dt;
+        v.z -= cb * (pa.z - a.z) * dt;
+        v.w -= cb * (pa.w - a.w) * dt;
+        s.r[i] = r;
+        s.v[i] = v;
+        const MaterialD& mt = mats[ph.nmat > 1 ? s.mat[i] : 0];
+        double rho = s.rho[i], drho = s.drho[i];
+        rho -= 0.5 * (s.pdrho[i] - drho) * dt;
+        clampDeriv(rho, drho, mt.rho_lo, mt.rho_hi);
+        s.rho[i] = rho;
+        s.drho[i] = drho;
+        double u = s.u[i], du = s.du[i];
+        u -= 0.5 * (s.pdu[i] - du) * dt;
+        clampDeriv(u, du, mt.u_lo, mt.u_hi);
+        s.u[i] = u;
+        s.du[i] = du;
+        if (ph.solid) {
+            for (int c = 0; c < 5; ++c) {
+                s.S[c * n + i] -= 0.5 * (s.pdS[c * n + i] - s.dS[c * n + i]) * dt;
+            }
+            if (ph.damage) {
+                double D = s.D[i], dD = s.dD[i];
+                D -= 0.5 * (s.pdD[i] - dD) * dt;
+                clampDeriv(D, dD, mt.d_lo, mt.d_hi);
+                s.D[i] = D;
+                s.dD[i] = dD;
+            }
+        }
+        const double cs = s.cs[i];
+        if (cs > 0.) {
+            local = ph.courant * r.w / cs;
+        }
+    }
+    blockMinToGlobal(local, dtMin);
+}
+
+// LeapFrog::stepParticles first drift (TimeStepping.cpp:356-362) + materials initialize
+__global__ void leapFrogDriftKernel(DState s, Physics ph, const MaterialD* __restrict__ mats, const double* __restrict__ dtp) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= s.n) {
+        return;
+    }
+    const double dt = *dtp;
+    dbl4 r = s.r[i];
+    const dbl4 v = s.v[i];
+    r.x += v.x * 0.5 * dt;
+    r.y += v.y * 0.5 * dt;
+    r.z += v.z * 0.5 * dt;
+    r.w += v.w * 0.5 * dt;
+    s.r[i] = r;
+    materialInit(s, ph, mats, i);
+}
+
+// LeapFrog: first-order Euler update, kick, second drift (TimeStepping.cpp:367-388) + Courant minimum
+__global__ void leapFrogKickKernel(DState s, Physics ph, const MaterialD* __restrict__ mats,
+    const double* __restrict__ dtp, double* dtMin) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = s.n;
+    double local = DBL_MAX;
+    if (i < n) {
+        const double dt = *dtp;
+        const MaterialD& mt = mats[ph.nmat > 1 ? s.mat[i] : 0];
+        double rho = s.rho[i], drho = s.drho[i];
+        rho += drho * dt;
+        clampDeriv(rho, drho, mt.rho_lo, mt.rho_hi);
+        s.rho[i] = rho;
+        s.drho[i] = drho;
+        double u = s.u[i], du = s.du[i];
+        u += du * dt;
+        clampDeriv(u, du, mt.u_lo, mt.u_hi);
+        s.u[i] = u;
+        s.du[i] = du;
+        if (ph.solid) {
+            for (int c = 0; c < 5; ++c) {
+                s.S[c * n + i] += s.dS[c * n + i] * dt;
+            }
+            if (ph.damage) {
+                double D = s.D[i], dD = s.dD[i];
+                D += dD * dt;
+                clampDeriv(D, dD, mt.d_lo, mt.d_hi);
+                s.D[i] = D;
+                s.dD[i] = dD;
+            }
+        }
+        dbl4 v = s.v[i];
+        const dbl4 a = s.dv[i];
+        v.x += a.x * dt;
+        v.y += a.y * dt;
+        v.z += a.z * dt;
+        v.w += a.w * dt;
+        dbl4 r = s.r[i];
+        r.x += v.x * 0.5 * dt;
+        r.y += v.y * 0.5 * dt;
+        r.z += v.z * 0.5 * dt;
+        r.w += v.w * 0.5 * dt;
+        s.v[i] = v;
+        s.r[i] = r;
+        const double cs = s.cs[i];
+        if (cs > 0.) {
+            local = ph.courant * r.w / cs;
+        }
+    }
+    blockMinToGlobal(local, dtMin);
+}
+
+__global__ void courantFinishKernel(double* dt, double* dtMin, double maxDt) {
+    const double m = *dtMin;
+    *dt = m > maxDt ? maxDt : m;
+    *dtMin = DBL_MAX;
+}
+
+// Neumaier-compensated block partial sums of the conserved totals, then one block adds the partials in a
+// fixed order: deterministic for a fixed grid
+constexpr int TOT_BLOCKS = 256;
+constexpr int TOT_THREADS = 256;
+
+__device__ __forceinline__ void kahanAdd(double& sum, double& c, double x) {
+    const double t = sum + x;
+    if (fabs(sum) >= fabs(x)) {
+        c += (sum - t) + x;
+    } else {
+        c += (x - t) + sum;
+    }
+    sum = t;
+}
+
+__global__ void totalsKernel(DState s, double* partial) {
+    double sum[9], comp[9];
+    for (int k = 0; k < 9; ++k) {
+        sum[k] = 0.;
+        comp[k] = 0.;
+    }
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < s.n; i += gridDim.x * blockDim.x) {
+        const dbl4 r = s.r[i], v = s.v[i];
+        const double m = s.m[i];
+        kahanAdd(sum[0], comp[0], m * v.x);
+        kahanAdd(sum[1], comp[1], m * v.y);
+        kahanAdd(sum[2], comp[2], m * v.z);
+        kahanAdd(sum[3], comp[3], m * (r.y * v.z - r.z * v.y));
+        kahanAdd(sum[4], comp[4], m * (r.z * v.x - r.x * v.z));
+        kahanAdd(sum[5], comp[5], m * (r.x * v.y - r.y * v.x));
+        kahanAdd(sum[6], comp[6], 0.5 * m * (v.x * v.x + v.y * v.y + v.z * v.z));
+        kahanAdd(sum[7], comp[7], m * s.u[i]);
+        kahanAdd(sum[8], comp[8], m);
+    }
+    __shared__ double sh[9][TOT_THREADS];
+    for (int k = 0; k < 9; ++k) {
+        sh[k][threadIdx.x] = sum[k] + comp[k];
+    }
+    __syncthreads();
+    if (threadIdx.x < 9) {
+        double acc = 0., c = 0.;
+        for (int t = 0; t < TOT_THREADS; ++t) {
+            kahanAdd(acc, c, sh[threadIdx.x][t]);
+        }
+        partial[blockIdx.x * 9 + threadIdx.x] = acc + c;
+    }
+}
+
+__global__ void totalsFinish(const double* partial, double* out) {
+    if (threadIdx.x < 9) {
+        double acc = 0., c = 0.;
+        for (int b = 0; b < TOT_BLOCKS; ++b) {
+            kahanAdd(acc, c, partial[b * 9 + threadIdx.x]);
+        }
+        out[threadIdx.x] = acc + c;
+    }
+}
+
+__device__ __forceinline__ bool finite4(const dbl4& a) {
+    return isfinite(a.x) && isfinite(a.y) && isfinite(a.z) && isfinite(a.w);
+}
+
+__global__ void checkFiniteKernel(DState s, unsigned long long* firstBad) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < s.n; i += gridDim.x * blockDim.x) {
+        bool ok = finite4(s.r[i]) && finite4(s.v[i]) && finite4(s.dv[i]) && isfinite(s.rho[i]) &&
+                  isfinite(s.u[i]) && isfinite(s.drho[i]) && isfinite(s.du[i]) && isfinite(s.p[i]) &&
+                  isfinite(s.cs[i]);
+        if (s.S) {
+            for (int c = 0; c < 5; ++c) {
+                ok = ok && isfinite(s.S[c * s.n + i]) && isfinite(s.dS[c * s.n + i]);
+            }
+        }
+        if (s.D) {
+            ok = ok && isfinite(s.D[i]) && isfinite(s.dD[i]);
+        }
+        if (!ok) {
+            atomicMin(firstBad, (unsigned long long)i);
+        }
+    }
+}
+
+} // namespace
+
+void launchMaterialsInit(const DState& s, const Physics& ph, const MaterialD* mats, cudaStream_t st) {
+    if (s.n) {
+        materialsInitKernel<<<ceilDiv(s.n, 256), 256, 0, st>>>(s, ph, mats);
+    }
+}
+
+void launchPairSum64(const DState& s, const Grid& g, const Physics& ph, const MaterialD* mats, const double* lut,
+    cudaStream_t st) {
+    if (!s.n) {
+        return;
+    }
+    if (ph.solid) {
+        pairSum64Kernel<true><<<ceilDiv(s.n, 128), 128, 0, st>>>(s, g, ph, mats, lut);
+    } else {
+        pairSum64Kernel<false><<<ceilDiv(s.n, 128), 128, 0, st>>>(s, g, ph, mats, lut);
+    }
+}
+
+void launchPredict(const DState& s, const Physics& ph, const MaterialD* mats, const double* dt, cudaStream_t st) {
+    if (s.n) {
+        predictKernel<<<ceilDiv(s.n, 256), 256, 0, st>>>(s, ph, mats, dt);
+    }
+}
+
+void launchCorrect(const DState& s, const Physics& ph, const MaterialD* mats, const double* dt, double* dtMin,
+    cudaStream_t st) {
+    if (s.n) {
+        correctKernel<<<ceilDiv(s.n, 256), 256, 0, st>>>(s, ph, mats, dt, dtMin);
+    }
+}
+
+void launchLeapFrogDriftInit(const DState& s, const Physics& ph, const MaterialD* mats, const double* dt,
+    cudaStream_t st) {
+    if (s.n) {
+        leapFrogDriftKernel<<<ceilDiv(s.n, 256), 256, 0, st>>>(s, ph, mats, dt);
+    }
+}
+
+void launchLeapFrogKick(const DState& s, const Physics& ph, const MaterialD* mats, const double* dt, double* dtMin,
+    cudaStream_t st) {
+    if (s.n) {
+        leapFrogKickKernel<<<ceilDiv(s.n, 256), 256, 0, st>>>(s, ph, mats, dt, dtMin);
+    }
+}
+
+void launchCourantFinish(double* dt, double* dtMin, double maxDt, cudaStream_t st) {
+    courantFinishKernel<<<1, 1, 0, st>>>(dt, dtMin, maxDt);
+}
+
+void launchTotals(const DState& s, double* partial, double* out, cudaStream_t st) {
+    totalsKernel<<<TOT_BLOCKS, TOT_THREADS, 0, st>>>(s, partial);
+    totalsFinish<<<1, 32, 0, st>>>(partial, out);
+}
+
+void launchCheckFinite(const DState& s, unsigned long long* firstBad, cudaStream_t st) {
+    if (s.n) {
+        checkFiniteKernel<<<min(ceilDiv(s.n, 256), 152 * 8), 256, 0, st>>>(s, firstBad);
+    }
+}
+
+} // namespace sphgpu

@@ -1,0 +1,192 @@
+// state.h — device state of one sphgpu handle and the launchers of each translation unit.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace sphgpu {
+
+// Particle state in HBM, in the reference's storage order. Vector quantities keep the reference layout
+// {x, y, z, h} (one 32-byte dbl4 per particle); tensors are stored component-major (SoA, component c
+// of particle i at [c * n + i]) so that a thread-per-particle kernel reads them coalesced.
+struct DState {
+    uint32_t n;
+    dbl4* r;
+    dbl4* v;
+    dbl4* dv;
+    double* m;
+    double* rho;
+    double* drho;
+    double* u;
+    double* du;
+    double* p;
+    double* cs;
+    double* divv;
+    uint32_t* ncnt;
+    uint32_t* flag;
+    uint32_t* mat;
+    double* S;      // 5 x n: xx, yy, xy, xz, yz
+    double* dS;     // 5 x n
+    double* gradv;  // 6 x n: xx, yy, zz, xy, xz, yz
+    double* reduce;
+    double* D;
+    double* dD;
+    double* eps_min;
+    double* m_zero;
+    double* growth;
+    uint32_t* n_flaws;
+    // derivatives saved by the predictor (PredictorCorrector::predictions)
+    dbl4* pdv;
+    double* pdrho;
+    double* pdu;
+    double* pdS;
+    double* pdD;
+    // self-gravity acceleration of the current evaluation
+    dbl4* agrav;
+};
+
+// Physics switches and constants of one handle
+struct Physics {
+    int solid;           // SOLID_STRESS with a stress tensor
+    int damage;          // any material with a fracture model
+    int gravity;
+    int adaptive_h;
+    int sum_only_undamaged;
+    int integrator;
+    int precision;
+    int multipole_order;
+    int kernel_radius;   // 0: point masses, 2: gravity kernel of the cubic spline
+    uint32_t leaf_size;
+    uint32_t nmat;
+    double h_lo, h_hi;
+    double av_alpha, av_beta;
+    double G;
+    double theta_inv;
+    double courant;
+    double max_dt;
+};
+
+// Neighbour grid buffers (cell-sorted copies of the pair-loop inputs)
+struct Grid {
+    uint32_t cell_capacity = 0;
+    GridInfo* info = nullptr;          // device
+    unsigned long long* bounds = nullptr; // device: flipped min x,y,z, max x,y,z, max h
+    uint32_t* keys = nullptr;
+    uint32_t* keys_sorted = nullptr;
+    uint32_t* perm_in = nullptr;
+    uint32_t* perm = nullptr;          // sorted position -> particle index
+    uint32_t* cell_start = nullptr;
+    uint32_t* cell_end = nullptr;
+    void* sort_temp = nullptr;
+    size_t sort_temp_bytes = 0;
+    // cell-sorted copies
+    dbl4* rs = nullptr;
+    dbl4* vs = nullptr;
+    double* ms = nullptr;
+    double* rhos = nullptr;
+    double* ps = nullptr;
+    double* css = nullptr;
+    double* Ss = nullptr;      // 5 x n
+    double* reduces = nullptr;
+    uint32_t* flags = nullptr;
+    // mixed-precision copies (cell-sorted): positions relative to the particle's own cell origin, velocities
+    // as unevaluated float pairs (hi + lo) so that neighbour differences keep FP64-level accuracy
+    float4* mx0 = nullptr;     // x - cell_x, y - cell_y, z - cell_z, h
+    float4* mx1 = nullptr;     // vx_hi, vy_hi, vz_hi, m
+    float4* mx2 = nullptr;     // vx_lo, vy_lo, vz_lo, rho
+    float4* mx3 = nullptr;     // p / rho^2, cs, stress reducing, flag (bit pattern)
+    float* mxS = nullptr;      // 5 x n: S / rho^2
+    uint32_t launches = 0;     // own kernels launched by the last build / gather (library sort excluded)
+};
+
+// Barnes-Hut tree buffers
+struct BhNodeGeom {
+    double lo[3];
+    double hi[3];
+    double com[3];
+    double r_open;
+    int32_t left, right;    // children (-1 for leaves)
+    uint32_t from, to;      // particle range in the index permutation (leaves)
+    int32_t parent;
+    int32_t level;
+};
+
+struct BhNodeMoments {
+    double m0;
+    double q2[6];  // xx xy xz yy yz zz
+    double q3[10]; // xxx xxy xxz xyy xyz xzz yyy yyz yzz zzz
+    double pad;
+};
+
+struct BhSegment {
+    uint32_t from, to;
+    int32_t node;
+    uint32_t sliding;
+    double lo[3], hi[3];
+};
+
+struct Tree {
+    uint32_t node_capacity = 0;
+    uint32_t seg_capacity = 0;
+    uint32_t* idx = nullptr;          // permutation of particles (KdTree::idxs)
+    uint32_t* scratch_b = nullptr;    // positions of elements above the split (per segment)
+    uint32_t* scratch_s = nullptr;    // positions of elements below the split
+    BhNodeGeom* geom = nullptr;
+    BhNodeMoments* mom = nullptr;
+    BhSegment* seg[2] = { nullptr, nullptr };
+    uint32_t* counters = nullptr;     // device: [0] node count, [1] next-level segment count, [2] leaf count
+    uint32_t* counters_host = nullptr; // pinned mirror
+    uint32_t* leaves = nullptr;       // leaf node ids
+    int32_t* walk_scratch = nullptr;  // per-warp checklists
+    uint32_t walk_warps = 0;
+    uint32_t walk_capacity = 0;       // entries per list per warp
+    unsigned long long* stats = nullptr; // device: approx, exact
+    unsigned long long* bbox = nullptr;  // device: flipped bounding box of the root
+    std::vector<uint32_t> level_start; // host: first node id of each level
+    uint32_t node_count = 0;
+    uint32_t leaf_count = 0;
+    uint32_t launches = 0;            // kernels launched by the last build
+    bool built = false;
+};
+
+// ---- launchers (grid.cu) ----
+void launchGridBuild(const DState& s, Grid& g, const Physics& ph, cudaStream_t st);
+void launchGatherSorted(const DState& s, Grid& g, const Physics& ph, cudaStream_t st);
+cudaError_t gridAllocate(Grid& g, uint32_t n, bool solid);
+void gridFree(Grid& g);
+void launchCountPairs(const DState& s, const Grid& g, unsigned long long* count, cudaStream_t st);
+void launchListPairs(const DState& s, const Grid& g, uint32_t* pi, uint32_t* pj, unsigned long long* count,
+    unsigned long long capacity, cudaStream_t st);
+
+// ---- launchers (sph64.cu) ----
+void launchMaterialsInit(const DState& s, const Physics& ph, const MaterialD* mats, cudaStream_t st);
+void launchPairSum64(const DState& s, const Grid& g, const Physics& ph, const MaterialD* mats,
+    const double* lut_grad, cudaStream_t st);
+void launchPredict(const DState& s, const Physics& ph, const MaterialD* mats, const double* dt, cudaStream_t st);
+void launchCorrect(const DState& s, const Physics& ph, const MaterialD* mats, const double* dt, double* dt_min,
+    cudaStream_t st);
+void launchLeapFrogDriftInit(const DState& s, const Physics& ph, const MaterialD* mats, const double* dt,
+    cudaStream_t st);
+void launchLeapFrogKick(const DState& s, const Physics& ph, const MaterialD* mats, const double* dt,
+    double* dt_min, cudaStream_t st);
+void launchCourantFinish(double* dt, double* dt_min, double max_dt, cudaStream_t st);
+void launchTotals(const DState& s, double* partial, double* out, cudaStream_t st);
+void launchCheckFinite(const DState& s, unsigned long long* first_bad, cudaStream_t st);
+void launchPairSumMixed(const DState& s, const Grid& g, const Physics& ph, const MaterialD* mats,
+    const float* lut_grad_f, cudaStream_t st);
+
+// ---- launchers (gravity.cu) ----
+cudaError_t treeAllocate(Tree& t, uint32_t n, uint32_t leaf_size);
+void treeFree(Tree& t);
+cudaError_t treeBuild(const DState& s, Tree& t, const Physics& ph, uint32_t* dev_error, cudaStream_t st);
+void launchGravityWalk(const DState& s, Tree& t, const Physics& ph, const double* lut_grad, uint32_t* dev_error,
+    cudaStream_t st);
+void launchGravityPoints(const DState& s, const Tree& t, const Physics& ph, const double* lut_grad,
+    const dbl4* points, dbl4* acc, uint32_t npoints, cudaStream_t st);
+
+} // namespace sphgpu

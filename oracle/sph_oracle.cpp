@@ -1119,7 +1119,7 @@ void integrate(const sphgpu_config& cfg, ora_state& s) {
         bh.leafSize = cfg.gravity_leaf_size;
         bh.thetaInv = 1. / cfg.gravity_opening_angle;
         bh.order = cfg.gravity_multipole_order;
-        bh.kernelRadius = 2;
+        bh.kernelRadius = cfg.gravity_kernel == SPHGPU_GRAVITY_KERNEL_POINT_PARTICLES ? 0 : 2;
         bh.build(n, s.r, s.m, cfg.gravity_constant);
         bh.evalSelfGravity(acc.data());
     }

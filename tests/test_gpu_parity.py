@@ -1,0 +1,207 @@
+"""GPU parity: the CUDA path (through the C ABI) against the reference's golden vectors and the CPU oracle.
+
+Mirrors the reference's own tests of the path (core/objects/finders/test/Finders.cpp, core/gravity/test/
+BarnesHut.cpp, core/sph/solvers/test/Solvers.cpp) plus seeded cases at sizes the oracle finishes in seconds.
+Tolerances: neighbour pair sets and neighbour counts bit-exact; one derivative evaluation within 1e-12 and
+the fixture's time steps within 1e-10 of each quantity's magnitude (FP64 path; the sums over neighbours run
+in a different order than the reference's scatter); the mixed path within its stated bound.
+"""
+import numpy as np
+import pytest
+
+import cases
+from opensph_gb300 import abi
+from opensph_gb300.solver import GpuSolver, SphGpuError
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+TOL_EVAL = 1e-12
+TOL_STEPS = 1e-10
+
+
+def gas_solver(r, **kw):
+    n = len(r) // 4
+    mats = [abi.ideal_gas()]
+    cfg, keep = abi.make_config(n, mats, forces=abi.FORCE_PRESSURE, **kw)
+    g = GpuSolver(cfg, keep)
+    st = {"r": r, "v": np.zeros(4 * n), "dv": np.zeros(4 * n), "m": np.ones(n), "rho": np.ones(n),
+          "drho": np.zeros(n), "u": np.ones(n), "du": np.zeros(n), "flag": np.zeros(n, "u4"),
+          "mat": np.zeros(n, "u4")}
+    g.set_state(st)
+    return g
+
+
+def test_pair_set_matches_reference():
+    fx = cases.load("pairs_n1500")
+    with gas_solver(fx["r"]) as g:
+        pi, pj = g.pairs()
+    mine = set(zip(pi.tolist(), pj.tolist()))
+    ref = {(min(i, j), max(i, j)) for i, j in zip(fx["pair_i"].tolist(), fx["pair_j"].tolist())}
+    assert mine == ref
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_pair_set_matches_oracle_random(seed):
+    rng = np.random.default_rng(seed)
+    n = 20000
+    r = np.zeros((n, 4))
+    r[:, :3] = rng.random((n, 3))
+    r[:, 3] = 0.01 + 0.01 * rng.random(n)
+    with gas_solver(r.ravel()) as g:
+        pi, pj = g.pairs()
+    oi, oj = oracle.pairs(r.ravel())
+    np.testing.assert_array_equal(pi, oi)
+    np.testing.assert_array_equal(pj, oj)
+
+
+def test_pair_set_lattice_ties():
+    # HCP-like lattice: many pairs exactly at the same distance, exact FP64 test decides
+    fx = cases.load("sphere_n1000")
+    r = fx["s0_r"]
+    with gas_solver(r) as g:
+        pi, pj = g.pairs()
+    oi, oj = oracle.pairs(r)
+    np.testing.assert_array_equal(pi, oi)
+    np.testing.assert_array_equal(pj, oj)
+
+
+def grav_solver(r, m, theta, leaf_size=25, order=3, kernel=abi.GRAVITY_KERNEL_SPH_KERNEL):
+    n = len(m)
+    cfg, keep = abi.make_config(n, [abi.ideal_gas()], forces=abi.FORCE_PRESSURE | abi.FORCE_SELF_GRAVITY,
+                                gravity_constant=1.0, gravity_opening_angle=theta, gravity_leaf_size=leaf_size,
+                                gravity_multipole_order=order, gravity_kernel=kernel)
+    g = GpuSolver(cfg, keep)
+    g.set_quantity(abi.Q_POSITION, 0, r)
+    g.set_quantity(abi.Q_MASS, 0, m)
+    return g
+
+
+@pytest.mark.parametrize("name", ["gravity_n3000", "gravity_n3000_t07"])
+def test_barnes_hut_matches_reference(name):
+    fx = cases.load(name)
+    theta = float(str(fx["driver_args"]).split()[2])
+    with grav_solver(fx["r"], fx["m"], theta) as g:
+        dv = g.gravity()
+        stats = g.gravity_stats()
+    assert stats == [int(fx["nodes_approx"][0]), int(fx["nodes_exact"][0]), int(fx["node_count"][0])]
+    assert cases.scale_err(cases.vec3(dv), cases.vec3(fx["a_bh"])) < 1e-13
+
+
+def test_barnes_hut_matches_oracle_plummer_20k():
+    rng = np.random.default_rng(5)
+    n = 20000
+    x = rng.random(n)
+    rad = 1.0 / np.sqrt(np.power(x, -2.0 / 3.0) - 1.0)
+    rad = np.minimum(rad, 20.0)
+    ct = 2 * rng.random(n) - 1
+    ph = 2 * np.pi * rng.random(n)
+    st = np.sqrt(1 - ct * ct)
+    r = np.stack([rad * st * np.cos(ph), rad * st * np.sin(ph), rad * ct, np.full(n, 1e-3)], 1).ravel()
+    m = np.full(n, 1.0 / n)
+    with grav_solver(r, m, 0.5) as g:
+        dv = g.gravity()
+        stats = g.gravity_stats()
+    odv, ostats = oracle.gravity_bh(r, m, G=1.0, theta=0.5)
+    assert stats == ostats
+    assert cases.scale_err(cases.vec3(dv), cases.vec3(odv)) < 1e-13
+
+
+def test_barnes_hut_six_particle_known_answer():
+    # core/gravity/test/BarnesHut.cpp:23-45, 138-158: point masses, leaf size 1, theta 0.5
+    r = np.array([[2, 3, 0, 1], [5, 4, 0, 1], [9, 6, 0, 1], [4, 7, 0, 1], [8, 1, 0, 1], [7, 2, 0, 1]], "f8")
+    expected = np.array([0.020169998934707004, -0.007912678499211458, 0.0])
+    for order, eps in [(0, 4e-4), (2, 8e-5), (3, 1e-5)]:
+        with grav_solver(r.ravel(), np.ones(6), 0.5, leaf_size=1, order=order,
+                         kernel=abi.GRAVITY_KERNEL_POINT_PARTICLES) as g:
+            g.gravity()
+            a = g.gravity_points(np.array([-10.0, 10.0, 0.0, 1.0]))[:3]
+        o = oracle.gravity_points(r.ravel(), np.ones(6), np.array([-10.0, 10.0, 0.0, 1.0]), G=1.0, theta=0.5,
+                                  order=order, leaf_size=1, kernel_radius=0)[:3]
+        np.testing.assert_allclose(a, o, rtol=1e-13, atol=1e-17)
+        d2 = np.sum((a - expected) ** 2)
+        assert d2 <= eps * eps * (1.0 + max(np.sum(a ** 2), np.sum(expected ** 2)))
+
+
+@pytest.mark.parametrize("name", ["sphere_n1000", "impact_n1200", "gas_n1500"])
+def test_integrate_matches_reference(name):
+    fx = cases.load(name)
+    cfg, keep = cases.config_of(fx)
+    with GpuSolver(cfg, keep) as g:
+        g.set_state(cases.state_of(fx, "s0_"))
+        g.integrate()
+        got = g.get_state()
+    for f in ["dv", "drho", "du", "divv", "p", "cs", "gradv", "dS", "dD", "reduce", "S"]:
+        if "d0_" + f in fx:
+            assert cases.scale_err(got[f], fx["d0_" + f]) < TOL_EVAL, f
+    np.testing.assert_array_equal(got["ncnt"], fx["d0_ncnt"])
+
+
+@pytest.mark.parametrize("name", ["sphere_n1000", "impact_n1200", "gas_n1500"])
+def test_steps_match_reference(name):
+    fx = cases.load(name)
+    cfg, keep = cases.config_of(fx)
+    steps = len(fx["dts"]) - 1
+    with GpuSolver(cfg, keep) as g:
+        g.set_state(cases.state_of(fx, "s0_"))
+        g.timestep = float(fx["dts"][0])
+        dts = []
+        for k in range(steps):
+            g.step(1)
+            dts.append(g.timestep)
+        got = g.get_state()
+    np.testing.assert_allclose(dts, fx["dts"][1:], rtol=1e-10)
+    for f in ["r", "v", "dv", "rho", "drho", "u", "du", "divv", "S", "dS", "D", "dD"]:
+        if "sN_" + f in fx:
+            assert cases.scale_err(got[f], fx["sN_" + f]) < TOL_STEPS, f
+
+
+def test_deterministic_fp64():
+    fx = cases.load("impact_n1200")
+    cfg, keep = cases.config_of(fx)
+    out = []
+    for _ in range(2):
+        with GpuSolver(cfg, keep) as g:
+            g.set_state(cases.state_of(fx, "s0_"))
+            g.step(3)
+            out.append(g.get_state(["r", "v", "rho", "u", "S", "D"]))
+    for f in out[0]:
+        np.testing.assert_array_equal(out[0][f], out[1][f])
+
+
+def test_nonfinite_input_is_reported():
+    fx = cases.load("sphere_n1000")
+    cfg, keep = cases.config_of(fx)
+    st = cases.state_of(fx, "s0_")
+    st["u"][17] = np.nan
+    with GpuSolver(cfg, keep) as g:
+        g.set_state(st)
+        g.integrate()
+        rc, bad = g.check_finite()
+    assert rc == abi.ERR_NONFINITE
+    assert bad <= 17
+
+
+def test_quantity_size_mismatch_is_rejected():
+    fx = cases.load("sphere_n1000")
+    cfg, keep = cases.config_of(fx)
+    with GpuSolver(cfg, keep) as g:
+        small = np.ones(5)
+        # through the C ABI: a count that does not match the handle's particle count is rejected
+        assert g._lib.sphgpu_set_quantity(g._h, abi.Q_MASS, 0, small.ctypes.data, 5) == abi.ERR_ARGUMENT
+        assert b"5 values" in g._lib.sphgpu_last_error(g._h)
+        # unknown quantity id and a quantity the configured physics does not hold
+        assert g._lib.sphgpu_set_quantity(g._h, 999, 0, small.ctypes.data, g.n) == abi.ERR_ARGUMENT
+        with pytest.raises(SphGpuError):
+            g.get_quantity(abi.Q_DEVIATORIC_STRESS, 0)
+
+
+def test_single_particle_and_pairless():
+    r = np.array([0.0, 0.0, 0.0, 1.0])
+    with gas_solver(r) as g:
+        pi, pj = g.pairs()
+        g.integrate()
+        st = g.get_state(["dv", "ncnt"])
+    assert pi.size == 0
+    assert st["ncnt"][0] == 0
+    np.testing.assert_array_equal(st["dv"], 0.0)

@@ -1,0 +1,345 @@
+"""Benchmark of the per-step SPH + Barnes-Hut gravity hot path on GB300.
+
+Workload (the mixed-precision configuration of the headline metric): a basalt target of 1,000,000
+requested HCP particles (R = 50 km) hit by a 20,000-particle impactor (R = 5 km) at 5 km/s and 45 degrees;
+Hooke + von Mises + Grady-Kipp damage, SolidStressForce + StandardAV, adaptive h, Barnes-Hut theta = 0.5
+octupole, predictor-corrector with the Courant criterion. One step is one ITimeStepping::step over the whole
+particle set. The state (~300 B per particle) exceeds the 129 MB L2, so no flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line (rank 0). `value` is the mixed-precision path with the state resident in HBM; `e2e`
+is the same metric through the public API with host buffers (positions and velocities uploaded from pinned
+host memory and positions, velocities, density and energy read back every step); `fp64` reports the plain
+FP64 GPU path on the same workload and the mixed path's error against it. `--impl reference` times the CPU
+implementation of the path (the oracle restatement of the reference, all host threads) on the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "particle-steps/s (1M SPH+gravity): mixed vs FP64 GPU at stated err; adjoint/fwd"
+UNIT = "particle-steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--n-target", type=int, default=1_000_000)
+    ap.add_argument("--n-impactor", type=int, default=20_000)
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--cpu-steps", type=int, default=1)
+    ap.add_argument("--profile-only", action="store_true", help="warm-up + timed steps only (for ncu)")
+    return ap.parse_args()
+
+
+def workload(args):
+    from opensph_gb300 import abi, initial
+
+    st, mats = initial.impact_state(args.n_target, 5.0e4, args.n_impactor, 5.0e3, speed=5.0e3, angle_deg=45.0,
+                                    seed=1234)
+    n = len(st["m"])
+    return st, mats, n
+
+
+def make_config(n, mats, precision):
+    from opensph_gb300 import abi
+
+    return abi.make_config(n, mats, forces=abi.FORCE_PRESSURE | abi.FORCE_SOLID_STRESS | abi.FORCE_SELF_GRAVITY,
+                           adaptive_h=True, precision=precision, initial_timestep=0.03)
+
+
+def config_json(args, n):
+    return {"workload": f"solid impact: basalt target {args.n_target} HCP requested (R 50 km) + impactor "
+                        f"{args.n_impactor} (R 5 km) at 5 km/s, 45 deg; von Mises + Grady-Kipp, adaptive h, "
+                        f"BH theta 0.5 octupole, predictor-corrector + Courant",
+            "particles": n, "precision": "mixed (FP32 pair sums, FP64 state/integrator)",
+            "l2": "state larger than L2 (no flush)", "parallelism": "replicas"}
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+# algorithmic bytes per particle of the pair-loop kernel of this workload (solid physics, mixed inputs):
+# reads the particle's own packed inputs (4 x float4 = 64 B, S/rho^2 5 x 4 B, FP64 r, rho, p, S for the
+# finalize 32 + 16 + 40 B, agrav 32 B, flaw data eps_min, m_zero, growth, n_flaws, D 36 B, mat 4 B) = 244 B;
+# writes dv 32, du, drho, divv 24, ncnt 4, gradv 48, dS 40, dD 8, v.h 8 = 164 B. Neighbour data are
+# re-read from cache, not counted.
+PAIR_BYTES_PER_PARTICLE = 244 + 164
+
+
+def run_gpu(args, rank, world):
+    import torch
+
+    from opensph_gb300 import abi
+    from opensph_gb300.solver import GpuSolver
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    st, mats, n = workload(args)
+    cfg, keep = make_config(n, mats, abi.PRECISION_MIXED)
+    cfg.device = dev
+    g = GpuSolver(cfg, keep)
+    g.set_state(st)
+    stream = torch.cuda.ExternalStream(g.stream)
+    g.step(args.warmup)
+    g.synchronize()
+    if args.profile_only:
+        g.step(args.steps)
+        g.synchronize()
+        return None
+    g.set_profiling(True)
+    g.phase_times()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev) as clk:
+        start.record(stream)
+        g.step(args.steps)
+        end.record(stream)
+        end.synchronize()
+    torch.cuda.synchronize()
+    ms = start.elapsed_time(end)
+    phases, launches = g.phase_times()
+    g.set_profiling(False)
+    ms_t = torch.tensor([ms], device=f"cuda:{dev}")
+    if world > 1:
+        torch.distributed.all_reduce(ms_t, op=torch.distributed.ReduceOp.MAX)
+    ms = float(ms_t.item())
+    value = n * args.steps * world / (ms * 1e-3)
+
+    # end-to-end through the public API with host buffers
+    pinned = {k: torch.empty(4 * n, dtype=torch.float64, pin_memory=True) for k in ("r", "v")}
+    outs = {k: torch.empty(sz, dtype=torch.float64, pin_memory=True) for k, sz in
+            (("r", 4 * n), ("v", 4 * n), ("rho", n), ("u", n))}
+    state_now = g.get_state(["r", "v"])
+    pinned["r"].numpy()[:] = state_now["r"]
+    pinned["v"].numpy()[:] = state_now["v"]
+    lib, hnd = g._lib, g._h
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_start = torch.cuda.Event(enable_timing=True)
+    e2e_end = torch.cuda.Event(enable_timing=True)
+    e2e_start.record(stream)
+    for _ in range(args.steps):
+        g._check(lib.sphgpu_set_quantity(hnd, abi.Q_POSITION, 0, pinned["r"].data_ptr(), n))
+        g._check(lib.sphgpu_set_quantity(hnd, abi.Q_POSITION, 1, pinned["v"].data_ptr(), n))
+        g.step(1)
+        g._check(lib.sphgpu_get_quantity(hnd, abi.Q_POSITION, 0, outs["r"].data_ptr(), n))
+        g._check(lib.sphgpu_get_quantity(hnd, abi.Q_POSITION, 1, outs["v"].data_ptr(), n))
+        g._check(lib.sphgpu_get_quantity(hnd, abi.Q_DENSITY, 0, outs["rho"].data_ptr(), n))
+        g._check(lib.sphgpu_get_quantity(hnd, abi.Q_ENERGY, 0, outs["u"].data_ptr(), n))
+        pinned["r"].copy_(outs["r"])
+        pinned["v"].copy_(outs["v"])
+    e2e_end.record(stream)
+    e2e_end.synchronize()
+    e2e_wall = time.perf_counter() - t0
+    e2e_ms = max(e2e_start.elapsed_time(e2e_end), e2e_wall * 1e3)
+    e2e_t = torch.tensor([e2e_ms], device=f"cuda:{dev}")
+    if world > 1:
+        torch.distributed.all_reduce(e2e_t, op=torch.distributed.ReduceOp.MAX)
+    e2e_value = n * args.steps * world / (float(e2e_t.item()) * 1e-3)
+    g.close()
+
+    result = {"n": n, "ms": ms, "value": value, "phases": phases, "launches": launches,
+              "clocks": clk.summary(), "e2e": {"value": e2e_value, "unit": UNIT,
+                                                 "h2d_bytes_per_step": 2 * 32 * n,
+                                                 "d2h_bytes_per_step": (32 + 32 + 8 + 8) * n}}
+    if rank == 0 and not args.no_fp64:
+        result["fp64"] = compare_fp64(args, st, mats, n, cfg, dev)
+    return result
+
+
+def compare_fp64(args, st, mats, n, mixed_cfg, dev):
+    """Plain FP64 GPU path on the same workload: speed, and the mixed path's error against it."""
+    import torch
+
+    from opensph_gb300 import abi
+    from opensph_gb300.solver import GpuSolver
+
+    steps = args.warmup + args.steps
+    out = {}
+    states = {}
+    for name, prec in (("fp64", abi.PRECISION_FP64), ("mixed", abi.PRECISION_MIXED)):
+        cfg, keep = make_config(n, mats, prec)
+        cfg.device = dev
+        with GpuSolver(cfg, keep) as g:
+            g.set_state({k: v.copy() for k, v in st.items()})
+            stream = torch.cuda.ExternalStream(g.stream)
+            if name == "fp64":
+                g.step(args.warmup)
+                s0 = torch.cuda.Event(enable_timing=True)
+                s1 = torch.cuda.Event(enable_timing=True)
+                s0.record(stream)
+                g.step(args.steps)
+                s1.record(stream)
+                s1.synchronize()
+                out["value"] = n * args.steps / (s0.elapsed_time(s1) * 1e-3)
+            else:
+                g.step(steps)
+            states[name] = g.get_state(["r", "v", "rho", "u", "D"])
+    ref, mix = states["fp64"], states["mixed"]
+
+    def rel(a, b):
+        return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+    vref = ref["v"].reshape(-1, 4)[:, :3]
+    vmix = mix["v"].reshape(-1, 4)[:, :3]
+    out["steps_compared"] = steps
+    out["rel_err_density"] = rel(mix["rho"], ref["rho"])
+    out["rel_err_velocity"] = rel(vmix, vref)
+    out["rel_err_energy"] = rel(mix["u"], ref["u"])
+    out["max_abs_err_damage"] = float(np.max(np.abs(mix["D"] - ref["D"])))
+    return out
+
+
+def cpu_sample(args, st, mats, n, steps):
+    """The CPU implementation (oracle restatement of the reference, all host threads) on the same state."""
+    from opensph_gb300 import abi
+    from oracle import oracle
+
+    cfg, keep = make_config(n, mats, abi.PRECISION_FP64)
+    work = {k: v.copy() for k, v in st.items()}
+    oracle.set_threads(0)
+    t0 = time.perf_counter()
+    oracle.run(cfg, work, steps, 0.03)
+    dt = time.perf_counter() - t0
+    return n * steps / dt, dt
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        st, mats, n = workload(args)
+        cores = os.cpu_count() or 1
+        steps = args.warmup + args.steps
+        value, secs = cpu_sample(args, st, mats, n, steps)
+        line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs * 1e3 / steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": config_json(args, n),
+                "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                                 "sample": f"{steps} full steps of the {n}-particle workload (FP64 oracle)"},
+                "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+    import torch
+
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    res = run_gpu(args, rank, world)
+    if res is None or rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+    n = res["n"]
+    ms_step = res["ms"] / args.steps
+    pair_ms = res["phases"]["sph_eval"] / args.steps
+    peak, peak_kind = peaks()
+    achieved = PAIR_BYTES_PER_PARTICLE * n / (pair_ms * 1e-3) / 1e9 if pair_ms > 0 else None
+    line = {
+        "metric": METRIC, "value": res["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32/f64", "data": "synthetic", "config": config_json(args, n),
+        "e2e": res["e2e"], "gpu_launches": res["launches"], "clocks": res["clocks"],
+        "phases_ms_per_step": {k: v / args.steps for k, v in res["phases"].items()},
+        "roofline": {"kernel": "pairSumMixedKernel", "bound": "hbm", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak if achieved else None, "traffic": None,
+                     "peak_source": peak_kind,
+                     "algorithmic_bytes_per_particle": PAIR_BYTES_PER_PARTICLE},
+    }
+    if "fp64" in res:
+        line["fp64"] = res["fp64"]
+    if not args.no_cpu:
+        st, mats, n2 = workload(args)
+        value, secs = cpu_sample(args, st, mats, n2, args.cpu_steps)
+        line["cpu_baseline"] = {"value": value, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+                                "sample": f"{args.cpu_steps} full step(s) of the {n2}-particle workload "
+                                          f"({secs:.1f} s, FP64 oracle, all host threads)"}
+    print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

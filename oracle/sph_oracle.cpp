@@ -38,14 +38,14 @@ int threadCount() {
     return hc ? int(hc) : 1;
 }
 
-void parallelFor(uint64_t n, const std::function<void(uint64_t, uint64_t)>& body) {
+void parallelFor(uint64_t n, const std::function<void(uint64_t, uint64_t)>& body, uint64_t grain = 64) {
     const int nt = threadCount();
-    if (nt <= 1 || n < 1024) {
+    if (nt <= 1 || n <= grain) {
         body(0, n);
         return;
     }
     // dynamic chunks so that irregular work (tree walk, neighbour counts) balances
-    const uint64_t chunk = std::max<uint64_t>(64, n / (uint64_t(nt) * 16));
+    const uint64_t chunk = std::max<uint64_t>(grain, n / (uint64_t(nt) * 16));
     std::atomic<uint64_t> next{ 0 };
     std::vector<std::thread> pool;
     for (int t = 0; t < nt; ++t) {
@@ -507,13 +507,12 @@ inline int i2(int a, int b) {
     static const int t[3][3] = { { 0, 1, 2 }, { 1, 3, 4 }, { 2, 4, 5 } };
     return t[a][b];
 }
+// index of the symmetric rank-3 component (a, b, c) in {xxx xxy xxz xyy xyz xzz yyy yyz yzz zzz}
+static const int kI3[3][3][3] = { { { 0, 1, 2 }, { 1, 3, 4 }, { 2, 4, 5 } },
+    { { 1, 3, 4 }, { 3, 6, 7 }, { 4, 7, 8 } },
+    { { 2, 4, 5 }, { 4, 7, 8 }, { 5, 8, 9 } } };
 inline int i3(int a, int b, int c) {
-    int s[3] = { a, b, c };
-    std::sort(s, s + 3);
-    static const int t[3][3][3] = { { { 0, 1, 2 }, { 1, 3, 4 }, { 2, 4, 5 } },
-        { { 1, 3, 4 }, { 3, 6, 7 }, { 4, 7, 8 } },
-        { { 2, 4, 5 }, { 4, 7, 8 }, { 5, 8, 9 } } };
-    return t[s[0]][s[1]][s[2]];
+    return kI3[a][b][c];
 }
 
 struct BhNode {
@@ -970,7 +969,7 @@ struct BarnesHutTree {
             std::vector<int> check, plist, nlist;
         };
         std::vector<Task> tasks{ Task{ 0, {}, {}, {} } };
-        for (int level = 0; level < 8; ++level) {
+        for (int level = 0; level < 12; ++level) {
             std::vector<Task> next;
             bool expanded = false;
             for (Task& t : tasks) {
@@ -1015,11 +1014,14 @@ struct BarnesHutTree {
                 break;
             }
         }
-        parallelFor(tasks.size(), [&](uint64_t from, uint64_t to) {
-            for (uint64_t k = from; k < to; ++k) {
-                evalNode(tasks[k].node, tasks[k].check, tasks[k].plist, tasks[k].nlist, dv);
-            }
-        });
+        parallelFor(
+            tasks.size(),
+            [&](uint64_t from, uint64_t to) {
+                for (uint64_t k = from; k < to; ++k) {
+                    evalNode(tasks[k].node, tasks[k].check, tasks[k].plist, tasks[k].nlist, dv);
+                }
+            },
+            1);
     }
 
     // BarnesHut::evalImpl / evalExact (core/gravity/BarnesHut.cpp:118-175, :364-374)

@@ -28,6 +28,7 @@ UNITS = {
     "sph64.cu": ["-fmad=false"],
     "gravity.cu": ["-fmad=false"],
     "sph32.cu": [],
+    "gravity32.cu": [],
 }
 
 

@@ -27,6 +27,7 @@ struct sphgpu_handle {
     double* d_lut_sph = nullptr;   // LutKernel<3>(CubicSpline<3>) gradient table
     double* d_lut_grav = nullptr;  // LutKernel<3>(GravityKernel<CubicSpline<3>>) gradient table
     float* d_lut_sph_f = nullptr;
+    float* d_lut_grav_f = nullptr;
     double* d_dt = nullptr;
     double* d_dt_min = nullptr;
     uint32_t* d_err = nullptr;
@@ -303,8 +304,13 @@ sphgpu_status evalGravity(sphgpu_handle* h) {
     }
     {
         Phase ph(h, SPHGPU_PHASE_GRAVITY_EVAL);
-        launchGravityWalk(h->s, h->tree, h->ph, h->d_lut_grav, h->d_err, h->stream);
-        h->launches += 1;
+        if (h->ph.precision == SPHGPU_PRECISION_MIXED) {
+            launchGravityWalkMixed(h->s, h->tree, h->ph, h->d_lut_grav_f, h->d_err, h->stream);
+            h->launches += 2;
+        } else {
+            launchGravityWalk(h->s, h->tree, h->ph, h->d_lut_grav, h->d_err, h->stream);
+            h->launches += 2;
+        }
     }
     h->gravity_current = true;
     return SPHGPU_OK;
@@ -499,6 +505,7 @@ sphgpu_status sphgpu_create(const sphgpu_config* config, sphgpu_handle** out) {
     A(&h->d_lut_sph, LUT_ENTRIES + 1);
     A(&h->d_lut_grav, LUT_ENTRIES + 1);
     A(&h->d_lut_sph_f, LUT_ENTRIES + 1);
+    A(&h->d_lut_grav_f, LUT_ENTRIES + 1);
     A(&h->d_dt, 1);
     A(&h->d_dt_min, 1);
     A(&h->d_err, 1);
@@ -527,6 +534,7 @@ sphgpu_status sphgpu_create(const sphgpu_config* config, sphgpu_handle** out) {
     const std::vector<double> lutS = makeLut(cubicGrad);
     const std::vector<double> lutG = makeLut(gravGrad);
     std::vector<float> lutSf(lutS.begin(), lutS.end());
+    std::vector<float> lutGf(lutG.begin(), lutG.end());
     const double dt0 = config->initial_timestep;
     const double big = 1.7976931348623157e308;
     e = cudaMemcpy(h->d_mats, md.data(), md.size() * sizeof(MaterialD), cudaMemcpyHostToDevice);
@@ -538,6 +546,9 @@ sphgpu_status sphgpu_create(const sphgpu_config* config, sphgpu_handle** out) {
     }
     if (e == cudaSuccess) {
         e = cudaMemcpy(h->d_lut_sph_f, lutSf.data(), lutSf.size() * sizeof(float), cudaMemcpyHostToDevice);
+    }
+    if (e == cudaSuccess) {
+        e = cudaMemcpy(h->d_lut_grav_f, lutGf.data(), lutGf.size() * sizeof(float), cudaMemcpyHostToDevice);
     }
     if (e == cudaSuccess) {
         e = cudaMemcpy(h->d_dt, &dt0, sizeof(double), cudaMemcpyHostToDevice);

@@ -20,7 +20,7 @@
 // particle list and node list. Each lane owns one particle of the leaf (leaf size <= 32) and evaluates the
 // exact softened pair terms and octupole expansions as soon as the warp classifies them.
 
-#include "state.h"
+#include "tree.cuh"
 
 namespace sphgpu {
 
@@ -556,38 +556,6 @@ __global__ void __launch_bounds__(BUILD_THREADS) splitLevelKernel(PosView pv, ui
     }
 }
 
-// symmetric tensor index helpers: rank 2 {xx xy xz yy yz zz}, rank 3 {xxx xxy xxz xyy xyz xzz yyy yyz yzz zzz}
-__device__ __forceinline__ int i2(int a, int b) {
-    const int lo = min(a, b), hi = max(a, b);
-    return lo == 0 ? hi : (lo == 1 ? 2 + hi : 5);
-}
-__device__ __forceinline__ int i3(int a, int b, int c) {
-    int x = a, y = b, z = c, t;
-    if (x > y) {
-        t = x;
-        x = y;
-        y = t;
-    }
-    if (y > z) {
-        t = y;
-        y = z;
-        z = t;
-    }
-    if (x > y) {
-        t = x;
-        x = y;
-        y = t;
-    }
-    // index of the sorted triple in {000 001 002 011 012 022 111 112 122 222}
-    if (x == 0) {
-        return y == 0 ? z : (y == 1 ? 2 + z : 5);
-    }
-    if (x == 1) {
-        return y == 1 ? 5 + z : 8;
-    }
-    return 9;
-}
-
 // BarnesHut::buildLeaf (core/gravity/BarnesHut.cpp:376-437), one thread per leaf
 __device__ void buildLeaf(const dbl4* __restrict__ r, const double* __restrict__ m, double G,
     const uint32_t* __restrict__ idx, double thetaInv, BhNodeGeom& g, BhNodeMoments& mo) {
@@ -738,111 +706,6 @@ __global__ void momentsLevelKernel(const dbl4* __restrict__ r, const double* __r
 }
 
 // ---------------------------------------------------------------------------------------------------------
-// evaluation helpers
-// ---------------------------------------------------------------------------------------------------------
-
-// GravityLutKernel::grad (core/sph/kernel/GravityKernel.h:69-80) of LutKernel<3>(GravityKernel<CubicSpline>)
-__device__ __forceinline__ void gravGrad(double rx, double ry, double rz, double h, const double* __restrict__ lut,
-    int kernelRadius, double& gx, double& gy, double& gz) {
-    const double hInv = 1. / h;
-    const double sx = rx * hInv, sy = ry * hInv, sz = rz * hInv;
-    const double qSqr = sx * sx + sy * sy + sz * sz;
-    const double rad = double(kernelRadius);
-    if (qSqr + SPH_EPS >= rad * rad) {
-        const double len = sqrt(rx * rx + ry * ry + rz * rz);
-        const double l3 = len * len * len;
-        gx = rx / l3;
-        gy = ry / l3;
-        gz = rz / l3;
-        return;
-    }
-    const double floatIdx = (double(LUT_ENTRIES) * (1. / (2. * 2.))) * qSqr;
-    const int idx1 = int(floatIdx);
-    const double ratio = floatIdx - double(idx1);
-    const double g = __ldg(lut + idx1) * (1. - ratio) + __ldg(lut + idx1 + 1) * ratio;
-    const double h3 = hInv * hInv * hInv;
-    gx = (h3 * rx) * g;
-    gy = (h3 * ry) * g;
-    gz = (h3 * rz) * g;
-}
-
-// evaluateGravity (core/gravity/Moments.h:336-360) at dr = r_i - com, accumulated into a
-__device__ __forceinline__ void evalMultipole(double drx, double dry, double drz, const BhNodeMoments& mo, int order,
-    double& ax, double& ay, double& az) {
-    const double invDistSqr = 1. / (drx * drx + dry * dry + drz * drz);
-    double gamma[5];
-    gamma[0] = -sqrt(invDistSqr);
-    for (int i = 1; i < 5; ++i) {
-        gamma[i] = -(2. * i - 1.) * invDistSqr * gamma[i - 1];
-    }
-    const double x[3] = { -drx, -dry, -drz };
-    double a[3] = { 0., 0., 0. };
-    if (order >= 3) {
-        double Q1[3], Q0 = 0.;
-        for (int i = 0; i < 3; ++i) {
-            double s = 0.;
-            for (int j = 0; j < 3; ++j) {
-                for (int k = 0; k < 3; ++k) {
-                    s += mo.q3[i3(i, j, k)] * x[j] * x[k];
-                }
-            }
-            Q1[i] = s * 0.5;
-            Q0 += s * x[i];
-        }
-        Q0 *= 1. / 6.;
-        for (int i = 0; i < 3; ++i) {
-            a[i] += gamma[4] * x[i] * Q0 + gamma[3] * Q1[i];
-        }
-    }
-    if (order >= 2) {
-        double Q1[3], Q0 = 0.;
-        for (int i = 0; i < 3; ++i) {
-            Q1[i] = mo.q2[i2(i, 0)] * x[0] + mo.q2[i2(i, 1)] * x[1] + mo.q2[i2(i, 2)] * x[2];
-            Q0 += Q1[i] * x[i];
-        }
-        Q0 *= 0.5;
-        for (int i = 0; i < 3; ++i) {
-            a[i] += gamma[3] * x[i] * Q0 + gamma[2] * Q1[i];
-        }
-    }
-    for (int i = 0; i < 3; ++i) {
-        a[i] += gamma[1] * x[i] * mo.m0;
-    }
-    ax += a[0];
-    ay += a[1];
-    az += a[2];
-}
-
-// Sphere::intersectsBox: 0 box outside, 1 intersection, 2 box inside the sphere
-__device__ int intersectsBox(const double p[3], double rad, const double lo[3], const double hi[3]) {
-    double l2 = 0., r2 = 0.;
-    for (int d = 0; d < 3; ++d) {
-        const double lft = fmax(lo[d] - p[d], 0.);
-        const double rgt = fmax(p[d] - hi[d], 0.);
-        l2 = d == 0 ? lft * lft : l2 + lft * lft;
-        r2 = d == 0 ? rgt * rgt : r2 + rgt * rgt;
-    }
-    const double rSqr = rad * rad;
-    const double distSqr = rSqr - l2 - r2;
-    if (!(distSqr > 0.)) {
-        return 0;
-    }
-    const double sx = hi[0] - lo[0], sy = hi[1] - lo[1], sz = hi[2] - lo[2];
-    const double vx[8] = { lo[0], lo[0] + sx, lo[0] + 0., lo[0] + 0., hi[0], hi[0] - sx, hi[0] - 0., hi[0] - 0. };
-    const double vy[8] = { lo[1], lo[1] + 0., lo[1] + sy, lo[1] + 0., hi[1], hi[1] - 0., hi[1] - sy, hi[1] - 0. };
-    const double vz[8] = { lo[2], lo[2] + 0., lo[2] + 0., lo[2] + sz, hi[2], hi[2] - 0., hi[2] - 0., hi[2] - sz };
-    for (int k = 0; k < 8; ++k) {
-        const double dx = vx[k] - p[0], dy = vy[k] - p[1], dz = vz[k] - p[2];
-        if (!(dx * dx + dy * dy + dz * dz < rSqr)) {
-            return 1;
-        }
-    }
-    return 2;
-}
-
-enum : int { CL_KEEP = 0, CL_PARTICLES = 1, CL_NODE = 2, CL_OPEN = 3 };
-
-// ---------------------------------------------------------------------------------------------------------
 // walk: one warp per leaf
 // ---------------------------------------------------------------------------------------------------------
 
@@ -850,9 +713,9 @@ constexpr int WALK_THREADS = 128;
 
 __global__ void __launch_bounds__(WALK_THREADS) walkKernel(const dbl4* __restrict__ r,
     const double* __restrict__ m, double G, const uint32_t* __restrict__ idx, const BhNodeGeom* __restrict__ geom,
-    const BhNodeMoments* __restrict__ mom, const uint32_t* __restrict__ leaves, uint32_t nLeaves,
-    const double* __restrict__ lut, int kernelRadius, int order, int32_t* scratch, uint32_t listCap,
-    dbl4* agrav, unsigned long long* stats, uint32_t* devError) {
+    const BhNodeMoments* __restrict__ mom, const float* __restrict__ nodef, const uint32_t* __restrict__ leaves,
+    uint32_t nLeaves, const double* __restrict__ lut, int kernelRadius, int order, int32_t* scratch,
+    uint32_t listCap, dbl4* agrav, unsigned long long* stats, uint32_t* devError) {
     __shared__ int32_t pathSh[WALK_THREADS / 32][MAX_PATH];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
@@ -888,6 +751,8 @@ __global__ void __launch_bounds__(WALK_THREADS) walkKernel(const dbl4* __restric
         depth = __shfl_sync(0xffffffffu, depth, 0);
         __syncwarp();
         const bool active = uint32_t(lane) < cnt;
+        const float* lf = nodef + size_t(leaf) * NODEF;
+        const double lcom[3] = { lg.com[0], lg.com[1], lg.com[2] };
         uint32_t pi = 0;
         dbl4 ri = mkd4(0., 0., 0., 1.);
         if (active) {
@@ -904,11 +769,11 @@ __global__ void __launch_bounds__(WALK_THREADS) walkKernel(const dbl4* __restric
             const int par = path[k - 1];
             const BhNodeGeom& pg = geom[par];
             const int sib = pg.left == ev ? pg.right : pg.left;
-            const bool evLeaf = (k == depth);
-            double elo[3], ehi[3];
+            WalkFrame fr;
+            setFrame(fr, geom[ev], lcom, k == depth);
             for (int d = 0; d < 3; ++d) {
-                elo[d] = geom[ev].lo[d];
-                ehi[d] = geom[ev].hi[d];
+                fr.lh[d] = lf[d];
+                fr.ll[d] = lf[3 + d];
             }
             if (lane == 0) {
                 cur[ncur] = sib;
@@ -922,19 +787,7 @@ __global__ void __launch_bounds__(WALK_THREADS) walkKernel(const dbl4* __restric
                 int node = -1, cls = CL_KEEP;
                 if (uint32_t(lane) < batch) {
                     node = cur[e];
-                    const BhNodeGeom& ng = geom[node];
-                    if (ng.r_open == 0.) {
-                        cls = CL_PARTICLES;
-                    } else {
-                        const int res = intersectsBox(ng.com, ng.r_open, elo, ehi);
-                        if (res == 2 || (evLeaf && res != 0)) {
-                            cls = ng.left < 0 ? CL_PARTICLES : CL_OPEN;
-                        } else if (res == 0) {
-                            cls = CL_NODE;
-                        } else {
-                            cls = CL_KEEP;
-                        }
-                    }
+                    cls = classifyEntry(node, geom, nodef, fr);
                 }
                 const unsigned mKeep = __ballot_sync(0xffffffffu, uint32_t(lane) < batch && cls == CL_KEEP);
                 const unsigned mOpen = __ballot_sync(0xffffffffu, cls == CL_OPEN);
@@ -1102,6 +955,9 @@ cudaError_t treeAllocate(Tree& t, uint32_t n, uint32_t leafSize) {
     alloc((void**)&t.walk_scratch, size_t(t.walk_warps) * 2 * t.walk_capacity * sizeof(int32_t));
     alloc((void**)&t.stats, 4 * sizeof(unsigned long long));
     alloc((void**)&t.bbox, 8 * sizeof(unsigned long long));
+    alloc((void**)&t.nodef, size_t(t.node_capacity) * 28 * sizeof(float));
+    alloc((void**)&t.pf, nn * sizeof(float4));
+    alloc((void**)&t.mf, nn * sizeof(float));
     if (e == cudaSuccess) {
         e = cudaMallocHost((void**)&t.counters_host, 8 * sizeof(uint32_t));
     }
@@ -1110,7 +966,7 @@ cudaError_t treeAllocate(Tree& t, uint32_t n, uint32_t leafSize) {
 
 void treeFree(Tree& t) {
     void* ptrs[] = { t.idx, t.scratch_b, t.scratch_s, t.geom, t.mom, t.seg[0], t.seg[1], t.counters, t.leaves,
-        t.walk_scratch, t.stats, t.bbox };
+        t.walk_scratch, t.stats, t.bbox, t.nodef, t.pf, t.mf };
     for (void* p : ptrs) {
         if (p) {
             cudaFree(p);
@@ -1190,7 +1046,9 @@ void launchGravityWalk(const DState& s, Tree& t, const Physics& ph, const double
         return;
     }
     const int blocks = int(t.walk_warps / (WALK_THREADS / 32));
-    walkKernel<<<blocks, WALK_THREADS, 0, st>>>(s.r, s.m, ph.G, t.idx, t.geom, t.mom, t.leaves, t.leaf_count, lut,
+    launchPrepareWalk(s, t, ph, st);
+    walkKernel<<<blocks, WALK_THREADS, 0, st>>>(s.r, s.m, ph.G, t.idx, t.geom, t.mom, t.nodef, t.leaves,
+        t.leaf_count, lut,
         ph.kernel_radius,
         ph.multipole_order, t.walk_scratch, t.walk_capacity, s.agrav, t.stats, devError);
 }

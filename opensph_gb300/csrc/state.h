@@ -147,6 +147,9 @@ struct Tree {
     uint32_t walk_capacity = 0;       // entries per list per warp
     unsigned long long* stats = nullptr; // device: approx, exact
     unsigned long long* bbox = nullptr;  // device: flipped bounding box of the root
+    float* nodef = nullptr;           // mixed walk: FP32 evaluation record per node (28 floats)
+    float4* pf = nullptr;             // mixed walk: particle position relative to its leaf's centre of mass, h
+    float* mf = nullptr;              // mixed walk: G * m in tree order
     std::vector<uint32_t> level_start; // host: first node id of each level
     uint32_t node_count = 0;
     uint32_t leaf_count = 0;
@@ -186,6 +189,9 @@ void treeFree(Tree& t);
 cudaError_t treeBuild(const DState& s, Tree& t, const Physics& ph, uint32_t* dev_error, cudaStream_t st);
 void launchGravityWalk(const DState& s, Tree& t, const Physics& ph, const double* lut_grad, uint32_t* dev_error,
     cudaStream_t st);
+void launchPrepareWalk(const DState& s, Tree& t, const Physics& ph, cudaStream_t st);
+void launchGravityWalkMixed(const DState& s, Tree& t, const Physics& ph, const float* lut_grad_f,
+    uint32_t* dev_error, cudaStream_t st);
 void launchGravityPoints(const DState& s, const Tree& t, const Physics& ph, const double* lut_grad,
     const dbl4* points, dbl4* acc, uint32_t npoints, cudaStream_t st);
 

@@ -43,6 +43,8 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--cpu-steps", type=int, default=1)
+    ap.add_argument("--error-steps", type=int, default=100,
+                    help="steps after which the mixed path is compared with the FP64 GPU path")
     ap.add_argument("--profile-only", action="store_true", help="warm-up + timed steps only (for ncu)")
     return ap.parse_args()
 
@@ -233,7 +235,7 @@ def compare_fp64(args, st, mats, n, mixed_cfg, dev):
     from opensph_gb300 import abi
     from opensph_gb300.solver import GpuSolver
 
-    steps = args.warmup + args.steps
+    steps = max(args.error_steps, args.warmup + args.steps)
     out = {}
     states = {}
     for name, prec in (("fp64", abi.PRECISION_FP64), ("mixed", abi.PRECISION_MIXED)):
@@ -251,9 +253,12 @@ def compare_fp64(args, st, mats, n, mixed_cfg, dev):
                 s1.record(stream)
                 s1.synchronize()
                 out["value"] = n * args.steps / (s0.elapsed_time(s1) * 1e-3)
+                out["ms_per_step"] = s0.elapsed_time(s1) / args.steps
+                g.step(steps - args.warmup - args.steps)
             else:
                 g.step(steps)
             states[name] = g.get_state(["r", "v", "rho", "u", "D"])
+            out[f"{name}_final_timestep"] = g.timestep
     ref, mix = states["fp64"], states["mixed"]
 
     def rel(a, b):

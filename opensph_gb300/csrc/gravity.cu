@@ -232,6 +232,8 @@ __global__ void initRootKernel(uint32_t n, uint32_t* idx, BhSegment* seg, BhNode
         counters[0] = 1;
         counters[1] = 0;
         counters[2] = 0;
+        counters[3] = 0;
+        counters[4] = 0;
     }
 }
 
@@ -348,7 +350,8 @@ __device__ void blockArgExtreme(double& val, uint32_t& pos, bool isMax, double* 
 
 __global__ void __launch_bounds__(BUILD_THREADS) splitLevelKernel(PosView pv, uint32_t* idx, uint32_t* posB,
     uint32_t* posS, const BhSegment* segIn, uint32_t nIn, BhSegment* segOut, BhNodeGeom* geom, uint32_t* counters,
-    uint32_t* leaves, uint32_t leafSize, uint32_t nodeCapacity, uint32_t segCapacity, uint32_t* devError) {
+    uint32_t* leaves, uint32_t leafSize, uint32_t nodeCapacity, uint32_t segCapacity, uint32_t* devError,
+    uint32_t maxSize) {
     __shared__ uint32_t shScan[32];
     __shared__ double shV[32];
     __shared__ uint32_t shP[32];
@@ -358,6 +361,9 @@ __global__ void __launch_bounds__(BUILD_THREADS) splitLevelKernel(PosView pv, ui
         const BhSegment sg = segIn[sidx];
         const uint32_t from = sg.from, to = sg.to;
         const int node = sg.node;
+        if (to - from > maxSize) {
+            continue; // large segments are split by the multi-CTA pipeline below
+        }
         if (to - from <= leafSize) {
             // KdTree::addLeaf: tight box of the leaf's points
             double lo[3] = { DBL_MAX, DBL_MAX, DBL_MAX }, hi[3] = { -DBL_MAX, -DBL_MAX, -DBL_MAX };
@@ -551,8 +557,306 @@ __global__ void __launch_bounds__(BUILD_THREADS) splitLevelKernel(PosView pv, ui
             }
             segOut[slot] = l;
             segOut[slot + 1] = r;
+            atomicMax(&counters[4], max(n1 - from, to - n1));
         }
         __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------------
+// multi-CTA split of large segments (same partition as splitLevelKernel, spread over chunks of CHUNK
+// elements): A chunk statistics for the three candidate dimensions -> B per-segment decision and chunk
+// offsets -> E global ranks of the elements above / below the split -> F pair count K, sliding midpoint,
+// nth_element, child segments -> G the K swaps of the two-pointer partition.
+// ---------------------------------------------------------------------------------------------------------
+
+__global__ void chunkListKernel(const BhSegment* __restrict__ segIn, uint32_t nIn, uint32_t maxSize,
+    uint32_t* counters, BhChunk* chunks, BhSegWork* work, uint32_t chunkCapacity, uint32_t* devError) {
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < nIn; s += gridDim.x * blockDim.x) {
+        const uint32_t len = segIn[s].to - segIn[s].from;
+        if (len <= maxSize) {
+            continue;
+        }
+        const uint32_t nc = (len + BH_CHUNK - 1) / BH_CHUNK;
+        const uint32_t c0 = atomicAdd(&counters[3], nc);
+        if (c0 + nc > chunkCapacity) {
+            atomicOr(devError, uint32_t(DEV_ERR_SEGMENT_CAPACITY));
+            continue;
+        }
+        for (uint32_t k = 0; k < nc; ++k) {
+            chunks[c0 + k].seg = s;
+            chunks[c0 + k].index = k;
+            chunks[c0 + k].first = c0;
+            chunks[c0 + k].count = nc;
+        }
+    }
+    (void)work;
+}
+
+__device__ __forceinline__ bool betterArg(double v, uint32_t p, double bv, uint32_t bp, bool isMax) {
+    return isMax ? (v > bv || (v == bv && p < bp)) : (v < bv || (v == bv && p < bp));
+}
+
+__global__ void __launch_bounds__(BUILD_THREADS) chunkStatsKernel(PosView pv, const uint32_t* __restrict__ idx,
+    const BhSegment* __restrict__ segIn, const BhChunk* __restrict__ chunks, BhChunkStats* stats) {
+    __shared__ uint32_t shScan[32];
+    __shared__ double shV[32];
+    __shared__ uint32_t shP[32];
+    const BhChunk ch = chunks[blockIdx.x];
+    const BhSegment sg = segIn[ch.seg];
+    const uint32_t from = sg.from + ch.index * BH_CHUNK;
+    const uint32_t to = min(sg.to, from + BH_CHUNK);
+    double center[3], last[3];
+    const uint32_t il = idx[sg.to - 1];
+    for (int d = 0; d < 3; ++d) {
+        center[d] = 0.5 * (sg.lo[d] + sg.hi[d]);
+        last[d] = pv.val(il, d);
+    }
+    uint32_t nb[3] = { 0, 0, 0 }, ns[3] = { 0, 0, 0 };
+    bool diff[3] = { false, false, false };
+    double mnv[3] = { DBL_MAX, DBL_MAX, DBL_MAX }, mxv[3] = { -DBL_MAX, -DBL_MAX, -DBL_MAX };
+    uint32_t mnp[3] = { 0xffffffffu, 0xffffffffu, 0xffffffffu }, mxp[3] = { 0xffffffffu, 0xffffffffu, 0xffffffffu };
+    for (uint32_t k = from + threadIdx.x; k < to; k += BUILD_THREADS) {
+        const dbl4 p = pv.r[idx[k]];
+        const double x[3] = { p.x, p.y, p.z };
+        for (int d = 0; d < 3; ++d) {
+            nb[d] += x[d] > center[d] ? 1u : 0u;
+            ns[d] += x[d] < center[d] ? 1u : 0u;
+            diff[d] = diff[d] || (x[d] != last[d]);
+            if (betterArg(x[d], k, mnv[d], mnp[d], false)) {
+                mnv[d] = x[d];
+                mnp[d] = k;
+            }
+            if (betterArg(x[d], k, mxv[d], mxp[d], true)) {
+                mxv[d] = x[d];
+                mxp[d] = k;
+            }
+        }
+    }
+    BhChunkStats out;
+    for (int d = 0; d < 3; ++d) {
+        out.nb[d] = blockSum(nb[d], shScan);
+        out.ns[d] = blockSum(ns[d], shScan);
+        out.diff[d] = __syncthreads_or(diff[d] ? 1 : 0) ? 1u : 0u;
+        double v = mnv[d];
+        uint32_t q = mnp[d];
+        blockArgExtreme(v, q, false, shV, shP);
+        out.minv[d] = v;
+        out.minp[d] = q;
+        v = mxv[d];
+        q = mxp[d];
+        blockArgExtreme(v, q, true, shV, shP);
+        out.maxv[d] = v;
+        out.maxp[d] = q;
+    }
+    if (threadIdx.x == 0) {
+        stats[blockIdx.x] = out;
+    }
+}
+
+// one thread per large segment (the thread of its first chunk)
+__global__ void segDecideKernel(const BhSegment* __restrict__ segIn, const BhChunk* __restrict__ chunks,
+    uint32_t nChunks, const BhChunkStats* __restrict__ stats, uint32_t* chunkOffB, uint32_t* chunkOffS,
+    BhSegWork* work) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nChunks || chunks[c].index != 0) {
+        return;
+    }
+    const BhChunk ch = chunks[c];
+    const BhSegment sg = segIn[ch.seg];
+    bool nonSingular[3] = { false, false, false };
+    for (uint32_t k = 0; k < ch.count; ++k) {
+        for (int d = 0; d < 3; ++d) {
+            nonSingular[d] = nonSingular[d] || stats[ch.first + k].diff[d] != 0;
+        }
+    }
+    double boxSize[3];
+    for (int d = 0; d < 3; ++d) {
+        boxSize[d] = sg.hi[d] - sg.lo[d];
+    }
+    int splitIdx = argMax3(boxSize);
+    bool degenerated = false;
+    for (int dim = 0; dim < 3; ++dim) {
+        if (!nonSingular[splitIdx]) {
+            boxSize[splitIdx] = 0.;
+            splitIdx = argMax3(boxSize);
+            if (boxSize[0] == 0. && boxSize[1] == 0. && boxSize[2] == 0.) {
+                degenerated = true;
+                break;
+            }
+        } else {
+            break;
+        }
+    }
+    BhSegWork w;
+    w.splitIdx = splitIdx;
+    w.mode = degenerated ? 2 : (sg.sliding <= 5 ? 0 : 1);
+    uint32_t ob = 0, os = 0;
+    double mnv = DBL_MAX, mxv = -DBL_MAX;
+    uint32_t mnp = 0xffffffffu, mxp = 0xffffffffu;
+    for (uint32_t k = 0; k < ch.count; ++k) {
+        const BhChunkStats& st = stats[ch.first + k];
+        chunkOffB[ch.first + k] = ob;
+        chunkOffS[ch.first + k] = os;
+        ob += st.nb[splitIdx];
+        os += st.ns[splitIdx];
+        if (betterArg(st.minv[splitIdx], st.minp[splitIdx], mnv, mnp, false)) {
+            mnv = st.minv[splitIdx];
+            mnp = st.minp[splitIdx];
+        }
+        if (betterArg(st.maxv[splitIdx], st.maxp[splitIdx], mxv, mxp, true)) {
+            mxv = st.maxv[splitIdx];
+            mxp = st.maxp[splitIdx];
+        }
+    }
+    w.nB = ob;
+    w.nS = os;
+    w.minv = mnv;
+    w.minp = mnp;
+    w.maxv = mxv;
+    w.maxp = mxp;
+    w.K = 0;
+    work[ch.seg] = w;
+}
+
+__global__ void __launch_bounds__(BUILD_THREADS) chunkRanksKernel(PosView pv, const uint32_t* __restrict__ idx,
+    const BhSegment* __restrict__ segIn, const BhChunk* __restrict__ chunks, const uint32_t* __restrict__ chunkOffB,
+    const uint32_t* __restrict__ chunkOffS, const BhSegWork* __restrict__ work, uint32_t* posB, uint32_t* posS) {
+    __shared__ uint32_t shScan[32];
+    const BhChunk ch = chunks[blockIdx.x];
+    const BhSegment sg = segIn[ch.seg];
+    const BhSegWork w = work[ch.seg];
+    if (w.mode != 0) {
+        return;
+    }
+    const int d = w.splitIdx;
+    const double split = 0.5 * (sg.lo[d] + sg.hi[d]);
+    const uint32_t from = sg.from + ch.index * BH_CHUNK;
+    const uint32_t to = min(sg.to, from + BH_CHUNK);
+    uint32_t baseB = sg.from + chunkOffB[blockIdx.x], baseS = sg.from + chunkOffS[blockIdx.x];
+    for (uint32_t k0 = from; k0 < to; k0 += BUILD_THREADS) {
+        const uint32_t k = k0 + threadIdx.x;
+        bool isB = false, isS = false;
+        if (k < to) {
+            const double x = pv.val(idx[k], d);
+            isB = x > split;
+            isS = x < split;
+        }
+        uint32_t totB, totS;
+        const uint32_t rb = blockExclusiveScan(isB ? 1u : 0u, totB, shScan);
+        const uint32_t rs = blockExclusiveScan(isS ? 1u : 0u, totS, shScan);
+        if (isB) {
+            posB[baseB + rb] = k;
+        }
+        if (isS) {
+            posS[baseS + rs] = k;
+        }
+        baseB += totB;
+        baseS += totS;
+    }
+}
+
+// one thread per large segment: the pair count K of the two-pointer partition, the split and the children
+__global__ void segFinishKernel(PosView pv, uint32_t* idx, const uint32_t* __restrict__ posB,
+    const uint32_t* __restrict__ posS, const BhSegment* __restrict__ segIn, const BhChunk* __restrict__ chunks,
+    uint32_t nChunks, BhSegWork* work, BhSegment* segOut, BhNodeGeom* geom, uint32_t* counters,
+    uint32_t nodeCapacity, uint32_t segCapacity, uint32_t* devError) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nChunks || chunks[c].index != 0) {
+        return;
+    }
+    const uint32_t s = chunks[c].seg;
+    const BhSegment sg = segIn[s];
+    BhSegWork w = work[s];
+    const uint32_t from = sg.from, to = sg.to;
+    const int d = w.splitIdx;
+    double splitPosition = 0.5 * (sg.lo[d] + sg.hi[d]);
+    uint32_t n1;
+    bool sliding = false;
+    double cut;
+    if (w.mode == 0) {
+        const uint32_t nB = w.nB, nS = w.nS;
+        // first k with posB[k] >= posS[nS - 1 - k] (the predicate is monotone in k)
+        uint32_t lo = 0, hi = min(nB, nS);
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (posB[from + mid] < posS[from + nS - 1 - mid]) {
+                lo = mid + 1;
+            } else {
+                hi = mid;
+            }
+        }
+        const uint32_t K = lo;
+        w.K = K;
+        n1 = K < nB ? posB[from + K] : to;
+        if (K >= 1) {
+            n1 = min(n1, posS[from + nS - K]);
+        }
+        if (n1 == from || n1 == to) {
+            const bool isMax = (n1 == to);
+            const uint32_t dst = isMax ? to - 1 : from;
+            const uint32_t src = isMax ? w.maxp : w.minp;
+            const uint32_t t = idx[dst];
+            idx[dst] = idx[src];
+            idx[src] = t;
+            splitPosition = isMax ? w.maxv : w.minv;
+            n1 = isMax ? to - 1 : from + 1;
+            sliding = true;
+        }
+        cut = splitPosition;
+    } else {
+        w.K = 0;
+        n1 = (from + to) >> 1;
+        if (w.mode == 1) {
+            NthCtx ctx{ idx, pv, d };
+            nthElement(ctx, long(from), long(n1), long(to));
+        }
+        cut = pv.val(idx[n1], d);
+    }
+    work[s] = w;
+    uint32_t child = atomicAdd(&counters[0], 2u);
+    const uint32_t slot = atomicAdd(&counters[1], 2u);
+    if (child + 2 > nodeCapacity || slot + 2 > segCapacity) {
+        atomicOr(devError, child + 2 > nodeCapacity ? uint32_t(DEV_ERR_NODE_CAPACITY) : uint32_t(DEV_ERR_SEGMENT_CAPACITY));
+        return;
+    }
+    BhNodeGeom& g = geom[sg.node];
+    g.left = int32_t(child);
+    g.right = int32_t(child + 1);
+    g.from = from;
+    g.to = to;
+    const int lvl = g.level;
+    geom[child].parent = sg.node;
+    geom[child].level = lvl + 1;
+    geom[child + 1].parent = sg.node;
+    geom[child + 1].level = lvl + 1;
+    const uint32_t next = sliding ? sg.sliding + 1 : 0;
+    BhSegment l = sg, r = sg;
+    l.to = n1;
+    l.node = int32_t(child);
+    l.sliding = next;
+    l.hi[d] = cut;
+    r.from = n1;
+    r.node = int32_t(child + 1);
+    r.sliding = next;
+    r.lo[d] = cut;
+    segOut[slot] = l;
+    segOut[slot + 1] = r;
+    atomicMax(&counters[4], max(n1 - from, to - n1));
+}
+
+__global__ void chunkSwapKernel(uint32_t* idx, const uint32_t* __restrict__ posB, const uint32_t* __restrict__ posS,
+    const BhSegment* __restrict__ segIn, const BhChunk* __restrict__ chunks, const BhSegWork* __restrict__ work) {
+    const BhChunk ch = chunks[blockIdx.x];
+    const BhSegWork w = work[ch.seg];
+    const uint32_t from = segIn[ch.seg].from;
+    const uint32_t k0 = ch.index * BH_CHUNK;
+    const uint32_t k1 = min(w.K, k0 + BH_CHUNK);
+    for (uint32_t k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+        const uint32_t a = posB[from + k], b = posS[from + w.nS - 1 - k];
+        const uint32_t t = idx[a];
+        idx[a] = idx[b];
+        idx[b] = t;
     }
 }
 
@@ -752,7 +1056,6 @@ __global__ void __launch_bounds__(WALK_THREADS) walkKernel(const dbl4* __restric
         __syncwarp();
         const bool active = uint32_t(lane) < cnt;
         const float* lf = nodef + size_t(leaf) * NODEF;
-        const double lcom[3] = { lg.com[0], lg.com[1], lg.com[2] };
         uint32_t pi = 0;
         dbl4 ri = mkd4(0., 0., 0., 1.);
         if (active) {
@@ -770,11 +1073,11 @@ __global__ void __launch_bounds__(WALK_THREADS) walkKernel(const dbl4* __restric
             const BhNodeGeom& pg = geom[par];
             const int sib = pg.left == ev ? pg.right : pg.left;
             WalkFrame fr;
-            setFrame(fr, geom[ev], lcom, k == depth);
             for (int d = 0; d < 3; ++d) {
                 fr.lh[d] = lf[d];
                 fr.ll[d] = lf[3 + d];
             }
+            setFrame(fr, geom[ev], nodef + size_t(ev) * NODEF, k == depth);
             if (lane == 0) {
                 cur[ncur] = sib;
             }
@@ -955,7 +1258,13 @@ cudaError_t treeAllocate(Tree& t, uint32_t n, uint32_t leafSize) {
     alloc((void**)&t.walk_scratch, size_t(t.walk_warps) * 2 * t.walk_capacity * sizeof(int32_t));
     alloc((void**)&t.stats, 4 * sizeof(unsigned long long));
     alloc((void**)&t.bbox, 8 * sizeof(unsigned long long));
-    alloc((void**)&t.nodef, size_t(t.node_capacity) * 28 * sizeof(float));
+    alloc((void**)&t.nodef, size_t(t.node_capacity) * NODEF * sizeof(float));
+    t.chunk_capacity = 2 * nn / BH_CHUNK + 64;
+    alloc((void**)&t.chunks, size_t(t.chunk_capacity) * sizeof(BhChunk));
+    alloc((void**)&t.chunk_stats, size_t(t.chunk_capacity) * sizeof(BhChunkStats));
+    alloc((void**)&t.chunk_off_b, size_t(t.chunk_capacity) * sizeof(uint32_t));
+    alloc((void**)&t.chunk_off_s, size_t(t.chunk_capacity) * sizeof(uint32_t));
+    alloc((void**)&t.work, size_t(t.seg_capacity) * sizeof(BhSegWork));
     alloc((void**)&t.pf, nn * sizeof(float4));
     alloc((void**)&t.mf, nn * sizeof(float));
     if (e == cudaSuccess) {
@@ -966,7 +1275,8 @@ cudaError_t treeAllocate(Tree& t, uint32_t n, uint32_t leafSize) {
 
 void treeFree(Tree& t) {
     void* ptrs[] = { t.idx, t.scratch_b, t.scratch_s, t.geom, t.mom, t.seg[0], t.seg[1], t.counters, t.leaves,
-        t.walk_scratch, t.stats, t.bbox, t.nodef, t.pf, t.mf };
+        t.walk_scratch, t.stats, t.bbox, t.nodef, t.pf, t.mf, t.chunks, t.chunk_stats, t.chunk_off_b, t.chunk_off_s,
+        t.work };
     for (void* p : ptrs) {
         if (p) {
             cudaFree(p);
@@ -998,18 +1308,52 @@ cudaError_t treeBuild(const DState& s, Tree& t, const Physics& ph, uint32_t* dev
     int cur = 0;
     t.level_start.push_back(0);
     t.level_start.push_back(1);
+    // the largest segment of a level, known on the host (the root at level 0, then bounded by halving)
+    uint32_t maxSeg = n;
     for (int level = 0; nIn > 0; ++level) {
         const int grid = int(min(nIn, 152u * 16u));
-        t.launches++;
+        const bool big = maxSeg > BH_SMALL_SEGMENT;
+        uint32_t nChunks = 0;
+        if (big) {
+            cudaMemsetAsync(t.counters + 3, 0, sizeof(uint32_t), st);
+            chunkListKernel<<<ceilDiv(nIn, 256), 256, 0, st>>>(t.seg[cur], nIn, BH_SMALL_SEGMENT, t.counters,
+                t.chunks, t.work, t.chunk_capacity, devError);
+            t.launches++;
+        }
         splitLevelKernel<<<grid, BUILD_THREADS, 0, st>>>(pv, t.idx, t.scratch_b, t.scratch_s, t.seg[cur], nIn,
-            t.seg[1 - cur], t.geom, t.counters, t.leaves, ph.leaf_size, t.node_capacity, t.seg_capacity, devError);
-        cudaMemcpyAsync(t.counters_host, t.counters, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+            t.seg[1 - cur], t.geom, t.counters, t.leaves, ph.leaf_size, t.node_capacity, t.seg_capacity, devError,
+            BH_SMALL_SEGMENT);
+        t.launches++;
+        if (big) {
+            cudaMemcpyAsync(t.counters_host, t.counters, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+            cudaError_t e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) {
+                return e;
+            }
+            nChunks = min(t.counters_host[3], t.chunk_capacity);
+        }
+        if (nChunks > 0) {
+            chunkStatsKernel<<<nChunks, BUILD_THREADS, 0, st>>>(pv, t.idx, t.seg[cur], t.chunks, t.chunk_stats);
+            segDecideKernel<<<ceilDiv(nChunks, 128), 128, 0, st>>>(t.seg[cur], t.chunks, nChunks, t.chunk_stats,
+                t.chunk_off_b, t.chunk_off_s, t.work);
+            chunkRanksKernel<<<nChunks, BUILD_THREADS, 0, st>>>(pv, t.idx, t.seg[cur], t.chunks, t.chunk_off_b,
+                t.chunk_off_s, t.work, t.scratch_b, t.scratch_s);
+            segFinishKernel<<<ceilDiv(nChunks, 128), 128, 0, st>>>(pv, t.idx, t.scratch_b, t.scratch_s, t.seg[cur],
+                t.chunks, nChunks, t.work, t.seg[1 - cur], t.geom, t.counters, t.node_capacity, t.seg_capacity,
+                devError);
+            chunkSwapKernel<<<nChunks, BUILD_THREADS, 0, st>>>(t.idx, t.scratch_b, t.scratch_s, t.seg[cur], t.chunks,
+                t.work);
+            t.launches += 5;
+        }
+        cudaMemcpyAsync(t.counters_host, t.counters, 5 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
         cudaMemsetAsync(t.counters + 1, 0, sizeof(uint32_t), st);
+        cudaMemsetAsync(t.counters + 4, 0, sizeof(uint32_t), st);
         cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) {
             return e;
         }
         nIn = t.counters_host[1];
+        maxSeg = t.counters_host[4];
         t.node_count = t.counters_host[0];
         t.leaf_count = t.counters_host[2];
         if (nIn > 0) {

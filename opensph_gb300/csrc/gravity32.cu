@@ -43,6 +43,10 @@ __global__ void prepareMixedKernel(const dbl4* __restrict__ r, const double* __r
     }
     o[NODEF_ROPEN] = float(g.r_open);
     o[NODEF_ZERO] = g.r_open == 0. ? 1.f : 0.f;
+    for (int d = 0; d < 3; ++d) {
+        splitF(g.lo[d], o[NODEF_BOX + d], o[NODEF_BOX + 3 + d]);
+        splitF(g.hi[d], o[NODEF_BOX + 6 + d], o[NODEF_BOX + 9 + d]);
+    }
     if (g.left < 0) {
         for (uint32_t k = g.from; k < g.to; ++k) {
             const uint32_t i = idx[k];
@@ -169,7 +173,6 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 6) walkMixedKernel(const uint3
         __syncwarp();
         const bool active = uint32_t(lane) < cnt;
         const float* lf = nodef + size_t(leaf) * NODEF;
-        const double lcom[3] = { lg.com[0], lg.com[1], lg.com[2] };
         const float lhx = lf[0], lhy = lf[1], lhz = lf[2], llx = lf[3], lly = lf[4], llz = lf[5];
         float4 di = make_float4(0.f, 0.f, 0.f, 1.f);
         uint32_t pi = 0;
@@ -188,11 +191,11 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 6) walkMixedKernel(const uint3
             const BhNodeGeom& pg = geom[par];
             const int sib = pg.left == ev ? pg.right : pg.left;
             WalkFrame fr;
-            setFrame(fr, geom[ev], lcom, k == depth);
             for (int d = 0; d < 3; ++d) {
                 fr.lh[d] = lf[d];
                 fr.ll[d] = lf[3 + d];
             }
+            setFrame(fr, geom[ev], nodef + size_t(ev) * NODEF, k == depth);
             if (lane == 0) {
                 cur[ncur] = sib;
             }

@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(128) pairSumMixedKernel(DState s, Grid g, Phys
     const float rhoiInv = 1.f / pi2.w;
     const float alpha = float(ph.av_alpha), beta = float(ph.av_beta);
     Kahan ax, ay, az, du, divv;
-    float gv[6] = { 0, 0, 0, 0, 0, 0 };
+    Kahan gv[6];
     uint32_t cnt = 0;
     const int dxc = gi->dims[0], dyc = gi->dims[1], dzc = gi->dims[2];
     const uint32_t key = g.keys_sorted[si];
@@ -128,12 +128,12 @@ __global__ void __launch_bounds__(128) pairSumMixedKernel(DState s, Grid g, Phys
                                                (__float_as_uint(pi3.w) == __float_as_uint(pj3.w) && pi3.z != 0.f &&
                                                    pj3.z != 0.f);
                         if (undamaged) {
-                            gv[0] += mr * (dvx * gx);
-                            gv[1] += mr * (dvy * gy);
-                            gv[2] += mr * (dvz * gz);
-                            gv[3] += mr * (0.5f * (dvx * gy + dvy * gx));
-                            gv[4] += mr * (0.5f * (dvx * gz + dvz * gx));
-                            gv[5] += mr * (0.5f * (dvy * gz + dvz * gy));
+                            gv[0].add(mr * (dvx * gx));
+                            gv[1].add(mr * (dvy * gy));
+                            gv[2].add(mr * (dvz * gz));
+                            gv[3].add(mr * (0.5f * (dvx * gy + dvy * gx)));
+                            gv[4].add(mr * (0.5f * (dvx * gz + dvz * gx)));
+                            gv[5].add(mr * (0.5f * (dvy * gz + dvz * gy)));
                             float tt[5];
                             for (int k = 0; k < 5; ++k) {
                                 tt[k] = Sif[k] + g.mxS[k * n + t];
@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(128) pairSumMixedKernel(DState s, Grid g, Phys
     double Si[5] = { 0, 0, 0, 0, 0 };
     double gvd[6];
     for (int c = 0; c < 6; ++c) {
-        gvd[c] = gv[c];
+        gvd[c] = gv[c].value();
     }
     if (Solid) {
         for (int c = 0; c < 5; ++c) {

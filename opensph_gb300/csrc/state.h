@@ -130,6 +130,34 @@ struct BhSegment {
     double lo[3], hi[3];
 };
 
+// multi-CTA split of large k-d tree segments
+constexpr uint32_t BH_CHUNK = 4096;          // elements per chunk
+constexpr uint32_t BH_SMALL_SEGMENT = 16384; // segments up to this size are split by one CTA
+
+struct BhChunk {
+    uint32_t seg;    // segment index in the level's list
+    uint32_t index;  // chunk index within the segment
+    uint32_t first;  // slot of the segment's first chunk
+    uint32_t count;  // chunks of the segment
+};
+
+struct BhChunkStats {
+    uint32_t nb[3], ns[3];  // elements above / below the box centre, per dimension
+    uint32_t diff[3];       // any element differs from the segment's last one, per dimension
+    uint32_t pad;
+    double minv[3], maxv[3];
+    uint32_t minp[3], maxp[3]; // first positions of the extremes
+};
+
+struct BhSegWork {
+    int32_t splitIdx;
+    int32_t mode;      // 0 two-pointer partition, 1 nth_element, 2 degenerate box
+    uint32_t nB, nS, K;
+    uint32_t minp, maxp;
+    uint32_t pad;
+    double minv, maxv;
+};
+
 struct Tree {
     uint32_t node_capacity = 0;
     uint32_t seg_capacity = 0;
@@ -150,6 +178,12 @@ struct Tree {
     float* nodef = nullptr;           // mixed walk: FP32 evaluation record per node (28 floats)
     float4* pf = nullptr;             // mixed walk: particle position relative to its leaf's centre of mass, h
     float* mf = nullptr;              // mixed walk: G * m in tree order
+    uint32_t chunk_capacity = 0;
+    BhChunk* chunks = nullptr;
+    BhChunkStats* chunk_stats = nullptr;
+    uint32_t* chunk_off_b = nullptr;
+    uint32_t* chunk_off_s = nullptr;
+    BhSegWork* work = nullptr;
     std::vector<uint32_t> level_start; // host: first node id of each level
     uint32_t node_count = 0;
     uint32_t leaf_count = 0;

@@ -145,10 +145,12 @@ __device__ int intersectsBox(const double p[3], double rad, const double lo[3], 
 
 enum : int { CL_KEEP = 0, CL_PARTICLES = 1, CL_NODE = 2, CL_OPEN = 3 };
 
-// per-node FP32 record shared by both walks: com hi[3], com lo[3], m0, q2[6], q3[10], r_open, r_open == 0
-constexpr int NODEF = 28;
+// per-node FP32 record shared by both walks: com hi[3], com lo[3], m0, q2[6], q3[10], r_open, r_open == 0,
+// box lower corner hi[3] + lo[3], box upper corner hi[3] + lo[3] (40 floats)
+constexpr int NODEF = 40;
 constexpr int NODEF_ROPEN = 23;
 constexpr int NODEF_ZERO = 24;
+constexpr int NODEF_BOX = 25;
 
 // Sphere::intersectsBox evaluated in FP32 on coordinates relative to the walking leaf's centre of mass,
 // with a guard band: returns the reference's answer (0 outside, 1 intersection, 2 inside) whenever the FP32
@@ -219,12 +221,16 @@ __device__ __forceinline__ int classifyEntry(int node, const BhNodeGeom* __restr
     return res == 0 ? CL_NODE : CL_KEEP;
 }
 
-__device__ __forceinline__ void setFrame(WalkFrame& f, const BhNodeGeom& ev, const double lcom[3], bool evLeaf) {
+// The evaluated node's box relative to the leaf centre, formed from hi + lo float pairs (no FP64 arithmetic);
+// the FP64 box is loaded for the rare undecided classifications.
+__device__ __forceinline__ void setFrame(WalkFrame& f, const BhNodeGeom& ev, const float* __restrict__ evf,
+    bool evLeaf) {
+    const float* b = evf + NODEF_BOX;
     for (int d = 0; d < 3; ++d) {
         f.elo[d] = ev.lo[d];
         f.ehi[d] = ev.hi[d];
-        f.elof[d] = float(ev.lo[d] - lcom[d]);
-        f.ehif[d] = float(ev.hi[d] - lcom[d]);
+        f.elof[d] = (b[d] - f.lh[d]) + (b[3 + d] - f.ll[d]);
+        f.ehif[d] = (b[6 + d] - f.lh[d]) + (b[9 + d] - f.ll[d]);
     }
     f.evLeaf = evLeaf;
 }

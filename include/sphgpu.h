@@ -184,6 +184,19 @@ sphgpu_status sphgpu_totals(sphgpu_handle* h, double out[9]);
 /* Device NaN/Inf scan of the integrated state; SPHGPU_ERR_NONFINITE with the first bad particle index. */
 sphgpu_status sphgpu_check_finite(sphgpu_handle* h, uint64_t* first_bad);
 
+/* Conserved totals without any allocation (no counterpart in the reference). For callers that cannot call
+ * cudaMalloc: an application that owns the device memory budget and passes only its own buffers, or a
+ * per-step hook that must not risk the implicit synchronisation of an allocation. r, v (4 doubles per
+ * particle), m, u (1 double per particle) and totals (9 doubles, layout of sphgpu_totals) are DEVICE
+ * pointers of the current device; the work is queued on `stream` (a cudaStream_t, NULL for the default
+ * stream) and the call returns without synchronising. The scratch is a fixed 72 KiB array inside the
+ * library, shared by all calls: calls whose kernels overlap on the GPU race, so serialise them. The first
+ * call on a device looks up that array's device address (make it before any stream capture).
+ * n above SPHGPU_TOTALS_NOALLOC_MAX_PARTICLES returns SPHGPU_ERR_CAPACITY (use sphgpu_totals). */
+#define SPHGPU_TOTALS_NOALLOC_MAX_PARTICLES 4194304u
+sphgpu_status sphgpu_totals_noalloc(const double* r, const double* v, const double* m, const double* u, uint64_t n,
+    double* totals, void* stream);
+
 /* Phases of a step, timed with CUDA events when profiling is on; the GPU counterparts of the reference's
  * StatisticsId::GRAVITY_BUILD_TIME, GRAVITY_EVAL_TIME and SPH_EVAL_TIME (core/system/Statistics.h:108-160,
  * set at core/sph/solvers/GravitySolver.cpp:71-90). */

@@ -29,6 +29,7 @@ UNITS = {
     "gravity.cu": ["-fmad=false"],
     "sph32.cu": [],
     "gravity32.cu": [],
+    "noalloc.cu": [],
 }
 
 

@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--error-steps", type=int, default=100,
                     help="steps after which the mixed path is compared with the FP64 GPU path")
     ap.add_argument("--profile-only", action="store_true", help="warm-up + timed steps only (for ncu)")
+    ap.add_argument("--no-nbody", action="store_true", help="skip the gravity-only Plummer measurement")
+    ap.add_argument("--nbody-n", type=int, default=4_194_304)
     return ap.parse_args()
 
 
@@ -225,6 +227,8 @@ def run_gpu(args, rank, world):
                                                  "d2h_bytes_per_step": (32 + 32 + 8 + 8) * n}}
     if rank == 0 and not args.no_fp64:
         result["fp64"] = compare_fp64(args, st, mats, n, cfg, dev)
+    if rank == 0 and not args.no_nbody:
+        result["nbody"] = nbody(args, dev)
     return result
 
 
@@ -271,6 +275,56 @@ def compare_fp64(args, st, mats, n, mixed_cfg, dev):
     out["rel_err_velocity"] = rel(vmix, vref)
     out["rel_err_energy"] = rel(mix["u"], ref["u"])
     out["max_abs_err_damage"] = float(np.max(np.abs(mix["D"] - ref["D"])))
+    return out
+
+
+# FP32 operations of one particle-multipole evaluation (evalMultipoleF, csrc/gravity32.cu: octupole) and the
+# N-body convention for one softened particle-particle interaction
+FLOP_PN = 120
+FLOP_PP = 20
+FP32_PEAK_NOMINAL = 152 * 128 * 2 * 2.07e9 / 1e12  # TFLOP/s at the maximum SM clock
+
+
+def nbody(args, dev):
+    """Gravity-only workload: Plummer sphere (scale radius 1, M = 1, G = 1, softening 1e-3 as h), Barnes-Hut
+    theta = 0.5 octupole; tree build + walk timed for the mixed (FP32 evaluation) and the FP64 walk."""
+    import torch
+
+    from opensph_gb300 import abi, initial
+    from opensph_gb300.solver import GpuSolver
+
+    n = args.nbody_n
+    r, m = initial.plummer(n, seed=7, softening=1e-3)
+    r = r.ravel()
+    out = {"particles": n, "theta": 0.5, "workload": "Plummer sphere, G = 1, softening 1e-3, octupole"}
+    accs = {}
+    for name, prec in (("mixed", abi.PRECISION_MIXED), ("fp64", abi.PRECISION_FP64)):
+        cfg, keep = abi.make_config(n, [abi.ideal_gas()], forces=abi.FORCE_PRESSURE | abi.FORCE_SELF_GRAVITY,
+                                    gravity_constant=1.0, gravity_opening_angle=0.5, precision=prec)
+        cfg.device = dev
+        with GpuSolver(cfg, keep) as g:
+            g.set_quantity(abi.Q_POSITION, 0, r)
+            g.set_quantity(abi.Q_MASS, 0, m)
+            g.gravity()
+            g.set_profiling(True)
+            g.phase_times()
+            reps = 3 if name == "mixed" else 1
+            for _ in range(reps):
+                accs[name] = g.gravity()
+            phases, _ = g.phase_times()
+            inter = g.gravity_interactions()
+        walk_ms = phases["gravity_eval"] / reps
+        build_ms = phases["gravity_build"] / reps
+        total = inter[0] + inter[1]
+        flops = inter[0] * FLOP_PN + inter[1] * FLOP_PP
+        out[name] = {"walk_ms": walk_ms, "build_ms": build_ms, "interactions": total,
+                     "particle_node": inter[0], "particle_particle": inter[1],
+                     "interactions_per_s": total / (walk_ms * 1e-3), "walk_tflops": flops / (walk_ms * 1e-3) / 1e12}
+    out["mixed"]["fp32_frac_of_nominal_peak"] = out["mixed"]["walk_tflops"] / FP32_PEAK_NOMINAL
+    out["walk_speedup_mixed_vs_fp64"] = out["fp64"]["walk_ms"] / out["mixed"]["walk_ms"]
+    a, b = accs["mixed"].reshape(-1, 4)[:, :3], accs["fp64"].reshape(-1, 4)[:, :3]
+    out["mixed_vs_fp64_rel_err"] = float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+    torch.cuda.synchronize()
     return out
 
 
@@ -335,6 +389,8 @@ def main():
     }
     if "fp64" in res:
         line["fp64"] = res["fp64"]
+    if "nbody" in res:
+        line["nbody_plummer"] = res["nbody"]
     if not args.no_cpu:
         st, mats, n2 = workload(args)
         value, secs = cpu_sample(args, st, mats, n2, args.cpu_steps)

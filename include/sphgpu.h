@@ -156,13 +156,18 @@ sphgpu_status sphgpu_get_pairs(sphgpu_handle* h, uint32_t* pair_i, uint32_t* pai
 
 /* IGravity::build + evalSelfGravity (core/gravity/IGravity.h:16-62, core/gravity/BarnesHut.cpp:50-99):
  * builds the k-d tree and multipole moments, then adds the self-gravity acceleration of every particle to
- * dv (host array of 4*count doubles, may be NULL to only update the internal acceleration buffer). */
+ * dv (host array of 4*count doubles, may be NULL to only update the internal acceleration buffer). The walk
+ * runs in the handle's precision (FP64, or FP32 evaluation with FP64 decisions for SPHGPU_PRECISION_MIXED). */
 sphgpu_status sphgpu_gravity_build(sphgpu_handle* h);
 sphgpu_status sphgpu_gravity_eval(sphgpu_handle* h, double* dv, uint64_t count);
 /* IGravity::evalAcceleration (core/gravity/BarnesHut.cpp:118-160) at npoints host points (4 doubles each). */
 sphgpu_status sphgpu_gravity_eval_points(sphgpu_handle* h, const double* points, uint64_t npoints, double* acc);
 /* StatisticsId::GRAVITY_NODES_APPROX / GRAVITY_NODES_EXACT / GRAVITY_NODE_COUNT of the last evaluation. */
 sphgpu_status sphgpu_gravity_stats(sphgpu_handle* h, uint64_t out[3]);
+/* Interactions evaluated by the last walk: out[0] particle-multipole evaluations (sum over leaves of
+ * particles x node-list length), out[1] particle-particle kernel evaluations (particle lists and pairs
+ * inside each leaf). */
+sphgpu_status sphgpu_gravity_interactions(sphgpu_handle* h, uint64_t out[2]);
 
 /* ISolver::integrate (core/sph/solvers/SymmetricSolver.cpp:58-95 wrapped by GravitySolver::loop,
  * core/sph/solvers/GravitySolver.cpp:64-91): materials initialize, gravity, pair loop, finalize. The

@@ -752,9 +752,13 @@ sphgpu_status sphgpu_gravity_build(sphgpu_handle* h) {
     if (!h->ph.gravity) {
         return fail(h, SPHGPU_ERR_STATE, "self-gravity is not enabled in the configuration");
     }
-    cudaError_t e = treeBuild(h->s, h->tree, h->ph, h->d_err, h->stream);
-    if (e != cudaSuccess) {
-        return cudaFail(h, e, "gravity build");
+    {
+        Phase ph(h, SPHGPU_PHASE_GRAVITY_BUILD);
+        cudaError_t e = treeBuild(h->s, h->tree, h->ph, h->d_err, h->stream);
+        if (e != cudaSuccess) {
+            return cudaFail(h, e, "gravity build");
+        }
+        h->launches += h->tree.launches;
     }
     return checkDeviceError(h);
 }
@@ -770,7 +774,15 @@ sphgpu_status sphgpu_gravity_eval(sphgpu_handle* h, double* dv, uint64_t count) 
         return fail(h, SPHGPU_ERR_ARGUMENT, "dv holds %llu particles, state has %u", (unsigned long long)count,
             h->s.n);
     }
-    launchGravityWalk(h->s, h->tree, h->ph, h->d_lut_grav, h->d_err, h->stream);
+    {
+        Phase ph(h, SPHGPU_PHASE_GRAVITY_EVAL);
+        if (h->ph.precision == SPHGPU_PRECISION_MIXED) {
+            launchGravityWalkMixed(h->s, h->tree, h->ph, h->d_lut_grav_f, h->d_err, h->stream);
+        } else {
+            launchGravityWalk(h->s, h->tree, h->ph, h->d_lut_grav, h->d_err, h->stream);
+        }
+        h->launches += 2;
+    }
     CUDA_TRY(h, cudaGetLastError());
     const sphgpu_status st = checkDeviceError(h);
     if (st != SPHGPU_OK) {
@@ -837,6 +849,21 @@ sphgpu_status sphgpu_gravity_stats(sphgpu_handle* h, uint64_t out[3]) {
     out[0] = h->h_pinned[0];
     out[1] = h->h_pinned[1];
     out[2] = h->tree.node_count;
+    return SPHGPU_OK;
+}
+
+sphgpu_status sphgpu_gravity_interactions(sphgpu_handle* h, uint64_t out[2]) {
+    if (!h || !out) {
+        return SPHGPU_ERR_ARGUMENT;
+    }
+    if (!h->ph.gravity) {
+        return fail(h, SPHGPU_ERR_STATE, "self-gravity is not enabled");
+    }
+    CUDA_TRY(h, cudaMemcpyAsync(h->h_pinned, h->tree.stats + 2, 2 * sizeof(unsigned long long),
+        cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    out[0] = h->h_pinned[0];
+    out[1] = h->h_pinned[1];
     return SPHGPU_OK;
 }
 

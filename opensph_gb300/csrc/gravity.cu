@@ -1028,7 +1028,7 @@ __global__ void __launch_bounds__(WALK_THREADS) walkKernel(const dbl4* __restric
     int32_t* listA = scratch + size_t(warpGlobal) * 2 * listCap;
     int32_t* listB = listA + listCap;
     int32_t* path = pathSh[wib];
-    unsigned long long nApprox = 0, nExact = 0;
+    unsigned long long nApprox = 0, nExact = 0, nPn = 0, nPp = 0;
 
     for (uint32_t li = warpGlobal; li < nLeaves; li += nWarps) {
         const int leaf = int(leaves[li]);
@@ -1122,6 +1122,7 @@ __global__ void __launch_bounds__(WALK_THREADS) walkKernel(const dbl4* __restric
                     const int pn = __shfl_sync(0xffffffffu, node, src);
                     const uint32_t f0 = geom[pn].from, f1 = geom[pn].to;
                     nExact += 1;
+                    nPp += uint64_t(cnt) * (f1 - f0);
                     for (uint32_t t = f0; t < f1; ++t) {
                         const uint32_t j = idx[t];
                         const dbl4 rj = r[j];
@@ -1143,6 +1144,7 @@ __global__ void __launch_bounds__(WALK_THREADS) walkKernel(const dbl4* __restric
                     mn &= mn - 1;
                     const int nn = __shfl_sync(0xffffffffu, node, src);
                     nApprox += 1;
+                    nPn += cnt;
                     if (active) {
                         const BhNodeGeom& ng = geom[nn];
                         evalMultipole(ri.x - ng.com[0], ri.y - ng.com[1], ri.z - ng.com[2], mom[nn], order, ax, ay, az);
@@ -1163,6 +1165,7 @@ __global__ void __launch_bounds__(WALK_THREADS) walkKernel(const dbl4* __restric
             continue;
         }
         // intra-leaf pairs
+        nPp += uint64_t(cnt) * (cnt - 1);
         for (uint32_t t = lg.from; t < lg.to; ++t) {
             const uint32_t j = idx[t];
             const dbl4 rj = r[j];
@@ -1182,6 +1185,8 @@ __global__ void __launch_bounds__(WALK_THREADS) walkKernel(const dbl4* __restric
     if (lane == 0) {
         atomicAdd(&stats[0], nApprox);
         atomicAdd(&stats[1], nExact);
+        atomicAdd(&stats[2], nPn);
+        atomicAdd(&stats[3], nPp);
     }
 }
 
@@ -1380,7 +1385,7 @@ cudaError_t treeBuild(const DState& s, Tree& t, const Physics& ph, uint32_t* dev
 
 void launchGravityWalk(const DState& s, Tree& t, const Physics& ph, const double* lut, uint32_t* devError,
     cudaStream_t st) {
-    cudaMemsetAsync(t.stats, 0, 2 * sizeof(unsigned long long), st);
+    cudaMemsetAsync(t.stats, 0, 4 * sizeof(unsigned long long), st);
     if (s.n == 0) {
         return;
     }

@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 6) walkMixedKernel(const uint3
     int32_t* listA = scratch + size_t(warpGlobal) * 2 * listCap;
     int32_t* listB = listA + listCap;
     int32_t* path = pathSh[wib];
-    unsigned long long nApprox = 0, nExact = 0;
+    unsigned long long nApprox = 0, nExact = 0, nPn = 0, nPp = 0;
 
     for (uint32_t li = warpGlobal; li < nLeaves; li += nWarps) {
         const int leaf = int(leaves[li]);
@@ -243,6 +243,7 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 6) walkMixedKernel(const uint3
                     const float Dz = (pfn[2] - lhz) + (pfn[5] - llz);
                     const uint32_t f0 = geom[pn].from, f1 = geom[pn].to;
                     nExact += 1;
+                    nPp += uint64_t(cnt) * (f1 - f0);
                     float sx = 0.f, sy = 0.f, sz = 0.f;
                     for (uint32_t t = f0; t < f1; ++t) {
                         const float4 dj = pf[t];
@@ -270,6 +271,7 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 6) walkMixedKernel(const uint3
                     const float Dy = (o[1] - lhy) + (o[4] - lly);
                     const float Dz = (o[2] - lhz) + (o[5] - llz);
                     nApprox += 1;
+                    nPn += cnt;
                     float sx = 0.f, sy = 0.f, sz = 0.f;
                     evalMultipoleF(di.x - Dx, di.y - Dy, di.z - Dz, o, order, sx, sy, sz);
                     if (active) {
@@ -291,6 +293,7 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 6) walkMixedKernel(const uint3
             }
             continue;
         }
+        nPp += uint64_t(cnt) * (cnt - 1);
         float sx = 0.f, sy = 0.f, sz = 0.f;
         for (uint32_t t = lg.from; t < lg.to; ++t) {
             const float4 dj = pf[t];
@@ -313,6 +316,8 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 6) walkMixedKernel(const uint3
     if (lane == 0) {
         atomicAdd(&stats[0], nApprox);
         atomicAdd(&stats[1], nExact);
+        atomicAdd(&stats[2], nPn);
+        atomicAdd(&stats[3], nPp);
     }
 }
 
@@ -328,7 +333,7 @@ void launchPrepareWalk(const DState& s, Tree& t, const Physics& ph, cudaStream_t
 
 void launchGravityWalkMixed(const DState& s, Tree& t, const Physics& ph, const float* lutF, uint32_t* devError,
     cudaStream_t st) {
-    cudaMemsetAsync(t.stats, 0, 2 * sizeof(unsigned long long), st);
+    cudaMemsetAsync(t.stats, 0, 4 * sizeof(unsigned long long), st);
     if (s.n == 0 || t.node_count == 0) {
         return;
     }

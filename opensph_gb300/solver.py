@@ -51,6 +51,7 @@ def library():
     lib.sphgpu_gravity_eval.argtypes = [h, _F8P, ctypes.c_uint64]
     lib.sphgpu_gravity_eval_points.argtypes = [h, _F8P, ctypes.c_uint64, _F8P]
     lib.sphgpu_gravity_stats.argtypes = [h, ctypes.POINTER(ctypes.c_uint64)]
+    lib.sphgpu_gravity_interactions.argtypes = [h, ctypes.POINTER(ctypes.c_uint64)]
     lib.sphgpu_integrate.argtypes = [h]
     lib.sphgpu_step.argtypes = [h, ctypes.c_uint32]
     lib.sphgpu_get_timestep.argtypes = [h, _F8P]
@@ -204,6 +205,11 @@ class GpuSolver:
     def gravity_stats(self):
         out = (ctypes.c_uint64 * 3)()
         self._check(self._lib.sphgpu_gravity_stats(self._h, out))
+        return list(out)
+
+    def gravity_interactions(self):
+        out = (ctypes.c_uint64 * 2)()
+        self._check(self._lib.sphgpu_gravity_interactions(self._h, out))
         return list(out)
 
     def totals(self):

@@ -1563,3 +1563,163 @@ int ora_totals(const ora_state* s, double out[9]) {
 }
 
 } // extern "C"
+
+// ---------------------------------------------------------------------------------------------------------
+// Frozen-list model of the adjoint workload, in forward-mode dual numbers (tangent-linear reference)
+// ---------------------------------------------------------------------------------------------------------
+
+namespace {
+
+struct Dual {
+    double v = 0., d = 0.;
+    Dual() = default;
+    Dual(double a, double b = 0.) : v(a), d(b) {}
+};
+inline Dual operator+(Dual a, Dual b) { return Dual(a.v + b.v, a.d + b.d); }
+inline Dual operator-(Dual a, Dual b) { return Dual(a.v - b.v, a.d - b.d); }
+inline Dual operator-(Dual a) { return Dual(-a.v, -a.d); }
+inline Dual operator*(Dual a, Dual b) { return Dual(a.v * b.v, a.d * b.v + a.v * b.d); }
+inline Dual operator/(Dual a, Dual b) { return Dual(a.v / b.v, (a.d * b.v - a.v * b.d) / (b.v * b.v)); }
+inline Dual sqrtD(Dual a) {
+    const double s = std::sqrt(a.v);
+    return Dual(s, a.d / (2. * s));
+}
+
+// LutKernel<3> gradient table as a piecewise-linear function of q^2, with its derivative
+inline Dual lutGradD(Dual q2) {
+    const Lut& lut = sphLut();
+    if (q2.v >= 4.) {
+        return Dual(0., 0.);
+    }
+    const double f = lut.qSqrToIdx * q2.v;
+    const int i1 = int(f);
+    const double ratio = f - double(i1);
+    const double g0 = lut.grads[i1], g1 = lut.grads[i1 + 1];
+    return Dual(g0 * (1. - ratio) + g1 * ratio, (g1 - g0) * lut.qSqrToIdx * q2.d);
+}
+
+struct FrozenModel {
+    const ora_frozen_params& p;
+    uint64_t n;
+    const double* m;
+    std::vector<Dual> r, v, rho, u; // r, v: 3 per particle
+    std::vector<double> h;
+    Dual alpha;
+    Neighbours nb;
+
+    void rebuild() {
+        std::vector<double> pos(4 * n);
+        for (uint64_t i = 0; i < n; ++i) {
+            for (int k = 0; k < 3; ++k) {
+                pos[4 * i + k] = r[3 * i + k].v;
+            }
+            pos[4 * i + 3] = h[i];
+        }
+        nb = findNeighbours(n, pos.data());
+    }
+
+    void step() {
+        const double dt = p.dt, gamma = p.gamma, beta = p.beta;
+        std::vector<Dual> rp(3 * n), pr(n), cs(n);
+        for (uint64_t i = 0; i < n; ++i) {
+            for (int k = 0; k < 3; ++k) {
+                rp[3 * i + k] = r[3 * i + k] + v[3 * i + k] * Dual(0.5 * dt);
+            }
+            pr[i] = Dual(gamma - 1.) * u[i] * rho[i];
+            cs[i] = sqrtD(Dual(gamma) * pr[i] / rho[i]);
+        }
+        std::vector<Dual> nv(3 * n), nr(3 * n), nrho(n), nu(n);
+        parallelFor(n, [&](uint64_t a, uint64_t b) {
+            for (uint64_t i = a; i < b; ++i) {
+                Dual ax, ay, az, divv, heat;
+                const Dual Pi_ = pr[i] / (rho[i] * rho[i]);
+                for (uint64_t kk = nb.start[i]; kk < nb.start[i + 1]; ++kk) {
+                    const uint32_t j = nb.idx[kk];
+                    const double hbar = 0.5 * (h[i] + h[j]);
+                    const Dual dx = rp[3 * i] - rp[3 * j], dy = rp[3 * i + 1] - rp[3 * j + 1],
+                               dz = rp[3 * i + 2] - rp[3 * j + 2];
+                    const Dual s = dx * dx + dy * dy + dz * dz;
+                    const double hInv = 1. / hbar;
+                    const double h5 = hInv * hInv * hInv * hInv * hInv;
+                    const Dual F = Dual(h5) * lutGradD(s * Dual(hInv * hInv));
+                    const Dual gx = dx * F, gy = dy * F, gz = dz * F;
+                    const double mj = m[j];
+                    const Dual vjx = v[3 * j] - v[3 * i], vjy = v[3 * j + 1] - v[3 * i + 1],
+                               vjz = v[3 * j + 2] - v[3 * i + 2];
+                    divv = divv + Dual(mj) / rho[i] * (vjx * gx + vjy * gy + vjz * gz);
+                    const Dual Pj = pr[j] / (rho[j] * rho[j]);
+                    Dual coef = -(Pi_ + Pj);
+                    const Dual wd = -(vjx * dx + vjy * dy + vjz * dz);
+                    if (wd.v < 0.) {
+                        const Dual D = s + Dual(1.e-2 * hbar * hbar);
+                        const Dual mu = Dual(hbar) * wd / D;
+                        const Dual rb = Dual(0.5) * (rho[i] + rho[j]);
+                        const Dual cb = Dual(0.5) * (cs[i] + cs[j]);
+                        const Dual Pi = (-alpha * cb * mu + Dual(beta) * mu * mu) / rb;
+                        coef = coef - Pi;
+                        heat = heat + Dual(mj) * Dual(0.5) * Pi * -(vjx * gx + vjy * gy + vjz * gz);
+                    }
+                    ax = ax + Dual(mj) * coef * gx;
+                    ay = ay + Dual(mj) * coef * gy;
+                    az = az + Dual(mj) * coef * gz;
+                }
+                const Dual drho = -rho[i] * divv;
+                const Dual du = heat - pr[i] / rho[i] * divv;
+                nrho[i] = rho[i] + drho * Dual(dt);
+                nu[i] = u[i] + du * Dual(dt);
+                const Dual acc[3] = { ax, ay, az };
+                for (int k = 0; k < 3; ++k) {
+                    nv[3 * i + k] = v[3 * i + k] + acc[k] * Dual(dt);
+                    nr[3 * i + k] = rp[3 * i + k] + nv[3 * i + k] * Dual(0.5 * dt);
+                }
+            }
+        });
+        r.swap(nr);
+        v.swap(nv);
+        rho.swap(nrho);
+        u.swap(nu);
+    }
+};
+
+} // namespace
+
+extern "C" int ora_frozen_loss(const ora_frozen_params* prm, uint64_t n, const double* r, const double* v,
+    const double* m, const double* rho, const double* u, const double* tr, const double* tv, const double* trho,
+    const double* tu, double talpha, double* loss, double* dloss) {
+    if (!prm || !r || !v || !m || !rho || !u || !loss || prm->rebuild_every == 0) {
+        return SPHGPU_ERR_ARGUMENT;
+    }
+    FrozenModel fm{ *prm, n, m };
+    fm.r.resize(3 * n);
+    fm.v.resize(3 * n);
+    fm.rho.resize(n);
+    fm.u.resize(n);
+    fm.h.resize(n);
+    for (uint64_t i = 0; i < n; ++i) {
+        for (int k = 0; k < 3; ++k) {
+            fm.r[3 * i + k] = Dual(r[4 * i + k], tr ? tr[4 * i + k] : 0.);
+            fm.v[3 * i + k] = Dual(v[4 * i + k], tv ? tv[4 * i + k] : 0.);
+        }
+        fm.h[i] = r[4 * i + 3];
+        fm.rho[i] = Dual(rho[i], trho ? trho[i] : 0.);
+        fm.u[i] = Dual(u[i], tu ? tu[i] : 0.);
+    }
+    fm.alpha = Dual(prm->alpha, talpha);
+    for (uint32_t s = 0; s < prm->steps; ++s) {
+        if (s % prm->rebuild_every == 0) {
+            fm.rebuild();
+        }
+        fm.step();
+    }
+    Dual L;
+    for (uint64_t i = 0; i < std::min<uint64_t>(prm->n_target, n); ++i) {
+        for (int k = 0; k < 3; ++k) {
+            L = L + fm.v[3 * i + k] * fm.v[3 * i + k];
+        }
+    }
+    *loss = L.v;
+    if (dloss) {
+        *dloss = L.d;
+    }
+    return SPHGPU_OK;
+}

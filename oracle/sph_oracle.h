@@ -78,6 +78,26 @@ int ora_run(const sphgpu_config* cfg, ora_state* s, uint32_t nsteps, double* dt,
 /* Conserved totals, same layout as sphgpu_totals. */
 int ora_totals(const ora_state* s, double out[9]);
 
+/* Frozen-list hydrodynamic model of the adjoint workload: ideal gas, ContinuityEquation + PressureForce +
+ * StandardAV, leap-frog with a fixed time step, constant h, neighbour lists rebuilt every rebuild_every
+ * steps and held fixed in between. Loss = sum over particles [0, n_target) of |v|^2 after `steps` steps.
+ * With tangent inputs (any may be NULL = zero) it also returns the directional derivative of the loss
+ * (forward-mode, dual numbers): the FP64 tangent-linear reference of the GPU adjoint. */
+typedef struct {
+    uint32_t steps;
+    uint32_t rebuild_every;
+    uint32_t n_target;
+    uint32_t reserved;
+    double dt;
+    double gamma;
+    double alpha;
+    double beta;
+} ora_frozen_params;
+
+int ora_frozen_loss(const ora_frozen_params* prm, uint64_t n, const double* r, const double* v, const double* m,
+    const double* rho, const double* u, const double* tr, const double* tv, const double* trho, const double* tu,
+    double talpha, double* loss, double* dloss);
+
 #ifdef __cplusplus
 }
 #endif

@@ -309,3 +309,34 @@ def test_barnes_hut_sliding_midpoint_nth_element():
     r[:, 0] = xs
     r[:, 3] = 1e-30
     _bh_compare(r.ravel(), np.ones(n), tol=1e-12)
+
+
+# ---- gravity-only N-body (Plummer sphere, G = 1, softening 1e-3 as h): FP32 walk with FP64 moments and
+# ---- decisions against FP64 direct summation on a seeded subset of targets (BarnesHut vs BruteForceGravity)
+
+@pytest.mark.parametrize("theta", [0.3, 0.5, 0.7])
+def test_plummer_walks_against_direct_sum(theta):
+    from opensph_gb300 import initial
+
+    n = 131072
+    r, m = initial.plummer(n, seed=21, softening=1e-3)
+    r = r.ravel()
+    targets = np.random.default_rng(4).choice(n, 4096, replace=False).astype("u4")
+    direct = cases.vec3(oracle.gravity_direct(r, m, G=1.0, targets=targets))
+    out = {}
+    for prec in (abi.PRECISION_FP64, abi.PRECISION_MIXED):
+        cfg, keep = abi.make_config(n, [abi.ideal_gas()], forces=abi.FORCE_PRESSURE | abi.FORCE_SELF_GRAVITY,
+                                    gravity_constant=1.0, gravity_opening_angle=theta, precision=prec)
+        with GpuSolver(cfg, keep) as g:
+            g.set_quantity(abi.Q_POSITION, 0, r)
+            g.set_quantity(abi.Q_MASS, 0, m)
+            out[prec] = cases.vec3(g.gravity())
+    fp64, mixed = out[abi.PRECISION_FP64], out[abi.PRECISION_MIXED]
+    # mixed vs FP64 walk: the same interaction lists, FP32 evaluation
+    assert cases.scale_err(mixed, fp64) < 2e-6
+    # both vs direct summation: the Barnes-Hut approximation error of the opening angle
+    bound = {0.3: 1e-4, 0.5: 1e-3, 0.7: 5e-3}[theta]
+    for a in (fp64, mixed):
+        rel = np.linalg.norm(a[targets] - direct, axis=1) / np.linalg.norm(direct, axis=1)
+        assert np.median(rel) < bound / 5
+        assert np.percentile(rel, 99) < bound

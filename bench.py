@@ -48,6 +48,9 @@ def parse():
     ap.add_argument("--profile-only", action="store_true", help="warm-up + timed steps only (for ncu)")
     ap.add_argument("--no-nbody", action="store_true", help="skip the gravity-only Plummer measurement")
     ap.add_argument("--nbody-n", type=int, default=4_194_304)
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurement")
+    ap.add_argument("--adjoint-target", type=int, default=100_000)
+    ap.add_argument("--adjoint-impactor", type=int, default=2_000)
     return ap.parse_args()
 
 
@@ -229,6 +232,8 @@ def run_gpu(args, rank, world):
         result["fp64"] = compare_fp64(args, st, mats, n, cfg, dev)
     if rank == 0 and not args.no_nbody:
         result["nbody"] = nbody(args, dev)
+    if rank == 0 and not args.no_adjoint:
+        result["adjoint"] = adjoint(args, dev)
     return result
 
 
@@ -328,6 +333,88 @@ def nbody(args, dev):
     return out
 
 
+ADJ_STEPS = 50
+ADJ_DT = 1.0e-3
+ADJ_REBUILD = 10
+ADJ_CHECKPOINT = 10
+
+
+def adjoint(args, dev):
+    """Adjoint workload: ideal-gas sphere (rho 1, p 1) + impactor at Mach 3, 50 leap-frog steps of continuity +
+    pressure + standard AV over lists rebuilt every 10 steps, checkpoints every 10 steps, loss = sum |v_target|^2.
+    Times sphgpu_adjoint_forward and sphgpu_adjoint_backward (host wall clock around each call, which ends with
+    the results on the host) in FP64 and mixed precision, and checks each gradient against FP64 central finite
+    differences (the FP64 forward, eps 1e-6) in 8 seeded smooth directions of all positions, the impactor
+    velocity and the AV alpha."""
+    from opensph_gb300 import abi, initial
+    from opensph_gb300.solver import GpuSolver
+
+    st, nt = initial.gas_impact(args.adjoint_target, args.adjoint_impactor)
+    n = len(st["m"])
+    pos = st["r"].reshape(-1, 4)[:, :3]
+
+    def solver(state):
+        cfg, keep = abi.make_config(n, [abi.ideal_gas()], forces=abi.FORCE_PRESSURE)
+        cfg.device = dev
+        g = GpuSolver(cfg, keep)
+        g.set_state({k: state[k] for k in ("r", "v", "m", "rho", "u")})
+        return g
+
+    def acfg(prec, alpha=1.5):
+        return abi.make_adjoint_config(ADJ_STEPS, ADJ_DT, nt, rebuild_every=ADJ_REBUILD,
+                                       checkpoint_every=ADJ_CHECKPOINT, alpha=alpha, precision=prec)
+
+    out = {"particles": n, "targets": nt, "steps": ADJ_STEPS, "dt": ADJ_DT, "rebuild_every": ADJ_REBUILD,
+           "checkpoint_every": ADJ_CHECKPOINT,
+           "workload": f"ideal gas (gamma 5/3) sphere {nt} + impactor {n - nt} at Mach 3, contracting at 5% c_s; "
+                       "continuity + pressure + standard AV, leap-frog, frozen lists; loss = sum |v_target|^2"}
+    grads = {}
+    for name, prec in (("fp64", abi.PRECISION_FP64), ("mixed", abi.PRECISION_MIXED)):
+        with solver(st) as g:
+            g.adjoint_forward(acfg(prec))  # warm-up (allocation, list capacity)
+            g.adjoint_backward()
+            fw, bw = [], []
+            for _ in range(3):
+                t0 = time.perf_counter()
+                loss = g.adjoint_forward(acfg(prec))
+                t1 = time.perf_counter()
+                grads[name] = g.adjoint_backward()
+                t2 = time.perf_counter()
+                fw.append(t1 - t0)
+                bw.append(t2 - t1)
+        f, b = min(fw) * 1e3, min(bw) * 1e3
+        out[name] = {"loss": loss, "forward_ms": f, "backward_ms": b, "forward_ms_per_step": f / ADJ_STEPS,
+                     "backward_ms_per_step": b / ADJ_STEPS, "adjoint_over_forward": b / f}
+    rng = np.random.default_rng(5)
+    eps = 1e-6
+    errs = {"fp64": 0.0, "mixed": 0.0}
+    for _ in range(8):
+        dr = np.zeros((n, 4))
+        for _m in range(3):
+            k = 2.0 * rng.standard_normal(3)
+            ph = 2.0 * np.pi * rng.random()
+            amp = rng.standard_normal(3)
+            dr[:, :3] += np.sin(pos @ k + ph)[:, None] * amp[None, :]
+        dv = np.zeros((n, 4))
+        dv[nt:, :3] = rng.standard_normal(3)
+        da = float(rng.standard_normal())
+        vals = []
+        for sgn in (1.0, -1.0):
+            sp = dict(st)
+            sp["r"] = st["r"] + sgn * eps * dr.ravel()
+            sp["v"] = st["v"] + sgn * eps * dv.ravel()
+            with solver(sp) as g:
+                vals.append(g.adjoint_forward(acfg(abi.PRECISION_FP64, 1.5 + sgn * eps * da)))
+        fd = (vals[0] - vals[1]) / (2 * eps)
+        for name, gr in grads.items():
+            mine = float(np.dot(gr["r"], dr.ravel()) + np.dot(gr["v"], dv.ravel())) + gr["alpha"] * da
+            errs[name] = max(errs[name], abs(mine - fd) / abs(fd))
+    for name in errs:
+        out[name]["fd_max_rel_err_8_directions"] = errs[name]
+    out["mixed_vs_fp64_loss_rel_err"] = abs(out["mixed"]["loss"] - out["fp64"]["loss"]) / abs(out["fp64"]["loss"])
+    return out
+
+
 def cpu_sample(args, st, mats, n, steps):
     """The CPU implementation (oracle restatement of the reference, all host threads) on the same state."""
     from opensph_gb300 import abi
@@ -391,6 +478,8 @@ def main():
         line["fp64"] = res["fp64"]
     if "nbody" in res:
         line["nbody_plummer"] = res["nbody"]
+    if "adjoint" in res:
+        line["adjoint"] = res["adjoint"]
     if not args.no_cpu:
         st, mats, n2 = workload(args)
         value, secs = cpu_sample(args, st, mats, n2, args.cpu_steps)

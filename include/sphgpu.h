@@ -202,6 +202,36 @@ sphgpu_status sphgpu_check_finite(sphgpu_handle* h, uint64_t* first_bad);
 sphgpu_status sphgpu_totals_noalloc(const double* r, const double* v, const double* m, const double* u, uint64_t n,
     double* totals, void* stream);
 
+/* Adjoint of the frozen-list hydrodynamic step (no counterpart in the reference, which has no
+ * differentiation). The model: ideal gas p = (gamma - 1) u rho (IdealGasEos, core/physics/Eos.cpp:42-45),
+ * ContinuityEquation + PressureForce + StandardAV (core/sph/equations/EquationTerm.cpp:42-99, 289-316,
+ * core/sph/equations/av/Standard.h:63-83) with the cubic-spline LUT kernel, leap-frog
+ * (core/timestepping/TimeStepping.cpp:352-391) with the fixed step dt and constant h. The neighbour lists
+ * (|r_i - r_j| < 2 * 0.5 (h_i + h_j)) are rebuilt every rebuild_every steps and held fixed in between.
+ * Loss = sum over particles [0, n_target) of |v|^2 after `steps` steps.
+ * sphgpu_adjoint_forward runs the model from the handle's r, v, m, rho, u (left unchanged) and returns the
+ * loss; it keeps a checkpoint every checkpoint_every steps in device memory (checkpoint_every must divide
+ * rebuild_every). sphgpu_adjoint_backward then returns loss_bar times the gradient of the loss with respect
+ * to the initial r and v (4 doubles per particle, the 4th = 0: h is not differentiated), rho, u and the AV
+ * alpha, recomputing each segment between checkpoints; outputs are host buffers, any may be NULL. Both use
+ * the handle's neighbour grid (call sphgpu_build_neighbors again before sphgpu_get_pairs). precision:
+ * SPHGPU_PRECISION_FP64 or SPHGPU_PRECISION_MIXED (FP32 pair terms, FP64 state and update). */
+typedef struct {
+    uint32_t steps;
+    uint32_t rebuild_every;
+    uint32_t checkpoint_every;
+    uint32_t n_target;
+    double dt;
+    double gamma;   /* adiabatic index */
+    double alpha;   /* StandardAV alpha (differentiated) */
+    double beta;    /* StandardAV beta */
+    int32_t precision;
+    uint32_t reserved;
+} sphgpu_adjoint_config;
+sphgpu_status sphgpu_adjoint_forward(sphgpu_handle* h, const sphgpu_adjoint_config* cfg, double* loss);
+sphgpu_status sphgpu_adjoint_backward(sphgpu_handle* h, double loss_bar, double* grad_r, double* grad_v,
+    double* grad_rho, double* grad_u, double* grad_alpha);
+
 /* Phases of a step, timed with CUDA events when profiling is on; the GPU counterparts of the reference's
  * StatisticsId::GRAVITY_BUILD_TIME, GRAVITY_EVAL_TIME and SPH_EVAL_TIME (core/system/Statistics.h:108-160,
  * set at core/sph/solvers/GravitySolver.cpp:71-90). */

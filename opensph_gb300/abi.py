@@ -211,5 +211,38 @@ def make_config(n, materials, forces=FORCE_PRESSURE | FORCE_SELF_GRAVITY, adapti
     return c, arr
 
 
+class AdjointConfig(ctypes.Structure):
+    """sphgpu_adjoint_config: the frozen-list hydrodynamic model differentiated by sphgpu_adjoint_*."""
+    _fields_ = [
+        ("steps", ctypes.c_uint32),
+        ("rebuild_every", ctypes.c_uint32),
+        ("checkpoint_every", ctypes.c_uint32),
+        ("n_target", ctypes.c_uint32),
+        ("dt", ctypes.c_double),
+        ("gamma", ctypes.c_double),
+        ("alpha", ctypes.c_double),
+        ("beta", ctypes.c_double),
+        ("precision", ctypes.c_int32),
+        ("reserved", ctypes.c_uint32),
+    ]
+
+
+def make_adjoint_config(steps, dt, n_target, rebuild_every=10, checkpoint_every=10, gamma=5.0 / 3.0, alpha=1.5,
+                        beta=3.0, precision=PRECISION_FP64):
+    """StandardAV defaults alpha 1.5, beta 3 (core/system/Settings.cpp:575-578)."""
+    c = AdjointConfig()
+    c.steps = steps
+    c.rebuild_every = rebuild_every
+    c.checkpoint_every = checkpoint_every
+    c.n_target = n_target
+    c.dt = dt
+    c.gamma = gamma
+    c.alpha = alpha
+    c.beta = beta
+    c.precision = precision
+    c.reserved = 0
+    return c
+
+
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIBRARY_PATH = os.path.join(_HERE, "libsphgpu.so")

@@ -30,6 +30,7 @@ UNITS = {
     "sph32.cu": [],
     "gravity32.cu": [],
     "noalloc.cu": [],
+    "adjoint.cu": ["-fmad=false"],
 }
 
 

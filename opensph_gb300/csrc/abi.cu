@@ -45,6 +45,8 @@ struct sphgpu_handle {
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> marks;
     double phase_ms[SPHGPU_PHASE_COUNT] = { 0 };
     unsigned long long launches = 0;
+    // adjoint of the frozen-list hydrodynamic step (allocated by the first sphgpu_adjoint_forward)
+    AdjointState* adjoint = nullptr;
 };
 
 namespace {
@@ -594,6 +596,7 @@ sphgpu_status sphgpu_destroy(sphgpu_handle* h) {
     }
     gridFree(h->grid);
     treeFree(h->tree);
+    adjointFree(h->adjoint);
     if (h->h_pinned) {
         cudaFreeHost(h->h_pinned);
     }
@@ -1000,6 +1003,62 @@ sphgpu_status sphgpu_phase_times(sphgpu_handle* h, double out[SPHGPU_PHASE_COUNT
         h->phase_ms[k] = 0.;
     }
     h->launches = 0;
+    return SPHGPU_OK;
+}
+
+sphgpu_status sphgpu_adjoint_forward(sphgpu_handle* h, const sphgpu_adjoint_config* cfg, double* loss) {
+    if (!h || !cfg || !loss) {
+        return SPHGPU_ERR_ARGUMENT;
+    }
+    if (cfg->rebuild_every == 0 || cfg->checkpoint_every == 0 || cfg->rebuild_every % cfg->checkpoint_every != 0) {
+        return fail(h, SPHGPU_ERR_ARGUMENT,
+            "adjoint: rebuild_every (%u) must be a positive multiple of checkpoint_every (%u)", cfg->rebuild_every,
+            cfg->checkpoint_every);
+    }
+    if (!(cfg->dt > 0.) || !std::isfinite(cfg->dt) || !(cfg->gamma > 1.) || !std::isfinite(cfg->gamma) ||
+        !std::isfinite(cfg->alpha) || !std::isfinite(cfg->beta)) {
+        return fail(h, SPHGPU_ERR_ARGUMENT, "adjoint: dt must be positive, gamma above 1, alpha and beta finite");
+    }
+    if (cfg->precision != SPHGPU_PRECISION_FP64 && cfg->precision != SPHGPU_PRECISION_MIXED) {
+        return fail(h, SPHGPU_ERR_ARGUMENT, "adjoint: unknown precision %d", cfg->precision);
+    }
+    cudaError_t e = adjointConfigure(h->adjoint, h->s.n, *cfg);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(h, SPHGPU_ERR_ALLOCATION, "adjoint: allocation failed: %s", cudaGetErrorString(e));
+    }
+    e = adjointForward(h->adjoint, h->s, h->grid, h->ph, h->d_lut_sph, h->d_lut_sph_f, loss, h->stream);
+    h->launches += adjointTakeLaunches(h->adjoint);
+    if (e != cudaSuccess) {
+        return cudaFail(h, e, "adjoint forward");
+    }
+    return SPHGPU_OK;
+}
+
+sphgpu_status sphgpu_adjoint_backward(sphgpu_handle* h, double loss_bar, double* grad_r, double* grad_v,
+    double* grad_rho, double* grad_u, double* grad_alpha) {
+    if (!h) {
+        return SPHGPU_ERR_ARGUMENT;
+    }
+    if (!adjointForwardDone(h->adjoint)) {
+        return fail(h, SPHGPU_ERR_STATE, "adjoint: sphgpu_adjoint_forward has not run on this handle");
+    }
+    if (!std::isfinite(loss_bar)) {
+        return fail(h, SPHGPU_ERR_ARGUMENT, "adjoint: loss_bar must be finite");
+    }
+    double alphaBar = 0.;
+    cudaError_t e = adjointBackward(h->adjoint, h->s, h->grid, h->ph, h->d_lut_sph, h->d_lut_sph_f, loss_bar,
+        &alphaBar, h->stream);
+    if (e == cudaSuccess) {
+        e = adjointGradients(h->adjoint, grad_r, grad_v, grad_rho, grad_u, h->stream);
+    }
+    h->launches += adjointTakeLaunches(h->adjoint);
+    if (e != cudaSuccess) {
+        return cudaFail(h, e, "adjoint backward");
+    }
+    if (grad_alpha) {
+        *grad_alpha = alphaBar;
+    }
     return SPHGPU_OK;
 }
 

@@ -229,4 +229,18 @@ void launchGravityWalkMixed(const DState& s, Tree& t, const Physics& ph, const f
 void launchGravityPoints(const DState& s, const Tree& t, const Physics& ph, const double* lut_grad,
     const dbl4* points, dbl4* acc, uint32_t npoints, cudaStream_t st);
 
+// ---- adjoint of the frozen-list hydrodynamic step (adjoint.cu) ----
+struct AdjointState;
+cudaError_t adjointConfigure(AdjointState*& a, uint32_t n, const sphgpu_adjoint_config& cfg);
+void adjointFree(AdjointState* a);
+cudaError_t adjointForward(AdjointState* a, const DState& s, Grid& grid, const Physics& ph, const double* lut,
+    const float* lutf, double* loss, cudaStream_t st);
+cudaError_t adjointBackward(AdjointState* a, const DState& s, Grid& grid, const Physics& ph, const double* lut,
+    const float* lutf, double lossBar, double* alphaBar, cudaStream_t st);
+cudaError_t adjointGradients(AdjointState* a, double* gr, double* gv, double* grho, double* gu, cudaStream_t st);
+bool adjointForwardDone(const AdjointState* a);
+bool adjointBackwardDone(const AdjointState* a);
+uint64_t adjointListEntries(const AdjointState* a);
+unsigned long long adjointTakeLaunches(AdjointState* a);
+
 } // namespace sphgpu

@@ -10,6 +10,8 @@ Storage built by InitialConditions; these helpers build such states for the benc
                  target at the origin, impactor at ((R_t+R_i) cos phi + 4 h, (R_t+R_i) sin phi, 0) moving with
                  (-v, 0, 0); FLAG 0 / 1; flaws of ScalarGradyKippModel::setFlaws
                  (core/physics/Damage.cpp:17-126) drawn from a seeded numpy generator.
+* gas_impact   — ideal-gas sphere (rho 1, p 1) hit by a small ideal-gas impactor at a given Mach number: the
+                 workload of the adjoint (the target's particles come first).
 * plummer      — equal-mass Plummer sphere (gravity-only workload; the reference has no Plummer generator).
 """
 import math
@@ -146,6 +148,43 @@ def impact_state(n_target, r_target, n_imp, r_imp, speed=5.0e3, angle_deg=45.0, 
         "n_flaws": np.concatenate([b["n_flaws"] for b in parts]),
     }
     return st, mats
+
+
+def gas_impact(n_target, n_imp, gamma=5.0 / 3.0, mach=3.0, radius=1.0, imp_radius=None, eta=1.3,
+               compression=0.05):
+    """Ideal-gas target sphere (radius 1, rho 1, p 1, so u = 1 / ((gamma - 1) rho)) at the origin and an impactor
+    of the same gas and density, touching it at 45 degrees and moving with -mach * c_s along x. Returns a state
+    dict (r, v as 4 per particle, m, rho, u) and the number of target particles.
+
+    Both bodies also contract uniformly about their centres, v += -kappa (r - centre) with
+    kappa = compression * c_s / radius (the target's surface moves inwards at `compression` c_s). A body at rest
+    or in rigid translation has v_ij . r_ij = 0 for every pair, exactly the switch of the artificial viscosity
+    (core/sph/equations/av/Standard.h:75-77), where the loss has a kink; the contraction moves every initial
+    pair off it. compression=0 gives the bodies at rest / in translation."""
+    rho0, p0 = 1.0, 1.0
+    u0 = p0 / ((gamma - 1.0) * rho0)
+    cs = math.sqrt(gamma * p0 / rho0)
+    if imp_radius is None:
+        imp_radius = radius * (n_imp / n_target) ** (1.0 / 3.0)
+    t = _body(n_target, radius, (0.0, 0.0, 0.0), rho0, u0, eta, 0)
+    phi = math.radians(45.0)
+    h_t = float(t["r"][0, 3])
+    dist = radius + imp_radius
+    center = (dist * math.cos(phi) + 0.5 * h_t, dist * math.sin(phi), 0.0)
+    im = _body(n_imp, imp_radius, center, rho0, u0, eta, 1)
+    im["v"][:, 0] = -mach * cs
+    kappa = compression * cs / radius
+    for b, c in ((t, (0.0, 0.0, 0.0)), (im, center)):
+        b["v"][:, :3] -= kappa * (b["r"][:, :3] - np.asarray(c))
+    parts = [t, im]
+    st = {
+        "r": np.concatenate([b["r"] for b in parts]).ravel(),
+        "v": np.concatenate([b["v"] for b in parts]).ravel(),
+        "m": np.concatenate([b["m"] for b in parts]),
+        "rho": np.concatenate([b["rho"] for b in parts]),
+        "u": np.concatenate([b["u"] for b in parts]),
+    }
+    return st, len(t["m"])
 
 
 def plummer(n, seed=7, softening=1.0e-3, rmax=20.0):

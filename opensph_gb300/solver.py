@@ -60,6 +60,8 @@ def library():
     lib.sphgpu_check_finite.argtypes = [h, ctypes.POINTER(ctypes.c_uint64)]
     lib.sphgpu_set_profiling.argtypes = [h, ctypes.c_int32]
     lib.sphgpu_phase_times.argtypes = [h, _F8P, ctypes.POINTER(ctypes.c_uint64)]
+    lib.sphgpu_adjoint_forward.argtypes = [h, ctypes.POINTER(abi.AdjointConfig), _F8P]
+    lib.sphgpu_adjoint_backward.argtypes = [h, ctypes.c_double, _F8P, _F8P, _F8P, _F8P, _F8P]
     _LIB = lib
     return lib
 
@@ -228,6 +230,22 @@ class GpuSolver:
         launches = ctypes.c_uint64(0)
         self._check(self._lib.sphgpu_phase_times(self._h, out.ctypes.data_as(_F8P), ctypes.byref(launches)))
         return dict(zip(self.PHASES, out.tolist())), launches.value
+
+    def adjoint_forward(self, cfg):
+        """Loss of the frozen-list hydrodynamic model run from the current state (which stays unchanged)."""
+        loss = ctypes.c_double(0.0)
+        self._check(self._lib.sphgpu_adjoint_forward(self._h, ctypes.byref(cfg), ctypes.byref(loss)))
+        return loss.value
+
+    def adjoint_backward(self, loss_bar=1.0):
+        """loss_bar x gradient of the last adjoint_forward's loss: dict r, v (4 per particle), rho, u, alpha."""
+        g = {"r": np.zeros(4 * self.n), "v": np.zeros(4 * self.n), "rho": np.zeros(self.n), "u": np.zeros(self.n)}
+        alpha = ctypes.c_double(0.0)
+        self._check(self._lib.sphgpu_adjoint_backward(
+            self._h, float(loss_bar), g["r"].ctypes.data_as(_F8P), g["v"].ctypes.data_as(_F8P),
+            g["rho"].ctypes.data_as(_F8P), g["u"].ctypes.data_as(_F8P), ctypes.byref(alpha)))
+        g["alpha"] = alpha.value
+        return g
 
     def check_finite(self):
         bad = ctypes.c_uint64(0)

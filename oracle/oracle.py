@@ -199,3 +199,39 @@ def kernel_values(qsqr):
     return (np.array([lib.ora_sph_kernel_value(float(q)) for q in qsqr]),
             np.array([lib.ora_sph_kernel_grad(float(q)) for q in qsqr]),
             np.array([lib.ora_gravity_kernel_grad(float(q)) for q in qsqr]))
+
+
+class FrozenParams(ctypes.Structure):
+    _fields_ = [("steps", ctypes.c_uint32), ("rebuild_every", ctypes.c_uint32), ("n_target", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32), ("dt", ctypes.c_double), ("gamma", ctypes.c_double),
+                ("alpha", ctypes.c_double), ("beta", ctypes.c_double)]
+
+
+def frozen_loss(r, v, m, rho, u, steps, dt, n_target, rebuild_every=10, gamma=5.0 / 3.0, alpha=1.5, beta=3.0,
+                tangent=None):
+    """Loss of the frozen-list model (ora_frozen_loss) and, with tangent = dict of optional r, v (4 per
+    particle), rho, u arrays and an alpha float, its directional derivative. Returns (loss, dloss)."""
+    prm = FrozenParams(steps, rebuild_every, n_target, 0, dt, gamma, alpha, beta)
+    arrs = [np.ascontiguousarray(a, dtype="f8") for a in (r, v, m, rho, u)]
+    n = arrs[2].size
+    tan = tangent or {}
+    tarr = []
+    for name, comps in (("r", 4), ("v", 4), ("rho", 1), ("u", 1)):
+        t = tan.get(name)
+        if t is None:
+            tarr.append(None)
+            continue
+        t = np.ascontiguousarray(t, dtype="f8")
+        if t.size != comps * n:
+            raise ValueError(f"tangent {name}: expected {comps * n} values")
+        tarr.append(t)
+    ptr = [a.ctypes.data_as(_F8) for a in arrs]
+    tptr = [None if t is None else t.ctypes.data_as(_F8) for t in tarr]
+    loss = ctypes.c_double(0.0)
+    dloss = ctypes.c_double(0.0)
+    rc = _lib().ora_frozen_loss(ctypes.byref(prm), ctypes.c_uint64(n), *ptr, *tptr,
+                                ctypes.c_double(float(tan.get("alpha", 0.0))), ctypes.byref(loss),
+                                ctypes.byref(dloss))
+    if rc:
+        raise RuntimeError(f"ora_frozen_loss failed: {rc}")
+    return loss.value, dloss.value

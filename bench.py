@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--no-nbody", action="store_true", help="skip the gravity-only Plummer measurement")
     ap.add_argument("--nbody-n", type=int, default=4_194_304)
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurement")
+    ap.add_argument("--only", choices=["nbody", "adjoint"], default=None,
+                    help="run only the gravity-only or the adjoint measurement and print its JSON (for profiling)")
     ap.add_argument("--adjoint-target", type=int, default=100_000)
     ap.add_argument("--adjoint-impactor", type=int, default=2_000)
     return ap.parse_args()
@@ -452,6 +454,13 @@ def main():
         print(json.dumps(line))
         return
     import torch
+
+    if args.only is not None:
+        dev = int(os.environ.get("LOCAL_RANK", "0"))
+        torch.cuda.set_device(dev)
+        out = nbody(args, dev) if args.only == "nbody" else adjoint(args, dev)
+        print(json.dumps({args.only: out}))
+        return
 
     if world > 1:
         torch.distributed.init_process_group("nccl")

@@ -20,6 +20,8 @@
 // particle list and node list. Each lane owns one particle of the leaf (leaf size <= 32) and evaluates the
 // exact softened pair terms and octupole expansions as soon as the warp classifies them.
 
+#include <algorithm>
+
 #include "tree.cuh"
 
 namespace sphgpu {
@@ -1029,8 +1031,18 @@ __global__ void __launch_bounds__(WALK_THREADS) walkKernel(const dbl4* __restric
     int32_t* listB = listA + listCap;
     int32_t* path = pathSh[wib];
     unsigned long long nApprox = 0, nExact = 0, nPn = 0, nPp = 0;
+    (void)nWarps;
 
-    for (uint32_t li = warpGlobal; li < nLeaves; li += nWarps) {
+    // leaves are taken from a shared counter (stats[4]) so that warps that drew cheap leaves take more
+    for (;;) {
+        uint32_t li = 0;
+        if (lane == 0) {
+            li = uint32_t(atomicAdd(&stats[4], 1ull));
+        }
+        li = __shfl_sync(0xffffffffu, li, 0);
+        if (li >= nLeaves) {
+            break;
+        }
         const int leaf = int(leaves[li]);
         const BhNodeGeom lg = geom[leaf];
         const uint32_t cnt = lg.to - lg.from;
@@ -1055,7 +1067,13 @@ __global__ void __launch_bounds__(WALK_THREADS) walkKernel(const dbl4* __restric
         depth = __shfl_sync(0xffffffffu, depth, 0);
         __syncwarp();
         const bool active = uint32_t(lane) < cnt;
-        const float* lf = nodef + size_t(leaf) * NODEF;
+        const float4* nf = reinterpret_cast<const float4*>(nodef);
+        float lh[3], ll[3];
+        {
+            const float4 a = nodeGroup(nf, leaf, NF_COM_HI), b = nodeGroup(nf, leaf, NF_COM_LO);
+            lh[0] = a.x, lh[1] = a.y, lh[2] = a.z;
+            ll[0] = b.x, ll[1] = b.y, ll[2] = b.z;
+        }
         uint32_t pi = 0;
         dbl4 ri = mkd4(0., 0., 0., 1.);
         if (active) {
@@ -1073,11 +1091,7 @@ __global__ void __launch_bounds__(WALK_THREADS) walkKernel(const dbl4* __restric
             const BhNodeGeom& pg = geom[par];
             const int sib = pg.left == ev ? pg.right : pg.left;
             WalkFrame fr;
-            for (int d = 0; d < 3; ++d) {
-                fr.lh[d] = lf[d];
-                fr.ll[d] = lf[3 + d];
-            }
-            setFrame(fr, geom[ev], nodef + size_t(ev) * NODEF, k == depth);
+            setFrame(fr, nf, ev, k == depth, lh, ll);
             if (lane == 0) {
                 cur[ncur] = sib;
             }
@@ -1090,7 +1104,7 @@ __global__ void __launch_bounds__(WALK_THREADS) walkKernel(const dbl4* __restric
                 int node = -1, cls = CL_KEEP;
                 if (uint32_t(lane) < batch) {
                     node = cur[e];
-                    cls = classifyEntry(node, geom, nodef, fr);
+                    cls = classifyEntry(node, geom, nf, fr, lh, ll);
                 }
                 const unsigned mKeep = __ballot_sync(0xffffffffu, uint32_t(lane) < batch && cls == CL_KEEP);
                 const unsigned mOpen = __ballot_sync(0xffffffffu, cls == CL_OPEN);
@@ -1242,7 +1256,9 @@ cudaError_t treeAllocate(Tree& t, uint32_t n, uint32_t leafSize) {
     const uint32_t nn = n > 0 ? n : 1;
     t.node_capacity = 2 * nn + 8;
     t.seg_capacity = nn + 8;
-    t.walk_warps = 152 * 8 * (WALK_THREADS / 32);
+    // one check-list pair per resident warp: at most 64 warps on each of the 152 SMs, never more warps than
+    // particles (a leaf holds at least one)
+    t.walk_warps = std::min<uint32_t>(152u * 64u, (nn + 3) & ~3u);
     t.walk_capacity = 4096;
     (void)leafSize;
     cudaError_t e = cudaSuccess;
@@ -1261,7 +1277,7 @@ cudaError_t treeAllocate(Tree& t, uint32_t n, uint32_t leafSize) {
     alloc((void**)&t.counters, 8 * sizeof(uint32_t));
     alloc((void**)&t.leaves, nn * sizeof(uint32_t));
     alloc((void**)&t.walk_scratch, size_t(t.walk_warps) * 2 * t.walk_capacity * sizeof(int32_t));
-    alloc((void**)&t.stats, 4 * sizeof(unsigned long long));
+    alloc((void**)&t.stats, 8 * sizeof(unsigned long long)); // 4 interaction counters, [4] next leaf of the walk
     alloc((void**)&t.bbox, 8 * sizeof(unsigned long long));
     alloc((void**)&t.nodef, size_t(t.node_capacity) * NODEF * sizeof(float));
     t.chunk_capacity = 2 * nn / BH_CHUNK + 64;
@@ -1385,7 +1401,7 @@ cudaError_t treeBuild(const DState& s, Tree& t, const Physics& ph, uint32_t* dev
 
 void launchGravityWalk(const DState& s, Tree& t, const Physics& ph, const double* lut, uint32_t* devError,
     cudaStream_t st) {
-    cudaMemsetAsync(t.stats, 0, 4 * sizeof(unsigned long long), st);
+    cudaMemsetAsync(t.stats, 0, 5 * sizeof(unsigned long long), st);
     if (s.n == 0) {
         return;
     }
@@ -1394,7 +1410,14 @@ void launchGravityWalk(const DState& s, Tree& t, const Physics& ph, const double
         // one warp owns a leaf: larger leaves are not supported by this walk
         return;
     }
-    const int blocks = int(t.walk_warps / (WALK_THREADS / 32));
+    static int residentBlocks = 0;
+    if (residentBlocks == 0) {
+        int perSm = 0, sms = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, walkKernel, WALK_THREADS, 0);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+        residentBlocks = std::max(1, perSm * sms);
+    }
+    const int blocks = std::max(1, std::min(residentBlocks, int(t.walk_warps / (WALK_THREADS / 32))));
     launchPrepareWalk(s, t, ph, st);
     walkKernel<<<blocks, WALK_THREADS, 0, st>>>(s.r, s.m, ph.G, t.idx, t.geom, t.mom, t.nodef, t.leaves,
         t.leaf_count, lut,

@@ -145,12 +145,24 @@ __device__ int intersectsBox(const double p[3], double rad, const double lo[3], 
 
 enum : int { CL_KEEP = 0, CL_PARTICLES = 1, CL_NODE = 2, CL_OPEN = 3 };
 
-// per-node FP32 record shared by both walks: com hi[3], com lo[3], m0, q2[6], q3[10], r_open, r_open == 0,
-// box lower corner hi[3] + lo[3], box upper corner hi[3] + lo[3] (40 floats)
+// Per-node FP32 record shared by both walks, 40 floats (160 B) in float4 groups so that every group is one
+// vector load:
+//   [0] com hi x, y, z, M0           [1] com lo x, y, z, signed r_open
+//   [2] q2 xx xy xz yy  [3] q2 yz zz, q3 xxx xxy  [4] q3 xxz xyy xyz xzz  [5] q3 yyy yyz yzz zzz
+//   [6] box lower corner hi  [7] box lower corner lo  [8] box upper corner hi  [9] box upper corner lo
+// Centres and corners are unevaluated float pairs (hi + lo) of the FP64 values. The signed r_open is
+// -r_open for leaves and +r_open for inner nodes; it is (either signed) zero exactly when the FP64 r_open is
+// zero (a tiny positive r_open is stored as the smallest normal float).
 constexpr int NODEF = 40;
-constexpr int NODEF_ROPEN = 23;
-constexpr int NODEF_ZERO = 24;
-constexpr int NODEF_BOX = 25;
+constexpr int NODEF4 = NODEF / 4;
+constexpr int NF_COM_HI = 0;
+constexpr int NF_COM_LO = 1;
+constexpr int NF_MOM = 2;
+constexpr int NF_BOX = 6;
+
+__device__ __forceinline__ float4 nodeGroup(const float4* __restrict__ nf, int node, int group) {
+    return __ldg(nf + size_t(node) * NODEF4 + group);
+}
 
 // Sphere::intersectsBox evaluated in FP32 on coordinates relative to the walking leaf's centre of mass,
 // with a guard band: returns the reference's answer (0 outside, 1 intersection, 2 inside) whenever the FP32
@@ -193,48 +205,58 @@ __device__ __forceinline__ int intersectsBoxGuarded(const float p[3], float rad,
     return ambiguous ? -1 : 2;
 }
 
-// Classification of one check-list entry against the evaluated node (BarnesHut::evalNode,
-// core/gravity/BarnesHut.cpp:233-276): FP32 guarded test first, FP64 test only when it is undecided.
+// The evaluated node (an ancestor of the walking leaf, or the leaf itself) of one level of the dual walk:
+// its box relative to the leaf centre of mass in FP32; the FP64 box is read from the node only for the rare
+// classifications that the guarded FP32 test leaves undecided.
 struct WalkFrame {
-    double elo[3], ehi[3];   // evaluated node box (FP64)
-    float elof[3], ehif[3];  // the same relative to the leaf centre of mass (FP32)
-    float lh[3], ll[3];      // leaf centre of mass as hi + lo floats
+    float elof[3], ehif[3];
+    int ev;
     bool evLeaf;
 };
 
-__device__ __forceinline__ int classifyEntry(int node, const BhNodeGeom* __restrict__ geom,
-    const float* __restrict__ nodef, const WalkFrame& f) {
-    const float* o = nodef + size_t(node) * NODEF;
-    const BhNodeGeom& ng = geom[node];
-    if (o[NODEF_ZERO] != 0.f) {
-        return CL_PARTICLES;
-    }
-    const float p[3] = { (o[0] - f.lh[0]) + (o[3] - f.ll[0]), (o[1] - f.lh[1]) + (o[4] - f.ll[1]),
-        (o[2] - f.lh[2]) + (o[5] - f.ll[2]) };
-    int res = intersectsBoxGuarded(p, o[NODEF_ROPEN], f.elof, f.ehif);
-    if (res < 0) {
-        res = intersectsBox(ng.com, ng.r_open, f.elo, f.ehi);
-    }
-    if (res == 2 || (f.evLeaf && res != 0)) {
-        return ng.left < 0 ? CL_PARTICLES : CL_OPEN;
-    }
-    return res == 0 ? CL_NODE : CL_KEEP;
-}
-
-// The evaluated node's box relative to the leaf centre, formed from hi + lo float pairs (no FP64 arithmetic);
-// the FP64 box is loaded for the rare undecided classifications.
-__device__ __forceinline__ void setFrame(WalkFrame& f, const BhNodeGeom& ev, const float* __restrict__ evf,
-    bool evLeaf) {
-    const float* b = evf + NODEF_BOX;
-    for (int d = 0; d < 3; ++d) {
-        f.elo[d] = ev.lo[d];
-        f.ehi[d] = ev.hi[d];
-        f.elof[d] = (b[d] - f.lh[d]) + (b[3 + d] - f.ll[d]);
-        f.ehif[d] = (b[6 + d] - f.lh[d]) + (b[9 + d] - f.ll[d]);
-    }
+// lh / ll: the leaf centre of mass as hi + lo floats
+__device__ __forceinline__ void setFrame(WalkFrame& f, const float4* __restrict__ nf, int ev, bool evLeaf,
+    const float lh[3], const float ll[3]) {
+    const float4 lo_h = nodeGroup(nf, ev, NF_BOX), lo_l = nodeGroup(nf, ev, NF_BOX + 1);
+    const float4 hi_h = nodeGroup(nf, ev, NF_BOX + 2), hi_l = nodeGroup(nf, ev, NF_BOX + 3);
+    f.elof[0] = (lo_h.x - lh[0]) + (lo_l.x - ll[0]);
+    f.elof[1] = (lo_h.y - lh[1]) + (lo_l.y - ll[1]);
+    f.elof[2] = (lo_h.z - lh[2]) + (lo_l.z - ll[2]);
+    f.ehif[0] = (hi_h.x - lh[0]) + (hi_l.x - ll[0]);
+    f.ehif[1] = (hi_h.y - lh[1]) + (hi_l.y - ll[1]);
+    f.ehif[2] = (hi_h.z - lh[2]) + (hi_l.z - ll[2]);
+    f.ev = ev;
     f.evLeaf = evLeaf;
 }
 
+// FP64 sphere-box test of a node's opening sphere against the evaluated node's box, for the classifications
+// the FP32 test leaves undecided (rare; kept out of line so that it adds no registers to the walk loops)
+__device__ __noinline__ int intersectsNodeBox(const BhNodeGeom* __restrict__ geom, int node, int ev) {
+    const BhNodeGeom& ng = geom[node];
+    const BhNodeGeom& eg = geom[ev];
+    return intersectsBox(ng.com, ng.r_open, eg.lo, eg.hi);
+}
+
+// Classification of one check-list entry against the evaluated node (BarnesHut::evalNode,
+// core/gravity/BarnesHut.cpp:233-276): FP32 guarded test first, FP64 test only when it is undecided.
+__device__ __forceinline__ int classifyEntry(int node, const BhNodeGeom* __restrict__ geom,
+    const float4* __restrict__ nf, const WalkFrame& f, const float lh[3], const float ll[3]) {
+    const float4 a = nodeGroup(nf, node, NF_COM_HI), b = nodeGroup(nf, node, NF_COM_LO);
+    const float ro = fabsf(b.w);
+    const bool leaf = signbit(b.w);
+    if (ro == 0.f) {
+        return CL_PARTICLES;
+    }
+    const float p[3] = { (a.x - lh[0]) + (b.x - ll[0]), (a.y - lh[1]) + (b.y - ll[1]), (a.z - lh[2]) + (b.z - ll[2]) };
+    int res = intersectsBoxGuarded(p, ro, f.elof, f.ehif);
+    if (res < 0) {
+        res = intersectsNodeBox(geom, node, f.ev);
+    }
+    if (res == 2 || (f.evLeaf && res != 0)) {
+        return leaf ? CL_PARTICLES : CL_OPEN;
+    }
+    return res == 0 ? CL_NODE : CL_KEEP;
+}
 
 } // namespace
 } // namespace sphgpu

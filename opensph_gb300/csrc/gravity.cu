@@ -12,7 +12,7 @@
 // with the reference's first-occurrence tie rule; after more than five consecutive slides the reference's
 // std::nth_element is replayed by one thread (libstdc++ introselect). Leaf membership and the order of the
 // particles inside each leaf are therefore identical to the reference's, and so are the leaf boxes and
-// centres of mass. Moments are then formed bottom-up, one launch per level.
+// centres of mass. Moments are then formed bottom-up in one launch (momentsUpKernel).
 //
 // Walk: one warp per leaf replays the reference's dual walk along the leaf's root path: at each ancestor
 // the pending check-list entries are classified against that ancestor's box with the reference's
@@ -353,7 +353,7 @@ __device__ void blockArgExtreme(double& val, uint32_t& pos, bool isMax, double* 
 __global__ void __launch_bounds__(BUILD_THREADS) splitLevelKernel(PosView pv, uint32_t* idx, uint32_t* posB,
     uint32_t* posS, const BhSegment* segIn, uint32_t nIn, BhSegment* segOut, BhNodeGeom* geom, uint32_t* counters,
     uint32_t* leaves, uint32_t leafSize, uint32_t nodeCapacity, uint32_t segCapacity, uint32_t* devError,
-    uint32_t maxSize) {
+    uint32_t minSize, uint32_t maxSize) {
     __shared__ uint32_t shScan[32];
     __shared__ double shV[32];
     __shared__ uint32_t shP[32];
@@ -363,8 +363,8 @@ __global__ void __launch_bounds__(BUILD_THREADS) splitLevelKernel(PosView pv, ui
         const BhSegment sg = segIn[sidx];
         const uint32_t from = sg.from, to = sg.to;
         const int node = sg.node;
-        if (to - from > maxSize) {
-            continue; // large segments are split by the multi-CTA pipeline below
+        if (to - from > maxSize || to - from <= minSize) {
+            continue; // large segments: the multi-CTA pipeline below; small ones: splitWarpKernel
         }
         if (to - from <= leafSize) {
             // KdTree::addLeaf: tight box of the leaf's points
@@ -562,6 +562,235 @@ __global__ void __launch_bounds__(BUILD_THREADS) splitLevelKernel(PosView pv, ui
             atomicMax(&counters[4], max(n1 - from, to - n1));
         }
         __syncthreads();
+    }
+}
+
+// The same split for segments of at most WARP_SEGMENT elements (the deep levels, tens of thousands of small
+// segments): one warp per segment, warp ballots and shuffles instead of block scans and barriers. The
+// partition, the sliding-midpoint moves and the child segments are identical to splitLevelKernel's.
+constexpr uint32_t WARP_SEGMENT = 1024;
+constexpr int SPLIT_WARP_THREADS = 256;
+
+__device__ __forceinline__ void warpArgExtreme(double& val, uint32_t& pos, bool isMax) {
+    for (int off = 16; off > 0; off >>= 1) {
+        const double ov = __shfl_xor_sync(0xffffffffu, val, off);
+        const uint32_t op = __shfl_xor_sync(0xffffffffu, pos, off);
+        const bool better = isMax ? (ov > val || (ov == val && op < pos)) : (ov < val || (ov == val && op < pos));
+        if (better) {
+            val = ov;
+            pos = op;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(SPLIT_WARP_THREADS) splitWarpKernel(PosView pv, uint32_t* idx, uint32_t* posB,
+    uint32_t* posS, const BhSegment* segIn, uint32_t nIn, BhSegment* segOut, BhNodeGeom* geom, uint32_t* counters,
+    uint32_t* leaves, uint32_t leafSize, uint32_t nodeCapacity, uint32_t segCapacity, uint32_t* devError,
+    uint32_t maxSize) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t warpGlobal = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nWarps = (gridDim.x * blockDim.x) >> 5;
+    const unsigned below = (1u << lane) - 1u;
+    for (uint32_t sidx = warpGlobal; sidx < nIn; sidx += nWarps) {
+        const BhSegment sg = segIn[sidx];
+        const uint32_t from = sg.from, to = sg.to;
+        const int node = sg.node;
+        if (to - from > maxSize) {
+            continue;
+        }
+        if (to - from <= leafSize) {
+            // KdTree::addLeaf: tight box of the leaf's points (min / max are exact in any order)
+            double lo[3] = { DBL_MAX, DBL_MAX, DBL_MAX }, hi[3] = { -DBL_MAX, -DBL_MAX, -DBL_MAX };
+            for (uint32_t k = from + lane; k < to; k += 32) {
+                const dbl4 p = pv.r[idx[k]];
+                const double x[3] = { p.x, p.y, p.z };
+                for (int d = 0; d < 3; ++d) {
+                    lo[d] = fmin(lo[d], x[d]);
+                    hi[d] = fmax(hi[d], x[d]);
+                }
+            }
+            for (int off = 16; off > 0; off >>= 1) {
+                for (int d = 0; d < 3; ++d) {
+                    lo[d] = fmin(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], off));
+                    hi[d] = fmax(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], off));
+                }
+            }
+            if (lane == 0) {
+                BhNodeGeom& g = geom[node];
+                for (int d = 0; d < 3; ++d) {
+                    g.lo[d] = lo[d];
+                    g.hi[d] = hi[d];
+                }
+                g.left = -1;
+                g.right = -1;
+                g.from = from;
+                g.to = to;
+                const uint32_t slot = atomicAdd(&counters[2], 1u);
+                leaves[slot] = uint32_t(node);
+            }
+            continue;
+        }
+        double boxSize[3];
+        for (int d = 0; d < 3; ++d) {
+            boxSize[d] = sg.hi[d] - sg.lo[d];
+        }
+        int splitIdx = argMax3(boxSize);
+        bool diff[3] = { false, false, false };
+        {
+            const uint32_t il = idx[to - 1];
+            const dbl4 pl = pv.r[il];
+            const double last[3] = { pl.x, pl.y, pl.z };
+            for (uint32_t k = from + lane; k < to; k += 32) {
+                const dbl4 p = pv.r[idx[k]];
+                const double x[3] = { p.x, p.y, p.z };
+                for (int d = 0; d < 3; ++d) {
+                    diff[d] = diff[d] || (x[d] != last[d]);
+                }
+            }
+        }
+        bool nonSingular[3];
+        for (int d = 0; d < 3; ++d) {
+            nonSingular[d] = __any_sync(0xffffffffu, diff[d]);
+        }
+        bool degenerated = false;
+        for (int dim = 0; dim < 3; ++dim) {
+            if (!nonSingular[splitIdx]) {
+                boxSize[splitIdx] = 0.;
+                splitIdx = argMax3(boxSize);
+                if (boxSize[0] == 0. && boxSize[1] == 0. && boxSize[2] == 0.) {
+                    degenerated = true;
+                    break;
+                }
+            } else {
+                break;
+            }
+        }
+        double splitPosition = 0.5 * (sg.lo[splitIdx] + sg.hi[splitIdx]);
+        uint32_t n1;
+        bool sliding = false;
+        double lo1[3], hi1[3], lo2[3], hi2[3];
+        for (int d = 0; d < 3; ++d) {
+            lo1[d] = lo2[d] = sg.lo[d];
+            hi1[d] = hi2[d] = sg.hi[d];
+        }
+        if (sg.sliding <= 5 && !degenerated) {
+            uint32_t nB = 0, nS = 0;
+            for (uint32_t k0 = from; k0 < to; k0 += 32) {
+                const uint32_t k = k0 + lane;
+                bool isB = false, isS = false;
+                if (k < to) {
+                    const double x = pv.val(idx[k], splitIdx);
+                    isB = x > splitPosition;
+                    isS = x < splitPosition;
+                }
+                const unsigned mB = __ballot_sync(0xffffffffu, isB), mS = __ballot_sync(0xffffffffu, isS);
+                if (isB) {
+                    posB[from + nB + __popc(mB & below)] = k;
+                }
+                if (isS) {
+                    posS[from + nS + __popc(mS & below)] = k;
+                }
+                nB += __popc(mB);
+                nS += __popc(mS);
+            }
+            __syncwarp();
+            const uint32_t m = min(nB, nS);
+            uint32_t cntLocal = 0;
+            for (uint32_t k = lane; k < m; k += 32) {
+                cntLocal += (posB[from + k] < posS[from + nS - 1 - k]) ? 1u : 0u;
+            }
+            const uint32_t K = __reduce_add_sync(0xffffffffu, cntLocal);
+            for (uint32_t k = lane; k < K; k += 32) {
+                const uint32_t a = posB[from + k], b = posS[from + nS - 1 - k];
+                const uint32_t t = idx[a];
+                idx[a] = idx[b];
+                idx[b] = t;
+            }
+            __syncwarp();
+            uint32_t n1b = K < nB ? posB[from + K] : to;
+            if (K >= 1) {
+                n1b = min(n1b, posS[from + nS - K]);
+            }
+            n1 = n1b;
+            if (n1 == from || n1 == to) {
+                const bool isMax = (n1 == to);
+                double val = isMax ? -DBL_MAX : DBL_MAX;
+                uint32_t pos = 0xffffffffu;
+                for (uint32_t k = from + lane; k < to; k += 32) {
+                    const double x = pv.val(idx[k], splitIdx);
+                    const bool better = isMax ? (x > val || (x == val && k < pos)) : (x < val || (x == val && k < pos));
+                    if (better) {
+                        val = x;
+                        pos = k;
+                    }
+                }
+                warpArgExtreme(val, pos, isMax);
+                __syncwarp();
+                if (lane == 0) {
+                    const uint32_t dst = isMax ? to - 1 : from;
+                    const uint32_t t = idx[dst];
+                    idx[dst] = idx[pos];
+                    idx[pos] = t;
+                }
+                __syncwarp();
+                splitPosition = val;
+                n1 = isMax ? to - 1 : from + 1;
+                sliding = true;
+            }
+            hi1[splitIdx] = splitPosition;
+            lo2[splitIdx] = splitPosition;
+        } else {
+            n1 = (from + to) >> 1;
+            if (!degenerated && lane == 0) {
+                NthCtx c{ idx, pv, splitIdx };
+                nthElement(c, long(from), long(n1), long(to));
+            }
+            __syncwarp();
+            const double x = pv.val(idx[n1], splitIdx);
+            hi1[splitIdx] = x;
+            lo2[splitIdx] = x;
+        }
+        if (lane == 0) {
+            uint32_t child = atomicAdd(&counters[0], 2u);
+            const uint32_t slot = atomicAdd(&counters[1], 2u);
+            if (child + 2 > nodeCapacity || slot + 2 > segCapacity) {
+                atomicOr(devError, child + 2 > nodeCapacity ? uint32_t(DEV_ERR_NODE_CAPACITY)
+                                                            : uint32_t(DEV_ERR_SEGMENT_CAPACITY));
+                child = 0xffffffffu;
+            }
+            if (child != 0xffffffffu) {
+                BhNodeGeom& g = geom[node];
+                g.left = int32_t(child);
+                g.right = int32_t(child + 1);
+                g.from = from;
+                g.to = to;
+                const int lvl = g.level;
+                geom[child].parent = node;
+                geom[child].level = lvl + 1;
+                geom[child + 1].parent = node;
+                geom[child + 1].level = lvl + 1;
+                const uint32_t next = sliding ? sg.sliding + 1 : 0;
+                BhSegment l, r;
+                l.from = from;
+                l.to = n1;
+                l.node = int32_t(child);
+                l.sliding = next;
+                r.from = n1;
+                r.to = to;
+                r.node = int32_t(child + 1);
+                r.sliding = next;
+                for (int d = 0; d < 3; ++d) {
+                    l.lo[d] = lo1[d];
+                    l.hi[d] = hi1[d];
+                    r.lo[d] = lo2[d];
+                    r.hi[d] = hi2[d];
+                }
+                segOut[slot] = l;
+                segOut[slot + 1] = r;
+                atomicMax(&counters[4], max(n1 - from, to - n1));
+            }
+        }
+        __syncwarp();
     }
 }
 
@@ -960,55 +1189,92 @@ __device__ void shiftAdd(const BhNodeMoments& c, const double d[3], double q2[6]
     }
 }
 
-__global__ void momentsLevelKernel(const dbl4* __restrict__ r, const double* __restrict__ m, double G,
-    const uint32_t* __restrict__ idx, double thetaInv, BhNodeGeom* geom, BhNodeMoments* mom, uint32_t first,
-    uint32_t last) {
-    const uint32_t id = first + blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= last) {
+// BarnesHut::buildInner (core/gravity/BarnesHut.cpp:439-489): box, centre of mass, opening radius and the
+// children's moments moved to the new centre (left child first)
+__device__ void buildInner(double thetaInv, BhNodeGeom& g, const BhNodeGeom& gl, const BhNodeGeom& gr,
+    const BhNodeMoments& ml, const BhNodeMoments& mr, BhNodeMoments& mo) {
+    for (int d = 0; d < 3; ++d) {
+        g.lo[d] = fmin(gl.lo[d], gr.lo[d]);
+        g.hi[d] = fmax(gl.hi[d], gr.hi[d]);
+    }
+    const double mt = ml.m0 + mr.m0;
+    for (int k = 0; k < 6; ++k) {
+        mo.q2[k] = 0.;
+    }
+    for (int k = 0; k < 10; ++k) {
+        mo.q3[k] = 0.;
+    }
+    mo.pad = 0.;
+    if (mt == 0.) {
+        mo.m0 = 0.;
+        g.com[0] = g.com[1] = g.com[2] = 0.;
+        g.r_open = 0.;
         return;
     }
-    BhNodeGeom g = geom[id];
-    BhNodeMoments mo;
-    if (g.left < 0) {
-        buildLeaf(r, m, G, idx, thetaInv, g, mo);
-    } else {
-        // BarnesHut::buildInner (core/gravity/BarnesHut.cpp:439-489)
-        const BhNodeGeom& gl = geom[g.left];
-        const BhNodeGeom& gr = geom[g.right];
-        for (int d = 0; d < 3; ++d) {
-            g.lo[d] = fmin(gl.lo[d], gr.lo[d]);
-            g.hi[d] = fmax(gl.hi[d], gr.hi[d]);
-        }
-        const BhNodeMoments& ml = mom[g.left];
-        const BhNodeMoments& mr = mom[g.right];
-        const double mt = ml.m0 + mr.m0;
-        for (int k = 0; k < 6; ++k) {
-            mo.q2[k] = 0.;
-        }
-        for (int k = 0; k < 10; ++k) {
-            mo.q3[k] = 0.;
-        }
-        if (mt == 0.) {
-            mo.m0 = 0.;
-            g.com[0] = g.com[1] = g.com[2] = 0.;
-            g.r_open = 0.;
-        } else {
-            for (int d = 0; d < 3; ++d) {
-                g.com[d] = (ml.m0 * gl.com[d] + mr.m0 * gr.com[d]) / mt;
-            }
-            const double rmx = fmax(g.com[0] - g.lo[0], g.hi[0] - g.com[0]);
-            const double rmy = fmax(g.com[1] - g.lo[1], g.hi[1] - g.com[1]);
-            const double rmz = fmax(g.com[2] - g.lo[2], g.hi[2] - g.com[2]);
-            g.r_open = 2. / sqrt(3.) * thetaInv * sqrt(rmx * rmx + rmy * rmy + rmz * rmz);
-            mo.m0 = mt;
-            const double dl[3] = { gl.com[0] - g.com[0], gl.com[1] - g.com[1], gl.com[2] - g.com[2] };
-            shiftAdd(ml, dl, mo.q2, mo.q3);
-            const double dr[3] = { gr.com[0] - g.com[0], gr.com[1] - g.com[1], gr.com[2] - g.com[2] };
-            shiftAdd(mr, dr, mo.q2, mo.q3);
-        }
+    for (int d = 0; d < 3; ++d) {
+        g.com[d] = (ml.m0 * gl.com[d] + mr.m0 * gr.com[d]) / mt;
     }
-    geom[id] = g;
-    mom[id] = mo;
+    const double rmx = fmax(g.com[0] - g.lo[0], g.hi[0] - g.com[0]);
+    const double rmy = fmax(g.com[1] - g.lo[1], g.hi[1] - g.com[1]);
+    const double rmz = fmax(g.com[2] - g.lo[2], g.hi[2] - g.com[2]);
+    g.r_open = 2. / sqrt(3.) * thetaInv * sqrt(rmx * rmx + rmy * rmy + rmz * rmz);
+    mo.m0 = mt;
+    const double dl[3] = { gl.com[0] - g.com[0], gl.com[1] - g.com[1], gl.com[2] - g.com[2] };
+    shiftAdd(ml, dl, mo.q2, mo.q3);
+    const double dr[3] = { gr.com[0] - g.com[0], gr.com[1] - g.com[1], gr.com[2] - g.com[2] };
+    shiftAdd(mr, dr, mo.q2, mo.q3);
+}
+
+// loads that bypass L1 (the sibling subtree was written by another SM during this launch)
+template <typename T>
+__device__ __forceinline__ T loadCG(const T* p) {
+    static_assert(sizeof(T) % 8 == 0, "8-byte multiple");
+    T out;
+    const unsigned long long* src = reinterpret_cast<const unsigned long long*>(p);
+    unsigned long long* dst = reinterpret_cast<unsigned long long*>(&out);
+    for (size_t k = 0; k < sizeof(T) / 8; ++k) {
+        dst[k] = __ldcg(src + k);
+    }
+    return out;
+}
+
+// All moments in one launch, bottom-up: one thread per leaf forms the leaf's moments, then climbs; at each
+// inner node the thread that arrives second (atomic counter per node) forms the node from its two finished
+// children, the first one stops. Nothing waits, so the launch always completes; every node gets the same
+// values in any arrival order (children combined left then right).
+__global__ void momentsUpKernel(const dbl4* __restrict__ r, const double* __restrict__ m, double G,
+    const uint32_t* __restrict__ idx, double thetaInv, BhNodeGeom* geom, BhNodeMoments* mom,
+    const uint32_t* __restrict__ leaves, uint32_t nLeaves, uint32_t* visits) {
+    const uint32_t li = blockIdx.x * blockDim.x + threadIdx.x;
+    if (li >= nLeaves) {
+        return;
+    }
+    int node = int(leaves[li]);
+    {
+        BhNodeGeom g = geom[node];
+        BhNodeMoments mo;
+        buildLeaf(r, m, G, idx, thetaInv, g, mo);
+        geom[node] = g;
+        mom[node] = mo;
+    }
+    int parent = loadCG(&geom[node]).parent;
+    while (parent >= 0) {
+        __threadfence();
+        if (atomicAdd(&visits[parent], 1u) == 0) {
+            return;
+        }
+        __threadfence();
+        BhNodeGeom g = loadCG(&geom[parent]);
+        const BhNodeGeom gl = loadCG(&geom[g.left]);
+        const BhNodeGeom gr = loadCG(&geom[g.right]);
+        const BhNodeMoments ml = loadCG(&mom[g.left]);
+        const BhNodeMoments mr = loadCG(&mom[g.right]);
+        BhNodeMoments mo;
+        buildInner(thetaInv, g, gl, gr, ml, mr, mo);
+        geom[parent] = g;
+        mom[parent] = mo;
+        parent = g.parent;
+    }
 }
 
 // ---------------------------------------------------------------------------------------------------------
@@ -1276,6 +1542,7 @@ cudaError_t treeAllocate(Tree& t, uint32_t n, uint32_t leafSize) {
     alloc((void**)&t.seg[1], size_t(t.seg_capacity) * sizeof(BhSegment));
     alloc((void**)&t.counters, 8 * sizeof(uint32_t));
     alloc((void**)&t.leaves, nn * sizeof(uint32_t));
+    alloc((void**)&t.visits, size_t(t.node_capacity) * sizeof(uint32_t));
     alloc((void**)&t.walk_scratch, size_t(t.walk_warps) * 2 * t.walk_capacity * sizeof(int32_t));
     alloc((void**)&t.stats, 8 * sizeof(unsigned long long)); // 4 interaction counters, [4] next leaf of the walk
     alloc((void**)&t.bbox, 8 * sizeof(unsigned long long));
@@ -1295,7 +1562,7 @@ cudaError_t treeAllocate(Tree& t, uint32_t n, uint32_t leafSize) {
 }
 
 void treeFree(Tree& t) {
-    void* ptrs[] = { t.idx, t.scratch_b, t.scratch_s, t.geom, t.mom, t.seg[0], t.seg[1], t.counters, t.leaves,
+    void* ptrs[] = { t.idx, t.scratch_b, t.scratch_s, t.geom, t.mom, t.seg[0], t.seg[1], t.counters, t.leaves, t.visits,
         t.walk_scratch, t.stats, t.bbox, t.nodef, t.pf, t.mf, t.chunks, t.chunk_stats, t.chunk_off_b, t.chunk_off_s,
         t.work };
     for (void* p : ptrs) {
@@ -1341,9 +1608,16 @@ cudaError_t treeBuild(const DState& s, Tree& t, const Physics& ph, uint32_t* dev
                 t.chunks, t.work, t.chunk_capacity, devError);
             t.launches++;
         }
-        splitLevelKernel<<<grid, BUILD_THREADS, 0, st>>>(pv, t.idx, t.scratch_b, t.scratch_s, t.seg[cur], nIn,
-            t.seg[1 - cur], t.geom, t.counters, t.leaves, ph.leaf_size, t.node_capacity, t.seg_capacity, devError,
-            BH_SMALL_SEGMENT);
+        if (maxSeg > WARP_SEGMENT) {
+            splitLevelKernel<<<grid, BUILD_THREADS, 0, st>>>(pv, t.idx, t.scratch_b, t.scratch_s, t.seg[cur], nIn,
+                t.seg[1 - cur], t.geom, t.counters, t.leaves, ph.leaf_size, t.node_capacity, t.seg_capacity, devError,
+                WARP_SEGMENT, BH_SMALL_SEGMENT);
+            t.launches++;
+        }
+        const uint32_t warpBlocks = min(uint32_t(ceilDiv(nIn, SPLIT_WARP_THREADS / 32)), 152u * 8u);
+        splitWarpKernel<<<warpBlocks, SPLIT_WARP_THREADS, 0, st>>>(pv, t.idx, t.scratch_b, t.scratch_s, t.seg[cur],
+            nIn, t.seg[1 - cur], t.geom, t.counters, t.leaves, ph.leaf_size, t.node_capacity, t.seg_capacity,
+            devError, WARP_SEGMENT);
         t.launches++;
         if (big) {
             cudaMemcpyAsync(t.counters_host, t.counters, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
@@ -1385,15 +1659,12 @@ cudaError_t treeBuild(const DState& s, Tree& t, const Physics& ph, uint32_t* dev
             break;
         }
     }
-    // bottom-up moments, deepest level first
-    const double G = ph.G;
-    for (int L = int(t.level_start.size()) - 2; L >= 0; --L) {
-        const uint32_t first = t.level_start[L], last = t.level_start[L + 1];
-        if (last > first) {
-            t.launches++;
-            momentsLevelKernel<<<ceilDiv(last - first, 128), 128, 0, st>>>(s.r, s.m, G, t.idx, ph.theta_inv, t.geom,
-                t.mom, first, last);
-        }
+    // moments, bottom-up in one launch
+    cudaMemsetAsync(t.visits, 0, size_t(t.node_count) * sizeof(uint32_t), st);
+    if (t.leaf_count > 0) {
+        momentsUpKernel<<<ceilDiv(t.leaf_count, 128), 128, 0, st>>>(s.r, s.m, ph.G, t.idx, ph.theta_inv, t.geom,
+            t.mom, t.leaves, t.leaf_count, t.visits);
+        t.launches++;
     }
     t.built = true;
     return cudaGetLastError();

@@ -170,6 +170,7 @@ struct Tree {
     uint32_t* counters = nullptr;     // device: [0] node count, [1] next-level segment count, [2] leaf count
     uint32_t* counters_host = nullptr; // pinned mirror
     uint32_t* leaves = nullptr;       // leaf node ids
+    uint32_t* visits = nullptr;       // per node: children finished (bottom-up moments)
     int32_t* walk_scratch = nullptr;  // per-warp checklists
     uint32_t walk_warps = 0;
     uint32_t walk_capacity = 0;       // entries per list per warp

@@ -47,6 +47,10 @@ struct sphgpu_handle {
     unsigned long long launches = 0;
     // adjoint of the frozen-list hydrodynamic step (allocated by the first sphgpu_adjoint_forward)
     AdjointState* adjoint = nullptr;
+    // self-gravity runs on its own higher-priority stream, concurrently with the SPH pair loop
+    cudaStream_t gstream = nullptr;
+    cudaEvent_t ev_fork = nullptr;
+    cudaEvent_t ev_join = nullptr;
 };
 
 namespace {
@@ -86,17 +90,19 @@ cudaEvent_t takeEvent(sphgpu_handle* h) {
 struct Phase {
     sphgpu_handle* h;
     int id;
+    cudaStream_t stream;
     cudaEvent_t start = nullptr;
-    Phase(sphgpu_handle* hh, int phase) : h(hh), id(phase) {
+    Phase(sphgpu_handle* hh, int phase) : Phase(hh, phase, hh->stream) {}
+    Phase(sphgpu_handle* hh, int phase, cudaStream_t st) : h(hh), id(phase), stream(st) {
         if (h->profiling) {
             start = takeEvent(h);
-            cudaEventRecord(start, h->stream);
+            cudaEventRecord(start, stream);
         }
     }
     ~Phase() {
         if (h->profiling && start) {
             cudaEvent_t end = takeEvent(h);
-            cudaEventRecord(end, h->stream);
+            cudaEventRecord(end, stream);
             h->marks.push_back({ id, { start, end } });
         }
     }
@@ -295,22 +301,23 @@ sphgpu_status checkDeviceError(sphgpu_handle* h) {
 }
 
 // gravity build + walk into s.agrav (GravitySolver::loop, first half)
-sphgpu_status evalGravity(sphgpu_handle* h) {
+// BarnesHut::build + evalSelfGravity into s.agrav, queued on stream st
+sphgpu_status evalGravity(sphgpu_handle* h, cudaStream_t st) {
     {
-        Phase ph(h, SPHGPU_PHASE_GRAVITY_BUILD);
-        cudaError_t e = treeBuild(h->s, h->tree, h->ph, h->d_err, h->stream);
+        Phase ph(h, SPHGPU_PHASE_GRAVITY_BUILD, st);
+        cudaError_t e = treeBuild(h->s, h->tree, h->ph, h->d_err, st);
         if (e != cudaSuccess) {
             return cudaFail(h, e, "gravity build");
         }
         h->launches += h->tree.launches;
     }
     {
-        Phase ph(h, SPHGPU_PHASE_GRAVITY_EVAL);
+        Phase ph(h, SPHGPU_PHASE_GRAVITY_EVAL, st);
         if (h->ph.precision == SPHGPU_PRECISION_MIXED) {
-            launchGravityWalkMixed(h->s, h->tree, h->ph, h->d_lut_grav_f, h->d_err, h->stream);
+            launchGravityWalkMixed(h->s, h->tree, h->ph, h->d_lut_grav_f, h->d_err, st);
             h->launches += 2;
         } else {
-            launchGravityWalk(h->s, h->tree, h->ph, h->d_lut_grav, h->d_err, h->stream);
+            launchGravityWalk(h->s, h->tree, h->ph, h->d_lut_grav, h->d_err, st);
             h->launches += 2;
         }
     }
@@ -318,14 +325,8 @@ sphgpu_status evalGravity(sphgpu_handle* h) {
     return SPHGPU_OK;
 }
 
-// the derivative evaluation of ISolver::integrate after the materials were initialized
-sphgpu_status evalDerivatives(sphgpu_handle* h) {
-    if (h->ph.gravity) {
-        const sphgpu_status st = evalGravity(h);
-        if (st != SPHGPU_OK) {
-            return st;
-        }
-    }
+// neighbour grid + pair loop on the main stream; gravityInLoop: the pair loop adds s.agrav itself
+void evalSph(sphgpu_handle* h, bool gravityInLoop) {
     {
         Phase ph(h, SPHGPU_PHASE_NEIGHBORS);
         launchGridBuild(h->s, h->grid, h->ph, h->stream);
@@ -333,13 +334,40 @@ sphgpu_status evalDerivatives(sphgpu_handle* h) {
         launchGatherSorted(h->s, h->grid, h->ph, h->stream);
         h->launches += h->grid.launches;
     }
+    Phase ph(h, SPHGPU_PHASE_SPH_EVAL);
+    Physics phs = h->ph;
+    phs.gravity = gravityInLoop ? h->ph.gravity : 0;
+    if (h->ph.precision == SPHGPU_PRECISION_MIXED) {
+        launchPairSumMixed(h->s, h->grid, phs, h->d_mats, h->d_lut_sph_f, h->stream);
+    } else {
+        launchPairSum64(h->s, h->grid, phs, h->d_mats, h->d_lut_sph, h->stream);
+    }
+    h->launches += 1;
+}
+
+// the derivative evaluation of ISolver::integrate after the materials were initialized. With self-gravity
+// the order of GravitySolver::loop (core/sph/solvers/GravitySolver.cpp:64-91: gravity into the accumulator,
+// then the pair loop) is kept in the arithmetic, not in time: the pair loop (main stream) and the tree build
+// + walk (gravity stream, higher priority) run concurrently, and after both dv = a_gravity + a_sph, the same
+// sum the reference forms. The pair loop is queued first because the tree build waits on the host for
+// its own stream between levels.
+sphgpu_status evalDerivatives(sphgpu_handle* h) {
+    if (!h->ph.gravity) {
+        evalSph(h, false);
+        return SPHGPU_OK;
+    }
+    CUDA_TRY(h, cudaEventRecord(h->ev_fork, h->stream));
+    CUDA_TRY(h, cudaStreamWaitEvent(h->gstream, h->ev_fork, 0));
+    evalSph(h, false);
+    const sphgpu_status st = evalGravity(h, h->gstream);
+    if (st != SPHGPU_OK) {
+        return st;
+    }
+    CUDA_TRY(h, cudaEventRecord(h->ev_join, h->gstream));
+    CUDA_TRY(h, cudaStreamWaitEvent(h->stream, h->ev_join, 0));
     {
         Phase ph(h, SPHGPU_PHASE_SPH_EVAL);
-        if (h->ph.precision == SPHGPU_PRECISION_MIXED) {
-            launchPairSumMixed(h->s, h->grid, h->ph, h->d_mats, h->d_lut_sph_f, h->stream);
-        } else {
-            launchPairSum64(h->s, h->grid, h->ph, h->d_mats, h->d_lut_sph, h->stream);
-        }
+        launchAddGravity(h->s, h->stream);
         h->launches += 1;
     }
     return SPHGPU_OK;
@@ -461,6 +489,19 @@ sphgpu_status sphgpu_create(const sphgpu_config* config, sphgpu_handle** out) {
     (void)anyRheology;
 
     cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) {
+        int leastPriority = 0, greatestPriority = 0;
+        e = cudaDeviceGetStreamPriorityRange(&leastPriority, &greatestPriority);
+        if (e == cudaSuccess) {
+            e = cudaStreamCreateWithPriority(&h->gstream, cudaStreamNonBlocking, greatestPriority);
+        }
+    }
+    if (e == cudaSuccess) {
+        e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) {
+        e = cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming);
+    }
     DState& s = h->s;
     s.n = n;
     const size_t nn = std::max<uint32_t>(n, 1);
@@ -599,6 +640,16 @@ sphgpu_status sphgpu_destroy(sphgpu_handle* h) {
     adjointFree(h->adjoint);
     if (h->h_pinned) {
         cudaFreeHost(h->h_pinned);
+    }
+    if (h->gstream) {
+        cudaStreamSynchronize(h->gstream);
+        cudaStreamDestroy(h->gstream);
+    }
+    if (h->ev_fork) {
+        cudaEventDestroy(h->ev_fork);
+    }
+    if (h->ev_join) {
+        cudaEventDestroy(h->ev_join);
     }
     if (h->stream) {
         cudaStreamDestroy(h->stream);

@@ -511,6 +511,23 @@ void launchTotals(const DState& s, double* partial, double* out, cudaStream_t st
     totalsFinish<<<1, 32, 0, st>>>(partial, out);
 }
 
+// dv = a_gravity + a_sph: the sum GravitySolver::loop forms (gravity first in the accumulator), for pair
+// loops that ran concurrently with the walk
+__global__ void addGravityKernel(DState s) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= s.n) {
+        return;
+    }
+    const dbl4 a = s.agrav[i], d = s.dv[i];
+    s.dv[i] = mkd4(a.x + d.x, a.y + d.y, a.z + d.z, d.w);
+}
+
+void launchAddGravity(const DState& s, cudaStream_t st) {
+    if (s.n) {
+        addGravityKernel<<<ceilDiv(s.n, 256), 256, 0, st>>>(s);
+    }
+}
+
 void launchCheckFinite(const DState& s, unsigned long long* firstBad, cudaStream_t st) {
     if (s.n) {
         checkFiniteKernel<<<min(ceilDiv(s.n, 256), 152 * 8), 256, 0, st>>>(s, firstBad);

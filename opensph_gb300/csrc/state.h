@@ -215,6 +215,7 @@ void launchLeapFrogKick(const DState& s, const Physics& ph, const MaterialD* mat
 void launchCourantFinish(double* dt, double* dt_min, double max_dt, cudaStream_t st);
 void launchTotals(const DState& s, double* partial, double* out, cudaStream_t st);
 void launchCheckFinite(const DState& s, unsigned long long* first_bad, cudaStream_t st);
+void launchAddGravity(const DState& s, cudaStream_t st);
 void launchPairSumMixed(const DState& s, const Grid& g, const Physics& ph, const MaterialD* mats,
     const float* lut_grad_f, cudaStream_t st);
 

@@ -174,6 +174,7 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 12) walkMixedKernel(const uint
     // interaction counters of the warp (approximated nodes, particle lists, particle-node and particle-particle
     // evaluations), kept in shared memory to leave the registers to the walk
     __shared__ unsigned long long countSh[WALK_THREADS_F / 32][4];
+    __shared__ WalkFrame frameSh[WALK_THREADS_F / 32];
     unsigned long long* wc = countSh[wib];
     if (lane < 4) {
         wc[lane] = 0;
@@ -238,8 +239,11 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 12) walkMixedKernel(const uint
             const int par = path[k - 1];
             const int pl = geom[par].left;
             const int sib = pl == ev ? geom[par].right : pl;
-            WalkFrame fr;
-            setFrame(fr, nf, ev, k == depth, lh, ll);
+            // the frame is the same for the whole warp: kept in shared memory, not in 8 registers per lane
+            WalkFrame& fr = frameSh[wib];
+            if (lane == 0) {
+                setFrame(fr, nf, ev, k == depth, lh, ll);
+            }
             if (lane == 0) {
                 cur[ncur] = sib;
             }
@@ -277,6 +281,8 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 12) walkMixedKernel(const uint
                 ncur += 2 * nOpen;
                 nnxt += nKeep;
                 __syncwarp();
+                // plain FP32 partial sums over this batch's interactions, added to the compensated totals once
+                float bx = 0.f, by = 0.f, bz = 0.f;
                 // particle lists: every particle of the listed leaves, split over the lane groups
                 unsigned mp = mPart;
                 while (mp) {
@@ -293,7 +299,6 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 12) walkMixedKernel(const uint
                         wc[3] += uint64_t(cnt) * (range.y - range.x);
                     }
                     if (inGroup) {
-                        float sx = 0.f, sy = 0.f, sz = 0.f;
 #pragma unroll 2
                         for (uint32_t t = range.x + grp; t < range.y; t += g) {
                             const float4 dj = pf[t];
@@ -301,13 +306,10 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 12) walkMixedKernel(const uint
                             float gx, gy, gz;
                             gravGradF((Dx + dj.x) - di.x, (Dy + dj.y) - di.y, (Dz + dj.z) - di.z, 0.5f * (dj.w + di.w),
                                 lut, kernelRadius, gx, gy, gz);
-                            sx += mj * gx;
-                            sy += mj * gy;
-                            sz += mj * gz;
+                            bx += mj * gx;
+                            by += mj * gy;
+                            bz += mj * gz;
                         }
-                        ax.add(sx);
-                        ay.add(sy);
-                        az.add(sz);
                     }
                 }
                 // multipole expansions: rounds of g nodes, node q of a round to lane group q
@@ -334,12 +336,13 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 12) walkMixedKernel(const uint
                         const float Dx = (c0.x - lh[0]) + (c1.x - ll[0]);
                         const float Dy = (c0.y - lh[1]) + (c1.y - ll[1]);
                         const float Dz = (c0.z - lh[2]) + (c1.z - ll[2]);
-                        float sx = 0.f, sy = 0.f, sz = 0.f;
-                        evalMultipoleF(di.x - Dx, di.y - Dy, di.z - Dz, c0.w, c2, c3, c4, c5, order, sx, sy, sz);
-                        ax.add(sx);
-                        ay.add(sy);
-                        az.add(sz);
+                        evalMultipoleF(di.x - Dx, di.y - Dy, di.z - Dz, c0.w, c2, c3, c4, c5, order, bx, by, bz);
                     }
+                }
+                if (inGroup) {
+                    ax.add(bx);
+                    ay.add(by);
+                    az.add(bz);
                 }
             }
             int32_t* t = cur;

@@ -874,6 +874,7 @@ sphgpu_status sphgpu_gravity_eval_points(sphgpu_handle* h, const double* points,
         e = cudaMemcpyAsync(dp, points, npoints * sizeof(dbl4), cudaMemcpyHostToDevice, h->stream);
     }
     if (e == cudaSuccess) {
+        treeEnsureFp64Moments(h->s, h->tree, h->ph, h->stream);
         launchGravityPoints(h->s, h->tree, h->ph, h->d_lut_grav, dp, da, uint32_t(npoints), h->stream);
         e = cudaMemcpyAsync(acc, da, npoints * sizeof(dbl4), cudaMemcpyDeviceToHost, h->stream);
     }

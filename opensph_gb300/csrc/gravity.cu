@@ -1091,25 +1091,21 @@ __global__ void chunkSwapKernel(uint32_t* idx, const uint32_t* __restrict__ posB
     }
 }
 
-// BarnesHut::buildLeaf (core/gravity/BarnesHut.cpp:376-437), one thread per leaf
-__device__ void buildLeaf(const dbl4* __restrict__ r, const double* __restrict__ m, double G,
-    const uint32_t* __restrict__ idx, double thetaInv, BhNodeGeom& g, BhNodeMoments& mo) {
+// BarnesHut::buildLeaf (core/gravity/BarnesHut.cpp:376-437), geometry part: mass, centre of mass and opening
+// radius of the leaf in FP64, summed in the leaf's particle order (the walk's decisions depend on these bits).
+// Returns false for a single-particle leaf (no moments beyond the mass).
+__device__ bool buildLeafGeom(const dbl4* __restrict__ r, const double* __restrict__ m, double G,
+    const uint32_t* __restrict__ idx, double thetaInv, BhNodeGeom& g, double& m0) {
     const uint32_t cnt = g.to - g.from;
-    for (int k = 0; k < 6; ++k) {
-        mo.q2[k] = 0.;
-    }
-    for (int k = 0; k < 10; ++k) {
-        mo.q3[k] = 0.;
-    }
     if (cnt == 1) {
         const uint32_t i = idx[g.from];
         const dbl4 p = r[i];
         g.com[0] = p.x;
         g.com[1] = p.y;
         g.com[2] = p.z;
-        mo.m0 = G * m[i];
+        m0 = G * m[i];
         g.r_open = 0.;
-        return;
+        return false;
     }
     double cx = 0., cy = 0., cz = 0., mLeaf = 0.;
     for (uint32_t k = g.from; k < g.to; ++k) {
@@ -1130,12 +1126,45 @@ __device__ void buildLeaf(const dbl4* __restrict__ r, const double* __restrict__
     const double rmx = fmax(cx - g.lo[0], g.hi[0] - cx), rmy = fmax(cy - g.lo[1], g.hi[1] - cy),
                  rmz = fmax(cz - g.lo[2], g.hi[2] - cz);
     g.r_open = 2. / sqrt(3.) * thetaInv * sqrt(rmx * rmx + rmy * rmy + rmz * rmz);
-    double M2[6] = { 0, 0, 0, 0, 0, 0 }, M3[10] = { 0, 0, 0, 0, 0, 0, 0, 0, 0, 0 };
+    m0 = mLeaf;
+    return true;
+}
+
+// reduced (traceless) multipoles from the raw second and third moments (computeReducedMultipole,
+// core/gravity/Moments.h:90-111)
+template <typename T>
+__device__ __forceinline__ void reduceMoments(const T M2[6], const T M3[10], T q2[6], T q3[10]) {
+    const T tr = M2[0] + M2[3] + M2[5];
+    for (int a = 0; a < 3; ++a) {
+        for (int b = a; b < 3; ++b) {
+            q2[i2(a, b)] = M2[i2(a, b)] + (a == b ? tr : T(0)) * T(-1. / 3.);
+        }
+    }
+    T T1[3];
+    for (int k = 0; k < 3; ++k) {
+        T1[k] = M3[i3(0, 0, k)] + M3[i3(1, 1, k)] + M3[i3(2, 2, k)];
+    }
+    for (int a = 0; a < 3; ++a) {
+        for (int b = a; b < 3; ++b) {
+            for (int c = b; c < 3; ++c) {
+                const T perm = (a == b ? T1[c] : T(0)) + (b == c ? T1[a] : T(0)) + (c == a ? T1[b] : T(0));
+                q3[i3(a, b, c)] = M3[i3(a, b, c)] + perm * T(-1. / 5.);
+            }
+        }
+    }
+}
+
+// moments of a leaf about its centre of mass: T = double for the FP64 walk, float for the mixed walk (the
+// separations are formed in FP64 and rounded once)
+template <typename T>
+__device__ void leafMoments(const dbl4* __restrict__ r, const double* __restrict__ m, double G,
+    const uint32_t* __restrict__ idx, const BhNodeGeom& g, T q2[6], T q3[10]) {
+    T M2[6] = { 0, 0, 0, 0, 0, 0 }, M3[10] = { 0, 0, 0, 0, 0, 0, 0, 0, 0, 0 };
     for (uint32_t k = g.from; k < g.to; ++k) {
         const uint32_t i = idx[k];
         const dbl4 p = r[i];
-        const double mi = G * m[i];
-        const double d[3] = { p.x - cx, p.y - cy, p.z - cz };
+        const T mi = T(G * m[i]);
+        const T d[3] = { T(p.x - g.com[0]), T(p.y - g.com[1]), T(p.z - g.com[2]) };
         for (int a = 0; a < 3; ++a) {
             for (int b = a; b < 3; ++b) {
                 M2[i2(a, b)] += (d[a] * d[b]) * mi;
@@ -1145,59 +1174,12 @@ __device__ void buildLeaf(const dbl4* __restrict__ r, const double* __restrict__
             }
         }
     }
-    const double tr = M2[0] + M2[3] + M2[5];
-    for (int a = 0; a < 3; ++a) {
-        for (int b = a; b < 3; ++b) {
-            mo.q2[i2(a, b)] = M2[i2(a, b)] + (a == b ? tr : 0.) * (-1. / 3.);
-        }
-    }
-    double T1[3];
-    for (int k = 0; k < 3; ++k) {
-        T1[k] = M3[i3(0, 0, k)] + M3[i3(1, 1, k)] + M3[i3(2, 2, k)];
-    }
-    for (int a = 0; a < 3; ++a) {
-        for (int b = a; b < 3; ++b) {
-            for (int c = b; c < 3; ++c) {
-                const double perm = (a == b ? T1[c] : 0.) + (b == c ? T1[a] : 0.) + (c == a ? T1[b] : 0.);
-                mo.q3[i3(a, b, c)] = M3[i3(a, b, c)] + perm * (-1. / 5.);
-            }
-        }
-    }
-    mo.m0 = mLeaf;
+    reduceMoments(M2, M3, q2, q3);
 }
 
-// parallelAxisTheorem for orders 2 and 3 (core/gravity/Moments.h:182-295), accumulated into (q2, q3)
-__device__ void shiftAdd(const BhNodeMoments& c, const double d[3], double q2[6], double q3[10]) {
-    const double Q = c.m0;
-    const double dd = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-    double Qd[3];
-    for (int k = 0; k < 3; ++k) {
-        Qd[k] = c.q2[i2(k, 0)] * d[0] + c.q2[i2(k, 1)] * d[1] + c.q2[i2(k, 2)] * d[2];
-    }
-    for (int a = 0; a < 3; ++a) {
-        for (int b = a; b < 3; ++b) {
-            const double f2 = d[a] * d[b] + (a == b ? dd : 0.) * (-1. / 3.);
-            q2[i2(a, b)] += c.q2[i2(a, b)] + f2 * Q;
-            for (int cc = b; cc < 3; ++cc) {
-                const double perm = (a == b ? d[cc] : 0.) + (b == cc ? d[a] : 0.) + (cc == a ? d[b] : 0.);
-                const double f3 = d[a] * d[b] * d[cc] + perm * dd * (-1. / 5.);
-                const double pq = c.q2[i2(a, b)] * d[cc] + c.q2[i2(b, cc)] * d[a] + c.q2[i2(cc, a)] * d[b];
-                const double t2 = (a == b ? Qd[cc] : 0.) + (a == cc ? Qd[b] : 0.) + (b == cc ? Qd[a] : 0.);
-                q3[i3(a, b, cc)] += c.q3[i3(a, b, cc)] + f3 * Q + pq + (-2. / 5.) * t2;
-            }
-        }
-    }
-}
-
-// BarnesHut::buildInner (core/gravity/BarnesHut.cpp:439-489): box, centre of mass, opening radius and the
-// children's moments moved to the new centre (left child first)
-__device__ void buildInner(double thetaInv, BhNodeGeom& g, const BhNodeGeom& gl, const BhNodeGeom& gr,
-    const BhNodeMoments& ml, const BhNodeMoments& mr, BhNodeMoments& mo) {
-    for (int d = 0; d < 3; ++d) {
-        g.lo[d] = fmin(gl.lo[d], gr.lo[d]);
-        g.hi[d] = fmax(gl.hi[d], gr.hi[d]);
-    }
-    const double mt = ml.m0 + mr.m0;
+// BarnesHut::buildLeaf with FP64 moments, one thread per leaf
+__device__ void buildLeaf(const dbl4* __restrict__ r, const double* __restrict__ m, double G,
+    const uint32_t* __restrict__ idx, double thetaInv, BhNodeGeom& g, BhNodeMoments& mo) {
     for (int k = 0; k < 6; ++k) {
         mo.q2[k] = 0.;
     }
@@ -1205,24 +1187,78 @@ __device__ void buildInner(double thetaInv, BhNodeGeom& g, const BhNodeGeom& gl,
         mo.q3[k] = 0.;
     }
     mo.pad = 0.;
+    if (buildLeafGeom(r, m, G, idx, thetaInv, g, mo.m0)) {
+        leafMoments(r, m, G, idx, g, mo.q2, mo.q3);
+    }
+}
+
+// parallelAxisTheorem for orders 2 and 3 (core/gravity/Moments.h:182-295): the child's moments (mass Q,
+// reduced cq2, cq3) moved by d = child centre - new centre, accumulated into (q2, q3)
+template <typename T>
+__device__ void shiftAdd(T Q, const T cq2[6], const T cq3[10], const T d[3], T q2[6], T q3[10]) {
+    const T dd = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    T Qd[3];
+    for (int k = 0; k < 3; ++k) {
+        Qd[k] = cq2[i2(k, 0)] * d[0] + cq2[i2(k, 1)] * d[1] + cq2[i2(k, 2)] * d[2];
+    }
+    for (int a = 0; a < 3; ++a) {
+        for (int b = a; b < 3; ++b) {
+            const T f2 = d[a] * d[b] + (a == b ? dd : T(0)) * T(-1. / 3.);
+            q2[i2(a, b)] += cq2[i2(a, b)] + f2 * Q;
+            for (int cc = b; cc < 3; ++cc) {
+                const T perm = (a == b ? d[cc] : T(0)) + (b == cc ? d[a] : T(0)) + (cc == a ? d[b] : T(0));
+                const T f3 = d[a] * d[b] * d[cc] + perm * dd * T(-1. / 5.);
+                const T pq = cq2[i2(a, b)] * d[cc] + cq2[i2(b, cc)] * d[a] + cq2[i2(cc, a)] * d[b];
+                const T t2 = (a == b ? Qd[cc] : T(0)) + (a == cc ? Qd[b] : T(0)) + (b == cc ? Qd[a] : T(0));
+                q3[i3(a, b, cc)] += cq3[i3(a, b, cc)] + f3 * Q + pq + T(-2. / 5.) * t2;
+            }
+        }
+    }
+}
+
+// BarnesHut::buildInner (core/gravity/BarnesHut.cpp:439-489), geometry part: box, mass, centre of mass and
+// opening radius from the two children (FP64). Returns false for a massless node.
+__device__ bool buildInnerGeom(double thetaInv, BhNodeGeom& g, const BhNodeGeom& gl, const BhNodeGeom& gr, double ml,
+    double mr, double& m0) {
+    for (int d = 0; d < 3; ++d) {
+        g.lo[d] = fmin(gl.lo[d], gr.lo[d]);
+        g.hi[d] = fmax(gl.hi[d], gr.hi[d]);
+    }
+    const double mt = ml + mr;
     if (mt == 0.) {
-        mo.m0 = 0.;
+        m0 = 0.;
         g.com[0] = g.com[1] = g.com[2] = 0.;
         g.r_open = 0.;
-        return;
+        return false;
     }
     for (int d = 0; d < 3; ++d) {
-        g.com[d] = (ml.m0 * gl.com[d] + mr.m0 * gr.com[d]) / mt;
+        g.com[d] = (ml * gl.com[d] + mr * gr.com[d]) / mt;
     }
     const double rmx = fmax(g.com[0] - g.lo[0], g.hi[0] - g.com[0]);
     const double rmy = fmax(g.com[1] - g.lo[1], g.hi[1] - g.com[1]);
     const double rmz = fmax(g.com[2] - g.lo[2], g.hi[2] - g.com[2]);
     g.r_open = 2. / sqrt(3.) * thetaInv * sqrt(rmx * rmx + rmy * rmy + rmz * rmz);
-    mo.m0 = mt;
+    m0 = mt;
+    return true;
+}
+
+// BarnesHut::buildInner with FP64 moments (left child first)
+__device__ void buildInner(double thetaInv, BhNodeGeom& g, const BhNodeGeom& gl, const BhNodeGeom& gr,
+    const BhNodeMoments& ml, const BhNodeMoments& mr, BhNodeMoments& mo) {
+    for (int k = 0; k < 6; ++k) {
+        mo.q2[k] = 0.;
+    }
+    for (int k = 0; k < 10; ++k) {
+        mo.q3[k] = 0.;
+    }
+    mo.pad = 0.;
+    if (!buildInnerGeom(thetaInv, g, gl, gr, ml.m0, mr.m0, mo.m0)) {
+        return;
+    }
     const double dl[3] = { gl.com[0] - g.com[0], gl.com[1] - g.com[1], gl.com[2] - g.com[2] };
-    shiftAdd(ml, dl, mo.q2, mo.q3);
+    shiftAdd(ml.m0, ml.q2, ml.q3, dl, mo.q2, mo.q3);
     const double dr[3] = { gr.com[0] - g.com[0], gr.com[1] - g.com[1], gr.com[2] - g.com[2] };
-    shiftAdd(mr, dr, mo.q2, mo.q3);
+    shiftAdd(mr.m0, mr.q2, mr.q3, dr, mo.q2, mo.q3);
 }
 
 // loads that bypass L1 (the sibling subtree was written by another SM during this launch)
@@ -1238,26 +1274,58 @@ __device__ __forceinline__ T loadCG(const T* p) {
     return out;
 }
 
+// FP32 reduced moments of a node in the mixed walk's node record (groups NF_MOM .. NF_MOM + 3)
+__device__ __forceinline__ void writeMomentsF(float* nodef, int node, const float q2[6], const float q3[10]) {
+    float4* o = reinterpret_cast<float4*>(nodef) + size_t(node) * NODEF4 + NF_MOM;
+    o[0] = make_float4(q2[0], q2[1], q2[2], q2[3]);
+    o[1] = make_float4(q2[4], q2[5], q3[0], q3[1]);
+    o[2] = make_float4(q3[2], q3[3], q3[4], q3[5]);
+    o[3] = make_float4(q3[6], q3[7], q3[8], q3[9]);
+}
+
+__device__ __forceinline__ void readMomentsF(const float* nodef, int node, float q2[6], float q3[10]) {
+    const float4* o = reinterpret_cast<const float4*>(nodef) + size_t(node) * NODEF4 + NF_MOM;
+    const float4 a = __ldcg(o), b = __ldcg(o + 1), c = __ldcg(o + 2), d = __ldcg(o + 3);
+    q2[0] = a.x, q2[1] = a.y, q2[2] = a.z, q2[3] = a.w, q2[4] = b.x, q2[5] = b.y;
+    q3[0] = b.z, q3[1] = b.w, q3[2] = c.x, q3[3] = c.y, q3[4] = c.z, q3[5] = c.w;
+    q3[6] = d.x, q3[7] = d.y, q3[8] = d.z, q3[9] = d.w;
+}
+
 // All moments in one launch, bottom-up: one thread per leaf forms the leaf's moments, then climbs; at each
 // inner node the thread that arrives second (atomic counter per node) forms the node from its two finished
 // children, the first one stops. Nothing waits, so the launch always completes; every node gets the same
-// values in any arrival order (children combined left then right).
+// values in any arrival order (children combined left then right). Mixed: the geometry (mass, centre of
+// mass, opening radius, box) is formed in FP64 exactly as for the FP64 walk, so both walks take the same
+// decisions, while the reduced moments, which the mixed walk evaluates in FP32, are formed in FP32 directly
+// into its node records.
+template <bool Mixed>
 __global__ void momentsUpKernel(const dbl4* __restrict__ r, const double* __restrict__ m, double G,
-    const uint32_t* __restrict__ idx, double thetaInv, BhNodeGeom* geom, BhNodeMoments* mom,
+    const uint32_t* __restrict__ idx, double thetaInv, BhNodeGeom* geom, BhNodeMoments* mom, float* nodef,
     const uint32_t* __restrict__ leaves, uint32_t nLeaves, uint32_t* visits) {
     const uint32_t li = blockIdx.x * blockDim.x + threadIdx.x;
     if (li >= nLeaves) {
         return;
     }
-    int node = int(leaves[li]);
+    const int node = int(leaves[li]);
+    int parent;
     {
         BhNodeGeom g = geom[node];
-        BhNodeMoments mo;
-        buildLeaf(r, m, G, idx, thetaInv, g, mo);
+        if (Mixed) {
+            double m0;
+            float q2[6] = { 0, 0, 0, 0, 0, 0 }, q3[10] = { 0, 0, 0, 0, 0, 0, 0, 0, 0, 0 };
+            if (buildLeafGeom(r, m, G, idx, thetaInv, g, m0)) {
+                leafMoments(r, m, G, idx, g, q2, q3);
+            }
+            mom[node].m0 = m0;
+            writeMomentsF(nodef, node, q2, q3);
+        } else {
+            BhNodeMoments mo;
+            buildLeaf(r, m, G, idx, thetaInv, g, mo);
+            mom[node] = mo;
+        }
         geom[node] = g;
-        mom[node] = mo;
+        parent = g.parent;
     }
-    int parent = loadCG(&geom[node]).parent;
     while (parent >= 0) {
         __threadfence();
         if (atomicAdd(&visits[parent], 1u) == 0) {
@@ -1267,12 +1335,31 @@ __global__ void momentsUpKernel(const dbl4* __restrict__ r, const double* __rest
         BhNodeGeom g = loadCG(&geom[parent]);
         const BhNodeGeom gl = loadCG(&geom[g.left]);
         const BhNodeGeom gr = loadCG(&geom[g.right]);
-        const BhNodeMoments ml = loadCG(&mom[g.left]);
-        const BhNodeMoments mr = loadCG(&mom[g.right]);
-        BhNodeMoments mo;
-        buildInner(thetaInv, g, gl, gr, ml, mr, mo);
+        if (Mixed) {
+            const double ml = __ldcg(&mom[g.left].m0), mr = __ldcg(&mom[g.right].m0);
+            double m0;
+            float q2[6] = { 0, 0, 0, 0, 0, 0 }, q3[10] = { 0, 0, 0, 0, 0, 0, 0, 0, 0, 0 };
+            if (buildInnerGeom(thetaInv, g, gl, gr, ml, mr, m0)) {
+                float cq2[6], cq3[10];
+                readMomentsF(nodef, g.left, cq2, cq3);
+                const float dl[3] = { float(gl.com[0] - g.com[0]), float(gl.com[1] - g.com[1]),
+                    float(gl.com[2] - g.com[2]) };
+                shiftAdd(float(ml), cq2, cq3, dl, q2, q3);
+                readMomentsF(nodef, g.right, cq2, cq3);
+                const float dr[3] = { float(gr.com[0] - g.com[0]), float(gr.com[1] - g.com[1]),
+                    float(gr.com[2] - g.com[2]) };
+                shiftAdd(float(mr), cq2, cq3, dr, q2, q3);
+            }
+            mom[parent].m0 = m0;
+            writeMomentsF(nodef, parent, q2, q3);
+        } else {
+            const BhNodeMoments ml = loadCG(&mom[g.left]);
+            const BhNodeMoments mr = loadCG(&mom[g.right]);
+            BhNodeMoments mo;
+            buildInner(thetaInv, g, gl, gr, ml, mr, mo);
+            mom[parent] = mo;
+        }
         geom[parent] = g;
-        mom[parent] = mo;
         parent = g.parent;
     }
 }
@@ -1576,6 +1663,31 @@ void treeFree(Tree& t) {
     t = Tree();
 }
 
+namespace {
+
+void launchMoments(const DState& s, Tree& t, const Physics& ph, bool mixed, cudaStream_t st) {
+    cudaMemsetAsync(t.visits, 0, size_t(t.node_count) * sizeof(uint32_t), st);
+    if (t.leaf_count == 0) {
+        return;
+    }
+    if (mixed) {
+        momentsUpKernel<true><<<ceilDiv(t.leaf_count, 128), 128, 0, st>>>(s.r, s.m, ph.G, t.idx, ph.theta_inv, t.geom,
+            t.mom, t.nodef, t.leaves, t.leaf_count, t.visits);
+    } else {
+        momentsUpKernel<false><<<ceilDiv(t.leaf_count, 128), 128, 0, st>>>(s.r, s.m, ph.G, t.idx, ph.theta_inv,
+            t.geom, t.mom, t.nodef, t.leaves, t.leaf_count, t.visits);
+    }
+}
+
+} // namespace
+
+void treeEnsureFp64Moments(const DState& s, Tree& t, const Physics& ph, cudaStream_t st) {
+    if (t.built && t.mixed_moments) {
+        launchMoments(s, t, ph, false, st);
+        t.mixed_moments = false;
+    }
+}
+
 cudaError_t treeBuild(const DState& s, Tree& t, const Physics& ph, uint32_t* devError, cudaStream_t st) {
     const uint32_t n = s.n;
     t.built = false;
@@ -1660,12 +1772,9 @@ cudaError_t treeBuild(const DState& s, Tree& t, const Physics& ph, uint32_t* dev
         }
     }
     // moments, bottom-up in one launch
-    cudaMemsetAsync(t.visits, 0, size_t(t.node_count) * sizeof(uint32_t), st);
-    if (t.leaf_count > 0) {
-        momentsUpKernel<<<ceilDiv(t.leaf_count, 128), 128, 0, st>>>(s.r, s.m, ph.G, t.idx, ph.theta_inv, t.geom,
-            t.mom, t.leaves, t.leaf_count, t.visits);
-        t.launches++;
-    }
+    t.mixed_moments = ph.precision == SPHGPU_PRECISION_MIXED;
+    launchMoments(s, t, ph, t.mixed_moments, st);
+    t.launches++;
     t.built = true;
     return cudaGetLastError();
 }

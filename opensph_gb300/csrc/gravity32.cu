@@ -26,7 +26,7 @@ __device__ __forceinline__ void splitF(double x, float& hi, float& lo) {
 
 __global__ void prepareMixedKernel(const dbl4* __restrict__ r, const double* __restrict__ m, double G,
     const uint32_t* __restrict__ idx, const BhNodeGeom* __restrict__ geom, const BhNodeMoments* __restrict__ mom,
-    uint32_t nodeCount, float* __restrict__ nodef, float4* __restrict__ pf, float* __restrict__ mf) {
+    uint32_t nodeCount, float* __restrict__ nodef, float4* __restrict__ pf, float* __restrict__ mf, bool moments) {
     const uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= nodeCount) {
         return;
@@ -44,15 +44,18 @@ __global__ void prepareMixedKernel(const dbl4* __restrict__ r, const double* __r
     }
     o[NF_COM_HI] = make_float4(ch[0], ch[1], ch[2], float(mo.m0));
     o[NF_COM_LO] = make_float4(cl[0], cl[1], cl[2], g.left < 0 ? -ro : ro);
-    float q[16];
-    for (int k = 0; k < 6; ++k) {
-        q[k] = float(mo.q2[k]);
-    }
-    for (int k = 0; k < 10; ++k) {
-        q[6 + k] = float(mo.q3[k]);
-    }
-    for (int k = 0; k < 4; ++k) {
-        o[NF_MOM + k] = make_float4(q[4 * k], q[4 * k + 1], q[4 * k + 2], q[4 * k + 3]);
+    if (moments) {
+        // the reduced moments, rounded from FP64 (a tree built with FP32 moments already holds them)
+        float q[16];
+        for (int k = 0; k < 6; ++k) {
+            q[k] = float(mo.q2[k]);
+        }
+        for (int k = 0; k < 10; ++k) {
+            q[6 + k] = float(mo.q3[k]);
+        }
+        for (int k = 0; k < 4; ++k) {
+            o[NF_MOM + k] = make_float4(q[4 * k], q[4 * k + 1], q[4 * k + 2], q[4 * k + 3]);
+        }
     }
     float bh[2][3], bl[2][3];
     for (int d = 0; d < 3; ++d) {
@@ -412,7 +415,7 @@ void launchPrepareWalk(const DState& s, Tree& t, const Physics& ph, cudaStream_t
         return;
     }
     prepareMixedKernel<<<ceilDiv(t.node_count, 128), 128, 0, st>>>(s.r, s.m, ph.G, t.idx, t.geom, t.mom,
-        t.node_count, t.nodef, t.pf, t.mf);
+        t.node_count, t.nodef, t.pf, t.mf, !t.mixed_moments);
 }
 
 void launchGravityWalkMixed(const DState& s, Tree& t, const Physics& ph, const float* lutF, uint32_t* devError,

@@ -190,6 +190,7 @@ struct Tree {
     uint32_t leaf_count = 0;
     uint32_t launches = 0;            // kernels launched by the last build
     bool built = false;
+    bool mixed_moments = false;       // reduced moments only in FP32 (node records), not in mom
 };
 
 // ---- launchers (grid.cu) ----
@@ -223,6 +224,8 @@ void launchPairSumMixed(const DState& s, const Grid& g, const Physics& ph, const
 cudaError_t treeAllocate(Tree& t, uint32_t n, uint32_t leaf_size);
 void treeFree(Tree& t);
 cudaError_t treeBuild(const DState& s, Tree& t, const Physics& ph, uint32_t* dev_error, cudaStream_t st);
+// forms the FP64 moments of a tree built with FP32 moments (for the FP64 point evaluation)
+void treeEnsureFp64Moments(const DState& s, Tree& t, const Physics& ph, cudaStream_t st);
 void launchGravityWalk(const DState& s, Tree& t, const Physics& ph, const double* lut_grad, uint32_t* dev_error,
     cudaStream_t st);
 void launchPrepareWalk(const DState& s, Tree& t, const Physics& ph, cudaStream_t st);

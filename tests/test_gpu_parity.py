@@ -66,11 +66,12 @@ def test_pair_set_lattice_ties():
     np.testing.assert_array_equal(pj, oj)
 
 
-def grav_solver(r, m, theta, leaf_size=25, order=3, kernel=abi.GRAVITY_KERNEL_SPH_KERNEL):
+def grav_solver(r, m, theta, leaf_size=25, order=3, kernel=abi.GRAVITY_KERNEL_SPH_KERNEL,
+                precision=abi.PRECISION_FP64):
     n = len(m)
     cfg, keep = abi.make_config(n, [abi.ideal_gas()], forces=abi.FORCE_PRESSURE | abi.FORCE_SELF_GRAVITY,
                                 gravity_constant=1.0, gravity_opening_angle=theta, gravity_leaf_size=leaf_size,
-                                gravity_multipole_order=order, gravity_kernel=kernel)
+                                gravity_multipole_order=order, gravity_kernel=kernel, precision=precision)
     g = GpuSolver(cfg, keep)
     g.set_quantity(abi.Q_POSITION, 0, r)
     g.set_quantity(abi.Q_MASS, 0, m)
@@ -121,6 +122,26 @@ def test_barnes_hut_six_particle_known_answer():
         np.testing.assert_allclose(a, o, rtol=1e-13, atol=1e-17)
         d2 = np.sum((a - expected) ** 2)
         assert d2 <= eps * eps * (1.0 + max(np.sum(a ** 2), np.sum(expected ** 2)))
+
+
+def test_point_queries_after_mixed_walk_use_fp64_moments():
+    # the mixed walk builds its moments in FP32; a later point query (evalAcceleration) forms the FP64 moments
+    # of the same tree first, so it equals the FP64 handle's answer bit for bit
+    rng = np.random.default_rng(3)
+    n = 20000
+    r = np.zeros((n, 4))
+    r[:, :3] = rng.standard_normal((n, 3))
+    r[:, 3] = 1e-2
+    m = rng.random(n) + 0.5
+    pts = np.zeros((64, 4))
+    pts[:, :3] = 3.0 * rng.standard_normal((64, 3))
+    pts[:, 3] = 1e-2
+    out = {}
+    for prec in (abi.PRECISION_FP64, abi.PRECISION_MIXED):
+        with grav_solver(r.ravel(), m, 0.5, precision=prec) as g:
+            g.gravity()
+            out[prec] = g.gravity_points(pts.ravel())
+    np.testing.assert_array_equal(out[abi.PRECISION_MIXED], out[abi.PRECISION_FP64])
 
 
 @pytest.mark.parametrize("name", ["sphere_n1000", "impact_n1200", "gas_n1500"])

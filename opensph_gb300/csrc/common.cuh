@@ -80,6 +80,16 @@ __device__ __forceinline__ double doubleUnflip(unsigned long long u) {
     return __longlong_as_double(static_cast<long long>(u));
 }
 
+// Order key of a double that is not NaN: x < y <=> orderKey(x) < orderKey(y) and x == y <=> equal keys
+// (-0 and +0 map to one key). Comparisons and minima on keys run on the integer pipe.
+__device__ __forceinline__ unsigned long long orderKey(double f) {
+    unsigned long long u = static_cast<unsigned long long>(__double_as_longlong(f));
+    if (u == 0x8000000000000000ull) {
+        u = 0ull;
+    }
+    return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
+}
+
 inline int ceilDiv(long long a, long long b) {
     return int((a + b - 1) / b);
 }

@@ -34,8 +34,11 @@ constexpr int MAX_PATH = 512;
 struct PosView {
     const dbl4* r;
     __device__ __forceinline__ double val(uint32_t i, int dim) const {
-        const dbl4 p = r[i];
-        return dim == 0 ? p.x : (dim == 1 ? p.y : p.z);
+        return __ldg(reinterpret_cast<const double*>(r) + 4 * size_t(i) + dim);
+    }
+    // orderKey of the coordinate: the build compares keys (integer pipe) instead of doubles (slow FP64 pipe)
+    __device__ __forceinline__ unsigned long long key(uint32_t i, int dim) const {
+        return orderKey(val(i, dim));
     }
 };
 
@@ -315,10 +318,11 @@ __device__ __forceinline__ bool blockAny(bool v, int* sh) {
     return r != 0;
 }
 
-// (value, position) lexicographic minimum across the block; dir = +1 for min, -1 for max
-__device__ void blockArgExtreme(double& val, uint32_t& pos, bool isMax, double* shv, uint32_t* shp) {
+// (key, position) lexicographic minimum (maximum) across the block, the first occurrence on ties
+__device__ void blockArgExtreme(unsigned long long& val, uint32_t& pos, bool isMax, unsigned long long* shv,
+    uint32_t* shp) {
     for (int off = 16; off > 0; off >>= 1) {
-        const double ov = __shfl_xor_sync(0xffffffffu, val, off);
+        const unsigned long long ov = __shfl_xor_sync(0xffffffffu, val, off);
         const uint32_t op = __shfl_xor_sync(0xffffffffu, pos, off);
         const bool better = isMax ? (ov > val || (ov == val && op < pos)) : (ov < val || (ov == val && op < pos));
         if (better) {
@@ -334,7 +338,7 @@ __device__ void blockArgExtreme(double& val, uint32_t& pos, bool isMax, double* 
     __syncthreads();
     if (threadIdx.x == 0) {
         for (int w = 1; w < BUILD_THREADS / 32; ++w) {
-            const double ov = shv[w];
+            const unsigned long long ov = shv[w];
             const uint32_t op = shp[w];
             const bool better =
                 isMax ? (ov > shv[0] || (ov == shv[0] && op < shp[0])) : (ov < shv[0] || (ov == shv[0] && op < shp[0]));
@@ -355,7 +359,7 @@ __global__ void __launch_bounds__(BUILD_THREADS) splitLevelKernel(PosView pv, ui
     uint32_t* leaves, uint32_t leafSize, uint32_t nodeCapacity, uint32_t segCapacity, uint32_t* devError,
     uint32_t minSize, uint32_t maxSize) {
     __shared__ uint32_t shScan[32];
-    __shared__ double shV[32];
+    __shared__ unsigned long long shV[32];
     __shared__ uint32_t shP[32];
     __shared__ int shAny[4];
     __shared__ uint32_t shNode[2];
@@ -401,11 +405,14 @@ __global__ void __launch_bounds__(BUILD_THREADS) splitLevelKernel(PosView pv, ui
         int splitIdx = argMax3(boxSize);
         // singularity of each dimension: all values equal to the last one
         bool diff[3] = { false, false, false };
-        for (uint32_t k = from + threadIdx.x; k < to; k += BUILD_THREADS) {
-            const uint32_t i = idx[k];
+        {
             const uint32_t il = idx[to - 1];
-            for (int d = 0; d < 3; ++d) {
-                diff[d] = diff[d] || (pv.val(i, d) != pv.val(il, d));
+            const unsigned long long last[3] = { pv.key(il, 0), pv.key(il, 1), pv.key(il, 2) };
+            for (uint32_t k = from + threadIdx.x; k < to; k += BUILD_THREADS) {
+                const uint32_t i = idx[k];
+                for (int d = 0; d < 3; ++d) {
+                    diff[d] = diff[d] || (pv.key(i, d) != last[d]);
+                }
             }
         }
         bool nonSingular[3];
@@ -435,14 +442,15 @@ __global__ void __launch_bounds__(BUILD_THREADS) splitLevelKernel(PosView pv, ui
         }
         if (sg.sliding <= 5 && !degenerated) {
             // ranks of the elements above (B) and below (S) the split position, left to right
+            const unsigned long long splitKey = orderKey(splitPosition);
             uint32_t baseB = 0, baseS = 0;
             for (uint32_t k0 = from; k0 < to; k0 += BUILD_THREADS) {
                 const uint32_t k = k0 + threadIdx.x;
                 bool isB = false, isS = false;
                 if (k < to) {
-                    const double x = pv.val(idx[k], splitIdx);
-                    isB = x > splitPosition;
-                    isS = x < splitPosition;
+                    const unsigned long long x = pv.key(idx[k], splitIdx);
+                    isB = x > splitKey;
+                    isS = x < splitKey;
                 }
                 uint32_t totB, totS;
                 const uint32_t rb = blockExclusiveScan(isB ? 1u : 0u, totB, shScan);
@@ -481,10 +489,10 @@ __global__ void __launch_bounds__(BUILD_THREADS) splitLevelKernel(PosView pv, ui
             if (n1 == from || n1 == to) {
                 // sliding midpoint: move the extreme element (first occurrence) to the empty side
                 const bool isMax = (n1 == to);
-                double val = isMax ? -DBL_MAX : DBL_MAX;
+                unsigned long long val = isMax ? 0ull : ~0ull;
                 uint32_t pos = 0xffffffffu;
                 for (uint32_t k = from + threadIdx.x; k < to; k += BUILD_THREADS) {
-                    const double x = pv.val(idx[k], splitIdx);
+                    const unsigned long long x = pv.key(idx[k], splitIdx);
                     const bool better = isMax ? (x > val || (x == val && k < pos)) : (x < val || (x == val && k < pos));
                     if (better) {
                         val = x;
@@ -492,6 +500,9 @@ __global__ void __launch_bounds__(BUILD_THREADS) splitLevelKernel(PosView pv, ui
                     }
                 }
                 blockArgExtreme(val, pos, isMax, shV, shP);
+                // the extreme coordinate itself (its key was formed from it)
+                const double extreme = pv.val(idx[pos], splitIdx);
+                __syncthreads();
                 if (threadIdx.x == 0) {
                     const uint32_t dst = isMax ? to - 1 : from;
                     const uint32_t t = idx[dst];
@@ -499,7 +510,7 @@ __global__ void __launch_bounds__(BUILD_THREADS) splitLevelKernel(PosView pv, ui
                     idx[pos] = t;
                 }
                 __syncthreads();
-                splitPosition = val;
+                splitPosition = extreme;
                 n1 = isMax ? to - 1 : from + 1;
                 sliding = true;
             }
@@ -571,9 +582,9 @@ __global__ void __launch_bounds__(BUILD_THREADS) splitLevelKernel(PosView pv, ui
 constexpr uint32_t WARP_SEGMENT = 1024;
 constexpr int SPLIT_WARP_THREADS = 256;
 
-__device__ __forceinline__ void warpArgExtreme(double& val, uint32_t& pos, bool isMax) {
+__device__ __forceinline__ void warpArgExtreme(unsigned long long& val, uint32_t& pos, bool isMax) {
     for (int off = 16; off > 0; off >>= 1) {
-        const double ov = __shfl_xor_sync(0xffffffffu, val, off);
+        const unsigned long long ov = __shfl_xor_sync(0xffffffffu, val, off);
         const uint32_t op = __shfl_xor_sync(0xffffffffu, pos, off);
         const bool better = isMax ? (ov > val || (ov == val && op < pos)) : (ov < val || (ov == val && op < pos));
         if (better) {
@@ -639,10 +650,10 @@ __global__ void __launch_bounds__(SPLIT_WARP_THREADS) splitWarpKernel(PosView pv
         {
             const uint32_t il = idx[to - 1];
             const dbl4 pl = pv.r[il];
-            const double last[3] = { pl.x, pl.y, pl.z };
+            const unsigned long long last[3] = { orderKey(pl.x), orderKey(pl.y), orderKey(pl.z) };
             for (uint32_t k = from + lane; k < to; k += 32) {
                 const dbl4 p = pv.r[idx[k]];
-                const double x[3] = { p.x, p.y, p.z };
+                const unsigned long long x[3] = { orderKey(p.x), orderKey(p.y), orderKey(p.z) };
                 for (int d = 0; d < 3; ++d) {
                     diff[d] = diff[d] || (x[d] != last[d]);
                 }
@@ -674,14 +685,15 @@ __global__ void __launch_bounds__(SPLIT_WARP_THREADS) splitWarpKernel(PosView pv
             hi1[d] = hi2[d] = sg.hi[d];
         }
         if (sg.sliding <= 5 && !degenerated) {
+            const unsigned long long splitKey = orderKey(splitPosition);
             uint32_t nB = 0, nS = 0;
             for (uint32_t k0 = from; k0 < to; k0 += 32) {
                 const uint32_t k = k0 + lane;
                 bool isB = false, isS = false;
                 if (k < to) {
-                    const double x = pv.val(idx[k], splitIdx);
-                    isB = x > splitPosition;
-                    isS = x < splitPosition;
+                    const unsigned long long x = pv.key(idx[k], splitIdx);
+                    isB = x > splitKey;
+                    isS = x < splitKey;
                 }
                 const unsigned mB = __ballot_sync(0xffffffffu, isB), mS = __ballot_sync(0xffffffffu, isS);
                 if (isB) {
@@ -714,10 +726,10 @@ __global__ void __launch_bounds__(SPLIT_WARP_THREADS) splitWarpKernel(PosView pv
             n1 = n1b;
             if (n1 == from || n1 == to) {
                 const bool isMax = (n1 == to);
-                double val = isMax ? -DBL_MAX : DBL_MAX;
+                unsigned long long val = isMax ? 0ull : ~0ull;
                 uint32_t pos = 0xffffffffu;
                 for (uint32_t k = from + lane; k < to; k += 32) {
-                    const double x = pv.val(idx[k], splitIdx);
+                    const unsigned long long x = pv.key(idx[k], splitIdx);
                     const bool better = isMax ? (x > val || (x == val && k < pos)) : (x < val || (x == val && k < pos));
                     if (better) {
                         val = x;
@@ -725,6 +737,7 @@ __global__ void __launch_bounds__(SPLIT_WARP_THREADS) splitWarpKernel(PosView pv
                     }
                 }
                 warpArgExtreme(val, pos, isMax);
+                const double extreme = pv.val(idx[pos], splitIdx);
                 __syncwarp();
                 if (lane == 0) {
                     const uint32_t dst = isMax ? to - 1 : from;
@@ -733,7 +746,7 @@ __global__ void __launch_bounds__(SPLIT_WARP_THREADS) splitWarpKernel(PosView pv
                     idx[pos] = t;
                 }
                 __syncwarp();
-                splitPosition = val;
+                splitPosition = extreme;
                 n1 = isMax ? to - 1 : from + 1;
                 sliding = true;
             }
@@ -824,32 +837,33 @@ __global__ void chunkListKernel(const BhSegment* __restrict__ segIn, uint32_t nI
     (void)work;
 }
 
-__device__ __forceinline__ bool betterArg(double v, uint32_t p, double bv, uint32_t bp, bool isMax) {
+__device__ __forceinline__ bool betterArg(unsigned long long v, uint32_t p, unsigned long long bv, uint32_t bp,
+    bool isMax) {
     return isMax ? (v > bv || (v == bv && p < bp)) : (v < bv || (v == bv && p < bp));
 }
 
 __global__ void __launch_bounds__(BUILD_THREADS) chunkStatsKernel(PosView pv, const uint32_t* __restrict__ idx,
     const BhSegment* __restrict__ segIn, const BhChunk* __restrict__ chunks, BhChunkStats* stats) {
     __shared__ uint32_t shScan[32];
-    __shared__ double shV[32];
+    __shared__ unsigned long long shV[32];
     __shared__ uint32_t shP[32];
     const BhChunk ch = chunks[blockIdx.x];
     const BhSegment sg = segIn[ch.seg];
     const uint32_t from = sg.from + ch.index * BH_CHUNK;
     const uint32_t to = min(sg.to, from + BH_CHUNK);
-    double center[3], last[3];
+    unsigned long long center[3], last[3];
     const uint32_t il = idx[sg.to - 1];
     for (int d = 0; d < 3; ++d) {
-        center[d] = 0.5 * (sg.lo[d] + sg.hi[d]);
-        last[d] = pv.val(il, d);
+        center[d] = orderKey(0.5 * (sg.lo[d] + sg.hi[d]));
+        last[d] = pv.key(il, d);
     }
     uint32_t nb[3] = { 0, 0, 0 }, ns[3] = { 0, 0, 0 };
     bool diff[3] = { false, false, false };
-    double mnv[3] = { DBL_MAX, DBL_MAX, DBL_MAX }, mxv[3] = { -DBL_MAX, -DBL_MAX, -DBL_MAX };
+    unsigned long long mnv[3] = { ~0ull, ~0ull, ~0ull }, mxv[3] = { 0ull, 0ull, 0ull };
     uint32_t mnp[3] = { 0xffffffffu, 0xffffffffu, 0xffffffffu }, mxp[3] = { 0xffffffffu, 0xffffffffu, 0xffffffffu };
     for (uint32_t k = from + threadIdx.x; k < to; k += BUILD_THREADS) {
         const dbl4 p = pv.r[idx[k]];
-        const double x[3] = { p.x, p.y, p.z };
+        const unsigned long long x[3] = { orderKey(p.x), orderKey(p.y), orderKey(p.z) };
         for (int d = 0; d < 3; ++d) {
             nb[d] += x[d] > center[d] ? 1u : 0u;
             ns[d] += x[d] < center[d] ? 1u : 0u;
@@ -869,7 +883,7 @@ __global__ void __launch_bounds__(BUILD_THREADS) chunkStatsKernel(PosView pv, co
         out.nb[d] = blockSum(nb[d], shScan);
         out.ns[d] = blockSum(ns[d], shScan);
         out.diff[d] = __syncthreads_or(diff[d] ? 1 : 0) ? 1u : 0u;
-        double v = mnv[d];
+        unsigned long long v = mnv[d];
         uint32_t q = mnp[d];
         blockArgExtreme(v, q, false, shV, shP);
         out.minv[d] = v;
@@ -885,21 +899,27 @@ __global__ void __launch_bounds__(BUILD_THREADS) chunkStatsKernel(PosView pv, co
     }
 }
 
-// one thread per large segment (the thread of its first chunk)
+// one warp per large segment (the warp of its first chunk): split dimension and mode, chunk offsets of the
+// elements above / below the box centre (warp scan), extremes of the split coordinate
 __global__ void segDecideKernel(const BhSegment* __restrict__ segIn, const BhChunk* __restrict__ chunks,
     uint32_t nChunks, const BhChunkStats* __restrict__ stats, uint32_t* chunkOffB, uint32_t* chunkOffS,
     BhSegWork* work) {
-    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (c >= nChunks || chunks[c].index != 0) {
         return;
     }
     const BhChunk ch = chunks[c];
     const BhSegment sg = segIn[ch.seg];
-    bool nonSingular[3] = { false, false, false };
-    for (uint32_t k = 0; k < ch.count; ++k) {
+    bool anyDiff[3] = { false, false, false };
+    for (uint32_t k = lane; k < ch.count; k += 32) {
         for (int d = 0; d < 3; ++d) {
-            nonSingular[d] = nonSingular[d] || stats[ch.first + k].diff[d] != 0;
+            anyDiff[d] = anyDiff[d] || stats[ch.first + k].diff[d] != 0;
         }
+    }
+    bool nonSingular[3];
+    for (int d = 0; d < 3; ++d) {
+        nonSingular[d] = __any_sync(0xffffffffu, anyDiff[d]);
     }
     double boxSize[3];
     for (int d = 0; d < 3; ++d) {
@@ -919,35 +939,56 @@ __global__ void segDecideKernel(const BhSegment* __restrict__ segIn, const BhChu
             break;
         }
     }
-    BhSegWork w;
-    w.splitIdx = splitIdx;
-    w.mode = degenerated ? 2 : (sg.sliding <= 5 ? 0 : 1);
     uint32_t ob = 0, os = 0;
-    double mnv = DBL_MAX, mxv = -DBL_MAX;
+    unsigned long long mnv = ~0ull, mxv = 0ull;
     uint32_t mnp = 0xffffffffu, mxp = 0xffffffffu;
-    for (uint32_t k = 0; k < ch.count; ++k) {
-        const BhChunkStats& st = stats[ch.first + k];
-        chunkOffB[ch.first + k] = ob;
-        chunkOffS[ch.first + k] = os;
-        ob += st.nb[splitIdx];
-        os += st.ns[splitIdx];
-        if (betterArg(st.minv[splitIdx], st.minp[splitIdx], mnv, mnp, false)) {
-            mnv = st.minv[splitIdx];
-            mnp = st.minp[splitIdx];
+    for (uint32_t k0 = 0; k0 < ch.count; k0 += 32) {
+        const uint32_t k = k0 + lane;
+        uint32_t nb = 0, ns = 0;
+        if (k < ch.count) {
+            const BhChunkStats& st = stats[ch.first + k];
+            nb = st.nb[splitIdx];
+            ns = st.ns[splitIdx];
+            if (betterArg(st.minv[splitIdx], st.minp[splitIdx], mnv, mnp, false)) {
+                mnv = st.minv[splitIdx];
+                mnp = st.minp[splitIdx];
+            }
+            if (betterArg(st.maxv[splitIdx], st.maxp[splitIdx], mxv, mxp, true)) {
+                mxv = st.maxv[splitIdx];
+                mxp = st.maxp[splitIdx];
+            }
         }
-        if (betterArg(st.maxv[splitIdx], st.maxp[splitIdx], mxv, mxp, true)) {
-            mxv = st.maxv[splitIdx];
-            mxp = st.maxp[splitIdx];
+        // inclusive scans of the counts across the lanes
+        uint32_t xb = nb, xs = ns;
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t yb = __shfl_up_sync(0xffffffffu, xb, off), ys = __shfl_up_sync(0xffffffffu, xs, off);
+            if (lane >= off) {
+                xb += yb;
+                xs += ys;
+            }
         }
+        if (k < ch.count) {
+            chunkOffB[ch.first + k] = ob + xb - nb;
+            chunkOffS[ch.first + k] = os + xs - ns;
+        }
+        ob += __shfl_sync(0xffffffffu, xb, 31);
+        os += __shfl_sync(0xffffffffu, xs, 31);
     }
-    w.nB = ob;
-    w.nS = os;
-    w.minv = mnv;
-    w.minp = mnp;
-    w.maxv = mxv;
-    w.maxp = mxp;
-    w.K = 0;
-    work[ch.seg] = w;
+    warpArgExtreme(mnv, mnp, false);
+    warpArgExtreme(mxv, mxp, true);
+    if (lane == 0) {
+        BhSegWork w;
+        w.splitIdx = splitIdx;
+        w.mode = degenerated ? 2 : (sg.sliding <= 5 ? 0 : 1);
+        w.nB = ob;
+        w.nS = os;
+        w.minv = mnv;
+        w.minp = mnp;
+        w.maxv = mxv;
+        w.maxp = mxp;
+        w.K = 0;
+        work[ch.seg] = w;
+    }
 }
 
 __global__ void __launch_bounds__(BUILD_THREADS) chunkRanksKernel(PosView pv, const uint32_t* __restrict__ idx,
@@ -961,7 +1002,7 @@ __global__ void __launch_bounds__(BUILD_THREADS) chunkRanksKernel(PosView pv, co
         return;
     }
     const int d = w.splitIdx;
-    const double split = 0.5 * (sg.lo[d] + sg.hi[d]);
+    const unsigned long long split = orderKey(0.5 * (sg.lo[d] + sg.hi[d]));
     const uint32_t from = sg.from + ch.index * BH_CHUNK;
     const uint32_t to = min(sg.to, from + BH_CHUNK);
     uint32_t baseB = sg.from + chunkOffB[blockIdx.x], baseS = sg.from + chunkOffS[blockIdx.x];
@@ -969,7 +1010,7 @@ __global__ void __launch_bounds__(BUILD_THREADS) chunkRanksKernel(PosView pv, co
         const uint32_t k = k0 + threadIdx.x;
         bool isB = false, isS = false;
         if (k < to) {
-            const double x = pv.val(idx[k], d);
+            const unsigned long long x = pv.key(idx[k], d);
             isB = x > split;
             isS = x < split;
         }
@@ -1027,10 +1068,10 @@ __global__ void segFinishKernel(PosView pv, uint32_t* idx, const uint32_t* __res
             const bool isMax = (n1 == to);
             const uint32_t dst = isMax ? to - 1 : from;
             const uint32_t src = isMax ? w.maxp : w.minp;
+            splitPosition = pv.val(idx[src], d);
             const uint32_t t = idx[dst];
             idx[dst] = idx[src];
             idx[src] = t;
-            splitPosition = isMax ? w.maxv : w.minv;
             n1 = isMax ? to - 1 : from + 1;
             sliding = true;
         }
@@ -1741,7 +1782,7 @@ cudaError_t treeBuild(const DState& s, Tree& t, const Physics& ph, uint32_t* dev
         }
         if (nChunks > 0) {
             chunkStatsKernel<<<nChunks, BUILD_THREADS, 0, st>>>(pv, t.idx, t.seg[cur], t.chunks, t.chunk_stats);
-            segDecideKernel<<<ceilDiv(nChunks, 128), 128, 0, st>>>(t.seg[cur], t.chunks, nChunks, t.chunk_stats,
+            segDecideKernel<<<ceilDiv(nChunks, 4), 128, 0, st>>>(t.seg[cur], t.chunks, nChunks, t.chunk_stats,
                 t.chunk_off_b, t.chunk_off_s, t.work);
             chunkRanksKernel<<<nChunks, BUILD_THREADS, 0, st>>>(pv, t.idx, t.seg[cur], t.chunks, t.chunk_off_b,
                 t.chunk_off_s, t.work, t.scratch_b, t.scratch_s);

@@ -145,7 +145,7 @@ struct BhChunkStats {
     uint32_t nb[3], ns[3];  // elements above / below the box centre, per dimension
     uint32_t diff[3];       // any element differs from the segment's last one, per dimension
     uint32_t pad;
-    double minv[3], maxv[3];
+    unsigned long long minv[3], maxv[3]; // orderKey of the extremes
     uint32_t minp[3], maxp[3]; // first positions of the extremes
 };
 
@@ -155,7 +155,7 @@ struct BhSegWork {
     uint32_t nB, nS, K;
     uint32_t minp, maxp;
     uint32_t pad;
-    double minv, maxv;
+    unsigned long long minv, maxv; // orderKey of the extremes
 };
 
 struct Tree {

@@ -224,9 +224,10 @@ def run_gpu(args, rank, world):
     if world > 1:
         torch.distributed.all_reduce(e2e_t, op=torch.distributed.ReduceOp.MAX)
     e2e_value = n * args.steps * world / (float(e2e_t.item()) * 1e-3)
+    interactions = g.gravity_interactions()
     g.close()
 
-    result = {"n": n, "ms": ms, "value": value, "phases": phases, "launches": launches,
+    result = {"n": n, "ms": ms, "value": value, "phases": phases, "launches": launches, "interactions": interactions,
               "clocks": clk.summary(), "e2e": {"value": e2e_value, "unit": UNIT,
                                                  "h2d_bytes_per_step": 2 * 32 * n,
                                                  "d2h_bytes_per_step": (32 + 32 + 8 + 8) * n}}
@@ -284,6 +285,11 @@ def compare_fp64(args, st, mats, n, mixed_cfg, dev):
     out["max_abs_err_damage"] = float(np.max(np.abs(mix["D"] - ref["D"])))
     return out
 
+
+# DRAM bytes (read + write) of one walkMixedKernel launch of the default workload, from the ncu capture
+# summarised in profiles/walkMixedKernel_impact1M.md
+WALK_TRAFFIC_BYTES = (762.39 + 351.86) * 1e6
+WALK_TRAFFIC_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, profiles/walkMixedKernel_impact1M.md"
 
 # FP32 operations of one particle-multipole evaluation (evalMultipoleF, csrc/gravity32.cu: octupole) and the
 # N-body convention for one softened particle-particle interaction
@@ -474,16 +480,31 @@ def main():
     pair_ms = res["phases"]["sph_eval"] / args.steps
     peak, peak_kind = peaks()
     achieved = PAIR_BYTES_PER_PARTICLE * n / (pair_ms * 1e-3) / 1e9 if pair_ms > 0 else None
+    # dominant kernel: the mixed tree walk, FP32-pipe bound; algorithmic FLOPs of the last step's walk
+    # (interaction counts of the walk itself) over its CUDA-event time on the gravity stream
+    walk_ms = res["phases"]["gravity_eval"] / args.steps
+    pn, pp = res["interactions"]
+    walk_flops = pn * FLOP_PN + pp * FLOP_PP
+    walk_tf = walk_flops / (walk_ms * 1e-3) / 1e12 if walk_ms > 0 else None
     line = {
         "metric": METRIC, "value": res["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32/f64", "data": "synthetic", "config": config_json(args, n),
         "e2e": res["e2e"], "gpu_launches": res["launches"], "clocks": res["clocks"],
         "phases_ms_per_step": {k: v / args.steps for k, v in res["phases"].items()},
-        "roofline": {"kernel": "pairSumMixedKernel", "bound": "hbm", "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak if achieved else None, "traffic": None,
-                     "peak_source": peak_kind,
-                     "algorithmic_bytes_per_particle": PAIR_BYTES_PER_PARTICLE},
+        "roofline": {"kernel": "walkMixedKernel", "bound": "fp32", "achieved": walk_tf, "peak": FP32_PEAK_NOMINAL,
+                     "unit": "TFLOP/s", "frac": walk_tf / FP32_PEAK_NOMINAL if walk_tf else None,
+                     "traffic": WALK_TRAFFIC_BYTES, "traffic_source": WALK_TRAFFIC_SOURCE,
+                     "peak_source": "nominal FP32 (152 SMs x 128 lanes x 2 x 2.07 GHz); MEASURED_PEAKS.json has no "
+                                    "FP32 figure",
+                     "flops_per_launch": walk_flops, "particle_node": pn, "particle_particle": pp,
+                     "flop_per_particle_node": FLOP_PN, "flop_per_particle_particle": FLOP_PP,
+                     "launch_ms": walk_ms},
+        "roofline_pair": {"kernel": "pairSumMixedKernel", "bound": "hbm", "achieved": achieved, "peak": peak,
+                          "unit": "GB/s", "frac": achieved / peak if achieved else None,
+                          "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                          "algorithmic_bytes_per_particle": PAIR_BYTES_PER_PARTICLE,
+                          "note": "timed while the tree build runs concurrently on the gravity stream"},
     }
     if "fp64" in res:
         line["fp64"] = res["fp64"]

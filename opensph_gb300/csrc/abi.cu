@@ -315,10 +315,10 @@ sphgpu_status evalGravity(sphgpu_handle* h, cudaStream_t st) {
         Phase ph(h, SPHGPU_PHASE_GRAVITY_EVAL, st);
         if (h->ph.precision == SPHGPU_PRECISION_MIXED) {
             launchGravityWalkMixed(h->s, h->tree, h->ph, h->d_lut_grav_f, h->d_err, st);
-            h->launches += 2;
+            h->launches += 1;
         } else {
             launchGravityWalk(h->s, h->tree, h->ph, h->d_lut_grav, h->d_err, st);
-            h->launches += 2;
+            h->launches += 1;
         }
     }
     h->gravity_current = true;
@@ -835,7 +835,7 @@ sphgpu_status sphgpu_gravity_eval(sphgpu_handle* h, double* dv, uint64_t count) 
         } else {
             launchGravityWalk(h->s, h->tree, h->ph, h->d_lut_grav, h->d_err, h->stream);
         }
-        h->launches += 2;
+        h->launches += 1;
     }
     CUDA_TRY(h, cudaGetLastError());
     const sphgpu_status st = checkDeviceError(h);

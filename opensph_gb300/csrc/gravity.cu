@@ -1815,7 +1815,9 @@ cudaError_t treeBuild(const DState& s, Tree& t, const Physics& ph, uint32_t* dev
     // moments, bottom-up in one launch
     t.mixed_moments = ph.precision == SPHGPU_PRECISION_MIXED;
     launchMoments(s, t, ph, t.mixed_moments, st);
-    t.launches++;
+    // FP32 node records of the walks (classification geometry; for the mixed walk also the evaluation data)
+    launchPrepareWalk(s, t, ph, st);
+    t.launches += 2;
     t.built = true;
     return cudaGetLastError();
 }
@@ -1839,7 +1841,6 @@ void launchGravityWalk(const DState& s, Tree& t, const Physics& ph, const double
         residentBlocks = std::max(1, perSm * sms);
     }
     const int blocks = std::max(1, std::min(residentBlocks, int(t.walk_warps / (WALK_THREADS / 32))));
-    launchPrepareWalk(s, t, ph, st);
     walkKernel<<<blocks, WALK_THREADS, 0, st>>>(s.r, s.m, ph.G, t.idx, t.geom, t.mom, t.nodef, t.leaves,
         t.leaf_count, lut,
         ph.kernel_radius,

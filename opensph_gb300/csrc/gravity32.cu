@@ -424,7 +424,6 @@ void launchGravityWalkMixed(const DState& s, Tree& t, const Physics& ph, const f
     if (s.n == 0 || t.node_count == 0) {
         return;
     }
-    launchPrepareWalk(s, t, ph, st);
     static int residentBlocks = 0;
     if (residentBlocks == 0) {
         int perSm = 0, sms = 0;

@@ -21,7 +21,7 @@
 extern "C" {
 #endif
 
-#define SPHGPU_ABI_VERSION 1
+#define SPHGPU_ABI_VERSION 2
 
 typedef enum {
     SPHGPU_OK = 0,
@@ -69,6 +69,15 @@ enum { SPHGPU_DAMAGE_NONE = 0, SPHGPU_DAMAGE_SCALAR_GRADY_KIPP = 1 };
 enum { SPHGPU_INTEGRATOR_PREDICTOR_CORRECTOR = 0, SPHGPU_INTEGRATOR_LEAP_FROG = 1 };
 /* GravityKernelEnum (core/system/Settings.h): point masses or the gravity kernel of the SPH kernel */
 enum { SPHGPU_GRAVITY_KERNEL_POINT_PARTICLES = 0, SPHGPU_GRAVITY_KERNEL_SPH_KERNEL = 1 };
+/* Time-step criteria: the reference's TimeStepCriterionEnum bits (core/system/Settings.h:577-592), evaluated
+ * after every step as in MultiCriterion::compute (core/timestepping/TimeStepCriterion.cpp:139-389). */
+enum {
+    SPHGPU_CRITERION_COURANT = 1 << 1,      /* C h / c_s */
+    SPHGPU_CRITERION_DERIVATIVES = 1 << 2,  /* f (|x| + x_min) / (|dx/dt| + EPS) of first-order quantities */
+    SPHGPU_CRITERION_ACCELERATION = 1 << 3, /* f (h / |dv/dt|)^(1/2) */
+    SPHGPU_CRITERION_DIVERGENCE = 1 << 4,   /* f_div / |div v| */
+    SPHGPU_CRITERION_ALL = (1 << 1) | (1 << 2) | (1 << 3) | (1 << 4)
+};
 enum {
     SPHGPU_PRECISION_FP64 = 0, /* every operation in FP64; pair terms IEEE-identical to the reference */
     SPHGPU_PRECISION_MIXED = 1 /* FP32 cell-relative pair sums and walk, FP64 state/integrator/totals */
@@ -100,6 +109,12 @@ typedef struct {
     double density_range[2];
     double energy_range[2];
     double damage_range[2];
+    /* IMaterial::minimal of the first-order quantities (DENSITY_MIN, ENERGY_MIN, STRESS_TENSOR_MIN, DAMAGE_MIN;
+     * reference defaults 100, 1, 1e5, 0.03), used by the derivative time-step criterion */
+    double density_min;
+    double energy_min;
+    double stress_min;
+    double damage_min;
 } sphgpu_material;
 
 /* Run settings (the reference's RunSettingsId entries of the path). */
@@ -125,6 +140,11 @@ typedef struct {
     double initial_timestep;
     int32_t precision;                 /* SPHGPU_PRECISION_* */
     int32_t device;                    /* CUDA device ordinal */
+    uint32_t timestep_criteria;        /* SPHGPU_CRITERION_* bits; 0 = Courant only */
+    int32_t reserved1;
+    double derivative_factor;          /* TIMESTEPPING_DERIVATIVE_FACTOR (0.2), also the acceleration factor */
+    double divergence_factor;          /* TIMESTEPPING_DIVERGENCE_FACTOR (0.005) */
+    double max_change;                 /* TIMESTEPPING_MAX_INCREASE: relative growth limit per step, INFINITY = off */
 } sphgpu_config;
 
 typedef struct sphgpu_handle sphgpu_handle;

@@ -53,6 +53,12 @@ GRAVITY_KERNEL_SPH_KERNEL = 1
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
 
+CRITERION_COURANT = 1 << 1
+CRITERION_DERIVATIVES = 1 << 2
+CRITERION_ACCELERATION = 1 << 3
+CRITERION_DIVERGENCE = 1 << 4
+CRITERION_ALL = CRITERION_COURANT | CRITERION_DERIVATIVES | CRITERION_ACCELERATION | CRITERION_DIVERGENCE
+
 # (components, numpy dtype) of each quantity across the boundary
 QUANTITY_LAYOUT = {
     Q_POSITION: (4, "f8"),
@@ -100,6 +106,10 @@ class Material(ctypes.Structure):
         ("density_range", ctypes.c_double * 2),
         ("energy_range", ctypes.c_double * 2),
         ("damage_range", ctypes.c_double * 2),
+        ("density_min", ctypes.c_double),
+        ("energy_min", ctypes.c_double),
+        ("stress_min", ctypes.c_double),
+        ("damage_min", ctypes.c_double),
     ]
 
 
@@ -126,6 +136,11 @@ class Config(ctypes.Structure):
         ("initial_timestep", ctypes.c_double),
         ("precision", ctypes.c_int32),
         ("device", ctypes.c_int32),
+        ("timestep_criteria", ctypes.c_uint32),
+        ("reserved1", ctypes.c_int32),
+        ("derivative_factor", ctypes.c_double),
+        ("divergence_factor", ctypes.c_double),
+        ("max_change", ctypes.c_double),
     ]
 
 
@@ -158,6 +173,10 @@ def basalt(**overrides):
     m.density_range[:] = [50.0, INFTY]
     m.energy_range[:] = [0.0, INFTY]
     m.damage_range[:] = [0.0, 1.0]
+    m.density_min = 100.0
+    m.energy_min = 1.0
+    m.stress_min = 1.0e5
+    m.damage_min = 0.03
     for k, v in overrides.items():
         if k.endswith("_range"):
             getattr(m, k)[:] = v
@@ -203,6 +222,10 @@ def make_config(n, materials, forces=FORCE_PRESSURE | FORCE_SELF_GRAVITY, adapti
     c.initial_timestep = 0.03
     c.precision = precision
     c.device = 0
+    c.timestep_criteria = CRITERION_COURANT
+    c.derivative_factor = 0.2
+    c.divergence_factor = 0.005
+    c.max_change = INFTY
     for k, v in kw.items():
         if k == "smoothing_length_range":
             c.smoothing_length_range[:] = v

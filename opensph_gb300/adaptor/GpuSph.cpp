@@ -67,6 +67,10 @@ sphgpu_material toMaterial(const IMaterial& m) {
     out.energy_range[1] = u.upper();
     out.damage_range[0] = d.lower();
     out.damage_range[1] = d.upper();
+    out.density_min = m.minimal(QuantityId::DENSITY);
+    out.energy_min = m.minimal(QuantityId::ENERGY);
+    out.stress_min = m.minimal(QuantityId::DEVIATORIC_STRESS);
+    out.damage_min = m.minimal(QuantityId::DAMAGE);
     return out;
 }
 
@@ -128,6 +132,19 @@ DeviceState::DeviceState(const RunSettings& settings, const Storage& storage, in
     config.courant_number = settings.get<Float>(RunSettingsId::TIMESTEPPING_COURANT_NUMBER);
     config.max_timestep = settings.get<Float>(RunSettingsId::TIMESTEPPING_MAX_TIMESTEP);
     config.initial_timestep = settings.get<Float>(RunSettingsId::TIMESTEPPING_INITIAL_TIMESTEP);
+    const Flags<TimeStepCriterionEnum> crit =
+        settings.getFlags<TimeStepCriterionEnum>(RunSettingsId::TIMESTEPPING_CRITERION);
+    config.timestep_criteria = (crit.has(TimeStepCriterionEnum::COURANT) ? SPHGPU_CRITERION_COURANT : 0) |
+                               (crit.has(TimeStepCriterionEnum::DERIVATIVES) ? SPHGPU_CRITERION_DERIVATIVES : 0) |
+                               (crit.has(TimeStepCriterionEnum::ACCELERATION) ? SPHGPU_CRITERION_ACCELERATION : 0) |
+                               (crit.has(TimeStepCriterionEnum::DIVERGENCE) ? SPHGPU_CRITERION_DIVERGENCE : 0);
+    config.derivative_factor = settings.get<Float>(RunSettingsId::TIMESTEPPING_DERIVATIVE_FACTOR);
+    config.divergence_factor = settings.get<Float>(RunSettingsId::TIMESTEPPING_DIVERGENCE_FACTOR);
+    config.max_change = settings.get<Float>(RunSettingsId::TIMESTEPPING_MAX_INCREASE);
+    if (settings.get<Float>(RunSettingsId::TIMESTEPPING_MEAN_POWER) > -1.e3_f &&
+        crit.has(TimeStepCriterionEnum::DERIVATIVES)) {
+        raise(true, "GPU path implements the minimal-step derivative criterion only (timestep.mean_power = -inf)");
+    }
     config.precision = precision;
     config.device = 0;
     const int rc = sphgpu_create(&config, &handle);

@@ -188,6 +188,10 @@ MaterialD toDevice(const sphgpu_material& m) {
     d.u_hi = m.energy_range[1];
     d.d_lo = m.damage_range[0];
     d.d_hi = m.damage_range[1];
+    d.rho_min = m.density_min;
+    d.u_min = m.energy_min;
+    d.s_min = m.stress_min;
+    d.d_min = m.damage_min;
     return d;
 }
 
@@ -405,6 +409,19 @@ sphgpu_status validate(const sphgpu_config* c) {
     if (c->precision != SPHGPU_PRECISION_FP64 && c->precision != SPHGPU_PRECISION_MIXED) {
         return fail(nullptr, SPHGPU_ERR_UNSUPPORTED, "unknown precision %d", c->precision);
     }
+    if (c->timestep_criteria & ~uint32_t(SPHGPU_CRITERION_ALL)) {
+        return fail(nullptr, SPHGPU_ERR_UNSUPPORTED, "unknown time-step criterion bits 0x%x", c->timestep_criteria);
+    }
+    if ((c->timestep_criteria & (SPHGPU_CRITERION_DERIVATIVES | SPHGPU_CRITERION_ACCELERATION)) &&
+        !(c->derivative_factor > 0.)) {
+        return fail(nullptr, SPHGPU_ERR_ARGUMENT, "derivative_factor must be positive");
+    }
+    if ((c->timestep_criteria & SPHGPU_CRITERION_DIVERGENCE) && !(c->divergence_factor > 0.)) {
+        return fail(nullptr, SPHGPU_ERR_ARGUMENT, "divergence_factor must be positive");
+    }
+    if (!(c->max_change > 0.)) {
+        return fail(nullptr, SPHGPU_ERR_ARGUMENT, "max_change must be positive (1.7976931348623157e308 = no limit)");
+    }
     if (!(c->forces & SPHGPU_FORCE_PRESSURE)) {
         return fail(nullptr, SPHGPU_ERR_UNSUPPORTED, "the pressure force is required");
     }
@@ -486,6 +503,10 @@ sphgpu_status sphgpu_create(const sphgpu_config* config, sphgpu_handle** out) {
     ph.theta_inv = config->gravity_opening_angle > 0. ? 1. / config->gravity_opening_angle : 2.;
     ph.courant = config->courant_number;
     ph.max_dt = config->max_timestep;
+    ph.criteria = config->timestep_criteria ? config->timestep_criteria : uint32_t(SPHGPU_CRITERION_COURANT);
+    ph.derivative_factor = config->derivative_factor;
+    ph.divergence_factor = config->divergence_factor;
+    ph.max_change = config->max_change;
     (void)anyRheology;
 
     cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
@@ -966,7 +987,7 @@ sphgpu_status sphgpu_step(sphgpu_handle* h, uint32_t nsteps) {
             } else {
                 launchCorrect(h->s, h->ph, h->d_mats, h->d_dt, h->d_dt_min, h->stream);
             }
-            launchCourantFinish(h->d_dt, h->d_dt_min, h->ph.max_dt, h->stream);
+            launchCourantFinish(h->d_dt, h->d_dt_min, h->ph.max_dt, h->ph.max_change, h->stream);
             h->launches += 2;
         }
         CUDA_TRY(h, cudaGetLastError());

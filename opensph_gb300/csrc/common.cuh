@@ -39,6 +39,7 @@ struct MaterialD {
     double rho0, A, B, a, b, alpha, beta, u0, uiv, ucv, gamma;
     double mu, limit, u_melt, young;
     double rho_lo, rho_hi, u_lo, u_hi, d_lo, d_hi;
+    double rho_min, u_min, s_min, d_min; // IMaterial::minimal (derivative time-step criterion)
 };
 
 // Uniform grid of the neighbour search (computed on the device each step)

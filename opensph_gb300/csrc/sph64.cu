@@ -246,7 +246,63 @@ __device__ __forceinline__ void blockMinToGlobal(double local, double* out) {
     }
 }
 
-// PredictorCorrector::makeCorrections (TimeStepping.cpp:302-322) + CourantCriterion partial minimum
+// The per-particle candidates of MultiCriterion::compute (core/timestepping/TimeStepCriterion.cpp:139-389) on the
+// state after the step: CourantCriterion C h / c_s (c_s > 0); DerivativeCriterion f (|x| + x_min) / (|dx| + EPS)
+// for every component of the first-order quantities (density, energy, deviatoric stress with its zz component
+// -xx - yy, damage) whose |x| >= 2 x_min; AccelerationCriterion f (h^2 / |dv|^2)^(1/4) for |dv|^2 > EPS;
+// DivergenceCriterion f_div / |div v| for |div v| > EPS. The global minimum of these, capped by the maximal
+// step, is the minimum over the criteria the reference forms.
+__device__ __forceinline__ double derivStep(double factor, double x, double dx, double xmin, double cur) {
+    const double ax = fabs(x);
+    if (ax < 2. * xmin) {
+        return cur;
+    }
+    return fmin(cur, factor * (ax + xmin) / (fabs(dx) + SPH_EPS));
+}
+
+__device__ __forceinline__ double criteriaStep(const DState& s, const Physics& ph, const MaterialD& mt, uint32_t i,
+    const dbl4& r, double rho, double drho, double u, double du, const double* S, const double* dS, double D,
+    double dD) {
+    double local = DBL_MAX;
+    if (ph.criteria & SPHGPU_CRITERION_COURANT) {
+        const double cs = s.cs[i];
+        if (cs > 0.) {
+            local = ph.courant * r.w / cs;
+        }
+    }
+    if (ph.criteria & SPHGPU_CRITERION_DERIVATIVES) {
+        const double f = ph.derivative_factor;
+        local = derivStep(f, rho, drho, mt.rho_min, local);
+        local = derivStep(f, u, du, mt.u_min, local);
+        if (ph.solid) {
+            // TracelessTensor components xx, yy, zz = -xx - yy, xy, xz, yz
+            const double sv[6] = { S[0], S[1], -S[0] - S[1], S[2], S[3], S[4] };
+            const double dsv[6] = { dS[0], dS[1], -dS[0] - dS[1], dS[2], dS[3], dS[4] };
+            for (int c = 0; c < 6; ++c) {
+                local = derivStep(f, sv[c], dsv[c], mt.s_min, local);
+            }
+            if (ph.damage) {
+                local = derivStep(f, D, dD, mt.d_min, local);
+            }
+        }
+    }
+    if (ph.criteria & SPHGPU_CRITERION_ACCELERATION) {
+        const dbl4 a = s.dv[i];
+        const double a2 = a.x * a.x + a.y * a.y + a.z * a.z;
+        if (a2 > SPH_EPS) {
+            local = fmin(local, ph.derivative_factor * sqrt(sqrt(r.w * r.w / a2)));
+        }
+    }
+    if (ph.criteria & SPHGPU_CRITERION_DIVERGENCE) {
+        const double dv = fabs(s.divv[i]);
+        if (dv > SPH_EPS) {
+            local = fmin(local, ph.divergence_factor / dv);
+        }
+    }
+    return local;
+}
+
+// PredictorCorrector::makeCorrections (TimeStepping.cpp:302-322) + the time-step criteria partial minimum
 __global__ void correctKernel(DState s, Physics ph, const MaterialD* __restrict__ mats, const double* __restrict__ dtp,
     double* dtMin) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -279,22 +335,23 @@ __global__ void correctKernel(DState s, Physics ph, const MaterialD* __restrict_
         clampDeriv(u, du, mt.u_lo, mt.u_hi);
         s.u[i] = u;
         s.du[i] = du;
+        double S[5] = { 0, 0, 0, 0, 0 }, dS[5] = { 0, 0, 0, 0, 0 }, D = 0., dD = 0.;
         if (ph.solid) {
             for (int c = 0; c < 5; ++c) {
-                s.S[c * n + i] -= 0.5 * (s.pdS[c * n + i] - s.dS[c * n + i]) * dt;
+                dS[c] = s.dS[c * n + i];
+                S[c] = s.S[c * n + i] - 0.5 * (s.pdS[c * n + i] - dS[c]) * dt;
+                s.S[c * n + i] = S[c];
             }
             if (ph.damage) {
-                double D = s.D[i], dD = s.dD[i];
+                D = s.D[i];
+                dD = s.dD[i];
                 D -= 0.5 * (s.pdD[i] - dD) * dt;
                 clampDeriv(D, dD, mt.d_lo, mt.d_hi);
                 s.D[i] = D;
                 s.dD[i] = dD;
             }
         }
-        const double cs = s.cs[i];
-        if (cs > 0.) {
-            local = ph.courant * r.w / cs;
-        }
+        local = criteriaStep(s, ph, mt, i, r, rho, drho, u, du, S, dS, D, dD);
     }
     blockMinToGlobal(local, dtMin);
 }
@@ -335,12 +392,16 @@ __global__ void leapFrogKickKernel(DState s, Physics ph, const MaterialD* __rest
         clampDeriv(u, du, mt.u_lo, mt.u_hi);
         s.u[i] = u;
         s.du[i] = du;
+        double S[5] = { 0, 0, 0, 0, 0 }, dS[5] = { 0, 0, 0, 0, 0 }, D = 0., dD = 0.;
         if (ph.solid) {
             for (int c = 0; c < 5; ++c) {
-                s.S[c * n + i] += s.dS[c * n + i] * dt;
+                dS[c] = s.dS[c * n + i];
+                S[c] = s.S[c * n + i] + dS[c] * dt;
+                s.S[c * n + i] = S[c];
             }
             if (ph.damage) {
-                double D = s.D[i], dD = s.dD[i];
+                D = s.D[i];
+                dD = s.dD[i];
                 D += dD * dt;
                 clampDeriv(D, dD, mt.d_lo, mt.d_hi);
                 s.D[i] = D;
@@ -360,17 +421,23 @@ __global__ void leapFrogKickKernel(DState s, Physics ph, const MaterialD* __rest
         r.w += v.w * 0.5 * dt;
         s.v[i] = v;
         s.r[i] = r;
-        const double cs = s.cs[i];
-        if (cs > 0.) {
-            local = ph.courant * r.w / cs;
-        }
+        local = criteriaStep(s, ph, mt, i, r, rho, drho, u, du, S, dS, D, dD);
     }
     blockMinToGlobal(local, dtMin);
 }
 
-__global__ void courantFinishKernel(double* dt, double* dtMin, double maxDt) {
-    const double m = *dtMin;
-    *dt = m > maxDt ? maxDt : m;
+// the step minimum capped by the maximal step, then limited to (1 + maxChange) times the previous step
+// (MultiCriterion::compute's smoothing, off for maxChange >= DBL_MAX)
+__global__ void courantFinishKernel(double* dt, double* dtMin, double maxDt, double maxChange) {
+    double m = *dtMin;
+    m = m > maxDt ? maxDt : m;
+    if (maxChange < DBL_MAX) {
+        const double lim = *dt * (1. + maxChange);
+        if (m > lim) {
+            m = lim;
+        }
+    }
+    *dt = m;
     *dtMin = DBL_MAX;
 }
 
@@ -502,8 +569,8 @@ void launchLeapFrogKick(const DState& s, const Physics& ph, const MaterialD* mat
     }
 }
 
-void launchCourantFinish(double* dt, double* dtMin, double maxDt, cudaStream_t st) {
-    courantFinishKernel<<<1, 1, 0, st>>>(dt, dtMin, maxDt);
+void launchCourantFinish(double* dt, double* dtMin, double maxDt, double maxChange, cudaStream_t st) {
+    courantFinishKernel<<<1, 1, 0, st>>>(dt, dtMin, maxDt, maxChange);
 }
 
 void launchTotals(const DState& s, double* partial, double* out, cudaStream_t st) {

@@ -69,6 +69,10 @@ struct Physics {
     double theta_inv;
     double courant;
     double max_dt;
+    uint32_t criteria;        // SPHGPU_CRITERION_* bits
+    double derivative_factor; // derivative and acceleration criteria
+    double divergence_factor;
+    double max_change;        // relative growth limit of the step (off when >= DBL_MAX)
 };
 
 // Neighbour grid buffers (cell-sorted copies of the pair-loop inputs)
@@ -213,7 +217,7 @@ void launchLeapFrogDriftInit(const DState& s, const Physics& ph, const MaterialD
     cudaStream_t st);
 void launchLeapFrogKick(const DState& s, const Physics& ph, const MaterialD* mats, const double* dt,
     double* dt_min, cudaStream_t st);
-void launchCourantFinish(double* dt, double* dt_min, double max_dt, cudaStream_t st);
+void launchCourantFinish(double* dt, double* dt_min, double max_dt, double max_change, cudaStream_t st);
 void launchTotals(const DState& s, double* partial, double* out, cudaStream_t st);
 void launchCheckFinite(const DState& s, unsigned long long* first_bad, cudaStream_t st);
 void launchAddGravity(const DState& s, cudaStream_t st);

@@ -176,6 +176,7 @@ void dumpMaterials(Writer& w, Storage& s) {
     std::vector<uint32_t> mat(s.getParticleCnt(), 0);
     std::vector<double> ranges;
     std::vector<double> young;
+    std::vector<double> minimals;
     for (Size k = 0; k < s.getMaterialCnt(); ++k) {
         MaterialView mv = s.getMaterial(k);
         for (Size i : mv.sequence()) {
@@ -187,10 +188,16 @@ void dumpMaterials(Writer& w, Storage& s) {
             ranges.push_back(range.upper());
         }
         young.push_back(mv->getParam<Float>(BodySettingsId::YOUNG_MODULUS));
+        // IMaterial::minimal of the first-order quantities (DerivativeCriterion)
+        for (QuantityId id :
+            { QuantityId::DENSITY, QuantityId::ENERGY, QuantityId::DEVIATORIC_STRESS, QuantityId::DAMAGE }) {
+            minimals.push_back(mv->minimal(id));
+        }
     }
     w.u32("mat", mat);
     w.f64("mat_ranges", ranges);
     w.f64("mat_young", young);
+    w.f64("mat_minimals", minimals);
 }
 
 void randomVelocities(Storage& s, uint64_t seed, double sigma) {
@@ -236,6 +243,10 @@ void runSteps(Writer& w, RunSettings& settings, SharedPtr<Storage> storage, int 
     dumpState(w, "sN_", *storage);
 }
 
+// the time-step criteria of the golden runs: COURANT, or every criterion (the reference's default ALL) when
+// the mode name ends in "_all"
+bool gAllCriteria = false;
+
 RunSettings baseSettings() {
     RunSettings settings;
     settings.set(RunSettingsId::RUN_THREAD_CNT, 1);
@@ -247,7 +258,11 @@ RunSettings baseSettings() {
     settings.set(RunSettingsId::GRAVITY_MULTIPOLE_ORDER, 3);
     settings.set(RunSettingsId::GRAVITY_KERNEL, GravityKernelEnum::SPH_KERNEL);
     settings.set(RunSettingsId::TIMESTEPPING_INTEGRATOR, TimesteppingEnum::PREDICTOR_CORRECTOR);
-    settings.set(RunSettingsId::TIMESTEPPING_CRITERION, TimeStepCriterionEnum::COURANT);
+    if (gAllCriteria) {
+        settings.set(RunSettingsId::TIMESTEPPING_CRITERION, TimeStepCriterionEnum::ALL);
+    } else {
+        settings.set(RunSettingsId::TIMESTEPPING_CRITERION, TimeStepCriterionEnum::COURANT);
+    }
     return settings;
 }
 
@@ -435,7 +450,11 @@ int main(int argc, char** argv) {
         return 2;
     }
     Writer w(argv[1]);
-    const std::string mode = argv[2];
+    std::string mode = argv[2];
+    if (mode.size() > 4 && mode.compare(mode.size() - 4, 4, "_all") == 0) {
+        gAllCriteria = true;
+        mode = mode.substr(0, mode.size() - 4);
+    }
     auto arg = [&](int k, double dflt) { return argc > k ? std::atof(argv[k]) : dflt; };
     try {
         if (mode == "sphere") {

@@ -1309,14 +1309,88 @@ const double* rangeOf(const sphgpu_material& mt, int k) {
     return k == 0 ? mt.density_range : (k == 1 ? mt.energy_range : mt.damage_range);
 }
 
-double courant(const sphgpu_config& cfg, const ora_state& s) {
+// MultiCriterion::compute (core/timestepping/TimeStepCriterion.cpp:331-389) over the criteria of the settings:
+// CourantCriterion (:294-329), DerivativeCriterion with the minimal step (:139-206), AccelerationCriterion
+// (:212-246), DivergenceCriterion (:252-288); each capped by the maximal step, then the smoothing by max_change
+// against the previous step.
+double criterionStep(const sphgpu_config& cfg, const ora_state& s, double lastStep) {
+    const uint32_t crit = cfg.timestep_criteria ? cfg.timestep_criteria : uint32_t(SPHGPU_CRITERION_COURANT);
+    const bool solid = (cfg.forces & SPHGPU_FORCE_SOLID_STRESS) != 0;
+    auto capped = [&](double step) { return step > cfg.max_timestep ? cfg.max_timestep : step; };
     double minStep = INFTY;
-    for (uint64_t i = 0; i < s.n; ++i) {
-        if (s.cs[i] > 0.) {
-            minStep = std::min(minStep, cfg.courant_number * s.r[4 * i + 3] / s.cs[i]);
+    if (crit & SPHGPU_CRITERION_COURANT) {
+        double m = INFTY;
+        for (uint64_t i = 0; i < s.n; ++i) {
+            if (s.cs[i] > 0.) {
+                m = std::min(m, cfg.courant_number * s.r[4 * i + 3] / s.cs[i]);
+            }
         }
+        minStep = std::min(minStep, capped(m));
     }
-    return minStep > cfg.max_timestep ? cfg.max_timestep : minStep;
+    bool anyDamage = false;
+    for (uint32_t k = 0; k < cfg.material_count; ++k) {
+        anyDamage = anyDamage ||
+                    (cfg.materials[k].yielding != SPHGPU_YIELDING_NONE && cfg.materials[k].damage != SPHGPU_DAMAGE_NONE);
+    }
+    if (crit & SPHGPU_CRITERION_DERIVATIVES) {
+        const double f = cfg.derivative_factor;
+        double m = INFTY;
+        auto add = [&](double v, double dv, double minValue) {
+            const double av = std::abs(v), adv = std::abs(dv);
+            if (std::abs(av) < 2. * minValue) {
+                return;
+            }
+            m = std::min(m, f * (av + minValue) / (adv + EPS));
+        };
+        for (uint64_t i = 0; i < s.n; ++i) {
+            const sphgpu_material& mt = cfg.materials[cfg.material_count > 1 ? s.mat[i] : 0];
+            add(s.rho[i], s.drho[i], mt.density_min);
+            add(s.u[i], s.du[i], mt.energy_min);
+            if (solid && s.S) {
+                const double* S = s.S;
+                const double* dS = s.dS;
+                const uint64_t n = s.n;
+                // TracelessTensor components xx, yy, zz, xy, xz, yz (getComponents, TracelessTensor.h:393)
+                const double sv[6] = { S[i], S[n + i], -S[i] - S[n + i], S[2 * n + i], S[3 * n + i], S[4 * n + i] };
+                const double dsv[6] = { dS[i], dS[n + i], -dS[i] - dS[n + i], dS[2 * n + i], dS[3 * n + i],
+                    dS[4 * n + i] };
+                for (int c = 0; c < 6; ++c) {
+                    add(sv[c], dsv[c], mt.stress_min);
+                }
+            }
+            // DAMAGE is a first-order quantity of the whole storage when any material has a fracture model
+            if (solid && anyDamage && s.D && s.dD) {
+                add(s.D[i], s.dD[i], mt.damage_min);
+            }
+        }
+        minStep = std::min(minStep, capped(m));
+    }
+    if (crit & SPHGPU_CRITERION_ACCELERATION) {
+        double m = INFTY;
+        for (uint64_t i = 0; i < s.n; ++i) {
+            const double ax = s.dv[4 * i], ay = s.dv[4 * i + 1], az = s.dv[4 * i + 2];
+            const double a2 = ax * ax + ay * ay + az * az;
+            if (a2 > EPS) {
+                const double h = s.r[4 * i + 3];
+                m = std::min(m, cfg.derivative_factor * std::sqrt(std::sqrt(h * h / a2)));
+            }
+        }
+        minStep = std::min(minStep, capped(m));
+    }
+    if (crit & SPHGPU_CRITERION_DIVERGENCE) {
+        double m = INFTY;
+        for (uint64_t i = 0; i < s.n; ++i) {
+            const double dv = std::abs(s.divv[i]);
+            if (dv > EPS) {
+                m = std::min(m, cfg.divergence_factor / dv);
+            }
+        }
+        minStep = std::min(minStep, capped(m));
+    }
+    if (cfg.max_change < INFTY) {
+        minStep = std::min(minStep, lastStep * (1. + cfg.max_change));
+    }
+    return minStep;
 }
 
 void stepPC(const sphgpu_config& cfg, ora_state& s, double dt) {
@@ -1536,7 +1610,7 @@ int ora_run(const sphgpu_config* cfg, ora_state* s, uint32_t nsteps, double* dt,
         } else {
             stepPC(*cfg, *s, *dt);
         }
-        *dt = courant(*cfg, *s);
+        *dt = criterionStep(*cfg, *s, *dt);
     }
     return SPHGPU_OK;
 }

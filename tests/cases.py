@@ -22,7 +22,14 @@ def load(name):
 
 
 def kind(fx):
-    return str(fx["driver_args"]).split()[0]
+    """Physics of the fixture (sphere, impact, gas, ...), without the "_all" suffix of the runs with every
+    time-step criterion."""
+    k = str(fx["driver_args"]).split()[0]
+    return k[:-4] if k.endswith("_all") else k
+
+
+def all_criteria(fx):
+    return str(fx["driver_args"]).split()[0].endswith("_all")
 
 
 def materials_of(fx):
@@ -42,6 +49,9 @@ def materials_of(fx):
         m.energy_range[:] = rg[2:4]
         m.damage_range[:] = rg[4:6]
         m.young_modulus = float(fx["mat_young"][i])
+        if "mat_minimals" in fx:
+            m.density_min, m.energy_min, m.stress_min, m.damage_min = (float(x) for x in
+                                                                       fx["mat_minimals"][4 * i:4 * i + 4])
         mats.append(m)
     return mats
 
@@ -50,15 +60,17 @@ def config_of(fx, precision=abi.PRECISION_FP64):
     k = kind(fx)
     n = len(fx["s0_m"])
     mats = materials_of(fx)
+    crit = abi.CRITERION_ALL if all_criteria(fx) else abi.CRITERION_COURANT
     if k == "sphere":
         return abi.make_config(n, mats, forces=abi.FORCE_PRESSURE | abi.FORCE_SELF_GRAVITY,
-                               gravity_constant=float(fx["G"][0]), precision=precision)
+                               gravity_constant=float(fx["G"][0]), precision=precision, timestep_criteria=crit)
     if k == "impact":
         return abi.make_config(n, mats, forces=abi.FORCE_PRESSURE | abi.FORCE_SOLID_STRESS | abi.FORCE_SELF_GRAVITY,
-                               adaptive_h=True, gravity_constant=float(fx["G"][0]), precision=precision)
+                               adaptive_h=True, gravity_constant=float(fx["G"][0]), precision=precision,
+                               timestep_criteria=crit)
     if k == "gas":
         return abi.make_config(n, mats, forces=abi.FORCE_PRESSURE, integrator=abi.INTEGRATOR_LEAP_FROG,
-                               initial_timestep=1e-3, precision=precision)
+                               initial_timestep=1e-3, precision=precision, timestep_criteria=crit)
     raise ValueError(k)
 
 

@@ -35,7 +35,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_abi_version():
     lib = ctypes.CDLL(_lib_path())
-    assert lib.sphgpu_abi_version() == 1
+    assert lib.sphgpu_abi_version() == 2
 
 
 def test_struct_layout_matches_header(tmp_path):

@@ -51,7 +51,7 @@ def test_autograd_wrapper_matches_abi_and_references():
     with ac.solver_for(st) as g:
         direct_loss = g.adjoint_forward(ac.config(nt))
         direct = g.adjoint_backward(3.0)
-    assert float(loss) == direct_loss
+    assert float(loss.detach()) == direct_loss
     np.testing.assert_array_equal(gr.numpy(), direct["r"])
     np.testing.assert_array_equal(gv.numpy(), direct["v"])
     assert float(ga) == direct["alpha"]

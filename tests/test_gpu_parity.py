@@ -158,7 +158,8 @@ def test_integrate_matches_reference(name):
     np.testing.assert_array_equal(got["ncnt"], fx["d0_ncnt"])
 
 
-@pytest.mark.parametrize("name", ["sphere_n1000", "impact_n1200", "gas_n1500"])
+@pytest.mark.parametrize("name", ["sphere_n1000", "impact_n1200", "gas_n1500", "impact_all_n1200",
+                                  "gas_all_n1500"])
 def test_steps_match_reference(name):
     fx = cases.load(name)
     cfg, keep = cases.config_of(fx)
@@ -175,6 +176,34 @@ def test_steps_match_reference(name):
     for f in ["r", "v", "dv", "rho", "drho", "u", "du", "divv", "S", "dS", "D", "dD"]:
         if "sN_" + f in fx:
             assert cases.scale_err(got[f], fx["sN_" + f]) < TOL_STEPS, f
+
+
+@pytest.mark.parametrize("crit", ["DERIVATIVES", "ACCELERATION", "DIVERGENCE", "ALL"])
+def test_timestep_criteria_match_oracle(crit):
+    # each criterion alone (and all together, with the max-change smoothing) against the oracle, whose
+    # criteria are pinned to the reference by the *_all fixtures; on the gas run each one limits the step
+    # (the derivative criterion once the minimal values are below the density and energy of the gas)
+    fx = cases.load("gas_n1500")
+    cfg, keep = cases.config_of(fx)
+    cfg.timestep_criteria = getattr(abi, "CRITERION_" + crit)
+    if crit == "DERIVATIVES":
+        for m in keep:
+            m.density_min = 0.1
+            m.energy_min = 0.1
+    if crit == "ALL":
+        cfg.max_change = 0.5
+    steps = 4
+    dt0 = float(fx["dts"][0])
+    st = cases.state_of(fx, "s0_")
+    _, odts = oracle.run(cfg, {k: v.copy() for k, v in st.items()}, steps + 1, dt0)
+    with GpuSolver(cfg, keep) as g:
+        g.set_state(st)
+        g.timestep = dt0
+        dts = []
+        for _ in range(steps):
+            g.step(1)
+            dts.append(g.timestep)
+    np.testing.assert_allclose(dts, odts[1:steps + 1], rtol=1e-10)
 
 
 def test_deterministic_fp64():

@@ -116,7 +116,8 @@ def test_integrate_matches_reference(name):
     np.testing.assert_array_equal(st["ncnt"], fx["d0_ncnt"])
 
 
-@pytest.mark.parametrize("name", ["sphere_n1000", "impact_n1200", "gas_n1500"])
+@pytest.mark.parametrize("name", ["sphere_n1000", "impact_n1200", "gas_n1500", "impact_all_n1200",
+                                  "gas_all_n1500"])
 def test_steps_match_reference(name):
     fx = cases.load(name)
     cfg, keep = cases.config_of(fx)

@@ -51,6 +51,7 @@ enum {
     SPHGPU_Q_STRESS_REDUCING = 16,     /* double */
     SPHGPU_Q_VELOCITY_GRADIENT = 26,   /* symmetric tensor */
     SPHGPU_Q_VELOCITY_DIVERGENCE = 27, /* double */
+    SPHGPU_Q_STRAIN_RATE_CORRECTION_TENSOR = 29, /* symmetric tensor (read only; with correction_tensor) */
     SPHGPU_Q_NEIGHBOR_CNT = 38,        /* uint32 */
     SPHGPU_Q_FLAG = 42,                /* uint32 */
     SPHGPU_Q_MATERIAL_ID = 43          /* uint32, index into sphgpu_config.materials */
@@ -67,6 +68,10 @@ enum { SPHGPU_EOS_TILLOTSON = 0, SPHGPU_EOS_IDEAL_GAS = 1 };
 enum { SPHGPU_YIELDING_NONE = 0, SPHGPU_YIELDING_VON_MISES = 1 };
 enum { SPHGPU_DAMAGE_NONE = 0, SPHGPU_DAMAGE_SCALAR_GRADY_KIPP = 1 };
 enum { SPHGPU_INTEGRATOR_PREDICTOR_CORRECTOR = 0, SPHGPU_INTEGRATOR_LEAP_FROG = 1 };
+/* SolverEnum (core/system/Settings.h:707-729): SymmetricSolver or AsymmetricSolver. Both sum each particle's
+ * neighbours in the same gather kernels here; they differ in the reference's summation order only, and the
+ * asymmetric solver admits the strain-rate correction tensor. */
+enum { SPHGPU_SOLVER_SYMMETRIC = 0, SPHGPU_SOLVER_ASYMMETRIC = 1 };
 /* GravityKernelEnum (core/system/Settings.h): point masses or the gravity kernel of the SPH kernel */
 enum { SPHGPU_GRAVITY_KERNEL_POINT_PARTICLES = 0, SPHGPU_GRAVITY_KERNEL_SPH_KERNEL = 1 };
 /* Time-step criteria: the reference's TimeStepCriterionEnum bits (core/system/Settings.h:577-592), evaluated
@@ -130,7 +135,7 @@ typedef struct {
     int32_t sum_only_undamaged;
     int32_t gravity_multipole_order;   /* 0 (monopole), 2 (quadrupole) or 3 (octupole) */
     int32_t gravity_kernel;            /* SPHGPU_GRAVITY_KERNEL_* */
-    int32_t reserved0;
+    int32_t solver_type;               /* SPHGPU_SOLVER_* */
     double gravity_constant;
     double gravity_opening_angle;
     uint32_t gravity_leaf_size;
@@ -141,7 +146,8 @@ typedef struct {
     int32_t precision;                 /* SPHGPU_PRECISION_* */
     int32_t device;                    /* CUDA device ordinal */
     uint32_t timestep_criteria;        /* SPHGPU_CRITERION_* bits; 0 = Courant only */
-    int32_t reserved1;
+    int32_t correction_tensor;         /* SPH_STRAIN_RATE_CORRECTION_TENSOR (CorrectionTensor, core/sph/equations/
+                                        * Derivative.cpp:36-74); asymmetric solver with solid stress only */
     double derivative_factor;          /* TIMESTEPPING_DERIVATIVE_FACTOR (0.2), also the acceleration factor */
     double divergence_factor;          /* TIMESTEPPING_DIVERGENCE_FACTOR (0.005) */
     double max_change;                 /* TIMESTEPPING_MAX_INCREASE: relative growth limit per step, INFINITY = off */

@@ -32,6 +32,7 @@ Q_N_FLAWS = 14
 Q_STRESS_REDUCING = 16
 Q_VELOCITY_GRADIENT = 26
 Q_VELOCITY_DIVERGENCE = 27
+Q_STRAIN_RATE_CORRECTION_TENSOR = 29
 Q_NEIGHBOR_CNT = 38
 Q_FLAG = 42
 Q_MATERIAL_ID = 43
@@ -52,6 +53,9 @@ GRAVITY_KERNEL_POINT_PARTICLES = 0
 GRAVITY_KERNEL_SPH_KERNEL = 1
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
+
+SOLVER_SYMMETRIC = 0
+SOLVER_ASYMMETRIC = 1
 
 CRITERION_COURANT = 1 << 1
 CRITERION_DERIVATIVES = 1 << 2
@@ -76,6 +80,7 @@ QUANTITY_LAYOUT = {
     Q_STRESS_REDUCING: (1, "f8"),
     Q_VELOCITY_GRADIENT: (6, "f8"),
     Q_VELOCITY_DIVERGENCE: (1, "f8"),
+    Q_STRAIN_RATE_CORRECTION_TENSOR: (6, "f8"),
     Q_NEIGHBOR_CNT: (1, "u4"),
     Q_FLAG: (1, "u4"),
     Q_MATERIAL_ID: (1, "u4"),
@@ -126,7 +131,7 @@ class Config(ctypes.Structure):
         ("sum_only_undamaged", ctypes.c_int32),
         ("gravity_multipole_order", ctypes.c_int32),
         ("gravity_kernel", ctypes.c_int32),
-        ("reserved0", ctypes.c_int32),
+        ("solver_type", ctypes.c_int32),
         ("gravity_constant", ctypes.c_double),
         ("gravity_opening_angle", ctypes.c_double),
         ("gravity_leaf_size", ctypes.c_uint32),
@@ -137,7 +142,7 @@ class Config(ctypes.Structure):
         ("precision", ctypes.c_int32),
         ("device", ctypes.c_int32),
         ("timestep_criteria", ctypes.c_uint32),
-        ("reserved1", ctypes.c_int32),
+        ("correction_tensor", ctypes.c_int32),
         ("derivative_factor", ctypes.c_double),
         ("divergence_factor", ctypes.c_double),
         ("max_change", ctypes.c_double),

@@ -145,6 +145,12 @@ DeviceState::DeviceState(const RunSettings& settings, const Storage& storage, in
         crit.has(TimeStepCriterionEnum::DERIVATIVES)) {
         raise(true, "GPU path implements the minimal-step derivative criterion only (timestep.mean_power = -inf)");
     }
+    const SolverEnum solver = settings.get<SolverEnum>(RunSettingsId::SPH_SOLVER_TYPE);
+    if (solver != SolverEnum::SYMMETRIC_SOLVER && solver != SolverEnum::ASYMMETRIC_SOLVER) {
+        raise(true, "GPU path implements the symmetric and asymmetric solvers");
+    }
+    config.solver_type = solver == SolverEnum::ASYMMETRIC_SOLVER ? SPHGPU_SOLVER_ASYMMETRIC : SPHGPU_SOLVER_SYMMETRIC;
+    config.correction_tensor = settings.get<bool>(RunSettingsId::SPH_STRAIN_RATE_CORRECTION_TENSOR) ? 1 : 0;
     config.precision = precision;
     config.device = 0;
     const int rc = sphgpu_create(&config, &handle);

@@ -270,6 +270,11 @@ bool slotOf(sphgpu_handle* h, int id, int order, QuantitySlot& q) {
     case SPHGPU_Q_VELOCITY_DIVERGENCE:
         q.dev = s.divv;
         return order == 0;
+    case SPHGPU_Q_STRAIN_RATE_CORRECTION_TENSOR:
+        q.comps = 6;
+        q.soa = true;
+        q.dev = s.corr;
+        return order == 0;
     case SPHGPU_Q_NEIGHBOR_CNT:
         q.bytes = 4;
         q.dev = s.ncnt;
@@ -341,6 +346,15 @@ void evalSph(sphgpu_handle* h, bool gravityInLoop) {
     Phase ph(h, SPHGPU_PHASE_SPH_EVAL);
     Physics phs = h->ph;
     phs.gravity = gravityInLoop ? h->ph.gravity : 0;
+    if (h->ph.correction) {
+        // CorrectionTensor is a PRECOMPUTE derivative: every C_i before the velocity gradients
+        if (h->ph.precision == SPHGPU_PRECISION_MIXED) {
+            launchCorrectionMixed(h->s, h->grid, phs, h->d_lut_sph_f, h->stream);
+        } else {
+            launchCorrection64(h->s, h->grid, phs, h->d_lut_sph, h->stream);
+        }
+        h->launches += 1;
+    }
     if (h->ph.precision == SPHGPU_PRECISION_MIXED) {
         launchPairSumMixed(h->s, h->grid, phs, h->d_mats, h->d_lut_sph_f, h->stream);
     } else {
@@ -352,9 +366,10 @@ void evalSph(sphgpu_handle* h, bool gravityInLoop) {
 // the derivative evaluation of ISolver::integrate after the materials were initialized. With self-gravity
 // the order of GravitySolver::loop (core/sph/solvers/GravitySolver.cpp:64-91: gravity into the accumulator,
 // then the pair loop) is kept in the arithmetic, not in time: the pair loop (main stream) and the tree build
-// + walk (gravity stream, higher priority) run concurrently, and after both dv = a_gravity + a_sph, the same
-// sum the reference forms. The pair loop is queued first because the tree build waits on the host for
-// its own stream between levels.
+// + walk (gravity stream, higher priority) run concurrently, and after both dv = a_gravity + a_sph: the same
+// terms as the reference's accumulator, with the gravity term added after the pair sum instead of before it
+// (a difference of rounding only). The pair loop is queued first because the tree build waits on the host
+// for its own stream between levels.
 sphgpu_status evalDerivatives(sphgpu_handle* h) {
     if (!h->ph.gravity) {
         evalSph(h, false);
@@ -408,6 +423,14 @@ sphgpu_status validate(const sphgpu_config* c) {
     }
     if (c->precision != SPHGPU_PRECISION_FP64 && c->precision != SPHGPU_PRECISION_MIXED) {
         return fail(nullptr, SPHGPU_ERR_UNSUPPORTED, "unknown precision %d", c->precision);
+    }
+    if (c->solver_type != SPHGPU_SOLVER_SYMMETRIC && c->solver_type != SPHGPU_SOLVER_ASYMMETRIC) {
+        return fail(nullptr, SPHGPU_ERR_UNSUPPORTED, "unknown solver type %d", c->solver_type);
+    }
+    if (c->correction_tensor &&
+        (c->solver_type != SPHGPU_SOLVER_ASYMMETRIC || !(c->forces & SPHGPU_FORCE_SOLID_STRESS))) {
+        return fail(nullptr, SPHGPU_ERR_UNSUPPORTED,
+            "the correction tensor needs the asymmetric solver and the solid stress force");
     }
     if (c->timestep_criteria & ~uint32_t(SPHGPU_CRITERION_ALL)) {
         return fail(nullptr, SPHGPU_ERR_UNSUPPORTED, "unknown time-step criterion bits 0x%x", c->timestep_criteria);
@@ -507,6 +530,7 @@ sphgpu_status sphgpu_create(const sphgpu_config* config, sphgpu_handle** out) {
     ph.derivative_factor = config->derivative_factor;
     ph.divergence_factor = config->divergence_factor;
     ph.max_change = config->max_change;
+    ph.correction = config->correction_tensor ? 1 : 0;
     (void)anyRheology;
 
     cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
@@ -554,6 +578,9 @@ sphgpu_status sphgpu_create(const sphgpu_config* config, sphgpu_handle** out) {
         A(&s.dS, 5 * nn);
         A(&s.pdS, 5 * nn);
         A(&s.gradv, 6 * nn);
+        if (ph.correction) {
+            A(&s.corr, 6 * nn);
+        }
         A(&s.reduce, nn);
     }
     if (ph.damage) {
@@ -580,7 +607,7 @@ sphgpu_status sphgpu_create(const sphgpu_config* config, sphgpu_handle** out) {
         e = cudaMallocHost((void**)&h->h_pinned, 64 * sizeof(unsigned long long));
     }
     if (e == cudaSuccess) {
-        e = gridAllocate(h->grid, n, ph.solid != 0);
+        e = gridAllocate(h->grid, n, ph.solid != 0, ph.correction != 0);
     }
     if (e == cudaSuccess && ph.gravity) {
         e = treeAllocate(h->tree, n, ph.leaf_size);

@@ -249,7 +249,7 @@ __global__ void pairsKernel(uint32_t n, const dbl4* __restrict__ rs, const uint3
 
 } // namespace
 
-cudaError_t gridAllocate(Grid& g, uint32_t n, bool solid) {
+cudaError_t gridAllocate(Grid& g, uint32_t n, bool solid, bool correction) {
     const uint32_t nn = n > 0 ? n : 1;
     g.cell_capacity = max(1u << 12, min(4u * nn, 1u << 26));
     cudaError_t e = cudaSuccess;
@@ -282,6 +282,9 @@ cudaError_t gridAllocate(Grid& g, uint32_t n, bool solid) {
         alloc((void**)&g.flags, nn * sizeof(uint32_t));
         alloc((void**)&g.mxS, 5 * size_t(nn) * sizeof(float));
     }
+    if (correction) {
+        alloc((void**)&g.mxC, 6 * size_t(nn) * sizeof(float));
+    }
     if (e != cudaSuccess) {
         return e;
     }
@@ -297,7 +300,7 @@ cudaError_t gridAllocate(Grid& g, uint32_t n, bool solid) {
 void gridFree(Grid& g) {
     void* ptrs[] = { g.info, g.bounds, g.keys, g.keys_sorted, g.perm_in, g.perm, g.cell_start, g.cell_end,
         g.sort_temp, g.rs, g.vs, g.ms, g.rhos, g.ps, g.css, g.Ss, g.reduces, g.flags, g.mx0, g.mx1, g.mx2, g.mx3,
-        g.mxS };
+        g.mxS, g.mxC };
     for (void* p : ptrs) {
         if (p) {
             cudaFree(p);

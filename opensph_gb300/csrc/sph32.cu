@@ -39,6 +39,87 @@ __device__ __forceinline__ float lutGradF(const float* __restrict__ lut, float q
     return g0 + (g1 - g0) * ratio;
 }
 
+// CorrectionTensor::evalNeighs (core/sph/equations/Derivative.cpp:36-74) in mixed precision: the sum of
+// m_j / rho_j sym((r_j - r_i) x grad W_ij) in FP32 with compensation, its determinant and inverse in FP64; the
+// result is written in FP64 (particle order, the quantity) and FP32 (cell order, for the pair loop).
+__global__ void __launch_bounds__(128) correctionMixedKernel(DState s, Grid g, Physics ph,
+    const float* __restrict__ lut) {
+    const uint32_t n = s.n;
+    const uint32_t si = blockIdx.x * blockDim.x + threadIdx.x;
+    if (si >= n) {
+        return;
+    }
+    const GridInfo* gi = g.info;
+    const float4 pi0 = g.mx0[si], pi3 = g.mx3[si];
+    const float cellf = float(gi->cell);
+    Kahan c[6];
+    const int dxc = gi->dims[0], dyc = gi->dims[1], dzc = gi->dims[2];
+    const uint32_t key = g.keys_sorted[si];
+    const int cx = int(key % uint32_t(dxc)), cy = int((key / uint32_t(dxc)) % uint32_t(dyc)),
+              cz = int(key / (uint32_t(dxc) * uint32_t(dyc)));
+    for (int off = 0; off < 27; ++off) {
+        const int ox = off % 3 - 1, oy = (off / 3) % 3 - 1, oz = off / 9 - 1;
+        const int x = cx + ox, y = cy + oy, z = cz + oz;
+        if (x < 0 || x >= dxc || y < 0 || y >= dyc || z < 0 || z >= dzc) {
+            continue;
+        }
+        const uint32_t cell = (uint32_t(z) * uint32_t(dyc) + uint32_t(y)) * uint32_t(dxc) + uint32_t(x);
+        const uint32_t te = g.cell_end[cell];
+        const float sx = float(ox) * cellf, sy = float(oy) * cellf, sz = float(oz) * cellf;
+        for (uint32_t t = g.cell_start[cell]; t < te; ++t) {
+            if (t == si) {
+                continue;
+            }
+            const float4 pj0 = g.mx0[t];
+            const float drx = (pi0.x - pj0.x) - sx, dry = (pi0.y - pj0.y) - sy, drz = (pi0.z - pj0.z) - sz;
+            const float d2 = drx * drx + dry * dry + drz * drz;
+            const float hbar = 0.5f * (pi0.w + pj0.w);
+            const float rad = 2.f * hbar;
+            if (!(d2 < rad * rad)) {
+                continue;
+            }
+            const float4 pj3 = g.mx3[t];
+            if (ph.sum_only_undamaged &&
+                !(__float_as_uint(pi3.w) == __float_as_uint(pj3.w) && pi3.z != 0.f && pj3.z != 0.f)) {
+                continue;
+            }
+            const float4 pj1 = g.mx1[t], pj2 = g.mx2[t];
+            const float hInv = 1.f / hbar;
+            const float h2 = hInv * hInv;
+            const float gl = lutGradF(lut, d2 * h2) * (h2 * h2 * hInv);
+            const float gx = drx * gl, gy = dry * gl, gz = drz * gl;
+            const float f = pj1.w / pj2.w;
+            c[0].add(f * (-drx * gx));
+            c[1].add(f * (-dry * gy));
+            c[2].add(f * (-drz * gz));
+            c[3].add(f * (-0.5f * (drx * gy + dry * gx)));
+            c[4].add(f * (-0.5f * (drx * gz + drz * gx)));
+            c[5].add(f * (-0.5f * (dry * gz + drz * gy)));
+        }
+    }
+    double cd[6];
+    for (int k = 0; k < 6; ++k) {
+        cd[k] = c[k].value();
+    }
+    const bool isNull = cd[0] == 0. && cd[1] == 0. && cd[2] == 0. && cd[3] == 0. && cd[4] == 0. && cd[5] == 0.;
+    const double det = cd[0] * cd[1] * cd[2] + 2. * cd[3] * cd[4] * cd[5] -
+                       (cd[3] * cd[3] * cd[2] + cd[4] * cd[4] * cd[1] + cd[5] * cd[5] * cd[0]);
+    double inv[6] = { 1., 1., 1., 0., 0., 0. };
+    if (!isNull && det > 0.01) {
+        inv[0] = (cd[1] * cd[2] - cd[5] * cd[5]) / det;
+        inv[1] = (cd[2] * cd[0] - cd[4] * cd[4]) / det;
+        inv[2] = (cd[0] * cd[1] - cd[3] * cd[3]) / det;
+        inv[3] = (cd[4] * cd[5] - cd[2] * cd[3]) / det;
+        inv[4] = (cd[5] * cd[3] - cd[1] * cd[4]) / det;
+        inv[5] = (cd[3] * cd[4] - cd[0] * cd[5]) / det;
+    }
+    const uint32_t i = g.perm[si];
+    for (int k = 0; k < 6; ++k) {
+        s.corr[k * n + i] = inv[k];
+        g.mxC[k * n + si] = float(inv[k]);
+    }
+}
+
 // Candidates of the 27 cells are first tested (cheap: one float4 load and a distance test per candidate,
 // every lane busy) and the interacting ones queued per lane in shared memory; the pair terms are then
 // evaluated from the queues, when any lane's queue is full and at the end. The pair terms thus run with
@@ -69,6 +150,13 @@ __global__ void __launch_bounds__(PAIR_THREADS) pairSumMixedKernel(DState s, Gri
     const float alpha = float(ph.av_alpha), beta = float(ph.av_beta);
     Kahan ax, ay, az, du, divv;
     Kahan gv[6];
+    // strain-rate correction tensor of the velocity gradient (identity without it)
+    float Ci[6] = { 1.f, 1.f, 1.f, 0.f, 0.f, 0.f };
+    if (Solid && ph.correction) {
+        for (int k = 0; k < 6; ++k) {
+            Ci[k] = g.mxC[k * n + sv];
+        }
+    }
     uint32_t cnt = 0;
     const int dxc = gi->dims[0], dyc = gi->dims[1], dzc = gi->dims[2];
     const uint32_t key = g.keys_sorted[sv];
@@ -122,12 +210,18 @@ __global__ void __launch_bounds__(PAIR_THREADS) pairSumMixedKernel(DState s, Gri
                                        (__float_as_uint(pi3.w) == __float_as_uint(pj3.w) && pi3.z != 0.f &&
                                            pj3.z != 0.f);
                 if (undamaged) {
-                    gv[0].add(mr * (dvx * gx));
-                    gv[1].add(mr * (dvy * gy));
-                    gv[2].add(mr * (dvz * gz));
-                    gv[3].add(mr * (0.5f * (dvx * gy + dvy * gx)));
-                    gv[4].add(mr * (0.5f * (dvx * gz + dvz * gx)));
-                    gv[5].add(mr * (0.5f * (dvy * gz + dvz * gy)));
+                    float hx = gx, hy = gy, hz = gz;
+                    if (ph.correction) {
+                        hx = Ci[0] * gx + Ci[3] * gy + Ci[4] * gz;
+                        hy = Ci[3] * gx + Ci[1] * gy + Ci[5] * gz;
+                        hz = Ci[4] * gx + Ci[5] * gy + Ci[2] * gz;
+                    }
+                    gv[0].add(mr * (dvx * hx));
+                    gv[1].add(mr * (dvy * hy));
+                    gv[2].add(mr * (dvz * hz));
+                    gv[3].add(mr * (0.5f * (dvx * hy + dvy * hx)));
+                    gv[4].add(mr * (0.5f * (dvx * hz + dvz * hx)));
+                    gv[5].add(mr * (0.5f * (dvy * hz + dvz * hy)));
                     float tt[5];
                     for (int k = 0; k < 5; ++k) {
                         tt[k] = Sif[k] + g.mxS[k * n + t];
@@ -207,6 +301,12 @@ __global__ void __launch_bounds__(PAIR_THREADS) pairSumMixedKernel(DState s, Gri
 }
 
 } // namespace
+
+void launchCorrectionMixed(const DState& s, const Grid& g, const Physics& ph, const float* lut, cudaStream_t st) {
+    if (s.n) {
+        correctionMixedKernel<<<ceilDiv(s.n, 128), 128, 0, st>>>(s, g, ph, lut);
+    }
+}
 
 void launchPairSumMixed(const DState& s, const Grid& g, const Physics& ph, const MaterialD* mats, const float* lut,
     cudaStream_t st) {

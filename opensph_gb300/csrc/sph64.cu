@@ -52,6 +52,99 @@ __device__ __forceinline__ bool interacts64(const dbl4& a, const dbl4& b) {
     return d2 < rad * rad;
 }
 
+// Inverse of the correction-tensor sum, or the identity when the sum is null or nearly singular
+// (CorrectionTensor::evalNeighs, core/sph/equations/Derivative.cpp:59-72; SymmetricTensor::determinant /
+// inverse, core/objects/geometry/SymmetricTensor.h:193-231). c: xx, yy, zz, xy, xz, yz.
+__device__ __forceinline__ void invertCorrection(double c[6]) {
+    const bool isNull = c[0] == 0. && c[1] == 0. && c[2] == 0. && c[3] == 0. && c[4] == 0. && c[5] == 0.;
+    const double det = c[0] * c[1] * c[2] + 2. * c[3] * c[4] * c[5] - (c[3] * c[3] * c[2] + c[4] * c[4] * c[1] +
+                                                                         c[5] * c[5] * c[0]);
+    if (isNull || !(det > 0.01)) {
+        c[0] = c[1] = c[2] = 1.;
+        c[3] = c[4] = c[5] = 0.;
+        return;
+    }
+    const double d0 = c[1] * c[2] - c[5] * c[5];
+    const double d1 = c[2] * c[0] - c[4] * c[4];
+    const double d2 = c[0] * c[1] - c[3] * c[3];
+    const double o0 = c[4] * c[5] - c[2] * c[3];
+    const double o1 = c[5] * c[3] - c[1] * c[4];
+    const double o2 = c[3] * c[4] - c[0] * c[5];
+    c[0] = d0 / det;
+    c[1] = d1 / det;
+    c[2] = d2 / det;
+    c[3] = o0 / det;
+    c[4] = o1 / det;
+    c[5] = o2 / det;
+}
+
+// CorrectionTensor::evalNeighs (core/sph/equations/Derivative.cpp:36-74): C_i = (sum_j m_j / rho_j
+// sym((r_j - r_i) x grad W_ij))^-1 over the pairs the velocity gradient sums (the SUM_ONLY_UNDAMAGED filter)
+__global__ void __launch_bounds__(128) correction64Kernel(DState s, Grid g, Physics ph,
+    const double* __restrict__ lut) {
+    const uint32_t n = s.n;
+    const uint32_t si = blockIdx.x * blockDim.x + threadIdx.x;
+    if (si >= n) {
+        return;
+    }
+    const GridInfo* gi = g.info;
+    const uint32_t i = g.perm[si];
+    const dbl4 ri = g.rs[si];
+    const double redi = g.reduces[si];
+    const uint32_t flagi = g.flags[si];
+    double c[6] = { 0, 0, 0, 0, 0, 0 };
+    const int dxc = gi->dims[0], dyc = gi->dims[1], dzc = gi->dims[2];
+    const uint32_t key = g.keys_sorted[si];
+    const int cx = int(key % uint32_t(dxc)), cy = int((key / uint32_t(dxc)) % uint32_t(dyc)),
+              cz = int(key / (uint32_t(dxc) * uint32_t(dyc)));
+    for (int z = max(cz - 1, 0); z <= min(cz + 1, dzc - 1); ++z) {
+        for (int y = max(cy - 1, 0); y <= min(cy + 1, dyc - 1); ++y) {
+            const uint32_t rowBase = (uint32_t(z) * uint32_t(dyc) + uint32_t(y)) * uint32_t(dxc);
+            const uint32_t c0 = rowBase + uint32_t(max(cx - 1, 0));
+            const uint32_t c1 = rowBase + uint32_t(min(cx + 1, dxc - 1));
+            uint32_t tb = 0xffffffffu, tEnd = 0;
+            for (uint32_t cc = c0; cc <= c1; ++cc) {
+                const uint32_t cs0 = g.cell_start[cc], ce0 = g.cell_end[cc];
+                if (ce0 > cs0) {
+                    tb = min(tb, cs0);
+                    tEnd = max(tEnd, ce0);
+                }
+            }
+            for (uint32_t t = tb; t < tEnd; ++t) {
+                if (t == si) {
+                    continue;
+                }
+                const dbl4 rj = g.rs[t];
+                if (!interacts64(ri, rj)) {
+                    continue;
+                }
+                if (ph.sum_only_undamaged && (flagi != g.flags[t] || redi == 0. || g.reduces[t] == 0.)) {
+                    continue;
+                }
+                const double hbar = 0.5 * (ri.w + rj.w);
+                const double drx = ri.x - rj.x, dry = ri.y - rj.y, drz = ri.z - rj.z;
+                const double hInv = 1. / hbar;
+                const double h2 = hInv * hInv;
+                const double h5 = (h2 * h2) * hInv;
+                const double gl = lutGrad(lut, (drx * drx + dry * dry + drz * drz) * (hInv * hInv));
+                const double gx = (drx * h5) * gl, gy = (dry * h5) * gl, gz = (drz * h5) * gl;
+                const double ex = rj.x - ri.x, ey = rj.y - ri.y, ez = rj.z - ri.z;
+                const double f = g.ms[t] / g.rhos[t];
+                c[0] += f * (ex * gx);
+                c[1] += f * (ey * gy);
+                c[2] += f * (ez * gz);
+                c[3] += f * (0.5 * (ex * gy + ey * gx));
+                c[4] += f * (0.5 * (ex * gz + ez * gx));
+                c[5] += f * (0.5 * (ey * gz + ez * gy));
+            }
+        }
+    }
+    invertCorrection(c);
+    for (int k = 0; k < 6; ++k) {
+        s.corr[k * n + i] = c[k];
+    }
+}
+
 template <bool Solid>
 __global__ void __launch_bounds__(128) pairSum64Kernel(DState s, Grid g, Physics ph,
     const MaterialD* __restrict__ mats, const double* __restrict__ lut) {
@@ -86,6 +179,13 @@ __global__ void __launch_bounds__(128) pairSum64Kernel(DState s, Grid g, Physics
     double gv[6] = { 0, 0, 0, 0, 0, 0 };
     uint32_t cnt = 0;
     const double alpha = ph.av_alpha, beta = ph.av_beta;
+    // strain-rate correction tensor of the velocity gradient (identity without it)
+    double Ci[6] = { 1., 1., 1., 0., 0., 0. };
+    if (Solid && ph.correction) {
+        for (int k = 0; k < 6; ++k) {
+            Ci[k] = s.corr[k * n + i];
+        }
+    }
     const int dxc = gi->dims[0], dyc = gi->dims[1], dzc = gi->dims[2];
     const uint32_t key = g.keys_sorted[si];
     const int cx = int(key % uint32_t(dxc)), cy = int((key / uint32_t(dxc)) % uint32_t(dyc)),
@@ -156,12 +256,19 @@ __global__ void __launch_bounds__(128) pairSum64Kernel(DState s, Grid g, Physics
                         !ph.sum_only_undamaged || (flagi == g.flags[t] && redi != 0. && g.reduces[t] != 0.);
                     if (undamaged) {
                         const double f = mj / rhoi;
-                        gv[0] += f * (dvx * gx);
-                        gv[1] += f * (dvy * gy);
-                        gv[2] += f * (dvz * gz);
-                        gv[3] += f * (0.5 * (dvx * gy + dvy * gx));
-                        gv[4] += f * (0.5 * (dvx * gz + dvz * gx));
-                        gv[5] += f * (0.5 * (dvy * gz + dvz * gy));
+                        // C_i grad W (SymmetricTensor::operator*(Vector), SymmetricTensor.h:102-107)
+                        double hx = gx, hy = gy, hz = gz;
+                        if (ph.correction) {
+                            hx = Ci[0] * gx + Ci[3] * gy + Ci[4] * gz;
+                            hy = Ci[3] * gx + Ci[1] * gy + Ci[5] * gz;
+                            hz = Ci[4] * gx + Ci[5] * gy + Ci[2] * gz;
+                        }
+                        gv[0] += f * (dvx * hx);
+                        gv[1] += f * (dvy * hy);
+                        gv[2] += f * (dvz * hz);
+                        gv[3] += f * (0.5 * (dvx * hy + dvy * hx));
+                        gv[4] += f * (0.5 * (dvx * hz + dvz * hx));
+                        gv[5] += f * (0.5 * (dvy * hz + dvz * hy));
                         const double rhoj2 = rhoj * rhoj;
                         double tt[5];
                         for (int c = 0; c < 5; ++c) {
@@ -578,8 +685,8 @@ void launchTotals(const DState& s, double* partial, double* out, cudaStream_t st
     totalsFinish<<<1, 32, 0, st>>>(partial, out);
 }
 
-// dv = a_gravity + a_sph: the sum GravitySolver::loop forms (gravity first in the accumulator), for pair
-// loops that ran concurrently with the walk
+// dv = a_gravity + a_sph for pair loops that ran concurrently with the walk (GravitySolver::loop puts the gravity
+// term into the accumulator before the pair terms; here it is added to their sum)
 __global__ void addGravityKernel(DState s) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= s.n) {
@@ -592,6 +699,12 @@ __global__ void addGravityKernel(DState s) {
 void launchAddGravity(const DState& s, cudaStream_t st) {
     if (s.n) {
         addGravityKernel<<<ceilDiv(s.n, 256), 256, 0, st>>>(s);
+    }
+}
+
+void launchCorrection64(const DState& s, const Grid& g, const Physics& ph, const double* lut, cudaStream_t st) {
+    if (s.n) {
+        correction64Kernel<<<ceilDiv(s.n, 128), 128, 0, st>>>(s, g, ph, lut);
     }
 }
 

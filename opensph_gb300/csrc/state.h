@@ -48,6 +48,8 @@ struct DState {
     double* pdD;
     // self-gravity acceleration of the current evaluation
     dbl4* agrav;
+    // strain-rate correction tensor (6 x n: xx, yy, zz, xy, xz, yz), with the correction tensor only
+    double* corr;
 };
 
 // Physics switches and constants of one handle
@@ -73,6 +75,7 @@ struct Physics {
     double derivative_factor; // derivative and acceleration criteria
     double divergence_factor;
     double max_change;        // relative growth limit of the step (off when >= DBL_MAX)
+    int correction;           // strain-rate correction tensor applied to the velocity gradient
 };
 
 // Neighbour grid buffers (cell-sorted copies of the pair-loop inputs)
@@ -105,6 +108,7 @@ struct Grid {
     float4* mx2 = nullptr;     // vx_lo, vy_lo, vz_lo, rho
     float4* mx3 = nullptr;     // p / rho^2, cs, stress reducing, flag (bit pattern)
     float* mxS = nullptr;      // 5 x n: S / rho^2
+    float* mxC = nullptr;      // 6 x n: correction tensor (mixed path, cell-sorted)
     uint32_t launches = 0;     // own kernels launched by the last build / gather (library sort excluded)
 };
 
@@ -200,7 +204,7 @@ struct Tree {
 // ---- launchers (grid.cu) ----
 void launchGridBuild(const DState& s, Grid& g, const Physics& ph, cudaStream_t st);
 void launchGatherSorted(const DState& s, Grid& g, const Physics& ph, cudaStream_t st);
-cudaError_t gridAllocate(Grid& g, uint32_t n, bool solid);
+cudaError_t gridAllocate(Grid& g, uint32_t n, bool solid, bool correction = false);
 void gridFree(Grid& g);
 void launchCountPairs(const DState& s, const Grid& g, unsigned long long* count, cudaStream_t st);
 void launchListPairs(const DState& s, const Grid& g, uint32_t* pi, uint32_t* pj, unsigned long long* count,
@@ -223,6 +227,10 @@ void launchCheckFinite(const DState& s, unsigned long long* first_bad, cudaStrea
 void launchAddGravity(const DState& s, cudaStream_t st);
 void launchPairSumMixed(const DState& s, const Grid& g, const Physics& ph, const MaterialD* mats,
     const float* lut_grad_f, cudaStream_t st);
+// CorrectionTensor (core/sph/equations/Derivative.cpp:36-74) of every particle, before the pair loop
+void launchCorrection64(const DState& s, const Grid& g, const Physics& ph, const double* lut_grad, cudaStream_t st);
+void launchCorrectionMixed(const DState& s, const Grid& g, const Physics& ph, const float* lut_grad_f,
+    cudaStream_t st);
 
 // ---- launchers (gravity.cu) ----
 cudaError_t treeAllocate(Tree& t, uint32_t n, uint32_t leaf_size);

@@ -76,6 +76,7 @@ STATE_QUANTITIES = {
     "gradv": (abi.Q_VELOCITY_GRADIENT, 0), "reduce": (abi.Q_STRESS_REDUCING, 0), "D": (abi.Q_DAMAGE, 0),
     "dD": (abi.Q_DAMAGE, 1), "eps_min": (abi.Q_EPS_MIN, 0), "m_zero": (abi.Q_M_ZERO, 0),
     "growth": (abi.Q_EXPLICIT_GROWTH, 0), "n_flaws": (abi.Q_N_FLAWS, 0),
+    "corr": (abi.Q_STRAIN_RATE_CORRECTION_TENSOR, 0),
 }
 # inputs of a run (the outputs are recomputed by integrate/step)
 INPUT_FIELDS = ["r", "v", "dv", "m", "rho", "drho", "u", "du", "flag", "mat", "S", "dS", "reduce", "D", "dD",
@@ -159,6 +160,8 @@ class GpuSolver:
             if not self.solid and name in ("S", "dS", "reduce", "gradv"):
                 continue
             if not self._has_damage() and name in ("D", "dD", "eps_min", "m_zero", "growth", "n_flaws"):
+                continue
+            if name == "corr" and not self.config.correction_tensor:
                 continue
             out[name] = self.get_quantity(qid, order)
         return out

@@ -25,7 +25,7 @@ FIELDS = [
     ("divv", _F8, 1, "f8"), ("ncnt", _U4, 1, "u4"), ("flag", _U4, 1, "u4"), ("mat", _U4, 1, "u4"),
     ("S", _F8, 5, "f8"), ("dS", _F8, 5, "f8"), ("gradv", _F8, 6, "f8"), ("reduce", _F8, 1, "f8"),
     ("D", _F8, 1, "f8"), ("dD", _F8, 1, "f8"), ("eps_min", _F8, 1, "f8"), ("m_zero", _F8, 1, "f8"),
-    ("growth", _F8, 1, "f8"), ("n_flaws", _U4, 1, "u4"),
+    ("growth", _F8, 1, "f8"), ("n_flaws", _U4, 1, "u4"), ("corr", _F8, 6, "f8"),
 ]
 REQUIRED = ["r", "v", "dv", "m", "rho", "drho", "u", "du", "p", "cs", "divv", "ncnt", "flag", "mat"]
 SOLID = ["S", "dS", "gradv", "reduce"]

@@ -155,6 +155,9 @@ void dumpState(Writer& w, const std::string& pre, Storage& s) {
     if (s.has(QuantityId::VELOCITY_GRADIENT)) {
         w.f64(pre + "gradv", symmetric(s.getValue<SymmetricTensor>(QuantityId::VELOCITY_GRADIENT)));
     }
+    if (s.has(QuantityId::STRAIN_RATE_CORRECTION_TENSOR)) {
+        w.f64(pre + "corr", symmetric(s.getValue<SymmetricTensor>(QuantityId::STRAIN_RATE_CORRECTION_TENSOR)));
+    }
     if (s.has(QuantityId::DAMAGE)) {
         ArrayView<const Float> D, dD;
         tie(D, dD) = s.getAll<Float>(QuantityId::DAMAGE);
@@ -246,6 +249,8 @@ void runSteps(Writer& w, RunSettings& settings, SharedPtr<Storage> storage, int 
 // the time-step criteria of the golden runs: COURANT, or every criterion (the reference's default ALL) when
 // the mode name ends in "_all"
 bool gAllCriteria = false;
+// the AsymmetricSolver with the strain-rate correction tensor (mode name ending in "_asym")
+bool gAsymmetric = false;
 
 RunSettings baseSettings() {
     RunSettings settings;
@@ -262,6 +267,10 @@ RunSettings baseSettings() {
         settings.set(RunSettingsId::TIMESTEPPING_CRITERION, TimeStepCriterionEnum::ALL);
     } else {
         settings.set(RunSettingsId::TIMESTEPPING_CRITERION, TimeStepCriterionEnum::COURANT);
+    }
+    if (gAsymmetric) {
+        settings.set(RunSettingsId::SPH_SOLVER_TYPE, SolverEnum::ASYMMETRIC_SOLVER);
+        settings.set(RunSettingsId::SPH_STRAIN_RATE_CORRECTION_TENSOR, true);
     }
     return settings;
 }
@@ -454,6 +463,10 @@ int main(int argc, char** argv) {
     if (mode.size() > 4 && mode.compare(mode.size() - 4, 4, "_all") == 0) {
         gAllCriteria = true;
         mode = mode.substr(0, mode.size() - 4);
+    }
+    if (mode.size() > 5 && mode.compare(mode.size() - 5, 5, "_asym") == 0) {
+        gAsymmetric = true;
+        mode = mode.substr(0, mode.size() - 5);
     }
     auto arg = [&](int k, double dflt) { return argc > k ? std::atof(argv[k]) : dflt; };
     try {

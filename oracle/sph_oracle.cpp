@@ -1128,6 +1128,55 @@ void integrate(const sphgpu_config& cfg, ora_state& s) {
     // pair loop
     const Neighbours nb = findNeighbours(n, s.r);
     const double alpha = cfg.av_alpha, beta = cfg.av_beta;
+    // CorrectionTensor (core/sph/equations/Derivative.cpp:36-74), a PRECOMPUTE derivative of the
+    // AsymmetricSolver: C_i = (sum_j m_j / rho_j sym((r_j - r_i) x grad W_ij))^-1, identity when the sum is null
+    // or its determinant is at most 0.01
+    const bool corrected = fl.solid && cfg.correction_tensor != 0;
+    std::vector<double> corr;
+    if (corrected) {
+        corr.assign(6 * n, 0.);
+        parallelFor(n, [&](uint64_t a, uint64_t b) {
+            for (uint64_t i = a; i < b; ++i) {
+                const V4 ri = load4(s.r, i);
+                double c[6] = { 0, 0, 0, 0, 0, 0 };
+                for (uint64_t k = nb.start[i]; k < nb.start[i + 1]; ++k) {
+                    const uint32_t j = nb.idx[k];
+                    if (fl.sumOnlyUndamaged && (s.flag[i] != s.flag[j] || s.reduce[i] == 0. || s.reduce[j] == 0.)) {
+                        continue;
+                    }
+                    const V4 rj = load4(s.r, j);
+                    const V4 grad = sphGrad(sub(ri, rj), 0.5 * (ri.h + rj.h));
+                    const V4 e = sub(rj, ri);
+                    const double f = s.m[j] / s.rho[j];
+                    c[0] += f * (e.x * grad.x);
+                    c[1] += f * (e.y * grad.y);
+                    c[2] += f * (e.z * grad.z);
+                    c[3] += f * (0.5 * (e.x * grad.y + e.y * grad.x));
+                    c[4] += f * (0.5 * (e.x * grad.z + e.z * grad.x));
+                    c[5] += f * (0.5 * (e.y * grad.z + e.z * grad.y));
+                }
+                const bool isNull = c[0] == 0. && c[1] == 0. && c[2] == 0. && c[3] == 0. && c[4] == 0. && c[5] == 0.;
+                const double det = c[0] * c[1] * c[2] + 2. * c[3] * c[4] * c[5] -
+                                   (c[3] * c[3] * c[2] + c[4] * c[4] * c[1] + c[5] * c[5] * c[0]);
+                double* out = corr.data() + 6 * i;
+                double* dst = s.corr ? s.corr + 6 * i : nullptr;
+                if (isNull || !(det > 0.01)) {
+                    out[0] = out[1] = out[2] = 1.;
+                    out[3] = out[4] = out[5] = 0.;
+                } else {
+                    out[0] = (c[1] * c[2] - c[5] * c[5]) / det;
+                    out[1] = (c[2] * c[0] - c[4] * c[4]) / det;
+                    out[2] = (c[0] * c[1] - c[3] * c[3]) / det;
+                    out[3] = (c[4] * c[5] - c[2] * c[3]) / det;
+                    out[4] = (c[5] * c[3] - c[1] * c[4]) / det;
+                    out[5] = (c[3] * c[4] - c[0] * c[5]) / det;
+                }
+                if (dst) {
+                    std::copy(out, out + 6, dst);
+                }
+            }
+        });
+    }
     parallelFor(n, [&](uint64_t a, uint64_t b) {
         for (uint64_t i = a; i < b; ++i) {
             const V4 ri = load4(s.r, i), vi = load4(s.v, i);
@@ -1174,14 +1223,22 @@ void integrate(const sphgpu_config& cfg, ora_state& s) {
                     const bool undamaged = !fl.sumOnlyUndamaged ||
                                            (s.flag[i] == s.flag[j] && s.reduce[i] != 0. && s.reduce[j] != 0.);
                     if (undamaged) {
-                        // VelocityGradient (DerivativeHelpers.h:347-361, SymmetricTensor.h:362-368)
+                        // VelocityGradient (DerivativeHelpers.h:347-361, SymmetricTensor.h:362-368), with the
+                        // corrected gradient C_i grad W when the correction tensor is on (DerivativeHelpers.h:100-104)
+                        V4 cg = grad;
+                        if (corrected) {
+                            const double* C = corr.data() + 6 * i;
+                            cg.x = C[0] * grad.x + C[3] * grad.y + C[4] * grad.z;
+                            cg.y = C[3] * grad.x + C[1] * grad.y + C[5] * grad.z;
+                            cg.z = C[4] * grad.x + C[5] * grad.y + C[2] * grad.z;
+                        }
                         const double f = mj / rhoi;
-                        const double o0 = 0.5 * (dvji.x * grad.y + dvji.y * grad.x);
-                        const double o1 = 0.5 * (dvji.x * grad.z + dvji.z * grad.x);
-                        const double o2 = 0.5 * (dvji.y * grad.z + dvji.z * grad.y);
-                        gv[0] += f * (dvji.x * grad.x);
-                        gv[1] += f * (dvji.y * grad.y);
-                        gv[2] += f * (dvji.z * grad.z);
+                        const double o0 = 0.5 * (dvji.x * cg.y + dvji.y * cg.x);
+                        const double o1 = 0.5 * (dvji.x * cg.z + dvji.z * cg.x);
+                        const double o2 = 0.5 * (dvji.y * cg.z + dvji.z * cg.y);
+                        gv[0] += f * (dvji.x * cg.x);
+                        gv[1] += f * (dvji.y * cg.y);
+                        gv[2] += f * (dvji.z * cg.z);
                         gv[3] += f * o0;
                         gv[4] += f * o1;
                         gv[5] += f * o2;

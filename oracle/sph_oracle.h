@@ -43,6 +43,7 @@ typedef struct {
     double* m_zero;
     double* growth;
     uint32_t* n_flaws;
+    double* corr;    /* 6n, optional: strain-rate correction tensor (xx, yy, zz, xy, xz, yz) */
 } ora_state;
 
 /* Number of worker threads used by the parallel loops (0 = hardware concurrency). */

@@ -12,7 +12,7 @@ from opensph_gb300 import abi
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
-STATE_FIELDS = ["r", "v", "dv", "m", "rho", "drho", "u", "du", "p", "cs", "divv", "ncnt", "flag",
+STATE_FIELDS = ["r", "v", "dv", "m", "rho", "drho", "u", "du", "p", "cs", "divv", "ncnt", "flag", "corr",
                 "S", "dS", "gradv", "reduce", "D", "dD", "eps_min", "m_zero", "growth", "n_flaws"]
 
 
@@ -25,11 +25,19 @@ def kind(fx):
     """Physics of the fixture (sphere, impact, gas, ...), without the "_all" suffix of the runs with every
     time-step criterion."""
     k = str(fx["driver_args"]).split()[0]
-    return k[:-4] if k.endswith("_all") else k
+    for suffix in ("_all", "_asym"):
+        if k.endswith(suffix):
+            k = k[:-len(suffix)]
+    return k
 
 
 def all_criteria(fx):
     return str(fx["driver_args"]).split()[0].endswith("_all")
+
+
+def asymmetric(fx):
+    """Fixture run with the AsymmetricSolver and the strain-rate correction tensor."""
+    return str(fx["driver_args"]).split()[0].endswith("_asym")
 
 
 def materials_of(fx):
@@ -65,9 +73,12 @@ def config_of(fx, precision=abi.PRECISION_FP64):
         return abi.make_config(n, mats, forces=abi.FORCE_PRESSURE | abi.FORCE_SELF_GRAVITY,
                                gravity_constant=float(fx["G"][0]), precision=precision, timestep_criteria=crit)
     if k == "impact":
+        extra = {}
+        if asymmetric(fx):
+            extra = {"solver_type": abi.SOLVER_ASYMMETRIC, "correction_tensor": 1}
         return abi.make_config(n, mats, forces=abi.FORCE_PRESSURE | abi.FORCE_SOLID_STRESS | abi.FORCE_SELF_GRAVITY,
                                adaptive_h=True, gravity_constant=float(fx["G"][0]), precision=precision,
-                               timestep_criteria=crit)
+                               timestep_criteria=crit, **extra)
     if k == "gas":
         return abi.make_config(n, mats, forces=abi.FORCE_PRESSURE, integrator=abi.INTEGRATOR_LEAP_FROG,
                                initial_timestep=1e-3, precision=precision, timestep_criteria=crit)

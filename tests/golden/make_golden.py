@@ -30,6 +30,9 @@ FIXTURES = {
     # the same two runs with every time-step criterion (Courant, derivatives, acceleration, divergence)
     "impact_all_n1200": ["impact_all", "1200", "5e4", "80", "5e3", "6", "5e3", "45"],
     "gas_all_n1500": ["gas_all", "1500", "80", "6"],
+    # solid impact with the AsymmetricSolver and the strain-rate correction tensor (the settings of the
+    # reference's impact regression, regression/impact/impact.sph)
+    "impact_asym_n1200": ["impact_asym", "1200", "5e4", "80", "5e3", "4", "5e3", "45"],
     # gravity only: Plummer sphere, BH theta 0.5 octupole vs brute force
     "gravity_n3000": ["gravity", "3000", "0.5", "7", "1e-3"],
     "gravity_n3000_t07": ["gravity", "3000", "0.7", "11", "1e-2"],

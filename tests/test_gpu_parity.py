@@ -144,7 +144,7 @@ def test_point_queries_after_mixed_walk_use_fp64_moments():
     np.testing.assert_array_equal(out[abi.PRECISION_MIXED], out[abi.PRECISION_FP64])
 
 
-@pytest.mark.parametrize("name", ["sphere_n1000", "impact_n1200", "gas_n1500"])
+@pytest.mark.parametrize("name", ["sphere_n1000", "impact_n1200", "gas_n1500", "impact_asym_n1200"])
 def test_integrate_matches_reference(name):
     fx = cases.load(name)
     cfg, keep = cases.config_of(fx)
@@ -152,14 +152,14 @@ def test_integrate_matches_reference(name):
         g.set_state(cases.state_of(fx, "s0_"))
         g.integrate()
         got = g.get_state()
-    for f in ["dv", "drho", "du", "divv", "p", "cs", "gradv", "dS", "dD", "reduce", "S"]:
+    for f in ["dv", "drho", "du", "divv", "p", "cs", "gradv", "dS", "dD", "reduce", "S", "corr"]:
         if "d0_" + f in fx:
             assert cases.scale_err(got[f], fx["d0_" + f]) < TOL_EVAL, f
     np.testing.assert_array_equal(got["ncnt"], fx["d0_ncnt"])
 
 
 @pytest.mark.parametrize("name", ["sphere_n1000", "impact_n1200", "gas_n1500", "impact_all_n1200",
-                                  "gas_all_n1500"])
+                                  "gas_all_n1500", "impact_asym_n1200"])
 def test_steps_match_reference(name):
     fx = cases.load(name)
     cfg, keep = cases.config_of(fx)
@@ -292,7 +292,7 @@ def test_mixed_gravity_close_to_reference(name):
     assert cases.scale_err(cases.vec3(dv), cases.vec3(dv64)) < 2e-6
 
 
-@pytest.mark.parametrize("name", ["sphere_n1000", "impact_n1200", "gas_n1500"])
+@pytest.mark.parametrize("name", ["sphere_n1000", "impact_n1200", "gas_n1500", "impact_asym_n1200"])
 def test_mixed_integrate_error_bound(name):
     fx = cases.load(name)
     cfg, keep = cases.config_of(fx, precision=abi.PRECISION_MIXED)
@@ -300,13 +300,13 @@ def test_mixed_integrate_error_bound(name):
         g.set_state(cases.state_of(fx, "s0_"))
         g.integrate()
         got = g.get_state()
-    for f in ["dv", "drho", "du", "divv", "gradv", "dS"]:
+    for f in ["dv", "drho", "du", "divv", "gradv", "dS", "corr"]:
         if "d0_" + f in fx:
             assert cases.scale_err(got[f], fx["d0_" + f]) < 1e-5, f
     np.testing.assert_array_equal(got["p"], fx["d0_p"])
 
 
-@pytest.mark.parametrize("name", ["sphere_n1000", "impact_n1200", "gas_n1500"])
+@pytest.mark.parametrize("name", ["sphere_n1000", "impact_n1200", "gas_n1500", "impact_asym_n1200"])
 def test_mixed_steps_error_bound(name):
     fx = cases.load(name)
     cfg, keep = cases.config_of(fx, precision=abi.PRECISION_MIXED)

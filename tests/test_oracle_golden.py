@@ -104,20 +104,20 @@ def test_barnes_hut_small_theta_is_brute_force():
     assert cases.scale_err(cases.vec3(dv), cases.vec3(fx["a_direct"])) < 1e-13
 
 
-@pytest.mark.parametrize("name", ["sphere_n1000", "impact_n1200", "gas_n1500"])
+@pytest.mark.parametrize("name", ["sphere_n1000", "impact_n1200", "gas_n1500", "impact_asym_n1200"])
 def test_integrate_matches_reference(name):
     fx = cases.load(name)
     cfg, keep = cases.config_of(fx)
     st = cases.state_of(fx, "s0_")
     oracle.integrate(cfg, st)
-    for f in ["dv", "drho", "du", "divv", "p", "cs", "gradv", "dS", "dD", "reduce", "S"]:
+    for f in ["dv", "drho", "du", "divv", "p", "cs", "gradv", "dS", "dD", "reduce", "S", "corr"]:
         if "d0_" + f in fx:
             assert cases.scale_err(st[f], fx["d0_" + f]) < TOL_EVAL, f
     np.testing.assert_array_equal(st["ncnt"], fx["d0_ncnt"])
 
 
 @pytest.mark.parametrize("name", ["sphere_n1000", "impact_n1200", "gas_n1500", "impact_all_n1200",
-                                  "gas_all_n1500"])
+                                  "gas_all_n1500", "impact_asym_n1200"])
 def test_steps_match_reference(name):
     fx = cases.load(name)
     cfg, keep = cases.config_of(fx)

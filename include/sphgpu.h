@@ -150,7 +150,8 @@ typedef struct {
                                         * Derivative.cpp:36-74); asymmetric solver with solid stress only */
     double derivative_factor;          /* TIMESTEPPING_DERIVATIVE_FACTOR (0.2), also the acceleration factor */
     double divergence_factor;          /* TIMESTEPPING_DIVERGENCE_FACTOR (0.005) */
-    double max_change;                 /* TIMESTEPPING_MAX_INCREASE: relative growth limit per step, INFINITY = off */
+    double max_change;                 /* TIMESTEPPING_MAX_INCREASE: relative growth limit of the step; 0 or
+                                        * >= 1.7976931348623157e308 (the reference's INFTY, its default) = off */
 } sphgpu_config;
 
 typedef struct sphgpu_handle sphgpu_handle;

@@ -2,6 +2,7 @@
 /// \brief Reference-side adaptors over the libsphgpu C ABI (see GpuSph.h).
 
 #include "GpuSph.h"
+#include "timestepping/TimeStepCriterion.h"
 
 #include "objects/Exceptions.h"
 #include "sph/solvers/StandardSets.h"
@@ -325,8 +326,43 @@ void GpuSolver::create(Storage& storage, IMaterial& material) const {
     getStandardEquations(settings).create(storage, material);
 }
 
-GpuTimeStepping::GpuTimeStepping(const SharedPtr<Storage>& storage, const RunSettings& settings)
-    : ITimeStepping(storage, settings) {
+namespace {
+
+/// The time step computed by the device at the end of its step (the criteria of the settings, evaluated by
+/// sphgpu_step); replaces the host-side MultiCriterion so that ITimeStepping::step reads no host quantity.
+class GpuCriterion : public ITimeStepCriterion {
+    std::shared_ptr<GpuTimeStepping::Link> link;
+    Float initial;
+
+public:
+    GpuCriterion(std::shared_ptr<GpuTimeStepping::Link> link, const Float initial)
+        : link(std::move(link))
+        , initial(initial) {}
+
+    virtual TimeStep compute(IScheduler& UNUSED(scheduler),
+        Storage& UNUSED(storage),
+        const Float maxStep,
+        Statistics& UNUSED(stats),
+        ArrayView<TimeStep> UNUSED(dts)) override {
+        if (!link->device) {
+            return { initial, CriterionId::INITIAL_VALUE };
+        }
+        double dt = 0.;
+        link->device->check(sphgpu_get_timestep(link->device->get(), &dt));
+        return { Float(dt), dt >= maxStep ? CriterionId::MAXIMAL_VALUE : CriterionId::CFL_CONDITION };
+    }
+};
+
+} // namespace
+
+GpuTimeStepping::GpuTimeStepping(const SharedPtr<Storage>& storage, const RunSettings& settings, const SyncMode mode)
+    : ITimeStepping(storage,
+          settings,
+          makeAuto<GpuCriterion>(std::make_shared<Link>(), settings.get<Float>(RunSettingsId::TIMESTEPPING_INITIAL_TIMESTEP)))
+    , mode(mode) {
+    // the criterion constructed above owns the first Link; share it
+    link = std::make_shared<Link>();
+    criterion = makeAuto<GpuCriterion>(link, settings.get<Float>(RunSettingsId::TIMESTEPPING_INITIAL_TIMESTEP));
     storage->zeroHighestDerivatives(SEQUENTIAL);
 }
 
@@ -336,10 +372,44 @@ void GpuTimeStepping::stepParticles(IScheduler& UNUSED(scheduler), ISolver& solv
         raise(true, "GpuTimeStepping requires GpuSolver");
     }
     DeviceState& dev = gpu->getDevice(*storage);
-    dev.upload(*storage);
+    if (link->device != &dev) {
+        link->device = &dev;
+        uploaded = false;
+    }
+    if (mode == SyncMode::EVERY_STEP || !uploaded) {
+        dev.upload(*storage);
+        uploaded = true;
+    }
     dev.check(sphgpu_set_timestep(dev.get(), timeStep));
     dev.check(sphgpu_step(dev.get(), 1));
-    dev.download(*storage, false);
+    hostCurrent = false;
+    if (mode == SyncMode::EVERY_STEP) {
+        this->sync();
+    }
+}
+
+void GpuTimeStepping::sync() {
+    if (hostCurrent || !link->device) {
+        return;
+    }
+    link->device->download(*storage, false);
+    hostCurrent = true;
+    syncs++;
+}
+
+void GpuTimeStepping::invalidate() {
+    uploaded = false;
+    hostCurrent = true;
+}
+
+GpuOutput::GpuOutput(AutoPtr<IOutput>&& output, GpuTimeStepping& stepping)
+    : IOutput(OutputFile())
+    , output(std::move(output))
+    , stepping(stepping) {}
+
+Expected<Path> GpuOutput::dump(const Storage& storage, const Statistics& stats) {
+    stepping.sync();
+    return output->dump(storage, stats);
 }
 
 // ---------------------------------------------------------------------------------------------------------

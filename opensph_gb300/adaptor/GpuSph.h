@@ -8,10 +8,13 @@
 ///   - GpuTimeStepping  : ITimeStepping (PredictorCorrector / LeapFrog with the step on the device)
 ///   - GpuBarnesHut     : IGravity      (replaces BarnesHut, Factory::getGravity)
 ///   - GpuFinder        : ISymmetricFinder (replaces KdTree, Factory::getFinder)
+///   - GpuOutput        : IOutput decorator bringing the host Storage up to date before each dump, so that
+///                        the reference's BinaryOutput (.ssf) writes the device state without per-step syncs
 /// Errors reported by the library are rethrown as the reference's InvalidSetup (configuration) or
 /// Exception (runtime) types.
 
 #include "gravity/IGravity.h"
+#include "io/Output.h"
 #include "objects/finders/NeighborFinder.h"
 #include "quantities/Storage.h"
 #include "system/Settings.h"
@@ -71,14 +74,62 @@ public:
     DeviceState& getDevice(const Storage& storage) const;
 };
 
-/// ITimeStepping drop-in running the whole predictor-corrector (or leap-frog) step and the Courant
-/// criterion on the device; the host storage is synchronised after each step.
+/// When GpuTimeStepping copies the device state into the host Storage.
+enum class SyncMode {
+    EVERY_STEP, ///< after every step (every host consumer sees the current state)
+    ON_DEMAND   ///< only in sync(): the device is the authoritative copy between outputs
+};
+
+/// ITimeStepping drop-in running the whole predictor-corrector (or leap-frog) step and the time-step
+/// criteria on the device. The time step of ITimeStepping::step comes from the device (GpuCriterion), so the
+/// host Storage needs no update between steps in ON_DEMAND mode; it is uploaded before the first step and
+/// after invalidate() (a resumed run, host-side edits).
 class GpuTimeStepping : public ITimeStepping {
 public:
-    GpuTimeStepping(const SharedPtr<Storage>& storage, const RunSettings& settings);
+    struct Link {
+        DeviceState* device = nullptr;
+    };
+
+private:
+    std::shared_ptr<Link> link;
+    SyncMode mode;
+    bool uploaded = false;
+    bool hostCurrent = true;
+
+public:
+    GpuTimeStepping(const SharedPtr<Storage>& storage, const RunSettings& settings,
+        SyncMode mode = SyncMode::EVERY_STEP);
+
+    /// Copies the device state into the host Storage if it is behind (ON_DEMAND mode).
+    void sync();
+
+    /// The host Storage was replaced or changed (BinaryInput::load of a resumed run, host-side edits):
+    /// upload it before the next step.
+    void invalidate();
+
+    /// Number of device-to-host synchronisations so far.
+    Size syncCount() const {
+        return syncs;
+    }
+
+private:
+    Size syncs = 0;
 
 protected:
     virtual void stepParticles(IScheduler& scheduler, ISolver& solver, Statistics& stats) override;
+};
+
+/// IOutput decorator (e.g. around BinaryOutput, core/io/Output.cpp:481): synchronises the device state
+/// into the host Storage, then lets the wrapped output write it. IRun::run calls dump only at output times
+/// (core/run/IRun.cpp:251-256), so the device-to-host traffic happens at output times only.
+class GpuOutput : public IOutput {
+    AutoPtr<IOutput> output;
+    GpuTimeStepping& stepping;
+
+public:
+    GpuOutput(AutoPtr<IOutput>&& output, GpuTimeStepping& stepping);
+
+    virtual Expected<Path> dump(const Storage& storage, const Statistics& stats) override;
 };
 
 /// IGravity drop-in: k-d tree, moments and tree walk on the device.

@@ -442,8 +442,8 @@ sphgpu_status validate(const sphgpu_config* c) {
     if ((c->timestep_criteria & SPHGPU_CRITERION_DIVERGENCE) && !(c->divergence_factor > 0.)) {
         return fail(nullptr, SPHGPU_ERR_ARGUMENT, "divergence_factor must be positive");
     }
-    if (!(c->max_change > 0.)) {
-        return fail(nullptr, SPHGPU_ERR_ARGUMENT, "max_change must be positive (1.7976931348623157e308 = no limit)");
+    if (!(c->max_change >= 0.)) {
+        return fail(nullptr, SPHGPU_ERR_ARGUMENT, "max_change must not be negative (0 = no limit)");
     }
     if (!(c->forces & SPHGPU_FORCE_PRESSURE)) {
         return fail(nullptr, SPHGPU_ERR_UNSUPPORTED, "the pressure force is required");
@@ -529,7 +529,7 @@ sphgpu_status sphgpu_create(const sphgpu_config* config, sphgpu_handle** out) {
     ph.criteria = config->timestep_criteria ? config->timestep_criteria : uint32_t(SPHGPU_CRITERION_COURANT);
     ph.derivative_factor = config->derivative_factor;
     ph.divergence_factor = config->divergence_factor;
-    ph.max_change = config->max_change;
+    ph.max_change = config->max_change > 0. ? config->max_change : DBL_MAX;
     ph.correction = config->correction_tensor ? 1 : 0;
     (void)anyRheology;
 

@@ -1444,7 +1444,7 @@ double criterionStep(const sphgpu_config& cfg, const ora_state& s, double lastSt
         }
         minStep = std::min(minStep, capped(m));
     }
-    if (cfg.max_change < INFTY) {
+    if (cfg.max_change > 0. && cfg.max_change < INFTY) {
         minStep = std::min(minStep, lastStep * (1. + cfg.max_change));
     }
     return minStep;

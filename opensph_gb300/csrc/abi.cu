@@ -334,8 +334,14 @@ sphgpu_status evalGravity(sphgpu_handle* h, cudaStream_t st) {
     return SPHGPU_OK;
 }
 
-// neighbour grid + pair loop on the main stream; gravityInLoop: the pair loop adds s.agrav itself
+// materials initialize (EOS, rheology), neighbour grid and pair loop on the main stream; gravityInLoop: the
+// pair loop adds s.agrav itself
 void evalSph(sphgpu_handle* h, bool gravityInLoop) {
+    {
+        Phase ph(h, SPHGPU_PHASE_PREDICT);
+        launchMaterialsInit(h->s, h->ph, h->d_mats, h->stream);
+        h->launches += 1;
+    }
     {
         Phase ph(h, SPHGPU_PHASE_NEIGHBORS);
         launchGridBuild(h->s, h->grid, h->ph, h->stream);
@@ -363,10 +369,11 @@ void evalSph(sphgpu_handle* h, bool gravityInLoop) {
     h->launches += 1;
 }
 
-// the derivative evaluation of ISolver::integrate after the materials were initialized. With self-gravity
-// the order of GravitySolver::loop (core/sph/solvers/GravitySolver.cpp:64-91: gravity into the accumulator,
-// then the pair loop) is kept in the arithmetic, not in time: the pair loop (main stream) and the tree build
-// + walk (gravity stream, higher priority) run concurrently, and after both dv = a_gravity + a_sph: the same
+// ISolver::integrate on a state whose h is already clamped: materials initialize, gravity, pair loop,
+// finalize. With self-gravity the order of GravitySolver::loop (core/sph/solvers/GravitySolver.cpp:64-91:
+// gravity into the accumulator, then the pair loop) is kept in the arithmetic, not in time: the materials
+// initialize and the pair loop (main stream) and the tree build + walk (gravity stream, higher priority; they
+// read only positions, h and masses) run concurrently, and after both dv = a_gravity + a_sph: the same
 // terms as the reference's accumulator, with the gravity term added after the pair sum instead of before it
 // (a difference of rounding only). The pair loop is queued first because the tree build waits on the host
 // for its own stream between levels.
@@ -976,8 +983,9 @@ sphgpu_status sphgpu_integrate(sphgpu_handle* h) {
     }
     {
         Phase ph(h, SPHGPU_PHASE_PREDICT);
-        launchMaterialsInit(h->s, h->ph, h->d_mats, h->stream);
-        h->launches += 1;
+        if (launchClampH(h->s, h->ph, h->stream)) {
+            h->launches += 1;
+        }
     }
     sphgpu_status st = evalDerivatives(h);
     if (st != SPHGPU_OK) {

@@ -103,7 +103,17 @@ __device__ void eigenvalues(const double t[6], double sig[3]) {
     sig[2] = (t1 * cos((phi + 4. * SPH_PI) / 3.) - p3) * n;
 }
 
-// materials initialize (EOS, von Mises) + AdaptiveSmoothingLength::initialize for particle i
+// AdaptiveSmoothingLength::initialize (core/sph/equations/EquationTerm.cpp:356-364): h clamped to its range.
+// Applied with the position update, before the tree build reads h as the gravitational softening.
+__device__ __forceinline__ void clampSmoothingLength(const DState& s, const Physics& ph, uint32_t i) {
+    if (ph.adaptive_h) {
+        dbl4 r = s.r[i];
+        r.w = fmax(ph.h_lo, fmin(r.w, ph.h_hi));
+        s.r[i] = r;
+    }
+}
+
+// materials initialize (EOS, von Mises) for particle i; does not read h
 __device__ void materialInit(const DState& s, const Physics& ph, const MaterialD* __restrict__ mats, uint32_t i) {
     const MaterialD mt = mats[ph.nmat > 1 ? s.mat[i] : 0];
     double p, cs;
@@ -137,11 +147,6 @@ __device__ void materialInit(const DState& s, const Physics& ph, const MaterialD
     }
     s.p[i] = p;
     s.cs[i] = cs;
-    if (ph.adaptive_h) {
-        dbl4 r = s.r[i];
-        r.w = fmax(ph.h_lo, fmin(r.w, ph.h_hi));
-        s.r[i] = r;
-    }
 }
 
 // clampWithDerivative (core/objects/wrappers/Interval.h:159-162)

@@ -330,7 +330,7 @@ __global__ void predictKernel(DState s, Physics ph, const MaterialD* __restrict_
             s.dD[i] = dD;
         }
     }
-    materialInit(s, ph, mats, i);
+    clampSmoothingLength(s, ph, i);
 }
 
 __device__ __forceinline__ void blockMinToGlobal(double local, double* out) {
@@ -477,7 +477,16 @@ __global__ void leapFrogDriftKernel(DState s, Physics ph, const MaterialD* __res
     r.z += v.z * 0.5 * dt;
     r.w += v.w * 0.5 * dt;
     s.r[i] = r;
-    materialInit(s, ph, mats, i);
+    clampSmoothingLength(s, ph, i);
+    (void)mats;
+}
+
+// AdaptiveSmoothingLength::initialize alone (ISolver::integrate on a state set by the caller)
+__global__ void clampHKernel(DState s, Physics ph) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < s.n) {
+        clampSmoothingLength(s, ph, i);
+    }
 }
 
 // LeapFrog: first-order Euler update, kick, second drift (TimeStepping.cpp:367-388) + Courant minimum
@@ -635,6 +644,14 @@ void launchMaterialsInit(const DState& s, const Physics& ph, const MaterialD* ma
     if (s.n) {
         materialsInitKernel<<<ceilDiv(s.n, 256), 256, 0, st>>>(s, ph, mats);
     }
+}
+
+bool launchClampH(const DState& s, const Physics& ph, cudaStream_t st) {
+    if (s.n && ph.adaptive_h) {
+        clampHKernel<<<ceilDiv(s.n, 256), 256, 0, st>>>(s, ph);
+        return true;
+    }
+    return false;
 }
 
 void launchPairSum64(const DState& s, const Grid& g, const Physics& ph, const MaterialD* mats, const double* lut,

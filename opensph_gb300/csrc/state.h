@@ -212,6 +212,8 @@ void launchListPairs(const DState& s, const Grid& g, uint32_t* pi, uint32_t* pj,
 
 // ---- launchers (sph64.cu) ----
 void launchMaterialsInit(const DState& s, const Physics& ph, const MaterialD* mats, cudaStream_t st);
+// the smoothing-length clamp of adaptive h alone; returns whether a kernel was launched
+bool launchClampH(const DState& s, const Physics& ph, cudaStream_t st);
 void launchPairSum64(const DState& s, const Grid& g, const Physics& ph, const MaterialD* mats,
     const double* lut_grad, cudaStream_t st);
 void launchPredict(const DState& s, const Physics& ph, const MaterialD* mats, const double* dt, cudaStream_t st);

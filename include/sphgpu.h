@@ -21,7 +21,7 @@
 extern "C" {
 #endif
 
-#define SPHGPU_ABI_VERSION 2
+#define SPHGPU_ABI_VERSION 3
 
 typedef enum {
     SPHGPU_OK = 0,
@@ -49,6 +49,7 @@ enum {
     SPHGPU_Q_EXPLICIT_GROWTH = 13,     /* double */
     SPHGPU_Q_N_FLAWS = 14,             /* uint32 */
     SPHGPU_Q_STRESS_REDUCING = 16,     /* double */
+    SPHGPU_Q_ANGULAR_FREQUENCY = 20,   /* Vector {x, y, z, 0}; N-body solver only */
     SPHGPU_Q_VELOCITY_GRADIENT = 26,   /* symmetric tensor */
     SPHGPU_Q_VELOCITY_DIVERGENCE = 27, /* double */
     SPHGPU_Q_STRAIN_RATE_CORRECTION_TENSOR = 29, /* symmetric tensor (read only; with correction_tensor) */
@@ -72,8 +73,37 @@ enum { SPHGPU_INTEGRATOR_PREDICTOR_CORRECTOR = 0, SPHGPU_INTEGRATOR_LEAP_FROG = 
  * neighbours in the same gather kernels here; they differ in the reference's summation order only, and the
  * asymmetric solver admits the strain-rate correction tensor. */
 enum { SPHGPU_SOLVER_SYMMETRIC = 0, SPHGPU_SOLVER_ASYMMETRIC = 1 };
-/* GravityKernelEnum (core/system/Settings.h): point masses or the gravity kernel of the SPH kernel */
-enum { SPHGPU_GRAVITY_KERNEL_POINT_PARTICLES = 0, SPHGPU_GRAVITY_KERNEL_SPH_KERNEL = 1 };
+/* HardSphereSolver (core/gravity/NBodySolver.h:24-140): hard spheres under Barnes-Hut self-gravity with
+ * collisions and overlaps resolved in time order each collide(); the state is r (radius as h), v, m and the
+ * angular frequency; leap-frog only (the N-body run's integrator, core/run/jobs/SimulationJobs.cpp:467). */
+enum { SPHGPU_SOLVER_NBODY_HARD_SPHERE = 2 };
+/* GravityKernelEnum (core/system/Settings.h:804-814): point masses, the gravity kernel of the SPH kernel, or
+ * the solid-sphere kernel of the N-body run (SolidSphereKernel, core/sph/kernel/GravityKernel.h:121-136) */
+enum {
+    SPHGPU_GRAVITY_KERNEL_POINT_PARTICLES = 0,
+    SPHGPU_GRAVITY_KERNEL_SPH_KERNEL = 1,
+    SPHGPU_GRAVITY_KERNEL_SOLID_SPHERES = 2
+};
+/* CollisionHandlerEnum (core/system/Settings.h:816-832, Factory::getCollisionHandler core/system/Factory.cpp:
+ * 415-429): NONE ignores collisions; PERFECT_MERGING merges unconditionally; ELASTIC_BOUNCE bounces with the
+ * restitution coefficients; MERGE_OR_BOUNCE merges bound pairs (escape speed and break-up spin limits) and
+ * bounces the rest. */
+enum {
+    SPHGPU_COLLISION_NONE = 0,
+    SPHGPU_COLLISION_PERFECT_MERGING = 1,
+    SPHGPU_COLLISION_ELASTIC_BOUNCE = 2,
+    SPHGPU_COLLISION_MERGE_OR_BOUNCE = 3
+};
+/* OverlapEnum (core/system/Settings.h:834-852, Factory::getOverlapHandler core/system/Factory.cpp:431-450,
+ * handlers core/gravity/Collision.h:360-567). */
+enum {
+    SPHGPU_OVERLAP_NONE = 0,            /* overlapping pairs are ignored */
+    SPHGPU_OVERLAP_FORCE_MERGE = 1,     /* merged unconditionally */
+    SPHGPU_OVERLAP_REPEL = 2,           /* moved apart to touch, then bounced */
+    SPHGPU_OVERLAP_REPEL_OR_MERGE = 3,  /* moved apart, then merged if bound, else bounced */
+    SPHGPU_OVERLAP_INTERNAL_BOUNCE = 4, /* bounced while approaching */
+    SPHGPU_OVERLAP_PASS_OR_MERGE = 5    /* merged if bound, else allowed to pass */
+};
 /* Time-step criteria: the reference's TimeStepCriterionEnum bits (core/system/Settings.h:577-592), evaluated
  * after every step as in MultiCriterion::compute (core/timestepping/TimeStepCriterion.cpp:139-389). */
 enum {
@@ -152,6 +182,16 @@ typedef struct {
     double divergence_factor;          /* TIMESTEPPING_DIVERGENCE_FACTOR (0.005) */
     double max_change;                 /* TIMESTEPPING_MAX_INCREASE: relative growth limit of the step; 0 or
                                         * >= 1.7976931348623157e308 (the reference's INFTY, its default) = off */
+    /* HardSphereSolver settings (SPHGPU_SOLVER_NBODY_HARD_SPHERE; core/system/Settings.cpp:650-675) */
+    int32_t collision_handler;         /* SPHGPU_COLLISION_* (COLLISION_HANDLER) */
+    int32_t overlap_handler;           /* SPHGPU_OVERLAP_* (COLLISION_OVERLAP) */
+    double restitution_normal;         /* COLLISION_RESTITUTION_NORMAL */
+    double restitution_tangent;        /* COLLISION_RESTITUTION_TANGENT */
+    double allowed_overlap;            /* COLLISION_ALLOWED_OVERLAP */
+    double bounce_merge_limit;         /* COLLISION_BOUNCE_MERGE_LIMIT */
+    double rotation_merge_limit;       /* COLLISION_ROTATION_MERGE_LIMIT */
+    uint32_t max_bounces;              /* COLLISION_MAX_BOUNCES */
+    uint32_t reserved2;
 } sphgpu_config;
 
 typedef struct sphgpu_handle sphgpu_handle;
@@ -198,15 +238,29 @@ sphgpu_status sphgpu_gravity_interactions(sphgpu_handle* h, uint64_t out[2]);
 
 /* ISolver::integrate (core/sph/solvers/SymmetricSolver.cpp:58-95 wrapped by GravitySolver::loop,
  * core/sph/solvers/GravitySolver.cpp:64-91): materials initialize, gravity, pair loop, finalize. The
- * highest derivatives are overwritten (the caller's zeroHighestDerivatives is implied). */
+ * highest derivatives are overwritten (the caller's zeroHighestDerivatives is implied). With the N-body solver
+ * HardSphereSolver::integrate (core/gravity/NBodySolver.cpp:97-117): dv = self-gravity, h derivatives 0. */
 sphgpu_status sphgpu_integrate(sphgpu_handle* h);
 
 /* ITimeStepping::step x nsteps (core/timestepping/TimeStepping.cpp:34-75, PredictorCorrector :272-346,
- * LeapFrog :352-391) followed each step by the Courant criterion (core/timestepping/TimeStepCriterion.cpp:
- * 315-356). Runs asynchronously on the handle's stream; the time step stays on the device. */
+ * LeapFrog :352-391) followed each step by the time-step criteria (core/timestepping/TimeStepCriterion.cpp:
+ * 139-389). Runs asynchronously on the handle's stream; the time step stays on the device. With the N-body
+ * solver each leap-frog step is collide(dt/2), drift, integrate, kick, collide(dt/2), drift (the collisions
+ * synchronise the stream twice per step). */
 sphgpu_status sphgpu_step(sphgpu_handle* h, uint32_t nsteps);
 sphgpu_status sphgpu_get_timestep(sphgpu_handle* h, double* dt);
 sphgpu_status sphgpu_set_timestep(sphgpu_handle* h, double dt);
+
+/* HardSphereSolver::collide (core/gravity/NBodySolver.cpp:329-484) over the interval [0, dt): finds every
+ * particle's earliest collision or overlap, resolves them in time order (re-searching the particles whose
+ * pending collisions were invalidated), and removes merged particles, keeping the order of the others
+ * (Storage::remove). N-body solver only; sphgpu_step calls it twice per leap-frog step. */
+sphgpu_status sphgpu_collide(sphgpu_handle* h, double dt);
+/* Current particle count (changes when collisions merge particles). */
+sphgpu_status sphgpu_particle_count(sphgpu_handle* h, uint64_t* n);
+/* StatisticsId::TOTAL_COLLISION_COUNT, MERGER_COUNT, BOUNCE_COUNT, OVERLAP_COUNT (core/gravity/NBodySolver.cpp:
+ * 119-163), summed over all collide calls since the handle was created. */
+sphgpu_status sphgpu_collision_stats(sphgpu_handle* h, uint64_t out[4]);
 
 /* Conserved totals (core/physics/Integrals.h:62-148) as compensated FP64 device reductions:
  * out[0..2] momentum, out[3..5] angular momentum about the origin, out[6] kinetic energy,
@@ -269,7 +323,8 @@ enum {
     SPHGPU_PHASE_NEIGHBORS = 3,     /* neighbour grid build + cell-sorted copies */
     SPHGPU_PHASE_SPH_EVAL = 4,      /* pair loop + finalize + fracture model */
     SPHGPU_PHASE_CORRECT = 5,       /* corrector (or leap-frog kick) + Courant criterion */
-    SPHGPU_PHASE_COUNT = 6
+    SPHGPU_PHASE_COLLIDE = 6,       /* N-body collision search and resolution (COLLISION_EVAL_TIME) */
+    SPHGPU_PHASE_COUNT = 7
 };
 sphgpu_status sphgpu_set_profiling(sphgpu_handle* h, int32_t enabled);
 /* Device milliseconds per phase and the number of this library's kernel launches since the last call

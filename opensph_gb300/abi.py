@@ -30,6 +30,7 @@ Q_M_ZERO = 12
 Q_EXPLICIT_GROWTH = 13
 Q_N_FLAWS = 14
 Q_STRESS_REDUCING = 16
+Q_ANGULAR_FREQUENCY = 20
 Q_VELOCITY_GRADIENT = 26
 Q_VELOCITY_DIVERGENCE = 27
 Q_STRAIN_RATE_CORRECTION_TENSOR = 29
@@ -51,11 +52,25 @@ INTEGRATOR_PREDICTOR_CORRECTOR = 0
 INTEGRATOR_LEAP_FROG = 1
 GRAVITY_KERNEL_POINT_PARTICLES = 0
 GRAVITY_KERNEL_SPH_KERNEL = 1
+GRAVITY_KERNEL_SOLID_SPHERES = 2
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
 
 SOLVER_SYMMETRIC = 0
 SOLVER_ASYMMETRIC = 1
+SOLVER_NBODY_HARD_SPHERE = 2
+
+# CollisionHandlerEnum / OverlapEnum (core/system/Settings.h:816-852)
+COLLISION_NONE = 0
+COLLISION_PERFECT_MERGING = 1
+COLLISION_ELASTIC_BOUNCE = 2
+COLLISION_MERGE_OR_BOUNCE = 3
+OVERLAP_NONE = 0
+OVERLAP_FORCE_MERGE = 1
+OVERLAP_REPEL = 2
+OVERLAP_REPEL_OR_MERGE = 3
+OVERLAP_INTERNAL_BOUNCE = 4
+OVERLAP_PASS_OR_MERGE = 5
 
 CRITERION_COURANT = 1 << 1
 CRITERION_DERIVATIVES = 1 << 2
@@ -78,6 +93,7 @@ QUANTITY_LAYOUT = {
     Q_EXPLICIT_GROWTH: (1, "f8"),
     Q_N_FLAWS: (1, "u4"),
     Q_STRESS_REDUCING: (1, "f8"),
+    Q_ANGULAR_FREQUENCY: (4, "f8"),
     Q_VELOCITY_GRADIENT: (6, "f8"),
     Q_VELOCITY_DIVERGENCE: (1, "f8"),
     Q_STRAIN_RATE_CORRECTION_TENSOR: (6, "f8"),
@@ -146,6 +162,15 @@ class Config(ctypes.Structure):
         ("derivative_factor", ctypes.c_double),
         ("divergence_factor", ctypes.c_double),
         ("max_change", ctypes.c_double),
+        ("collision_handler", ctypes.c_int32),
+        ("overlap_handler", ctypes.c_int32),
+        ("restitution_normal", ctypes.c_double),
+        ("restitution_tangent", ctypes.c_double),
+        ("allowed_overlap", ctypes.c_double),
+        ("bounce_merge_limit", ctypes.c_double),
+        ("rotation_merge_limit", ctypes.c_double),
+        ("max_bounces", ctypes.c_uint32),
+        ("reserved2", ctypes.c_uint32),
     ]
 
 
@@ -231,12 +256,48 @@ def make_config(n, materials, forces=FORCE_PRESSURE | FORCE_SELF_GRAVITY, adapti
     c.derivative_factor = 0.2
     c.divergence_factor = 0.005
     c.max_change = INFTY
+    # HardSphereSolver settings: RunSettings defaults (core/system/Settings.cpp:650-675)
+    c.collision_handler = COLLISION_MERGE_OR_BOUNCE
+    c.overlap_handler = OVERLAP_REPEL
+    c.restitution_normal = 0.8
+    c.restitution_tangent = 1.0
+    c.allowed_overlap = 0.01
+    c.bounce_merge_limit = 1.0
+    c.rotation_merge_limit = 1.0
+    c.max_bounces = 100
     for k, v in kw.items():
         if k == "smoothing_length_range":
             c.smoothing_length_range[:] = v
         else:
             setattr(c, k, v)
     return c, arr
+
+
+def make_nbody_config(n, **kw):
+    """The N-body run's settings (NBodyJob::getDefaultSettings, core/run/jobs/SimulationJobs.cpp:462-494):
+    HardSphereSolver, leap-frog, acceleration criterion (factor 0.2), max step 10 s, initial step 0.01 s, BH
+    theta 0.8 with the solid-sphere kernel and leaf size 20, MERGE_OR_BOUNCE collisions with PASS_OR_MERGE
+    overlaps, restitution 0.5 / 1, merge limits 4 / 1. No materials."""
+    c, keep = make_config(n, [basalt()], forces=FORCE_SELF_GRAVITY, integrator=INTEGRATOR_LEAP_FROG)
+    c.material_count = 0
+    c.materials = None
+    c.solver_type = SOLVER_NBODY_HARD_SPHERE
+    c.gravity_kernel = GRAVITY_KERNEL_SOLID_SPHERES
+    c.gravity_opening_angle = 0.8
+    c.gravity_leaf_size = 20
+    c.timestep_criteria = CRITERION_ACCELERATION
+    c.max_timestep = 10.0
+    c.initial_timestep = 0.01
+    c.collision_handler = COLLISION_MERGE_OR_BOUNCE
+    c.overlap_handler = OVERLAP_PASS_OR_MERGE
+    c.restitution_normal = 0.5
+    c.restitution_tangent = 1.0
+    c.allowed_overlap = 0.01
+    c.bounce_merge_limit = 4.0
+    c.rotation_merge_limit = 1.0
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c, keep
 
 
 class AdjointConfig(ctypes.Structure):

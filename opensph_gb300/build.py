@@ -31,6 +31,7 @@ UNITS = {
     "gravity32.cu": [],
     "noalloc.cu": [],
     "adjoint.cu": ["-fmad=false"],
+    "nbody.cu": ["-fmad=false"],
 }
 
 

@@ -51,6 +51,10 @@ struct sphgpu_handle {
     cudaStream_t gstream = nullptr;
     cudaEvent_t ev_fork = nullptr;
     cudaEvent_t ev_join = nullptr;
+    // HardSphereSolver: collision work space and settings, and the interval of sphgpu_collide
+    Collide coll;
+    CollideParams cp;
+    double* d_dtc = nullptr;
 };
 
 namespace {
@@ -262,6 +266,10 @@ bool slotOf(sphgpu_handle* h, int id, int order, QuantitySlot& q) {
     case SPHGPU_Q_STRESS_REDUCING:
         q.dev = s.reduce;
         return order == 0;
+    case SPHGPU_Q_ANGULAR_FREQUENCY:
+        q.comps = 4;
+        q.dev = s.omega;
+        return order == 0;
     case SPHGPU_Q_VELOCITY_GRADIENT:
         q.comps = 6;
         q.soa = true;
@@ -399,6 +407,72 @@ sphgpu_status evalDerivatives(sphgpu_handle* h) {
     return SPHGPU_OK;
 }
 
+// HardSphereSolver::collide over [0, factor * dt) (dt on the device)
+sphgpu_status collideNbody(sphgpu_handle* h, const double* dt, double factor) {
+    Phase ph(h, SPHGPU_PHASE_COLLIDE);
+    uint32_t capacityError = 0;
+    const int st = nbodyCollide(h->s, h->grid, h->coll, h->cp, dt, factor, &capacityError, h->stream);
+    h->launches += h->coll.launches;
+    if (st == SPHGPU_ERR_CAPACITY) {
+        return fail(h, SPHGPU_ERR_CAPACITY, "collision work space exhausted (bits 0x%x: 1 records, 2 heap, "
+                                            "4 invalidated particles, 8 moved-particle lists)", capacityError);
+    }
+    if (st != SPHGPU_OK) {
+        return cudaFail(h, cudaGetLastError(), "collide");
+    }
+    h->gravity_current = false;
+    return SPHGPU_OK;
+}
+
+// HardSphereSolver::integrate, optionally followed by the leap-frog kick
+sphgpu_status integrateNbody(sphgpu_handle* h, bool kick) {
+    if (h->ph.gravity) {
+        const sphgpu_status st = evalGravity(h, h->stream);
+        if (st != SPHGPU_OK) {
+            return st;
+        }
+    }
+    Phase ph(h, SPHGPU_PHASE_CORRECT);
+    launchNbodyIntegrate(h->s, h->ph.gravity != 0, h->d_dt, kick, h->stream);
+    h->launches += 1;
+    return SPHGPU_OK;
+}
+
+// LeapFrog::stepParticles with the N-body solver (core/timestepping/TimeStepping.cpp:352-391) and the
+// acceleration criterion
+sphgpu_status stepNbody(sphgpu_handle* h) {
+    sphgpu_status st = collideNbody(h, h->d_dt, 0.5);
+    if (st != SPHGPU_OK) {
+        return st;
+    }
+    {
+        Phase ph(h, SPHGPU_PHASE_PREDICT);
+        launchNbodyDrift(h->s, h->ph, h->d_dt, h->d_dt_min, false, h->stream);
+        h->launches += 1;
+    }
+    st = integrateNbody(h, true);
+    if (st != SPHGPU_OK) {
+        return st;
+    }
+    st = collideNbody(h, h->d_dt, 0.5);
+    if (st != SPHGPU_OK) {
+        return st;
+    }
+    Phase ph(h, SPHGPU_PHASE_CORRECT);
+    const bool criterion = (h->ph.criteria & SPHGPU_CRITERION_ACCELERATION) != 0;
+    launchNbodyDrift(h->s, h->ph, h->d_dt, h->d_dt_min, criterion, h->stream);
+    h->launches += 1;
+    if (criterion) {
+        launchCourantFinish(h->d_dt, h->d_dt_min, h->ph.max_dt, h->ph.max_change, h->stream);
+        h->launches += 1;
+    }
+    return SPHGPU_OK;
+}
+
+sphgpu_status requireSph(sphgpu_handle* h) {
+    return h->ph.nbody ? fail(h, SPHGPU_ERR_UNSUPPORTED, "not available with the N-body solver") : SPHGPU_OK;
+}
+
 void swapPredictions(sphgpu_handle* h) {
     DState& s = h->s;
     std::swap(s.dv, s.pdv);
@@ -412,8 +486,16 @@ sphgpu_status validate(const sphgpu_config* c) {
     if (!c) {
         return fail(nullptr, SPHGPU_ERR_ARGUMENT, "config is NULL");
     }
-    if (c->material_count == 0 || !c->materials) {
+    const bool nbody = c->solver_type == SPHGPU_SOLVER_NBODY_HARD_SPHERE;
+    if (!nbody && (c->material_count == 0 || !c->materials)) {
         return fail(nullptr, SPHGPU_ERR_ARGUMENT, "at least one material is required");
+    }
+    if (c->material_count > 0 && !c->materials) {
+        return fail(nullptr, SPHGPU_ERR_ARGUMENT, "materials is NULL");
+    }
+    if (c->gravity_kernel < SPHGPU_GRAVITY_KERNEL_POINT_PARTICLES ||
+        c->gravity_kernel > SPHGPU_GRAVITY_KERNEL_SOLID_SPHERES) {
+        return fail(nullptr, SPHGPU_ERR_UNSUPPORTED, "unknown gravity kernel %d", c->gravity_kernel);
     }
     if (c->gravity_leaf_size == 0 || c->gravity_leaf_size > 32) {
         return fail(nullptr, SPHGPU_ERR_UNSUPPORTED, "gravity_leaf_size must be in [1, 32] (got %u)",
@@ -431,8 +513,36 @@ sphgpu_status validate(const sphgpu_config* c) {
     if (c->precision != SPHGPU_PRECISION_FP64 && c->precision != SPHGPU_PRECISION_MIXED) {
         return fail(nullptr, SPHGPU_ERR_UNSUPPORTED, "unknown precision %d", c->precision);
     }
-    if (c->solver_type != SPHGPU_SOLVER_SYMMETRIC && c->solver_type != SPHGPU_SOLVER_ASYMMETRIC) {
+    if (c->solver_type != SPHGPU_SOLVER_SYMMETRIC && c->solver_type != SPHGPU_SOLVER_ASYMMETRIC && !nbody) {
         return fail(nullptr, SPHGPU_ERR_UNSUPPORTED, "unknown solver type %d", c->solver_type);
+    }
+    if (nbody) {
+        if (c->integrator != SPHGPU_INTEGRATOR_LEAP_FROG) {
+            return fail(nullptr, SPHGPU_ERR_UNSUPPORTED, "the N-body solver is integrated by leap-frog only");
+        }
+        if (c->forces & ~uint32_t(SPHGPU_FORCE_SELF_GRAVITY)) {
+            return fail(nullptr, SPHGPU_ERR_UNSUPPORTED, "the N-body solver has self-gravity as its only force");
+        }
+        if (c->timestep_criteria & ~uint32_t(SPHGPU_CRITERION_ACCELERATION)) {
+            return fail(nullptr, SPHGPU_ERR_UNSUPPORTED,
+                "the N-body solver supports the acceleration criterion only (0 = constant step)");
+        }
+        if ((c->timestep_criteria & SPHGPU_CRITERION_ACCELERATION) && !(c->derivative_factor > 0.)) {
+            return fail(nullptr, SPHGPU_ERR_ARGUMENT, "derivative_factor must be positive");
+        }
+        if (c->collision_handler < SPHGPU_COLLISION_NONE || c->collision_handler > SPHGPU_COLLISION_MERGE_OR_BOUNCE) {
+            return fail(nullptr, SPHGPU_ERR_UNSUPPORTED, "unknown collision handler %d", c->collision_handler);
+        }
+        if (c->overlap_handler < SPHGPU_OVERLAP_NONE || c->overlap_handler > SPHGPU_OVERLAP_PASS_OR_MERGE) {
+            return fail(nullptr, SPHGPU_ERR_UNSUPPORTED, "unknown overlap handler %d", c->overlap_handler);
+        }
+        if (!(c->allowed_overlap >= 0.)) {
+            return fail(nullptr, SPHGPU_ERR_ARGUMENT, "allowed_overlap must not be negative");
+        }
+        if (!(c->max_change >= 0.)) {
+            return fail(nullptr, SPHGPU_ERR_ARGUMENT, "max_change must not be negative (0 = no limit)");
+        }
+        return SPHGPU_OK;
     }
     if (c->correction_tensor &&
         (c->solver_type != SPHGPU_SOLVER_ASYMMETRIC || !(c->forces & SPHGPU_FORCE_SOLID_STRESS))) {
@@ -533,12 +643,24 @@ sphgpu_status sphgpu_create(const sphgpu_config* config, sphgpu_handle** out) {
     ph.theta_inv = config->gravity_opening_angle > 0. ? 1. / config->gravity_opening_angle : 2.;
     ph.courant = config->courant_number;
     ph.max_dt = config->max_timestep;
-    ph.criteria = config->timestep_criteria ? config->timestep_criteria : uint32_t(SPHGPU_CRITERION_COURANT);
+    ph.nbody = config->solver_type == SPHGPU_SOLVER_NBODY_HARD_SPHERE ? 1 : 0;
+    ph.criteria = config->timestep_criteria || ph.nbody ? config->timestep_criteria
+                                                         : uint32_t(SPHGPU_CRITERION_COURANT);
     ph.derivative_factor = config->derivative_factor;
     ph.divergence_factor = config->divergence_factor;
     ph.max_change = config->max_change > 0. ? config->max_change : DBL_MAX;
     ph.correction = config->correction_tensor ? 1 : 0;
     (void)anyRheology;
+    CollideParams& cp = h->cp;
+    std::memset(&cp, 0, sizeof(cp));
+    cp.handler = config->collision_handler;
+    cp.overlap = config->overlap_handler;
+    cp.rest_n = config->restitution_normal;
+    cp.rest_t = config->restitution_tangent;
+    cp.allowed = config->allowed_overlap;
+    cp.bounce_limit = config->bounce_merge_limit;
+    cp.rotation_limit = config->rotation_merge_limit;
+    cp.max_bounces = config->max_bounces;
 
     cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) {
@@ -565,21 +687,32 @@ sphgpu_status sphgpu_create(const sphgpu_config* config, sphgpu_handle** out) {
     A(&s.r, nn);
     A(&s.v, nn);
     A(&s.dv, nn);
-    A(&s.pdv, nn);
     A(&s.agrav, nn);
     A(&s.m, nn);
-    A(&s.rho, nn);
-    A(&s.drho, nn);
-    A(&s.pdrho, nn);
     A(&s.u, nn);
-    A(&s.du, nn);
-    A(&s.pdu, nn);
-    A(&s.p, nn);
-    A(&s.cs, nn);
-    A(&s.divv, nn);
-    A(&s.ncnt, nn);
-    A(&s.flag, nn);
-    A(&s.mat, nn);
+    if (ph.nbody) {
+        // HardSphereSolver state: r (radius as h), v, dv, m, angular frequency; u stays 0 for the totals
+        A(&s.omega, nn);
+        A(&h->coll.tmp_r, nn);
+        A(&h->coll.tmp_v, nn);
+        A(&h->coll.tmp_dv, nn);
+        A(&h->coll.tmp_w, nn);
+        A(&h->coll.tmp_m, nn);
+        A(&h->d_dtc, 1);
+    } else {
+        A(&s.pdv, nn);
+        A(&s.rho, nn);
+        A(&s.drho, nn);
+        A(&s.pdrho, nn);
+        A(&s.du, nn);
+        A(&s.pdu, nn);
+        A(&s.p, nn);
+        A(&s.cs, nn);
+        A(&s.divv, nn);
+        A(&s.ncnt, nn);
+        A(&s.flag, nn);
+        A(&s.mat, nn);
+    }
     if (ph.solid) {
         A(&s.S, 5 * nn);
         A(&s.dS, 5 * nn);
@@ -599,7 +732,7 @@ sphgpu_status sphgpu_create(const sphgpu_config* config, sphgpu_handle** out) {
         A(&s.growth, nn);
         A(&s.n_flaws, nn);
     }
-    A(&h->d_mats, h->materials.size());
+    A(&h->d_mats, std::max<size_t>(h->materials.size(), 1));
     A(&h->d_lut_sph, LUT_ENTRIES + 1);
     A(&h->d_lut_grav, LUT_ENTRIES + 1);
     A(&h->d_lut_sph_f, LUT_ENTRIES + 1);
@@ -614,10 +747,13 @@ sphgpu_status sphgpu_create(const sphgpu_config* config, sphgpu_handle** out) {
         e = cudaMallocHost((void**)&h->h_pinned, 64 * sizeof(unsigned long long));
     }
     if (e == cudaSuccess) {
-        e = gridAllocate(h->grid, n, ph.solid != 0, ph.correction != 0);
+        e = gridAllocate(h->grid, n, ph.solid != 0, ph.correction != 0, !ph.nbody);
     }
     if (e == cudaSuccess && ph.gravity) {
         e = treeAllocate(h->tree, n, ph.leaf_size);
+    }
+    if (e == cudaSuccess && ph.nbody) {
+        e = collideAllocate(h->coll, n, h->grid.cell_capacity);
     }
     if (e != cudaSuccess) {
         const std::string msg = std::string("device allocation failed: ") + cudaGetErrorString(e);
@@ -630,7 +766,11 @@ sphgpu_status sphgpu_create(const sphgpu_config* config, sphgpu_handle** out) {
         md.push_back(toDevice(m));
     }
     const std::vector<double> lutS = makeLut(cubicGrad);
-    const std::vector<double> lutG = makeLut(gravGrad);
+    // LutKernel<3> of the gravity kernel: GravityKernel<CubicSpline<3>>, or SolidSphereKernel, whose gradImpl
+    // is 1 everywhere (core/sph/kernel/GravityKernel.h:121-136)
+    const std::vector<double> lutG = config->gravity_kernel == SPHGPU_GRAVITY_KERNEL_SOLID_SPHERES
+                                         ? makeLut([](double) { return 1.; })
+                                         : makeLut(gravGrad);
     std::vector<float> lutSf(lutS.begin(), lutS.end());
     std::vector<float> lutGf(lutG.begin(), lutG.end());
     const double dt0 = config->initial_timestep;
@@ -653,6 +793,13 @@ sphgpu_status sphgpu_create(const sphgpu_config* config, sphgpu_handle** out) {
     }
     if (e == cudaSuccess) {
         e = cudaMemcpy(h->d_dt_min, &big, sizeof(double), cudaMemcpyHostToDevice);
+    }
+    if (e == cudaSuccess) {
+        e = cudaMemset(s.u, 0, nn * sizeof(double));
+    }
+    if (e == cudaSuccess && s.omega) {
+        // HardSphereSolver::create inserts ANGULAR_FREQUENCY = 0 (core/gravity/NBodySolver.cpp:487-490)
+        e = cudaMemset(s.omega, 0, nn * sizeof(dbl4));
     }
     if (e == cudaSuccess) {
         // reference defaults: every particle has STRESS_REDUCING = 1 (VonMisesRheology::create)
@@ -692,6 +839,7 @@ sphgpu_status sphgpu_destroy(sphgpu_handle* h) {
     }
     gridFree(h->grid);
     treeFree(h->tree);
+    collideFree(h->coll);
     adjointFree(h->adjoint);
     if (h->h_pinned) {
         cudaFreeHost(h->h_pinned);
@@ -792,6 +940,9 @@ sphgpu_status sphgpu_get_quantity(sphgpu_handle* h, int32_t id, int32_t order, v
 sphgpu_status sphgpu_build_neighbors(sphgpu_handle* h) {
     if (!h) {
         return SPHGPU_ERR_ARGUMENT;
+    }
+    if (requireSph(h) != SPHGPU_OK) {
+        return SPHGPU_ERR_UNSUPPORTED;
     }
     launchGridBuild(h->s, h->grid, h->ph, h->stream);
     launchGatherSorted(h->s, h->grid, h->ph, h->stream);
@@ -981,6 +1132,14 @@ sphgpu_status sphgpu_integrate(sphgpu_handle* h) {
     if (!h) {
         return SPHGPU_ERR_ARGUMENT;
     }
+    if (h->ph.nbody) {
+        const sphgpu_status st = integrateNbody(h, false);
+        if (st != SPHGPU_OK) {
+            return st;
+        }
+        CUDA_TRY(h, cudaGetLastError());
+        return checkDeviceError(h);
+    }
     {
         Phase ph(h, SPHGPU_PHASE_PREDICT);
         if (launchClampH(h->s, h->ph, h->stream)) {
@@ -1000,6 +1159,14 @@ sphgpu_status sphgpu_step(sphgpu_handle* h, uint32_t nsteps) {
         return SPHGPU_ERR_ARGUMENT;
     }
     for (uint32_t k = 0; k < nsteps; ++k) {
+        if (h->ph.nbody) {
+            const sphgpu_status st = stepNbody(h);
+            if (st != SPHGPU_OK) {
+                return st;
+            }
+            CUDA_TRY(h, cudaGetLastError());
+            continue;
+        }
         const bool lf = h->ph.integrator == SPHGPU_INTEGRATOR_LEAP_FROG;
         {
             Phase ph(h, SPHGPU_PHASE_PREDICT);
@@ -1118,6 +1285,9 @@ sphgpu_status sphgpu_adjoint_forward(sphgpu_handle* h, const sphgpu_adjoint_conf
     if (!h || !cfg || !loss) {
         return SPHGPU_ERR_ARGUMENT;
     }
+    if (requireSph(h) != SPHGPU_OK) {
+        return SPHGPU_ERR_UNSUPPORTED;
+    }
     if (cfg->rebuild_every == 0 || cfg->checkpoint_every == 0 || cfg->rebuild_every % cfg->checkpoint_every != 0) {
         return fail(h, SPHGPU_ERR_ARGUMENT,
             "adjoint: rebuild_every (%u) must be a positive multiple of checkpoint_every (%u)", cfg->rebuild_every,
@@ -1166,6 +1336,43 @@ sphgpu_status sphgpu_adjoint_backward(sphgpu_handle* h, double loss_bar, double*
     }
     if (grad_alpha) {
         *grad_alpha = alphaBar;
+    }
+    return SPHGPU_OK;
+}
+
+sphgpu_status sphgpu_collide(sphgpu_handle* h, double dt) {
+    if (!h) {
+        return SPHGPU_ERR_ARGUMENT;
+    }
+    if (!h->ph.nbody) {
+        return fail(h, SPHGPU_ERR_UNSUPPORTED, "collide needs the N-body solver");
+    }
+    if (!(dt >= 0.)) {
+        return fail(h, SPHGPU_ERR_ARGUMENT, "collide: dt must not be negative");
+    }
+    CUDA_TRY(h, cudaMemcpyAsync(h->d_dtc, &dt, sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    const sphgpu_status st = collideNbody(h, h->d_dtc, 1.);
+    if (st != SPHGPU_OK) {
+        return st;
+    }
+    CUDA_TRY(h, cudaGetLastError());
+    return SPHGPU_OK;
+}
+
+sphgpu_status sphgpu_particle_count(sphgpu_handle* h, uint64_t* n) {
+    if (!h || !n) {
+        return SPHGPU_ERR_ARGUMENT;
+    }
+    *n = h->s.n;
+    return SPHGPU_OK;
+}
+
+sphgpu_status sphgpu_collision_stats(sphgpu_handle* h, uint64_t out[4]) {
+    if (!h || !out) {
+        return SPHGPU_ERR_ARGUMENT;
+    }
+    for (int k = 0; k < 4; ++k) {
+        out[k] = h->coll.totals[k];
     }
     return SPHGPU_OK;
 }

@@ -26,7 +26,9 @@ __global__ void resetBounds(unsigned long long* b) {
     }
 }
 
-__global__ void boundsKernel(const dbl4* __restrict__ r, uint32_t n, unsigned long long* b) {
+// bounding box of the positions and the maximum of h (rad == nullptr) or of rad
+__global__ void boundsKernel(const dbl4* __restrict__ r, const double* __restrict__ rad, uint32_t n,
+    unsigned long long* b) {
     unsigned long long mn[3] = { ~0ull, ~0ull, ~0ull }, mx[3] = { 0, 0, 0 }, hm = 0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const dbl4 p = r[i];
@@ -37,7 +39,7 @@ __global__ void boundsKernel(const dbl4* __restrict__ r, uint32_t n, unsigned lo
         mx[0] = max(mx[0], fx);
         mx[1] = max(mx[1], fy);
         mx[2] = max(mx[2], fz);
-        hm = max(hm, doubleFlip(p.w));
+        hm = max(hm, doubleFlip(rad ? rad[i] : p.w));
     }
     for (int off = 16; off > 0; off >>= 1) {
         for (int k = 0; k < 3; ++k) {
@@ -249,7 +251,7 @@ __global__ void pairsKernel(uint32_t n, const dbl4* __restrict__ rs, const uint3
 
 } // namespace
 
-cudaError_t gridAllocate(Grid& g, uint32_t n, bool solid, bool correction) {
+cudaError_t gridAllocate(Grid& g, uint32_t n, bool solid, bool correction, bool copies) {
     const uint32_t nn = n > 0 ? n : 1;
     g.cell_capacity = max(1u << 12, min(4u * nn, 1u << 26));
     cudaError_t e = cudaSuccess;
@@ -266,16 +268,18 @@ cudaError_t gridAllocate(Grid& g, uint32_t n, bool solid, bool correction) {
     alloc((void**)&g.perm, nn * sizeof(uint32_t));
     alloc((void**)&g.cell_start, size_t(g.cell_capacity) * sizeof(uint32_t));
     alloc((void**)&g.cell_end, size_t(g.cell_capacity) * sizeof(uint32_t));
-    alloc((void**)&g.rs, nn * sizeof(dbl4));
-    alloc((void**)&g.vs, nn * sizeof(dbl4));
-    alloc((void**)&g.ms, nn * sizeof(double));
-    alloc((void**)&g.rhos, nn * sizeof(double));
-    alloc((void**)&g.ps, nn * sizeof(double));
-    alloc((void**)&g.css, nn * sizeof(double));
-    alloc((void**)&g.mx0, nn * sizeof(float4));
-    alloc((void**)&g.mx1, nn * sizeof(float4));
-    alloc((void**)&g.mx2, nn * sizeof(float4));
-    alloc((void**)&g.mx3, nn * sizeof(float4));
+    if (copies) {
+        alloc((void**)&g.rs, nn * sizeof(dbl4));
+        alloc((void**)&g.vs, nn * sizeof(dbl4));
+        alloc((void**)&g.ms, nn * sizeof(double));
+        alloc((void**)&g.rhos, nn * sizeof(double));
+        alloc((void**)&g.ps, nn * sizeof(double));
+        alloc((void**)&g.css, nn * sizeof(double));
+        alloc((void**)&g.mx0, nn * sizeof(float4));
+        alloc((void**)&g.mx1, nn * sizeof(float4));
+        alloc((void**)&g.mx2, nn * sizeof(float4));
+        alloc((void**)&g.mx3, nn * sizeof(float4));
+    }
     if (solid) {
         alloc((void**)&g.Ss, 5 * size_t(nn) * sizeof(double));
         alloc((void**)&g.reduces, nn * sizeof(double));
@@ -311,18 +315,21 @@ void gridFree(Grid& g) {
 
 void launchGridBuild(const DState& s, Grid& g, const Physics& ph, cudaStream_t st) {
     (void)ph;
-    const uint32_t n = s.n;
+    launchGridBuildRadius(s.r, nullptr, s.n, g, st);
+}
+
+void launchGridBuildRadius(const dbl4* r, const double* radius, uint32_t n, Grid& g, cudaStream_t st) {
     g.launches = n > 0 ? 6 : 2;
     resetBounds<<<1, 32, 0, st>>>(g.bounds);
     if (n > 0) {
         const int blocks = min(ceilDiv(n, 256), 152 * 8);
-        boundsKernel<<<blocks, 256, 0, st>>>(s.r, n, g.bounds);
+        boundsKernel<<<blocks, 256, 0, st>>>(r, radius, n, g.bounds);
     }
     gridSetupKernel<<<1, 1, 0, st>>>(g.bounds, g.cell_capacity, n, g.info);
     if (n == 0) {
         return;
     }
-    keysKernel<<<ceilDiv(n, 256), 256, 0, st>>>(s.r, n, g.info, g.keys, g.perm_in);
+    keysKernel<<<ceilDiv(n, 256), 256, 0, st>>>(r, n, g.info, g.keys, g.perm_in);
     int bits = 1;
     while ((1u << bits) < g.cell_capacity && bits < 32) {
         ++bits;

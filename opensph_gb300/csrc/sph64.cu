@@ -621,9 +621,14 @@ __device__ __forceinline__ bool finite4(const dbl4& a) {
 
 __global__ void checkFiniteKernel(DState s, unsigned long long* firstBad) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < s.n; i += gridDim.x * blockDim.x) {
-        bool ok = finite4(s.r[i]) && finite4(s.v[i]) && finite4(s.dv[i]) && isfinite(s.rho[i]) &&
-                  isfinite(s.u[i]) && isfinite(s.drho[i]) && isfinite(s.du[i]) && isfinite(s.p[i]) &&
-                  isfinite(s.cs[i]);
+        bool ok = finite4(s.r[i]) && finite4(s.v[i]) && finite4(s.dv[i]) && isfinite(s.m[i]);
+        if (s.rho) {
+            ok = ok && isfinite(s.rho[i]) && isfinite(s.u[i]) && isfinite(s.drho[i]) && isfinite(s.du[i]) &&
+                 isfinite(s.p[i]) && isfinite(s.cs[i]);
+        }
+        if (s.omega) {
+            ok = ok && finite4(s.omega[i]);
+        }
         if (s.S) {
             for (int c = 0; c < 5; ++c) {
                 ok = ok && isfinite(s.S[c * s.n + i]) && isfinite(s.dS[c * s.n + i]);

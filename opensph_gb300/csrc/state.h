@@ -50,6 +50,8 @@ struct DState {
     dbl4* agrav;
     // strain-rate correction tensor (6 x n: xx, yy, zz, xy, xz, yz), with the correction tensor only
     double* corr;
+    // N-body solver: angular frequency {x, y, z, 0} (QuantityId::ANGULAR_FREQUENCY)
+    dbl4* omega;
 };
 
 // Physics switches and constants of one handle
@@ -76,6 +78,57 @@ struct Physics {
     double divergence_factor;
     double max_change;        // relative growth limit of the step (off when >= DBL_MAX)
     int correction;           // strain-rate correction tensor applied to the velocity gradient
+    int nbody;                // HardSphereSolver instead of the SPH solver
+};
+
+// HardSphereSolver collision settings (core/gravity/NBodySolver.cpp:29-44, core/gravity/Collision.h)
+struct CollideParams {
+    int handler;              // SPHGPU_COLLISION_*
+    int overlap;              // SPHGPU_OVERLAP_*
+    double rest_n, rest_t;    // coefficients of restitution
+    double allowed;           // allowed overlap ratio
+    double bounce_limit;      // merge limit on the relative speed (in escape speeds squared)
+    double rotation_limit;    // merge limit on the spin of the merger
+    uint32_t max_bounces;
+    uint32_t pad;
+};
+
+// Device work space of HardSphereSolver::collide (nbody.cu)
+struct Collide {
+    uint32_t capacity = 0;       // particles
+    uint32_t pool_capacity = 0;  // collision records: one per particle for the first pass + later ones
+    uint32_t extra_capacity = 0; // entries of the moved-particle cell lists
+    double* s = nullptr;         // search radius h + |v| dt
+    double* srad = nullptr;      // searchRadii of the reference: s of the writer, 0 without one
+    int* nsel = nullptr;         // device: first-pass record count
+    int32_t* writer = nullptr;   // highest index of the particles whose first-pass search found this one
+    uint32_t* ver = nullptr;     // per particle: number of processed collisions that involved it
+    uint32_t* bounces = nullptr;
+    uint32_t* removed = nullptr;
+    uint32_t* prev_removed = nullptr; // flags of the indices removed by the previous call
+    int32_t* head = nullptr;     // per particle: newest record that involves it
+    int32_t* moved_cell = nullptr; // per particle: cell it is listed in last
+    void* pool = nullptr;        // collision records
+    uint32_t* valid = nullptr;   // first-pass record flags
+    uint32_t* order_a = nullptr;
+    uint32_t* order_b = nullptr;
+    unsigned long long* key_a = nullptr;
+    unsigned long long* key_b = nullptr;
+    int32_t* extra_head = nullptr; // per grid cell
+    int32_t* extra = nullptr;      // 3 ints per entry: particle, next, cell
+    unsigned long long* counters = nullptr; // device, see nbody.cu
+    unsigned long long* counters_host = nullptr; // pinned mirror
+    void* temp = nullptr;
+    size_t temp_bytes = 0;
+    uint32_t* scan = nullptr;    // compaction offsets
+    // compaction targets, swapped with the state arrays (allocated and freed with the state arrays)
+    dbl4* tmp_r = nullptr;
+    dbl4* tmp_v = nullptr;
+    dbl4* tmp_dv = nullptr;
+    dbl4* tmp_w = nullptr;
+    double* tmp_m = nullptr;
+    uint32_t launches = 0;
+    unsigned long long totals[4] = { 0, 0, 0, 0 }; // collisions, mergers, bounces, overlaps (host copy)
 };
 
 // Neighbour grid buffers (cell-sorted copies of the pair-loop inputs)
@@ -204,11 +257,15 @@ struct Tree {
 // ---- launchers (grid.cu) ----
 void launchGridBuild(const DState& s, Grid& g, const Physics& ph, cudaStream_t st);
 void launchGatherSorted(const DState& s, Grid& g, const Physics& ph, cudaStream_t st);
-cudaError_t gridAllocate(Grid& g, uint32_t n, bool solid, bool correction = false);
+// copies: the cell-sorted copies of the SPH pair loops (not needed by the collision search)
+cudaError_t gridAllocate(Grid& g, uint32_t n, bool solid, bool correction = false, bool copies = true);
 void gridFree(Grid& g);
 void launchCountPairs(const DState& s, const Grid& g, unsigned long long* count, cudaStream_t st);
 void launchListPairs(const DState& s, const Grid& g, uint32_t* pi, uint32_t* pj, unsigned long long* count,
     unsigned long long capacity, cudaStream_t st);
+
+// grid of cell edge >= 2 max(radius) over the positions r (radius NULL: the h of r), for the collision search
+void launchGridBuildRadius(const dbl4* r, const double* radius, uint32_t n, Grid& g, cudaStream_t st);
 
 // ---- launchers (sph64.cu) ----
 void launchMaterialsInit(const DState& s, const Physics& ph, const MaterialD* mats, cudaStream_t st);
@@ -247,6 +304,19 @@ void launchGravityWalkMixed(const DState& s, Tree& t, const Physics& ph, const f
     uint32_t* dev_error, cudaStream_t st);
 void launchGravityPoints(const DState& s, const Tree& t, const Physics& ph, const double* lut_grad,
     const dbl4* points, dbl4* acc, uint32_t npoints, cudaStream_t st);
+
+// ---- HardSphereSolver (nbody.cu) ----
+cudaError_t collideAllocate(Collide& c, uint32_t n, uint32_t cell_capacity);
+void collideFree(Collide& c);
+// HardSphereSolver::collide over [0, factor * (*dt)); compacts the state when particles merged (s.n shrinks).
+// Synchronises the stream. Returns SPHGPU_OK or an error status (capacity bits in *capacity_error).
+int nbodyCollide(DState& s, Grid& g, Collide& c, const CollideParams& p, const double* dt, double factor,
+    uint32_t* capacity_error, cudaStream_t st);
+// leap-frog drift r += v dt / 2; with criteria, the acceleration time-step minimum into dt_min
+void launchNbodyDrift(const DState& s, const Physics& ph, const double* dt, double* dt_min, bool criterion,
+    cudaStream_t st);
+// HardSphereSolver::integrate: dv = a_gravity (0 without gravity), v.h = dv.h = 0; with kick, then v += dv dt
+void launchNbodyIntegrate(const DState& s, bool gravity, const double* dt, bool kick, cudaStream_t st);
 
 // ---- adjoint of the frozen-list hydrodynamic step (adjoint.cu) ----
 struct AdjointState;

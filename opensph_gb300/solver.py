@@ -62,6 +62,9 @@ def library():
     lib.sphgpu_phase_times.argtypes = [h, _F8P, ctypes.POINTER(ctypes.c_uint64)]
     lib.sphgpu_adjoint_forward.argtypes = [h, ctypes.POINTER(abi.AdjointConfig), _F8P]
     lib.sphgpu_adjoint_backward.argtypes = [h, ctypes.c_double, _F8P, _F8P, _F8P, _F8P, _F8P]
+    lib.sphgpu_collide.argtypes = [h, ctypes.c_double]
+    lib.sphgpu_particle_count.argtypes = [h, ctypes.POINTER(ctypes.c_uint64)]
+    lib.sphgpu_collision_stats.argtypes = [h, ctypes.POINTER(ctypes.c_uint64)]
     _LIB = lib
     return lib
 
@@ -77,7 +80,10 @@ STATE_QUANTITIES = {
     "dD": (abi.Q_DAMAGE, 1), "eps_min": (abi.Q_EPS_MIN, 0), "m_zero": (abi.Q_M_ZERO, 0),
     "growth": (abi.Q_EXPLICIT_GROWTH, 0), "n_flaws": (abi.Q_N_FLAWS, 0),
     "corr": (abi.Q_STRAIN_RATE_CORRECTION_TENSOR, 0),
+    "w": (abi.Q_ANGULAR_FREQUENCY, 0),
 }
+# the state of the N-body solver (HardSphereSolver): r (radius as h), v, dv, m, angular frequency
+NBODY_FIELDS = ["r", "v", "dv", "m", "w"]
 # inputs of a run (the outputs are recomputed by integrate/step)
 INPUT_FIELDS = ["r", "v", "dv", "m", "rho", "drho", "u", "du", "flag", "mat", "S", "dS", "reduce", "D", "dD",
                 "eps_min", "m_zero", "growth", "n_flaws", "p", "cs"]
@@ -94,6 +100,7 @@ class GpuSolver:
         if rc:
             raise SphGpuError(rc, self._lib.sphgpu_last_error(None).decode())
         self.solid = bool(config.forces & abi.FORCE_SOLID_STRESS)
+        self.nbody = config.solver_type == abi.SOLVER_NBODY_HARD_SPHERE
 
     def close(self):
         if self._h:
@@ -137,6 +144,12 @@ class GpuSolver:
         return a
 
     def set_state(self, st):
+        if self.nbody:
+            for name in NBODY_FIELDS:
+                if name in st and st[name] is not None:
+                    qid, order = STATE_QUANTITIES[name]
+                    self.set_quantity(qid, order, st[name])
+            return
         for name in INPUT_FIELDS:
             if name in st and st[name] is not None:
                 qid, order = STATE_QUANTITIES[name]
@@ -157,6 +170,8 @@ class GpuSolver:
         for name, (qid, order) in STATE_QUANTITIES.items():
             if fields is not None and name not in fields:
                 continue
+            if (self.nbody and name not in NBODY_FIELDS) or (not self.nbody and name == "w"):
+                continue
             if not self.solid and name in ("S", "dS", "reduce", "gradv"):
                 continue
             if not self._has_damage() and name in ("D", "dD", "eps_min", "m_zero", "growth", "n_flaws"):
@@ -171,6 +186,23 @@ class GpuSolver:
 
     def step(self, nsteps=1):
         self._check(self._lib.sphgpu_step(self._h, nsteps))
+        self._refresh_count()
+
+    def _refresh_count(self):
+        cnt = ctypes.c_uint64(0)
+        self._check(self._lib.sphgpu_particle_count(self._h, ctypes.byref(cnt)))
+        self.n = int(cnt.value)
+
+    def collide(self, dt):
+        """HardSphereSolver::collide over [0, dt) (N-body solver); merged particles are removed."""
+        self._check(self._lib.sphgpu_collide(self._h, float(dt)))
+        self._refresh_count()
+
+    def collision_stats(self):
+        """Collisions, mergers, bounces and overlaps summed over all collide calls of this handle."""
+        out = (ctypes.c_uint64 * 4)()
+        self._check(self._lib.sphgpu_collision_stats(self._h, out))
+        return list(out)
 
     @property
     def timestep(self):
@@ -222,7 +254,7 @@ class GpuSolver:
         self._check(self._lib.sphgpu_totals(self._h, out.ctypes.data_as(_F8P)))
         return out
 
-    PHASES = ["predict", "gravity_build", "gravity_eval", "neighbors", "sph_eval", "correct"]
+    PHASES = ["predict", "gravity_build", "gravity_eval", "neighbors", "sph_eval", "correct", "collide"]
 
     def set_profiling(self, enabled=True):
         self._check(self._lib.sphgpu_set_profiling(self._h, 1 if enabled else 0))

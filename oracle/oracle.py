@@ -235,3 +235,81 @@ def frozen_loss(r, v, m, rho, u, steps, dt, n_target, rebuild_every=10, gamma=5.
     if rc:
         raise RuntimeError(f"ora_frozen_loss failed: {rc}")
     return loss.value, dloss.value
+
+
+# ---- HardSphereSolver (ora_nbody_*) ----------------------------------------------------------------------
+
+class OraNbodyState(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_uint32), ("r", _F8), ("v", _F8), ("dv", _F8), ("m", _F8), ("w", _F8)]
+
+
+def _pack_nbody(st):
+    n = len(st["m"])
+    for name in ("r", "v", "dv", "w"):
+        if st.get(name) is None:
+            st[name] = np.zeros(4 * n)
+        st[name] = np.ascontiguousarray(st[name], dtype="f8").reshape(-1).copy()
+    st["m"] = np.ascontiguousarray(st["m"], dtype="f8").copy()
+    s = OraNbodyState()
+    s.n = n
+    for name in ("r", "v", "dv", "m", "w"):
+        setattr(s, name, st[name].ctypes.data_as(_F8))
+    return s
+
+
+def _unpack_nbody(st, n):
+    for name in ("r", "v", "dv", "w"):
+        st[name] = st[name][:4 * n].copy()
+    st["m"] = st["m"][:n].copy()
+
+
+def nbody_collide(cfg, st, dt, origin=False, prev_removed=None):
+    """HardSphereSolver::collide over [0, dt) on the state dict (r, v, dv, m, w; shrunk in place).
+    Returns (stats[4], ambiguous) and, with origin, the index before the call of each kept particle.
+    prev_removed: a list holding the indices removed by the previous call (updated in place)."""
+    s = _pack_nbody(st)
+    stats = np.zeros(4, dtype=np.uint64)
+    amb = ctypes.c_uint64(0)
+    org = np.zeros(max(s.n, 1), dtype=np.uint32)
+    prev = np.zeros(max(s.n, 1), dtype=np.uint32)
+    cnt = ctypes.c_uint32(0)
+    if prev_removed is not None:
+        cnt.value = len(prev_removed)
+        prev[:len(prev_removed)] = prev_removed
+    rc = _lib().ora_nbody_collide(ctypes.byref(cfg), ctypes.byref(s), ctypes.c_double(dt),
+                                  stats.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), ctypes.byref(amb),
+                                  org.ctypes.data_as(_U4), prev.ctypes.data_as(_U4), ctypes.byref(cnt))
+    if prev_removed is not None:
+        prev_removed[:] = prev[:cnt.value].tolist()
+    if rc:
+        raise RuntimeError(f"ora_nbody_collide failed: {rc}")
+    _unpack_nbody(st, s.n)
+    if origin:
+        return stats, amb.value, org[:s.n].copy()
+    return stats, amb.value
+
+
+def nbody_integrate(cfg, st):
+    s = _pack_nbody(st)
+    rc = _lib().ora_nbody_integrate(ctypes.byref(cfg), ctypes.byref(s))
+    if rc:
+        raise RuntimeError(f"ora_nbody_integrate failed: {rc}")
+    _unpack_nbody(st, s.n)
+    return st
+
+
+def nbody_run(cfg, st, steps, dt):
+    """steps leap-frog steps of the N-body solver. Returns (next dt, dts, counts, stats[4], ambiguous)."""
+    s = _pack_nbody(st)
+    dtv = ctypes.c_double(dt)
+    dts = np.zeros(max(steps, 1))
+    counts = np.zeros(max(steps, 1), dtype=np.uint32)
+    stats = np.zeros(4, dtype=np.uint64)
+    amb = ctypes.c_uint64(0)
+    rc = _lib().ora_nbody_run(ctypes.byref(cfg), ctypes.byref(s), ctypes.c_uint32(steps), ctypes.byref(dtv),
+                              dts.ctypes.data_as(_F8), stats.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                              ctypes.byref(amb), counts.ctypes.data_as(_U4))
+    if rc:
+        raise RuntimeError(f"ora_nbody_run failed: {rc}")
+    _unpack_nbody(st, s.n)
+    return dtv.value, dts[:steps], counts[:steps], stats, amb.value

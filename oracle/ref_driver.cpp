@@ -14,6 +14,7 @@
 #include "gravity/BarnesHut.h"
 #include "gravity/BruteForceGravity.h"
 #include "gravity/Moments.h"
+#include "gravity/NBodySolver.h"
 #include "objects/finders/KdTree.h"
 #include "sph/kernel/GravityKernel.h"
 
@@ -453,6 +454,153 @@ int modeEos(Writer& w) {
 
 } // namespace
 
+// HardSphereSolver wrapper that sums the collision statistics of every collide() call (the reference sets
+// them per call, core/gravity/NBodySolver.cpp:119-163)
+void dumpNbody(Writer& w, const std::string& pre, Storage& s);
+
+class CountingSolver : public ISolver {
+public:
+    HardSphereSolver inner;
+    std::vector<double> totals = std::vector<double>(4, 0.);
+    // the states before and after the collide calls from call number traceFrom on are written to trace
+    Writer* trace = nullptr;
+    int traceFrom = 1 << 30;
+    int calls = 0;
+
+    CountingSolver(IScheduler& scheduler, const RunSettings& settings)
+        : inner(scheduler, settings) {}
+
+    virtual void integrate(Storage& storage, Statistics& stats) override {
+        inner.integrate(storage, stats);
+    }
+    virtual void collide(Storage& storage, Statistics& stats, const Float dt) override {
+        const StatisticsId ids[4] = { StatisticsId::TOTAL_COLLISION_COUNT, StatisticsId::MERGER_COUNT,
+            StatisticsId::BOUNCE_COUNT, StatisticsId::OVERLAP_COUNT };
+        for (StatisticsId id : ids) {
+            stats.set(id, 0);
+        }
+        const bool traced = trace && calls >= traceFrom;
+        if (traced) {
+            dumpNbody(*trace, "pre" + std::to_string(calls) + "_", storage);
+            trace->scalar("dt" + std::to_string(calls), dt);
+        }
+        inner.collide(storage, stats, dt);
+        if (traced) {
+            dumpNbody(*trace, "post" + std::to_string(calls) + "_", storage);
+        }
+        ++calls;
+        for (int k = 0; k < 4; ++k) {
+            totals[k] += stats.get<int>(ids[k]);
+        }
+    }
+    virtual void create(Storage& storage, IMaterial& material) const override {
+        inner.create(storage, material);
+    }
+};
+
+void dumpNbody(Writer& w, const std::string& pre, Storage& s) {
+    ArrayView<const Vector> r, v, dv;
+    tie(r, v, dv) = s.getAll<Vector>(QuantityId::POSITION);
+    w.f64(pre + "r", vec4(r));
+    w.f64(pre + "v", vec4(v));
+    w.f64(pre + "dv", vec4(dv));
+    w.f64(pre + "m", flt(s.getValue<Float>(QuantityId::MASS)));
+    w.f64(pre + "w", vec4(s.getValue<Vector>(QuantityId::ANGULAR_FREQUENCY)));
+}
+
+// N-body cloud: n hard spheres of radius h (times 1 + 0.5 u, u uniform in [0, 1)) and density 2500, placed
+// uniformly in a sphere of radius R without overlaps, moving inward with velocity -k r plus a normal
+// velocity dispersion sigma; HardSphereSolver with BH self-gravity (solid spheres, theta 0.8, leaf 20),
+// leap-frog with the acceleration criterion (factor 0.2), the N-body run's settings otherwise
+// (core/run/jobs/SimulationJobs.cpp:462-494) except the handlers given here.
+int modeNbody(Writer& w, int n, int steps, int handler, int overlap, double R, double h, double k, double sigma,
+    uint64_t seed, double G, double maxDt) {
+    RunSettings settings;
+    settings.set(RunSettingsId::RUN_THREAD_CNT, 1);
+    settings.set(RunSettingsId::SPH_FINDER, FinderEnum::KD_TREE);
+    settings.set(RunSettingsId::FINDER_LEAF_SIZE, 20);
+    settings.set(RunSettingsId::GRAVITY_SOLVER, GravityEnum::BARNES_HUT);
+    settings.set(RunSettingsId::GRAVITY_KERNEL, GravityKernelEnum::SOLID_SPHERES);
+    settings.set(RunSettingsId::GRAVITY_OPENING_ANGLE, 0.8_f);
+    settings.set(RunSettingsId::GRAVITY_MULTIPOLE_ORDER, 3);
+    settings.set(RunSettingsId::GRAVITY_CONSTANT, G);
+    settings.set(RunSettingsId::COLLISION_HANDLER, CollisionHandlerEnum(handler));
+    settings.set(RunSettingsId::COLLISION_OVERLAP, OverlapEnum(overlap));
+    settings.set(RunSettingsId::COLLISION_RESTITUTION_NORMAL, 0.5_f);
+    settings.set(RunSettingsId::COLLISION_RESTITUTION_TANGENT, 1._f);
+    settings.set(RunSettingsId::COLLISION_ALLOWED_OVERLAP, 0.01_f);
+    settings.set(RunSettingsId::COLLISION_BOUNCE_MERGE_LIMIT, 4._f);
+    settings.set(RunSettingsId::COLLISION_ROTATION_MERGE_LIMIT, 1._f);
+    settings.set(RunSettingsId::NBODY_INERTIA_TENSOR, false);
+    settings.set(RunSettingsId::TIMESTEPPING_INITIAL_TIMESTEP, maxDt);
+    settings.set(RunSettingsId::TIMESTEPPING_MAX_TIMESTEP, maxDt);
+    settings.set(RunSettingsId::TIMESTEPPING_CRITERION, TimeStepCriterionEnum::ACCELERATION);
+    settings.set(RunSettingsId::TIMESTEPPING_DERIVATIVE_FACTOR, 0.2_f);
+
+    SplitMix rng{ seed };
+    Array<Vector> r;
+    Array<Float> m;
+    while (r.size() < Size(n)) {
+        const double x = (2. * rng.uniform() - 1.) * R, y = (2. * rng.uniform() - 1.) * R,
+                     z = (2. * rng.uniform() - 1.) * R;
+        if (x * x + y * y + z * z > R * R) {
+            continue;
+        }
+        const double hi = h * (1. + 0.5 * rng.uniform());
+        bool free = true;
+        for (Size j = 0; j < r.size() && free; ++j) {
+            const double dx = r[j][X] - x, dy = r[j][Y] - y, dz = r[j][Z] - z;
+            free = dx * dx + dy * dy + dz * dz > (hi + r[j][H]) * (hi + r[j][H]);
+        }
+        if (free) {
+            r.push(Vector(x, y, z, hi));
+            m.push(2500. * 4. / 3. * 3.14159265358979323846 * hi * hi * hi);
+        }
+    }
+    Array<Vector> v(r.size());
+    for (Size i = 0; i < r.size(); ++i) {
+        v[i] = Vector(-k * r[i][X] + sigma * rng.normal(), -k * r[i][Y] + sigma * rng.normal(),
+            -k * r[i][Z] + sigma * rng.normal(), 0._f);
+    }
+    SharedPtr<Storage> storage = makeShared<Storage>(makeAuto<NullMaterial>(BodySettings::getDefaults()));
+    storage->insert<Vector>(QuantityId::POSITION, OrderEnum::SECOND, std::move(r));
+    storage->getDt<Vector>(QuantityId::POSITION).fill(Vector(0._f));
+    {
+        ArrayView<Vector> vv = storage->getDt<Vector>(QuantityId::POSITION);
+        for (Size i = 0; i < vv.size(); ++i) {
+            vv[i] = v[i];
+        }
+    }
+    storage->insert<Float>(QuantityId::MASS, OrderEnum::ZERO, std::move(m));
+    SharedPtr<IScheduler> scheduler = Factory::getScheduler(settings);
+    CountingSolver solver(*scheduler, settings);
+    solver.create(*storage, storage->getMaterial(0));
+    if (std::getenv("NBODY_TRACE_LAST_STEP")) {
+        solver.trace = &w;
+        solver.traceFrom = 2 * (steps - 1);
+    }
+    w.scalar("G", G);
+    w.f64("settings", { double(handler), double(overlap), 0.5, 1., 0.01, 4., 1., 0.8, 20., maxDt, 0.2 });
+    dumpNbody(w, "s0_", *storage);
+    LeapFrog ts(storage, settings);
+    Statistics stats;
+    std::vector<double> dts, counts;
+    for (int step = 0; step < steps; ++step) {
+        dts.push_back(ts.getTimeStep());
+        ts.step(*scheduler, solver, stats);
+        counts.push_back(double(storage->getParticleCnt()));
+        if (step == 0) {
+            dumpNbody(w, "s1_", *storage);
+        }
+    }
+    dts.push_back(ts.getTimeStep());
+    w.f64("dts", dts);
+    w.f64("counts", counts);
+    w.f64("collision_stats", solver.totals);
+    dumpNbody(w, "sN_", *storage);
+    return 0;
+}
+
 int main(int argc, char** argv) {
     if (argc < 3) {
         std::fprintf(stderr, "usage: refdriver <out> <mode> [args]\n");
@@ -489,6 +637,10 @@ int main(int argc, char** argv) {
             return modePairs(w, int(arg(3, 1000)), uint64_t(arg(4, 3)));
         } else if (mode == "eos") {
             return modeEos(w);
+        } else if (mode == "nbody") {
+            return modeNbody(w, int(arg(3, 1000)), int(arg(4, 20)), int(arg(5, 3)), int(arg(6, 5)), arg(7, 2000.),
+                arg(8, 40.), arg(9, 1.e-3), arg(10, 0.05), uint64_t(arg(11, 5)), arg(12, 6.67408e-11),
+                arg(13, 10.));
         }
     } catch (const std::exception& e) {
         std::fprintf(stderr, "reference threw: %s\n", e.what());

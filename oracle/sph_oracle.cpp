@@ -229,18 +229,30 @@ inline V4 sphGrad(const V4& r, double h) {
     return V4{ (r.x * h5) * g, (r.y * h5) * g, (r.z * h5) * g, 0. };
 }
 
-// GravityLutKernel::grad (core/sph/kernel/GravityKernel.h:69-80); radius 0 = point masses
+// LutKernel<3> of SolidSphereKernel (core/sph/kernel/GravityKernel.h:121-136): gradImpl = 1, radius 2
+const Lut& solidLut() {
+    static const Lut lut = [] {
+        Lut l;
+        l.init(
+            2., [](double) { return 0.; }, [](double) { return 1.; });
+        return l;
+    }();
+    return lut;
+}
+
+// GravityLutKernel::grad (core/sph/kernel/GravityKernel.h:69-80); kernelRadius 0 = point masses, 2 = the
+// gravity kernel of the cubic spline, -2 = the solid-sphere kernel (radius 2)
 inline V4 gravGradV(const V4& r, double h, int kernelRadius) {
     const double hInv = 1. / h;
     const V4 rh{ r.x * hInv, r.y * hInv, r.z * hInv, 0. };
     const double qSqr = sqrLen(rh);
-    const double rad = double(kernelRadius);
+    const double rad = double(kernelRadius < 0 ? -kernelRadius : kernelRadius);
     if (qSqr + EPS >= rad * rad) {
         const double len = std::sqrt(sqrLen(r));
         const double l3 = len * len * len;
         return V4{ r.x / l3, r.y / l3, r.z / l3, 0. };
     }
-    const double g = gravLut().grad(qSqr);
+    const double g = (kernelRadius < 0 ? solidLut() : gravLut()).grad(qSqr);
     const double h3 = hInv * hInv * hInv;
     return V4{ (h3 * r.x) * g, (h3 * r.y) * g, (h3 * r.z) * g, 0. };
 }
@@ -526,6 +538,18 @@ struct BhNode {
     double q2[6] = { 0 };
     double q3[10] = { 0 };
 };
+
+// the kernel selector of BarnesHutTree / gravGradV for a configuration (GravityKernelEnum)
+inline int kernelRadiusOf(const sphgpu_config& cfg) {
+    switch (cfg.gravity_kernel) {
+    case SPHGPU_GRAVITY_KERNEL_POINT_PARTICLES:
+        return 0;
+    case SPHGPU_GRAVITY_KERNEL_SOLID_SPHERES:
+        return -2;
+    default:
+        return 2;
+    }
+}
 
 struct BarnesHutTree {
     const double* r = nullptr;
@@ -1121,7 +1145,7 @@ void integrate(const sphgpu_config& cfg, ora_state& s) {
         bh.leafSize = cfg.gravity_leaf_size;
         bh.thetaInv = 1. / cfg.gravity_opening_angle;
         bh.order = cfg.gravity_multipole_order;
-        bh.kernelRadius = cfg.gravity_kernel == SPHGPU_GRAVITY_KERNEL_POINT_PARTICLES ? 0 : 2;
+        bh.kernelRadius = kernelRadiusOf(cfg);
         bh.build(n, s.r, s.m, cfg.gravity_constant);
         bh.evalSelfGravity(acc.data());
     }
@@ -1854,3 +1878,750 @@ extern "C" int ora_frozen_loss(const ora_frozen_params* prm, uint64_t n, const d
     }
     return SPHGPU_OK;
 }
+
+// ---------------------------------------------------------------------------------------------------------
+// HardSphereSolver (core/gravity/NBodySolver.cpp:17-597) with the handlers of core/gravity/Collision.h.
+// The collision loop keeps the reference's own data structures: an ordered set of records with the order
+// (time, -overlap, i, j) and an index -> record multimap (CollisionSet, NBodySolver.cpp:213-327).
+// Deterministic choices where the reference depends on its k-d tree traversal order or on std::sort's order
+// of equal keys: rank ties are broken by index; of several overlapping neighbours the record smallest in the
+// record order is taken (the reference returns the first one its traversal meets) and every neighbour found
+// by the first-pass search writes its search radius. Searches that the reference might resolve differently
+// are counted as "ambiguous" so that fixtures can be checked to contain none.
+// ---------------------------------------------------------------------------------------------------------
+
+#include <map>
+#include <set>
+#include <unordered_map>
+
+namespace {
+
+// Constants::gravity (core/physics/Constants.h:32)
+const double G_PHYS = 6.67408e-11;
+
+inline V4 add4(const V4& a, const V4& b) {
+    return V4{ a.x + b.x, a.y + b.y, a.z + b.z, a.h + b.h };
+}
+inline V4 div4(const V4& a, double f) {
+    return V4{ a.x / f, a.y / f, a.z / f, a.h / f };
+}
+inline V4 cross3(const V4& a, const V4& b) {
+    return V4{ a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x, 0. };
+}
+inline double pow3(double x) {
+    return x * x * x;
+}
+// weightedAverage (core/gravity/Collision.h:81-85)
+inline V4 weightedAverage(const V4& a, double wa, const V4& b, double wb) {
+    return div4(add4(scale(a, wa), scale(b, wb)), wa + wb);
+}
+
+struct SymT {
+    double d[3], o[3];
+};
+// Rigid::sphereInertia (core/physics/Functions.h:61-63)
+inline SymT sphereInertia(double m, double r) {
+    const double k = 0.4 * m * (r * r);
+    return SymT{ { 1. * k, 1. * k, 1. * k }, { 0. * k, 0. * k, 0. * k } };
+}
+// SymmetricTensor * Vector (core/objects/geometry/SymmetricTensor.h:102-107)
+inline V4 symMul(const SymT& t, const V4& v) {
+    return V4{ t.d[0] * v.x + t.o[0] * v.y + t.o[1] * v.z, t.o[0] * v.x + t.d[1] * v.y + t.o[2] * v.z,
+        t.o[1] * v.x + t.o[2] * v.y + t.d[2] * v.z, 0. };
+}
+// SymmetricTensor::determinant / inverse (SymmetricTensor.h:193-231)
+inline SymT symInverse(const SymT& t) {
+    const double det = t.d[0] * t.d[1] * t.d[2] + 2. * t.o[0] * t.o[1] * t.o[2] -
+                       ((t.o[0] * t.o[0]) * t.d[2] + (t.o[1] * t.o[1]) * t.d[1] + (t.o[2] * t.o[2]) * t.d[0]);
+    SymT r;
+    r.d[0] = (t.d[1] * t.d[2] - t.o[2] * t.o[2]) / det;
+    r.d[1] = (t.d[2] * t.d[0] - t.o[1] * t.o[1]) / det;
+    r.d[2] = (t.d[0] * t.d[1] - t.o[0] * t.o[0]) / det;
+    r.o[0] = (t.o[1] * t.o[2] - t.d[2] * t.o[0]) / det;
+    r.o[1] = (t.o[2] * t.o[0] - t.d[1] * t.o[1]) / det;
+    r.o[2] = (t.o[0] * t.o[1] - t.d[0] * t.o[2]) / det;
+    return r;
+}
+
+// areParticlesBound (Collision.h:86-91)
+inline bool particlesBound(double mSum, double hSum, const V4& dv, double limit) {
+    const double vEscSqr = 2. * G_PHYS * mSum / hSum;
+    return sqrLen(dv) * limit < vEscSqr;
+}
+
+struct NbParts {
+    std::vector<V4> r, v, dv, w;
+    std::vector<double> m;
+    std::vector<char> removed;
+};
+
+struct MergerO {
+    double h, m;
+    V4 r, v, w;
+};
+// MergingCollisionHandler::collide without the inertia tensor (Collision.h:160-215)
+MergerO mergerOf(const NbParts& P, uint32_t i, uint32_t j) {
+    const V4 &ri = P.r[i], &rj = P.r[j], &vi = P.v[i], &vj = P.v[j];
+    const double mi = P.m[i], mj = P.m[j];
+    MergerO g;
+    g.h = std::cbrt(pow3(ri.h) + pow3(rj.h));
+    g.m = mi + mj;
+    g.r = weightedAverage(ri, mi, rj, mj);
+    g.v = weightedAverage(vi, mi, vj, mj);
+    V4 L = add4(scale(cross3(sub(ri, g.r), sub(vi, g.v)), mi), scale(cross3(sub(rj, g.r), sub(vj, g.v)), mj));
+    L = add4(L, symMul(sphereInertia(mi, ri.h), P.w[i]));
+    L = add4(L, symMul(sphereInertia(mj, rj.h), P.w[j]));
+    g.w = symMul(symInverse(sphereInertia(g.m, g.h)), L);
+    return g;
+}
+
+enum { NB_NONE = 0, NB_BOUNCE = 1, NB_MERGER = 2 };
+
+// MergingCollisionHandler::collide + acceptMerge (Collision.h:160-261)
+int mergeCollide(NbParts& P, uint32_t i, uint32_t j, double bounceLimit, double rotationLimit) {
+    const MergerO g = mergerOf(P, i, j);
+    if (!particlesBound(P.m[i] + P.m[j], P.r[i].h + P.r[j].h, sub(P.v[i], P.v[j]), bounceLimit)) {
+        return NB_NONE;
+    }
+    const double omegaCritSqr = G_PHYS * (P.m[i] + P.m[j]) / pow3(g.h);
+    if (sqrLen(g.w) * rotationLimit > omegaCritSqr) {
+        return NB_NONE;
+    }
+    P.m[i] = g.m;
+    P.r[i] = V4{ g.r.x, g.r.y, g.r.z, g.h };
+    P.v[i] = V4{ g.v.x, g.v.y, g.v.z, 0. };
+    P.w[i] = g.w;
+    P.removed[j] = 1;
+    return NB_MERGER;
+}
+
+// ElasticBounceHandler::reflect (Collision.h:316-326)
+inline V4 reflect(const V4& v, const V4& vCom, const V4& dir, double rn, double rt) {
+    const V4 vRel = sub(v, vCom);
+    const double proj = dot3(vRel, dir);
+    const V4 vT = sub(vRel, scale(dir, proj));
+    const V4 vN = scale(dir, proj);
+    return add4(sub(scale(vT, rt), scale(vN, rn)), vCom);
+}
+
+// ElasticBounceHandler::collide (Collision.h:301-313)
+int bounceCollide(NbParts& P, uint32_t i, uint32_t j, double rn, double rt) {
+    const V4 d = sub(P.r[i], P.r[j]);
+    const V4 dr = div4(d, std::sqrt(sqrLen(d)));
+    const V4 ndr{ -dr.x, -dr.y, -dr.z, -dr.h };
+    const V4 vCom = weightedAverage(P.v[i], P.m[i], P.v[j], P.m[j]);
+    const V4 vi = reflect(P.v[i], vCom, ndr, rn, rt);
+    const V4 vj = reflect(P.v[j], vCom, dr, rn, rt);
+    P.v[i] = V4{ vi.x, vi.y, vi.z, 0. };
+    P.v[j] = V4{ vj.x, vj.y, vj.z, 0. };
+    return NB_BOUNCE;
+}
+
+// Factory::getCollisionHandler (core/system/Factory.cpp:415-429)
+int collisionHandler(NbParts& P, const sphgpu_config& c, uint32_t i, uint32_t j) {
+    switch (c.collision_handler) {
+    case SPHGPU_COLLISION_PERFECT_MERGING:
+        return mergeCollide(P, i, j, 0., 0.);
+    case SPHGPU_COLLISION_ELASTIC_BOUNCE:
+        return bounceCollide(P, i, j, c.restitution_normal, c.restitution_tangent);
+    default: {
+        const int res = mergeCollide(P, i, j, c.bounce_merge_limit, c.rotation_merge_limit);
+        return res != NB_NONE ? res : bounceCollide(P, i, j, c.restitution_normal, c.restitution_tangent);
+    }
+    }
+}
+
+// RepelHandler::handle before the follow-up handler (Collision.h:443-467)
+void repel(NbParts& P, uint32_t i, uint32_t j) {
+    const V4 d = sub(P.r[i], P.r[j]);
+    const double dist = std::sqrt(sqrLen(d));
+    V4 dir = div4(d, dist);
+    dir.h = 0.;
+    const double x1 = (P.r[i].h + P.r[j].h - dist) / (1. + P.m[i] / P.m[j]);
+    const double x2 = P.m[i] / P.m[j] * x1;
+    P.r[i] = add4(P.r[i], scale(dir, x1));
+    P.r[j] = sub(P.r[j], scale(dir, x2));
+}
+
+// Factory::getOverlapHandler (core/system/Factory.cpp:431-450): IOverlapHandler::handle
+void overlapHandle(NbParts& P, const sphgpu_config& c, uint32_t i, uint32_t j) {
+    const double rn = c.restitution_normal, rt = c.restitution_tangent;
+    switch (c.overlap_handler) {
+    case SPHGPU_OVERLAP_FORCE_MERGE:
+        mergeCollide(P, i, j, 0., 0.);
+        break;
+    case SPHGPU_OVERLAP_REPEL:
+        repel(P, i, j);
+        bounceCollide(P, i, j, rn, rt);
+        break;
+    case SPHGPU_OVERLAP_REPEL_OR_MERGE:
+        repel(P, i, j);
+        if (mergeCollide(P, i, j, c.bounce_merge_limit, c.rotation_merge_limit) == NB_NONE) {
+            bounceCollide(P, i, j, rn, rt);
+        }
+        break;
+    case SPHGPU_OVERLAP_INTERNAL_BOUNCE:
+        bounceCollide(P, i, j, rn, rt);
+        break;
+    case SPHGPU_OVERLAP_PASS_OR_MERGE:
+        mergeCollide(P, i, j, c.bounce_merge_limit, c.rotation_merge_limit);
+        break;
+    default:
+        break;
+    }
+}
+
+// IOverlapHandler::overlaps (Collision.h:379-381, 404-406, 439-442, 494-499, 537-560)
+bool overlapHandled(const NbParts& P, const sphgpu_config& c, uint32_t i, uint32_t j) {
+    switch (c.overlap_handler) {
+    case SPHGPU_OVERLAP_NONE:
+        return false;
+    case SPHGPU_OVERLAP_INTERNAL_BOUNCE:
+        return dot3(sub(P.r[i], P.r[j]), sub(P.v[i], P.v[j])) < 0.;
+    case SPHGPU_OVERLAP_PASS_OR_MERGE: {
+        if (!particlesBound(P.m[i] + P.m[j], P.r[i].h + P.r[j].h, sub(P.v[i], P.v[j]), c.bounce_merge_limit)) {
+            return false;
+        }
+        const MergerO g = mergerOf(P, i, j);
+        const double omegaCritSqr = G_PHYS * (P.m[i] + P.m[j]) / pow3(g.h);
+        return !(sqrLen(g.w) * c.rotation_merge_limit > omegaCritSqr);
+    }
+    default:
+        return true;
+    }
+}
+
+// HardSphereSolver::checkCollision (NBodySolver.cpp:565-597); +inf when there is no collision in [0, dt]
+double checkCollision(const V4& r1, const V4& v1, const V4& r2, const V4& v2, double dt) {
+    const V4 dr = sub(r1, r2);
+    const V4 dv = sub(v1, v2);
+    const double dvdr = dot3(dv, dr);
+    if (dvdr >= 0.) {
+        return INFINITY;
+    }
+    const V4 drPerp = sub(dr, div4(scale(dv, dvdr), sqrLen(dv)));
+    const double hs = r1.h + r2.h;
+    if (sqrLen(drPerp) <= hs * hs) {
+        const double dv2 = sqrLen(dv);
+        const double det = 1. - (sqrLen(dr) - hs * hs) / (dvdr * dvdr) * dv2;
+        const double sqrtDet = std::sqrt(std::max(0., det));
+        const double root = det > 1. ? 1. + sqrtDet : 1. - sqrtDet;
+        const double tColl = -dvdr / dv2 * root;
+        if (tColl <= dt) {
+            return tColl;
+        }
+    }
+    return INFINITY;
+}
+
+// CollisionRecord (NBodySolver.cpp:165-211)
+struct NbRec {
+    double t, nov; // time, minus the overlap
+    uint32_t i, j;
+    bool operator<(const NbRec& o) const {
+        if (t != o.t) {
+            return t < o.t;
+        }
+        if (nov != o.nov) {
+            return nov < o.nov;
+        }
+        if (i != o.i) {
+            return i < o.i;
+        }
+        return j < o.j;
+    }
+    bool operator==(const NbRec& o) const {
+        return t == o.t && nov == o.nov && i == o.i && j == o.j;
+    }
+};
+
+// CollisionSet (NBodySolver.cpp:213-327)
+struct NbCollisionSet {
+    std::set<NbRec> records;
+    std::multimap<uint32_t, NbRec> byIndex;
+
+    void insert(const NbRec& r) {
+        if (!records.insert(r).second) {
+            return;
+        }
+        byIndex.insert({ r.i, r });
+        byIndex.insert({ r.j, r });
+    }
+    void eraseIndexEntry(uint32_t idx, const NbRec& r) {
+        auto range = byIndex.equal_range(idx);
+        for (auto it = range.first; it != range.second; ++it) {
+            if (it->second == r) {
+                byIndex.erase(it);
+                return;
+            }
+        }
+    }
+    void removeByCollision(const NbRec& r) {
+        eraseIndexEntry(r.i, r);
+        eraseIndexEntry(r.j, r);
+        records.erase(r);
+    }
+    void removeByIndex(uint32_t idx, std::set<uint32_t>& invalid) {
+        invalid.insert(idx);
+        std::vector<NbRec> mine;
+        auto range = byIndex.equal_range(idx);
+        for (auto it = range.first; it != range.second; ++it) {
+            mine.push_back(it->second);
+        }
+        for (const NbRec& r : mine) {
+            const uint32_t other = r.i == idx ? r.j : r.i;
+            invalid.insert(other);
+            records.erase(r);
+            eraseIndexEntry(other, r);
+            eraseIndexEntry(idx, r);
+        }
+    }
+};
+
+struct NbCand {
+    double t = INFINITY, nov = 0.;
+    uint32_t j = 0;
+    bool less(const NbCand& o) const {
+        if (t != o.t) {
+            return t < o.t;
+        }
+        if (nov != o.nov) {
+            return nov < o.nov;
+        }
+        return j < o.j;
+    }
+};
+
+// HardSphereSolver::collide (NBodySolver.cpp:329-484) on the host state
+struct NbCollider {
+    const sphgpu_config& cfg;
+    NbParts& P;
+    uint32_t n;
+    double dt;
+    std::vector<double> s;       // h + |v| dt
+    std::vector<int64_t> writer; // searchRadii writer
+    std::vector<double> srad;
+    std::vector<uint32_t> bounces;
+    // grid of the positions at the start of the call, cell edge >= 2 max s, plus the particles moved since
+    double cell = 1., lo[3] = { 0, 0, 0 };
+    std::unordered_map<uint64_t, std::vector<uint32_t>> cells;
+    std::vector<uint32_t> moved;
+    std::vector<char> isMoved;
+    // indices removed by the previous call: the reference clears its `removed` set only after the first
+    // pass (NBodySolver.cpp:367-396), so the first-pass searches skip these indices of the new numbering
+    const std::vector<uint32_t>* prevRemoved = nullptr;
+    uint64_t ambiguous = 0;
+    uint64_t stats[4] = { 0, 0, 0, 0 };
+
+    NbCollider(const sphgpu_config& c, NbParts& p, uint32_t count, double interval)
+        : cfg(c), P(p), n(count), dt(interval) {}
+
+    void cellOf(const V4& r, int64_t out[3]) const {
+        out[0] = int64_t(std::floor((r.x - lo[0]) / cell));
+        out[1] = int64_t(std::floor((r.y - lo[1]) / cell));
+        out[2] = int64_t(std::floor((r.z - lo[2]) / cell));
+    }
+    static uint64_t key(int64_t x, int64_t y, int64_t z) {
+        return (uint64_t(x & 0x1fffff) << 42) | (uint64_t(y & 0x1fffff) << 21) | uint64_t(z & 0x1fffff);
+    }
+    void buildGrid() {
+        double smax = 0.;
+        lo[0] = lo[1] = lo[2] = INFINITY;
+        for (uint32_t i = 0; i < n; ++i) {
+            smax = std::max(smax, s[i]);
+            lo[0] = std::min(lo[0], P.r[i].x);
+            lo[1] = std::min(lo[1], P.r[i].y);
+            lo[2] = std::min(lo[2], P.r[i].z);
+        }
+        cell = smax > 0. ? 2. * smax * 1.0001 : 1.;
+        for (uint32_t i = 0; i < n; ++i) {
+            int64_t c[3];
+            cellOf(P.r[i], c);
+            cells[key(c[0], c[1], c[2])].push_back(i);
+        }
+    }
+    // every particle j != i with |r_j - r_i|^2 < radius^2, deduplicated, in index order
+    std::vector<uint32_t> within(uint32_t i, double radius) const {
+        std::vector<uint32_t> out;
+        const V4 ri = P.r[i];
+        const double radiusSqr = radius * radius;
+        int64_t c[3];
+        cellOf(ri, c);
+        auto consider = [&](uint32_t j) {
+            if (j != i && sqrLen(sub(P.r[j], ri)) < radiusSqr) {
+                out.push_back(j);
+            }
+        };
+        for (int64_t z = c[2] - 1; z <= c[2] + 1; ++z) {
+            for (int64_t y = c[1] - 1; y <= c[1] + 1; ++y) {
+                for (int64_t x = c[0] - 1; x <= c[0] + 1; ++x) {
+                    auto it = cells.find(key(x, y, z));
+                    if (it != cells.end()) {
+                        for (uint32_t j : it->second) {
+                            consider(j);
+                        }
+                    }
+                }
+            }
+        }
+        for (uint32_t j : moved) {
+            consider(j);
+        }
+        std::sort(out.begin(), out.end());
+        out.erase(std::unique(out.begin(), out.end()), out.end());
+        return out;
+    }
+    bool rankLess(uint32_t j, uint32_t i) const {
+        return s[j] < s[i] || (s[j] == s[i] && j < i);
+    }
+
+    // findClosestCollision (NBodySolver.cpp:509-563); first: FIND_LOWER_RANK over [0, dt], else USE_RADII
+    NbCand find(uint32_t i, bool first, double lower, double size) {
+        std::vector<uint32_t> neighs;
+        if (first) {
+            for (uint32_t j : within(i, 2. * s[i])) {
+                if (rankLess(j, i)) {
+                    neighs.push_back(j);
+                }
+            }
+        } else if (srad[i] > 0.) {
+            neighs = within(i, 2. * srad[i]);
+        }
+        NbCand best;
+        uint32_t overlapsHandled = 0;
+        for (uint32_t j : neighs) {
+            if (first) {
+                writer[j] = std::max<int64_t>(writer[j], i);
+                writer[i] = std::max<int64_t>(writer[i], i);
+            }
+            if (P.removed[j] || bounces[j] > cfg.max_bounces) {
+                continue;
+            }
+            if (first && prevRemoved && std::binary_search(prevRemoved->begin(), prevRemoved->end(), j)) {
+                continue;
+            }
+            const V4 r1 = add4(P.r[i], scale(P.v[i], lower));
+            const V4 r2 = add4(P.r[j], scale(P.v[j], lower));
+            const double hs = P.r[i].h + P.r[j].h;
+            const double overlapValue = 1. - sqrLen(sub(r1, r2)) / (hs * hs);
+            NbCand c;
+            c.j = j;
+            if (overlapValue > cfg.allowed_overlap * cfg.allowed_overlap) {
+                if (!overlapHandled(P, cfg, i, j)) {
+                    continue;
+                }
+                ++overlapsHandled;
+                c.t = lower;
+                c.nov = -overlapValue;
+            } else {
+                const double t = checkCollision(r1, P.v[i], r2, P.v[j], size);
+                if (!(t < INFINITY)) {
+                    continue;
+                }
+                c.t = t + lower;
+            }
+            if (c.less(best)) {
+                best = c;
+            }
+        }
+        // the reference returns the first overlap its traversal meets (and, in the first pass, stops writing
+        // search radii there): with more than one overlap, or an overlap among several first-pass
+        // neighbours, its result may differ from this one
+        if (overlapsHandled > 1 || (first && overlapsHandled > 0 && neighs.size() > 1)) {
+            ++ambiguous;
+        }
+        return best;
+    }
+
+    void run() {
+        if (cfg.collision_handler == SPHGPU_COLLISION_NONE || n == 0) {
+            return;
+        }
+        s.resize(n);
+        for (uint32_t i = 0; i < n; ++i) {
+            s[i] = P.r[i].h + std::sqrt(sqrLen(P.v[i])) * dt;
+        }
+        writer.assign(n, -1);
+        bounces.assign(n, 0);
+        isMoved.assign(n, 0);
+        P.removed.assign(n, 0);
+        buildGrid();
+        NbCollisionSet set;
+        for (uint32_t i = 0; i < n; ++i) {
+            const NbCand c = find(i, true, 0., dt);
+            if (c.t < INFINITY) {
+                set.insert(NbRec{ c.t, c.nov, i, c.j });
+            }
+        }
+        srad.assign(n, 0.);
+        for (uint32_t i = 0; i < n; ++i) {
+            srad[i] = writer[i] >= 0 ? s[size_t(writer[i])] : 0.;
+        }
+        while (!set.records.empty()) {
+            const NbRec col = *set.records.begin();
+            const uint32_t i = col.i, j = col.j;
+            const double t = col.t;
+            P.r[i] = add4(P.r[i], scale(P.v[i], t));
+            P.r[j] = add4(P.r[j], scale(P.v[j], t));
+            int result;
+            if (col.nov < 0.) {
+                overlapHandle(P, cfg, i, j);
+                result = NB_BOUNCE;
+                stats[3]++;
+            } else {
+                result = collisionHandler(P, cfg, i, j);
+                stats[0]++;
+                if (result == NB_MERGER) {
+                    stats[1]++;
+                } else if (result == NB_BOUNCE) {
+                    stats[2]++;
+                }
+            }
+            P.r[i] = sub(P.r[i], scale(P.v[i], t));
+            P.r[j] = sub(P.r[j], scale(P.v[j], t));
+            if (result == NB_NONE) {
+                set.removeByCollision(col);
+                continue;
+            }
+            std::set<uint32_t> invalid;
+            set.removeByIndex(i, invalid);
+            set.removeByIndex(j, invalid);
+            bounces[i]++;
+            bounces[j]++;
+            for (uint32_t q : { i, j }) {
+                if (!isMoved[q]) {
+                    isMoved[q] = 1;
+                    moved.push_back(q);
+                }
+            }
+            const double lower = t + EPS;
+            if (!(lower > dt)) {
+                for (uint32_t idx : invalid) {
+                    if (P.removed[idx] || bounces[idx] > cfg.max_bounces) {
+                        continue;
+                    }
+                    const NbCand c = find(idx, false, lower, dt - lower);
+                    if (!(c.t < INFINITY)) {
+                        continue;
+                    }
+                    if ((idx == i && c.j == j) || (c.j == i && idx == j)) {
+                        continue;
+                    }
+                    set.insert(NbRec{ c.t, c.nov, idx, c.j });
+                }
+            }
+        }
+    }
+};
+
+// Storage::remove of the merged particles, keeping the order of the others
+void nbCompact(NbParts& P, uint32_t& n) {
+    uint32_t k = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        if (!P.removed[i]) {
+            P.r[k] = P.r[i];
+            P.v[k] = P.v[i];
+            P.dv[k] = P.dv[i];
+            P.w[k] = P.w[i];
+            P.m[k] = P.m[i];
+            ++k;
+        }
+    }
+    n = k;
+}
+
+} // namespace
+
+namespace {
+
+NbParts nbLoad(const ora_nbody_state& st) {
+    NbParts P;
+    P.r.resize(st.n);
+    P.v.resize(st.n);
+    P.dv.resize(st.n);
+    P.w.resize(st.n);
+    P.m.assign(st.m, st.m + st.n);
+    for (uint32_t i = 0; i < st.n; ++i) {
+        P.r[i] = load4(st.r, i);
+        P.v[i] = load4(st.v, i);
+        P.dv[i] = st.dv ? load4(st.dv, i) : V4{ 0, 0, 0, 0 };
+        P.w[i] = st.w ? load4(st.w, i) : V4{ 0, 0, 0, 0 };
+    }
+    P.removed.assign(st.n, 0);
+    return P;
+}
+
+void nbStore(const NbParts& P, uint32_t n, ora_nbody_state& st) {
+    st.n = n;
+    for (uint32_t i = 0; i < n; ++i) {
+        store4(st.r, i, P.r[i]);
+        store4(st.v, i, P.v[i]);
+        if (st.dv) {
+            store4(st.dv, i, P.dv[i]);
+        }
+        if (st.w) {
+            store4(st.w, i, P.w[i]);
+        }
+        st.m[i] = P.m[i];
+    }
+}
+
+void nbCollide(const sphgpu_config& cfg, NbParts& P, uint32_t& n, double dt, uint64_t stats[4], uint64_t* ambiguous,
+    std::vector<uint32_t>& prevRemoved, uint32_t* origin = nullptr) {
+    NbCollider c(cfg, P, n, dt);
+    c.prevRemoved = &prevRemoved;
+    c.run();
+    if (cfg.collision_handler != SPHGPU_COLLISION_NONE && n > 0) {
+        prevRemoved.clear();
+        for (uint32_t i = 0; i < n; ++i) {
+            if (P.removed[i]) {
+                prevRemoved.push_back(i);
+            }
+        }
+    }
+    if (origin) {
+        uint32_t k = 0;
+        for (uint32_t i = 0; i < n; ++i) {
+            if (P.removed.empty() || !P.removed[i]) {
+                origin[k++] = i;
+            }
+        }
+    }
+    for (int k = 0; k < 4; ++k) {
+        stats[k] += c.stats[k];
+    }
+    if (ambiguous) {
+        *ambiguous += c.ambiguous;
+    }
+    if (cfg.collision_handler != SPHGPU_COLLISION_NONE && n > 0) {
+        nbCompact(P, n);
+    }
+}
+
+// HardSphereSolver::integrate (NBodySolver.cpp:97-117): dv = self-gravity, v.h = dv.h = 0
+void nbIntegrate(const sphgpu_config& cfg, NbParts& P, uint32_t n) {
+    std::vector<double> r(4 * size_t(n)), acc(4 * size_t(n), 0.);
+    for (uint32_t i = 0; i < n; ++i) {
+        store4(r.data(), i, P.r[i]);
+    }
+    if ((cfg.forces & SPHGPU_FORCE_SELF_GRAVITY) && n > 0) {
+        BarnesHutTree bh;
+        bh.leafSize = cfg.gravity_leaf_size;
+        bh.thetaInv = 1. / cfg.gravity_opening_angle;
+        bh.order = cfg.gravity_multipole_order;
+        bh.kernelRadius = kernelRadiusOf(cfg);
+        bh.build(n, r.data(), P.m.data(), cfg.gravity_constant);
+        bh.evalSelfGravity(acc.data());
+    }
+    for (uint32_t i = 0; i < n; ++i) {
+        const V4 a = load4(acc.data(), i);
+        P.dv[i] = V4{ a.x, a.y, a.z, 0. };
+        P.v[i].h = 0.;
+    }
+}
+
+// leap-frog drift (core/timestepping/TimeStepping.cpp:358-361, 385-388)
+void nbDrift(NbParts& P, uint32_t n, double dt) {
+    for (uint32_t i = 0; i < n; ++i) {
+        const V4 v = P.v[i];
+        P.r[i].x += v.x * 0.5 * dt;
+        P.r[i].y += v.y * 0.5 * dt;
+        P.r[i].z += v.z * 0.5 * dt;
+        P.r[i].h += v.h * 0.5 * dt;
+    }
+}
+
+bool nbValid(const sphgpu_config* cfg, const ora_nbody_state* st) {
+    return cfg && st && cfg->solver_type == SPHGPU_SOLVER_NBODY_HARD_SPHERE && (st->n == 0 || (st->r && st->v && st->m));
+}
+
+} // namespace
+
+extern "C" {
+
+int ora_nbody_collide(const sphgpu_config* cfg, ora_nbody_state* st, double dt, uint64_t stats[4],
+    uint64_t* ambiguous, uint32_t* origin, uint32_t* prev_removed, uint32_t* prev_count) {
+    if (!nbValid(cfg, st) || !stats) {
+        return SPHGPU_ERR_ARGUMENT;
+    }
+    NbParts P = nbLoad(*st);
+    uint32_t n = st->n;
+    std::vector<uint32_t> prev;
+    if (prev_removed && prev_count) {
+        prev.assign(prev_removed, prev_removed + *prev_count);
+    }
+    nbCollide(*cfg, P, n, dt, stats, ambiguous, prev, origin);
+    if (prev_removed && prev_count) {
+        std::copy(prev.begin(), prev.end(), prev_removed);
+        *prev_count = uint32_t(prev.size());
+    }
+    nbStore(P, n, *st);
+    return SPHGPU_OK;
+}
+
+int ora_nbody_integrate(const sphgpu_config* cfg, ora_nbody_state* st) {
+    if (!nbValid(cfg, st) || !st->dv) {
+        return SPHGPU_ERR_ARGUMENT;
+    }
+    NbParts P = nbLoad(*st);
+    nbIntegrate(*cfg, P, st->n);
+    nbStore(P, st->n, *st);
+    return SPHGPU_OK;
+}
+
+// LeapFrog::stepParticles with HardSphereSolver (core/timestepping/TimeStepping.cpp:352-391) and, with the
+// ACCELERATION bit, MultiCriterion of AccelerationCriterion (core/timestepping/TimeStepCriterion.cpp:221-257,
+// 389-420); without criteria the step stays fixed
+int ora_nbody_run(const sphgpu_config* cfg, ora_nbody_state* st, uint32_t nsteps, double* dt, double* dts,
+    uint64_t stats[4], uint64_t* ambiguous, uint32_t* counts) {
+    if (!nbValid(cfg, st) || !st->dv || !dt || !stats) {
+        return SPHGPU_ERR_ARGUMENT;
+    }
+    NbParts P = nbLoad(*st);
+    uint32_t n = st->n;
+    std::vector<uint32_t> prev;
+    const double maxChange = cfg->max_change > 0. ? cfg->max_change : INFTY;
+    for (uint32_t k = 0; k < nsteps; ++k) {
+        const double h = *dt;
+        if (dts) {
+            dts[k] = h;
+        }
+        nbCollide(*cfg, P, n, 0.5 * h, stats, ambiguous, prev);
+        nbDrift(P, n, h);
+        nbIntegrate(*cfg, P, n);
+        for (uint32_t i = 0; i < n; ++i) {
+            P.v[i].x += P.dv[i].x * h;
+            P.v[i].y += P.dv[i].y * h;
+            P.v[i].z += P.dv[i].z * h;
+            P.v[i].h += P.dv[i].h * h;
+        }
+        nbCollide(*cfg, P, n, 0.5 * h, stats, ambiguous, prev);
+        nbDrift(P, n, h);
+        if (cfg->timestep_criteria & SPHGPU_CRITERION_ACCELERATION) {
+            double minStep = INFTY;
+            for (uint32_t i = 0; i < n; ++i) {
+                const double a2 = sqrLen(P.dv[i]);
+                if (a2 > EPS) {
+                    minStep = std::min(minStep, cfg->derivative_factor * std::sqrt(std::sqrt(P.r[i].h * P.r[i].h / a2)));
+                }
+            }
+            if (minStep > cfg->max_timestep) {
+                minStep = cfg->max_timestep;
+            }
+            if (maxChange < INFTY) {
+                const double lim = h * (1. + maxChange);
+                if (minStep > lim) {
+                    minStep = lim;
+                }
+            }
+            *dt = minStep;
+        }
+        if (counts) {
+            counts[k] = n;
+        }
+    }
+    nbStore(P, n, *st);
+    return SPHGPU_OK;
+}
+
+} // extern "C"

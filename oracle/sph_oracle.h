@@ -99,6 +99,32 @@ int ora_frozen_loss(const ora_frozen_params* prm, uint64_t n, const double* r, c
     const double* rho, const double* u, const double* tr, const double* tv, const double* trho, const double* tu,
     double talpha, double* loss, double* dloss);
 
+/* HardSphereSolver state (core/gravity/NBodySolver.cpp): r (4n: x, y, z, radius), v, dv (4n), m, angular
+ * frequency w (4n, may be NULL = 0). Merged particles are removed in place, keeping the order of the others;
+ * n is updated. */
+typedef struct {
+    uint32_t n;
+    double* r;
+    double* v;
+    double* dv;
+    double* m;
+    double* w;
+} ora_nbody_state;
+
+/* HardSphereSolver::collide over [0, dt); stats (collisions, mergers, bounces, overlaps) are ADDED to;
+ * ambiguous (may be NULL) is increased by the number of searches whose result may depend on the reference's
+ * k-d tree traversal order; origin (n entries, may be NULL) receives the index before the call of each
+ * particle kept. prev_removed / prev_count (n entries and a count, may be NULL): in, the indices the previous
+ * call removed, which the first-pass searches skip as the reference's solver does; out, those of this call. */
+int ora_nbody_collide(const sphgpu_config* cfg, ora_nbody_state* s, double dt, uint64_t stats[4],
+    uint64_t* ambiguous, uint32_t* origin, uint32_t* prev_removed, uint32_t* prev_count);
+/* HardSphereSolver::integrate: dv = self-gravity (Barnes-Hut), v.h = dv.h = 0. */
+int ora_nbody_integrate(const sphgpu_config* cfg, ora_nbody_state* s);
+/* nsteps leap-frog steps of the N-body solver; *dt is the first step and receives the next one; dts and
+ * counts (particle count after each step) have nsteps entries and may be NULL. */
+int ora_nbody_run(const sphgpu_config* cfg, ora_nbody_state* s, uint32_t nsteps, double* dt, double* dts,
+    uint64_t stats[4], uint64_t* ambiguous, uint32_t* counts);
+
 #ifdef __cplusplus
 }
 #endif

@@ -40,6 +40,21 @@ FIXTURES = {
     "pairs_n1500": ["pairs", "1500", "3"],
     # Tillotson EOS values on a (rho, u) grid
     "eos_tillotson": ["eos"],
+    # HardSphereSolver clouds (1000 spheres of radius 400-600 m, density 2500, inflow -k r plus dispersion,
+    # BH self-gravity with solid spheres, leap-frog with the acceleration criterion, max step 100 s):
+    # arguments n, steps, collision handler, overlap handler, R, h, k, sigma, seed, G, max step
+    "nbody_bounce_n1000": ["nbody", "1000", "10", "2", "0", "12000", "400", "1e-4", "0.05", "11", "6.67408e-11",
+                           "100"],
+    "nbody_merge_n1000": ["nbody", "1000", "8", "1", "1", "17000", "400", "1e-4", "0.05", "7", "6.67408e-11",
+                          "100"],
+    "nbody_default_n1000": ["nbody", "1000", "20", "3", "5", "14000", "400", "2e-4", "0.05", "3", "6.67408e-11",
+                            "100"],
+    "nbody_repel_n1000": ["nbody", "1000", "12", "3", "2", "14000", "400", "2e-4", "0.05", "3", "6.67408e-11",
+                          "100"],
+    "nbody_repelmerge_n1000": ["nbody", "1000", "10", "3", "3", "17000", "400", "1e-4", "0.05", "7",
+                               "6.67408e-11", "100"],
+    "nbody_internal_n1000": ["nbody", "1000", "12", "3", "4", "14000", "400", "2e-4", "0.05", "3",
+                             "6.67408e-11", "100"],
 }
 
 

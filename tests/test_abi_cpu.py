@@ -35,7 +35,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_abi_version():
     lib = ctypes.CDLL(_lib_path())
-    assert lib.sphgpu_abi_version() == 2
+    assert lib.sphgpu_abi_version() == 3
 
 
 def test_struct_layout_matches_header(tmp_path):
@@ -44,12 +44,15 @@ def test_struct_layout_matches_header(tmp_path):
         '#include <stdio.h>\n#include <stddef.h>\n#include "sphgpu.h"\n'
         "int main(void){printf(\"%zu %zu %zu %zu %zu %zu\\n\", sizeof(sphgpu_material), sizeof(sphgpu_config),"
         " offsetof(sphgpu_config, gravity_constant), offsetof(sphgpu_config, precision),"
-        " offsetof(sphgpu_material, damage_range), offsetof(sphgpu_config, courant_number));return 0;}\n")
+        " offsetof(sphgpu_material, damage_range), offsetof(sphgpu_config, courant_number));"
+        "printf(\"%zu %zu\\n\", offsetof(sphgpu_config, restitution_normal), offsetof(sphgpu_config, max_bounces));"
+        "return 0;}\n")
     exe = tmp_path / "layout"
     subprocess.run(["gcc", "-I", os.path.join(REPO, "include"), str(src), "-o", str(exe)], check=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
     got = [ctypes.sizeof(abi.Material), ctypes.sizeof(abi.Config), abi.Config.gravity_constant.offset,
-           abi.Config.precision.offset, abi.Material.damage_range.offset, abi.Config.courant_number.offset]
+           abi.Config.precision.offset, abi.Material.damage_range.offset, abi.Config.courant_number.offset,
+           abi.Config.restitution_normal.offset, abi.Config.max_bounces.offset]
     assert [int(x) for x in out] == got
 
 
@@ -73,8 +76,34 @@ def test_create_rejects_invalid_settings_without_device():
     assert not h.value
 
 
+def test_create_rejects_invalid_nbody_settings_without_device():
+    lib = ctypes.CDLL(_lib_path())
+    lib.sphgpu_last_error.restype = ctypes.c_char_p
+    h = ctypes.c_void_p()
+    # the N-body solver is integrated by leap-frog only
+    cfg, keep = abi.make_nbody_config(10, integrator=abi.INTEGRATOR_PREDICTOR_CORRECTOR)
+    assert lib.sphgpu_create(ctypes.byref(cfg), ctypes.byref(h)) == abi.ERR_UNSUPPORTED
+    # self-gravity is its only force
+    cfg, keep = abi.make_nbody_config(10, forces=abi.FORCE_PRESSURE | abi.FORCE_SELF_GRAVITY)
+    assert lib.sphgpu_create(ctypes.byref(cfg), ctypes.byref(h)) == abi.ERR_UNSUPPORTED
+    # the Courant criterion needs sound speeds the N-body state does not have
+    cfg, keep = abi.make_nbody_config(10, timestep_criteria=abi.CRITERION_COURANT)
+    assert lib.sphgpu_create(ctypes.byref(cfg), ctypes.byref(h)) == abi.ERR_UNSUPPORTED
+    # unknown handlers
+    cfg, keep = abi.make_nbody_config(10, collision_handler=9)
+    assert lib.sphgpu_create(ctypes.byref(cfg), ctypes.byref(h)) == abi.ERR_UNSUPPORTED
+    cfg, keep = abi.make_nbody_config(10, overlap_handler=-1)
+    assert lib.sphgpu_create(ctypes.byref(cfg), ctypes.byref(h)) == abi.ERR_UNSUPPORTED
+    assert b"overlap" in lib.sphgpu_last_error(None)
+    cfg, keep = abi.make_nbody_config(10, allowed_overlap=-0.5)
+    assert lib.sphgpu_create(ctypes.byref(cfg), ctypes.byref(h)) == abi.ERR_ARGUMENT
+    assert not h.value
+
+
 def test_null_handle_calls_return_argument_error():
     lib = ctypes.CDLL(_lib_path())
+    assert lib.sphgpu_collide(None, ctypes.c_double(1.0)) == abi.ERR_ARGUMENT
+    assert lib.sphgpu_particle_count(None, None) == abi.ERR_ARGUMENT
     assert lib.sphgpu_integrate(None) == abi.ERR_ARGUMENT
     assert lib.sphgpu_step(None, 1) == abi.ERR_ARGUMENT
     assert lib.sphgpu_destroy(None) == abi.OK

@@ -197,8 +197,10 @@ def test_gpu_cloud_scenarios_match_oracle(handler, overlap, check):
     _, _, counts, ora_stats, _ = oracle.nbody_run(cfg, ref, 10000, 1e-4)
     assert stats == [int(x) for x in ora_stats]
     assert n == counts[-1]
-    for f in nc.FIELDS:
+    for f in ("r", "v", "dv", "m"):
         assert nc.scale_err(got[f], ref[f]) < 1e-9, f
+    # the spins of a symmetric cloud are rounding noise: compare them on the spin scale |v| / h = 400 / s
+    assert np.abs(got["w"] - ref["w"]).max() < 1e-9 * 400.0
 
 
 def test_gpu_no_handler_ignores_collisions_and_sph_calls_are_refused():

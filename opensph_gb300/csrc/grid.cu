@@ -24,12 +24,16 @@ __global__ void resetBounds(unsigned long long* b) {
     if (threadIdx.x == 6) {
         b[6] = 0ull;                // max h
     }
+    if (threadIdx.x == 7) {
+        b[7] = 0ull;                // sum of the radii (a double), for the mean-based cell of the collision grid
+    }
 }
 
 // bounding box of the positions and the maximum of h (rad == nullptr) or of rad
 __global__ void boundsKernel(const dbl4* __restrict__ r, const double* __restrict__ rad, uint32_t n,
     unsigned long long* b) {
     unsigned long long mn[3] = { ~0ull, ~0ull, ~0ull }, mx[3] = { 0, 0, 0 }, hm = 0;
+    double sum = 0.;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const dbl4 p = r[i];
         const unsigned long long fx = doubleFlip(p.x), fy = doubleFlip(p.y), fz = doubleFlip(p.z);
@@ -40,6 +44,7 @@ __global__ void boundsKernel(const dbl4* __restrict__ r, const double* __restric
         mx[1] = max(mx[1], fy);
         mx[2] = max(mx[2], fz);
         hm = max(hm, doubleFlip(rad ? rad[i] : p.w));
+        sum += rad ? rad[i] : 0.;
     }
     for (int off = 16; off > 0; off >>= 1) {
         for (int k = 0; k < 3; ++k) {
@@ -47,6 +52,7 @@ __global__ void boundsKernel(const dbl4* __restrict__ r, const double* __restric
             mx[k] = max(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], off));
         }
         hm = max(hm, __shfl_xor_sync(0xffffffffu, hm, off));
+        sum += __shfl_xor_sync(0xffffffffu, sum, off);
     }
     if ((threadIdx.x & 31) == 0) {
         for (int k = 0; k < 3; ++k) {
@@ -54,10 +60,16 @@ __global__ void boundsKernel(const dbl4* __restrict__ r, const double* __restric
             atomicMax(&b[3 + k], mx[k]);
         }
         atomicMax(&b[6], hm);
+        if (rad) {
+            atomicAdd(reinterpret_cast<double*>(&b[7]), sum);
+        }
     }
 }
 
-__global__ void gridSetupKernel(const unsigned long long* b, uint32_t capacity, uint32_t n, GridInfo* g) {
+// meanCell: cell edge 2 max(mean radius, max radius / 8) (the collision search scans the cells of each
+// particle's own search box), else 2 max radius (the 27-cell stencil of the SPH pair loops)
+__global__ void gridSetupKernel(const unsigned long long* b, uint32_t capacity, uint32_t n, int meanCell,
+    GridInfo* g) {
     if (threadIdx.x != 0 || blockIdx.x != 0) {
         return;
     }
@@ -71,6 +83,10 @@ __global__ void gridSetupKernel(const unsigned long long* b, uint32_t capacity, 
     // cell edge: kernel support 2 h_max, widened by 1e-4 so that rounding in the cell index can never
     // separate two interacting particles by more than one cell
     double cell = 2. * hmax * 1.0001;
+    if (meanCell && n) {
+        const double mean = __longlong_as_double(static_cast<long long>(b[7])) / double(n);
+        cell = 2. * fmax(mean, 0.125 * hmax) * 1.0001;
+    }
     const double extMax = fmax(fmax(ext[0], ext[1]), ext[2]);
     if (!(cell > 0.)) {
         cell = extMax > 0. ? extMax : 1.;
@@ -319,13 +335,14 @@ void launchGridBuild(const DState& s, Grid& g, const Physics& ph, cudaStream_t s
 }
 
 void launchGridBuildRadius(const dbl4* r, const double* radius, uint32_t n, Grid& g, cudaStream_t st) {
+    const int meanCell = radius ? 1 : 0;
     g.launches = n > 0 ? 6 : 2;
     resetBounds<<<1, 32, 0, st>>>(g.bounds);
     if (n > 0) {
         const int blocks = min(ceilDiv(n, 256), 152 * 8);
         boundsKernel<<<blocks, 256, 0, st>>>(r, radius, n, g.bounds);
     }
-    gridSetupKernel<<<1, 1, 0, st>>>(g.bounds, g.cell_capacity, n, g.info);
+    gridSetupKernel<<<1, 1, 0, st>>>(g.bounds, g.cell_capacity, n, meanCell, g.info);
     if (n == 0) {
         return;
     }

@@ -4,7 +4,8 @@
 // ISolver::integrate is the Barnes-Hut walk of gravity.cu / gravity32.cu (dv = a_gravity, h derivatives zeroed,
 // NBodySolver.cpp:97-117). ISolver::collide (NBodySolver.cpp:329-484) is split into
 //   1. a data-parallel first pass: search radius s_i = h_i + |v_i| dt, a uniform grid of cell edge
-//      >= 2 max s, and per particle the earliest collision or overlap with its lower-rank neighbours
+//      2 max(mean s, max s / 8) of which each particle scans the cells of its own search box, and per particle
+//      the earliest collision or overlap with its lower-rank neighbours
 //      (findClosestCollision with FIND_LOWER_RANK, NBodySolver.cpp:509-563; rank = order by s, ties by index);
 //   2. a stable sort of the found records by the reference's order (time, -overlap, i, j);
 //   3. one CTA that resolves the records in time order exactly as the reference's loop does: advance the
@@ -346,6 +347,19 @@ __device__ Cand evalPair(const CollideParams& p, uint32_t j, const dbl4& ri, con
     const dbl4 r1 = add4(ri, mul4(vi, lower));
     const dbl4 r2 = add4(rj, mul4(vj, lower));
     const double hs = ri.w + rj.w;
+    {
+        // Conservative FP32 rejection of the common case: the surfaces are further apart than the relative
+        // motion can close within the interval, |r1 - r2| > (h_i + h_j + |v_i - v_j| size)(1 + 1e-4). Such a
+        // pair neither overlaps nor touches before lower + size, so the FP64 test below would find nothing
+        // either; the differences are formed in FP64 first, so the FP32 error is relative (~1e-7).
+        const float dx = float(r1.x - r2.x), dy = float(r1.y - r2.y), dz = float(r1.z - r2.z);
+        const float ux = float(vi.x - vj.x), uy = float(vi.y - vj.y), uz = float(vi.z - vj.z);
+        const float dist = sqrtf(dx * dx + dy * dy + dz * dz);
+        const float reach = (float(hs) + sqrtf(ux * ux + uy * uy + uz * uz) * float(size)) * 1.0001f;
+        if (dist > reach) {
+            return c;
+        }
+    }
     const double overlapValue = 1. - len2(sub4(r1, r2)) / (hs * hs);
     if (overlapValue > p.allowed * p.allowed) {
         if (overlapHandled(p, ri, vi, mi, wi, rj, vj, mj, wj)) {
@@ -364,6 +378,14 @@ __device__ Cand evalPair(const CollideParams& p, uint32_t j, const dbl4& ri, con
 __device__ __forceinline__ int nbCellCoord(double x, double lo, double inv, int dim) {
     int c = int((x - lo) * inv);
     return min(max(c, 0), dim - 1);
+}
+
+// the cells of the box [x - R, x + R] along one axis, R widened by 1e-9 (relative to R and to the coordinates)
+// so that rounding in x -/+ R cannot drop the cell of a particle closer than R
+__device__ __forceinline__ void cellSpan(double x, double R, double lo, double inv, int dim, int& c0, int& c1) {
+    const double w = R * (1. + 1e-9) + 1e-9 * (fabs(x) + fabs(lo));
+    c0 = nbCellCoord(x - w, lo, inv, dim);
+    c1 = nbCellCoord(x + w, lo, inv, dim);
 }
 
 __device__ __forceinline__ uint32_t nbCellKey(const GridInfo& gi, const dbl4& p) {
@@ -391,48 +413,99 @@ __global__ void prepareKernel(DState s, Collide c, const double* __restrict__ dt
     c.head[i] = -1;
 }
 
-// findClosestCollision(i, FIND_LOWER_RANK, [0, dt]) of every particle (NBodySolver.cpp:367-374, 509-563): the
-// neighbours j of lower rank with |r_j - r_i|^2 < (2 s_i)^2 (KdTree::find, core/objects/finders/KdTree.inl.h:
-// 316-391, rank by s as in buildWithRank's comparator, :348-351); every neighbour found records i as a
-// writer of its search radius (searchRadii[i] = searchRadii[j] = s_i, the largest index writing last).
-__global__ void detectKernel(DState s, Grid g, Collide c, CollideParams p, const double* __restrict__ dtp,
-    double factor) {
+// cell-sorted copies for the first pass: FP64 positions, FP32 positions relative to the origin of the particle's
+// cell with the search radius, and the bit patterns of the search radii (non-negative doubles order like their
+// bit patterns)
+__global__ void gatherKernel(DState s, Grid g, Collide c) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= s.n) {
         return;
     }
     const GridInfo gi = *g.info;
     const uint32_t i = g.perm[k];
-    c.moved_cell[i] = int32_t(g.keys[i]);
-    const double dt = factor * *dtp;
-    const dbl4 ri = s.r[i], vi = s.v[i], wi = s.omega[i];
-    const double mi = s.m[i];
+    const uint32_t key = g.keys_sorted[k];
+    const uint32_t cx = key % uint32_t(gi.dims[0]);
+    const uint32_t cy = (key / uint32_t(gi.dims[0])) % uint32_t(gi.dims[1]);
+    const uint32_t cz = key / (uint32_t(gi.dims[0]) * uint32_t(gi.dims[1]));
+    const dbl4 r = s.r[i];
     const double si = c.s[i];
-    const double radius = 2. * si;
+    c.rs[k] = r;
+    c.posf[k] = make_float4(float(r.x - (gi.lo[0] + double(cx) * gi.cell)), float(r.y - (gi.lo[1] + double(cy) * gi.cell)),
+        float(r.z - (gi.lo[2] + double(cz) * gi.cell)), float(2. * si));
+    c.sbits[k] = static_cast<unsigned long long>(__double_as_longlong(si));
+    c.moved_cell[i] = int32_t(key);
+}
+
+// findClosestCollision(i, FIND_LOWER_RANK, [0, dt]) of every particle (NBodySolver.cpp:367-374, 509-563): the
+// neighbours j of lower rank with |r_j - r_i|^2 < (2 s_i)^2 (KdTree::find, core/objects/finders/KdTree.inl.h:
+// 316-391, rank by s as in buildWithRank's comparator, :348-351); every neighbour found records i as a
+// writer of its search radius (searchRadii[i] = searchRadii[j] = s_i, the largest index writing last).
+// The distance test runs on the FP32 cell-relative copies with a margin that bounds their rounding
+// (1e-6 of the radius plus 2e-5 of the cell edge); only candidates within the margin of the sphere are tested
+// again in FP64, so the neighbour set is exactly the FP64 one.
+__global__ void __launch_bounds__(128) detectKernel(DState s, Grid g, Collide c, CollideParams p,
+    const double* __restrict__ dtp, double factor) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= s.n) {
+        return;
+    }
+    const GridInfo gi = *g.info;
+    const uint32_t i = g.perm[k];
+    const double dt = factor * *dtp;
+    const dbl4 ri = c.rs[k];
+    const float4 pi = c.posf[k];
+    const unsigned long long sbi = c.sbits[k];
+    const double radius = 2. * __longlong_as_double(static_cast<long long>(sbi));
     const double radiusSqr = radius * radius;
-    const int cx = nbCellCoord(ri.x, gi.lo[0], gi.inv_cell, gi.dims[0]);
-    const int cy = nbCellCoord(ri.y, gi.lo[1], gi.inv_cell, gi.dims[1]);
-    const int cz = nbCellCoord(ri.z, gi.lo[2], gi.inv_cell, gi.dims[2]);
+    const float slack = float(radius) * 1e-6f + float(gi.cell) * 2e-5f;
+    const float rOut = float(radius) + slack;
+    const float rIn = float(radius) - slack;
+    const float rOut2 = rOut * rOut;
+    const float rIn2 = rIn > 0.f ? rIn * rIn : -1.f;
+    const uint32_t key = g.keys_sorted[k];
+    const int cx = int(key % uint32_t(gi.dims[0]));
+    const int cy = int((key / uint32_t(gi.dims[0])) % uint32_t(gi.dims[1]));
+    const int cz = int(key / (uint32_t(gi.dims[0]) * uint32_t(gi.dims[1])));
+    const float cellf = float(gi.cell);
+    int x0, x1, y0, y1, z0, z1;
+    cellSpan(ri.x, radius, gi.lo[0], gi.inv_cell, gi.dims[0], x0, x1);
+    cellSpan(ri.y, radius, gi.lo[1], gi.inv_cell, gi.dims[1], y0, y1);
+    cellSpan(ri.z, radius, gi.lo[2], gi.inv_cell, gi.dims[2], z0, z1);
     Cand best{ INFINITY, 0., 0u };
     bool any = false;
-    for (int z = max(cz - 1, 0); z <= min(cz + 1, gi.dims[2] - 1); ++z) {
-        for (int y = max(cy - 1, 0); y <= min(cy + 1, gi.dims[1] - 1); ++y) {
-            for (int x = max(cx - 1, 0); x <= min(cx + 1, gi.dims[0] - 1); ++x) {
+    dbl4 vi, wi;
+    double mi = 0.;
+    bool own = false;
+    for (int z = z0; z <= z1; ++z) {
+        const float oz = float(z - cz) * cellf - pi.z;
+        for (int y = y0; y <= y1; ++y) {
+            const float oy = float(y - cy) * cellf - pi.y;
+            for (int x = x0; x <= x1; ++x) {
+                const float ox = float(x - cx) * cellf - pi.x;
                 const uint32_t cell = (uint32_t(z) * uint32_t(gi.dims[1]) + uint32_t(y)) * uint32_t(gi.dims[0]) +
                                       uint32_t(x);
                 const uint32_t end = g.cell_end[cell];
                 for (uint32_t q = g.cell_start[cell]; q < end; ++q) {
+                    if (q == k) {
+                        continue;
+                    }
+                    const float4 pj = c.posf[q];
+                    const float dx = pj.x + ox, dy = pj.y + oy, dz = pj.z + oz;
+                    const float d2 = dx * dx + dy * dy + dz * dz;
+                    if (d2 > rOut2) {
+                        continue;
+                    }
+                    const unsigned long long sbj = c.sbits[q];
                     const uint32_t j = g.perm[q];
-                    if (j == i) {
+                    if (!(sbj < sbi || (sbj == sbi && j < i))) {
                         continue;
                     }
-                    const dbl4 rj = s.r[j];
-                    if (!(len2(sub4(rj, ri)) < radiusSqr)) {
-                        continue;
-                    }
-                    const double sj = c.s[j];
-                    if (!(sj < si || (sj == si && j < i))) {
-                        continue;
+                    dbl4 rj;
+                    if (d2 >= rIn2) {
+                        rj = c.rs[q];
+                        if (!(len2(sub4(rj, ri)) < radiusSqr)) {
+                            continue;
+                        }
                     }
                     any = true;
                     atomicMax(&c.writer[j], int32_t(i));
@@ -441,6 +514,13 @@ __global__ void detectKernel(DState s, Grid g, Collide c, CollideParams p, const
                         // first pass (it is cleared after it, NBodySolver.cpp:367-396)
                         continue;
                     }
+                    if (!own) {
+                        vi = s.v[i];
+                        wi = s.omega[i];
+                        mi = s.m[i];
+                        own = true;
+                    }
+                    rj = c.rs[q];
                     const Cand cd = evalPair(p, j, ri, vi, mi, wi, rj, s.v[j], s.m[j], s.omega[j], 0., dt);
                     if (candLess(cd, best)) {
                         best = cd;
@@ -658,9 +738,10 @@ __device__ Cand researchWarp(const DState& s, const Grid& g, const GridInfo& gi,
     const double radiusSqr = radius * radius;
     const dbl4 ri = s.r[idx], vi = s.v[idx], wi = s.omega[idx];
     const double mi = s.m[idx];
-    const int cx = nbCellCoord(ri.x, gi.lo[0], gi.inv_cell, gi.dims[0]);
-    const int cy = nbCellCoord(ri.y, gi.lo[1], gi.inv_cell, gi.dims[1]);
-    const int cz = nbCellCoord(ri.z, gi.lo[2], gi.inv_cell, gi.dims[2]);
+    int x0, x1, y0, y1, z0, z1;
+    cellSpan(ri.x, radius, gi.lo[0], gi.inv_cell, gi.dims[0], x0, x1);
+    cellSpan(ri.y, radius, gi.lo[1], gi.inv_cell, gi.dims[1], y0, y1);
+    cellSpan(ri.z, radius, gi.lo[2], gi.inv_cell, gi.dims[2], z0, z1);
     auto consider = [&](uint32_t j) {
         if (j == idx) {
             return;
@@ -677,22 +758,21 @@ __device__ Cand researchWarp(const DState& s, const Grid& g, const GridInfo& gi,
             best = cd;
         }
     };
-    for (int z = max(cz - 1, 0); z <= min(cz + 1, gi.dims[2] - 1); ++z) {
-        for (int y = max(cy - 1, 0); y <= min(cy + 1, gi.dims[1] - 1); ++y) {
-            for (int x = max(cx - 1, 0); x <= min(cx + 1, gi.dims[0] - 1); ++x) {
-                const uint32_t cell = (uint32_t(z) * uint32_t(gi.dims[1]) + uint32_t(y)) * uint32_t(gi.dims[0]) +
-                                      uint32_t(x);
-                const uint32_t end = g.cell_end[cell];
-                for (uint32_t q = g.cell_start[cell] + lane; q < end; q += 32) {
-                    consider(g.perm[q]);
-                }
-                uint32_t cnt = 0;
-                for (int32_t e = a.extraHead[cell]; e >= 0; e = a.extra[3 * e + 1], ++cnt) {
-                    if (int(cnt & 31u) == lane) {
-                        consider(uint32_t(a.extra[3 * e]));
-                    }
-                }
-            }
+    // the lanes take the cells of the box (a cell holds a few particles; the latency of the cell ranges is
+    // paid once per 32 cells instead of once per cell)
+    const int nx = x1 - x0 + 1, ny = y1 - y0 + 1;
+    const int ncell = nx * ny * (z1 - z0 + 1);
+    for (int b = lane; b < ncell; b += 32) {
+        const int x = x0 + b % nx;
+        const int y = y0 + (b / nx) % ny;
+        const int z = z0 + b / (nx * ny);
+        const uint32_t cell = (uint32_t(z) * uint32_t(gi.dims[1]) + uint32_t(y)) * uint32_t(gi.dims[0]) + uint32_t(x);
+        const uint32_t end = g.cell_end[cell];
+        for (uint32_t q = g.cell_start[cell]; q < end; ++q) {
+            consider(g.perm[q]);
+        }
+        for (int32_t e = a.extraHead[cell]; e >= 0; e = a.extra[3 * e + 1]) {
+            consider(uint32_t(a.extra[3 * e]));
         }
     }
     candShflMin(best);
@@ -1006,6 +1086,9 @@ cudaError_t collideAllocate(Collide& c, uint32_t n, uint32_t cellCapacity) {
     A(&c.extra, 3 * size_t(c.extra_capacity));
     A(&c.counters, CNT_COUNT);
     A(&c.scan, nn);
+    A(&c.rs, nn);
+    A(&c.posf, nn);
+    A(&c.sbits, nn);
     if (e == cudaSuccess) {
         e = cudaMallocHost((void**)&c.counters_host, CNT_COUNT * sizeof(unsigned long long));
     }
@@ -1036,7 +1119,8 @@ cudaError_t collideAllocate(Collide& c, uint32_t n, uint32_t cellCapacity) {
 
 void collideFree(Collide& c) {
     void* ptrs[] = { c.s, c.srad, c.nsel, c.writer, c.ver, c.bounces, c.removed, c.prev_removed, c.head, c.moved_cell, c.pool,
-        c.valid, c.order_a, c.order_b, c.key_a, c.key_b, c.extra_head, c.extra, c.counters, c.temp, c.scan };
+        c.valid, c.order_a, c.order_b, c.key_a, c.key_b, c.extra_head, c.extra, c.counters, c.temp, c.scan, c.rs,
+        c.posf, c.sbits };
     for (void* p : ptrs) {
         if (p) {
             cudaFree(p);
@@ -1059,8 +1143,9 @@ int nbodyCollide(DState& s, Grid& g, Collide& c, const CollideParams& p, const d
     const int blocks = ceilDiv(n, 256);
     prepareKernel<<<blocks, 256, 0, st>>>(s, c, dt, factor);
     launchGridBuildRadius(s.r, c.s, n, g, st);
+    gatherKernel<<<blocks, 256, 0, st>>>(s, g, c);
     detectKernel<<<ceilDiv(n, 128), 128, 0, st>>>(s, g, c, p, dt, factor);
-    c.launches += 2 + g.launches;
+    c.launches += 3 + g.launches;
     size_t bytes = c.temp_bytes;
     cudaError_t e = cub::DeviceScan::ExclusiveSum(c.temp, bytes, c.valid, c.scan, int(n), st);
     if (e != cudaSuccess) {

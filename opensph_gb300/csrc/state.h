@@ -121,6 +121,9 @@ struct Collide {
     void* temp = nullptr;
     size_t temp_bytes = 0;
     uint32_t* scan = nullptr;    // compaction offsets
+    dbl4* rs = nullptr;          // cell-sorted positions (first pass)
+    float4* posf = nullptr;      // cell-sorted FP32 positions relative to the cell origin, 2 s
+    unsigned long long* sbits = nullptr; // cell-sorted bit patterns of s
     // compaction targets, swapped with the state arrays (allocated and freed with the state arrays)
     dbl4* tmp_r = nullptr;
     dbl4* tmp_v = nullptr;
@@ -264,7 +267,8 @@ void launchCountPairs(const DState& s, const Grid& g, unsigned long long* count,
 void launchListPairs(const DState& s, const Grid& g, uint32_t* pi, uint32_t* pj, unsigned long long* count,
     unsigned long long capacity, cudaStream_t st);
 
-// grid of cell edge >= 2 max(radius) over the positions r (radius NULL: the h of r), for the collision search
+// grid over the positions r: radius NULL -> cell edge >= 2 max h (27-cell stencil of the pair loops); else the
+// collision grid, cell edge 2 max(mean radius, max radius / 8), searched over each particle's own cell box
 void launchGridBuildRadius(const dbl4* r, const double* radius, uint32_t n, Grid& g, cudaStream_t st);
 
 // ---- launchers (sph64.cu) ----

@@ -198,3 +198,38 @@ def plummer(n, seed=7, softening=1.0e-3, rmax=20.0):
     st = np.sqrt(1.0 - ct * ct)
     r = np.stack([rad * st * np.cos(ph), rad * st * np.sin(ph), rad * ct, np.full(n, softening)], 1)
     return r, np.full(n, 1.0 / n)
+
+
+def rubble_cloud(n, radius, h=400.0, density=2500.0, inflow=1.0e-4, sigma=0.05, seed=5):
+    """A cloud of n hard spheres for the N-body solver (the reaccumulation phase of the reference's
+    impact presets, core/run/jobs/Presets.cpp:48): radii h (1 + U/2), density `density`, centres on a
+    randomly jittered cubic lattice inside a sphere of `radius` (jitter small enough that no two spheres
+    overlap), velocity -inflow r plus a normal dispersion sigma. Returns a state dict r, v, dv, m, w."""
+    rng = np.random.default_rng(seed)
+    spacing = (4.0 / 3.0 * math.pi * radius ** 3 / n) ** (1.0 / 3.0)
+    hmax = 1.5 * h
+    if spacing <= 2.0 * hmax:
+        raise ValueError("the cloud is too dense for non-overlapping spheres")
+    m = int(math.ceil(2.0 * radius / spacing)) + 2
+    g = (np.arange(m) - (m - 1) / 2.0) * spacing
+    x, y, z = np.meshgrid(g, g, g, indexing="ij")
+    p = np.stack([x.ravel(), y.ravel(), z.ravel()], axis=1)
+    p = p[np.linalg.norm(p, axis=1) <= radius]
+    while len(p) < n:
+        spacing *= 0.99
+        g = (np.arange(m + 2) - (m + 1) / 2.0) * spacing
+        x, y, z = np.meshgrid(g, g, g, indexing="ij")
+        p = np.stack([x.ravel(), y.ravel(), z.ravel()], axis=1)
+        p = p[np.linalg.norm(p, axis=1) <= radius]
+        m += 2
+    p = p[rng.permutation(len(p))[:n]]
+    hi = h * (1.0 + 0.5 * rng.random(n))
+    jitter = 0.5 * (spacing - 2.0 * hmax) * 0.999
+    p = p + rng.uniform(-jitter, jitter, size=(n, 3))
+    r = np.zeros((n, 4))
+    r[:, :3] = p
+    r[:, 3] = hi
+    v = np.zeros((n, 4))
+    v[:, :3] = -inflow * p + sigma * rng.standard_normal((n, 3))
+    mass = density * 4.0 / 3.0 * math.pi * hi ** 3
+    return {"r": r.ravel(), "v": v.ravel(), "dv": np.zeros(4 * n), "m": mass, "w": np.zeros(4 * n)}

@@ -49,8 +49,10 @@ def parse():
     ap.add_argument("--no-nbody", action="store_true", help="skip the gravity-only Plummer measurement")
     ap.add_argument("--nbody-n", type=int, default=4_194_304)
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurement")
-    ap.add_argument("--only", choices=["nbody", "adjoint"], default=None,
-                    help="run only the gravity-only or the adjoint measurement and print its JSON (for profiling)")
+    ap.add_argument("--no-reaccumulation", action="store_true", help="skip the N-body collision measurement")
+    ap.add_argument("--reacc-n", type=int, default=1_000_000)
+    ap.add_argument("--only", choices=["nbody", "adjoint", "reaccumulation"], default=None,
+                    help="run only one of the secondary measurements and print its JSON (for profiling)")
     ap.add_argument("--adjoint-target", type=int, default=100_000)
     ap.add_argument("--adjoint-impactor", type=int, default=2_000)
     return ap.parse_args()
@@ -237,6 +239,8 @@ def run_gpu(args, rank, world):
         result["nbody"] = nbody(args, dev)
     if rank == 0 and not args.no_adjoint:
         result["adjoint"] = adjoint(args, dev)
+    if rank == 0 and not args.no_reaccumulation:
+        result["reaccumulation"] = reaccumulation(args, dev)
     return result
 
 
@@ -338,6 +342,64 @@ def nbody(args, dev):
     a, b = accs["mixed"].reshape(-1, 4)[:, :3], accs["fp64"].reshape(-1, 4)[:, :3]
     out["mixed_vs_fp64_rel_err"] = float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
     torch.cuda.synchronize()
+    return out
+
+
+def reaccumulation(args, dev):
+    """N-body workload (HardSphereSolver, the reaccumulation phase of the reference's impact presets): a cloud of
+    hard spheres (radius 400-600 m, density 2500, radius 140 km for 1M spheres, inflow 2e-4 r plus a 0.1 m/s
+    dispersion), the N-body run's settings (leap-frog, acceleration criterion, BH theta 0.8 with solid spheres,
+    merge-or-bounce collisions, pass-or-merge overlaps), max step 100 s. Mixed-precision walk; collisions in
+    FP64. Timed K steps after W warm-up steps; CPU baseline: one step of the oracle on all host cores."""
+    import torch
+
+    from opensph_gb300 import abi, initial
+    from opensph_gb300.solver import GpuSolver
+    from oracle import oracle
+
+    n = args.reacc_n
+    radius = 140000.0 * (n / 1.0e6) ** (1.0 / 3.0)
+    st = initial.rubble_cloud(n, radius, inflow=2e-4, sigma=0.1)
+    cfg, keep = abi.make_nbody_config(n, max_timestep=100.0, initial_timestep=100.0, precision=abi.PRECISION_MIXED)
+    cfg.device = dev
+    with GpuSolver(cfg, keep) as g:
+        g.set_state(st)
+        g.step(args.warmup)
+        g.synchronize()
+        stats0 = g.collision_stats()
+        g.set_profiling(True)
+        g.phase_times()
+        stream = torch.cuda.ExternalStream(g.stream)
+        torch.cuda.synchronize()
+        start = torch.cuda.Event(enable_timing=True)
+        end = torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        g.step(args.steps)
+        end.record(stream)
+        end.synchronize()
+        ms = start.elapsed_time(end)
+        phases, launches = g.phase_times()
+        stats1 = g.collision_stats()
+        n_end = g.n
+        dt_end = g.timestep
+    events = [(b - a) / args.steps for a, b in zip(stats0, stats1)]
+    out = {"particles": n, "particles_after": n_end, "workload": "rubble cloud, N-body with collisions",
+           "ms_per_step": ms / args.steps, "value": n * args.steps / (ms * 1e-3), "unit": UNIT,
+           "events_per_step": {"collisions": events[0], "mergers": events[1], "bounces": events[2],
+                               "overlaps": events[3]},
+           "phases_ms_per_step": {k: v / args.steps for k, v in phases.items() if v > 0},
+           "gpu_launches": launches, "timestep_after": dt_end}
+    if not args.no_cpu:
+        work = initial.rubble_cloud(n, radius, inflow=2e-4, sigma=0.1)
+        cfg64, keep64 = abi.make_nbody_config(n, max_timestep=100.0, initial_timestep=100.0)
+        oracle.set_threads(0)
+        t0 = time.perf_counter()
+        oracle.nbody_run(cfg64, work, 1, 100.0)
+        secs = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": n / secs, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+                               "sample": f"1 step of the {n}-particle cloud from its initial state ({secs:.1f} s, "
+                                         "FP64 oracle, gravity on all host threads, collisions sequential after "
+                                         "a parallel first pass)"}
     return out
 
 
@@ -464,7 +526,7 @@ def main():
     if args.only is not None:
         dev = int(os.environ.get("LOCAL_RANK", "0"))
         torch.cuda.set_device(dev)
-        out = nbody(args, dev) if args.only == "nbody" else adjoint(args, dev)
+        out = {"nbody": nbody, "adjoint": adjoint, "reaccumulation": reaccumulation}[args.only](args, dev)
         print(json.dumps({args.only: out}))
         return
 
@@ -512,6 +574,8 @@ def main():
         line["nbody_plummer"] = res["nbody"]
     if "adjoint" in res:
         line["adjoint"] = res["adjoint"]
+    if "reaccumulation" in res:
+        line["nbody_reaccumulation"] = res["reaccumulation"]
     if not args.no_cpu:
         st, mats, n2 = workload(args)
         value, secs = cpu_sample(args, st, mats, n2, args.cpu_steps)

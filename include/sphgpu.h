@@ -192,6 +192,10 @@ typedef struct {
     double rotation_merge_limit;       /* COLLISION_ROTATION_MERGE_LIMIT */
     uint32_t max_bounces;              /* COLLISION_MAX_BOUNCES */
     uint32_t reserved2;
+    /* GRAVITY_RECOMPUTATION_PERIOD (CachedGravity, core/gravity/CachedGravity.h): with a positive value the
+     * self-gravity accelerations are reused while the run time is less than this period after their last
+     * evaluation and the particle count is unchanged; 0 = every evaluation */
+    double gravity_recomputation_period;
 } sphgpu_config;
 
 typedef struct sphgpu_handle sphgpu_handle;
@@ -250,6 +254,9 @@ sphgpu_status sphgpu_integrate(sphgpu_handle* h);
 sphgpu_status sphgpu_step(sphgpu_handle* h, uint32_t nsteps);
 sphgpu_status sphgpu_get_timestep(sphgpu_handle* h, double* dt);
 sphgpu_status sphgpu_set_timestep(sphgpu_handle* h, double dt);
+/* Run time (StatisticsId::RUN_TIME): 0 at creation, advanced by every step by the step taken. */
+sphgpu_status sphgpu_get_time(sphgpu_handle* h, double* t);
+sphgpu_status sphgpu_set_time(sphgpu_handle* h, double t);
 
 /* HardSphereSolver::collide (core/gravity/NBodySolver.cpp:329-484) over the interval [0, dt): finds every
  * particle's earliest collision or overlap, resolves them in time order (re-searching the particles whose
@@ -261,6 +268,10 @@ sphgpu_status sphgpu_particle_count(sphgpu_handle* h, uint64_t* n);
 /* StatisticsId::TOTAL_COLLISION_COUNT, MERGER_COUNT, BOUNCE_COUNT, OVERLAP_COUNT (core/gravity/NBodySolver.cpp:
  * 119-163), summed over all collide calls since the handle was created. */
 sphgpu_status sphgpu_collision_stats(sphgpu_handle* h, uint64_t out[4]);
+/* Profile of the collision loop summed over all collide calls: out[0] records processed, out[1..3] SM clock
+ * cycles spent in its serial part (selection, handler, invalidation), in the re-searches and in inserting the
+ * new records. */
+sphgpu_status sphgpu_collision_profile(sphgpu_handle* h, uint64_t out[4]);
 
 /* Conserved totals (core/physics/Integrals.h:62-148) as compensated FP64 device reductions:
  * out[0..2] momentum, out[3..5] angular momentum about the origin, out[6] kinetic energy,

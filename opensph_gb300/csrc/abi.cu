@@ -30,6 +30,12 @@ struct sphgpu_handle {
     float* d_lut_grav_f = nullptr;
     double* d_dt = nullptr;
     double* d_dt_min = nullptr;
+    double* d_time = nullptr;      // run time (StatisticsId::RUN_TIME), advanced by every step
+    // CachedGravity (core/gravity/CachedGravity.h): time and particle count of the last gravity evaluation,
+    // and whether the current evaluation reuses it
+    double gravity_t_last = -INFINITY;
+    uint32_t gravity_n_last = 0;
+    bool gravity_cached = false;
     uint32_t* d_err = nullptr;
     double* d_tot_partial = nullptr;
     double* d_tot = nullptr;
@@ -320,6 +326,9 @@ sphgpu_status checkDeviceError(sphgpu_handle* h) {
 // gravity build + walk into s.agrav (GravitySolver::loop, first half)
 // BarnesHut::build + evalSelfGravity into s.agrav, queued on stream st
 sphgpu_status evalGravity(sphgpu_handle* h, cudaStream_t st) {
+    if (h->gravity_cached) {
+        return SPHGPU_OK; // CachedGravity: s.agrav still holds the accelerations of the last evaluation
+    }
     {
         Phase ph(h, SPHGPU_PHASE_GRAVITY_BUILD, st);
         cudaError_t e = treeBuild(h->s, h->tree, h->ph, h->d_err, st);
@@ -407,6 +416,29 @@ sphgpu_status evalDerivatives(sphgpu_handle* h) {
     return SPHGPU_OK;
 }
 
+// CachedGravity::evalSelfGravity (core/gravity/CachedGravity.h:45-63, wrapped around the gravity by
+// Factory::getGravity for a positive GRAVITY_RECOMPUTATION_PERIOD, core/system/Factory.cpp:405-409): the
+// accelerations of the last evaluation are reused while the run time is less than one period after it and the
+// particle count is unchanged. Reads the run time from the device (one synchronisation per evaluation, with a
+// positive period only).
+sphgpu_status decideGravityCache(sphgpu_handle* h) {
+    h->gravity_cached = false;
+    const double period = h->cfg.gravity_recomputation_period;
+    if (!(period > 0.) || !h->ph.gravity) {
+        return SPHGPU_OK;
+    }
+    CUDA_TRY(h, cudaMemcpyAsync(h->h_pinned, h->d_time, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    const double t = *reinterpret_cast<const double*>(h->h_pinned);
+    if (h->s.n == h->gravity_n_last && t - h->gravity_t_last < period) {
+        h->gravity_cached = true;
+    } else {
+        h->gravity_t_last = t;
+        h->gravity_n_last = h->s.n;
+    }
+    return SPHGPU_OK;
+}
+
 // HardSphereSolver::collide over [0, factor * dt) (dt on the device)
 sphgpu_status collideNbody(sphgpu_handle* h, const double* dt, double factor) {
     Phase ph(h, SPHGPU_PHASE_COLLIDE);
@@ -450,6 +482,10 @@ sphgpu_status stepNbody(sphgpu_handle* h) {
         launchNbodyDrift(h->s, h->ph, h->d_dt, h->d_dt_min, false, h->stream);
         h->launches += 1;
     }
+    st = decideGravityCache(h);
+    if (st != SPHGPU_OK) {
+        return st;
+    }
     st = integrateNbody(h, true);
     if (st != SPHGPU_OK) {
         return st;
@@ -461,11 +497,8 @@ sphgpu_status stepNbody(sphgpu_handle* h) {
     Phase ph(h, SPHGPU_PHASE_CORRECT);
     const bool criterion = (h->ph.criteria & SPHGPU_CRITERION_ACCELERATION) != 0;
     launchNbodyDrift(h->s, h->ph, h->d_dt, h->d_dt_min, criterion, h->stream);
-    h->launches += 1;
-    if (criterion) {
-        launchCourantFinish(h->d_dt, h->d_dt_min, h->ph.max_dt, h->ph.max_change, h->stream);
-        h->launches += 1;
-    }
+    launchStepEnd(h->d_dt, h->d_dt_min, h->ph.max_dt, h->ph.max_change, h->d_time, criterion, h->stream);
+    h->launches += 2;
     return SPHGPU_OK;
 }
 
@@ -492,6 +525,9 @@ sphgpu_status validate(const sphgpu_config* c) {
     }
     if (c->material_count > 0 && !c->materials) {
         return fail(nullptr, SPHGPU_ERR_ARGUMENT, "materials is NULL");
+    }
+    if (!(c->gravity_recomputation_period >= 0.)) {
+        return fail(nullptr, SPHGPU_ERR_ARGUMENT, "gravity_recomputation_period must not be negative");
     }
     if (c->gravity_kernel < SPHGPU_GRAVITY_KERNEL_POINT_PARTICLES ||
         c->gravity_kernel > SPHGPU_GRAVITY_KERNEL_SOLID_SPHERES) {
@@ -739,6 +775,7 @@ sphgpu_status sphgpu_create(const sphgpu_config* config, sphgpu_handle** out) {
     A(&h->d_lut_grav_f, LUT_ENTRIES + 1);
     A(&h->d_dt, 1);
     A(&h->d_dt_min, 1);
+    A(&h->d_time, 1);
     A(&h->d_err, 1);
     A(&h->d_tot_partial, 256 * 9);
     A(&h->d_tot, 9);
@@ -796,6 +833,9 @@ sphgpu_status sphgpu_create(const sphgpu_config* config, sphgpu_handle** out) {
     }
     if (e == cudaSuccess) {
         e = cudaMemset(s.u, 0, nn * sizeof(double));
+    }
+    if (e == cudaSuccess) {
+        e = cudaMemset(h->d_time, 0, sizeof(double));
     }
     if (e == cudaSuccess && s.omega) {
         // HardSphereSolver::create inserts ANGULAR_FREQUENCY = 0 (core/gravity/NBodySolver.cpp:487-490)
@@ -1132,6 +1172,10 @@ sphgpu_status sphgpu_integrate(sphgpu_handle* h) {
     if (!h) {
         return SPHGPU_ERR_ARGUMENT;
     }
+    const sphgpu_status cst = decideGravityCache(h);
+    if (cst != SPHGPU_OK) {
+        return cst;
+    }
     if (h->ph.nbody) {
         const sphgpu_status st = integrateNbody(h, false);
         if (st != SPHGPU_OK) {
@@ -1169,6 +1213,12 @@ sphgpu_status sphgpu_step(sphgpu_handle* h, uint32_t nsteps) {
         }
         const bool lf = h->ph.integrator == SPHGPU_INTEGRATOR_LEAP_FROG;
         {
+            const sphgpu_status cst = decideGravityCache(h);
+            if (cst != SPHGPU_OK) {
+                return cst;
+            }
+        }
+        {
             Phase ph(h, SPHGPU_PHASE_PREDICT);
             if (lf) {
                 launchLeapFrogDriftInit(h->s, h->ph, h->d_mats, h->d_dt, h->stream);
@@ -1189,7 +1239,7 @@ sphgpu_status sphgpu_step(sphgpu_handle* h, uint32_t nsteps) {
             } else {
                 launchCorrect(h->s, h->ph, h->d_mats, h->d_dt, h->d_dt_min, h->stream);
             }
-            launchCourantFinish(h->d_dt, h->d_dt_min, h->ph.max_dt, h->ph.max_change, h->stream);
+            launchStepEnd(h->d_dt, h->d_dt_min, h->ph.max_dt, h->ph.max_change, h->d_time, true, h->stream);
             h->launches += 2;
         }
         CUDA_TRY(h, cudaGetLastError());
@@ -1367,6 +1417,16 @@ sphgpu_status sphgpu_particle_count(sphgpu_handle* h, uint64_t* n) {
     return SPHGPU_OK;
 }
 
+sphgpu_status sphgpu_collision_profile(sphgpu_handle* h, uint64_t out[4]) {
+    if (!h || !out) {
+        return SPHGPU_ERR_ARGUMENT;
+    }
+    for (int k = 0; k < 4; ++k) {
+        out[k] = h->coll.profile[k];
+    }
+    return SPHGPU_OK;
+}
+
 sphgpu_status sphgpu_collision_stats(sphgpu_handle* h, uint64_t out[4]) {
     if (!h || !out) {
         return SPHGPU_ERR_ARGUMENT;
@@ -1374,6 +1434,24 @@ sphgpu_status sphgpu_collision_stats(sphgpu_handle* h, uint64_t out[4]) {
     for (int k = 0; k < 4; ++k) {
         out[k] = h->coll.totals[k];
     }
+    return SPHGPU_OK;
+}
+
+sphgpu_status sphgpu_get_time(sphgpu_handle* h, double* t) {
+    if (!h || !t) {
+        return SPHGPU_ERR_ARGUMENT;
+    }
+    CUDA_TRY(h, cudaMemcpyAsync(t, h->d_time, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return SPHGPU_OK;
+}
+
+sphgpu_status sphgpu_set_time(sphgpu_handle* h, double t) {
+    if (!h) {
+        return SPHGPU_ERR_ARGUMENT;
+    }
+    CUDA_TRY(h, cudaMemcpyAsync(h->d_time, &t, sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     return SPHGPU_OK;
 }
 

@@ -72,6 +72,9 @@ enum {
     CNT_REMOVED = 5,    // particles removed by this call
     CNT_ERROR = 6,      // capacity error bits
     CNT_EVENTS = 7,     // records processed
+    CNT_CYCLES_LEAD = 8,   // SM cycles of the event loop in its serial part (selection, handler, invalidation)
+    CNT_CYCLES_SEARCH = 9, // in the re-searches
+    CNT_CYCLES_INSERT = 10, // in the insertion of new records
     CNT_COUNT = 16
 };
 enum : unsigned long long {
@@ -796,6 +799,7 @@ __global__ void __launch_bounds__(EV_THREADS, 1) eventKernel(DState s, Grid g, E
         sh.heapSize = 0;
     }
     __syncthreads();
+    long long tLead = 0, tSearch = 0, tInsert = 0, t0 = clock64();
     while (true) {
         if (tid == 0) {
             sh.done = 1;
@@ -878,6 +882,11 @@ __global__ void __launch_bounds__(EV_THREADS, 1) eventKernel(DState s, Grid g, E
             }
         }
         __syncthreads();
+        if (tid == 0) {
+            const long long t1 = clock64();
+            tLead += t1 - t0;
+            t0 = t1;
+        }
         if (sh.done) {
             break;
         }
@@ -894,6 +903,11 @@ __global__ void __launch_bounds__(EV_THREADS, 1) eventKernel(DState s, Grid g, E
             }
         }
         __syncthreads();
+        if (tid == 0) {
+            const long long t1 = clock64();
+            tSearch += t1 - t0;
+            t0 = t1;
+        }
         if (tid == 0 && sh.search) {
             for (uint32_t k = 0; k < sh.invCount; ++k) {
                 const Cand c = sh.res[k];
@@ -931,6 +945,11 @@ __global__ void __launch_bounds__(EV_THREADS, 1) eventKernel(DState s, Grid g, E
             }
         }
         __syncthreads();
+        if (tid == 0) {
+            const long long t1 = clock64();
+            tInsert += t1 - t0;
+            t0 = t1;
+        }
     }
     if (tid == 0) {
         // the moved-particle lists start empty in the next call
@@ -944,6 +963,9 @@ __global__ void __launch_bounds__(EV_THREADS, 1) eventKernel(DState s, Grid g, E
         a.counters[CNT_REMOVED] = removedCount;
         a.counters[CNT_ERROR] = err;
         a.counters[CNT_EVENTS] = nEvents;
+        a.counters[CNT_CYCLES_LEAD] = (unsigned long long)tLead;
+        a.counters[CNT_CYCLES_SEARCH] = (unsigned long long)tSearch;
+        a.counters[CNT_CYCLES_INSERT] = (unsigned long long)tInsert;
     }
 }
 
@@ -1217,6 +1239,10 @@ int nbodyCollide(DState& s, Grid& g, Collide& c, const CollideParams& p, const d
     for (int k = 0; k < 4; ++k) {
         c.totals[k] += cnt[k];
     }
+    c.profile[0] += cnt[CNT_EVENTS];
+    c.profile[1] += cnt[CNT_CYCLES_LEAD];
+    c.profile[2] += cnt[CNT_CYCLES_SEARCH];
+    c.profile[3] += cnt[CNT_CYCLES_INSERT];
     const uint32_t removed = uint32_t(cnt[CNT_REMOVED]);
     if (removed > 0) {
         keepFlagsKernel<<<blocks, 256, 0, st>>>(n, c.removed, c.valid);

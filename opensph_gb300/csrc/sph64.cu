@@ -542,9 +542,14 @@ __global__ void leapFrogKickKernel(DState s, Physics ph, const MaterialD* __rest
     blockMinToGlobal(local, dtMin);
 }
 
-// the step minimum capped by the maximal step, then limited to (1 + maxChange) times the previous step
-// (MultiCriterion::compute's smoothing, off for maxChange >= DBL_MAX)
-__global__ void courantFinishKernel(double* dt, double* dtMin, double maxDt, double maxChange) {
+// end of a step: the run time advances by the step just taken; with criteria, the next step is the minimum
+// capped by the maximal step, then limited to (1 + maxChange) times the previous step (MultiCriterion::
+// compute's smoothing, off for maxChange >= DBL_MAX)
+__global__ void stepEndKernel(double* dt, double* dtMin, double maxDt, double maxChange, double* time, int criterion) {
+    *time += *dt;
+    if (!criterion) {
+        return;
+    }
     double m = *dtMin;
     m = m > maxDt ? maxDt : m;
     if (maxChange < DBL_MAX) {
@@ -698,8 +703,9 @@ void launchLeapFrogKick(const DState& s, const Physics& ph, const MaterialD* mat
     }
 }
 
-void launchCourantFinish(double* dt, double* dtMin, double maxDt, double maxChange, cudaStream_t st) {
-    courantFinishKernel<<<1, 1, 0, st>>>(dt, dtMin, maxDt, maxChange);
+void launchStepEnd(double* dt, double* dtMin, double maxDt, double maxChange, double* time, bool criterion,
+    cudaStream_t st) {
+    stepEndKernel<<<1, 1, 0, st>>>(dt, dtMin, maxDt, maxChange, time, criterion ? 1 : 0);
 }
 
 void launchTotals(const DState& s, double* partial, double* out, cudaStream_t st) {

@@ -132,6 +132,8 @@ struct Collide {
     double* tmp_m = nullptr;
     uint32_t launches = 0;
     unsigned long long totals[4] = { 0, 0, 0, 0 }; // collisions, mergers, bounces, overlaps (host copy)
+    // records processed by the event loop and its SM cycles in the serial part, the re-searches, the insertions
+    unsigned long long profile[4] = { 0, 0, 0, 0 };
 };
 
 // Neighbour grid buffers (cell-sorted copies of the pair-loop inputs)
@@ -284,7 +286,9 @@ void launchLeapFrogDriftInit(const DState& s, const Physics& ph, const MaterialD
     cudaStream_t st);
 void launchLeapFrogKick(const DState& s, const Physics& ph, const MaterialD* mats, const double* dt,
     double* dt_min, cudaStream_t st);
-void launchCourantFinish(double* dt, double* dt_min, double max_dt, double max_change, cudaStream_t st);
+// end of a step: time += dt; with criterion, dt = the criteria minimum capped by max_dt and max_change
+void launchStepEnd(double* dt, double* dt_min, double max_dt, double max_change, double* time, bool criterion,
+    cudaStream_t st);
 void launchTotals(const DState& s, double* partial, double* out, cudaStream_t st);
 void launchCheckFinite(const DState& s, unsigned long long* first_bad, cudaStream_t st);
 void launchAddGravity(const DState& s, cudaStream_t st);

@@ -55,6 +55,8 @@ def library():
     lib.sphgpu_integrate.argtypes = [h]
     lib.sphgpu_step.argtypes = [h, ctypes.c_uint32]
     lib.sphgpu_get_timestep.argtypes = [h, _F8P]
+    lib.sphgpu_get_time.argtypes = [h, _F8P]
+    lib.sphgpu_set_time.argtypes = [h, ctypes.c_double]
     lib.sphgpu_set_timestep.argtypes = [h, ctypes.c_double]
     lib.sphgpu_totals.argtypes = [h, _F8P]
     lib.sphgpu_check_finite.argtypes = [h, ctypes.POINTER(ctypes.c_uint64)]
@@ -65,6 +67,7 @@ def library():
     lib.sphgpu_collide.argtypes = [h, ctypes.c_double]
     lib.sphgpu_particle_count.argtypes = [h, ctypes.POINTER(ctypes.c_uint64)]
     lib.sphgpu_collision_stats.argtypes = [h, ctypes.POINTER(ctypes.c_uint64)]
+    lib.sphgpu_collision_profile.argtypes = [h, ctypes.POINTER(ctypes.c_uint64)]
     _LIB = lib
     return lib
 
@@ -198,6 +201,12 @@ class GpuSolver:
         self._check(self._lib.sphgpu_collide(self._h, float(dt)))
         self._refresh_count()
 
+    def collision_profile(self):
+        """Records processed by the collision loop and its SM cycles (serial part, re-searches, insertions)."""
+        out = (ctypes.c_uint64 * 4)()
+        self._check(self._lib.sphgpu_collision_profile(self._h, out))
+        return list(out)
+
     def collision_stats(self):
         """Collisions, mergers, bounces and overlaps summed over all collide calls of this handle."""
         out = (ctypes.c_uint64 * 4)()
@@ -213,6 +222,16 @@ class GpuSolver:
     @timestep.setter
     def timestep(self, dt):
         self._check(self._lib.sphgpu_set_timestep(self._h, float(dt)))
+
+    @property
+    def time(self):
+        v = ctypes.c_double()
+        self._check(self._lib.sphgpu_get_time(self._h, ctypes.byref(v)))
+        return v.value
+
+    @time.setter
+    def time(self, t):
+        self._check(self._lib.sphgpu_set_time(self._h, float(t)))
 
     def pairs(self):
         cnt = ctypes.c_uint64(0)

@@ -222,12 +222,15 @@ void runSteps(Writer& w, RunSettings& settings, SharedPtr<Storage> storage, int 
     }
     dumpMaterials(w, *storage);
 
-    // one derivative evaluation on a copy of the initial state (ISolver::integrate alone)
+    // one derivative evaluation on a copy of the initial state (ISolver::integrate alone), on a solver of its own
+    // (a cached gravity would otherwise keep its accelerations)
     {
+        AutoPtr<ISolver> probeSolver = Factory::getSolver(*scheduler, settings);
         Storage probe = storage->clone(VisitorEnum::ALL_BUFFERS);
         probe.zeroHighestDerivatives(*scheduler);
         Statistics stats;
-        solver->integrate(probe, stats);
+        stats.set(StatisticsId::RUN_TIME, 0._f);
+        probeSolver->integrate(probe, stats);
         dumpState(w, "d0_", probe);
     }
 
@@ -235,8 +238,12 @@ void runSteps(Writer& w, RunSettings& settings, SharedPtr<Storage> storage, int 
     dumpState(w, "s0_", *storage);
     std::vector<double> dts;
     Statistics stats;
+    double t = 0.;
     for (int step = 0; step < steps; ++step) {
         dts.push_back(ts->getTimeStep());
+        // the run time of the step, as the run loop sets it (core/run/IRun.cpp), read by CachedGravity
+        stats.set(StatisticsId::RUN_TIME, t);
+        t += ts->getTimeStep();
         ts->step(*scheduler, *solver, stats);
         if (step == 0) {
             dumpState(w, "s1_", *storage);
@@ -252,6 +259,8 @@ void runSteps(Writer& w, RunSettings& settings, SharedPtr<Storage> storage, int 
 bool gAllCriteria = false;
 // the AsymmetricSolver with the strain-rate correction tensor (mode name ending in "_asym")
 bool gAsymmetric = false;
+// CachedGravity with this recomputation period (mode name ending in "_cached"; the period is the last argument)
+double gRecomputationPeriod = 0.;
 
 RunSettings baseSettings() {
     RunSettings settings;
@@ -272,6 +281,9 @@ RunSettings baseSettings() {
     if (gAsymmetric) {
         settings.set(RunSettingsId::SPH_SOLVER_TYPE, SolverEnum::ASYMMETRIC_SOLVER);
         settings.set(RunSettingsId::SPH_STRAIN_RATE_CORRECTION_TENSOR, true);
+    }
+    if (gRecomputationPeriod > 0.) {
+        settings.set(RunSettingsId::GRAVITY_RECOMPUTATION_PERIOD, gRecomputationPeriod);
     }
     return settings;
 }
@@ -611,6 +623,11 @@ int main(int argc, char** argv) {
     if (mode.size() > 4 && mode.compare(mode.size() - 4, 4, "_all") == 0) {
         gAllCriteria = true;
         mode = mode.substr(0, mode.size() - 4);
+    }
+    if (mode.size() > 7 && mode.compare(mode.size() - 7, 7, "_cached") == 0) {
+        gRecomputationPeriod = std::atof(argv[argc - 1]);
+        --argc;
+        mode = mode.substr(0, mode.size() - 7);
     }
     if (mode.size() > 5 && mode.compare(mode.size() - 5, 5, "_asym") == 0) {
         gAsymmetric = true;

@@ -1117,6 +1117,38 @@ bool hasRheology(const sphgpu_material& mt) {
     return mt.yielding != SPHGPU_YIELDING_NONE;
 }
 
+// CachedGravity (core/gravity/CachedGravity.h:45-63): the run time of the current step and the accelerations
+// of the last evaluation, reused while the run time is less than the recomputation period after it and the
+// particle count is unchanged (reset at the start of every run)
+struct GravityCache {
+    double runTime = 0.;
+    double tLast = -INFINITY;
+    uint64_t n = 0;
+    std::vector<double> acc;
+};
+GravityCache gCache;
+
+// BarnesHut::evalSelfGravity into acc (4n, zeroed), through the cache for a positive recomputation period
+void selfGravity(const sphgpu_config& cfg, uint64_t n, const double* r, const double* m, std::vector<double>& acc) {
+    const double period = cfg.gravity_recomputation_period;
+    if (period > 0. && gCache.n == n && gCache.runTime - gCache.tLast < period) {
+        acc = gCache.acc;
+        return;
+    }
+    BarnesHutTree bh;
+    bh.leafSize = cfg.gravity_leaf_size;
+    bh.thetaInv = 1. / cfg.gravity_opening_angle;
+    bh.order = cfg.gravity_multipole_order;
+    bh.kernelRadius = kernelRadiusOf(cfg);
+    bh.build(n, r, m, cfg.gravity_constant);
+    bh.evalSelfGravity(acc.data());
+    if (period > 0.) {
+        gCache.acc = acc;
+        gCache.n = n;
+        gCache.tLast = gCache.runTime;
+    }
+}
+
 void integrate(const sphgpu_config& cfg, ora_state& s) {
     const uint64_t n = s.n;
     const Flags fl = flagsOf(cfg, s);
@@ -1141,13 +1173,7 @@ void integrate(const sphgpu_config& cfg, ora_state& s) {
     // gravity into the acceleration buffer (GravitySolver::loop)
     std::vector<double> acc(4 * n, 0.);
     if (fl.gravity) {
-        BarnesHutTree bh;
-        bh.leafSize = cfg.gravity_leaf_size;
-        bh.thetaInv = 1. / cfg.gravity_opening_angle;
-        bh.order = cfg.gravity_multipole_order;
-        bh.kernelRadius = kernelRadiusOf(cfg);
-        bh.build(n, s.r, s.m, cfg.gravity_constant);
-        bh.evalSelfGravity(acc.data());
+        selfGravity(cfg, n, s.r, s.m, acc);
     }
     // pair loop
     const Neighbours nb = findNeighbours(n, s.r);
@@ -1674,6 +1700,7 @@ int ora_integrate(const sphgpu_config* cfg, ora_state* s) {
     if (!validConfig(cfg, s)) {
         return SPHGPU_ERR_ARGUMENT;
     }
+    gCache = GravityCache();
     integrate(*cfg, *s);
     return SPHGPU_OK;
 }
@@ -1682,6 +1709,7 @@ int ora_run(const sphgpu_config* cfg, ora_state* s, uint32_t nsteps, double* dt,
     if (!validConfig(cfg, s) || !dt) {
         return SPHGPU_ERR_ARGUMENT;
     }
+    gCache = GravityCache();
     for (uint32_t k = 0; k < nsteps; ++k) {
         if (dts) {
             dts[k] = *dt;
@@ -1691,6 +1719,7 @@ int ora_run(const sphgpu_config* cfg, ora_state* s, uint32_t nsteps, double* dt,
         } else {
             stepPC(*cfg, *s, *dt);
         }
+        gCache.runTime += *dt;
         *dt = criterionStep(*cfg, *s, *dt);
     }
     return SPHGPU_OK;
@@ -2199,67 +2228,103 @@ struct NbCollider {
     uint32_t n;
     double dt;
     std::vector<double> s;       // h + |v| dt
-    std::vector<int64_t> writer; // searchRadii writer
+    std::vector<std::atomic<int64_t>> writer; // searchRadii writer (the largest index)
     std::vector<double> srad;
     std::vector<uint32_t> bounces;
-    // grid of the positions at the start of the call, cell edge >= 2 max s, plus the particles moved since
+    // dense grid of the positions at the start of the call (cell edge 2 max(mean s, max s / 8), grown until it
+    // has at most max(4 n, 4096) cells), plus the particles moved since
     double cell = 1., lo[3] = { 0, 0, 0 };
-    std::unordered_map<uint64_t, std::vector<uint32_t>> cells;
+    int64_t dims[3] = { 1, 1, 1 };
+    std::vector<uint32_t> cellStart, order;
     std::vector<uint32_t> moved;
     std::vector<char> isMoved;
     // indices removed by the previous call: the reference clears its `removed` set only after the first
     // pass (NBodySolver.cpp:367-396), so the first-pass searches skip these indices of the new numbering
     const std::vector<uint32_t>* prevRemoved = nullptr;
-    uint64_t ambiguous = 0;
+    std::atomic<uint64_t> ambiguous{ 0 };
     uint64_t stats[4] = { 0, 0, 0, 0 };
 
     NbCollider(const sphgpu_config& c, NbParts& p, uint32_t count, double interval)
-        : cfg(c), P(p), n(count), dt(interval) {}
+        : cfg(c), P(p), n(count), dt(interval), writer(count) {}
 
-    void cellOf(const V4& r, int64_t out[3]) const {
-        out[0] = int64_t(std::floor((r.x - lo[0]) / cell));
-        out[1] = int64_t(std::floor((r.y - lo[1]) / cell));
-        out[2] = int64_t(std::floor((r.z - lo[2]) / cell));
+    int64_t coord(double x, int k) const {
+        const double c = std::floor((x - lo[k]) / cell);
+        if (!(c > 0.)) {
+            return 0;
+        }
+        return c >= double(dims[k] - 1) ? dims[k] - 1 : int64_t(c);
     }
-    static uint64_t key(int64_t x, int64_t y, int64_t z) {
-        return (uint64_t(x & 0x1fffff) << 42) | (uint64_t(y & 0x1fffff) << 21) | uint64_t(z & 0x1fffff);
+    uint64_t cellIndex(int64_t x, int64_t y, int64_t z) const {
+        return (uint64_t(z) * uint64_t(dims[1]) + uint64_t(y)) * uint64_t(dims[0]) + uint64_t(x);
     }
     void buildGrid() {
-        double smax = 0.;
+        double smax = 0., ssum = 0., hi[3] = { -INFINITY, -INFINITY, -INFINITY };
         lo[0] = lo[1] = lo[2] = INFINITY;
         for (uint32_t i = 0; i < n; ++i) {
             smax = std::max(smax, s[i]);
-            lo[0] = std::min(lo[0], P.r[i].x);
-            lo[1] = std::min(lo[1], P.r[i].y);
-            lo[2] = std::min(lo[2], P.r[i].z);
+            ssum += s[i];
+            const double x[3] = { P.r[i].x, P.r[i].y, P.r[i].z };
+            for (int k = 0; k < 3; ++k) {
+                lo[k] = std::min(lo[k], x[k]);
+                hi[k] = std::max(hi[k], x[k]);
+            }
         }
-        cell = smax > 0. ? 2. * smax * 1.0001 : 1.;
+        cell = 2. * std::max(ssum / double(n), 0.125 * smax) * 1.0001;
+        if (!(cell > 0.)) {
+            cell = 1.;
+        }
+        const double capacity = std::max(4. * double(n), 4096.);
+        for (;;) {
+            double total = 1.;
+            for (int k = 0; k < 3; ++k) {
+                dims[k] = int64_t(std::floor((hi[k] - lo[k]) / cell)) + 1;
+                total *= double(dims[k]);
+            }
+            if (total <= capacity) {
+                break;
+            }
+            cell *= 1.25;
+        }
+        const size_t ncell = size_t(dims[0] * dims[1] * dims[2]);
+        std::vector<uint64_t> key(n);
+        cellStart.assign(ncell + 1, 0);
         for (uint32_t i = 0; i < n; ++i) {
-            int64_t c[3];
-            cellOf(P.r[i], c);
-            cells[key(c[0], c[1], c[2])].push_back(i);
+            key[i] = cellIndex(coord(P.r[i].x, 0), coord(P.r[i].y, 1), coord(P.r[i].z, 2));
+            cellStart[key[i] + 1]++;
+        }
+        for (size_t c = 0; c < ncell; ++c) {
+            cellStart[c + 1] += cellStart[c];
+        }
+        order.resize(n);
+        std::vector<uint32_t> fill(cellStart.begin(), cellStart.end() - 1);
+        for (uint32_t i = 0; i < n; ++i) {
+            order[fill[key[i]]++] = i;
         }
     }
-    // every particle j != i with |r_j - r_i|^2 < radius^2, deduplicated, in index order
-    std::vector<uint32_t> within(uint32_t i, double radius) const {
-        std::vector<uint32_t> out;
+    // every particle j != i with |r_j - r_i|^2 < radius^2, deduplicated, in index order: the cells of the box
+    // [r_i - R', r_i + R'] (R' = radius widened by 1e-9 against rounding) and the moved particles
+    void within(uint32_t i, double radius, std::vector<uint32_t>& out) const {
+        out.clear();
         const V4 ri = P.r[i];
         const double radiusSqr = radius * radius;
-        int64_t c[3];
-        cellOf(ri, c);
+        int64_t c0[3], c1[3];
+        const double x[3] = { ri.x, ri.y, ri.z };
+        for (int k = 0; k < 3; ++k) {
+            const double w = radius * (1. + 1e-9) + 1e-9 * (std::fabs(x[k]) + std::fabs(lo[k]));
+            c0[k] = coord(x[k] - w, k);
+            c1[k] = coord(x[k] + w, k);
+        }
         auto consider = [&](uint32_t j) {
             if (j != i && sqrLen(sub(P.r[j], ri)) < radiusSqr) {
                 out.push_back(j);
             }
         };
-        for (int64_t z = c[2] - 1; z <= c[2] + 1; ++z) {
-            for (int64_t y = c[1] - 1; y <= c[1] + 1; ++y) {
-                for (int64_t x = c[0] - 1; x <= c[0] + 1; ++x) {
-                    auto it = cells.find(key(x, y, z));
-                    if (it != cells.end()) {
-                        for (uint32_t j : it->second) {
-                            consider(j);
-                        }
+        for (int64_t z = c0[2]; z <= c1[2]; ++z) {
+            for (int64_t y = c0[1]; y <= c1[1]; ++y) {
+                for (int64_t xx = c0[0]; xx <= c1[0]; ++xx) {
+                    const uint64_t c = cellIndex(xx, y, z);
+                    for (uint32_t q = cellStart[c]; q < cellStart[c + 1]; ++q) {
+                        consider(order[q]);
                     }
                 }
             }
@@ -2269,7 +2334,11 @@ struct NbCollider {
         }
         std::sort(out.begin(), out.end());
         out.erase(std::unique(out.begin(), out.end()), out.end());
-        return out;
+    }
+    void writeRadius(uint32_t j, int64_t i) {
+        int64_t cur = writer[j].load(std::memory_order_relaxed);
+        while (cur < i && !writer[j].compare_exchange_weak(cur, i, std::memory_order_relaxed)) {
+        }
     }
     bool rankLess(uint32_t j, uint32_t i) const {
         return s[j] < s[i] || (s[j] == s[i] && j < i);
@@ -2277,22 +2346,24 @@ struct NbCollider {
 
     // findClosestCollision (NBodySolver.cpp:509-563); first: FIND_LOWER_RANK over [0, dt], else USE_RADII
     NbCand find(uint32_t i, bool first, double lower, double size) {
-        std::vector<uint32_t> neighs;
+        thread_local std::vector<uint32_t> found, neighs;
+        neighs.clear();
         if (first) {
-            for (uint32_t j : within(i, 2. * s[i])) {
+            within(i, 2. * s[i], found);
+            for (uint32_t j : found) {
                 if (rankLess(j, i)) {
                     neighs.push_back(j);
                 }
             }
         } else if (srad[i] > 0.) {
-            neighs = within(i, 2. * srad[i]);
+            within(i, 2. * srad[i], neighs);
         }
         NbCand best;
         uint32_t overlapsHandled = 0;
         for (uint32_t j : neighs) {
             if (first) {
-                writer[j] = std::max<int64_t>(writer[j], i);
-                writer[i] = std::max<int64_t>(writer[i], i);
+                writeRadius(j, i);
+                writeRadius(i, i);
             }
             if (P.removed[j] || bounces[j] > cfg.max_bounces) {
                 continue;
@@ -2328,7 +2399,7 @@ struct NbCollider {
         // search radii there): with more than one overlap, or an overlap among several first-pass
         // neighbours, its result may differ from this one
         if (overlapsHandled > 1 || (first && overlapsHandled > 0 && neighs.size() > 1)) {
-            ++ambiguous;
+            ambiguous.fetch_add(1, std::memory_order_relaxed);
         }
         return best;
     }
@@ -2341,21 +2412,30 @@ struct NbCollider {
         for (uint32_t i = 0; i < n; ++i) {
             s[i] = P.r[i].h + std::sqrt(sqrLen(P.v[i])) * dt;
         }
-        writer.assign(n, -1);
+        for (uint32_t i = 0; i < n; ++i) {
+            writer[i].store(-1, std::memory_order_relaxed);
+        }
         bounces.assign(n, 0);
         isMoved.assign(n, 0);
         P.removed.assign(n, 0);
         buildGrid();
+        // the first pass is independent per particle (parallel like the reference's parallelFor)
+        std::vector<NbCand> first(n);
+        parallelFor(n, [&](uint64_t a, uint64_t b) {
+            for (uint64_t i = a; i < b; ++i) {
+                first[i] = find(uint32_t(i), true, 0., dt);
+            }
+        });
         NbCollisionSet set;
         for (uint32_t i = 0; i < n; ++i) {
-            const NbCand c = find(i, true, 0., dt);
-            if (c.t < INFINITY) {
-                set.insert(NbRec{ c.t, c.nov, i, c.j });
+            if (first[i].t < INFINITY) {
+                set.insert(NbRec{ first[i].t, first[i].nov, i, first[i].j });
             }
         }
         srad.assign(n, 0.);
         for (uint32_t i = 0; i < n; ++i) {
-            srad[i] = writer[i] >= 0 ? s[size_t(writer[i])] : 0.;
+            const int64_t w = writer[i].load(std::memory_order_relaxed);
+            srad[i] = w >= 0 ? s[size_t(w)] : 0.;
         }
         while (!set.records.empty()) {
             const NbRec col = *set.records.begin();
@@ -2491,7 +2571,7 @@ void nbCollide(const sphgpu_config& cfg, NbParts& P, uint32_t& n, double dt, uin
         stats[k] += c.stats[k];
     }
     if (ambiguous) {
-        *ambiguous += c.ambiguous;
+        *ambiguous += c.ambiguous.load();
     }
     if (cfg.collision_handler != SPHGPU_COLLISION_NONE && n > 0) {
         nbCompact(P, n);
@@ -2505,13 +2585,7 @@ void nbIntegrate(const sphgpu_config& cfg, NbParts& P, uint32_t n) {
         store4(r.data(), i, P.r[i]);
     }
     if ((cfg.forces & SPHGPU_FORCE_SELF_GRAVITY) && n > 0) {
-        BarnesHutTree bh;
-        bh.leafSize = cfg.gravity_leaf_size;
-        bh.thetaInv = 1. / cfg.gravity_opening_angle;
-        bh.order = cfg.gravity_multipole_order;
-        bh.kernelRadius = kernelRadiusOf(cfg);
-        bh.build(n, r.data(), P.m.data(), cfg.gravity_constant);
-        bh.evalSelfGravity(acc.data());
+        selfGravity(cfg, n, r.data(), P.m.data(), acc);
     }
     for (uint32_t i = 0; i < n; ++i) {
         const V4 a = load4(acc.data(), i);
@@ -2564,6 +2638,7 @@ int ora_nbody_integrate(const sphgpu_config* cfg, ora_nbody_state* st) {
         return SPHGPU_ERR_ARGUMENT;
     }
     NbParts P = nbLoad(*st);
+    gCache = GravityCache();
     nbIntegrate(*cfg, P, st->n);
     nbStore(P, st->n, *st);
     return SPHGPU_OK;
@@ -2581,6 +2656,7 @@ int ora_nbody_run(const sphgpu_config* cfg, ora_nbody_state* st, uint32_t nsteps
     uint32_t n = st->n;
     std::vector<uint32_t> prev;
     const double maxChange = cfg->max_change > 0. ? cfg->max_change : INFTY;
+    gCache = GravityCache();
     for (uint32_t k = 0; k < nsteps; ++k) {
         const double h = *dt;
         if (dts) {
@@ -2597,6 +2673,7 @@ int ora_nbody_run(const sphgpu_config* cfg, ora_nbody_state* st, uint32_t nsteps
         }
         nbCollide(*cfg, P, n, 0.5 * h, stats, ambiguous, prev);
         nbDrift(P, n, h);
+        gCache.runTime += h;
         if (cfg->timestep_criteria & SPHGPU_CRITERION_ACCELERATION) {
             double minStep = INFTY;
             for (uint32_t i = 0; i < n; ++i) {

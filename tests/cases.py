@@ -25,10 +25,16 @@ def kind(fx):
     """Physics of the fixture (sphere, impact, gas, ...), without the "_all" suffix of the runs with every
     time-step criterion."""
     k = str(fx["driver_args"]).split()[0]
-    for suffix in ("_all", "_asym"):
+    for suffix in ("_cached", "_all", "_asym"):
         if k.endswith(suffix):
             k = k[:-len(suffix)]
     return k
+
+
+def recomputation_period(fx):
+    """gravity.recomputation_period of a run with CachedGravity (mode "<kind>_cached", last argument)."""
+    args = str(fx["driver_args"]).split()
+    return float(args[-1]) if args[0].endswith("_cached") else 0.0
 
 
 def all_criteria(fx):
@@ -71,7 +77,8 @@ def config_of(fx, precision=abi.PRECISION_FP64):
     crit = abi.CRITERION_ALL if all_criteria(fx) else abi.CRITERION_COURANT
     if k == "sphere":
         return abi.make_config(n, mats, forces=abi.FORCE_PRESSURE | abi.FORCE_SELF_GRAVITY,
-                               gravity_constant=float(fx["G"][0]), precision=precision, timestep_criteria=crit)
+                               gravity_constant=float(fx["G"][0]), precision=precision, timestep_criteria=crit,
+                               gravity_recomputation_period=recomputation_period(fx))
     if k == "impact":
         extra = {}
         if asymmetric(fx):

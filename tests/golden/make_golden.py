@@ -33,6 +33,8 @@ FIXTURES = {
     # solid impact with the AsymmetricSolver and the strain-rate correction tensor (the settings of the
     # reference's impact regression, regression/impact/impact.sph)
     "impact_asym_n1200": ["impact_asym", "1200", "5e4", "80", "5e3", "4", "5e3", "45"],
+    # the basalt sphere with CachedGravity (gravity.recomputation_period 0.35 s: recomputed at t = 0 and 0.47)
+    "sphere_cached_n1000": ["sphere_cached", "1000", "1e4", "6", "1", "0.35"],
     # gravity only: Plummer sphere, BH theta 0.5 octupole vs brute force
     "gravity_n3000": ["gravity", "3000", "0.5", "7", "1e-3"],
     "gravity_n3000_t07": ["gravity", "3000", "0.7", "11", "1e-2"],

@@ -73,6 +73,9 @@ def test_create_rejects_invalid_settings_without_device():
     # unknown integrator
     cfg, keep = abi.make_config(10, [abi.basalt()], integrator=7)
     assert lib.sphgpu_create(ctypes.byref(cfg), ctypes.byref(h)) == abi.ERR_UNSUPPORTED
+    # negative gravity recomputation period
+    cfg, keep = abi.make_config(10, [abi.basalt()], gravity_recomputation_period=-1.0)
+    assert lib.sphgpu_create(ctypes.byref(cfg), ctypes.byref(h)) == abi.ERR_ARGUMENT
     assert not h.value
 
 

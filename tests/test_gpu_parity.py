@@ -159,7 +159,7 @@ def test_integrate_matches_reference(name):
 
 
 @pytest.mark.parametrize("name", ["sphere_n1000", "impact_n1200", "gas_n1500", "impact_all_n1200",
-                                  "gas_all_n1500", "impact_asym_n1200"])
+                                  "gas_all_n1500", "impact_asym_n1200", "sphere_cached_n1000"])
 def test_steps_match_reference(name):
     fx = cases.load(name)
     cfg, keep = cases.config_of(fx)

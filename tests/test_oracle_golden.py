@@ -117,7 +117,7 @@ def test_integrate_matches_reference(name):
 
 
 @pytest.mark.parametrize("name", ["sphere_n1000", "impact_n1200", "gas_n1500", "impact_all_n1200",
-                                  "gas_all_n1500", "impact_asym_n1200"])
+                                  "gas_all_n1500", "impact_asym_n1200", "sphere_cached_n1000"])
 def test_steps_match_reference(name):
     fx = cases.load(name)
     cfg, keep = cases.config_of(fx)
@@ -129,3 +129,13 @@ def test_steps_match_reference(name):
     for f in ["r", "v", "dv", "rho", "drho", "u", "du", "divv", "S", "dS", "D", "dD"]:
         if "sN_" + f in fx:
             assert cases.scale_err(st[f], fx["sN_" + f]) < TOL_STEPS, f
+
+
+def test_cached_gravity_differs_from_recomputed_gravity():
+    # the cached run is not the plain run: the reference reused accelerations between recomputations
+    fx = cases.load("sphere_cached_n1000")
+    cfg, keep = cases.config_of(fx)
+    cfg.gravity_recomputation_period = 0.0
+    st = cases.state_of(fx, "s0_")
+    oracle.run(cfg, st, len(fx["dts"]) - 1, float(fx["dts"][0]))
+    assert cases.scale_err(st["v"], fx["sN_v"]) > 100 * TOL_STEPS

@@ -265,6 +265,11 @@ sphgpu_status sphgpu_set_time(sphgpu_handle* h, double t);
 sphgpu_status sphgpu_collide(sphgpu_handle* h, double dt);
 /* Current particle count (changes when collisions merge particles). */
 sphgpu_status sphgpu_particle_count(sphgpu_handle* h, uint64_t* n);
+/* The indices, ascending and in the numbering of the last call of this function (or of the last position
+ * upload), of the particles removed by merging since then; the numbering restarts from the current state. The
+ * argument of the reference's Storage::remove (core/quantities/Storage.h) for a host copy of the state. If
+ * more than `capacity` were removed, *count says how many and SPHGPU_ERR_CAPACITY is returned (call again). */
+sphgpu_status sphgpu_take_removed(sphgpu_handle* h, uint32_t* removed, uint64_t capacity, uint64_t* count);
 /* StatisticsId::TOTAL_COLLISION_COUNT, MERGER_COUNT, BOUNCE_COUNT, OVERLAP_COUNT (core/gravity/NBodySolver.cpp:
  * 119-163), summed over all collide calls since the handle was created. */
 sphgpu_status sphgpu_collision_stats(sphgpu_handle* h, uint64_t out[4]);

@@ -27,6 +27,18 @@ namespace {
     throw Exception(String::fromAscii(msg.c_str()));
 }
 
+// GravityKernelEnum (core/system/Settings.h:804-814) -> SPHGPU_GRAVITY_KERNEL_*
+int gravityKernel(const RunSettings& settings) {
+    switch (settings.get<GravityKernelEnum>(RunSettingsId::GRAVITY_KERNEL)) {
+    case GravityKernelEnum::POINT_PARTICLES:
+        return SPHGPU_GRAVITY_KERNEL_POINT_PARTICLES;
+    case GravityKernelEnum::SOLID_SPHERES:
+        return SPHGPU_GRAVITY_KERNEL_SOLID_SPHERES;
+    default:
+        return SPHGPU_GRAVITY_KERNEL_SPH_KERNEL;
+    }
+}
+
 sphgpu_material toMaterial(const IMaterial& m) {
     sphgpu_material out{};
     const EosEnum eos = m.getParam<EosEnum>(BodySettingsId::EOS);
@@ -119,10 +131,8 @@ DeviceState::DeviceState(const RunSettings& settings, const Storage& storage, in
     config.av_beta = settings.get<Float>(RunSettingsId::SPH_AV_BETA);
     config.sum_only_undamaged = settings.get<bool>(RunSettingsId::SPH_SUM_ONLY_UNDAMAGED);
     config.gravity_multipole_order = settings.get<int>(RunSettingsId::GRAVITY_MULTIPOLE_ORDER);
-    config.gravity_kernel = settings.get<GravityKernelEnum>(RunSettingsId::GRAVITY_KERNEL) ==
-                                    GravityKernelEnum::POINT_PARTICLES
-                                ? SPHGPU_GRAVITY_KERNEL_POINT_PARTICLES
-                                : SPHGPU_GRAVITY_KERNEL_SPH_KERNEL;
+    config.gravity_kernel = gravityKernel(settings);
+    config.gravity_recomputation_period = settings.get<Float>(RunSettingsId::GRAVITY_RECOMPUTATION_PERIOD);
     config.gravity_constant = settings.get<Float>(RunSettingsId::GRAVITY_CONSTANT);
     config.gravity_opening_angle = settings.get<Float>(RunSettingsId::GRAVITY_OPENING_ANGLE);
     config.gravity_leaf_size = settings.get<int>(RunSettingsId::FINDER_LEAF_SIZE);
@@ -541,6 +551,163 @@ Size GpuFinder::find(const Vector& pos, const Size index, const Float radius, Ar
 
 template Size GpuFinder::find<true>(const Vector&, const Size, const Float, Array<NeighborRecord>&) const;
 template Size GpuFinder::find<false>(const Vector&, const Size, const Float, Array<NeighborRecord>&) const;
+
+} // namespace Gpu
+
+NAMESPACE_SPH_END
+
+NAMESPACE_SPH_BEGIN
+
+namespace Gpu {
+
+GpuHardSphereSolver::GpuHardSphereSolver(IScheduler& UNUSED(scheduler), const RunSettings& settings, int precision)
+    : settings(settings)
+    , precision(precision) {
+    if (settings.get<bool>(RunSettingsId::NBODY_INERTIA_TENSOR)) {
+        raise(true, "GPU N-body solver: the inertia tensor of particles is not implemented");
+    }
+}
+
+GpuHardSphereSolver::~GpuHardSphereSolver() {
+    sphgpu_destroy(handle);
+}
+
+void GpuHardSphereSolver::check(int status) const {
+    if (status == SPHGPU_OK) {
+        return;
+    }
+    const std::string msg = std::string("sphgpu: ") + sphgpu_last_error(handle);
+    raise(status == SPHGPU_ERR_ARGUMENT || status == SPHGPU_ERR_UNSUPPORTED, msg);
+}
+
+void GpuHardSphereSolver::ensure(const Storage& storage) {
+    if (handle && count == storage.getParticleCnt()) {
+        return;
+    }
+    sphgpu_destroy(handle);
+    handle = nullptr;
+    sphgpu_config config{};
+    config.particle_count = storage.getParticleCnt();
+    config.solver_type = SPHGPU_SOLVER_NBODY_HARD_SPHERE;
+    config.integrator = SPHGPU_INTEGRATOR_LEAP_FROG;
+    config.forces = SPHGPU_FORCE_SELF_GRAVITY;
+    config.gravity_kernel = gravityKernel(settings);
+    config.gravity_multipole_order = settings.get<int>(RunSettingsId::GRAVITY_MULTIPOLE_ORDER);
+    config.gravity_constant = settings.get<Float>(RunSettingsId::GRAVITY_CONSTANT);
+    config.gravity_opening_angle = settings.get<Float>(RunSettingsId::GRAVITY_OPENING_ANGLE);
+    config.gravity_leaf_size = settings.get<int>(RunSettingsId::FINDER_LEAF_SIZE);
+    config.gravity_recomputation_period = settings.get<Float>(RunSettingsId::GRAVITY_RECOMPUTATION_PERIOD);
+    config.max_timestep = settings.get<Float>(RunSettingsId::TIMESTEPPING_MAX_TIMESTEP);
+    config.initial_timestep = settings.get<Float>(RunSettingsId::TIMESTEPPING_INITIAL_TIMESTEP);
+    config.derivative_factor = settings.get<Float>(RunSettingsId::TIMESTEPPING_DERIVATIVE_FACTOR);
+    config.max_change = settings.get<Float>(RunSettingsId::TIMESTEPPING_MAX_INCREASE);
+    // Factory::getCollisionHandler / getOverlapHandler (core/system/Factory.cpp:415-450)
+    switch (settings.get<CollisionHandlerEnum>(RunSettingsId::COLLISION_HANDLER)) {
+    case CollisionHandlerEnum::NONE:
+        config.collision_handler = SPHGPU_COLLISION_NONE;
+        break;
+    case CollisionHandlerEnum::PERFECT_MERGING:
+        config.collision_handler = SPHGPU_COLLISION_PERFECT_MERGING;
+        break;
+    case CollisionHandlerEnum::ELASTIC_BOUNCE:
+        config.collision_handler = SPHGPU_COLLISION_ELASTIC_BOUNCE;
+        break;
+    default:
+        config.collision_handler = SPHGPU_COLLISION_MERGE_OR_BOUNCE;
+        break;
+    }
+    config.overlap_handler = int32_t(settings.get<OverlapEnum>(RunSettingsId::COLLISION_OVERLAP));
+    config.restitution_normal = settings.get<Float>(RunSettingsId::COLLISION_RESTITUTION_NORMAL);
+    config.restitution_tangent = settings.get<Float>(RunSettingsId::COLLISION_RESTITUTION_TANGENT);
+    config.allowed_overlap = settings.get<Float>(RunSettingsId::COLLISION_ALLOWED_OVERLAP);
+    config.bounce_merge_limit = settings.get<Float>(RunSettingsId::COLLISION_BOUNCE_MERGE_LIMIT);
+    config.rotation_merge_limit = settings.get<Float>(RunSettingsId::COLLISION_ROTATION_MERGE_LIMIT);
+    config.max_bounces = uint32_t(settings.get<int>(RunSettingsId::COLLISION_MAX_BOUNCES));
+    config.precision = precision;
+    const int rc = sphgpu_create(&config, &handle);
+    if (rc != SPHGPU_OK) {
+        raise(rc == SPHGPU_ERR_ARGUMENT || rc == SPHGPU_ERR_UNSUPPORTED,
+            std::string("sphgpu: ") + sphgpu_last_error(nullptr));
+    }
+    count = config.particle_count;
+}
+
+void GpuHardSphereSolver::upload(const Storage& storage) {
+    const Size n = storage.getParticleCnt();
+    ArrayView<const Vector> r, v, dv;
+    tie(r, v, dv) = storage.getAll<Vector>(QuantityId::POSITION);
+    check(sphgpu_set_quantity(handle, SPHGPU_Q_POSITION, 0, &r[0][0], n));
+    check(sphgpu_set_quantity(handle, SPHGPU_Q_POSITION, 1, &v[0][0], n));
+    check(sphgpu_set_quantity(handle, SPHGPU_Q_MASS, 0, &storage.getValue<Float>(QuantityId::MASS)[0], n));
+    check(sphgpu_set_quantity(
+        handle, SPHGPU_Q_ANGULAR_FREQUENCY, 0, &storage.getValue<Vector>(QuantityId::ANGULAR_FREQUENCY)[0][0], n));
+}
+
+void GpuHardSphereSolver::download(Storage& storage, bool positions) {
+    const Size n = storage.getParticleCnt();
+    ArrayView<Vector> r, v, dv;
+    tie(r, v, dv) = storage.getAll<Vector>(QuantityId::POSITION);
+    check(sphgpu_get_quantity(handle, SPHGPU_Q_POSITION, 1, &v[0][0], n));
+    check(sphgpu_get_quantity(handle, SPHGPU_Q_POSITION, 2, &dv[0][0], n));
+    if (positions) {
+        check(sphgpu_get_quantity(handle, SPHGPU_Q_POSITION, 0, &r[0][0], n));
+        check(sphgpu_get_quantity(handle, SPHGPU_Q_MASS, 0, &storage.getValue<Float>(QuantityId::MASS)[0], n));
+        check(sphgpu_get_quantity(
+            handle, SPHGPU_Q_ANGULAR_FREQUENCY, 0, &storage.getValue<Vector>(QuantityId::ANGULAR_FREQUENCY)[0][0], n));
+    }
+}
+
+void GpuHardSphereSolver::integrate(Storage& storage, Statistics& stats) {
+    if (storage.getParticleCnt() == 0) {
+        return;
+    }
+    ensure(storage);
+    upload(storage);
+    check(sphgpu_integrate(handle));
+    download(storage, false);
+    double times[SPHGPU_PHASE_COUNT];
+    if (sphgpu_phase_times(handle, times, nullptr) == SPHGPU_OK) {
+        stats.set(StatisticsId::GRAVITY_EVAL_TIME, int(times[SPHGPU_PHASE_GRAVITY_BUILD] + times[SPHGPU_PHASE_GRAVITY_EVAL]));
+    }
+}
+
+void GpuHardSphereSolver::collide(Storage& storage, Statistics& stats, const Float dt) {
+    if (settings.get<CollisionHandlerEnum>(RunSettingsId::COLLISION_HANDLER) == CollisionHandlerEnum::NONE ||
+        storage.getParticleCnt() == 0) {
+        return; // HardSphereSolver::collide ignores all collisions without a handler
+    }
+    ensure(storage);
+    upload(storage);
+    check(sphgpu_collide(handle, dt));
+    // the particles merged away, as the argument of Storage::remove (NBodySolver.cpp:478-481)
+    uint64_t removedCount = 0;
+    std::vector<uint32_t> removed(storage.getParticleCnt());
+    check(sphgpu_take_removed(handle, removed.data(), removed.size(), &removedCount));
+    if (removedCount > 0) {
+        Array<Size> idxs(removedCount);
+        for (uint64_t k = 0; k < removedCount; ++k) {
+            idxs[k] = removed[k];
+        }
+        storage.remove(idxs, Storage::IndicesFlag::INDICES_SORTED | Storage::IndicesFlag::PROPAGATE);
+        count = storage.getParticleCnt();
+    }
+    download(storage, true);
+    // CollisionStats (NBodySolver.cpp:119-163): the counts of this call
+    uint64_t totals[4];
+    check(sphgpu_collision_stats(handle, totals));
+    stats.set(StatisticsId::TOTAL_COLLISION_COUNT, int(totals[0] - collisionTotals[0]));
+    stats.set(StatisticsId::MERGER_COUNT, int(totals[1] - collisionTotals[1]));
+    stats.set(StatisticsId::BOUNCE_COUNT, int(totals[2] - collisionTotals[2]));
+    stats.set(StatisticsId::OVERLAP_COUNT, int(totals[3] - collisionTotals[3]));
+    for (int k = 0; k < 4; ++k) {
+        collisionTotals[k] = totals[k];
+    }
+}
+
+void GpuHardSphereSolver::create(Storage& storage, IMaterial& UNUSED(material)) const {
+    // HardSphereSolver::create without the inertia tensor (core/gravity/NBodySolver.cpp:487-507)
+    storage.insert<Vector>(QuantityId::ANGULAR_FREQUENCY, OrderEnum::ZERO, Vector(0._f));
+}
 
 } // namespace Gpu
 

@@ -10,6 +10,7 @@
 ///   - GpuFinder        : ISymmetricFinder (replaces KdTree, Factory::getFinder)
 ///   - GpuOutput        : IOutput decorator bringing the host Storage up to date before each dump, so that
 ///                        the reference's BinaryOutput (.ssf) writes the device state without per-step syncs
+///   - GpuHardSphereSolver : ISolver   (replaces HardSphereSolver, the N-body solver with collisions)
 /// Errors reported by the library are rethrown as the reference's InvalidSetup (configuration) or
 /// Exception (runtime) types.
 
@@ -72,6 +73,31 @@ public:
 
     /// Device state shared with GpuTimeStepping (created on first use).
     DeviceState& getDevice(const Storage& storage) const;
+};
+
+/// ISolver drop-in for HardSphereSolver (core/gravity/NBodySolver.h:24-140): Barnes-Hut self-gravity
+/// (integrate) and the time-ordered collision loop with the configured handlers (collide) run on the GPU. The
+/// host Storage is uploaded before and read back after each call; particles merged on the device are removed
+/// from it with Storage::remove, as the reference solver does. Driven by the reference's own LeapFrog.
+class GpuHardSphereSolver : public ISolver {
+    RunSettings settings;
+    int precision;
+    sphgpu_handle* handle = nullptr;
+    Size count = 0;
+    uint64_t collisionTotals[4] = { 0, 0, 0, 0 };
+
+    void ensure(const Storage& storage);
+    void check(int status) const;
+    void upload(const Storage& storage);
+    void download(Storage& storage, bool positions);
+
+public:
+    GpuHardSphereSolver(IScheduler& scheduler, const RunSettings& settings, int precision = SPHGPU_PRECISION_FP64);
+    ~GpuHardSphereSolver() override;
+
+    virtual void integrate(Storage& storage, Statistics& stats) override;
+    virtual void collide(Storage& storage, Statistics& stats, const Float dt) override;
+    virtual void create(Storage& storage, IMaterial& material) const override;
 };
 
 /// When GpuTimeStepping copies the device state into the host Storage.

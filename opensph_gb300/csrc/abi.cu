@@ -61,6 +61,7 @@ struct sphgpu_handle {
     Collide coll;
     CollideParams cp;
     double* d_dtc = nullptr;
+    uint32_t n_sync = 0; // particle count at the last sphgpu_take_removed / position upload
 };
 
 namespace {
@@ -734,6 +735,8 @@ sphgpu_status sphgpu_create(const sphgpu_config* config, sphgpu_handle** out) {
         A(&h->coll.tmp_dv, nn);
         A(&h->coll.tmp_w, nn);
         A(&h->coll.tmp_m, nn);
+        A(&s.origin, nn);
+        A(&h->coll.tmp_origin, nn);
         A(&h->d_dtc, 1);
     } else {
         A(&s.pdv, nn);
@@ -841,6 +844,11 @@ sphgpu_status sphgpu_create(const sphgpu_config* config, sphgpu_handle** out) {
         // HardSphereSolver::create inserts ANGULAR_FREQUENCY = 0 (core/gravity/NBodySolver.cpp:487-490)
         e = cudaMemset(s.omega, 0, nn * sizeof(dbl4));
     }
+    if (e == cudaSuccess && s.origin) {
+        launchIota(s.origin, n, nullptr);
+        e = cudaGetLastError();
+        h->n_sync = n;
+    }
     if (e == cudaSuccess) {
         // reference defaults: every particle has STRESS_REDUCING = 1 (VonMisesRheology::create)
         if (s.reduce) {
@@ -944,6 +952,12 @@ sphgpu_status sphgpu_set_quantity(sphgpu_handle* h, int32_t id, int32_t order, c
         CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     }
     h->gravity_current = false;
+    if (h->s.origin && id == SPHGPU_Q_POSITION && order == 0) {
+        // a new state: removals are reported relative to it
+        launchIota(h->s.origin, h->s.n, h->stream);
+        CUDA_TRY(h, cudaGetLastError());
+        h->n_sync = h->s.n;
+    }
     return SPHGPU_OK;
 }
 
@@ -1452,6 +1466,46 @@ sphgpu_status sphgpu_set_time(sphgpu_handle* h, double t) {
     }
     CUDA_TRY(h, cudaMemcpyAsync(h->d_time, &t, sizeof(double), cudaMemcpyHostToDevice, h->stream));
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return SPHGPU_OK;
+}
+
+sphgpu_status sphgpu_take_removed(sphgpu_handle* h, uint32_t* removed, uint64_t capacity, uint64_t* count) {
+    if (!h || !count || (capacity && !removed)) {
+        return h ? fail(h, SPHGPU_ERR_ARGUMENT, "take_removed: NULL count or buffer") : SPHGPU_ERR_ARGUMENT;
+    }
+    if (!h->s.origin) {
+        return fail(h, SPHGPU_ERR_UNSUPPORTED, "take_removed needs the N-body solver");
+    }
+    const uint32_t n = h->s.n;
+    std::vector<uint32_t> origin(n);
+    if (n) {
+        CUDA_TRY(h, cudaMemcpyAsync(origin.data(), h->s.origin, n * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+            h->stream));
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    }
+    std::vector<char> kept(h->n_sync, 0);
+    for (uint32_t k : origin) {
+        if (k < h->n_sync) {
+            kept[k] = 1;
+        }
+    }
+    uint64_t cnt = 0;
+    for (uint32_t i = 0; i < h->n_sync; ++i) {
+        if (!kept[i]) {
+            if (cnt < capacity) {
+                removed[cnt] = i;
+            }
+            ++cnt;
+        }
+    }
+    *count = cnt;
+    if (cnt > capacity) {
+        return fail(h, SPHGPU_ERR_CAPACITY, "take_removed: %llu indices, room for %llu", (unsigned long long)cnt,
+            (unsigned long long)capacity);
+    }
+    launchIota(h->s.origin, n, h->stream);
+    CUDA_TRY(h, cudaGetLastError());
+    h->n_sync = n;
     return SPHGPU_OK;
 }
 

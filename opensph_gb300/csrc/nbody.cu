@@ -1000,6 +1000,14 @@ __global__ void compactKernel(DState s, Collide c, const uint32_t* __restrict__ 
     c.tmp_dv[d] = s.dv[i];
     c.tmp_w[d] = s.omega[i];
     c.tmp_m[d] = s.m[i];
+    c.tmp_origin[d] = s.origin[i];
+}
+
+__global__ void iotaKernel(uint32_t* a, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        a[i] = i;
+    }
 }
 
 // ---- integrator pieces (LeapFrog::stepParticles, core/timestepping/TimeStepping.cpp:352-391) ---------------------
@@ -1258,10 +1266,17 @@ int nbodyCollide(DState& s, Grid& g, Collide& c, const CollideParams& p, const d
         std::swap(s.dv, c.tmp_dv);
         std::swap(s.omega, c.tmp_w);
         std::swap(s.m, c.tmp_m);
+        std::swap(s.origin, c.tmp_origin);
         s.n = n - removed;
     }
     std::swap(c.removed, c.prev_removed);
     return SPHGPU_OK;
+}
+
+void launchIota(uint32_t* a, uint32_t n, cudaStream_t st) {
+    if (n) {
+        iotaKernel<<<ceilDiv(n, 256), 256, 0, st>>>(a, n);
+    }
 }
 
 void launchNbodyDrift(const DState& s, const Physics& ph, const double* dt, double* dtMin, bool criterion,

@@ -52,6 +52,8 @@ struct DState {
     double* corr;
     // N-body solver: angular frequency {x, y, z, 0} (QuantityId::ANGULAR_FREQUENCY)
     dbl4* omega;
+    // N-body solver: index of each particle at the last sphgpu_take_removed / position upload
+    uint32_t* origin;
 };
 
 // Physics switches and constants of one handle
@@ -130,6 +132,7 @@ struct Collide {
     dbl4* tmp_dv = nullptr;
     dbl4* tmp_w = nullptr;
     double* tmp_m = nullptr;
+    uint32_t* tmp_origin = nullptr;
     uint32_t launches = 0;
     unsigned long long totals[4] = { 0, 0, 0, 0 }; // collisions, mergers, bounces, overlaps (host copy)
     // records processed by the event loop and its SM cycles in the serial part, the re-searches, the insertions
@@ -320,6 +323,8 @@ void collideFree(Collide& c);
 // Synchronises the stream. Returns SPHGPU_OK or an error status (capacity bits in *capacity_error).
 int nbodyCollide(DState& s, Grid& g, Collide& c, const CollideParams& p, const double* dt, double factor,
     uint32_t* capacity_error, cudaStream_t st);
+// a[i] = i for i < n
+void launchIota(uint32_t* a, uint32_t n, cudaStream_t st);
 // leap-frog drift r += v dt / 2; with criteria, the acceleration time-step minimum into dt_min
 void launchNbodyDrift(const DState& s, const Physics& ph, const double* dt, double* dt_min, bool criterion,
     cudaStream_t st);

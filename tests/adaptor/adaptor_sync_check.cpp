@@ -5,7 +5,9 @@
 /// step and counts position uploads and downloads). Checks, for GpuTimeStepping in ON_DEMAND mode: one upload
 /// before the first step and no download between steps; GpuOutput downloads once before writing the .ssf;
 /// the file read back by BinaryInput holds the device state; invalidate() (a resumed run) uploads again; and
-/// EVERY_STEP mode downloads after every step. Prints "ok" and exits 0 on success.
+/// EVERY_STEP mode downloads after every step. It also checks that GpuHardSphereSolver::collide removes the
+/// particles merged on the device from the host Storage, in the numbering of each call. Prints "ok" and exits 0
+/// on success.
 
 #include "GpuSph.h"
 #include "Sph.h"
@@ -112,6 +114,35 @@ int main(int argc, char** argv) {
     counts(up2, down2, steps2);
     expect(down2 - down == 2 && up2 - up == 2, "EVERY_STEP uploads and downloads once per step");
     expect(every.syncCount() == 2, "EVERY_STEP sync count");
+
+    // N-body: GpuHardSphereSolver removes the particles merged on the device from the host Storage (the
+    // stand-in merges every odd particle into its even neighbour)
+    {
+        RunSettings nb;
+        nb.set(RunSettingsId::RUN_THREAD_CNT, 1);
+        nb.set(RunSettingsId::COLLISION_HANDLER, CollisionHandlerEnum::PERFECT_MERGING);
+        SharedPtr<Storage> s = makeShared<Storage>(makeAuto<NullMaterial>(BodySettings::getDefaults()));
+        Array<Vector> r;
+        Array<Float> m;
+        for (Size i = 0; i < 7; ++i) {
+            r.push(Vector(Float(i), 0._f, 0._f, 0.1_f));
+            m.push(1._f + Float(i));
+        }
+        s->insert<Vector>(QuantityId::POSITION, OrderEnum::SECOND, std::move(r));
+        s->insert<Float>(QuantityId::MASS, OrderEnum::ZERO, std::move(m));
+        Gpu::GpuHardSphereSolver hs(*scheduler, nb);
+        hs.create(*s, s->getMaterial(0));
+        Statistics nstats;
+        hs.collide(*s, nstats, 1._f);
+        expect(s->getParticleCnt() == 4, "N-body: three merged particles removed from the Storage");
+        ArrayView<const Vector> rr = s->getValue<Vector>(QuantityId::POSITION);
+        ArrayView<const Float> mm = s->getValue<Float>(QuantityId::MASS);
+        expect(rr[1][X] == 2._f && rr[3][X] == 6._f, "N-body: the order of the kept particles is unchanged");
+        expect(mm[0] == 3._f && mm[3] == 7._f, "N-body: the merged masses are read back");
+        expect(nstats.get<int>(StatisticsId::MERGER_COUNT) == 3, "N-body: merger count of the call");
+        hs.collide(*s, nstats, 1._f);
+        expect(s->getParticleCnt() == 2, "N-body: the second call removes relative to the new numbering");
+    }
 
     if (fails == 0) {
         std::printf("ok\n");

@@ -4,6 +4,7 @@
 // drift r += v dt (no physics); it counts the uploads and downloads of positions so that a test can check when
 // the adaptor moves data. It is compiled only by tests/test_adaptor_cpu.py and never linked into the library.
 
+#include <algorithm>
 #include <cstring>
 #include <map>
 #include <string>
@@ -16,6 +17,10 @@ struct sphgpu_handle {
     uint32_t n = 0;
     std::map<std::pair<int, int>, std::vector<unsigned char>> q;
     double dt = 0.;
+    // N-body stand-in: index of each particle at the last take_removed, removed indices, merges so far
+    std::vector<uint32_t> origin;
+    std::vector<uint32_t> removed;
+    uint64_t merges = 0;
 };
 
 namespace {
@@ -27,6 +32,7 @@ int gSteps = 0;
 size_t bytesOf(int id, uint64_t n) {
     switch (id) {
     case SPHGPU_Q_POSITION:
+    case SPHGPU_Q_ANGULAR_FREQUENCY:
         return 32 * n;
     case SPHGPU_Q_DEVIATORIC_STRESS:
         return 40 * n;
@@ -59,6 +65,9 @@ sphgpu_status sphgpu_create(const sphgpu_config* config, sphgpu_handle** out) {
     }
     *out = new sphgpu_handle();
     (*out)->n = config->particle_count;
+    for (uint32_t i = 0; i < config->particle_count; ++i) {
+        (*out)->origin.push_back(i);
+    }
     (*out)->dt = config->initial_timestep;
     return SPHGPU_OK;
 }
@@ -166,6 +175,70 @@ sphgpu_status sphgpu_gravity_stats(sphgpu_handle*, uint64_t*) {
 
 sphgpu_status sphgpu_gravity_eval_points(sphgpu_handle*, const double*, uint64_t, double*) {
     return SPHGPU_ERR_UNSUPPORTED;
+}
+
+} // extern "C"
+
+extern "C" {
+
+// N-body stand-in: a "collision" merges every odd-indexed particle into its even neighbour (mass added, the
+// odd one removed, the order of the others kept), so that a test can check how the adaptor shrinks the Storage
+sphgpu_status sphgpu_collide(sphgpu_handle* h, double) {
+    if (!h) {
+        return SPHGPU_ERR_ARGUMENT;
+    }
+    const uint32_t n = h->n;
+    auto compact = [&](int id, int order, size_t bytes) {
+        auto it = h->q.find({ id, order });
+        if (it == h->q.end()) {
+            return;
+        }
+        std::vector<unsigned char> out;
+        for (uint32_t i = 0; i < n; i += 2) {
+            out.insert(out.end(), it->second.begin() + i * bytes, it->second.begin() + (i + 1) * bytes);
+        }
+        it->second = out;
+    };
+    auto& m = h->q[{ SPHGPU_Q_MASS, 0 }];
+    double* mp = reinterpret_cast<double*>(m.data());
+    for (uint32_t i = 0; i + 1 < n; i += 2) {
+        mp[i] += mp[i + 1];
+        h->removed.push_back(h->origin[i + 1]);
+        h->merges++;
+    }
+    std::vector<uint32_t> origin;
+    for (uint32_t i = 0; i < n; i += 2) {
+        origin.push_back(h->origin[i]);
+    }
+    h->origin = origin;
+    for (int order = 0; order < 3; ++order) {
+        compact(SPHGPU_Q_POSITION, order, 32);
+    }
+    compact(SPHGPU_Q_MASS, 0, 8);
+    compact(SPHGPU_Q_ANGULAR_FREQUENCY, 0, 32);
+    h->n = (n + 1) / 2;
+    return SPHGPU_OK;
+}
+
+sphgpu_status sphgpu_take_removed(sphgpu_handle* h, uint32_t* removed, uint64_t capacity, uint64_t* count) {
+    *count = h->removed.size();
+    if (h->removed.size() > capacity) {
+        return SPHGPU_ERR_CAPACITY;
+    }
+    std::sort(h->removed.begin(), h->removed.end());
+    std::copy(h->removed.begin(), h->removed.end(), removed);
+    h->removed.clear();
+    h->origin.resize(h->n);
+    for (uint32_t i = 0; i < h->n; ++i) {
+        h->origin[i] = i;
+    }
+    return SPHGPU_OK;
+}
+
+sphgpu_status sphgpu_collision_stats(sphgpu_handle* h, uint64_t out[4]) {
+    out[0] = out[1] = h->merges;
+    out[2] = out[3] = 0;
+    return SPHGPU_OK;
 }
 
 } // extern "C"

@@ -436,6 +436,8 @@ __global__ void gatherKernel(DState s, Grid g, Collide c) {
     c.posf[k] = make_float4(float(r.x - (gi.lo[0] + double(cx) * gi.cell)), float(r.y - (gi.lo[1] + double(cy) * gi.cell)),
         float(r.z - (gi.lo[2] + double(cz) * gi.cell)), float(2. * si));
     c.sbits[k] = static_cast<unsigned long long>(__double_as_longlong(si));
+    const dbl4 v = s.v[i];
+    c.velf[k] = make_float4(float(v.x), float(v.y), float(v.z), float(r.w));
     c.moved_cell[i] = int32_t(key);
 }
 
@@ -461,6 +463,9 @@ __global__ void __launch_bounds__(128) detectKernel(DState s, Grid g, Collide c,
     const double radius = 2. * __longlong_as_double(static_cast<long long>(sbi));
     const double radiusSqr = radius * radius;
     const float slack = float(radius) * 1e-6f + float(gi.cell) * 2e-5f;
+    const float4 vfi = c.velf[k];
+    const float vabsi = sqrtf(vfi.x * vfi.x + vfi.y * vfi.y + vfi.z * vfi.z);
+    const float dtf = float(dt);
     const float rOut = float(radius) + slack;
     const float rIn = float(radius) - slack;
     const float rOut2 = rOut * rOut;
@@ -516,6 +521,21 @@ __global__ void __launch_bounds__(128) detectKernel(DState s, Grid g, Collide c,
                         // the reference's `removed` set still holds the previous call's indices during the
                         // first pass (it is cleared after it, NBodySolver.cpp:367-396)
                         continue;
+                    }
+                    {
+                        // the FP32 rejection of evalPair on the cell-sorted copies (no FP64 work for pairs
+                        // whose surfaces are further apart than their relative motion can close in dt); the
+                        // distance is bounded below by the copies' rounding slack, the velocity difference
+                        // widened by 1e-6 of the speeds
+                        const float4 vfj = c.velf[q];
+                        const float ux = vfi.x - vfj.x, uy = vfi.y - vfj.y, uz = vfi.z - vfj.z;
+                        const float vabsj = sqrtf(vfj.x * vfj.x + vfj.y * vfj.y + vfj.z * vfj.z);
+                        const float du = sqrtf(ux * ux + uy * uy + uz * uz);
+                        const float dist = sqrtf(d2) * (1.f - 1e-6f) - slack;
+                        const float reach = (vfi.w + vfj.w + du * dtf) * 1.0001f + 1e-6f * (vabsi + vabsj) * dtf;
+                        if (dist > reach) {
+                            continue;
+                        }
                     }
                     if (!own) {
                         vi = s.v[i];
@@ -1119,6 +1139,7 @@ cudaError_t collideAllocate(Collide& c, uint32_t n, uint32_t cellCapacity) {
     A(&c.rs, nn);
     A(&c.posf, nn);
     A(&c.sbits, nn);
+    A(&c.velf, nn);
     if (e == cudaSuccess) {
         e = cudaMallocHost((void**)&c.counters_host, CNT_COUNT * sizeof(unsigned long long));
     }
@@ -1150,7 +1171,7 @@ cudaError_t collideAllocate(Collide& c, uint32_t n, uint32_t cellCapacity) {
 void collideFree(Collide& c) {
     void* ptrs[] = { c.s, c.srad, c.nsel, c.writer, c.ver, c.bounces, c.removed, c.prev_removed, c.head, c.moved_cell, c.pool,
         c.valid, c.order_a, c.order_b, c.key_a, c.key_b, c.extra_head, c.extra, c.counters, c.temp, c.scan, c.rs,
-        c.posf, c.sbits };
+        c.posf, c.sbits, c.velf };
     for (void* p : ptrs) {
         if (p) {
             cudaFree(p);

@@ -126,6 +126,7 @@ struct Collide {
     dbl4* rs = nullptr;          // cell-sorted positions (first pass)
     float4* posf = nullptr;      // cell-sorted FP32 positions relative to the cell origin, 2 s
     unsigned long long* sbits = nullptr; // cell-sorted bit patterns of s
+    float4* velf = nullptr;      // cell-sorted FP32 velocity and radius h
     // compaction targets, swapped with the state arrays (allocated and freed with the state arrays)
     dbl4* tmp_r = nullptr;
     dbl4* tmp_v = nullptr;

@@ -68,6 +68,7 @@ def library():
     lib.sphgpu_particle_count.argtypes = [h, ctypes.POINTER(ctypes.c_uint64)]
     lib.sphgpu_collision_stats.argtypes = [h, ctypes.POINTER(ctypes.c_uint64)]
     lib.sphgpu_collision_profile.argtypes = [h, ctypes.POINTER(ctypes.c_uint64)]
+    lib.sphgpu_take_removed.argtypes = [h, _U4P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]
     _LIB = lib
     return lib
 
@@ -200,6 +201,18 @@ class GpuSolver:
         """HardSphereSolver::collide over [0, dt) (N-body solver); merged particles are removed."""
         self._check(self._lib.sphgpu_collide(self._h, float(dt)))
         self._refresh_count()
+
+    def take_removed(self):
+        """Indices (numbering of the previous call or of the last position upload) removed by merging since."""
+        cnt = ctypes.c_uint64(0)
+        rc = self._lib.sphgpu_take_removed(self._h, None, 0, ctypes.byref(cnt))
+        if rc not in (abi.OK, abi.ERR_CAPACITY):
+            self._check(rc)
+        out = np.zeros(cnt.value, dtype="u4")
+        if cnt.value:
+            self._check(self._lib.sphgpu_take_removed(self._h, out.ctypes.data_as(_U4P), cnt.value,
+                                                      ctypes.byref(cnt)))
+        return out
 
     def collision_profile(self):
         """Records processed by the collision loop and its SM cycles (serial part, re-searches, insertions)."""

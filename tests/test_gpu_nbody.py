@@ -70,6 +70,24 @@ def test_gpu_single_collide_matches_oracle(name):
         assert nc.scale_err(got[f], ref[f]) < TOL_CALL, f
 
 
+def test_gpu_take_removed_lists_the_merged_particles():
+    fx = nc.load("nbody_merge_n1000")
+    cfg, keep = nc.config_of(fx)
+    dt = 150.0
+    with GpuSolver(cfg, keep) as g:
+        g.set_state(nc.state_of(fx, "s0_"))
+        g.collide(dt)
+        removed = g.take_removed()
+        again = g.take_removed()
+        n = g.n
+    ref = nc.state_of(fx, "s0_")
+    _, _, origin = oracle.nbody_collide(cfg, ref, dt, origin=True, prev_removed=[])
+    expected = np.setdiff1d(np.arange(len(fx["s0_m"])), origin)
+    assert len(expected) > 0
+    np.testing.assert_array_equal(removed, expected)
+    assert len(again) == 0 and n == len(origin)
+
+
 def test_gpu_removed_indices_persist_to_the_next_call():
     # two collide calls: the second call's first pass skips the indices the first call removed
     fx = nc.load("nbody_merge_n1000")

@@ -290,10 +290,10 @@ def compare_fp64(args, st, mats, n, mixed_cfg, dev):
     return out
 
 
-# DRAM bytes (read + write) of one walkMixedKernel launch of the default workload, from the ncu capture
-# summarised in profiles/walkMixedKernel_impact1M.md
-WALK_TRAFFIC_BYTES = (762.39 + 351.86) * 1e6
-WALK_TRAFFIC_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, profiles/walkMixedKernel_impact1M.md"
+# DRAM bytes (read + write) of one mixed walk of the default workload (the evaluation launch plus the launches
+# that build the interaction lists), from the ncu capture summarised in profiles/evalListsKernel_impact1M.md
+WALK_TRAFFIC_BYTES = (266.2 + 29.8 + 176.8 + 47.2) * 1e6
+WALK_TRAFFIC_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, profiles/evalListsKernel_impact1M.md"
 
 # FP32 operations of one particle-multipole evaluation (evalMultipoleF, csrc/gravity32.cu: octupole) and the
 # N-body convention for one softened particle-particle interaction
@@ -554,7 +554,7 @@ def main():
         "vs_baseline": None, "dtype": "f32/f64", "data": "synthetic", "config": config_json(args, n),
         "e2e": res["e2e"], "gpu_launches": res["launches"], "clocks": res["clocks"],
         "phases_ms_per_step": {k: v / args.steps for k, v in res["phases"].items()},
-        "roofline": {"kernel": "walkMixedKernel", "bound": "fp32", "achieved": walk_tf, "peak": FP32_PEAK_NOMINAL,
+        "roofline": {"kernel": "evalListsKernel + listLevelKernel (mixed walk)", "bound": "fp32", "achieved": walk_tf, "peak": FP32_PEAK_NOMINAL,
                      "unit": "TFLOP/s", "frac": walk_tf / FP32_PEAK_NOMINAL if walk_tf else None,
                      "traffic": WALK_TRAFFIC_BYTES, "traffic_source": WALK_TRAFFIC_SOURCE,
                      "peak_source": "nominal FP32 (152 SMs x 128 lanes x 2 x 2.07 GHz); MEASURED_PEAKS.json has no "

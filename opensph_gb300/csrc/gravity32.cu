@@ -160,33 +160,169 @@ __device__ __forceinline__ void evalMultipoleF(float drx, float dry, float drz, 
 // particle of each particle list), and their partial sums are added to group 0 in group order at the end.
 constexpr uint32_t MAX_GROUPS = 4;
 
-__global__ void __launch_bounds__(WALK_THREADS_F, 12) walkMixedKernel(const uint32_t* __restrict__ idx,
-    const BhNodeGeom* __restrict__ geom, const float* __restrict__ nodef, const float4* __restrict__ pf,
-    const float* __restrict__ mf, const uint32_t* __restrict__ leaves, uint32_t nLeaves, const float* __restrict__ lut,
-    int kernelRadius, int order, int32_t* scratch, uint32_t listCap, dbl4* agrav, unsigned long long* stats,
+// ---- two-phase walk ----------------------------------------------------------------------------------------
+//
+// The dual walk of the reference (BarnesHut::evalNode, core/gravity/BarnesHut.cpp:212-312) classifies, at each
+// node ev on a leaf's path, the check list it inherits from ev's parent (plus ev's sibling) against ev's box:
+// entries that cannot be decided for all of ev are kept for ev's children. The classification at ev does not
+// depend on the leaf below it, so it is done once per node: phase 1 (listLevelKernel, one launch per tree
+// level, a warp per node) builds every node's node list N(ev), particle-list list P(ev) and kept list K(ev);
+// phase 2 (evalListsKernel, a warp per leaf) evaluates, for the particles of a leaf, the N and P lists of all
+// its ancestors and the pairs inside the leaf. The interaction lists are those of the per-leaf walk.
+
+constexpr int NL_META = 6; // per node: N offset, N length, P offset, P length, kept offset, kept length
+
+__global__ void flagErrorKernel(uint32_t* devError, uint32_t bit) {
+    atomicOr(devError, bit);
+}
+
+__global__ void __launch_bounds__(128) listLevelKernel(const BhNodeGeom* __restrict__ geom,
+    const float* __restrict__ nodef, uint32_t first, uint32_t last, int32_t* scratch, uint32_t cap,
+    int32_t* __restrict__ pool, uint32_t poolCap, const int32_t* __restrict__ keptIn, int32_t* __restrict__ keptOut,
+    uint32_t keptCap, uint32_t* __restrict__ meta, uint32_t* __restrict__ counters, int parity,
     uint32_t* devError) {
-    __shared__ int32_t pathSh[WALK_THREADS_F / 32][MAX_PATH_F];
+    __shared__ WalkFrame frameSh[4];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const uint32_t warpGlobal = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nWarps = (gridDim.x * blockDim.x) >> 5;
-    int32_t* listA = scratch + size_t(warpGlobal) * 2 * listCap;
-    int32_t* listB = listA + listCap;
+    int32_t* cur = scratch + size_t(warpGlobal) * 4 * cap;
+    int32_t* kept = cur + cap;
+    int32_t* lN = kept + cap;
+    int32_t* lP = lN + cap;
+    const float4* nf = reinterpret_cast<const float4*>(nodef);
+    const float zero3[3] = { 0.f, 0.f, 0.f };
+    for (uint32_t ev = first + warpGlobal; ev < last; ev += nWarps) {
+        const BhNodeGeom& eg = geom[ev];
+        const int par = eg.parent;
+        const int pl = geom[par].left;
+        const int sib = pl == int(ev) ? geom[par].right : pl;
+        const uint32_t kIn = meta[size_t(par) * NL_META + 5];
+        const uint32_t kOff = meta[size_t(par) * NL_META + 4];
+        bool overflow = kIn + 1 > cap;
+        uint32_t ncur = 0;
+        if (!overflow) {
+            for (uint32_t e = lane; e < kIn; e += 32) {
+                cur[e] = keptIn[kOff + e];
+            }
+            ncur = kIn + 1;
+            if (lane == 0) {
+                cur[kIn] = sib;
+            }
+        }
+        // the box of ev relative to its own centre of mass (the classification frame of the per-leaf walk
+        // used the leaf's centre; any frame gives the same FP64-guarded decisions)
+        float lh[3], ll[3];
+        {
+            const float4 a = nodeGroup(nf, int(ev), NF_COM_HI), b = nodeGroup(nf, int(ev), NF_COM_LO);
+            lh[0] = a.x, lh[1] = a.y, lh[2] = a.z;
+            ll[0] = b.x, ll[1] = b.y, ll[2] = b.z;
+        }
+        WalkFrame& fr = frameSh[wib];
+        if (lane == 0) {
+            setFrame(fr, nf, int(ev), eg.left < 0, lh, ll);
+        }
+        __syncwarp();
+        (void)zero3;
+        uint32_t nK = 0, nN = 0, nP = 0;
+        uint32_t pos = 0;
+        while (pos < ncur && !overflow) {
+            const uint32_t batch = min(32u, ncur - pos);
+            int node = -1, cls = CL_KEEP;
+            if (uint32_t(lane) < batch) {
+                node = cur[pos + lane];
+                cls = classifyEntry(node, geom, nf, fr, lh, ll);
+            }
+            const bool valid = uint32_t(lane) < batch;
+            const unsigned mKeep = __ballot_sync(0xffffffffu, valid && cls == CL_KEEP);
+            const unsigned mOpen = __ballot_sync(0xffffffffu, valid && cls == CL_OPEN);
+            const unsigned mPart = __ballot_sync(0xffffffffu, valid && cls == CL_PARTICLES);
+            const unsigned mNode = __ballot_sync(0xffffffffu, valid && cls == CL_NODE);
+            const unsigned below = (1u << lane) - 1u;
+            if (ncur + 2 * __popc(mOpen) > cap || nK + __popc(mKeep) > cap || nN + __popc(mNode) > cap ||
+                nP + __popc(mPart) > cap) {
+                overflow = true;
+                break;
+            }
+            if (valid) {
+                if (cls == CL_KEEP) {
+                    kept[nK + __popc(mKeep & below)] = node;
+                } else if (cls == CL_NODE) {
+                    lN[nN + __popc(mNode & below)] = node;
+                } else if (cls == CL_PARTICLES) {
+                    lP[nP + __popc(mPart & below)] = node;
+                } else {
+                    const uint32_t slot = ncur + 2 * __popc(mOpen & below);
+                    const int2 ch = *reinterpret_cast<const int2*>(&geom[node].left);
+                    cur[slot] = ch.x;
+                    cur[slot + 1] = ch.y;
+                }
+            }
+            pos += batch;
+            ncur += 2 * __popc(mOpen);
+            nK += __popc(mKeep);
+            nN += __popc(mNode);
+            nP += __popc(mPart);
+            __syncwarp();
+        }
+        // space in the pools: the counters keep counting past the capacities, so that the host can grow the
+        // pools to the need and build the lists again
+        uint32_t base = 0, kbase = 0;
+        if (lane == 0 && !overflow) {
+            base = atomicAdd(&counters[0], nN + nP);
+            kbase = nK ? atomicAdd(&counters[1 + parity], nK) : 0u;
+            atomicMax(&counters[3], kbase + nK);
+        }
+        base = __shfl_sync(0xffffffffu, base, 0);
+        kbase = __shfl_sync(0xffffffffu, kbase, 0);
+        if (overflow || base + nN + nP > poolCap || kbase + nK > keptCap) {
+            if (lane == 0) {
+                if (overflow) {
+                    atomicOr(devError, uint32_t(DEV_ERR_WALK_CAPACITY));
+                }
+                uint32_t* m = meta + size_t(ev) * NL_META;
+                m[0] = m[1] = m[2] = m[3] = m[4] = m[5] = 0;
+            }
+            continue;
+        }
+        for (uint32_t e = lane; e < nN; e += 32) {
+            pool[base + e] = lN[e];
+        }
+        for (uint32_t e = lane; e < nP; e += 32) {
+            pool[base + nN + e] = lP[e];
+        }
+        for (uint32_t e = lane; e < nK; e += 32) {
+            keptOut[kbase + e] = kept[e];
+        }
+        if (lane == 0) {
+            uint32_t* m = meta + size_t(ev) * NL_META;
+            m[0] = base;
+            m[1] = nN;
+            m[2] = base + nN;
+            m[3] = nP;
+            m[4] = kbase;
+            m[5] = nK;
+        }
+        __syncwarp();
+    }
+}
+
+__global__ void __launch_bounds__(WALK_THREADS_F, 8) evalListsKernel(const uint32_t* __restrict__ idx,
+    const BhNodeGeom* __restrict__ geom, const float* __restrict__ nodef, const float4* __restrict__ pf,
+    const float* __restrict__ mf, const uint32_t* __restrict__ leaves, uint32_t nLeaves,
+    const float* __restrict__ lut, int kernelRadius, int order, const int32_t* __restrict__ pool,
+    const uint32_t* __restrict__ meta, dbl4* agrav, unsigned long long* stats) {
+    __shared__ int32_t pathSh[WALK_THREADS_F / 32][MAX_PATH_F];
+    __shared__ unsigned long long countSh[WALK_THREADS_F / 32][4];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
     int32_t* path = pathSh[wib];
     const float4* nf = reinterpret_cast<const float4*>(nodef);
-    // interaction counters of the warp (approximated nodes, particle lists, particle-node and particle-particle
-    // evaluations), kept in shared memory to leave the registers to the walk
-    __shared__ unsigned long long countSh[WALK_THREADS_F / 32][4];
-    __shared__ WalkFrame frameSh[WALK_THREADS_F / 32];
     unsigned long long* wc = countSh[wib];
     if (lane < 4) {
         wc[lane] = 0;
     }
     __syncwarp();
-
-    (void)nWarps;
-
-    // leaves are taken from a shared counter (stats[4]) so that warps that drew cheap leaves take more
     for (;;) {
         uint32_t li = 0;
         if (lane == 0) {
@@ -212,9 +348,6 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 12) walkMixedKernel(const uint
                 path[k] = nd;
                 nd = geom[nd].parent;
             }
-            if (d >= MAX_PATH_F - 1) {
-                atomicOr(devError, uint32_t(DEV_ERR_WALK_CAPACITY));
-            }
         }
         depth = __shfl_sync(0xffffffffu, depth, 0);
         __syncwarp();
@@ -233,61 +366,15 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 12) walkMixedKernel(const uint
             di = pf[from + pid];
         }
         KahanF ax, ay, az;
-        int32_t* cur = listA;
-        int32_t* nxt = listB;
-        uint32_t ncur = 0, nnxt = 0;
-        bool overflow = false;
-        for (int k = 1; k <= depth && !overflow; ++k) {
-            const int ev = path[k];
-            const int par = path[k - 1];
-            const int pl = geom[par].left;
-            const int sib = pl == ev ? geom[par].right : pl;
-            // the frame is the same for the whole warp: kept in shared memory, not in 8 registers per lane
-            WalkFrame& fr = frameSh[wib];
-            if (lane == 0) {
-                setFrame(fr, nf, ev, k == depth, lh, ll);
-            }
-            if (lane == 0) {
-                cur[ncur] = sib;
-            }
-            ncur += 1;
-            __syncwarp();
-            uint32_t pos = 0;
-            while (pos < ncur) {
-                const uint32_t batch = min(32u, ncur - pos);
-                const uint32_t e = pos + lane;
-                int node = -1, cls = CL_KEEP;
-                if (uint32_t(lane) < batch) {
-                    node = cur[e];
-                    cls = classifyEntry(node, geom, nf, fr, lh, ll);
-                }
-                const unsigned mKeep = __ballot_sync(0xffffffffu, uint32_t(lane) < batch && cls == CL_KEEP);
-                const unsigned mOpen = __ballot_sync(0xffffffffu, cls == CL_OPEN);
-                const unsigned mPart = __ballot_sync(0xffffffffu, cls == CL_PARTICLES);
-                const unsigned mNode = __ballot_sync(0xffffffffu, cls == CL_NODE);
-                const unsigned below = (1u << lane) - 1u;
-                const uint32_t nOpen = __popc(mOpen), nKeep = __popc(mKeep);
-                if (ncur + 2 * nOpen > listCap || nnxt + nKeep > listCap) {
-                    overflow = true;
-                    break;
-                }
-                if (cls == CL_KEEP && uint32_t(lane) < batch) {
-                    nxt[nnxt + __popc(mKeep & below)] = node;
-                }
-                if (cls == CL_OPEN) {
-                    const uint32_t slot = ncur + 2 * __popc(mOpen & below);
-                    const int2 ch = *reinterpret_cast<const int2*>(&geom[node].left);
-                    cur[slot] = ch.x;
-                    cur[slot + 1] = ch.y;
-                }
-                pos += batch;
-                ncur += 2 * nOpen;
-                nnxt += nKeep;
-                __syncwarp();
-                // plain FP32 partial sums over this batch's interactions, added to the compensated totals once
+        for (int k = 1; k <= depth; ++k) {
+            const uint32_t* m = meta + size_t(path[k]) * NL_META;
+            const uint32_t nOff = m[0], nLen = m[1], pOff = m[2], pLen = m[3];
+            // particle lists of this level, then its nodes, 32 entries at a time
+            for (uint32_t c = 0; c < pLen; c += 32) {
+                const uint32_t batch = min(32u, pLen - c);
+                const int node = uint32_t(lane) < batch ? pool[pOff + c + lane] : -1;
                 float bx = 0.f, by = 0.f, bz = 0.f;
-                // particle lists: every particle of the listed leaves, split over the lane groups
-                unsigned mp = mPart;
+                unsigned mp = (batch == 32u) ? 0xffffffffu : ((1u << batch) - 1u);
                 while (mp) {
                     const int src = __ffs(mp) - 1;
                     mp &= mp - 1;
@@ -315,24 +402,25 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 12) walkMixedKernel(const uint
                         }
                     }
                 }
-                // multipole expansions: rounds of g nodes, node q of a round to lane group q
-                unsigned mn = mNode;
-                if (lane == 0) {
-                    const uint32_t nNodes = __popc(mNode);
-                    wc[0] += nNodes;
-                    wc[2] += uint64_t(cnt) * nNodes;
+                if (inGroup) {
+                    ax.add(bx);
+                    ay.add(by);
+                    az.add(bz);
                 }
-                while (mn) {
-                    int mysrc = -1;
-                    for (uint32_t q = 0; q < g && mn; ++q) {
-                        const int b = __ffs(mn) - 1;
-                        mn &= mn - 1;
-                        if (q == grp) {
-                            mysrc = b;
-                        }
-                    }
-                    const int nn = __shfl_sync(0xffffffffu, node, mysrc < 0 ? 0 : mysrc);
-                    if (inGroup && mysrc >= 0) {
+            }
+            for (uint32_t c = 0; c < nLen; c += 32) {
+                const uint32_t batch = min(32u, nLen - c);
+                const int node = uint32_t(lane) < batch ? pool[nOff + c + lane] : -1;
+                if (lane == 0) {
+                    wc[0] += batch;
+                    wc[2] += uint64_t(cnt) * batch;
+                }
+                float bx = 0.f, by = 0.f, bz = 0.f;
+                // rounds of g nodes, node q of a round to lane group q
+                for (uint32_t q0 = 0; q0 < batch; q0 += g) {
+                    const uint32_t q = q0 + grp;
+                    const int nn = __shfl_sync(0xffffffffu, node, int(min(q, 31u)));
+                    if (inGroup && q < batch) {
                         const float4 c0 = nodeGroup(nf, nn, NF_COM_HI), c1 = nodeGroup(nf, nn, NF_COM_LO);
                         const float4 c2 = nodeGroup(nf, nn, NF_MOM), c3 = nodeGroup(nf, nn, NF_MOM + 1);
                         const float4 c4 = nodeGroup(nf, nn, NF_MOM + 2), c5 = nodeGroup(nf, nn, NF_MOM + 3);
@@ -348,17 +436,6 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 12) walkMixedKernel(const uint
                     az.add(bz);
                 }
             }
-            int32_t* t = cur;
-            cur = nxt;
-            nxt = t;
-            ncur = nnxt;
-            nnxt = 0;
-        }
-        if (overflow) {
-            if (lane == 0) {
-                atomicOr(devError, uint32_t(DEV_ERR_WALK_CAPACITY));
-            }
-            continue;
         }
         // pairs inside the leaf
         if (lane == 0) {
@@ -401,12 +478,15 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 12) walkMixedKernel(const uint
             const uint32_t pi = idx[from + pid];
             agrav[pi] = mkd4(double(ax.s) - double(ax.c), double(ay.s) - double(ay.c), double(az.s) - double(az.c), 0.);
         }
+        __syncwarp();
     }
     __syncwarp();
     if (lane < 4) {
         atomicAdd(&stats[lane], wc[lane]);
     }
 }
+
+
 
 } // namespace
 
@@ -421,19 +501,77 @@ void launchPrepareWalk(const DState& s, Tree& t, const Physics& ph, cudaStream_t
 void launchGravityWalkMixed(const DState& s, Tree& t, const Physics& ph, const float* lutF, uint32_t* devError,
     cudaStream_t st) {
     cudaMemsetAsync(t.stats, 0, 5 * sizeof(unsigned long long), st);
+    t.walk_launches = 0;
     if (s.n == 0 || t.node_count == 0) {
         return;
+    }
+    if (!t.nl_meta) {
+        cudaMalloc(&t.nl_meta, size_t(t.node_capacity) * NL_META * sizeof(uint32_t));
+        cudaMalloc(&t.nl_counters, 8 * sizeof(uint32_t));
+        cudaMallocHost(&t.nl_host, 8 * sizeof(uint32_t));
+    }
+    // per-warp staging of one node's lists in the walk scratch: 4 lists of NL_STAGE entries
+    constexpr uint32_t NL_STAGE = 16384;
+    const uint32_t listWarps =
+        std::max(1u, uint32_t(size_t(t.walk_warps) * 2 * t.walk_capacity / (4 * size_t(NL_STAGE))));
+    uint32_t poolNeed = std::max<uint32_t>(1u << 20, 64u * t.node_count);
+    uint32_t keptNeed = std::max<uint32_t>(1u << 20, 32u * t.node_count);
+    const uint32_t levels = uint32_t(t.level_start.size());
+    // the lists of all levels; when a pool overflowed, grow it to twice the counted need (the count misses what
+    // the children of the nodes that did not fit would have added) and build them again
+    bool fits = false;
+    for (int attempt = 0; attempt < 4 && !fits; ++attempt) {
+        if (t.nl_capacity < poolNeed) {
+            cudaFree(t.nl_pool);
+            cudaMalloc(&t.nl_pool, size_t(poolNeed) * sizeof(int32_t));
+            t.nl_capacity = poolNeed;
+        }
+        if (t.nl_kept_capacity < keptNeed) {
+            cudaFree(t.nl_kept[0]);
+            cudaFree(t.nl_kept[1]);
+            cudaMalloc(&t.nl_kept[0], size_t(keptNeed) * sizeof(int32_t));
+            cudaMalloc(&t.nl_kept[1], size_t(keptNeed) * sizeof(int32_t));
+            t.nl_kept_capacity = keptNeed;
+        }
+        cudaMemsetAsync(t.nl_counters, 0, 8 * sizeof(uint32_t), st);
+        cudaMemsetAsync(t.nl_meta, 0, NL_META * sizeof(uint32_t), st); // the root: nothing kept
+        for (uint32_t level = 1; level < levels; ++level) {
+            const uint32_t first = t.level_start[level];
+            const uint32_t last = level + 1 < levels ? t.level_start[level + 1] : t.node_count;
+            if (last <= first) {
+                continue;
+            }
+            const int parity = int(level & 1u);
+            cudaMemsetAsync(t.nl_counters + 1 + parity, 0, sizeof(uint32_t), st);
+            const uint32_t warps = std::min(last - first, listWarps);
+            listLevelKernel<<<ceilDiv(warps, 4), 128, 0, st>>>(t.geom, t.nodef, first, last, t.walk_scratch, NL_STAGE,
+                t.nl_pool, t.nl_capacity, t.nl_kept[1 - parity], t.nl_kept[parity], t.nl_kept_capacity, t.nl_meta,
+                t.nl_counters, parity, devError);
+            t.walk_launches++;
+        }
+        cudaMemcpyAsync(t.nl_host, t.nl_counters, 8 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+        if (cudaStreamSynchronize(st) != cudaSuccess) {
+            return;
+        }
+        const uint32_t usedPool = t.nl_host[0], usedKept = t.nl_host[3];
+        fits = usedPool <= t.nl_capacity && usedKept <= t.nl_kept_capacity;
+        poolNeed = std::max(poolNeed, 2 * usedPool);
+        keptNeed = std::max(keptNeed, 2 * usedKept);
+    }
+    if (!fits) {
+        flagErrorKernel<<<1, 1, 0, st>>>(devError, uint32_t(DEV_ERR_WALK_CAPACITY));
     }
     static int residentBlocks = 0;
     if (residentBlocks == 0) {
         int perSm = 0, sms = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, walkMixedKernel, WALK_THREADS_F, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, evalListsKernel, WALK_THREADS_F, 0);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
         residentBlocks = std::max(1, perSm * sms);
     }
     const int blocks = std::max(1, std::min(residentBlocks, int(t.walk_warps / (WALK_THREADS_F / 32))));
-    walkMixedKernel<<<blocks, WALK_THREADS_F, 0, st>>>(t.idx, t.geom, t.nodef, t.pf, t.mf, t.leaves, t.leaf_count,
-        lutF, ph.kernel_radius, ph.multipole_order, t.walk_scratch, t.walk_capacity, s.agrav, t.stats, devError);
+    evalListsKernel<<<blocks, WALK_THREADS_F, 0, st>>>(t.idx, t.geom, t.nodef, t.pf, t.mf, t.leaves, t.leaf_count,
+        lutF, ph.kernel_radius, ph.multipole_order, t.nl_pool, t.nl_meta, s.agrav, t.stats);
+    t.walk_launches++;
 }
 
 } // namespace sphgpu

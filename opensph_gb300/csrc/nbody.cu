@@ -448,7 +448,7 @@ __global__ void gatherKernel(DState s, Grid g, Collide c) {
 // The distance test runs on the FP32 cell-relative copies with a margin that bounds their rounding
 // (1e-6 of the radius plus 2e-5 of the cell edge); only candidates within the margin of the sphere are tested
 // again in FP64, so the neighbour set is exactly the FP64 one.
-__global__ void __launch_bounds__(128) detectKernel(DState s, Grid g, Collide c, CollideParams p,
+__global__ void __launch_bounds__(128, 4) detectKernel(DState s, Grid g, Collide c, CollideParams p,
     const double* __restrict__ dtp, double factor) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= s.n) {

@@ -242,6 +242,16 @@ struct Tree {
     uint32_t* leaves = nullptr;       // leaf node ids
     uint32_t* visits = nullptr;       // per node: children finished (bottom-up moments)
     int32_t* walk_scratch = nullptr;  // per-warp checklists
+    // mixed walk in two phases: the interaction lists of every node, built once per node level by level, and
+    // the per-leaf evaluation over the lists of the leaf's ancestors
+    int32_t* nl_pool = nullptr;       // node (N) and particle-list (P) entries of all nodes
+    uint32_t nl_capacity = 0;
+    int32_t* nl_kept[2] = { nullptr, nullptr }; // kept (undecided) lists of two consecutive levels
+    uint32_t nl_kept_capacity = 0;
+    uint32_t* nl_meta = nullptr;      // per node: N offset, N length, P offset, P length, kept offset, kept length
+    uint32_t* nl_counters = nullptr;  // device: pool entries used, kept entries used (two levels), max kept
+    uint32_t* nl_host = nullptr;      // pinned mirror of nl_counters
+    uint32_t walk_launches = 0;       // kernels launched by the last mixed walk
     uint32_t walk_warps = 0;
     uint32_t walk_capacity = 0;       // entries per list per warp
     unsigned long long* stats = nullptr; // device: approx, exact

@@ -70,7 +70,8 @@ __global__ void prepareMixedKernel(const dbl4* __restrict__ r, const double* __r
         for (uint32_t k = g.from; k < g.to; ++k) {
             const uint32_t i = idx[k];
             const dbl4 p = r[i];
-            pf[k] = make_float4(float(p.x - g.com[0]), float(p.y - g.com[1]), float(p.z - g.com[2]), float(p.w));
+            // w: half the smoothing length, so that a pair's symmetrised length is one addition
+            pf[k] = make_float4(float(p.x - g.com[0]), float(p.y - g.com[1]), float(p.z - g.com[2]), 0.5f * float(p.w));
             mf[k] = float(G * m[i]);
         }
     }
@@ -86,72 +87,79 @@ struct KahanF {
     }
 };
 
-// GravityLutKernel::grad in FP32 (radius 0: point masses)
-__device__ __forceinline__ void gravGradF(float rx, float ry, float rz, float h, const float* __restrict__ lut,
-    int kernelRadius, float& gx, float& gy, float& gz) {
-    const float d2 = rx * rx + ry * ry + rz * rz;
-    const float hInv = 1.f / h;
-    const float qSqr = d2 * (hInv * hInv);
-    const float rad = float(kernelRadius);
-    if (qSqr >= rad * rad) {
+// GravityLutKernel::grad in FP32 (radius 0: point masses), accumulated as m (gx, gy, gz) into (bx, by, bz).
+// h is the pair's symmetrised smoothing length; rad2 the squared kernel radius (0: every pair is a point
+// pair). The point-mass branch is taken when |r| >= radius h, tested as |r|^2 >= radius^2 h^2 so that the
+// far pairs need no reciprocal of h; inside the kernel the LUT index is clamped to the table, so the rounding
+// of the test at the boundary (where the LUT equals the point-mass value) reads no entry past the last.
+__device__ __forceinline__ void gravAccF(float rx, float ry, float rz, float h, float m, const float* __restrict__ lut,
+    float rad2, float& bx, float& by, float& bz) {
+    const float d2 = fmaf(rz, rz, fmaf(ry, ry, rx * rx));
+    float g;
+    if (d2 >= rad2 * (h * h)) {
         const float inv = rsqrtf(d2);
-        const float inv3 = inv * inv * inv;
-        gx = rx * inv3;
-        gy = ry * inv3;
-        gz = rz * inv3;
-        return;
+        g = inv * inv * inv;
+    } else {
+        const float hInv = __frcp_rn(h);
+        const float hInv2 = hInv * hInv;
+        const float floatIdx = float(LUT_ENTRIES / 4) * (d2 * hInv2);
+        const int idx1 = min(int(floatIdx), LUT_ENTRIES - 1);
+        const float ratio = floatIdx - float(idx1);
+        const float g0 = __ldg(lut + idx1), g1 = __ldg(lut + idx1 + 1);
+        g = fmaf(g1 - g0, ratio, g0) * (hInv2 * hInv);
     }
-    const float floatIdx = float(LUT_ENTRIES / 4) * qSqr;
-    const int idx1 = min(int(floatIdx), LUT_ENTRIES - 1);
-    const float ratio = floatIdx - float(idx1);
-    const float g0 = __ldg(lut + idx1), g1 = __ldg(lut + idx1 + 1);
-    const float g = (g0 + (g1 - g0) * ratio) * (hInv * hInv * hInv);
-    gx = rx * g;
-    gy = ry * g;
-    gz = rz * g;
+    const float mg = m * g;
+    bx = fmaf(mg, rx, bx);
+    by = fmaf(mg, ry, by);
+    bz = fmaf(mg, rz, bz);
 }
 
-// evaluateGravity (core/gravity/Moments.h:336-360) in FP32 at dr = r_i - com; m0 = c0.w, the traceless
-// quadrupole and octupole in c2..c5 (layout of the node record)
-__device__ __forceinline__ void evalMultipoleF(float drx, float dry, float drz, float m0, const float4& c2,
-    const float4& c3, const float4& c4, const float4& c5, int order, float& ax, float& ay, float& az) {
-    const float d2 = drx * drx + dry * dry + drz * drz;
+// evaluateGravity (core/gravity/Moments.h:336-360) in FP32, accumulated into (bx, by, bz); (x, y, z) = com - r_i
+// (the reference's dr = r_i - com, negated), m0 = c0.w, the traceless quadrupole and octupole in c2..c5
+// (layout of the node record). The reference's terms g1 m0 x + g3 Q0q x + g2 Q1 + g4 Q0o x + g3 s / 2 (with
+// g1 = |x|^-3, g2 = -3 |x|^-5, g3 = 15 |x|^-7, g4 = -105 |x|^-9, Q1 = q2 . x, Q0q = x . Q1 / 2, s = q3 : x x,
+// Q0o = x . s / 6) are evaluated on the unit vector u = x / |x|:
+//   a = |x|^-2 [ (m0 + 7.5 |x|^-2 u.q2.u - 17.5 |x|^-3 q3:uuu) u - 3 |x|^-2 q2.u + 7.5 |x|^-3 q3:uu ],
+// so that no intermediate is a high power of 1/|x| (|x|^-9 is below the FP32 normal range at the separations of
+// kilometre-sized bodies; every factor here is of the order of m0).
+__device__ __forceinline__ void accMultipoleF(float x, float y, float z, float m0, const float4& c2, const float4& c3,
+    const float4& c4, const float4& c5, int order, float& bx, float& by, float& bz) {
+    const float d2 = fmaf(z, z, fmaf(y, y, x * x));
     const float inv = rsqrtf(d2);
-    const float invDistSqr = inv * inv;
-    const float g0 = -inv;
-    const float g1 = -invDistSqr * g0;
-    const float g2 = -3.f * invDistSqr * g1;
-    const float g3 = -5.f * invDistSqr * g2;
-    const float g4 = -7.f * invDistSqr * g3;
-    const float x = -drx, y = -dry, z = -drz;
-    float rx = g1 * x * m0, ry = g1 * y * m0, rz = g1 * z * m0;
+    const float t = inv * inv;
+    const float ux = x * inv, uy = y * inv, uz = z * inv;
+    float A = m0, cx = 0.f, cy = 0.f, cz = 0.f;
     if (order >= 2) {
         const float qxx = c2.x, qxy = c2.y, qxz = c2.z, qyy = c2.w, qyz = c3.x, qzz = c3.y;
-        const float Q1x = qxx * x + qxy * y + qxz * z;
-        const float Q1y = qxy * x + qyy * y + qyz * z;
-        const float Q1z = qxz * x + qyz * y + qzz * z;
-        const float Q0 = 0.5f * (Q1x * x + Q1y * y + Q1z * z);
-        rx += g3 * x * Q0 + g2 * Q1x;
-        ry += g3 * y * Q0 + g2 * Q1y;
-        rz += g3 * z * Q0 + g2 * Q1z;
+        const float Px = fmaf(qxz, uz, fmaf(qxy, uy, qxx * ux));
+        const float Py = fmaf(qyz, uz, fmaf(qyy, uy, qxy * ux));
+        const float Pz = fmaf(qzz, uz, fmaf(qyz, uy, qxz * ux));
+        const float t2 = -3.f * t;
+        A = fmaf(-2.5f * t2, fmaf(Pz, uz, fmaf(Py, uy, Px * ux)), A);
+        cx = t2 * Px;
+        cy = t2 * Py;
+        cz = t2 * Pz;
+        if (order >= 3) {
+            // xxx xxy xxz xyy xyz xzz yyy yyz yzz zzz
+            const float q0 = c3.z, q1 = c3.w, q2 = c4.x, q3 = c4.y, q4 = c4.z, q5 = c4.w, q6 = c5.x, q7 = c5.y,
+                        q8 = c5.z, q9 = c5.w;
+            const float t3 = t * inv;
+            const float ux2 = ux + ux, uy2 = uy + uy;
+            const float xx = ux * ux, yy = uy * uy, zz = uz * uz, xy2 = ux2 * uy, xz2 = ux2 * uz, yz2 = uy2 * uz;
+            // s_i = q_ijk u_j u_k
+            const float sx = fmaf(q4, yz2, fmaf(q2, xz2, fmaf(q1, xy2, fmaf(q5, zz, fmaf(q3, yy, q0 * xx)))));
+            const float sy = fmaf(q7, yz2, fmaf(q4, xz2, fmaf(q3, xy2, fmaf(q8, zz, fmaf(q6, yy, q1 * xx)))));
+            const float sz = fmaf(q8, yz2, fmaf(q5, xz2, fmaf(q4, xy2, fmaf(q9, zz, fmaf(q7, yy, q2 * xx)))));
+            const float o3 = 7.5f * t3;
+            A = fmaf(-17.5f * t3, fmaf(sz, uz, fmaf(sy, uy, sx * ux)), A);
+            cx = fmaf(o3, sx, cx);
+            cy = fmaf(o3, sy, cy);
+            cz = fmaf(o3, sz, cz);
+        }
     }
-    if (order >= 3) {
-        // xxx xxy xxz xyy xyz xzz yyy yyz yzz zzz
-        const float q0 = c3.z, q1 = c3.w, q2 = c4.x, q3 = c4.y, q4 = c4.z, q5 = c4.w, q6 = c5.x, q7 = c5.y,
-                    q8 = c5.z, q9 = c5.w;
-        const float xx = x * x, yy = y * y, zz = z * z, xy = x * y, xz = x * z, yz = y * z;
-        // s_i = q_ijk x_j x_k
-        const float sx = q0 * xx + q3 * yy + q5 * zz + 2.f * (q1 * xy + q2 * xz + q4 * yz);
-        const float sy = q1 * xx + q6 * yy + q8 * zz + 2.f * (q3 * xy + q4 * xz + q7 * yz);
-        const float sz = q2 * xx + q7 * yy + q9 * zz + 2.f * (q4 * xy + q5 * xz + q8 * yz);
-        const float Q0 = (sx * x + sy * y + sz * z) * (1.f / 6.f);
-        rx += g4 * x * Q0 + g3 * (0.5f * sx);
-        ry += g4 * y * Q0 + g3 * (0.5f * sy);
-        rz += g4 * z * Q0 + g3 * (0.5f * sz);
-    }
-    ax += rx;
-    ay += ry;
-    az += rz;
+    bx = fmaf(t, fmaf(A, ux, cx), bx);
+    by = fmaf(t, fmaf(A, uy, cy), by);
+    bz = fmaf(t, fmaf(A, uz, cz), bz);
 }
 
 // Leaves hold at most 32 particles. A leaf of cnt <= 16 particles splits its warp into g = min(32 / cnt, 4)
@@ -313,16 +321,14 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 8) evalListsKernel(const uint3
     const float* __restrict__ lut, int kernelRadius, int order, const int32_t* __restrict__ pool,
     const uint32_t* __restrict__ meta, dbl4* agrav, unsigned long long* stats) {
     __shared__ int32_t pathSh[WALK_THREADS_F / 32][MAX_PATH_F];
-    __shared__ unsigned long long countSh[WALK_THREADS_F / 32][4];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     int32_t* path = pathSh[wib];
     const float4* nf = reinterpret_cast<const float4*>(nodef);
-    unsigned long long* wc = countSh[wib];
-    if (lane < 4) {
-        wc[lane] = 0;
-    }
-    __syncwarp();
+    const float rad2 = float(kernelRadius) * float(kernelRadius);
+    // interaction counters (node lists, particle lists, particle-node and particle-particle evaluations), the
+    // same in every lane
+    unsigned long long cN = 0, cP = 0, cPN = 0, cPP = 0;
     for (;;) {
         uint32_t li = 0;
         if (lane == 0) {
@@ -355,20 +361,25 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 8) evalListsKernel(const uint3
         const uint32_t grp = cnt == 0 ? 0u : uint32_t(lane) / cnt;
         const uint32_t pid = uint32_t(lane) - grp * cnt;
         const bool inGroup = grp < g && cnt > 0;
-        float lh[3], ll[3];
+        float4 di = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (inGroup) {
+            di = pf[from + pid];
+        }
+        // the particle relative to the hi part of its leaf's centre: separations from a node centre c (hi + lo)
+        // are formed as (c.hi - leaf.hi) + (c.lo - pl), pl = leaf.lo + (r_i - leaf centre)
+        float lh[3], pl[3];
         {
             const float4 a = nodeGroup(nf, leaf, NF_COM_HI), b = nodeGroup(nf, leaf, NF_COM_LO);
             lh[0] = a.x, lh[1] = a.y, lh[2] = a.z;
-            ll[0] = b.x, ll[1] = b.y, ll[2] = b.z;
-        }
-        float4 di = make_float4(0.f, 0.f, 0.f, 1.f);
-        if (inGroup) {
-            di = pf[from + pid];
+            pl[0] = b.x + di.x, pl[1] = b.y + di.y, pl[2] = b.z + di.z;
         }
         KahanF ax, ay, az;
         for (int k = 1; k <= depth; ++k) {
             const uint32_t* m = meta + size_t(path[k]) * NL_META;
             const uint32_t nOff = m[0], nLen = m[1], pOff = m[2], pLen = m[3];
+            cN += nLen;
+            cP += pLen;
+            cPN += uint64_t(cnt) * nLen;
             // particle lists of this level, then its nodes, 32 entries at a time
             for (uint32_t c = 0; c < pLen; c += 32) {
                 const uint32_t batch = min(32u, pLen - c);
@@ -380,25 +391,17 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 8) evalListsKernel(const uint3
                     mp &= mp - 1;
                     const int pn = __shfl_sync(0xffffffffu, node, src);
                     const float4 a = nodeGroup(nf, pn, NF_COM_HI), b = nodeGroup(nf, pn, NF_COM_LO);
-                    const float Dx = (a.x - lh[0]) + (b.x - ll[0]);
-                    const float Dy = (a.y - lh[1]) + (b.y - ll[1]);
-                    const float Dz = (a.z - lh[2]) + (b.z - ll[2]);
+                    // separation of the source leaf's centre from particle i
+                    const float ox = (a.x - lh[0]) + (b.x - pl[0]);
+                    const float oy = (a.y - lh[1]) + (b.y - pl[1]);
+                    const float oz = (a.z - lh[2]) + (b.z - pl[2]);
                     const uint2 range = *reinterpret_cast<const uint2*>(&geom[pn].from);
-                    if (lane == 0) {
-                        wc[1] += 1;
-                        wc[3] += uint64_t(cnt) * (range.y - range.x);
-                    }
+                    cPP += uint64_t(cnt) * (range.y - range.x);
                     if (inGroup) {
 #pragma unroll 2
                         for (uint32_t t = range.x + grp; t < range.y; t += g) {
                             const float4 dj = pf[t];
-                            const float mj = mf[t];
-                            float gx, gy, gz;
-                            gravGradF((Dx + dj.x) - di.x, (Dy + dj.y) - di.y, (Dz + dj.z) - di.z, 0.5f * (dj.w + di.w),
-                                lut, kernelRadius, gx, gy, gz);
-                            bx += mj * gx;
-                            by += mj * gy;
-                            bz += mj * gz;
+                            gravAccF(ox + dj.x, oy + dj.y, oz + dj.z, dj.w + di.w, mf[t], lut, rad2, bx, by, bz);
                         }
                     }
                 }
@@ -411,10 +414,6 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 8) evalListsKernel(const uint3
             for (uint32_t c = 0; c < nLen; c += 32) {
                 const uint32_t batch = min(32u, nLen - c);
                 const int node = uint32_t(lane) < batch ? pool[nOff + c + lane] : -1;
-                if (lane == 0) {
-                    wc[0] += batch;
-                    wc[2] += uint64_t(cnt) * batch;
-                }
                 float bx = 0.f, by = 0.f, bz = 0.f;
                 // rounds of g nodes, node q of a round to lane group q
                 for (uint32_t q0 = 0; q0 < batch; q0 += g) {
@@ -424,10 +423,8 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 8) evalListsKernel(const uint3
                         const float4 c0 = nodeGroup(nf, nn, NF_COM_HI), c1 = nodeGroup(nf, nn, NF_COM_LO);
                         const float4 c2 = nodeGroup(nf, nn, NF_MOM), c3 = nodeGroup(nf, nn, NF_MOM + 1);
                         const float4 c4 = nodeGroup(nf, nn, NF_MOM + 2), c5 = nodeGroup(nf, nn, NF_MOM + 3);
-                        const float Dx = (c0.x - lh[0]) + (c1.x - ll[0]);
-                        const float Dy = (c0.y - lh[1]) + (c1.y - ll[1]);
-                        const float Dz = (c0.z - lh[2]) + (c1.z - ll[2]);
-                        evalMultipoleF(di.x - Dx, di.y - Dy, di.z - Dz, c0.w, c2, c3, c4, c5, order, bx, by, bz);
+                        accMultipoleF((c0.x - lh[0]) + (c1.x - pl[0]), (c0.y - lh[1]) + (c1.y - pl[1]),
+                            (c0.z - lh[2]) + (c1.z - pl[2]), c0.w, c2, c3, c4, c5, order, bx, by, bz);
                     }
                 }
                 if (inGroup) {
@@ -438,21 +435,13 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 8) evalListsKernel(const uint3
             }
         }
         // pairs inside the leaf
-        if (lane == 0) {
-            wc[3] += uint64_t(cnt) * (cnt - 1);
-        }
+        cPP += uint64_t(cnt) * (cnt - 1);
         if (inGroup) {
             float sx = 0.f, sy = 0.f, sz = 0.f;
             for (uint32_t t = from + grp; t < to; t += g) {
                 const float4 dj = pf[t];
-                const float mj = mf[t];
                 if (t != from + pid) {
-                    float gx, gy, gz;
-                    gravGradF(dj.x - di.x, dj.y - di.y, dj.z - di.z, 0.5f * (dj.w + di.w), lut, kernelRadius, gx, gy,
-                        gz);
-                    sx += mj * gx;
-                    sy += mj * gy;
-                    sz += mj * gz;
+                    gravAccF(dj.x - di.x, dj.y - di.y, dj.z - di.z, dj.w + di.w, mf[t], lut, rad2, sx, sy, sz);
                 }
             }
             ax.add(sx);
@@ -480,9 +469,11 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 8) evalListsKernel(const uint3
         }
         __syncwarp();
     }
-    __syncwarp();
-    if (lane < 4) {
-        atomicAdd(&stats[lane], wc[lane]);
+    if (lane == 0) {
+        atomicAdd(&stats[0], cN);
+        atomicAdd(&stats[1], cP);
+        atomicAdd(&stats[2], cPN);
+        atomicAdd(&stats[3], cPP);
     }
 }
 

@@ -184,11 +184,15 @@ __global__ void flagErrorKernel(uint32_t* devError, uint32_t bit) {
     atomicOr(devError, bit);
 }
 
-__global__ void __launch_bounds__(128) listLevelKernel(const BhNodeGeom* __restrict__ geom,
-    const float* __restrict__ nodef, uint32_t first, uint32_t last, int32_t* scratch, uint32_t cap,
-    int32_t* __restrict__ pool, uint32_t poolCap, const int32_t* __restrict__ keptIn, int32_t* __restrict__ keptOut,
-    uint32_t keptCap, uint32_t* __restrict__ meta, uint32_t* __restrict__ counters, int parity,
-    uint32_t* devError) {
+// Two passes per level: the first (deferPass == 0) runs every node of the level with
+// small per-warp staging lists and many warps; a node whose lists outgrow them is appended to the defer list and
+// left to the second pass (deferPass == 1), which runs only the deferred nodes with large staging lists. A node
+// that outgrows those too is a capacity error.
+__global__ void __launch_bounds__(128, 8) listLevelKernel(const BhNodeGeom* __restrict__ geom,
+    const float* __restrict__ nodef, uint32_t first, uint32_t last, int deferPass, uint32_t* __restrict__ defer,
+    int32_t* scratch, uint32_t cap, int32_t* __restrict__ pool, uint32_t poolCap,
+    const int32_t* __restrict__ keptIn, int32_t* __restrict__ keptOut, uint32_t keptCap, uint32_t* __restrict__ meta,
+    uint32_t* __restrict__ counters, int parity, uint32_t* devError) {
     __shared__ WalkFrame frameSh[4];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
@@ -200,7 +204,10 @@ __global__ void __launch_bounds__(128) listLevelKernel(const BhNodeGeom* __restr
     int32_t* lP = lN + cap;
     const float4* nf = reinterpret_cast<const float4*>(nodef);
     const float zero3[3] = { 0.f, 0.f, 0.f };
-    for (uint32_t ev = first + warpGlobal; ev < last; ev += nWarps) {
+    // counters[4]: the number of deferred nodes of this level
+    const uint32_t total = deferPass ? min(counters[4], last - first) : last - first;
+    for (uint32_t k = warpGlobal; k < total; k += nWarps) {
+        const uint32_t ev = deferPass ? defer[k] : first + k;
         const BhNodeGeom& eg = geom[ev];
         const int par = eg.parent;
         const int pl = geom[par].left;
@@ -272,6 +279,13 @@ __global__ void __launch_bounds__(128) listLevelKernel(const BhNodeGeom* __restr
             nN += __popc(mNode);
             nP += __popc(mPart);
             __syncwarp();
+        }
+        if (overflow && !deferPass) {
+            if (lane == 0) {
+                defer[atomicAdd(&counters[4], 1u)] = ev;
+            }
+            __syncwarp();
+            continue;
         }
         // space in the pools: the counters keep counting past the capacities, so that the host can grow the
         // pools to the need and build the lists again
@@ -501,10 +515,15 @@ void launchGravityWalkMixed(const DState& s, Tree& t, const Physics& ph, const f
         cudaMalloc(&t.nl_counters, 8 * sizeof(uint32_t));
         cudaMallocHost(&t.nl_host, 8 * sizeof(uint32_t));
     }
-    // per-warp staging of one node's lists in the walk scratch: 4 lists of NL_STAGE entries
-    constexpr uint32_t NL_STAGE = 16384;
-    const uint32_t listWarps =
-        std::max(1u, uint32_t(size_t(t.walk_warps) * 2 * t.walk_capacity / (4 * size_t(NL_STAGE))));
+    // per-warp staging of one node's lists in the walk scratch: 4 lists of NL_STAGE entries in the first pass
+    // of a level, of NL_STAGE_DEFER entries in the pass over the nodes deferred by the first
+    constexpr uint32_t NL_STAGE = 4096, NL_STAGE_DEFER = 16384;
+    const size_t scratchEntries = size_t(t.walk_warps) * 2 * t.walk_capacity;
+    const uint32_t listWarps = std::max(1u, uint32_t(scratchEntries / (4 * size_t(NL_STAGE))));
+    const uint32_t deferWarps = std::max(1u, uint32_t(scratchEntries / (4 * size_t(NL_STAGE_DEFER))));
+    if (!t.nl_defer) {
+        cudaMalloc(&t.nl_defer, size_t(t.node_capacity) * sizeof(uint32_t));
+    }
     uint32_t poolNeed = std::max<uint32_t>(1u << 20, 64u * t.node_count);
     uint32_t keptNeed = std::max<uint32_t>(1u << 20, 32u * t.node_count);
     const uint32_t levels = uint32_t(t.level_start.size());
@@ -534,11 +553,16 @@ void launchGravityWalkMixed(const DState& s, Tree& t, const Physics& ph, const f
             }
             const int parity = int(level & 1u);
             cudaMemsetAsync(t.nl_counters + 1 + parity, 0, sizeof(uint32_t), st);
+            cudaMemsetAsync(t.nl_counters + 4, 0, sizeof(uint32_t), st);
             const uint32_t warps = std::min(last - first, listWarps);
-            listLevelKernel<<<ceilDiv(warps, 4), 128, 0, st>>>(t.geom, t.nodef, first, last, t.walk_scratch, NL_STAGE,
-                t.nl_pool, t.nl_capacity, t.nl_kept[1 - parity], t.nl_kept[parity], t.nl_kept_capacity, t.nl_meta,
-                t.nl_counters, parity, devError);
-            t.walk_launches++;
+            listLevelKernel<<<ceilDiv(warps, 4), 128, 0, st>>>(t.geom, t.nodef, first, last, 0, t.nl_defer,
+                t.walk_scratch, NL_STAGE, t.nl_pool, t.nl_capacity, t.nl_kept[1 - parity], t.nl_kept[parity],
+                t.nl_kept_capacity, t.nl_meta, t.nl_counters, parity, devError);
+            const uint32_t dWarps = std::min(last - first, deferWarps);
+            listLevelKernel<<<ceilDiv(dWarps, 4), 128, 0, st>>>(t.geom, t.nodef, first, last, 1, t.nl_defer,
+                t.walk_scratch, NL_STAGE_DEFER, t.nl_pool, t.nl_capacity, t.nl_kept[1 - parity], t.nl_kept[parity],
+                t.nl_kept_capacity, t.nl_meta, t.nl_counters, parity, devError);
+            t.walk_launches += 2;
         }
         cudaMemcpyAsync(t.nl_host, t.nl_counters, 8 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
         if (cudaStreamSynchronize(st) != cudaSuccess) {

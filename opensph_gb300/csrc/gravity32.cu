@@ -329,6 +329,158 @@ __global__ void __launch_bounds__(128, 8) listLevelKernel(const BhNodeGeom* __re
     }
 }
 
+// The same classification with a CTA per node, for the levels with few nodes (the top of the tree, whose
+// inherited lists are long): each round classifies LB_THREADS queue entries, and block-wide prefix sums over the
+// warps' ballots place the outputs and the opened children in queue order. The queue is processed in order
+// whatever the round size (children are appended behind every entry of the round), so the lists are those of
+// listLevelKernel. Per-CTA staging of cap entries per list; outgrowing it is a capacity error.
+constexpr int LB_THREADS = 256;
+constexpr int LB_WARPS = LB_THREADS / 32;
+
+__global__ void __launch_bounds__(LB_THREADS, 4) listBlockKernel(const BhNodeGeom* __restrict__ geom,
+    const float* __restrict__ nodef, uint32_t first, uint32_t last, int32_t* scratch, uint32_t cap,
+    int32_t* __restrict__ pool, uint32_t poolCap, const int32_t* __restrict__ keptIn, int32_t* __restrict__ keptOut,
+    uint32_t keptCap, uint32_t* __restrict__ meta, uint32_t* __restrict__ counters, int parity,
+    uint32_t* devError) {
+    __shared__ WalkFrame fr;
+    __shared__ uint32_t warpCnt[LB_WARPS][4]; // per warp of a round: kept, opened, particle lists, nodes
+    __shared__ uint32_t baseSh[2];
+    const int tid = threadIdx.x;
+    const int lane = tid & 31;
+    const int w = tid >> 5;
+    int32_t* cur = scratch + size_t(blockIdx.x) * 4 * cap;
+    int32_t* kept = cur + cap;
+    int32_t* lN = kept + cap;
+    int32_t* lP = lN + cap;
+    const float4* nf = reinterpret_cast<const float4*>(nodef);
+    for (uint32_t ev = first + blockIdx.x; ev < last; ev += gridDim.x) {
+        const BhNodeGeom& eg = geom[ev];
+        const int par = eg.parent;
+        const int pl = geom[par].left;
+        const int sib = pl == int(ev) ? geom[par].right : pl;
+        const uint32_t kIn = meta[size_t(par) * NL_META + 5];
+        const uint32_t kOff = meta[size_t(par) * NL_META + 4];
+        bool overflow = kIn + 1 > cap;
+        uint32_t ncur = 0;
+        if (!overflow) {
+            for (uint32_t e = tid; e < kIn; e += LB_THREADS) {
+                cur[e] = keptIn[kOff + e];
+            }
+            ncur = kIn + 1;
+            if (tid == 0) {
+                cur[kIn] = sib;
+            }
+        }
+        float lh[3], ll[3];
+        {
+            const float4 a = nodeGroup(nf, int(ev), NF_COM_HI), b = nodeGroup(nf, int(ev), NF_COM_LO);
+            lh[0] = a.x, lh[1] = a.y, lh[2] = a.z;
+            ll[0] = b.x, ll[1] = b.y, ll[2] = b.z;
+        }
+        if (tid == 0) {
+            setFrame(fr, nf, int(ev), eg.left < 0, lh, ll);
+        }
+        __syncthreads();
+        uint32_t nK = 0, nN = 0, nP = 0;
+        uint32_t pos = 0;
+        while (pos < ncur && !overflow) {
+            const uint32_t batch = min(uint32_t(LB_THREADS), ncur - pos);
+            const bool valid = uint32_t(tid) < batch;
+            int node = -1, cls = CL_KEEP;
+            if (valid) {
+                node = cur[pos + tid];
+                cls = classifyEntry(node, geom, nf, fr, lh, ll);
+            }
+            const unsigned mKeep = __ballot_sync(0xffffffffu, valid && cls == CL_KEEP);
+            const unsigned mOpen = __ballot_sync(0xffffffffu, valid && cls == CL_OPEN);
+            const unsigned mPart = __ballot_sync(0xffffffffu, valid && cls == CL_PARTICLES);
+            const unsigned mNode = __ballot_sync(0xffffffffu, valid && cls == CL_NODE);
+            if (lane == 0) {
+                warpCnt[w][0] = __popc(mKeep);
+                warpCnt[w][1] = __popc(mOpen);
+                warpCnt[w][2] = __popc(mPart);
+                warpCnt[w][3] = __popc(mNode);
+            }
+            __syncthreads();
+            uint32_t pre[4] = { 0, 0, 0, 0 }, tot[4] = { 0, 0, 0, 0 };
+            for (int q = 0; q < LB_WARPS; ++q) {
+                for (int c = 0; c < 4; ++c) {
+                    const uint32_t v = warpCnt[q][c];
+                    pre[c] += q < w ? v : 0u;
+                    tot[c] += v;
+                }
+            }
+            const bool full = ncur + 2 * tot[1] > cap || nK + tot[0] > cap || nN + tot[3] > cap || nP + tot[2] > cap;
+            if (!full && valid) {
+                const unsigned below = (1u << lane) - 1u;
+                if (cls == CL_KEEP) {
+                    kept[nK + pre[0] + __popc(mKeep & below)] = node;
+                } else if (cls == CL_NODE) {
+                    lN[nN + pre[3] + __popc(mNode & below)] = node;
+                } else if (cls == CL_PARTICLES) {
+                    lP[nP + pre[2] + __popc(mPart & below)] = node;
+                } else {
+                    const uint32_t slot = ncur + 2 * (pre[1] + __popc(mOpen & below));
+                    const int2 ch = *reinterpret_cast<const int2*>(&geom[node].left);
+                    cur[slot] = ch.x;
+                    cur[slot + 1] = ch.y;
+                }
+            }
+            __syncthreads();
+            if (full) {
+                overflow = true;
+                break;
+            }
+            pos += batch;
+            ncur += 2 * tot[1];
+            nK += tot[0];
+            nN += tot[3];
+            nP += tot[2];
+        }
+        if (tid == 0) {
+            uint32_t base = 0, kbase = 0;
+            if (!overflow) {
+                base = atomicAdd(&counters[0], nN + nP);
+                kbase = nK ? atomicAdd(&counters[1 + parity], nK) : 0u;
+                atomicMax(&counters[3], kbase + nK);
+            }
+            baseSh[0] = base;
+            baseSh[1] = kbase;
+        }
+        __syncthreads();
+        const uint32_t base = baseSh[0], kbase = baseSh[1];
+        if (overflow || base + nN + nP > poolCap || kbase + nK > keptCap) {
+            if (tid == 0) {
+                if (overflow) {
+                    atomicOr(devError, uint32_t(DEV_ERR_WALK_CAPACITY));
+                }
+                uint32_t* m = meta + size_t(ev) * NL_META;
+                m[0] = m[1] = m[2] = m[3] = m[4] = m[5] = 0;
+            }
+        } else {
+            for (uint32_t e = tid; e < nN; e += LB_THREADS) {
+                pool[base + e] = lN[e];
+            }
+            for (uint32_t e = tid; e < nP; e += LB_THREADS) {
+                pool[base + nN + e] = lP[e];
+            }
+            for (uint32_t e = tid; e < nK; e += LB_THREADS) {
+                keptOut[kbase + e] = kept[e];
+            }
+            if (tid == 0) {
+                uint32_t* m = meta + size_t(ev) * NL_META;
+                m[0] = base;
+                m[1] = nN;
+                m[2] = base + nN;
+                m[3] = nP;
+                m[4] = kbase;
+                m[5] = nK;
+            }
+        }
+        __syncthreads();
+    }
+}
+
 __global__ void __launch_bounds__(WALK_THREADS_F, 8) evalListsKernel(const uint32_t* __restrict__ idx,
     const BhNodeGeom* __restrict__ geom, const float* __restrict__ nodef, const float4* __restrict__ pf,
     const float* __restrict__ mf, const uint32_t* __restrict__ leaves, uint32_t nLeaves,
@@ -553,6 +705,14 @@ void launchGravityWalkMixed(const DState& s, Tree& t, const Physics& ph, const f
             }
             const int parity = int(level & 1u);
             cudaMemsetAsync(t.nl_counters + 1 + parity, 0, sizeof(uint32_t), st);
+            if (last - first <= deferWarps) {
+                // few nodes: a CTA per node with the large staging lists
+                listBlockKernel<<<last - first, LB_THREADS, 0, st>>>(t.geom, t.nodef, first, last, t.walk_scratch,
+                    NL_STAGE_DEFER, t.nl_pool, t.nl_capacity, t.nl_kept[1 - parity], t.nl_kept[parity],
+                    t.nl_kept_capacity, t.nl_meta, t.nl_counters, parity, devError);
+                t.walk_launches++;
+                continue;
+            }
             cudaMemsetAsync(t.nl_counters + 4, 0, sizeof(uint32_t), st);
             const uint32_t warps = std::min(last - first, listWarps);
             listLevelKernel<<<ceilDiv(warps, 4), 128, 0, st>>>(t.geom, t.nodef, first, last, 0, t.nl_defer,

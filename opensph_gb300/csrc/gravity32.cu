@@ -486,15 +486,28 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 8) evalListsKernel(const uint3
     const float* __restrict__ mf, const uint32_t* __restrict__ leaves, uint32_t nLeaves,
     const float* __restrict__ lut, int kernelRadius, int order, const int32_t* __restrict__ pool,
     const uint32_t* __restrict__ meta, dbl4* agrav, unsigned long long* stats) {
-    __shared__ int32_t pathSh[WALK_THREADS_F / 32][MAX_PATH_F];
+    constexpr int W = WALK_THREADS_F / 32;
+    __shared__ int32_t pathSh[W][MAX_PATH_F];
+    // per warp: the node records of one batch of a node list ([record group][entry]), the source leaves of one
+    // batch of a particle list (centre relative to the leaf's hi centre + lo centre, particle range), and the
+    // particles of one source leaf
+    __shared__ float4 recSh[W][6][32];
+    __shared__ float4 srcSh[W][2][32];
+    __shared__ float4 partSh[W][32];
+    __shared__ float massSh[W][32];
+    // interaction counters of the warp: node lists, particle lists, particle-node and particle-particle evaluations
+    __shared__ unsigned long long countSh[W][4];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     int32_t* path = pathSh[wib];
     const float4* nf = reinterpret_cast<const float4*>(nodef);
     const float rad2 = float(kernelRadius) * float(kernelRadius);
-    // interaction counters (node lists, particle lists, particle-node and particle-particle evaluations), the
-    // same in every lane
-    unsigned long long cN = 0, cP = 0, cPN = 0, cPP = 0;
+    const int nRec = order >= 3 ? 6 : (order == 2 ? 4 : 2);
+    unsigned long long* wc = countSh[wib];
+    if (lane < 4) {
+        wc[lane] = 0;
+    }
+    __syncwarp();
     for (;;) {
         uint32_t li = 0;
         if (lane == 0) {
@@ -540,35 +553,49 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 8) evalListsKernel(const uint3
             pl[0] = b.x + di.x, pl[1] = b.y + di.y, pl[2] = b.z + di.z;
         }
         KahanF ax, ay, az;
+        // the leaf's list lengths and source particles (the same in every lane)
+        uint32_t leafN = 0, leafP = 0, leafSrc = 0;
         for (int k = 1; k <= depth; ++k) {
             const uint32_t* m = meta + size_t(path[k]) * NL_META;
             const uint32_t nOff = m[0], nLen = m[1], pOff = m[2], pLen = m[3];
-            cN += nLen;
-            cP += pLen;
-            cPN += uint64_t(cnt) * nLen;
+            leafN += nLen;
+            leafP += pLen;
             // particle lists of this level, then its nodes, 32 entries at a time
             for (uint32_t c = 0; c < pLen; c += 32) {
                 const uint32_t batch = min(32u, pLen - c);
-                const int node = uint32_t(lane) < batch ? pool[pOff + c + lane] : -1;
-                float bx = 0.f, by = 0.f, bz = 0.f;
-                unsigned mp = (batch == 32u) ? 0xffffffffu : ((1u << batch) - 1u);
-                while (mp) {
-                    const int src = __ffs(mp) - 1;
-                    mp &= mp - 1;
-                    const int pn = __shfl_sync(0xffffffffu, node, src);
+                if (uint32_t(lane) < batch) {
+                    const int pn = pool[pOff + c + lane];
                     const float4 a = nodeGroup(nf, pn, NF_COM_HI), b = nodeGroup(nf, pn, NF_COM_LO);
-                    // separation of the source leaf's centre from particle i
-                    const float ox = (a.x - lh[0]) + (b.x - pl[0]);
-                    const float oy = (a.y - lh[1]) + (b.y - pl[1]);
-                    const float oz = (a.z - lh[2]) + (b.z - pl[2]);
                     const uint2 range = *reinterpret_cast<const uint2*>(&geom[pn].from);
-                    cPP += uint64_t(cnt) * (range.y - range.x);
-                    if (inGroup) {
-#pragma unroll 2
-                        for (uint32_t t = range.x + grp; t < range.y; t += g) {
-                            const float4 dj = pf[t];
-                            gravAccF(ox + dj.x, oy + dj.y, oz + dj.z, dj.w + di.w, mf[t], lut, rad2, bx, by, bz);
+                    srcSh[wib][0][lane] = make_float4(a.x - lh[0], a.y - lh[1], a.z - lh[2], b.x);
+                    srcSh[wib][1][lane] = make_float4(b.y, b.z, __uint_as_float(range.x), __uint_as_float(range.y));
+                }
+                __syncwarp();
+                float bx = 0.f, by = 0.f, bz = 0.f;
+                for (uint32_t q = 0; q < batch; ++q) {
+                    const float4 s0 = srcSh[wib][0][q], s1 = srcSh[wib][1][q];
+                    // separation of the source leaf's centre from particle i
+                    const float ox = s0.x + (s0.w - pl[0]);
+                    const float oy = s0.y + (s1.x - pl[1]);
+                    const float oz = s0.z + (s1.y - pl[2]);
+                    const uint32_t r0 = __float_as_uint(s1.z), r1 = __float_as_uint(s1.w);
+                    leafSrc += r1 - r0;
+                    for (uint32_t base = r0; base < r1; base += 32) {
+                        const uint32_t ns = min(32u, r1 - base);
+                        if (uint32_t(lane) < ns) {
+                            partSh[wib][lane] = pf[base + lane];
+                            massSh[wib][lane] = mf[base + lane];
                         }
+                        __syncwarp();
+                        if (inGroup) {
+#pragma unroll 2
+                            for (uint32_t t = grp; t < ns; t += g) {
+                                const float4 dj = partSh[wib][t];
+                                gravAccF(ox + dj.x, oy + dj.y, oz + dj.z, dj.w + di.w, massSh[wib][t], lut, rad2, bx,
+                                    by, bz);
+                            }
+                        }
+                        __syncwarp();
                     }
                 }
                 if (inGroup) {
@@ -579,20 +606,30 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 8) evalListsKernel(const uint3
             }
             for (uint32_t c = 0; c < nLen; c += 32) {
                 const uint32_t batch = min(32u, nLen - c);
-                const int node = uint32_t(lane) < batch ? pool[nOff + c + lane] : -1;
+                if (uint32_t(lane) < batch) {
+                    const int nn = pool[nOff + c + lane];
+                    // record groups 0..5: centre hi, centre lo, reduced moments
+#pragma unroll
+                    for (int r = 0; r < 6; ++r) {
+                        if (r < nRec) {
+                            recSh[wib][r][lane] = nodeGroup(nf, nn, r);
+                        }
+                    }
+                }
+                __syncwarp();
                 float bx = 0.f, by = 0.f, bz = 0.f;
                 // rounds of g nodes, node q of a round to lane group q
                 for (uint32_t q0 = 0; q0 < batch; q0 += g) {
                     const uint32_t q = q0 + grp;
-                    const int nn = __shfl_sync(0xffffffffu, node, int(min(q, 31u)));
                     if (inGroup && q < batch) {
-                        const float4 c0 = nodeGroup(nf, nn, NF_COM_HI), c1 = nodeGroup(nf, nn, NF_COM_LO);
-                        const float4 c2 = nodeGroup(nf, nn, NF_MOM), c3 = nodeGroup(nf, nn, NF_MOM + 1);
-                        const float4 c4 = nodeGroup(nf, nn, NF_MOM + 2), c5 = nodeGroup(nf, nn, NF_MOM + 3);
+                        const float4 c0 = recSh[wib][0][q], c1 = recSh[wib][1][q];
+                        const float4 c2 = recSh[wib][2][q], c3 = recSh[wib][3][q];
+                        const float4 c4 = recSh[wib][4][q], c5 = recSh[wib][5][q];
                         accMultipoleF((c0.x - lh[0]) + (c1.x - pl[0]), (c0.y - lh[1]) + (c1.y - pl[1]),
                             (c0.z - lh[2]) + (c1.z - pl[2]), c0.w, c2, c3, c4, c5, order, bx, by, bz);
                     }
                 }
+                __syncwarp();
                 if (inGroup) {
                     ax.add(bx);
                     ay.add(by);
@@ -600,8 +637,13 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 8) evalListsKernel(const uint3
                 }
             }
         }
+        if (lane == 0) {
+            wc[0] += leafN;
+            wc[1] += leafP;
+            wc[2] += uint64_t(cnt) * leafN;
+            wc[3] += uint64_t(cnt) * (leafSrc + cnt - 1);
+        }
         // pairs inside the leaf
-        cPP += uint64_t(cnt) * (cnt - 1);
         if (inGroup) {
             float sx = 0.f, sy = 0.f, sz = 0.f;
             for (uint32_t t = from + grp; t < to; t += g) {
@@ -635,11 +677,9 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 8) evalListsKernel(const uint3
         }
         __syncwarp();
     }
-    if (lane == 0) {
-        atomicAdd(&stats[0], cN);
-        atomicAdd(&stats[1], cP);
-        atomicAdd(&stats[2], cPN);
-        atomicAdd(&stats[3], cPP);
+    __syncwarp();
+    if (lane < 4) {
+        atomicAdd(&stats[lane], wc[lane]);
     }
 }
 
@@ -739,6 +779,9 @@ void launchGravityWalkMixed(const DState& s, Tree& t, const Physics& ph, const f
     static int residentBlocks = 0;
     if (residentBlocks == 0) {
         int perSm = 0, sms = 0;
+        // the staging buffers of eight resident blocks need most of the unified L1 / shared memory
+        cudaFuncSetAttribute(evalListsKernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+            int(cudaSharedmemCarveoutMaxShared));
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, evalListsKernel, WALK_THREADS_F, 0);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
         residentBlocks = std::max(1, perSm * sms);

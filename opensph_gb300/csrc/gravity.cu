@@ -594,10 +594,14 @@ __device__ __forceinline__ void warpArgExtreme(unsigned long long& val, uint32_t
     }
 }
 
+// nInDev: when not null, the segment count of the level is read from the device (batched deep levels)
 __global__ void __launch_bounds__(SPLIT_WARP_THREADS) splitWarpKernel(PosView pv, uint32_t* idx, uint32_t* posB,
-    uint32_t* posS, const BhSegment* segIn, uint32_t nIn, BhSegment* segOut, BhNodeGeom* geom, uint32_t* counters,
-    uint32_t* leaves, uint32_t leafSize, uint32_t nodeCapacity, uint32_t segCapacity, uint32_t* devError,
-    uint32_t maxSize) {
+    uint32_t* posS, const BhSegment* segIn, uint32_t nIn, const uint32_t* nInDev, BhSegment* segOut,
+    BhNodeGeom* geom, uint32_t* counters, uint32_t* leaves, uint32_t leafSize, uint32_t nodeCapacity,
+    uint32_t segCapacity, uint32_t* devError, uint32_t maxSize) {
+    if (nInDev) {
+        nIn = *nInDev;
+    }
     const int lane = threadIdx.x & 31;
     const uint32_t warpGlobal = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nWarps = (gridDim.x * blockDim.x) >> 5;
@@ -840,6 +844,19 @@ __global__ void chunkListKernel(const BhSegment* __restrict__ segIn, uint32_t nI
 __device__ __forceinline__ bool betterArg(unsigned long long v, uint32_t p, unsigned long long bv, uint32_t bp,
     bool isMax) {
     return isMax ? (v > bv || (v == bv && p < bp)) : (v < bv || (v == bv && p < bp));
+}
+
+// End of a batched deep level: the node count at the start of the next level and its segment count go to
+// levelInfo[next] (2 words each), and the per-level counters are cleared. One thread.
+__global__ void levelEndKernel(uint32_t* counters, uint32_t* levelInfo, uint32_t next) {
+    levelInfo[2 * next] = counters[0];
+    levelInfo[2 * next + 1] = counters[1];
+    counters[1] = 0;
+    counters[4] = 0;
+}
+
+__global__ void setWordKernel(uint32_t* p, uint32_t v) {
+    *p = v;
 }
 
 __global__ void __launch_bounds__(BUILD_THREADS) chunkStatsKernel(PosView pv, const uint32_t* __restrict__ idx,
@@ -1669,6 +1686,7 @@ cudaError_t treeAllocate(Tree& t, uint32_t n, uint32_t leafSize) {
     alloc((void**)&t.seg[0], size_t(t.seg_capacity) * sizeof(BhSegment));
     alloc((void**)&t.seg[1], size_t(t.seg_capacity) * sizeof(BhSegment));
     alloc((void**)&t.counters, 8 * sizeof(uint32_t));
+    alloc((void**)&t.level_info, 64 * sizeof(uint32_t));
     alloc((void**)&t.leaves, nn * sizeof(uint32_t));
     alloc((void**)&t.visits, size_t(t.node_capacity) * sizeof(uint32_t));
     alloc((void**)&t.walk_scratch, size_t(t.walk_warps) * 2 * t.walk_capacity * sizeof(int32_t));
@@ -1686,13 +1704,16 @@ cudaError_t treeAllocate(Tree& t, uint32_t n, uint32_t leafSize) {
     if (e == cudaSuccess) {
         e = cudaMallocHost((void**)&t.counters_host, 8 * sizeof(uint32_t));
     }
+    if (e == cudaSuccess) {
+        e = cudaMallocHost((void**)&t.level_host, 64 * sizeof(uint32_t));
+    }
     return e;
 }
 
 void treeFree(Tree& t) {
     void* ptrs[] = { t.idx, t.scratch_b, t.scratch_s, t.geom, t.mom, t.seg[0], t.seg[1], t.counters, t.leaves, t.visits,
         t.walk_scratch, t.nl_pool, t.nl_kept[0], t.nl_kept[1], t.nl_meta, t.nl_counters, t.nl_defer, t.stats, t.bbox,
-        t.nodef, t.pf, t.mf, t.chunks, t.chunk_stats, t.chunk_off_b, t.chunk_off_s, t.work };
+        t.nodef, t.pf, t.mf, t.chunks, t.chunk_stats, t.chunk_off_b, t.chunk_off_s, t.work, t.level_info };
     for (void* p : ptrs) {
         if (p) {
             cudaFree(p);
@@ -1703,6 +1724,9 @@ void treeFree(Tree& t) {
     }
     if (t.nl_host) {
         cudaFreeHost(t.nl_host);
+    }
+    if (t.level_host) {
+        cudaFreeHost(t.level_host);
     }
     t = Tree();
 }
@@ -1772,8 +1796,8 @@ cudaError_t treeBuild(const DState& s, Tree& t, const Physics& ph, uint32_t* dev
         }
         const uint32_t warpBlocks = min(uint32_t(ceilDiv(nIn, SPLIT_WARP_THREADS / 32)), 152u * 8u);
         splitWarpKernel<<<warpBlocks, SPLIT_WARP_THREADS, 0, st>>>(pv, t.idx, t.scratch_b, t.scratch_s, t.seg[cur],
-            nIn, t.seg[1 - cur], t.geom, t.counters, t.leaves, ph.leaf_size, t.node_capacity, t.seg_capacity,
-            devError, WARP_SEGMENT);
+            nIn, nullptr, t.seg[1 - cur], t.geom, t.counters, t.leaves, ph.leaf_size, t.node_capacity,
+            t.seg_capacity, devError, WARP_SEGMENT);
         t.launches++;
         if (big) {
             cudaMemcpyAsync(t.counters_host, t.counters, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
@@ -1813,6 +1837,45 @@ cudaError_t treeBuild(const DState& s, Tree& t, const Physics& ph, uint32_t* dev
         cur = 1 - cur;
         if (level > 100000) {
             break;
+        }
+        if (nIn > 0 && maxSeg <= WARP_SEGMENT) {
+            // every remaining segment is split by warps (segments only shrink): LEVEL_BATCH levels per host
+            // round trip, the segment counts read by the kernels from levelInfo
+            constexpr uint32_t LEVEL_BATCH = 8;
+            setWordKernel<<<1, 1, 0, st>>>(t.level_info + 1, nIn);
+            t.launches++;
+            while (nIn > 0) {
+                for (uint32_t b = 0; b < LEVEL_BATCH; ++b) {
+                    splitWarpKernel<<<152u * 8u, SPLIT_WARP_THREADS, 0, st>>>(pv, t.idx, t.scratch_b, t.scratch_s,
+                        t.seg[cur], 0, t.level_info + 2 * b + 1, t.seg[1 - cur], t.geom, t.counters, t.leaves,
+                        ph.leaf_size, t.node_capacity, t.seg_capacity, devError, WARP_SEGMENT);
+                    levelEndKernel<<<1, 1, 0, st>>>(t.counters, t.level_info, b + 1);
+                    cur = 1 - cur;
+                }
+                t.launches += 2 * LEVEL_BATCH;
+                cudaMemcpyAsync(t.level_host, t.level_info, 2 * (LEVEL_BATCH + 1) * sizeof(uint32_t),
+                    cudaMemcpyDeviceToHost, st);
+                cudaMemcpyAsync(t.counters_host, t.counters, 5 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+                // the next batch starts from the last level's segment count
+                cudaMemcpyAsync(t.level_info + 1, t.level_info + 2 * LEVEL_BATCH + 1, sizeof(uint32_t),
+                    cudaMemcpyDeviceToDevice, st);
+                e = cudaStreamSynchronize(st);
+                if (e != cudaSuccess) {
+                    return e;
+                }
+                for (uint32_t b = 1; b <= LEVEL_BATCH; ++b) {
+                    if (t.level_host[2 * b + 1] > 0) {
+                        t.level_start.push_back(t.level_host[2 * b]);
+                    }
+                }
+                nIn = t.level_host[2 * LEVEL_BATCH + 1];
+                t.node_count = t.counters_host[0];
+                t.leaf_count = t.counters_host[2];
+                level += int(LEVEL_BATCH);
+                if (level > 100000) {
+                    break;
+                }
+            }
         }
     }
     // moments, bottom-up in one launch

@@ -239,6 +239,8 @@ struct Tree {
     BhSegment* seg[2] = { nullptr, nullptr };
     uint32_t* counters = nullptr;     // device: [0] node count, [1] next-level segment count, [2] leaf count
     uint32_t* counters_host = nullptr; // pinned mirror
+    uint32_t* level_info = nullptr;   // device: per batched deep level, node count at its start and segment count
+    uint32_t* level_host = nullptr;   // pinned mirror of level_info
     uint32_t* leaves = nullptr;       // leaf node ids
     uint32_t* visits = nullptr;       // per node: children finished (bottom-up moments)
     int32_t* walk_scratch = nullptr;  // per-warp checklists

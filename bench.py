@@ -292,10 +292,10 @@ def compare_fp64(args, st, mats, n, mixed_cfg, dev):
 
 # DRAM bytes (read + write) of one mixed walk of the default workload (the evaluation launch plus the launches
 # that build the interaction lists), from the ncu capture summarised in profiles/evalListsKernel_impact1M.md
-WALK_TRAFFIC_BYTES = (266.2 + 29.8 + 176.8 + 47.2) * 1e6
+WALK_TRAFFIC_BYTES = (277.7 + 35.1 + 175.4 + 76.1 + 15.2) * 1e6
 WALK_TRAFFIC_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, profiles/evalListsKernel_impact1M.md"
 
-# FP32 operations of one particle-multipole evaluation (evalMultipoleF, csrc/gravity32.cu: octupole) and the
+# FP32 operations of one particle-multipole evaluation (accMultipoleF, csrc/gravity32.cu: octupole) and the
 # N-body convention for one softened particle-particle interaction
 FLOP_PN = 120
 FLOP_PP = 20

@@ -181,28 +181,30 @@ __device__ __forceinline__ bool acceptMerge(const Merger& g, const dbl4& ri, con
     return !(omegaSqr * rotationLimit > omegaCritSqr);
 }
 
-// mutable view of the particle state used by the handlers
-struct Parts {
-    dbl4* r;
-    dbl4* v;
-    double* m;
-    dbl4* w;
-    uint32_t* removed;
+// The two particles of a collision, copied out of the state arrays for the handlers and written back after
+// them (the handlers' arithmetic on the copies is the same as on the arrays)
+struct PairState {
+    dbl4 ri, rj, vi, vj, wi, wj;
+    double mi, mj;
+    uint32_t removedJ;
 };
 
-// MergingCollisionHandler::collide (Collision.h:160-243)
-__device__ int mergeCollide(Parts& P, uint32_t i, uint32_t j, double bounceLimit, double rotationLimit) {
-    const dbl4 ri = P.r[i], rj = P.r[j], vi = P.v[i], vj = P.v[j];
-    const double mi = P.m[i], mj = P.m[j];
-    const Merger g = mergerOf(ri, vi, mi, P.w[i], rj, vj, mj, P.w[j]);
-    if (!acceptMerge(g, ri, vi, mi, rj, vj, mj, bounceLimit, rotationLimit)) {
+// MergingCollisionHandler::collide (Collision.h:160-243). acceptMerge tests boundness first and needs the merger
+// only for the rotation limit, so the merger is formed after that test (it has no side effects).
+__device__ int mergeCollide(PairState& S, double bounceLimit, double rotationLimit) {
+    if (!particlesBound(S.mi + S.mj, S.ri.w + S.rj.w, sub4(S.vi, S.vj), bounceLimit)) {
         return RES_NONE;
     }
-    P.m[i] = g.m;
-    P.r[i] = mkd4(g.r.x, g.r.y, g.r.z, g.h);
-    P.v[i] = mkd4(g.v.x, g.v.y, g.v.z, 0.);
-    P.w[i] = g.w;
-    P.removed[j] = 1;
+    const Merger g = mergerOf(S.ri, S.vi, S.mi, S.wi, S.rj, S.vj, S.mj, S.wj);
+    const double omegaCritSqr = G_PHYS * (S.mi + S.mj) / pow3(g.h);
+    if (len2(g.w) * rotationLimit > omegaCritSqr) {
+        return RES_NONE;
+    }
+    S.mi = g.m;
+    S.ri = mkd4(g.r.x, g.r.y, g.r.z, g.h);
+    S.vi = mkd4(g.v.x, g.v.y, g.v.z, 0.);
+    S.wi = g.w;
+    S.removedJ = 1;
     return RES_MERGER;
 }
 
@@ -216,67 +218,65 @@ __device__ __forceinline__ dbl4 reflect(const dbl4& v, const dbl4& vCom, const d
 }
 
 // ElasticBounceHandler::collide (Collision.h:301-313)
-__device__ int bounceCollide(Parts& P, uint32_t i, uint32_t j, double rn, double rt) {
-    const dbl4 d = sub4(P.r[i], P.r[j]);
+__device__ int bounceCollide(PairState& S, double rn, double rt) {
+    const dbl4 d = sub4(S.ri, S.rj);
     const dbl4 dr = div4(d, sqrt(len2(d)));
     const dbl4 ndr = mkd4(-dr.x, -dr.y, -dr.z, -dr.w);
-    const double mi = P.m[i], mj = P.m[j];
-    const dbl4 vCom = weightedAverage(P.v[i], mi, P.v[j], mj);
-    const dbl4 vi = reflect(P.v[i], vCom, ndr, rn, rt);
-    const dbl4 vj = reflect(P.v[j], vCom, dr, rn, rt);
-    P.v[i] = mkd4(vi.x, vi.y, vi.z, 0.);
-    P.v[j] = mkd4(vj.x, vj.y, vj.z, 0.);
+    const dbl4 vCom = weightedAverage(S.vi, S.mi, S.vj, S.mj);
+    const dbl4 vi = reflect(S.vi, vCom, ndr, rn, rt);
+    const dbl4 vj = reflect(S.vj, vCom, dr, rn, rt);
+    S.vi = mkd4(vi.x, vi.y, vi.z, 0.);
+    S.vj = mkd4(vj.x, vj.y, vj.z, 0.);
     return RES_BOUNCE;
 }
 
 // the collision handler of Factory::getCollisionHandler (core/system/Factory.cpp:415-429)
-__device__ int collisionHandler(Parts& P, const CollideParams& p, uint32_t i, uint32_t j) {
+__device__ int collisionHandler(PairState& S, const CollideParams& p) {
     switch (p.handler) {
     case SPHGPU_COLLISION_PERFECT_MERGING:
-        return mergeCollide(P, i, j, 0., 0.);
+        return mergeCollide(S, 0., 0.);
     case SPHGPU_COLLISION_ELASTIC_BOUNCE:
-        return bounceCollide(P, i, j, p.rest_n, p.rest_t);
+        return bounceCollide(S, p.rest_n, p.rest_t);
     default: { // MERGE_OR_BOUNCE: FallbackHandler<MergingCollisionHandler, ElasticBounceHandler>
-        const int res = mergeCollide(P, i, j, p.bounce_limit, p.rotation_limit);
-        return res != RES_NONE ? res : bounceCollide(P, i, j, p.rest_n, p.rest_t);
+        const int res = mergeCollide(S, p.bounce_limit, p.rotation_limit);
+        return res != RES_NONE ? res : bounceCollide(S, p.rest_n, p.rest_t);
     }
     }
 }
 
 // RepelHandler::handle before its follow-up handler (Collision.h:443-467)
-__device__ void repel(Parts& P, uint32_t i, uint32_t j) {
-    const dbl4 d = sub4(P.r[i], P.r[j]);
+__device__ void repel(PairState& S) {
+    const dbl4 d = sub4(S.ri, S.rj);
     const double dist = sqrt(len2(d));
     dbl4 dir = div4(d, dist);
     dir.w = 0.;
-    const double mi = P.m[i], mj = P.m[j];
-    const double x1 = (P.r[i].w + P.r[j].w - dist) / (1. + mi / mj);
-    const double x2 = mi / mj * x1;
-    P.r[i] = add4(P.r[i], mul4(dir, x1));
-    P.r[j] = sub4(P.r[j], mul4(dir, x2));
+    const double x1 = (S.ri.w + S.rj.w - dist) / (1. + S.mi / S.mj);
+    const double x2 = S.mi / S.mj * x1;
+    S.ri = add4(S.ri, mul4(dir, x1));
+    S.rj = sub4(S.rj, mul4(dir, x2));
 }
 
 // IOverlapHandler::handle of Factory::getOverlapHandler (core/system/Factory.cpp:431-450, Collision.h:372-567)
-__device__ void overlapHandle(Parts& P, const CollideParams& p, uint32_t i, uint32_t j) {
+__device__ void overlapHandle(PairState& S, const CollideParams& p) {
     switch (p.overlap) {
     case SPHGPU_OVERLAP_FORCE_MERGE:
-        mergeCollide(P, i, j, 0., 0.);
+        mergeCollide(S, 0., 0.);
         break;
     case SPHGPU_OVERLAP_REPEL:
-        repel(P, i, j);
-        bounceCollide(P, i, j, p.rest_n, p.rest_t);
+        repel(S);
+        bounceCollide(S, p.rest_n, p.rest_t);
         break;
     case SPHGPU_OVERLAP_REPEL_OR_MERGE:
-        repel(P, i, j);
-        if (mergeCollide(P, i, j, p.bounce_limit, p.rotation_limit) == RES_NONE) {
-            bounceCollide(P, i, j, p.rest_n, p.rest_t);
+        repel(S);
+        if (mergeCollide(S, p.bounce_limit, p.rotation_limit) == RES_NONE) {
+            bounceCollide(S, p.rest_n, p.rest_t);
         }
         break;
     case SPHGPU_OVERLAP_INTERNAL_BOUNCE:
-        bounceCollide(P, i, j, p.rest_n, p.rest_t);
+        bounceCollide(S, p.rest_n, p.rest_t);
         break;
     case SPHGPU_OVERLAP_PASS_OR_MERGE:
-        mergeCollide(P, i, j, p.bounce_limit, p.rotation_limit);
+        mergeCollide(S, p.bounce_limit, p.rotation_limit);
         break;
     default:
         break;
@@ -814,7 +814,6 @@ __global__ void __launch_bounds__(EV_THREADS, 1) eventKernel(DState s, Grid g, E
     // leader-only state
     uint32_t cursor = 0, poolNext = s.n, extraUsed = 0, removedCount = 0;
     unsigned long long nColl = 0, nMerge = 0, nBounce = 0, nOverlap = 0, nEvents = 0, err = 0;
-    Parts P{ s.r, s.v, s.m, s.omega, a.removed };
     if (tid == 0) {
         sh.heapSize = 0;
     }
@@ -854,17 +853,18 @@ __global__ void __launch_bounds__(EV_THREADS, 1) eventKernel(DState s, Grid g, E
                 const uint32_t i = rec.i, j = rec.j;
                 const double tColl = rec.t;
                 // advance the pair to the collision, resolve it, move back along the new velocities
-                P.r[i] = add4(P.r[i], mul4(P.v[i], tColl));
-                P.r[j] = add4(P.r[j], mul4(P.v[j], tColl));
+                PairState S{ s.r[i], s.r[j], s.v[i], s.v[j], s.omega[i], s.omega[j], s.m[i], s.m[j], a.removed[j] };
+                S.ri = add4(S.ri, mul4(S.vi, tColl));
+                S.rj = add4(S.rj, mul4(S.vj, tColl));
                 int result;
                 if (rec.nov < 0.) {
-                    const uint32_t before = a.removed[j];
-                    overlapHandle(P, p, i, j);
-                    removedCount += a.removed[j] - before;
+                    const uint32_t before = S.removedJ;
+                    overlapHandle(S, p);
+                    removedCount += S.removedJ - before;
                     result = RES_BOUNCE;
                     ++nOverlap;
                 } else {
-                    result = collisionHandler(P, p, i, j);
+                    result = collisionHandler(S, p);
                     ++nColl;
                     if (result == RES_MERGER) {
                         ++nMerge;
@@ -873,8 +873,17 @@ __global__ void __launch_bounds__(EV_THREADS, 1) eventKernel(DState s, Grid g, E
                         ++nBounce;
                     }
                 }
-                P.r[i] = sub4(P.r[i], mul4(P.v[i], tColl));
-                P.r[j] = sub4(P.r[j], mul4(P.v[j], tColl));
+                S.ri = sub4(S.ri, mul4(S.vi, tColl));
+                S.rj = sub4(S.rj, mul4(S.vj, tColl));
+                s.r[i] = S.ri;
+                s.r[j] = S.rj;
+                s.v[i] = S.vi;
+                s.v[j] = S.vj;
+                s.omega[i] = S.wi;
+                s.omega[j] = S.wj;
+                s.m[i] = S.mi;
+                s.m[j] = S.mj;
+                a.removed[j] = S.removedJ;
                 if (result == RES_NONE) {
                     rec.dead = 1;
                 } else {
@@ -889,8 +898,8 @@ __global__ void __launch_bounds__(EV_THREADS, 1) eventKernel(DState s, Grid g, E
                     a.ver[j] += 1;
                     a.bounces[i] += 1;
                     a.bounces[j] += 1;
-                    if (!listMoved(a, gi, P.r[i], i, extraUsed) ||
-                        (!a.removed[j] && !listMoved(a, gi, P.r[j], j, extraUsed))) {
+                    if (!listMoved(a, gi, S.ri, i, extraUsed) ||
+                        (!S.removedJ && !listMoved(a, gi, S.rj, j, extraUsed))) {
                         err |= COLL_ERR_EXTRA;
                     }
                     sh.evI = i;

@@ -153,7 +153,7 @@ __device__ __forceinline__ bool particlesBound(double mSum, double hSum, const d
 }
 
 // The would-be merger of i and j (MergingCollisionHandler::collide without the inertia tensor,
-// Collision.h:160-215) and its acceptance (acceptMerge, :249-261)
+// Collision.h:160-215); its acceptance (acceptMerge, :249-261) is tested in mergeCollide
 struct Merger {
     double h, m;
     dbl4 r, v, w;
@@ -171,16 +171,6 @@ __device__ Merger mergerOf(const dbl4& ri, const dbl4& vi, double mi, const dbl4
     g.w = symMul(symInverse(sphereInertia(g.m, g.h)), L);
     return g;
 }
-__device__ __forceinline__ bool acceptMerge(const Merger& g, const dbl4& ri, const dbl4& vi, double mi,
-    const dbl4& rj, const dbl4& vj, double mj, double bounceLimit, double rotationLimit) {
-    if (!particlesBound(mi + mj, ri.w + rj.w, sub4(vi, vj), bounceLimit)) {
-        return false;
-    }
-    const double omegaCritSqr = G_PHYS * (mi + mj) / pow3(g.h);
-    const double omegaSqr = len2(g.w);
-    return !(omegaSqr * rotationLimit > omegaCritSqr);
-}
-
 // The two particles of a collision, copied out of the state arrays for the handlers and written back after
 // them (the handlers' arithmetic on the copies is the same as on the arrays)
 struct PairState {
@@ -596,7 +586,7 @@ __global__ void linkKernel(CollRec* pool, const uint32_t* __restrict__ order, ui
 
 // ---- 3. the collision loop (NBodySolver.cpp:401-477) ------------------------------------------------------------
 
-constexpr int EV_THREADS = 128;
+constexpr int EV_THREADS = 256;
 constexpr int EV_WARPS = EV_THREADS / 32;
 constexpr int HEAP_CAP = 3072; // records made by re-searches and not yet processed
 constexpr int INV_CAP = 256;   // particles of the records invalidated by one collision
@@ -765,11 +755,10 @@ __device__ Cand researchWarp(const DState& s, const Grid& g, const GridInfo& gi,
     cellSpan(ri.x, radius, gi.lo[0], gi.inv_cell, gi.dims[0], x0, x1);
     cellSpan(ri.y, radius, gi.lo[1], gi.inv_cell, gi.dims[1], y0, y1);
     cellSpan(ri.z, radius, gi.lo[2], gi.inv_cell, gi.dims[2], z0, z1);
-    auto consider = [&](uint32_t j) {
+    auto consider = [&](uint32_t j, const dbl4& rj) {
         if (j == idx) {
             return;
         }
-        const dbl4 rj = s.r[j];
         if (!(len2(sub4(rj, ri)) < radiusSqr)) {
             return;
         }
@@ -782,7 +771,8 @@ __device__ Cand researchWarp(const DState& s, const Grid& g, const GridInfo& gi,
         }
     };
     // the lanes take the cells of the box (a cell holds a few particles; the latency of the cell ranges is
-    // paid once per 32 cells instead of once per cell)
+    // paid once per 32 cells instead of once per cell); within a cell the next particle's index and position
+    // are loaded while the current one is evaluated
     const int nx = x1 - x0 + 1, ny = y1 - y0 + 1;
     const int ncell = nx * ny * (z1 - z0 + 1);
     for (int b = lane; b < ncell; b += 32) {
@@ -791,11 +781,25 @@ __device__ Cand researchWarp(const DState& s, const Grid& g, const GridInfo& gi,
         const int z = z0 + b / (nx * ny);
         const uint32_t cell = (uint32_t(z) * uint32_t(gi.dims[1]) + uint32_t(y)) * uint32_t(gi.dims[0]) + uint32_t(x);
         const uint32_t end = g.cell_end[cell];
-        for (uint32_t q = g.cell_start[cell]; q < end; ++q) {
-            consider(g.perm[q]);
+        uint32_t q = g.cell_start[cell];
+        uint32_t jn = 0;
+        dbl4 rn = mkd4(0., 0., 0., 0.);
+        if (q < end) {
+            jn = g.perm[q];
+            rn = s.r[jn];
+        }
+        while (q < end) {
+            const uint32_t j = jn;
+            const dbl4 rj = rn;
+            if (++q < end) {
+                jn = g.perm[q];
+                rn = s.r[jn];
+            }
+            consider(j, rj);
         }
         for (int32_t e = a.extraHead[cell]; e >= 0; e = a.extra[3 * e + 1]) {
-            consider(uint32_t(a.extra[3 * e]));
+            const uint32_t j = uint32_t(a.extra[3 * e]);
+            consider(j, s.r[j]);
         }
     }
     candShflMin(best);

@@ -216,8 +216,9 @@ def run_gpu(args, rank, world):
         g._check(lib.sphgpu_get_quantity(hnd, abi.Q_POSITION, 1, outs["v"].data_ptr(), n))
         g._check(lib.sphgpu_get_quantity(hnd, abi.Q_DENSITY, 0, outs["rho"].data_ptr(), n))
         g._check(lib.sphgpu_get_quantity(hnd, abi.Q_ENERGY, 0, outs["u"].data_ptr(), n))
-        pinned["r"].copy_(outs["r"])
-        pinned["v"].copy_(outs["v"])
+        # the state read back is the next step's input (the pinned buffers swap roles)
+        pinned["r"], outs["r"] = outs["r"], pinned["r"]
+        pinned["v"], outs["v"] = outs["v"], pinned["v"]
     e2e_end.record(stream)
     e2e_end.synchronize()
     e2e_wall = time.perf_counter() - t0
@@ -369,6 +370,7 @@ def reaccumulation(args, dev):
         stats0 = g.collision_stats()
         g.set_profiling(True)
         g.phase_times()
+        prof0 = g.collision_profile()
         stream = torch.cuda.ExternalStream(g.stream)
         torch.cuda.synchronize()
         start = torch.cuda.Event(enable_timing=True)
@@ -380,6 +382,7 @@ def reaccumulation(args, dev):
         ms = start.elapsed_time(end)
         phases, launches = g.phase_times()
         stats1 = g.collision_stats()
+        prof1 = g.collision_profile()
         n_end = g.n
         dt_end = g.timestep
     events = [(b - a) / args.steps for a, b in zip(stats0, stats1)]
@@ -389,6 +392,13 @@ def reaccumulation(args, dev):
                                "overlaps": events[3]},
            "phases_ms_per_step": {k: v / args.steps for k, v in phases.items() if v > 0},
            "gpu_launches": launches, "timestep_after": dt_end}
+    # SM cycles of the collision loop per processed record: serial part (selection, handler, invalidation),
+    # re-searches, insertion of the new records (sphgpu_collision_profile)
+    rec = prof1[0] - prof0[0]
+    if rec > 0:
+        out["collision_loop"] = {"records": rec, "cycles_per_record": {
+            "serial": (prof1[1] - prof0[1]) / rec, "research": (prof1[2] - prof0[2]) / rec,
+            "insert": (prof1[3] - prof0[3]) / rec}}
     if not args.no_cpu:
         work = initial.rubble_cloud(n, radius, inflow=2e-4, sigma=0.1)
         cfg64, keep64 = abi.make_nbody_config(n, max_timestep=100.0, initial_timestep=100.0)

@@ -30,23 +30,29 @@ __device__ void eosEval(const MaterialD& mt, double rho, double u, double& p, do
     double dpdu = a * rho + b * rho / (denom * denom);
     double dpdrho = a * u + b * u * (3. * denom - 2.) / (denom * denom) + A / rho0 + 2. * B * mu / rho0;
     const double csc = dpdrho + dpdu * pc / (rho * rho);
-    const double rhoExp = rho0 / rho - 1.;
-    const double betaExp = exp(-fmin(beta * rhoExp, 70.));
-    const double alphaExp = exp(-fmin(alpha * (rhoExp * rhoExp), 70.));
-    const double pe = a * rho * u + (b * rho * u / denom + A * mu * betaExp) * alphaExp;
-    dpdu = a * rho + alphaExp * b * rho / (denom * denom);
-    dpdrho = a * u + alphaExp * (b * u * (3. * denom - 2.) / (denom * denom)) +
-             alphaExp * (b * u * rho / denom) * rho0 * (2. * alpha * rhoExp) / (rho * rho) +
-             alphaExp * A * betaExp * (1. / rho0 + rho0 * mu / (rho * rho) * (2. * alpha * rhoExp + beta));
-    double cse = dpdrho + dpdu * pe / (rho * rho);
-    cse = fmax(cse, 0.);
     double pp = pc, cc = csc;
-    if (rho <= rho0 && u > ucv) {
-        pp = pe;
-        cc = cse;
-    } else if (rho <= rho0 && u > uiv && u <= ucv) {
-        pp = ((u - uiv) * pe + (ucv - u) * pc) / (ucv - uiv);
-        cc = ((u - uiv) * cse + (ucv - u) * csc) / (ucv - uiv);
+    // the expanded phase enters only for rho <= rho0 above the incipient / complete vaporisation energies; it is
+    // formed only then (the reference forms it always and uses it only then: the same values)
+    const bool vapor = rho <= rho0 && u > ucv;
+    const bool blend = rho <= rho0 && u > uiv && u <= ucv;
+    if (vapor || blend) {
+        const double rhoExp = rho0 / rho - 1.;
+        const double betaExp = exp(-fmin(beta * rhoExp, 70.));
+        const double alphaExp = exp(-fmin(alpha * (rhoExp * rhoExp), 70.));
+        const double pe = a * rho * u + (b * rho * u / denom + A * mu * betaExp) * alphaExp;
+        dpdu = a * rho + alphaExp * b * rho / (denom * denom);
+        dpdrho = a * u + alphaExp * (b * u * (3. * denom - 2.) / (denom * denom)) +
+                 alphaExp * (b * u * rho / denom) * rho0 * (2. * alpha * rhoExp) / (rho * rho) +
+                 alphaExp * A * betaExp * (1. / rho0 + rho0 * mu / (rho * rho) * (2. * alpha * rhoExp + beta));
+        double cse = dpdrho + dpdu * pe / (rho * rho);
+        cse = fmax(cse, 0.);
+        if (vapor) {
+            pp = pe;
+            cc = cse;
+        } else {
+            pp = ((u - uiv) * pe + (ucv - u) * pc) / (ucv - uiv);
+            cc = ((u - uiv) * cse + (ucv - u) * csc) / (ucv - uiv);
+        }
     }
     cc = fmax(cc, 0.25 * A / rho0);
     p = pp;

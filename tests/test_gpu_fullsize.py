@@ -1,0 +1,116 @@
+"""The CUDA path at the benchmark's full size: the solid impact of 1,000,000 + 20,000 requested particles
+(1,083,803 on the lattice; basalt, von Mises + Grady-Kipp, adaptive h, Barnes-Hut theta 0.5 octupole).
+
+The oracle's neighbour search and one derivative evaluation finish in seconds at this size on the host cores,
+so the pair set is compared exactly and the FP64 derivatives within the small-case tolerance. Over several
+steps the mixed path is held to the stated bound against the FP64 GPU path (1e-6 of the magnitude in density
+and velocity), and the SPH pair terms of both paths to their antisymmetry (the total momentum rate of the
+pressure and stress forces vanishes up to rounding)."""
+import numpy as np
+import pytest
+
+from opensph_gb300 import abi, initial
+from opensph_gb300.solver import GpuSolver
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+N_TARGET, N_IMPACTOR = 1_000_000, 20_000
+FORCES = abi.FORCE_PRESSURE | abi.FORCE_SOLID_STRESS | abi.FORCE_SELF_GRAVITY
+TOL_EVAL = 1e-12
+STEPS = 10
+TOL_MIXED = 1e-6
+
+
+@pytest.fixture(scope="module")
+def impact():
+    st, mats = initial.impact_state(N_TARGET, 5.0e4, N_IMPACTOR, 5.0e3, speed=5.0e3, angle_deg=45.0, seed=1234)
+    return st, mats
+
+
+@pytest.fixture(scope="module")
+def stirred(impact):
+    """The impact state with seeded perturbations, so that every SPH term is active in one evaluation: density and
+    energy within about 1 %, a 10 m/s velocity dispersion, deviatoric stress of 10 MPa."""
+    st, mats = impact
+    rng = np.random.default_rng(7)
+    n = len(st["m"])
+    out = {k: v.copy() for k, v in st.items()}
+    out["rho"] *= 1.0 + 0.01 * rng.standard_normal(n)
+    out["u"] *= 1.0 + 0.01 * rng.random(n)
+    v = out["v"].reshape(-1, 4)
+    v[:, :3] += 10.0 * rng.standard_normal((n, 3))
+    out["S"] = 1.0e7 * rng.standard_normal(out["S"].shape)
+    return out, mats
+
+
+def config(n, mats, precision, forces=FORCES):
+    return abi.make_config(n, mats, forces=forces, adaptive_h=True, precision=precision, initial_timestep=0.03)
+
+
+def scale_err(a, b):
+    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+
+def fresh(st):
+    return {k: v.copy() for k, v in st.items()}
+
+
+def test_pair_set_full_size(impact):
+    st, mats = impact
+    n = len(st["m"])
+    cfg, keep = config(n, mats, abi.PRECISION_FP64)
+    with GpuSolver(cfg, keep) as g:
+        g.set_state(fresh(st))
+        pi, pj = g.pairs()
+    oracle.set_threads(0)
+    oi, oj = oracle.pairs(st["r"])
+    assert len(pi) > 30 * n
+    np.testing.assert_array_equal(pi, oi)
+    np.testing.assert_array_equal(pj, oj)
+
+
+def test_fp64_derivatives_full_size(stirred):
+    st, mats = stirred
+    n = len(st["m"])
+    cfg, keep = config(n, mats, abi.PRECISION_FP64)
+    with GpuSolver(cfg, keep) as g:
+        g.set_state(fresh(st))
+        g.integrate()
+        got = g.get_state(["dv", "drho", "du", "divv", "dS", "ncnt"])
+    ref = fresh(st)
+    oracle.set_threads(0)
+    oracle.integrate(cfg, ref)
+    for f in ["dv", "drho", "du", "divv", "dS"]:
+        assert scale_err(got[f], ref[f]) < TOL_EVAL, f
+    np.testing.assert_array_equal(got["ncnt"], ref["ncnt"])
+
+
+def test_mixed_within_bound_of_fp64_after_steps(impact):
+    st, mats = impact
+    n = len(st["m"])
+    out = {}
+    for name, prec in (("fp64", abi.PRECISION_FP64), ("mixed", abi.PRECISION_MIXED)):
+        cfg, keep = config(n, mats, prec)
+        with GpuSolver(cfg, keep) as g:
+            g.set_state(fresh(st))
+            g.step(STEPS)
+            out[name] = g.get_state(["r", "v", "rho"])
+    ref, mix = out["fp64"], out["mixed"]
+    assert scale_err(mix["rho"], ref["rho"]) < TOL_MIXED
+    assert scale_err(mix["v"].reshape(-1, 4)[:, :3], ref["v"].reshape(-1, 4)[:, :3]) < TOL_MIXED
+    assert scale_err(mix["r"].reshape(-1, 4)[:, :3], ref["r"].reshape(-1, 4)[:, :3]) < TOL_MIXED
+
+
+@pytest.mark.parametrize("precision,tol", [(abi.PRECISION_FP64, 1e-11), (abi.PRECISION_MIXED, 1e-5)])
+def test_sph_pair_terms_are_antisymmetric(stirred, precision, tol):
+    # pressure and stress forces only: sum_i m_i dv_i = 0 pair by pair, relative to sum_i m_i |dv_i|
+    st, mats = stirred
+    n = len(st["m"])
+    cfg, keep = config(n, mats, precision, forces=abi.FORCE_PRESSURE | abi.FORCE_SOLID_STRESS)
+    with GpuSolver(cfg, keep) as g:
+        g.set_state(fresh(st))
+        g.integrate()
+        dv = g.get_state(["dv"])["dv"].reshape(-1, 4)[:, :3]
+    mdv = st["m"][:, None] * dv
+    assert np.abs(mdv.sum(axis=0)).max() < tol * np.abs(mdv).sum(axis=0).max()

@@ -1,5 +1,6 @@
-"""The CUDA path at the benchmark's full size: the solid impact of 1,000,000 + 20,000 requested particles
-(1,083,803 on the lattice; basalt, von Mises + Grady-Kipp, adaptive h, Barnes-Hut theta 0.5 octupole).
+"""The CUDA path at the benchmark's full sizes: the solid impact of 1,000,000 + 20,000 requested particles
+(1,083,803 on the lattice; basalt, von Mises + Grady-Kipp, adaptive h, Barnes-Hut theta 0.5 octupole), and the
+gravity-only Plummer sphere of 4,194,304 particles.
 
 The oracle's neighbour search and one derivative evaluation finish in seconds at this size on the host cores,
 so the pair set is compared exactly and the FP64 derivatives within the small-case tolerance. Over several
@@ -114,3 +115,31 @@ def test_sph_pair_terms_are_antisymmetric(stirred, precision, tol):
         dv = g.get_state(["dv"])["dv"].reshape(-1, 4)[:, :3]
     mdv = st["m"][:, None] * dv
     assert np.abs(mdv.sum(axis=0)).max() < tol * np.abs(mdv).sum(axis=0).max()
+
+
+def test_plummer_full_size_against_direct_sum():
+    # gravity-only N-body at 4,194,304 particles (Plummer sphere, G = 1, softening 1e-3, theta 0.5, octupole):
+    # the FP64 and mixed walks take the same interactions, agree within 2e-6, and both are within the opening
+    # angle's approximation error of FP64 direct summation on a seeded subset of targets
+    n = 4_194_304
+    r, m = initial.plummer(n, seed=21, softening=1e-3)
+    r = r.ravel()
+    targets = np.random.default_rng(4).choice(n, 4096, replace=False).astype("u4")
+    oracle.set_threads(0)
+    direct = oracle.gravity_direct(r, m, G=1.0, targets=targets).reshape(-1, 4)[:, :3]
+    acc, inter = {}, {}
+    for prec in (abi.PRECISION_FP64, abi.PRECISION_MIXED):
+        cfg, keep = abi.make_config(n, [abi.ideal_gas()], forces=abi.FORCE_PRESSURE | abi.FORCE_SELF_GRAVITY,
+                                    gravity_constant=1.0, gravity_opening_angle=0.5, precision=prec)
+        with GpuSolver(cfg, keep) as g:
+            g.set_quantity(abi.Q_POSITION, 0, r)
+            g.set_quantity(abi.Q_MASS, 0, m)
+            acc[prec] = g.gravity().reshape(-1, 4)[:, :3]
+            inter[prec] = g.gravity_interactions()
+    fp64, mixed = acc[abi.PRECISION_FP64], acc[abi.PRECISION_MIXED]
+    assert list(inter[abi.PRECISION_FP64]) == list(inter[abi.PRECISION_MIXED])
+    assert scale_err(mixed, fp64) < 2e-6
+    for a in (fp64, mixed):
+        rel = np.linalg.norm(a[targets] - direct, axis=1) / np.linalg.norm(direct, axis=1)
+        assert np.median(rel) < 2e-4
+        assert np.percentile(rel, 99) < 1e-3

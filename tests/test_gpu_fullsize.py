@@ -1,6 +1,6 @@
 """The CUDA path at the benchmark's full sizes: the solid impact of 1,000,000 + 20,000 requested particles
 (1,083,803 on the lattice; basalt, von Mises + Grady-Kipp, adaptive h, Barnes-Hut theta 0.5 octupole), and the
-gravity-only Plummer sphere of 4,194,304 particles.
+gravity-only Plummer sphere of 4,194,304 particles, and the N-body rubble cloud of 1,000,000 hard spheres.
 
 The oracle's neighbour search and one derivative evaluation finish in seconds at this size on the host cores,
 so the pair set is compared exactly and the FP64 derivatives within the small-case tolerance. Over several
@@ -50,7 +50,10 @@ def config(n, mats, precision, forces=FORCES):
 
 
 def scale_err(a, b):
-    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+    """max |a - b| relative to the largest magnitude of b (absolute where b is zero everywhere)"""
+    s = np.max(np.abs(b))
+    d = np.max(np.abs(a - b))
+    return float(d / s) if s > 0 else float(d)
 
 
 def fresh(st):
@@ -143,3 +146,34 @@ def test_plummer_full_size_against_direct_sum():
         rel = np.linalg.norm(a[targets] - direct, axis=1) / np.linalg.norm(direct, axis=1)
         assert np.median(rel) < 2e-4
         assert np.percentile(rel, 99) < 1e-3
+
+
+@pytest.mark.parametrize("h,sigma,steps", [(400.0, 0.1, 3), (600.0, 0.02, 2)])
+def test_nbody_cloud_full_size_matches_oracle(h, sigma, steps):
+    # HardSphereSolver on 1,000,000 spheres (the rubble cloud of the N-body benchmark; with h = 600 m and a cold
+    # dispersion the first steps merge spheres, with the benchmark's parameters they bounce): the same collisions,
+    # mergers and bounces as the oracle, the same survivors, the states within the Barnes-Hut rounding
+    n = 1_000_000
+    st0 = initial.rubble_cloud(n, 140000.0, h=h, inflow=2e-4, sigma=sigma)
+    cfg, keep = abi.make_nbody_config(n, max_timestep=100.0, initial_timestep=100.0)
+    fields = ["r", "v", "dv", "m", "w"]
+    with GpuSolver(cfg, keep) as g:
+        g.set_state(fresh(st0))
+        g.timestep = 100.0
+        counts = []
+        for _ in range(steps):
+            g.step(1)
+            counts.append(g.n)
+        got = g.get_state(fields)
+        stats = g.collision_stats()
+        dt_next = g.timestep
+    ref = fresh(st0)
+    oracle.set_threads(0)
+    ora_dt, _, ora_counts, ora_stats, ambiguous = oracle.nbody_run(cfg, ref, steps, 100.0)
+    assert ambiguous == 0
+    assert stats == [int(x) for x in ora_stats] and stats[0] > 0
+    assert counts == [int(x) for x in ora_counts]
+    assert abs(dt_next - ora_dt) <= 1e-12 * ora_dt
+    for f in fields:
+        assert got[f].shape == ref[f].shape, f
+        assert scale_err(got[f], ref[f]) < 1e-10, f

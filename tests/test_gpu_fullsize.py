@@ -1,6 +1,7 @@
 """The CUDA path at the benchmark's full sizes: the solid impact of 1,000,000 + 20,000 requested particles
 (1,083,803 on the lattice; basalt, von Mises + Grady-Kipp, adaptive h, Barnes-Hut theta 0.5 octupole), and the
-gravity-only Plummer sphere of 4,194,304 particles, and the N-body rubble cloud of 1,000,000 hard spheres.
+gravity-only Plummer sphere of 4,194,304 particles, the N-body rubble cloud of 1,000,000 hard spheres and the
+adjoint workload of 102,000 requested particles.
 
 The oracle's neighbour search and one derivative evaluation finish in seconds at this size on the host cores,
 so the pair set is compared exactly and the FP64 derivatives within the small-case tolerance. Over several
@@ -177,3 +178,50 @@ def test_nbody_cloud_full_size_matches_oracle(h, sigma, steps):
     for f in fields:
         assert got[f].shape == ref[f].shape, f
         assert scale_err(got[f], ref[f]) < 1e-10, f
+
+
+@pytest.mark.parametrize("precision", [abi.PRECISION_FP64, abi.PRECISION_MIXED])
+def test_adjoint_full_size_against_central_differences(precision):
+    # the adjoint workload at its configured size: ideal-gas sphere of 100,000 requested particles + impactor of
+    # 2,000 at Mach 3, 50 leap-frog steps over lists rebuilt every 10, checkpoints every 10, loss = sum |v_t|^2;
+    # the gradient (all positions, impactor velocity, AV alpha) against FP64 central differences in 4 seeded
+    # smooth directions, within the 1e-4 bound
+    st, nt = initial.gas_impact(100_000, 2_000)
+    n = len(st["m"])
+    pos = st["r"].reshape(-1, 4)[:, :3]
+
+    def solver(state):
+        cfg, keep = abi.make_config(n, [abi.ideal_gas()], forces=abi.FORCE_PRESSURE)
+        g = GpuSolver(cfg, keep)
+        g.set_state({k: state[k] for k in ("r", "v", "m", "rho", "u")})
+        return g
+
+    def acfg(prec, alpha=1.5):
+        return abi.make_adjoint_config(50, 1.0e-3, nt, rebuild_every=10, checkpoint_every=10, alpha=alpha,
+                                       precision=prec)
+
+    with solver(st) as g:
+        g.adjoint_forward(acfg(precision))
+        grad = g.adjoint_backward()
+    rng = np.random.default_rng(5)
+    eps = 1e-7
+    for _ in range(4):
+        dr = np.zeros((n, 4))
+        for _m in range(3):
+            k = 2.0 * rng.standard_normal(3)
+            ph = 2.0 * np.pi * rng.random()
+            amp = rng.standard_normal(3)
+            dr[:, :3] += np.sin(pos @ k + ph)[:, None] * amp[None, :]
+        dv = np.zeros((n, 4))
+        dv[nt:, :3] = rng.standard_normal(3)
+        da = float(rng.standard_normal())
+        vals = []
+        for sgn in (1.0, -1.0):
+            sp = dict(st)
+            sp["r"] = st["r"] + sgn * eps * dr.ravel()
+            sp["v"] = st["v"] + sgn * eps * dv.ravel()
+            with solver(sp) as g:
+                vals.append(g.adjoint_forward(acfg(abi.PRECISION_FP64, 1.5 + sgn * eps * da)))
+        fd = (vals[0] - vals[1]) / (2 * eps)
+        mine = float(np.dot(grad["r"], dr.ravel()) + np.dot(grad["v"], dv.ravel())) + grad["alpha"] * da
+        assert abs(mine - fd) <= 1e-4 * abs(fd)

@@ -203,7 +203,6 @@ __global__ void __launch_bounds__(128, 8) listLevelKernel(const BhNodeGeom* __re
     int32_t* lN = kept + cap;
     int32_t* lP = lN + cap;
     const float4* nf = reinterpret_cast<const float4*>(nodef);
-    const float zero3[3] = { 0.f, 0.f, 0.f };
     // counters[4]: the number of deferred nodes of this level
     const uint32_t total = deferPass ? min(counters[4], last - first) : last - first;
     for (uint32_t k = warpGlobal; k < total; k += nWarps) {
@@ -238,7 +237,6 @@ __global__ void __launch_bounds__(128, 8) listLevelKernel(const BhNodeGeom* __re
             setFrame(fr, nf, int(ev), eg.left < 0, lh, ll);
         }
         __syncwarp();
-        (void)zero3;
         uint32_t nK = 0, nN = 0, nP = 0;
         uint32_t pos = 0;
         while (pos < ncur && !overflow) {
@@ -536,7 +534,8 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 8) evalListsKernel(const uint3
         }
         depth = __shfl_sync(0xffffffffu, depth, 0);
         __syncwarp();
-        const uint32_t g = cnt == 0 ? 1u : min(32u / cnt, MAX_GROUPS);
+        // (leaves hold at most 32 particles: the configuration refuses larger leaf sizes)
+        const uint32_t g = cnt == 0 ? 1u : max(1u, min(32u / cnt, MAX_GROUPS));
         const uint32_t grp = cnt == 0 ? 0u : uint32_t(lane) / cnt;
         const uint32_t pid = uint32_t(lane) - grp * cnt;
         const bool inGroup = grp < g && cnt > 0;

@@ -518,16 +518,12 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 8) evalListsKernel(const uint3
         const int leaf = int(leaves[li]);
         const uint32_t from = geom[leaf].from, to = geom[leaf].to;
         const uint32_t cnt = to - from;
+        // the root path, path[0] = root ... path[depth] = leaf, in one climb from the leaf's level
         int depth = 0;
         if (lane == 0) {
-            int d = 0, nd = leaf;
-            while (geom[nd].parent >= 0 && d < MAX_PATH_F - 1) {
-                nd = geom[nd].parent;
-                ++d;
-            }
-            depth = d;
-            nd = leaf;
-            for (int k = d; k >= 0; --k) {
+            depth = min(geom[leaf].level, MAX_PATH_F - 1);
+            int nd = leaf;
+            for (int k = depth; k >= 0; --k) {
                 path[k] = nd;
                 nd = geom[nd].parent;
             }

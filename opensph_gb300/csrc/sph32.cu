@@ -239,14 +239,25 @@ __global__ void __launch_bounds__(PAIR_THREADS) pairSumMixedKernel(DState s, Gri
     };
 
     uint32_t nq = 0;
-    for (int off = 0; off < 27; ++off) {
-        const int ox = off % 3 - 1, oy = (off / 3) % 3 - 1, oz = off / 9 - 1;
-        const int x = cx + ox, y = cy + oy, z = cz + oz;
-        uint32_t tb = 0, te = 0;
+    // the particle range of neighbour cell off (empty outside the grid); the next cell's range is loaded while the
+    // current cell's candidates are tested
+    auto cellRange = [&](int off, uint32_t& tb, uint32_t& te) {
+        const int x = cx + off % 3 - 1, y = cy + (off / 3) % 3 - 1, z = cz + off / 9 - 1;
+        tb = 0;
+        te = 0;
         if (valid && x >= 0 && x < dxc && y >= 0 && y < dyc && z >= 0 && z < dzc) {
             const uint32_t c = (uint32_t(z) * uint32_t(dyc) + uint32_t(y)) * uint32_t(dxc) + uint32_t(x);
             tb = g.cell_start[c];
             te = g.cell_end[c];
+        }
+    };
+    uint32_t nextB, nextE;
+    cellRange(0, nextB, nextE);
+    for (int off = 0; off < 27; ++off) {
+        const int ox = off % 3 - 1, oy = (off / 3) % 3 - 1, oz = off / 9 - 1;
+        const uint32_t tb = nextB, te = nextE;
+        if (off + 1 < 27) {
+            cellRange(off + 1, nextB, nextE);
         }
         const uint32_t len = te - tb;
         const uint32_t lmax = __reduce_max_sync(0xffffffffu, len);

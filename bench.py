@@ -156,10 +156,10 @@ PAIR_BYTES_PER_PARTICLE = 244 + 164
 def run_gpu(args, rank, world):
     import torch
 
-    from opensph_gb300 import abi
+    from opensph_gb300 import abi, replicas
     from opensph_gb300.solver import GpuSolver
 
-    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    dev = replicas.world_info()[2]
     torch.cuda.set_device(dev)
     st, mats, n = workload(args)
     cfg, keep = make_config(n, mats, abi.PRECISION_MIXED)
@@ -175,8 +175,7 @@ def run_gpu(args, rank, world):
         return None
     g.set_profiling(True)
     g.phase_times()
-    if world > 1:
-        torch.distributed.barrier()
+    replicas.barrier()
     torch.cuda.synchronize()
     start = torch.cuda.Event(enable_timing=True)
     end = torch.cuda.Event(enable_timing=True)
@@ -189,11 +188,8 @@ def run_gpu(args, rank, world):
     ms = start.elapsed_time(end)
     phases, launches = g.phase_times()
     g.set_profiling(False)
-    ms_t = torch.tensor([ms], device=f"cuda:{dev}")
-    if world > 1:
-        torch.distributed.all_reduce(ms_t, op=torch.distributed.ReduceOp.MAX)
-    ms = float(ms_t.item())
-    value = n * args.steps * world / (ms * 1e-3)
+    ms = replicas.max_over_ranks(ms, f"cuda:{dev}")
+    value = replicas.job_rate(n, args.steps, world, ms)
 
     # end-to-end through the public API with host buffers
     pinned = {k: torch.empty(4 * n, dtype=torch.float64, pin_memory=True) for k in ("r", "v")}
@@ -223,10 +219,7 @@ def run_gpu(args, rank, world):
     e2e_end.synchronize()
     e2e_wall = time.perf_counter() - t0
     e2e_ms = max(e2e_start.elapsed_time(e2e_end), e2e_wall * 1e3)
-    e2e_t = torch.tensor([e2e_ms], device=f"cuda:{dev}")
-    if world > 1:
-        torch.distributed.all_reduce(e2e_t, op=torch.distributed.ReduceOp.MAX)
-    e2e_value = n * args.steps * world / (float(e2e_t.item()) * 1e-3)
+    e2e_value = replicas.job_rate(n, args.steps, world, replicas.max_over_ranks(e2e_ms, f"cuda:{dev}"))
     interactions = g.gravity_interactions()
     g.close()
 
@@ -513,8 +506,7 @@ def cpu_sample(args, st, mats, n, steps):
 
 def main():
     args = parse()
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank, world = int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":
         if rank != 0:
             return

@@ -479,7 +479,7 @@ __global__ void __launch_bounds__(LB_THREADS, 4) listBlockKernel(const BhNodeGeo
     }
 }
 
-__global__ void __launch_bounds__(WALK_THREADS_F, 8) evalListsKernel(const uint32_t* __restrict__ idx,
+__global__ void __launch_bounds__(WALK_THREADS_F, 7) evalListsKernel(const uint32_t* __restrict__ idx,
     const BhNodeGeom* __restrict__ geom, const float* __restrict__ nodef, const float4* __restrict__ pf,
     const float* __restrict__ mf, const uint32_t* __restrict__ leaves, uint32_t nLeaves,
     const float* __restrict__ lut, int kernelRadius, int order, const int32_t* __restrict__ pool,

@@ -28,7 +28,10 @@ namespace sphgpu {
 
 namespace {
 
-constexpr int BUILD_THREADS = 256;
+// 128 threads per block, so that a block of each build kernel fits in the registers the concurrent pair loop
+// (main stream) leaves free on an SM: the build then starts its blocks at once instead of waiting for pair
+// blocks to retire
+constexpr int BUILD_THREADS = 128;
 constexpr int MAX_PATH = 512;
 
 struct PosView {
@@ -580,7 +583,7 @@ __global__ void __launch_bounds__(BUILD_THREADS) splitLevelKernel(PosView pv, ui
 // segments): one warp per segment, warp ballots and shuffles instead of block scans and barriers. The
 // partition, the sliding-midpoint moves and the child segments are identical to splitLevelKernel's.
 constexpr uint32_t WARP_SEGMENT = 1024;
-constexpr int SPLIT_WARP_THREADS = 256;
+constexpr int SPLIT_WARP_THREADS = 128;
 
 __device__ __forceinline__ void warpArgExtreme(unsigned long long& val, uint32_t& pos, bool isMax) {
     for (int off = 16; off > 0; off >>= 1) {
@@ -1794,7 +1797,7 @@ cudaError_t treeBuild(const DState& s, Tree& t, const Physics& ph, uint32_t* dev
                 WARP_SEGMENT, BH_SMALL_SEGMENT);
             t.launches++;
         }
-        const uint32_t warpBlocks = min(uint32_t(ceilDiv(nIn, SPLIT_WARP_THREADS / 32)), 152u * 8u);
+        const uint32_t warpBlocks = min(uint32_t(ceilDiv(nIn, SPLIT_WARP_THREADS / 32)), 152u * 64u * 32u / SPLIT_WARP_THREADS);
         splitWarpKernel<<<warpBlocks, SPLIT_WARP_THREADS, 0, st>>>(pv, t.idx, t.scratch_b, t.scratch_s, t.seg[cur],
             nIn, nullptr, t.seg[1 - cur], t.geom, t.counters, t.leaves, ph.leaf_size, t.node_capacity,
             t.seg_capacity, devError, WARP_SEGMENT);
@@ -1846,7 +1849,7 @@ cudaError_t treeBuild(const DState& s, Tree& t, const Physics& ph, uint32_t* dev
             t.launches++;
             while (nIn > 0) {
                 for (uint32_t b = 0; b < LEVEL_BATCH; ++b) {
-                    splitWarpKernel<<<152u * 8u, SPLIT_WARP_THREADS, 0, st>>>(pv, t.idx, t.scratch_b, t.scratch_s,
+                    splitWarpKernel<<<152u * 64u * 32u / SPLIT_WARP_THREADS, SPLIT_WARP_THREADS, 0, st>>>(pv, t.idx, t.scratch_b, t.scratch_s,
                         t.seg[cur], 0, t.level_info + 2 * b + 1, t.seg[1 - cur], t.geom, t.counters, t.leaves,
                         ph.leaf_size, t.node_capacity, t.seg_capacity, devError, WARP_SEGMENT);
                     levelEndKernel<<<1, 1, 0, st>>>(t.counters, t.level_info, b + 1);

@@ -282,6 +282,10 @@ sphgpu_status sphgpu_collision_profile(sphgpu_handle* h, uint64_t out[4]);
  * out[0..2] momentum, out[3..5] angular momentum about the origin, out[6] kinetic energy,
  * out[7] internal energy, out[8] total mass. */
 sphgpu_status sphgpu_totals(sphgpu_handle* h, double out[9]);
+/* The same totals in a frame rotating with frequency omega about z: TotalMomentum(omega) and
+ * TotalAngularMomentum(omega) (core/physics/Integrals.cpp:20-62) use v + omega x r; the kinetic energy uses v,
+ * as TotalEnergy(omega) does (Integrals.cpp:64-91). sphgpu_totals is omega = 0. */
+sphgpu_status sphgpu_totals_frame(sphgpu_handle* h, double omega, double out[9]);
 
 /* Device NaN/Inf scan of the integrated state; SPHGPU_ERR_NONFINITE with the first bad particle index. */
 sphgpu_status sphgpu_check_finite(sphgpu_handle* h, uint64_t* first_bad);

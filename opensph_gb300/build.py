@@ -27,6 +27,7 @@ UNITS = {
     "grid.cu": ["-fmad=false"],
     "sph64.cu": ["-fmad=false"],
     "gravity.cu": ["-fmad=false"],
+    "treebuild.cu": ["-fmad=false"],
     "sph32.cu": [],
     "gravity32.cu": [],
     "noalloc.cu": [],

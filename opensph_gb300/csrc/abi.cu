@@ -1301,10 +1301,17 @@ sphgpu_status sphgpu_set_timestep(sphgpu_handle* h, double dt) {
 }
 
 sphgpu_status sphgpu_totals(sphgpu_handle* h, double out[9]) {
+    return sphgpu_totals_frame(h, 0., out);
+}
+
+sphgpu_status sphgpu_totals_frame(sphgpu_handle* h, double omega, double out[9]) {
     if (!h || !out) {
         return SPHGPU_ERR_ARGUMENT;
     }
-    launchTotals(h->s, h->d_tot_partial, h->d_tot, h->stream);
+    if (!std::isfinite(omega)) {
+        return fail(h, SPHGPU_ERR_ARGUMENT, "frame frequency must be finite");
+    }
+    launchTotals(h->s, omega, h->d_tot_partial, h->d_tot, h->stream);
     CUDA_TRY(h, cudaMemcpyAsync(out, h->d_tot, 9 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     return SPHGPU_OK;

@@ -1,18 +1,8 @@
 // gravity.cu — Barnes-Hut self-gravity in FP64 (compiled with -fmad=false).
 //
-// Replaces BarnesHut::build / evalSelfGravity / evalAcceleration (core/gravity/BarnesHut.cpp:50-175,
-// 212-489) with the k-d tree of KdTree::buildTree (core/objects/finders/KdTree.inl.h:44-160) and the
-// moments of core/gravity/Moments.h.
-//
-// Build: level-synchronous. Every segment (tree node still to split) of a level is processed by one CTA,
-// which reproduces the reference partition exactly: the two-pointer partition of the reference around the
-// box centre is equivalent to pairing the k-th element above the split (from the left) with the k-th
-// element below it (from the right) while they are out of order, which a CTA computes with block scans;
-// the sliding-midpoint steps (single extreme element moved to one side) are arg-min/arg-max reductions
-// with the reference's first-occurrence tie rule; after more than five consecutive slides the reference's
-// std::nth_element is replayed by one thread (libstdc++ introselect). Leaf membership and the order of the
-// particles inside each leaf are therefore identical to the reference's, and so are the leaf boxes and
-// centres of mass. Moments are then formed bottom-up in one launch (momentsUpKernel).
+// Replaces BarnesHut::build (moments) / evalSelfGravity / evalAcceleration (core/gravity/BarnesHut.cpp:50-175,
+// 212-489) with the moments of core/gravity/Moments.h over the k-d tree of treebuild.cu. Moments are formed
+// bottom-up in one launch (momentsUpKernel).
 //
 // Walk: one warp per leaf replays the reference's dual walk along the leaf's root path: at each ancestor
 // the pending check-list entries are classified against that ancestor's box with the reference's
@@ -28,1129 +18,7 @@ namespace sphgpu {
 
 namespace {
 
-// 128 threads per block, so that a block of each build kernel fits in the registers the concurrent pair loop
-// (main stream) leaves free on an SM: the build then starts its blocks at once instead of waiting for pair
-// blocks to retire
-constexpr int BUILD_THREADS = 128;
 constexpr int MAX_PATH = 512;
-
-struct PosView {
-    const dbl4* r;
-    __device__ __forceinline__ double val(uint32_t i, int dim) const {
-        return __ldg(reinterpret_cast<const double*>(r) + 4 * size_t(i) + dim);
-    }
-    // orderKey of the coordinate: the build compares keys (integer pipe) instead of doubles (slow FP64 pipe)
-    __device__ __forceinline__ unsigned long long key(uint32_t i, int dim) const {
-        return orderKey(val(i, dim));
-    }
-};
-
-__device__ __forceinline__ int argMax3(const double s[3]) {
-    int m = 0;
-    if (s[1] > s[m]) {
-        m = 1;
-    }
-    if (s[2] > s[m]) {
-        m = 2;
-    }
-    return m;
-}
-
-// ---------------------------------------------------------------------------------------------------------
-// libstdc++ introselect, replayed for the rare nth_element split of KdTree::buildTree (single thread)
-// ---------------------------------------------------------------------------------------------------------
-
-struct NthCtx {
-    uint32_t* a;
-    PosView pv;
-    int dim;
-    __device__ __forceinline__ bool less(uint32_t x, uint32_t y) const {
-        return pv.val(x, dim) < pv.val(y, dim);
-    }
-};
-
-__device__ void pushHeap(NthCtx& c, long first, long hole, long top, uint32_t value) {
-    long parent = (hole - 1) / 2;
-    while (hole > top && c.less(c.a[first + parent], value)) {
-        c.a[first + hole] = c.a[first + parent];
-        hole = parent;
-        parent = (hole - 1) / 2;
-    }
-    c.a[first + hole] = value;
-}
-
-__device__ void adjustHeap(NthCtx& c, long first, long hole, long len, uint32_t value) {
-    const long top = hole;
-    long second = hole;
-    while (second < (len - 1) / 2) {
-        second = 2 * (second + 1);
-        if (c.less(c.a[first + second], c.a[first + second - 1])) {
-            second--;
-        }
-        c.a[first + hole] = c.a[first + second];
-        hole = second;
-    }
-    if ((len & 1) == 0 && second == (len - 2) / 2) {
-        second = 2 * (second + 1);
-        c.a[first + hole] = c.a[first + second - 1];
-        hole = second - 1;
-    }
-    pushHeap(c, first, hole, top, value);
-}
-
-__device__ void heapSelect(NthCtx& c, long first, long middle, long last) {
-    const long len = middle - first;
-    if (len >= 2) {
-        long parent = (len - 2) / 2;
-        while (true) {
-            adjustHeap(c, first, parent, len, c.a[first + parent]);
-            if (parent == 0) {
-                break;
-            }
-            parent--;
-        }
-    }
-    for (long i = middle; i < last; ++i) {
-        if (c.less(c.a[i], c.a[first])) {
-            const uint32_t value = c.a[i];
-            c.a[i] = c.a[first];
-            adjustHeap(c, first, 0, len, value);
-        }
-    }
-}
-
-__device__ __forceinline__ void iterSwap(uint32_t* a, long x, long y) {
-    const uint32_t t = a[x];
-    a[x] = a[y];
-    a[y] = t;
-}
-
-__device__ void moveMedianToFirst(NthCtx& c, long result, long x, long y, long z) {
-    if (c.less(c.a[x], c.a[y])) {
-        if (c.less(c.a[y], c.a[z])) {
-            iterSwap(c.a, result, y);
-        } else if (c.less(c.a[x], c.a[z])) {
-            iterSwap(c.a, result, z);
-        } else {
-            iterSwap(c.a, result, x);
-        }
-    } else if (c.less(c.a[x], c.a[z])) {
-        iterSwap(c.a, result, x);
-    } else if (c.less(c.a[y], c.a[z])) {
-        iterSwap(c.a, result, z);
-    } else {
-        iterSwap(c.a, result, y);
-    }
-}
-
-__device__ long unguardedPartition(NthCtx& c, long first, long last, long pivot) {
-    while (true) {
-        while (c.less(c.a[first], c.a[pivot])) {
-            ++first;
-        }
-        --last;
-        while (c.less(c.a[pivot], c.a[last])) {
-            --last;
-        }
-        if (!(first < last)) {
-            return first;
-        }
-        iterSwap(c.a, first, last);
-        ++first;
-    }
-}
-
-__device__ void insertionSort(NthCtx& c, long first, long last) {
-    if (first == last) {
-        return;
-    }
-    for (long i = first + 1; i != last; ++i) {
-        if (c.less(c.a[i], c.a[first])) {
-            const uint32_t val = c.a[i];
-            for (long k = i; k > first; --k) {
-                c.a[k] = c.a[k - 1];
-            }
-            c.a[first] = val;
-        } else {
-            const uint32_t val = c.a[i];
-            long last2 = i, next = i - 1;
-            while (c.less(val, c.a[next])) {
-                c.a[last2] = c.a[next];
-                last2 = next;
-                --next;
-            }
-            c.a[last2] = val;
-        }
-    }
-}
-
-__device__ void nthElement(NthCtx& c, long first, long nth, long last) {
-    if (first == last || nth == last) {
-        return;
-    }
-    long n = last - first;
-    int lg = 0;
-    while (n > 1) {
-        n >>= 1;
-        ++lg;
-    }
-    int depth = 2 * lg;
-    while (last - first > 3) {
-        if (depth == 0) {
-            heapSelect(c, first, nth + 1, last);
-            iterSwap(c.a, first, nth);
-            return;
-        }
-        --depth;
-        const long mid = first + (last - first) / 2;
-        moveMedianToFirst(c, first, first + 1, mid, last - 1);
-        const long cut = unguardedPartition(c, first + 1, last, first);
-        if (cut <= nth) {
-            first = cut;
-        } else {
-            last = cut;
-        }
-    }
-    insertionSort(c, first, last);
-}
-
-// ---------------------------------------------------------------------------------------------------------
-// build
-// ---------------------------------------------------------------------------------------------------------
-
-__global__ void initRootKernel(uint32_t n, uint32_t* idx, BhSegment* seg, BhNodeGeom* geom, uint32_t* counters,
-    const unsigned long long* bounds) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) {
-        idx[i] = i;
-    }
-    if (i == 0) {
-        BhSegment s;
-        s.from = 0;
-        s.to = n;
-        s.node = 0;
-        s.sliding = 0;
-        for (int k = 0; k < 3; ++k) {
-            s.lo[k] = doubleUnflip(bounds[k]);
-            s.hi[k] = doubleUnflip(bounds[3 + k]);
-        }
-        seg[0] = s;
-        geom[0].parent = -1;
-        geom[0].level = 0;
-        counters[0] = 1;
-        counters[1] = 0;
-        counters[2] = 0;
-        counters[3] = 0;
-        counters[4] = 0;
-    }
-}
-
-__global__ void boundsOnlyKernel(const dbl4* __restrict__ r, uint32_t n, unsigned long long* b) {
-    unsigned long long mn[3] = { ~0ull, ~0ull, ~0ull }, mx[3] = { 0, 0, 0 };
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const dbl4 p = r[i];
-        const unsigned long long f[3] = { doubleFlip(p.x), doubleFlip(p.y), doubleFlip(p.z) };
-        for (int k = 0; k < 3; ++k) {
-            mn[k] = min(mn[k], f[k]);
-            mx[k] = max(mx[k], f[k]);
-        }
-    }
-    for (int off = 16; off > 0; off >>= 1) {
-        for (int k = 0; k < 3; ++k) {
-            mn[k] = min(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], off));
-            mx[k] = max(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], off));
-        }
-    }
-    if ((threadIdx.x & 31) == 0) {
-        for (int k = 0; k < 3; ++k) {
-            atomicMin(&b[k], mn[k]);
-            atomicMax(&b[3 + k], mx[k]);
-        }
-    }
-}
-
-__global__ void resetBounds6(unsigned long long* b) {
-    if (threadIdx.x < 3) {
-        b[threadIdx.x] = ~0ull;
-        b[3 + threadIdx.x] = 0ull;
-    }
-}
-
-// block-wide helpers (BUILD_THREADS threads)
-__device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t& total, uint32_t* sh) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t x = v;
-    for (int off = 1; off < 32; off <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
-        if (lane >= off) {
-            x += y;
-        }
-    }
-    if (lane == 31) {
-        sh[warp] = x;
-    }
-    __syncthreads();
-    if (warp == 0) {
-        uint32_t w = lane < (BUILD_THREADS / 32) ? sh[lane] : 0;
-        for (int off = 1; off < 32; off <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, w, off);
-            if (lane >= off) {
-                w += y;
-            }
-        }
-        if (lane < (BUILD_THREADS / 32)) {
-            sh[lane] = w;
-        }
-    }
-    __syncthreads();
-    const uint32_t warpOffset = warp > 0 ? sh[warp - 1] : 0;
-    total = sh[BUILD_THREADS / 32 - 1];
-    __syncthreads();
-    return warpOffset + x - v;
-}
-
-__device__ __forceinline__ uint32_t blockSum(uint32_t v, uint32_t* sh) {
-    uint32_t total;
-    blockExclusiveScan(v, total, sh);
-    return total;
-}
-
-__device__ __forceinline__ bool blockAny(bool v, int* sh) {
-    const int r = __syncthreads_or(v ? 1 : 0);
-    (void)sh;
-    return r != 0;
-}
-
-// (key, position) lexicographic minimum (maximum) across the block, the first occurrence on ties
-__device__ void blockArgExtreme(unsigned long long& val, uint32_t& pos, bool isMax, unsigned long long* shv,
-    uint32_t* shp) {
-    for (int off = 16; off > 0; off >>= 1) {
-        const unsigned long long ov = __shfl_xor_sync(0xffffffffu, val, off);
-        const uint32_t op = __shfl_xor_sync(0xffffffffu, pos, off);
-        const bool better = isMax ? (ov > val || (ov == val && op < pos)) : (ov < val || (ov == val && op < pos));
-        if (better) {
-            val = ov;
-            pos = op;
-        }
-    }
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) {
-        shv[warp] = val;
-        shp[warp] = pos;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int w = 1; w < BUILD_THREADS / 32; ++w) {
-            const unsigned long long ov = shv[w];
-            const uint32_t op = shp[w];
-            const bool better =
-                isMax ? (ov > shv[0] || (ov == shv[0] && op < shp[0])) : (ov < shv[0] || (ov == shv[0] && op < shp[0]));
-            if (better) {
-                shv[0] = ov;
-                shp[0] = op;
-            }
-        }
-    }
-    __syncthreads();
-    val = shv[0];
-    pos = shp[0];
-    __syncthreads();
-}
-
-__global__ void __launch_bounds__(BUILD_THREADS) splitLevelKernel(PosView pv, uint32_t* idx, uint32_t* posB,
-    uint32_t* posS, const BhSegment* segIn, uint32_t nIn, BhSegment* segOut, BhNodeGeom* geom, uint32_t* counters,
-    uint32_t* leaves, uint32_t leafSize, uint32_t nodeCapacity, uint32_t segCapacity, uint32_t* devError,
-    uint32_t minSize, uint32_t maxSize) {
-    __shared__ uint32_t shScan[32];
-    __shared__ unsigned long long shV[32];
-    __shared__ uint32_t shP[32];
-    __shared__ int shAny[4];
-    __shared__ uint32_t shNode[2];
-    for (uint32_t sidx = blockIdx.x; sidx < nIn; sidx += gridDim.x) {
-        const BhSegment sg = segIn[sidx];
-        const uint32_t from = sg.from, to = sg.to;
-        const int node = sg.node;
-        if (to - from > maxSize || to - from <= minSize) {
-            continue; // large segments: the multi-CTA pipeline below; small ones: splitWarpKernel
-        }
-        if (to - from <= leafSize) {
-            // KdTree::addLeaf: tight box of the leaf's points
-            double lo[3] = { DBL_MAX, DBL_MAX, DBL_MAX }, hi[3] = { -DBL_MAX, -DBL_MAX, -DBL_MAX };
-            if (threadIdx.x == 0) {
-                for (uint32_t k = from; k < to; ++k) {
-                    const uint32_t i = idx[k];
-                    for (int d = 0; d < 3; ++d) {
-                        const double x = pv.val(i, d);
-                        lo[d] = fmin(lo[d], x);
-                        hi[d] = fmax(hi[d], x);
-                    }
-                }
-                BhNodeGeom& g = geom[node];
-                for (int d = 0; d < 3; ++d) {
-                    g.lo[d] = lo[d];
-                    g.hi[d] = hi[d];
-                }
-                g.left = -1;
-                g.right = -1;
-                g.from = from;
-                g.to = to;
-                const uint32_t slot = atomicAdd(&counters[2], 1u);
-                leaves[slot] = uint32_t(node);
-            }
-            __syncthreads();
-            continue;
-        }
-        // split by the dimension of largest extent of the (split) box
-        double boxSize[3];
-        for (int d = 0; d < 3; ++d) {
-            boxSize[d] = sg.hi[d] - sg.lo[d];
-        }
-        int splitIdx = argMax3(boxSize);
-        // singularity of each dimension: all values equal to the last one
-        bool diff[3] = { false, false, false };
-        {
-            const uint32_t il = idx[to - 1];
-            const unsigned long long last[3] = { pv.key(il, 0), pv.key(il, 1), pv.key(il, 2) };
-            for (uint32_t k = from + threadIdx.x; k < to; k += BUILD_THREADS) {
-                const uint32_t i = idx[k];
-                for (int d = 0; d < 3; ++d) {
-                    diff[d] = diff[d] || (pv.key(i, d) != last[d]);
-                }
-            }
-        }
-        bool nonSingular[3];
-        for (int d = 0; d < 3; ++d) {
-            nonSingular[d] = blockAny(diff[d], shAny);
-        }
-        bool degenerated = false;
-        for (int dim = 0; dim < 3; ++dim) {
-            if (!nonSingular[splitIdx]) {
-                boxSize[splitIdx] = 0.;
-                splitIdx = argMax3(boxSize);
-                if (boxSize[0] == 0. && boxSize[1] == 0. && boxSize[2] == 0.) {
-                    degenerated = true;
-                    break;
-                }
-            } else {
-                break;
-            }
-        }
-        double splitPosition = 0.5 * (sg.lo[splitIdx] + sg.hi[splitIdx]);
-        uint32_t n1;
-        bool sliding = false;
-        double lo1[3], hi1[3], lo2[3], hi2[3];
-        for (int d = 0; d < 3; ++d) {
-            lo1[d] = lo2[d] = sg.lo[d];
-            hi1[d] = hi2[d] = sg.hi[d];
-        }
-        if (sg.sliding <= 5 && !degenerated) {
-            // ranks of the elements above (B) and below (S) the split position, left to right
-            const unsigned long long splitKey = orderKey(splitPosition);
-            uint32_t baseB = 0, baseS = 0;
-            for (uint32_t k0 = from; k0 < to; k0 += BUILD_THREADS) {
-                const uint32_t k = k0 + threadIdx.x;
-                bool isB = false, isS = false;
-                if (k < to) {
-                    const unsigned long long x = pv.key(idx[k], splitIdx);
-                    isB = x > splitKey;
-                    isS = x < splitKey;
-                }
-                uint32_t totB, totS;
-                const uint32_t rb = blockExclusiveScan(isB ? 1u : 0u, totB, shScan);
-                const uint32_t rs = blockExclusiveScan(isS ? 1u : 0u, totS, shScan);
-                if (isB) {
-                    posB[from + baseB + rb] = k;
-                }
-                if (isS) {
-                    posS[from + baseS + rs] = k;
-                }
-                baseB += totB;
-                baseS += totS;
-            }
-            __syncthreads();
-            const uint32_t nB = baseB, nS = baseS;
-            // K = number of (k-th B from the left, k-th S from the right) pairs that are out of order
-            const uint32_t m = min(nB, nS);
-            uint32_t cntLocal = 0;
-            for (uint32_t k = threadIdx.x; k < m; k += BUILD_THREADS) {
-                cntLocal += (posB[from + k] < posS[from + nS - 1 - k]) ? 1u : 0u;
-            }
-            const uint32_t K = blockSum(cntLocal, shScan);
-            // the two-pointer partition swaps exactly these pairs
-            for (uint32_t k = threadIdx.x; k < K; k += BUILD_THREADS) {
-                const uint32_t a = posB[from + k], b = posS[from + nS - 1 - k];
-                const uint32_t t = idx[a];
-                idx[a] = idx[b];
-                idx[b] = t;
-            }
-            __syncthreads();
-            uint32_t n1b = K < nB ? posB[from + K] : to;
-            if (K >= 1) {
-                n1b = min(n1b, posS[from + nS - K]);
-            }
-            n1 = n1b;
-            if (n1 == from || n1 == to) {
-                // sliding midpoint: move the extreme element (first occurrence) to the empty side
-                const bool isMax = (n1 == to);
-                unsigned long long val = isMax ? 0ull : ~0ull;
-                uint32_t pos = 0xffffffffu;
-                for (uint32_t k = from + threadIdx.x; k < to; k += BUILD_THREADS) {
-                    const unsigned long long x = pv.key(idx[k], splitIdx);
-                    const bool better = isMax ? (x > val || (x == val && k < pos)) : (x < val || (x == val && k < pos));
-                    if (better) {
-                        val = x;
-                        pos = k;
-                    }
-                }
-                blockArgExtreme(val, pos, isMax, shV, shP);
-                // the extreme coordinate itself (its key was formed from it)
-                const double extreme = pv.val(idx[pos], splitIdx);
-                __syncthreads();
-                if (threadIdx.x == 0) {
-                    const uint32_t dst = isMax ? to - 1 : from;
-                    const uint32_t t = idx[dst];
-                    idx[dst] = idx[pos];
-                    idx[pos] = t;
-                }
-                __syncthreads();
-                splitPosition = extreme;
-                n1 = isMax ? to - 1 : from + 1;
-                sliding = true;
-            }
-            hi1[splitIdx] = splitPosition;
-            lo2[splitIdx] = splitPosition;
-        } else {
-            n1 = (from + to) >> 1;
-            if (!degenerated && threadIdx.x == 0) {
-                NthCtx c{ idx, pv, splitIdx };
-                nthElement(c, long(from), long(n1), long(to));
-            }
-            __syncthreads();
-            const double x = pv.val(idx[n1], splitIdx);
-            hi1[splitIdx] = x;
-            lo2[splitIdx] = x;
-        }
-        // inner node with two children; allocate ids and push the child segments of the next level
-        if (threadIdx.x == 0) {
-            uint32_t child = atomicAdd(&counters[0], 2u);
-            uint32_t slot = atomicAdd(&counters[1], 2u);
-            if (child + 2 > nodeCapacity || slot + 2 > segCapacity) {
-                atomicOr(devError, child + 2 > nodeCapacity ? uint32_t(DEV_ERR_NODE_CAPACITY)
-                                                            : uint32_t(DEV_ERR_SEGMENT_CAPACITY));
-                child = 0xffffffffu;
-            }
-            shNode[0] = child;
-            shNode[1] = slot;
-        }
-        __syncthreads();
-        const uint32_t child = shNode[0], slot = shNode[1];
-        if (threadIdx.x == 0 && child != 0xffffffffu) {
-            BhNodeGeom& g = geom[node];
-            g.left = int32_t(child);
-            g.right = int32_t(child + 1);
-            g.from = from;
-            g.to = to;
-            const int lvl = g.level;
-            geom[child].parent = node;
-            geom[child].level = lvl + 1;
-            geom[child + 1].parent = node;
-            geom[child + 1].level = lvl + 1;
-            const uint32_t next = sliding ? sg.sliding + 1 : 0;
-            BhSegment l, r;
-            l.from = from;
-            l.to = n1;
-            l.node = int32_t(child);
-            l.sliding = next;
-            r.from = n1;
-            r.to = to;
-            r.node = int32_t(child + 1);
-            r.sliding = next;
-            for (int d = 0; d < 3; ++d) {
-                l.lo[d] = lo1[d];
-                l.hi[d] = hi1[d];
-                r.lo[d] = lo2[d];
-                r.hi[d] = hi2[d];
-            }
-            segOut[slot] = l;
-            segOut[slot + 1] = r;
-            atomicMax(&counters[4], max(n1 - from, to - n1));
-        }
-        __syncthreads();
-    }
-}
-
-// The same split for segments of at most WARP_SEGMENT elements (the deep levels, tens of thousands of small
-// segments): one warp per segment, warp ballots and shuffles instead of block scans and barriers. The
-// partition, the sliding-midpoint moves and the child segments are identical to splitLevelKernel's.
-constexpr uint32_t WARP_SEGMENT = 1024;
-constexpr int SPLIT_WARP_THREADS = 128;
-
-__device__ __forceinline__ void warpArgExtreme(unsigned long long& val, uint32_t& pos, bool isMax) {
-    for (int off = 16; off > 0; off >>= 1) {
-        const unsigned long long ov = __shfl_xor_sync(0xffffffffu, val, off);
-        const uint32_t op = __shfl_xor_sync(0xffffffffu, pos, off);
-        const bool better = isMax ? (ov > val || (ov == val && op < pos)) : (ov < val || (ov == val && op < pos));
-        if (better) {
-            val = ov;
-            pos = op;
-        }
-    }
-}
-
-// nInDev: when not null, the segment count of the level is read from the device (batched deep levels)
-__global__ void __launch_bounds__(SPLIT_WARP_THREADS) splitWarpKernel(PosView pv, uint32_t* idx, uint32_t* posB,
-    uint32_t* posS, const BhSegment* segIn, uint32_t nIn, const uint32_t* nInDev, BhSegment* segOut,
-    BhNodeGeom* geom, uint32_t* counters, uint32_t* leaves, uint32_t leafSize, uint32_t nodeCapacity,
-    uint32_t segCapacity, uint32_t* devError, uint32_t maxSize) {
-    if (nInDev) {
-        nIn = *nInDev;
-    }
-    const int lane = threadIdx.x & 31;
-    const uint32_t warpGlobal = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nWarps = (gridDim.x * blockDim.x) >> 5;
-    const unsigned below = (1u << lane) - 1u;
-    for (uint32_t sidx = warpGlobal; sidx < nIn; sidx += nWarps) {
-        const BhSegment sg = segIn[sidx];
-        const uint32_t from = sg.from, to = sg.to;
-        const int node = sg.node;
-        if (to - from > maxSize) {
-            continue;
-        }
-        if (to - from <= leafSize) {
-            // KdTree::addLeaf: tight box of the leaf's points (min / max are exact in any order)
-            double lo[3] = { DBL_MAX, DBL_MAX, DBL_MAX }, hi[3] = { -DBL_MAX, -DBL_MAX, -DBL_MAX };
-            for (uint32_t k = from + lane; k < to; k += 32) {
-                const dbl4 p = pv.r[idx[k]];
-                const double x[3] = { p.x, p.y, p.z };
-                for (int d = 0; d < 3; ++d) {
-                    lo[d] = fmin(lo[d], x[d]);
-                    hi[d] = fmax(hi[d], x[d]);
-                }
-            }
-            for (int off = 16; off > 0; off >>= 1) {
-                for (int d = 0; d < 3; ++d) {
-                    lo[d] = fmin(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], off));
-                    hi[d] = fmax(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], off));
-                }
-            }
-            if (lane == 0) {
-                BhNodeGeom& g = geom[node];
-                for (int d = 0; d < 3; ++d) {
-                    g.lo[d] = lo[d];
-                    g.hi[d] = hi[d];
-                }
-                g.left = -1;
-                g.right = -1;
-                g.from = from;
-                g.to = to;
-                const uint32_t slot = atomicAdd(&counters[2], 1u);
-                leaves[slot] = uint32_t(node);
-            }
-            continue;
-        }
-        double boxSize[3];
-        for (int d = 0; d < 3; ++d) {
-            boxSize[d] = sg.hi[d] - sg.lo[d];
-        }
-        int splitIdx = argMax3(boxSize);
-        bool diff[3] = { false, false, false };
-        {
-            const uint32_t il = idx[to - 1];
-            const dbl4 pl = pv.r[il];
-            const unsigned long long last[3] = { orderKey(pl.x), orderKey(pl.y), orderKey(pl.z) };
-            for (uint32_t k = from + lane; k < to; k += 32) {
-                const dbl4 p = pv.r[idx[k]];
-                const unsigned long long x[3] = { orderKey(p.x), orderKey(p.y), orderKey(p.z) };
-                for (int d = 0; d < 3; ++d) {
-                    diff[d] = diff[d] || (x[d] != last[d]);
-                }
-            }
-        }
-        bool nonSingular[3];
-        for (int d = 0; d < 3; ++d) {
-            nonSingular[d] = __any_sync(0xffffffffu, diff[d]);
-        }
-        bool degenerated = false;
-        for (int dim = 0; dim < 3; ++dim) {
-            if (!nonSingular[splitIdx]) {
-                boxSize[splitIdx] = 0.;
-                splitIdx = argMax3(boxSize);
-                if (boxSize[0] == 0. && boxSize[1] == 0. && boxSize[2] == 0.) {
-                    degenerated = true;
-                    break;
-                }
-            } else {
-                break;
-            }
-        }
-        double splitPosition = 0.5 * (sg.lo[splitIdx] + sg.hi[splitIdx]);
-        uint32_t n1;
-        bool sliding = false;
-        double lo1[3], hi1[3], lo2[3], hi2[3];
-        for (int d = 0; d < 3; ++d) {
-            lo1[d] = lo2[d] = sg.lo[d];
-            hi1[d] = hi2[d] = sg.hi[d];
-        }
-        if (sg.sliding <= 5 && !degenerated) {
-            const unsigned long long splitKey = orderKey(splitPosition);
-            uint32_t nB = 0, nS = 0;
-            for (uint32_t k0 = from; k0 < to; k0 += 32) {
-                const uint32_t k = k0 + lane;
-                bool isB = false, isS = false;
-                if (k < to) {
-                    const unsigned long long x = pv.key(idx[k], splitIdx);
-                    isB = x > splitKey;
-                    isS = x < splitKey;
-                }
-                const unsigned mB = __ballot_sync(0xffffffffu, isB), mS = __ballot_sync(0xffffffffu, isS);
-                if (isB) {
-                    posB[from + nB + __popc(mB & below)] = k;
-                }
-                if (isS) {
-                    posS[from + nS + __popc(mS & below)] = k;
-                }
-                nB += __popc(mB);
-                nS += __popc(mS);
-            }
-            __syncwarp();
-            const uint32_t m = min(nB, nS);
-            uint32_t cntLocal = 0;
-            for (uint32_t k = lane; k < m; k += 32) {
-                cntLocal += (posB[from + k] < posS[from + nS - 1 - k]) ? 1u : 0u;
-            }
-            const uint32_t K = __reduce_add_sync(0xffffffffu, cntLocal);
-            for (uint32_t k = lane; k < K; k += 32) {
-                const uint32_t a = posB[from + k], b = posS[from + nS - 1 - k];
-                const uint32_t t = idx[a];
-                idx[a] = idx[b];
-                idx[b] = t;
-            }
-            __syncwarp();
-            uint32_t n1b = K < nB ? posB[from + K] : to;
-            if (K >= 1) {
-                n1b = min(n1b, posS[from + nS - K]);
-            }
-            n1 = n1b;
-            if (n1 == from || n1 == to) {
-                const bool isMax = (n1 == to);
-                unsigned long long val = isMax ? 0ull : ~0ull;
-                uint32_t pos = 0xffffffffu;
-                for (uint32_t k = from + lane; k < to; k += 32) {
-                    const unsigned long long x = pv.key(idx[k], splitIdx);
-                    const bool better = isMax ? (x > val || (x == val && k < pos)) : (x < val || (x == val && k < pos));
-                    if (better) {
-                        val = x;
-                        pos = k;
-                    }
-                }
-                warpArgExtreme(val, pos, isMax);
-                const double extreme = pv.val(idx[pos], splitIdx);
-                __syncwarp();
-                if (lane == 0) {
-                    const uint32_t dst = isMax ? to - 1 : from;
-                    const uint32_t t = idx[dst];
-                    idx[dst] = idx[pos];
-                    idx[pos] = t;
-                }
-                __syncwarp();
-                splitPosition = extreme;
-                n1 = isMax ? to - 1 : from + 1;
-                sliding = true;
-            }
-            hi1[splitIdx] = splitPosition;
-            lo2[splitIdx] = splitPosition;
-        } else {
-            n1 = (from + to) >> 1;
-            if (!degenerated && lane == 0) {
-                NthCtx c{ idx, pv, splitIdx };
-                nthElement(c, long(from), long(n1), long(to));
-            }
-            __syncwarp();
-            const double x = pv.val(idx[n1], splitIdx);
-            hi1[splitIdx] = x;
-            lo2[splitIdx] = x;
-        }
-        if (lane == 0) {
-            uint32_t child = atomicAdd(&counters[0], 2u);
-            const uint32_t slot = atomicAdd(&counters[1], 2u);
-            if (child + 2 > nodeCapacity || slot + 2 > segCapacity) {
-                atomicOr(devError, child + 2 > nodeCapacity ? uint32_t(DEV_ERR_NODE_CAPACITY)
-                                                            : uint32_t(DEV_ERR_SEGMENT_CAPACITY));
-                child = 0xffffffffu;
-            }
-            if (child != 0xffffffffu) {
-                BhNodeGeom& g = geom[node];
-                g.left = int32_t(child);
-                g.right = int32_t(child + 1);
-                g.from = from;
-                g.to = to;
-                const int lvl = g.level;
-                geom[child].parent = node;
-                geom[child].level = lvl + 1;
-                geom[child + 1].parent = node;
-                geom[child + 1].level = lvl + 1;
-                const uint32_t next = sliding ? sg.sliding + 1 : 0;
-                BhSegment l, r;
-                l.from = from;
-                l.to = n1;
-                l.node = int32_t(child);
-                l.sliding = next;
-                r.from = n1;
-                r.to = to;
-                r.node = int32_t(child + 1);
-                r.sliding = next;
-                for (int d = 0; d < 3; ++d) {
-                    l.lo[d] = lo1[d];
-                    l.hi[d] = hi1[d];
-                    r.lo[d] = lo2[d];
-                    r.hi[d] = hi2[d];
-                }
-                segOut[slot] = l;
-                segOut[slot + 1] = r;
-                atomicMax(&counters[4], max(n1 - from, to - n1));
-            }
-        }
-        __syncwarp();
-    }
-}
-
-// ---------------------------------------------------------------------------------------------------------
-// multi-CTA split of large segments (same partition as splitLevelKernel, spread over chunks of CHUNK
-// elements): A chunk statistics for the three candidate dimensions -> B per-segment decision and chunk
-// offsets -> E global ranks of the elements above / below the split -> F pair count K, sliding midpoint,
-// nth_element, child segments -> G the K swaps of the two-pointer partition.
-// ---------------------------------------------------------------------------------------------------------
-
-__global__ void chunkListKernel(const BhSegment* __restrict__ segIn, uint32_t nIn, uint32_t maxSize,
-    uint32_t* counters, BhChunk* chunks, BhSegWork* work, uint32_t chunkCapacity, uint32_t* devError) {
-    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < nIn; s += gridDim.x * blockDim.x) {
-        const uint32_t len = segIn[s].to - segIn[s].from;
-        if (len <= maxSize) {
-            continue;
-        }
-        const uint32_t nc = (len + BH_CHUNK - 1) / BH_CHUNK;
-        const uint32_t c0 = atomicAdd(&counters[3], nc);
-        if (c0 + nc > chunkCapacity) {
-            atomicOr(devError, uint32_t(DEV_ERR_SEGMENT_CAPACITY));
-            continue;
-        }
-        for (uint32_t k = 0; k < nc; ++k) {
-            chunks[c0 + k].seg = s;
-            chunks[c0 + k].index = k;
-            chunks[c0 + k].first = c0;
-            chunks[c0 + k].count = nc;
-        }
-    }
-    (void)work;
-}
-
-__device__ __forceinline__ bool betterArg(unsigned long long v, uint32_t p, unsigned long long bv, uint32_t bp,
-    bool isMax) {
-    return isMax ? (v > bv || (v == bv && p < bp)) : (v < bv || (v == bv && p < bp));
-}
-
-// End of a batched deep level: the node count at the start of the next level and its segment count go to
-// levelInfo[next] (2 words each), and the per-level counters are cleared. One thread.
-__global__ void levelEndKernel(uint32_t* counters, uint32_t* levelInfo, uint32_t next) {
-    levelInfo[2 * next] = counters[0];
-    levelInfo[2 * next + 1] = counters[1];
-    counters[1] = 0;
-    counters[4] = 0;
-}
-
-__global__ void setWordKernel(uint32_t* p, uint32_t v) {
-    *p = v;
-}
-
-__global__ void __launch_bounds__(BUILD_THREADS) chunkStatsKernel(PosView pv, const uint32_t* __restrict__ idx,
-    const BhSegment* __restrict__ segIn, const BhChunk* __restrict__ chunks, BhChunkStats* stats) {
-    __shared__ uint32_t shScan[32];
-    __shared__ unsigned long long shV[32];
-    __shared__ uint32_t shP[32];
-    const BhChunk ch = chunks[blockIdx.x];
-    const BhSegment sg = segIn[ch.seg];
-    const uint32_t from = sg.from + ch.index * BH_CHUNK;
-    const uint32_t to = min(sg.to, from + BH_CHUNK);
-    unsigned long long center[3], last[3];
-    const uint32_t il = idx[sg.to - 1];
-    for (int d = 0; d < 3; ++d) {
-        center[d] = orderKey(0.5 * (sg.lo[d] + sg.hi[d]));
-        last[d] = pv.key(il, d);
-    }
-    uint32_t nb[3] = { 0, 0, 0 }, ns[3] = { 0, 0, 0 };
-    bool diff[3] = { false, false, false };
-    unsigned long long mnv[3] = { ~0ull, ~0ull, ~0ull }, mxv[3] = { 0ull, 0ull, 0ull };
-    uint32_t mnp[3] = { 0xffffffffu, 0xffffffffu, 0xffffffffu }, mxp[3] = { 0xffffffffu, 0xffffffffu, 0xffffffffu };
-    for (uint32_t k = from + threadIdx.x; k < to; k += BUILD_THREADS) {
-        const dbl4 p = pv.r[idx[k]];
-        const unsigned long long x[3] = { orderKey(p.x), orderKey(p.y), orderKey(p.z) };
-        for (int d = 0; d < 3; ++d) {
-            nb[d] += x[d] > center[d] ? 1u : 0u;
-            ns[d] += x[d] < center[d] ? 1u : 0u;
-            diff[d] = diff[d] || (x[d] != last[d]);
-            if (betterArg(x[d], k, mnv[d], mnp[d], false)) {
-                mnv[d] = x[d];
-                mnp[d] = k;
-            }
-            if (betterArg(x[d], k, mxv[d], mxp[d], true)) {
-                mxv[d] = x[d];
-                mxp[d] = k;
-            }
-        }
-    }
-    BhChunkStats out;
-    for (int d = 0; d < 3; ++d) {
-        out.nb[d] = blockSum(nb[d], shScan);
-        out.ns[d] = blockSum(ns[d], shScan);
-        out.diff[d] = __syncthreads_or(diff[d] ? 1 : 0) ? 1u : 0u;
-        unsigned long long v = mnv[d];
-        uint32_t q = mnp[d];
-        blockArgExtreme(v, q, false, shV, shP);
-        out.minv[d] = v;
-        out.minp[d] = q;
-        v = mxv[d];
-        q = mxp[d];
-        blockArgExtreme(v, q, true, shV, shP);
-        out.maxv[d] = v;
-        out.maxp[d] = q;
-    }
-    if (threadIdx.x == 0) {
-        stats[blockIdx.x] = out;
-    }
-}
-
-// one warp per large segment (the warp of its first chunk): split dimension and mode, chunk offsets of the
-// elements above / below the box centre (warp scan), extremes of the split coordinate
-__global__ void segDecideKernel(const BhSegment* __restrict__ segIn, const BhChunk* __restrict__ chunks,
-    uint32_t nChunks, const BhChunkStats* __restrict__ stats, uint32_t* chunkOffB, uint32_t* chunkOffS,
-    BhSegWork* work) {
-    const uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (c >= nChunks || chunks[c].index != 0) {
-        return;
-    }
-    const BhChunk ch = chunks[c];
-    const BhSegment sg = segIn[ch.seg];
-    bool anyDiff[3] = { false, false, false };
-    for (uint32_t k = lane; k < ch.count; k += 32) {
-        for (int d = 0; d < 3; ++d) {
-            anyDiff[d] = anyDiff[d] || stats[ch.first + k].diff[d] != 0;
-        }
-    }
-    bool nonSingular[3];
-    for (int d = 0; d < 3; ++d) {
-        nonSingular[d] = __any_sync(0xffffffffu, anyDiff[d]);
-    }
-    double boxSize[3];
-    for (int d = 0; d < 3; ++d) {
-        boxSize[d] = sg.hi[d] - sg.lo[d];
-    }
-    int splitIdx = argMax3(boxSize);
-    bool degenerated = false;
-    for (int dim = 0; dim < 3; ++dim) {
-        if (!nonSingular[splitIdx]) {
-            boxSize[splitIdx] = 0.;
-            splitIdx = argMax3(boxSize);
-            if (boxSize[0] == 0. && boxSize[1] == 0. && boxSize[2] == 0.) {
-                degenerated = true;
-                break;
-            }
-        } else {
-            break;
-        }
-    }
-    uint32_t ob = 0, os = 0;
-    unsigned long long mnv = ~0ull, mxv = 0ull;
-    uint32_t mnp = 0xffffffffu, mxp = 0xffffffffu;
-    for (uint32_t k0 = 0; k0 < ch.count; k0 += 32) {
-        const uint32_t k = k0 + lane;
-        uint32_t nb = 0, ns = 0;
-        if (k < ch.count) {
-            const BhChunkStats& st = stats[ch.first + k];
-            nb = st.nb[splitIdx];
-            ns = st.ns[splitIdx];
-            if (betterArg(st.minv[splitIdx], st.minp[splitIdx], mnv, mnp, false)) {
-                mnv = st.minv[splitIdx];
-                mnp = st.minp[splitIdx];
-            }
-            if (betterArg(st.maxv[splitIdx], st.maxp[splitIdx], mxv, mxp, true)) {
-                mxv = st.maxv[splitIdx];
-                mxp = st.maxp[splitIdx];
-            }
-        }
-        // inclusive scans of the counts across the lanes
-        uint32_t xb = nb, xs = ns;
-        for (int off = 1; off < 32; off <<= 1) {
-            const uint32_t yb = __shfl_up_sync(0xffffffffu, xb, off), ys = __shfl_up_sync(0xffffffffu, xs, off);
-            if (lane >= off) {
-                xb += yb;
-                xs += ys;
-            }
-        }
-        if (k < ch.count) {
-            chunkOffB[ch.first + k] = ob + xb - nb;
-            chunkOffS[ch.first + k] = os + xs - ns;
-        }
-        ob += __shfl_sync(0xffffffffu, xb, 31);
-        os += __shfl_sync(0xffffffffu, xs, 31);
-    }
-    warpArgExtreme(mnv, mnp, false);
-    warpArgExtreme(mxv, mxp, true);
-    if (lane == 0) {
-        BhSegWork w;
-        w.splitIdx = splitIdx;
-        w.mode = degenerated ? 2 : (sg.sliding <= 5 ? 0 : 1);
-        w.nB = ob;
-        w.nS = os;
-        w.minv = mnv;
-        w.minp = mnp;
-        w.maxv = mxv;
-        w.maxp = mxp;
-        w.K = 0;
-        work[ch.seg] = w;
-    }
-}
-
-__global__ void __launch_bounds__(BUILD_THREADS) chunkRanksKernel(PosView pv, const uint32_t* __restrict__ idx,
-    const BhSegment* __restrict__ segIn, const BhChunk* __restrict__ chunks, const uint32_t* __restrict__ chunkOffB,
-    const uint32_t* __restrict__ chunkOffS, const BhSegWork* __restrict__ work, uint32_t* posB, uint32_t* posS) {
-    __shared__ uint32_t shScan[32];
-    const BhChunk ch = chunks[blockIdx.x];
-    const BhSegment sg = segIn[ch.seg];
-    const BhSegWork w = work[ch.seg];
-    if (w.mode != 0) {
-        return;
-    }
-    const int d = w.splitIdx;
-    const unsigned long long split = orderKey(0.5 * (sg.lo[d] + sg.hi[d]));
-    const uint32_t from = sg.from + ch.index * BH_CHUNK;
-    const uint32_t to = min(sg.to, from + BH_CHUNK);
-    uint32_t baseB = sg.from + chunkOffB[blockIdx.x], baseS = sg.from + chunkOffS[blockIdx.x];
-    for (uint32_t k0 = from; k0 < to; k0 += BUILD_THREADS) {
-        const uint32_t k = k0 + threadIdx.x;
-        bool isB = false, isS = false;
-        if (k < to) {
-            const unsigned long long x = pv.key(idx[k], d);
-            isB = x > split;
-            isS = x < split;
-        }
-        uint32_t totB, totS;
-        const uint32_t rb = blockExclusiveScan(isB ? 1u : 0u, totB, shScan);
-        const uint32_t rs = blockExclusiveScan(isS ? 1u : 0u, totS, shScan);
-        if (isB) {
-            posB[baseB + rb] = k;
-        }
-        if (isS) {
-            posS[baseS + rs] = k;
-        }
-        baseB += totB;
-        baseS += totS;
-    }
-}
-
-// one thread per large segment: the pair count K of the two-pointer partition, the split and the children
-__global__ void segFinishKernel(PosView pv, uint32_t* idx, const uint32_t* __restrict__ posB,
-    const uint32_t* __restrict__ posS, const BhSegment* __restrict__ segIn, const BhChunk* __restrict__ chunks,
-    uint32_t nChunks, BhSegWork* work, BhSegment* segOut, BhNodeGeom* geom, uint32_t* counters,
-    uint32_t nodeCapacity, uint32_t segCapacity, uint32_t* devError) {
-    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= nChunks || chunks[c].index != 0) {
-        return;
-    }
-    const uint32_t s = chunks[c].seg;
-    const BhSegment sg = segIn[s];
-    BhSegWork w = work[s];
-    const uint32_t from = sg.from, to = sg.to;
-    const int d = w.splitIdx;
-    double splitPosition = 0.5 * (sg.lo[d] + sg.hi[d]);
-    uint32_t n1;
-    bool sliding = false;
-    double cut;
-    if (w.mode == 0) {
-        const uint32_t nB = w.nB, nS = w.nS;
-        // first k with posB[k] >= posS[nS - 1 - k] (the predicate is monotone in k)
-        uint32_t lo = 0, hi = min(nB, nS);
-        while (lo < hi) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (posB[from + mid] < posS[from + nS - 1 - mid]) {
-                lo = mid + 1;
-            } else {
-                hi = mid;
-            }
-        }
-        const uint32_t K = lo;
-        w.K = K;
-        n1 = K < nB ? posB[from + K] : to;
-        if (K >= 1) {
-            n1 = min(n1, posS[from + nS - K]);
-        }
-        if (n1 == from || n1 == to) {
-            const bool isMax = (n1 == to);
-            const uint32_t dst = isMax ? to - 1 : from;
-            const uint32_t src = isMax ? w.maxp : w.minp;
-            splitPosition = pv.val(idx[src], d);
-            const uint32_t t = idx[dst];
-            idx[dst] = idx[src];
-            idx[src] = t;
-            n1 = isMax ? to - 1 : from + 1;
-            sliding = true;
-        }
-        cut = splitPosition;
-    } else {
-        w.K = 0;
-        n1 = (from + to) >> 1;
-        if (w.mode == 1) {
-            NthCtx ctx{ idx, pv, d };
-            nthElement(ctx, long(from), long(n1), long(to));
-        }
-        cut = pv.val(idx[n1], d);
-    }
-    work[s] = w;
-    uint32_t child = atomicAdd(&counters[0], 2u);
-    const uint32_t slot = atomicAdd(&counters[1], 2u);
-    if (child + 2 > nodeCapacity || slot + 2 > segCapacity) {
-        atomicOr(devError, child + 2 > nodeCapacity ? uint32_t(DEV_ERR_NODE_CAPACITY) : uint32_t(DEV_ERR_SEGMENT_CAPACITY));
-        return;
-    }
-    BhNodeGeom& g = geom[sg.node];
-    g.left = int32_t(child);
-    g.right = int32_t(child + 1);
-    g.from = from;
-    g.to = to;
-    const int lvl = g.level;
-    geom[child].parent = sg.node;
-    geom[child].level = lvl + 1;
-    geom[child + 1].parent = sg.node;
-    geom[child + 1].level = lvl + 1;
-    const uint32_t next = sliding ? sg.sliding + 1 : 0;
-    BhSegment l = sg, r = sg;
-    l.to = n1;
-    l.node = int32_t(child);
-    l.sliding = next;
-    l.hi[d] = cut;
-    r.from = n1;
-    r.node = int32_t(child + 1);
-    r.sliding = next;
-    r.lo[d] = cut;
-    segOut[slot] = l;
-    segOut[slot + 1] = r;
-    atomicMax(&counters[4], max(n1 - from, to - n1));
-}
-
-__global__ void chunkSwapKernel(uint32_t* idx, const uint32_t* __restrict__ posB, const uint32_t* __restrict__ posS,
-    const BhSegment* __restrict__ segIn, const BhChunk* __restrict__ chunks, const BhSegWork* __restrict__ work) {
-    const BhChunk ch = chunks[blockIdx.x];
-    const BhSegWork w = work[ch.seg];
-    const uint32_t from = segIn[ch.seg].from;
-    const uint32_t k0 = ch.index * BH_CHUNK;
-    const uint32_t k1 = min(w.K, k0 + BH_CHUNK);
-    for (uint32_t k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
-        const uint32_t a = posB[from + k], b = posS[from + w.nS - 1 - k];
-        const uint32_t t = idx[a];
-        idx[a] = idx[b];
-        idx[b] = t;
-    }
-}
 
 // BarnesHut::buildLeaf (core/gravity/BarnesHut.cpp:376-437), geometry part: mass, centre of mass and opening
 // radius of the leaf in FP64, summed in the leaf's particle order (the walk's decisions depend on these bits).
@@ -1360,14 +228,9 @@ __device__ __forceinline__ void readMomentsF(const float* nodef, int node, float
 // decisions, while the reduced moments, which the mixed walk evaluates in FP32, are formed in FP32 directly
 // into its node records.
 template <bool Mixed>
-__global__ void momentsUpKernel(const dbl4* __restrict__ r, const double* __restrict__ m, double G,
-    const uint32_t* __restrict__ idx, double thetaInv, BhNodeGeom* geom, BhNodeMoments* mom, float* nodef,
-    const uint32_t* __restrict__ leaves, uint32_t nLeaves, uint32_t* visits) {
-    const uint32_t li = blockIdx.x * blockDim.x + threadIdx.x;
-    if (li >= nLeaves) {
-        return;
-    }
-    const int node = int(leaves[li]);
+__device__ void momentsUpLeaf(const dbl4* __restrict__ r, const double* __restrict__ m, double G,
+    const uint32_t* __restrict__ idx, double thetaInv, BhNodeGeom* geom, BhNodeMoments* mom, float* nodef, int node,
+    uint32_t* visits) {
     int parent;
     {
         BhNodeGeom g = geom[node];
@@ -1422,6 +285,17 @@ __global__ void momentsUpKernel(const dbl4* __restrict__ r, const double* __rest
         }
         geom[parent] = g;
         parent = g.parent;
+    }
+}
+
+template <bool Mixed>
+__global__ void momentsUpKernel(const dbl4* __restrict__ r, const double* __restrict__ m, double G,
+    const uint32_t* __restrict__ idx, double thetaInv, BhNodeGeom* geom, BhNodeMoments* mom, float* nodef,
+    const uint32_t* __restrict__ leaves, const uint32_t* __restrict__ leafCount, uint32_t maxLeaves,
+    uint32_t* visits) {
+    const uint32_t nLeaves = min(*leafCount, maxLeaves);
+    for (uint32_t li = blockIdx.x * blockDim.x + threadIdx.x; li < nLeaves; li += gridDim.x * blockDim.x) {
+        momentsUpLeaf<Mixed>(r, m, G, idx, thetaInv, geom, mom, nodef, int(leaves[li]), visits);
     }
 }
 
@@ -1688,15 +562,14 @@ cudaError_t treeAllocate(Tree& t, uint32_t n, uint32_t leafSize) {
     alloc((void**)&t.mom, size_t(t.node_capacity) * sizeof(BhNodeMoments));
     alloc((void**)&t.seg[0], size_t(t.seg_capacity) * sizeof(BhSegment));
     alloc((void**)&t.seg[1], size_t(t.seg_capacity) * sizeof(BhSegment));
-    alloc((void**)&t.counters, 8 * sizeof(uint32_t));
-    alloc((void**)&t.level_info, 64 * sizeof(uint32_t));
+    alloc((void**)&t.counters, C_WORDS * sizeof(uint32_t));
     alloc((void**)&t.leaves, nn * sizeof(uint32_t));
     alloc((void**)&t.visits, size_t(t.node_capacity) * sizeof(uint32_t));
     alloc((void**)&t.walk_scratch, size_t(t.walk_warps) * 2 * t.walk_capacity * sizeof(int32_t));
     alloc((void**)&t.stats, 8 * sizeof(unsigned long long)); // 4 interaction counters, [4] next leaf of the walk
     alloc((void**)&t.bbox, 8 * sizeof(unsigned long long));
     alloc((void**)&t.nodef, size_t(t.node_capacity) * NODEF * sizeof(float));
-    t.chunk_capacity = 2 * nn / BH_CHUNK + 64;
+    t.chunk_capacity = treeChunkCapacity(nn);
     alloc((void**)&t.chunks, size_t(t.chunk_capacity) * sizeof(BhChunk));
     alloc((void**)&t.chunk_stats, size_t(t.chunk_capacity) * sizeof(BhChunkStats));
     alloc((void**)&t.chunk_off_b, size_t(t.chunk_capacity) * sizeof(uint32_t));
@@ -1705,10 +578,7 @@ cudaError_t treeAllocate(Tree& t, uint32_t n, uint32_t leafSize) {
     alloc((void**)&t.pf, nn * sizeof(float4));
     alloc((void**)&t.mf, nn * sizeof(float));
     if (e == cudaSuccess) {
-        e = cudaMallocHost((void**)&t.counters_host, 8 * sizeof(uint32_t));
-    }
-    if (e == cudaSuccess) {
-        e = cudaMallocHost((void**)&t.level_host, 64 * sizeof(uint32_t));
+        e = treeBuildAllocate(t, nn);
     }
     return e;
 }
@@ -1716,179 +586,45 @@ cudaError_t treeAllocate(Tree& t, uint32_t n, uint32_t leafSize) {
 void treeFree(Tree& t) {
     void* ptrs[] = { t.idx, t.scratch_b, t.scratch_s, t.geom, t.mom, t.seg[0], t.seg[1], t.counters, t.leaves, t.visits,
         t.walk_scratch, t.nl_pool, t.nl_kept[0], t.nl_kept[1], t.nl_meta, t.nl_counters, t.nl_defer, t.stats, t.bbox,
-        t.nodef, t.pf, t.mf, t.chunks, t.chunk_stats, t.chunk_off_b, t.chunk_off_s, t.work, t.level_info };
+        t.nodef, t.pf, t.mf, t.chunks, t.chunk_stats, t.chunk_off_b, t.chunk_off_s, t.work };
     for (void* p : ptrs) {
         if (p) {
             cudaFree(p);
         }
     }
-    if (t.counters_host) {
-        cudaFreeHost(t.counters_host);
-    }
     if (t.nl_host) {
         cudaFreeHost(t.nl_host);
     }
-    if (t.level_host) {
-        cudaFreeHost(t.level_host);
-    }
+    treeBuildFree(t);
     t = Tree();
 }
 
-namespace {
-
-void launchMoments(const DState& s, Tree& t, const Physics& ph, bool mixed, cudaStream_t st) {
-    cudaMemsetAsync(t.visits, 0, size_t(t.node_count) * sizeof(uint32_t), st);
-    if (t.leaf_count == 0) {
-        return;
+void launchMomentsDev(const DState& s, Tree& t, const Physics& ph, bool mixed, cudaStream_t st) {
+    cudaMemsetAsync(t.visits, 0, size_t(t.node_capacity) * sizeof(uint32_t), st);
+    static int grid = 0;
+    if (grid == 0) {
+        int perSm = 0, sms = 0, dev = 0;
+        cudaGetDevice(&dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, momentsUpKernel<false>, 128, 0);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        grid = std::max(1, perSm * sms);
     }
+    // the leaf count is read on the device (counters[C_LEAVES]); at most one leaf per particle
+    const int blocks = std::max(1, std::min(grid, ceilDiv(s.n, 128)));
     if (mixed) {
-        momentsUpKernel<true><<<ceilDiv(t.leaf_count, 128), 128, 0, st>>>(s.r, s.m, ph.G, t.idx, ph.theta_inv, t.geom,
-            t.mom, t.nodef, t.leaves, t.leaf_count, t.visits);
+        momentsUpKernel<true><<<blocks, 128, 0, st>>>(s.r, s.m, ph.G, t.idx, ph.theta_inv, t.geom, t.mom, t.nodef,
+            t.leaves, t.counters + C_LEAVES, s.n, t.visits);
     } else {
-        momentsUpKernel<false><<<ceilDiv(t.leaf_count, 128), 128, 0, st>>>(s.r, s.m, ph.G, t.idx, ph.theta_inv,
-            t.geom, t.mom, t.nodef, t.leaves, t.leaf_count, t.visits);
+        momentsUpKernel<false><<<blocks, 128, 0, st>>>(s.r, s.m, ph.G, t.idx, ph.theta_inv, t.geom, t.mom, t.nodef,
+            t.leaves, t.counters + C_LEAVES, s.n, t.visits);
     }
 }
-
-} // namespace
 
 void treeEnsureFp64Moments(const DState& s, Tree& t, const Physics& ph, cudaStream_t st) {
     if (t.built && t.mixed_moments) {
-        launchMoments(s, t, ph, false, st);
+        launchMomentsDev(s, t, ph, false, st);
         t.mixed_moments = false;
     }
-}
-
-cudaError_t treeBuild(const DState& s, Tree& t, const Physics& ph, uint32_t* devError, cudaStream_t st) {
-    const uint32_t n = s.n;
-    t.built = false;
-    t.level_start.clear();
-    if (n == 0) {
-        t.node_count = 0;
-        t.leaf_count = 0;
-        t.built = true;
-        return cudaSuccess;
-    }
-    // root box = bounding box of all points (KdTree::buildImpl)
-    t.launches = 3;
-    resetBounds6<<<1, 32, 0, st>>>(t.bbox);
-    boundsOnlyKernel<<<min(ceilDiv(n, 256), 152 * 8), 256, 0, st>>>(s.r, n, t.bbox);
-    initRootKernel<<<ceilDiv(n, 256), 256, 0, st>>>(n, t.idx, t.seg[0], t.geom, t.counters, t.bbox);
-    const PosView pv{ s.r };
-    uint32_t nIn = 1;
-    int cur = 0;
-    t.level_start.push_back(0);
-    t.level_start.push_back(1);
-    // the largest segment of a level, known on the host (the root at level 0, then bounded by halving)
-    uint32_t maxSeg = n;
-    for (int level = 0; nIn > 0; ++level) {
-        const int grid = int(min(nIn, 152u * 16u));
-        const bool big = maxSeg > BH_SMALL_SEGMENT;
-        uint32_t nChunks = 0;
-        if (big) {
-            cudaMemsetAsync(t.counters + 3, 0, sizeof(uint32_t), st);
-            chunkListKernel<<<ceilDiv(nIn, 256), 256, 0, st>>>(t.seg[cur], nIn, BH_SMALL_SEGMENT, t.counters,
-                t.chunks, t.work, t.chunk_capacity, devError);
-            t.launches++;
-        }
-        if (maxSeg > WARP_SEGMENT) {
-            splitLevelKernel<<<grid, BUILD_THREADS, 0, st>>>(pv, t.idx, t.scratch_b, t.scratch_s, t.seg[cur], nIn,
-                t.seg[1 - cur], t.geom, t.counters, t.leaves, ph.leaf_size, t.node_capacity, t.seg_capacity, devError,
-                WARP_SEGMENT, BH_SMALL_SEGMENT);
-            t.launches++;
-        }
-        const uint32_t warpBlocks = min(uint32_t(ceilDiv(nIn, SPLIT_WARP_THREADS / 32)), 152u * 64u * 32u / SPLIT_WARP_THREADS);
-        splitWarpKernel<<<warpBlocks, SPLIT_WARP_THREADS, 0, st>>>(pv, t.idx, t.scratch_b, t.scratch_s, t.seg[cur],
-            nIn, nullptr, t.seg[1 - cur], t.geom, t.counters, t.leaves, ph.leaf_size, t.node_capacity,
-            t.seg_capacity, devError, WARP_SEGMENT);
-        t.launches++;
-        if (big) {
-            cudaMemcpyAsync(t.counters_host, t.counters, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
-            cudaError_t e = cudaStreamSynchronize(st);
-            if (e != cudaSuccess) {
-                return e;
-            }
-            nChunks = min(t.counters_host[3], t.chunk_capacity);
-        }
-        if (nChunks > 0) {
-            chunkStatsKernel<<<nChunks, BUILD_THREADS, 0, st>>>(pv, t.idx, t.seg[cur], t.chunks, t.chunk_stats);
-            segDecideKernel<<<ceilDiv(nChunks, 4), 128, 0, st>>>(t.seg[cur], t.chunks, nChunks, t.chunk_stats,
-                t.chunk_off_b, t.chunk_off_s, t.work);
-            chunkRanksKernel<<<nChunks, BUILD_THREADS, 0, st>>>(pv, t.idx, t.seg[cur], t.chunks, t.chunk_off_b,
-                t.chunk_off_s, t.work, t.scratch_b, t.scratch_s);
-            segFinishKernel<<<ceilDiv(nChunks, 128), 128, 0, st>>>(pv, t.idx, t.scratch_b, t.scratch_s, t.seg[cur],
-                t.chunks, nChunks, t.work, t.seg[1 - cur], t.geom, t.counters, t.node_capacity, t.seg_capacity,
-                devError);
-            chunkSwapKernel<<<nChunks, BUILD_THREADS, 0, st>>>(t.idx, t.scratch_b, t.scratch_s, t.seg[cur], t.chunks,
-                t.work);
-            t.launches += 5;
-        }
-        cudaMemcpyAsync(t.counters_host, t.counters, 5 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
-        cudaMemsetAsync(t.counters + 1, 0, sizeof(uint32_t), st);
-        cudaMemsetAsync(t.counters + 4, 0, sizeof(uint32_t), st);
-        cudaError_t e = cudaStreamSynchronize(st);
-        if (e != cudaSuccess) {
-            return e;
-        }
-        nIn = t.counters_host[1];
-        maxSeg = t.counters_host[4];
-        t.node_count = t.counters_host[0];
-        t.leaf_count = t.counters_host[2];
-        if (nIn > 0) {
-            t.level_start.push_back(t.node_count);
-        }
-        cur = 1 - cur;
-        if (level > 100000) {
-            break;
-        }
-        if (nIn > 0 && maxSeg <= WARP_SEGMENT) {
-            // every remaining segment is split by warps (segments only shrink): LEVEL_BATCH levels per host
-            // round trip, the segment counts read by the kernels from levelInfo
-            constexpr uint32_t LEVEL_BATCH = 8;
-            setWordKernel<<<1, 1, 0, st>>>(t.level_info + 1, nIn);
-            t.launches++;
-            while (nIn > 0) {
-                for (uint32_t b = 0; b < LEVEL_BATCH; ++b) {
-                    splitWarpKernel<<<152u * 64u * 32u / SPLIT_WARP_THREADS, SPLIT_WARP_THREADS, 0, st>>>(pv, t.idx, t.scratch_b, t.scratch_s,
-                        t.seg[cur], 0, t.level_info + 2 * b + 1, t.seg[1 - cur], t.geom, t.counters, t.leaves,
-                        ph.leaf_size, t.node_capacity, t.seg_capacity, devError, WARP_SEGMENT);
-                    levelEndKernel<<<1, 1, 0, st>>>(t.counters, t.level_info, b + 1);
-                    cur = 1 - cur;
-                }
-                t.launches += 2 * LEVEL_BATCH;
-                cudaMemcpyAsync(t.level_host, t.level_info, 2 * (LEVEL_BATCH + 1) * sizeof(uint32_t),
-                    cudaMemcpyDeviceToHost, st);
-                cudaMemcpyAsync(t.counters_host, t.counters, 5 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
-                // the next batch starts from the last level's segment count
-                cudaMemcpyAsync(t.level_info + 1, t.level_info + 2 * LEVEL_BATCH + 1, sizeof(uint32_t),
-                    cudaMemcpyDeviceToDevice, st);
-                e = cudaStreamSynchronize(st);
-                if (e != cudaSuccess) {
-                    return e;
-                }
-                for (uint32_t b = 1; b <= LEVEL_BATCH; ++b) {
-                    if (t.level_host[2 * b + 1] > 0) {
-                        t.level_start.push_back(t.level_host[2 * b]);
-                    }
-                }
-                nIn = t.level_host[2 * LEVEL_BATCH + 1];
-                t.node_count = t.counters_host[0];
-                t.leaf_count = t.counters_host[2];
-                level += int(LEVEL_BATCH);
-                if (level > 100000) {
-                    break;
-                }
-            }
-        }
-    }
-    // moments, bottom-up in one launch
-    t.mixed_moments = ph.precision == SPHGPU_PRECISION_MIXED;
-    launchMoments(s, t, ph, t.mixed_moments, st);
-    // FP32 node records of the walks (classification geometry; for the mixed walk also the evaluation data)
-    launchPrepareWalk(s, t, ph, st);
-    t.launches += 2;
-    t.built = true;
-    return cudaGetLastError();
 }
 
 void launchGravityWalk(const DState& s, Tree& t, const Physics& ph, const double* lut, uint32_t* devError,

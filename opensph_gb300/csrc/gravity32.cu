@@ -24,13 +24,9 @@ __device__ __forceinline__ void splitF(double x, float& hi, float& lo) {
     lo = float(x - double(hi));
 }
 
-__global__ void prepareMixedKernel(const dbl4* __restrict__ r, const double* __restrict__ m, double G,
+__device__ void prepareNode(const dbl4* __restrict__ r, const double* __restrict__ m, double G,
     const uint32_t* __restrict__ idx, const BhNodeGeom* __restrict__ geom, const BhNodeMoments* __restrict__ mom,
-    uint32_t nodeCount, float* __restrict__ nodef, float4* __restrict__ pf, float* __restrict__ mf, bool moments) {
-    const uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= nodeCount) {
-        return;
-    }
+    uint32_t id, float* __restrict__ nodef, float4* __restrict__ pf, float* __restrict__ mf, bool moments) {
     const BhNodeGeom& g = geom[id];
     const BhNodeMoments& mo = mom[id];
     float4* o = reinterpret_cast<float4*>(nodef) + size_t(id) * NODEF4;
@@ -74,6 +70,16 @@ __global__ void prepareMixedKernel(const dbl4* __restrict__ r, const double* __r
             pf[k] = make_float4(float(p.x - g.com[0]), float(p.y - g.com[1]), float(p.z - g.com[2]), 0.5f * float(p.w));
             mf[k] = float(G * m[i]);
         }
+    }
+}
+
+__global__ void prepareMixedKernel(const dbl4* __restrict__ r, const double* __restrict__ m, double G,
+    const uint32_t* __restrict__ idx, const BhNodeGeom* __restrict__ geom, const BhNodeMoments* __restrict__ mom,
+    const uint32_t* __restrict__ nodeCountDev, uint32_t nodeCapacity, float* __restrict__ nodef,
+    float4* __restrict__ pf, float* __restrict__ mf, bool moments) {
+    const uint32_t nodeCount = min(*nodeCountDev, nodeCapacity);
+    for (uint32_t id = blockIdx.x * blockDim.x + threadIdx.x; id < nodeCount; id += gridDim.x * blockDim.x) {
+        prepareNode(r, m, G, idx, geom, mom, id, nodef, pf, mf, moments);
     }
 }
 
@@ -189,7 +195,8 @@ __global__ void flagErrorKernel(uint32_t* devError, uint32_t bit) {
 // left to the second pass (deferPass == 1), which runs only the deferred nodes with large staging lists. A node
 // that outgrows those too is a capacity error.
 __global__ void __launch_bounds__(128, 8) listLevelKernel(const BhNodeGeom* __restrict__ geom,
-    const float* __restrict__ nodef, uint32_t first, uint32_t last, int deferPass, uint32_t* __restrict__ defer,
+    const float* __restrict__ nodef, const uint32_t* __restrict__ levelNodes, uint32_t first, uint32_t last,
+    int deferPass, uint32_t* __restrict__ defer,
     int32_t* scratch, uint32_t cap, int32_t* __restrict__ pool, uint32_t poolCap,
     const int32_t* __restrict__ keptIn, int32_t* __restrict__ keptOut, uint32_t keptCap, uint32_t* __restrict__ meta,
     uint32_t* __restrict__ counters, int parity, uint32_t* devError) {
@@ -206,7 +213,7 @@ __global__ void __launch_bounds__(128, 8) listLevelKernel(const BhNodeGeom* __re
     // counters[4]: the number of deferred nodes of this level
     const uint32_t total = deferPass ? min(counters[4], last - first) : last - first;
     for (uint32_t k = warpGlobal; k < total; k += nWarps) {
-        const uint32_t ev = deferPass ? defer[k] : first + k;
+        const uint32_t ev = deferPass ? defer[k] : levelNodes[first + k];
         const BhNodeGeom& eg = geom[ev];
         const int par = eg.parent;
         const int pl = geom[par].left;
@@ -336,7 +343,8 @@ constexpr int LB_THREADS = 256;
 constexpr int LB_WARPS = LB_THREADS / 32;
 
 __global__ void __launch_bounds__(LB_THREADS, 4) listBlockKernel(const BhNodeGeom* __restrict__ geom,
-    const float* __restrict__ nodef, uint32_t first, uint32_t last, int32_t* scratch, uint32_t cap,
+    const float* __restrict__ nodef, const uint32_t* __restrict__ levelNodes, uint32_t first, uint32_t last,
+    int32_t* scratch, uint32_t cap,
     int32_t* __restrict__ pool, uint32_t poolCap, const int32_t* __restrict__ keptIn, int32_t* __restrict__ keptOut,
     uint32_t keptCap, uint32_t* __restrict__ meta, uint32_t* __restrict__ counters, int parity,
     uint32_t* devError) {
@@ -351,7 +359,8 @@ __global__ void __launch_bounds__(LB_THREADS, 4) listBlockKernel(const BhNodeGeo
     int32_t* lN = kept + cap;
     int32_t* lP = lN + cap;
     const float4* nf = reinterpret_cast<const float4*>(nodef);
-    for (uint32_t ev = first + blockIdx.x; ev < last; ev += gridDim.x) {
+    for (uint32_t e = first + blockIdx.x; e < last; e += gridDim.x) {
+        const uint32_t ev = levelNodes[e];
         const BhNodeGeom& eg = geom[ev];
         const int par = eg.parent;
         const int pl = geom[par].left;
@@ -682,12 +691,14 @@ __global__ void __launch_bounds__(WALK_THREADS_F, 7) evalListsKernel(const uint3
 
 } // namespace
 
-void launchPrepareWalk(const DState& s, Tree& t, const Physics& ph, cudaStream_t st) {
-    if (s.n == 0 || t.node_count == 0) {
+void launchPrepareWalkDev(const DState& s, Tree& t, const Physics& ph, cudaStream_t st) {
+    if (s.n == 0) {
         return;
     }
-    prepareMixedKernel<<<ceilDiv(t.node_count, 128), 128, 0, st>>>(s.r, s.m, ph.G, t.idx, t.geom, t.mom,
-        t.node_count, t.nodef, t.pf, t.mf, !t.mixed_moments);
+    // the node count is read on the device (counters[C_NODES]); at most 2 n nodes
+    const int blocks = std::max(1, std::min(ceilDiv(t.node_capacity, 128), 152 * 16));
+    prepareMixedKernel<<<blocks, 128, 0, st>>>(s.r, s.m, ph.G, t.idx, t.geom, t.mom, t.counters + C_NODES, t.node_capacity,
+        t.nodef, t.pf, t.mf, !t.mixed_moments);
 }
 
 void launchGravityWalkMixed(const DState& s, Tree& t, const Physics& ph, const float* lutF, uint32_t* devError,
@@ -713,7 +724,8 @@ void launchGravityWalkMixed(const DState& s, Tree& t, const Physics& ph, const f
     }
     uint32_t poolNeed = std::max<uint32_t>(1u << 20, 64u * t.node_count);
     uint32_t keptNeed = std::max<uint32_t>(1u << 20, 32u * t.node_count);
-    const uint32_t levels = uint32_t(t.level_start.size());
+    // level l holds the nodes level_nodes[level_first[l] .. level_first[l + 1])
+    const uint32_t levels = t.level_first.empty() ? 0u : uint32_t(t.level_first.size() - 1);
     // the lists of all levels; when a pool overflowed, grow it to twice the counted need (the count misses what
     // the children of the nodes that did not fit would have added) and build them again
     bool fits = false;
@@ -733,8 +745,8 @@ void launchGravityWalkMixed(const DState& s, Tree& t, const Physics& ph, const f
         cudaMemsetAsync(t.nl_counters, 0, 8 * sizeof(uint32_t), st);
         cudaMemsetAsync(t.nl_meta, 0, NL_META * sizeof(uint32_t), st); // the root: nothing kept
         for (uint32_t level = 1; level < levels; ++level) {
-            const uint32_t first = t.level_start[level];
-            const uint32_t last = level + 1 < levels ? t.level_start[level + 1] : t.node_count;
+            const uint32_t first = t.level_first[level];
+            const uint32_t last = t.level_first[level + 1];
             if (last <= first) {
                 continue;
             }
@@ -742,7 +754,8 @@ void launchGravityWalkMixed(const DState& s, Tree& t, const Physics& ph, const f
             cudaMemsetAsync(t.nl_counters + 1 + parity, 0, sizeof(uint32_t), st);
             if (last - first <= deferWarps) {
                 // few nodes: a CTA per node with the large staging lists
-                listBlockKernel<<<last - first, LB_THREADS, 0, st>>>(t.geom, t.nodef, first, last, t.walk_scratch,
+                listBlockKernel<<<last - first, LB_THREADS, 0, st>>>(t.geom, t.nodef, t.level_nodes, first, last,
+                    t.walk_scratch,
                     NL_STAGE_DEFER, t.nl_pool, t.nl_capacity, t.nl_kept[1 - parity], t.nl_kept[parity],
                     t.nl_kept_capacity, t.nl_meta, t.nl_counters, parity, devError);
                 t.walk_launches++;
@@ -750,11 +763,13 @@ void launchGravityWalkMixed(const DState& s, Tree& t, const Physics& ph, const f
             }
             cudaMemsetAsync(t.nl_counters + 4, 0, sizeof(uint32_t), st);
             const uint32_t warps = std::min(last - first, listWarps);
-            listLevelKernel<<<ceilDiv(warps, 4), 128, 0, st>>>(t.geom, t.nodef, first, last, 0, t.nl_defer,
+            listLevelKernel<<<ceilDiv(warps, 4), 128, 0, st>>>(t.geom, t.nodef, t.level_nodes, first, last, 0,
+                t.nl_defer,
                 t.walk_scratch, NL_STAGE, t.nl_pool, t.nl_capacity, t.nl_kept[1 - parity], t.nl_kept[parity],
                 t.nl_kept_capacity, t.nl_meta, t.nl_counters, parity, devError);
             const uint32_t dWarps = std::min(last - first, deferWarps);
-            listLevelKernel<<<ceilDiv(dWarps, 4), 128, 0, st>>>(t.geom, t.nodef, first, last, 1, t.nl_defer,
+            listLevelKernel<<<ceilDiv(dWarps, 4), 128, 0, st>>>(t.geom, t.nodef, t.level_nodes, first, last, 1,
+                t.nl_defer,
                 t.walk_scratch, NL_STAGE_DEFER, t.nl_pool, t.nl_capacity, t.nl_kept[1 - parity], t.nl_kept[parity],
                 t.nl_kept_capacity, t.nl_meta, t.nl_counters, parity, devError);
             t.walk_launches += 2;

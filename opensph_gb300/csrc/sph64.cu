@@ -577,7 +577,9 @@ __device__ __forceinline__ void kahanAdd(double& sum, double& c, double x) {
     sum = t;
 }
 
-__global__ void totalsKernel(DState s, double* partial) {
+// omega: frame frequency about z (TotalMomentum / TotalAngularMomentum(omega), core/physics/Integrals.cpp:24-62):
+// the momenta use v + omega x r; the kinetic energy uses v alone, as TotalEnergy does
+__global__ void totalsKernel(DState s, double omega, double* partial) {
     double sum[9], comp[9];
     for (int k = 0; k < 9; ++k) {
         sum[k] = 0.;
@@ -586,12 +588,13 @@ __global__ void totalsKernel(DState s, double* partial) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < s.n; i += gridDim.x * blockDim.x) {
         const dbl4 r = s.r[i], v = s.v[i];
         const double m = s.m[i];
-        kahanAdd(sum[0], comp[0], m * v.x);
-        kahanAdd(sum[1], comp[1], m * v.y);
-        kahanAdd(sum[2], comp[2], m * v.z);
-        kahanAdd(sum[3], comp[3], m * (r.y * v.z - r.z * v.y));
-        kahanAdd(sum[4], comp[4], m * (r.z * v.x - r.x * v.z));
-        kahanAdd(sum[5], comp[5], m * (r.x * v.y - r.y * v.x));
+        const double wx = v.x - omega * r.y, wy = v.y + omega * r.x, wz = v.z;
+        kahanAdd(sum[0], comp[0], m * wx);
+        kahanAdd(sum[1], comp[1], m * wy);
+        kahanAdd(sum[2], comp[2], m * wz);
+        kahanAdd(sum[3], comp[3], m * (r.y * wz - r.z * wy));
+        kahanAdd(sum[4], comp[4], m * (r.z * wx - r.x * wz));
+        kahanAdd(sum[5], comp[5], m * (r.x * wy - r.y * wx));
         kahanAdd(sum[6], comp[6], 0.5 * m * (v.x * v.x + v.y * v.y + v.z * v.z));
         kahanAdd(sum[7], comp[7], m * s.u[i]);
         kahanAdd(sum[8], comp[8], m);
@@ -708,8 +711,8 @@ void launchStepEnd(double* dt, double* dtMin, double maxDt, double maxChange, do
     stepEndKernel<<<1, 1, 0, st>>>(dt, dtMin, maxDt, maxChange, time, criterion ? 1 : 0);
 }
 
-void launchTotals(const DState& s, double* partial, double* out, cudaStream_t st) {
-    totalsKernel<<<TOT_BLOCKS, TOT_THREADS, 0, st>>>(s, partial);
+void launchTotals(const DState& s, double omega, double* partial, double* out, cudaStream_t st) {
+    totalsKernel<<<TOT_BLOCKS, TOT_THREADS, 0, st>>>(s, omega, partial);
     totalsFinish<<<1, 32, 0, st>>>(partial, out);
 }
 

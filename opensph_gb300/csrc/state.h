@@ -200,9 +200,20 @@ struct BhSegment {
     double lo[3], hi[3];
 };
 
-// multi-CTA split of large k-d tree segments
-constexpr uint32_t BH_CHUNK = 4096;          // elements per chunk
-constexpr uint32_t BH_SMALL_SEGMENT = 16384; // segments up to this size are split by one CTA
+// k-d tree build: deepest level of a node (the level lists of the mixed walk), and the device counters of the
+// build (Tree::counters)
+constexpr uint32_t TREE_MAX_LEVELS = 512;
+enum : int {
+    C_NODES = 0,
+    C_LEAVES = 1,
+    C_QUEUE = 2,     // segments in the queue of the per-warp subtree splits
+    C_TAKEN = 3,     // queue entries taken
+    C_R1_LEVELS = 4, // levels of the multi-CTA phase that had segments
+    C_DEPTH = 5,     // deepest node level + 1
+    C_SEGS = 6,      // [6], [7]: multi-CTA segment counts of two consecutive levels (by parity)
+    C_CHUNKS = 8,    // [8], [9]: chunk counts of two consecutive levels (by parity)
+    C_WORDS = 16
+};
 
 struct BhChunk {
     uint32_t seg;    // segment index in the level's list
@@ -232,15 +243,21 @@ struct Tree {
     uint32_t node_capacity = 0;
     uint32_t seg_capacity = 0;
     uint32_t* idx = nullptr;          // permutation of particles (KdTree::idxs)
+    unsigned long long* keys = nullptr; // order keys of x, y, z in tree order (3 x n), moved with idx
     uint32_t* scratch_b = nullptr;    // positions of elements above the split (per segment)
     uint32_t* scratch_s = nullptr;    // positions of elements below the split
     BhNodeGeom* geom = nullptr;
     BhNodeMoments* mom = nullptr;
-    BhSegment* seg[2] = { nullptr, nullptr };
-    uint32_t* counters = nullptr;     // device: [0] node count, [1] next-level segment count, [2] leaf count
-    uint32_t* counters_host = nullptr; // pinned mirror
-    uint32_t* level_info = nullptr;   // device: per batched deep level, node count at its start and segment count
-    uint32_t* level_host = nullptr;   // pinned mirror of level_info
+    BhSegment* seg[2] = { nullptr, nullptr }; // multi-CTA phase: segments of two consecutive levels
+    BhSegment* queue = nullptr;       // segments split to their leaves by one warp each
+    uint32_t* counters = nullptr;     // device: C_NODES ...
+    uint32_t* info_host = nullptr;    // pinned: the counters and the level counts after a build
+    uint32_t* level_count = nullptr;  // device: nodes per level
+    uint32_t* level_first_dev = nullptr; // device: first entry of each level in level_nodes
+    uint32_t* level_cursor = nullptr; // device: scatter cursors
+    uint32_t* level_nodes = nullptr;  // device: node ids ordered by level
+    std::vector<uint32_t> level_first; // host: first entry of each level in level_nodes (+ the total)
+    uint32_t r1_levels = 0;           // multi-CTA levels the last build used
     uint32_t* leaves = nullptr;       // leaf node ids
     uint32_t* visits = nullptr;       // per node: children finished (bottom-up moments)
     int32_t* walk_scratch = nullptr;  // per-warp checklists
@@ -269,7 +286,6 @@ struct Tree {
     uint32_t* chunk_off_b = nullptr;
     uint32_t* chunk_off_s = nullptr;
     BhSegWork* work = nullptr;
-    std::vector<uint32_t> level_start; // host: first node id of each level
     uint32_t node_count = 0;
     uint32_t leaf_count = 0;
     uint32_t launches = 0;            // kernels launched by the last build
@@ -307,7 +323,7 @@ void launchLeapFrogKick(const DState& s, const Physics& ph, const MaterialD* mat
 // end of a step: time += dt; with criterion, dt = the criteria minimum capped by max_dt and max_change
 void launchStepEnd(double* dt, double* dt_min, double max_dt, double max_change, double* time, bool criterion,
     cudaStream_t st);
-void launchTotals(const DState& s, double* partial, double* out, cudaStream_t st);
+void launchTotals(const DState& s, double omega, double* partial, double* out, cudaStream_t st);
 void launchCheckFinite(const DState& s, unsigned long long* first_bad, cudaStream_t st);
 void launchAddGravity(const DState& s, cudaStream_t st);
 void launchPairSumMixed(const DState& s, const Grid& g, const Physics& ph, const MaterialD* mats,
@@ -321,11 +337,17 @@ void launchCorrectionMixed(const DState& s, const Grid& g, const Physics& ph, co
 cudaError_t treeAllocate(Tree& t, uint32_t n, uint32_t leaf_size);
 void treeFree(Tree& t);
 cudaError_t treeBuild(const DState& s, Tree& t, const Physics& ph, uint32_t* dev_error, cudaStream_t st);
+// (treebuild.cu) the build's own buffers, and the chunk capacity of the multi-CTA phase for n particles
+cudaError_t treeBuildAllocate(Tree& t, uint32_t n);
+void treeBuildFree(Tree& t);
+uint32_t treeChunkCapacity(uint32_t n);
+// (gravity.cu, gravity32.cu) moments and FP32 node records of a tree whose node and leaf counts are on the device
+void launchMomentsDev(const DState& s, Tree& t, const Physics& ph, bool mixed, cudaStream_t st);
+void launchPrepareWalkDev(const DState& s, Tree& t, const Physics& ph, cudaStream_t st);
 // forms the FP64 moments of a tree built with FP32 moments (for the FP64 point evaluation)
 void treeEnsureFp64Moments(const DState& s, Tree& t, const Physics& ph, cudaStream_t st);
 void launchGravityWalk(const DState& s, Tree& t, const Physics& ph, const double* lut_grad, uint32_t* dev_error,
     cudaStream_t st);
-void launchPrepareWalk(const DState& s, Tree& t, const Physics& ph, cudaStream_t st);
 void launchGravityWalkMixed(const DState& s, Tree& t, const Physics& ph, const float* lut_grad_f,
     uint32_t* dev_error, cudaStream_t st);
 void launchGravityPoints(const DState& s, const Tree& t, const Physics& ph, const double* lut_grad,

@@ -59,6 +59,7 @@ def library():
     lib.sphgpu_set_time.argtypes = [h, ctypes.c_double]
     lib.sphgpu_set_timestep.argtypes = [h, ctypes.c_double]
     lib.sphgpu_totals.argtypes = [h, _F8P]
+    lib.sphgpu_totals_frame.argtypes = [h, ctypes.c_double, _F8P]
     lib.sphgpu_check_finite.argtypes = [h, ctypes.POINTER(ctypes.c_uint64)]
     lib.sphgpu_set_profiling.argtypes = [h, ctypes.c_int32]
     lib.sphgpu_phase_times.argtypes = [h, _F8P, ctypes.POINTER(ctypes.c_uint64)]
@@ -281,9 +282,14 @@ class GpuSolver:
         self._check(self._lib.sphgpu_gravity_interactions(self._h, out))
         return list(out)
 
-    def totals(self):
+    def totals(self, frame_frequency=None):
+        """Momentum (3), angular momentum (3), kinetic and internal energy and mass; with a frame frequency the
+        momenta of the frame rotating about z (TotalMomentum / TotalAngularMomentum(omega))."""
         out = np.zeros(9)
-        self._check(self._lib.sphgpu_totals(self._h, out.ctypes.data_as(_F8P)))
+        if frame_frequency is None:
+            self._check(self._lib.sphgpu_totals(self._h, out.ctypes.data_as(_F8P)))
+        else:
+            self._check(self._lib.sphgpu_totals_frame(self._h, float(frame_frequency), out.ctypes.data_as(_F8P)))
         return out
 
     PHASES = ["predict", "gravity_build", "gravity_eval", "neighbors", "sph_eval", "correct", "collide"]

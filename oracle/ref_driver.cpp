@@ -15,6 +15,7 @@
 #include "gravity/BruteForceGravity.h"
 #include "gravity/Moments.h"
 #include "gravity/NBodySolver.h"
+#include "physics/Integrals.h"
 #include "objects/finders/KdTree.h"
 #include "sph/kernel/GravityKernel.h"
 
@@ -23,6 +24,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -213,8 +215,170 @@ void randomVelocities(Storage& s, uint64_t seed, double sigma) {
     }
 }
 
+// Trajectory runs at the benchmark's sizes ("<kind>_traj" modes): every gDumpEvery steps (and after the first)
+// the state of a seeded sample of gSample particles, the maximum magnitude, sum and sum of squares of every
+// component over all particles, and the reference's integrals, so that a fixture stays small at 10^5 particles.
+int gDumpEvery = 0;
+int gSample = 0;
+// frame frequency of the second set of integrals (TotalMomentum / TotalAngularMomentum / TotalEnergy(omega))
+constexpr double TRAJ_FRAME_OMEGA = 1.e-4;
+
+struct Sampler {
+    std::vector<Size> idx;
+    void f64(Writer& w, const std::string& name, const std::vector<double>& all, int comps) {
+        const Size n = all.size() / comps;
+        std::vector<double> pick, mx(comps, 0.), sum(comps, 0.), sum2(comps, 0.);
+        for (Size i : idx) {
+            for (int c = 0; c < comps; ++c) {
+                pick.push_back(all[comps * i + c]);
+            }
+        }
+        for (Size i = 0; i < n; ++i) {
+            for (int c = 0; c < comps; ++c) {
+                const double x = all[comps * i + c];
+                mx[c] = std::max(mx[c], std::fabs(x));
+                sum[c] += x;
+                sum2[c] += x * x;
+            }
+        }
+        w.f64(name, pick);
+        w.f64(name + "@max", mx);
+        w.f64(name + "@sum", sum);
+        w.f64(name + "@sum2", sum2);
+    }
+    void u32(Writer& w, const std::string& name, const std::vector<uint32_t>& all) {
+        std::vector<uint32_t> pick;
+        double sum = 0.;
+        for (Size i : idx) {
+            pick.push_back(all[i]);
+        }
+        for (uint32_t x : all) {
+            sum += x;
+        }
+        w.u32(name, pick);
+        w.scalar(name + "@sum", sum);
+    }
+};
+
+void dumpIntegrals(Writer& w, const std::string& pre, const Storage& s) {
+    for (int k = 0; k < 2; ++k) {
+        const double omega = k == 0 ? 0. : TRAJ_FRAME_OMEGA;
+        const std::string suffix = k == 0 ? "" : "_frame";
+        const Vector p = TotalMomentum(omega).evaluate(s);
+        const Vector L = TotalAngularMomentum(omega).evaluate(s);
+        w.f64(pre + "momentum" + suffix, { p[X], p[Y], p[Z] });
+        w.f64(pre + "angular_momentum" + suffix, { L[X], L[Y], L[Z] });
+        w.scalar(pre + "energy" + suffix, TotalEnergy(omega).evaluate(s));
+    }
+    w.scalar(pre + "kinetic_energy", TotalKineticEnergy().evaluate(s));
+    w.scalar(pre + "internal_energy", TotalInternalEnergy().evaluate(s));
+}
+
+void dumpSampled(Writer& w, const std::string& pre, Storage& s, Sampler& smp) {
+    ArrayView<const Vector> r, v, dv;
+    tie(r, v, dv) = s.getAll<Vector>(QuantityId::POSITION);
+    smp.f64(w, pre + "r", vec4(r), 4);
+    smp.f64(w, pre + "v", vec4(v), 4);
+    smp.f64(w, pre + "dv", vec4(dv), 4);
+    {
+        ArrayView<const Float> rho, drho;
+        tie(rho, drho) = s.getAll<Float>(QuantityId::DENSITY);
+        smp.f64(w, pre + "rho", flt(rho), 1);
+        smp.f64(w, pre + "drho", flt(drho), 1);
+    }
+    {
+        ArrayView<const Float> u, du;
+        tie(u, du) = s.getAll<Float>(QuantityId::ENERGY);
+        smp.f64(w, pre + "u", flt(u), 1);
+        smp.f64(w, pre + "du", flt(du), 1);
+    }
+    smp.f64(w, pre + "p", flt(s.getValue<Float>(QuantityId::PRESSURE)), 1);
+    smp.f64(w, pre + "cs", flt(s.getValue<Float>(QuantityId::SOUND_SPEED)), 1);
+    if (s.has(QuantityId::NEIGHBOR_CNT)) {
+        smp.u32(w, pre + "ncnt", sz(s.getValue<Size>(QuantityId::NEIGHBOR_CNT)));
+    }
+    if (s.has(QuantityId::DEVIATORIC_STRESS)) {
+        ArrayView<const TracelessTensor> S, dS;
+        tie(S, dS) = s.getAll<TracelessTensor>(QuantityId::DEVIATORIC_STRESS);
+        smp.f64(w, pre + "S", traceless(S), 5);
+        smp.f64(w, pre + "dS", traceless(dS), 5);
+    }
+    if (s.has(QuantityId::DAMAGE)) {
+        ArrayView<const Float> D, dD;
+        tie(D, dD) = s.getAll<Float>(QuantityId::DAMAGE);
+        smp.f64(w, pre + "D", flt(D), 1);
+        smp.f64(w, pre + "dD", flt(dD), 1);
+    }
+    dumpIntegrals(w, pre, s);
+}
+
 // Runs `steps` time steps, dumping the state after the first step and at the end, plus the dt sequence.
+void runSteps(Writer& w, RunSettings& settings, SharedPtr<Storage> storage, int steps);
+
+// Trajectory variant of runSteps: the full initial state, then sampled dumps (see Sampler) after step 1 and
+// every gDumpEvery steps.
+void runTrajectory(Writer& w, RunSettings& settings, SharedPtr<Storage> storage, int steps) {
+    SharedPtr<IScheduler> scheduler = Factory::getScheduler(settings);
+    AutoPtr<ISolver> solver = Factory::getSolver(*scheduler, settings);
+    for (Size k = 0; k < storage->getMaterialCnt(); ++k) {
+        solver->create(*storage, storage->getMaterial(k));
+    }
+    dumpMaterials(w, *storage);
+    const Size n = storage->getParticleCnt();
+    Sampler smp;
+    {
+        // gSample distinct indices, sorted; a seeded partial Fisher-Yates shuffle
+        SplitMix rng{ 99 };
+        std::vector<Size> perm(n);
+        for (Size i = 0; i < n; ++i) {
+            perm[i] = i;
+        }
+        const Size k = std::min<Size>(Size(gSample), n);
+        for (Size i = 0; i < k; ++i) {
+            const Size j = i + Size(rng.next() % uint64_t(n - i));
+            std::swap(perm[i], perm[j]);
+        }
+        smp.idx.assign(perm.begin(), perm.begin() + k);
+        std::sort(smp.idx.begin(), smp.idx.end());
+        w.u32("sample_idx", std::vector<uint32_t>(smp.idx.begin(), smp.idx.end()));
+    }
+    {
+        AutoPtr<ISolver> probeSolver = Factory::getSolver(*scheduler, settings);
+        Storage probe = storage->clone(VisitorEnum::ALL_BUFFERS);
+        probe.zeroHighestDerivatives(*scheduler);
+        Statistics stats;
+        stats.set(StatisticsId::RUN_TIME, 0._f);
+        probeSolver->integrate(probe, stats);
+        dumpSampled(w, "d0_", probe, smp);
+    }
+    AutoPtr<ITimeStepping> ts = Factory::getTimeStepping(settings, storage);
+    dumpState(w, "s0_", *storage);
+    dumpIntegrals(w, "s0_", *storage);
+    std::vector<double> dts;
+    std::vector<uint32_t> dumped;
+    Statistics stats;
+    double t = 0.;
+    for (int step = 0; step < steps; ++step) {
+        dts.push_back(ts->getTimeStep());
+        stats.set(StatisticsId::RUN_TIME, t);
+        t += ts->getTimeStep();
+        ts->step(*scheduler, *solver, stats);
+        const int done = step + 1;
+        if (done == 1 || done % gDumpEvery == 0 || done == steps) {
+            dumpSampled(w, "t" + std::to_string(done) + "_", *storage, smp);
+            dumped.push_back(uint32_t(done));
+        }
+    }
+    dts.push_back(ts->getTimeStep());
+    w.f64("dts", dts);
+    w.u32("dumped_steps", dumped);
+}
+
 void runSteps(Writer& w, RunSettings& settings, SharedPtr<Storage> storage, int steps) {
+    if (gDumpEvery > 0) {
+        runTrajectory(w, settings, storage, steps);
+        return;
+    }
     SharedPtr<IScheduler> scheduler = Factory::getScheduler(settings);
     AutoPtr<ISolver> solver = Factory::getSolver(*scheduler, settings);
     for (Size k = 0; k < storage->getMaterialCnt(); ++k) {
@@ -632,6 +796,17 @@ int main(int argc, char** argv) {
     if (mode.size() > 5 && mode.compare(mode.size() - 5, 5, "_asym") == 0) {
         gAsymmetric = true;
         mode = mode.substr(0, mode.size() - 5);
+    }
+    if (mode.size() > 5 && mode.compare(mode.size() - 5, 5, "_traj") == 0) {
+        // the last two arguments: dump interval and sample size
+        gSample = std::atoi(argv[argc - 1]);
+        gDumpEvery = std::atoi(argv[argc - 2]);
+        argc -= 2;
+        mode = mode.substr(0, mode.size() - 5);
+        if (gDumpEvery <= 0 || gSample <= 0) {
+            std::fprintf(stderr, "trajectory mode needs a positive dump interval and sample size\n");
+            return 2;
+        }
     }
     auto arg = [&](int k, double dflt) { return argc > k ? std::atof(argv[k]) : dflt; };
     try {

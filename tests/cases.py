@@ -25,7 +25,7 @@ def kind(fx):
     """Physics of the fixture (sphere, impact, gas, ...), without the "_all" suffix of the runs with every
     time-step criterion."""
     k = str(fx["driver_args"]).split()[0]
-    for suffix in ("_cached", "_all", "_asym"):
+    for suffix in ("_traj", "_cached", "_all", "_asym"):
         if k.endswith(suffix):
             k = k[:-len(suffix)]
     return k

@@ -35,6 +35,11 @@ FIXTURES = {
     "impact_asym_n1200": ["impact_asym", "1200", "5e4", "80", "5e3", "4", "5e3", "45"],
     # the basalt sphere with CachedGravity (gravity.recomputation_period 0.35 s: recomputed at t = 0 and 0.47)
     "sphere_cached_n1000": ["sphere_cached", "1000", "1e4", "6", "1", "0.35"],
+    # trajectories at the benchmark's sizes (mode "<kind>_traj", last two arguments: dump interval, sample):
+    # the basalt sphere of 10,000 requested particles (10,648 on the lattice), 100 steps, dumped every 10;
+    # the solid impact of 200,000 + 5,000 requested particles (217,823), 10 steps, dumped after 1, 5 and 10
+    "sphere_traj_n10648": ["sphere_traj", "10000", "1e4", "100", "1", "10", "1024"],
+    "impact_traj_n217823": ["impact_traj", "200000", "5e4", "5000", "5e3", "10", "5e3", "45", "5", "2048"],
     # gravity only: Plummer sphere, BH theta 0.5 octupole vs brute force
     "gravity_n3000": ["gravity", "3000", "0.5", "7", "1e-3"],
     "gravity_n3000_t07": ["gravity", "3000", "0.7", "11", "1e-2"],

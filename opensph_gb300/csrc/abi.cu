@@ -418,10 +418,17 @@ sphgpu_status evalDerivatives(sphgpu_handle* h) {
     }
     CUDA_TRY(h, cudaEventRecord(h->ev_fork, h->stream));
     CUDA_TRY(h, cudaStreamWaitEvent(h->gstream, h->ev_fork, 0));
-    // the pair loop is queued before the tree build, whose host-side level loop would otherwise delay it (running
-    // it only after the build, concurrently with the walk alone, measured 15.1 instead of 13.8 ms per step)
-    evalSph(h, false);
-    const sphgpu_status st = evalGravity(h, h->gstream);
+    // The material update and the neighbour grid (short kernels) run beside the tree build; the pair loop is queued
+    // once the build has returned (it reads its level counts on the host), so that it runs beside the walk: the
+    // build is a chain of small dependent launches, which the pair loop's long-lived blocks would otherwise hold
+    // off the SMs.
+    evalSphPrepare(h);
+    sphgpu_status st = evalGravityBuild(h, h->gstream);
+    if (st != SPHGPU_OK) {
+        return st;
+    }
+    evalSphPairs(h, false);
+    st = evalGravityWalk(h, h->gstream);
     if (st != SPHGPU_OK) {
         return st;
     }

@@ -569,12 +569,6 @@ cudaError_t treeAllocate(Tree& t, uint32_t n, uint32_t leafSize) {
     alloc((void**)&t.stats, 8 * sizeof(unsigned long long)); // 4 interaction counters, [4] next leaf of the walk
     alloc((void**)&t.bbox, 8 * sizeof(unsigned long long));
     alloc((void**)&t.nodef, size_t(t.node_capacity) * NODEF * sizeof(float));
-    t.chunk_capacity = treeChunkCapacity(nn);
-    alloc((void**)&t.chunks, size_t(t.chunk_capacity) * sizeof(BhChunk));
-    alloc((void**)&t.chunk_stats, size_t(t.chunk_capacity) * sizeof(BhChunkStats));
-    alloc((void**)&t.chunk_off_b, size_t(t.chunk_capacity) * sizeof(uint32_t));
-    alloc((void**)&t.chunk_off_s, size_t(t.chunk_capacity) * sizeof(uint32_t));
-    alloc((void**)&t.work, size_t(t.seg_capacity) * sizeof(BhSegWork));
     alloc((void**)&t.pf, nn * sizeof(float4));
     alloc((void**)&t.mf, nn * sizeof(float));
     if (e == cudaSuccess) {
@@ -586,7 +580,7 @@ cudaError_t treeAllocate(Tree& t, uint32_t n, uint32_t leafSize) {
 void treeFree(Tree& t) {
     void* ptrs[] = { t.idx, t.scratch_b, t.scratch_s, t.geom, t.mom, t.seg[0], t.seg[1], t.counters, t.leaves, t.visits,
         t.walk_scratch, t.nl_pool, t.nl_kept[0], t.nl_kept[1], t.nl_meta, t.nl_counters, t.nl_defer, t.stats, t.bbox,
-        t.nodef, t.pf, t.mf, t.chunks, t.chunk_stats, t.chunk_off_b, t.chunk_off_s, t.work };
+        t.nodef, t.pf, t.mf };
     for (void* p : ptrs) {
         if (p) {
             cudaFree(p);

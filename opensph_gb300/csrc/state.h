@@ -239,11 +239,20 @@ struct BhSegWork {
     unsigned long long minv, maxv; // orderKey of the extremes
 };
 
+// One particle of the k-d tree build: the order keys of its coordinates and its index, one 32-byte sector, so
+// that a swap of the partition moves one sector per side
+struct alignas(32) TreeElem {
+    unsigned long long key[3];
+    uint32_t idx;
+    uint32_t pad;
+};
+
 struct Tree {
     uint32_t node_capacity = 0;
     uint32_t seg_capacity = 0;
     uint32_t* idx = nullptr;          // permutation of particles (KdTree::idxs)
-    unsigned long long* keys = nullptr; // order keys of x, y, z in tree order (3 x n), moved with idx
+    TreeElem* elems = nullptr;        // build: order keys of x, y, z and the particle index, in tree order
+    unsigned long long* subtree_keys = nullptr; // build: keys (3 x n) of segments split by one warp in global memory
     uint32_t* scratch_b = nullptr;    // positions of elements above the split (per segment)
     uint32_t* scratch_s = nullptr;    // positions of elements below the split
     BhNodeGeom* geom = nullptr;
@@ -285,6 +294,7 @@ struct Tree {
     BhChunkStats* chunk_stats = nullptr;
     uint32_t* chunk_off_b = nullptr;
     uint32_t* chunk_off_s = nullptr;
+    uint32_t* chunk_done = nullptr;   // per segment's first chunk: chunks finished in the two passes of a level
     BhSegWork* work = nullptr;
     uint32_t node_count = 0;
     uint32_t leaf_count = 0;

@@ -12,9 +12,10 @@
 // are out of order; this is what a block scan (ranks) and a binary search (K, the predicate is monotone)
 // compute in parallel.
 //
-// Layout: idx (KdTree::idxs) and the order keys of x, y and z of the particles in tree order
-// (keys[d * n + k] = orderKey(r[idx[k]][d]), moved together with idx by every swap), so that every pass over
-// a segment reads contiguous memory on the integer pipe.
+// Layout: the particles in tree order as 32-byte elements (order keys of x, y and z, and the particle index:
+// elems[k] = {orderKey(r[i][0..2]), i} with i = idx[k]), so that every pass over a segment reads contiguous
+// memory on the integer pipe and a swap of the partition moves one sector per side; idx (KdTree::idxs) is
+// written from them at the end.
 //
 // Two phases, with no host round trip between levels:
 //   1. segments of more than SUBTREE_MAX elements, level by level over all of them at once, a chunk of
@@ -38,12 +39,14 @@ namespace sphgpu {
 
 namespace {
 
+// 128-thread blocks, so that a block fits where one block of the concurrently running pair loop retired
 constexpr uint32_t R1_CHUNK = 2048;    // elements per CTA in phase 1
-constexpr int R1_THREADS = 256;
+constexpr int R1_THREADS = 128;
 constexpr int R1_PER_THREAD = int(R1_CHUNK) / R1_THREADS;
+constexpr int SWAP_THREADS = 512;      // the swaps of a chunk, four per thread
 constexpr uint32_t SUBTREE_MAX = 512;  // segments up to this size are split to their leaves by one warp
 constexpr int R2_WARPS = 4;            // warps per CTA of the subtree kernel
-constexpr int R2_STACK = 64;           // pending segments per warp
+constexpr int R2_STACK = 36;           // pending segments per warp
 
 __device__ __forceinline__ int argMax3(const double s[3]) {
     int m = 0;
@@ -58,6 +61,11 @@ __device__ __forceinline__ int argMax3(const double s[3]) {
 
 __device__ __forceinline__ double coord(const dbl4* __restrict__ r, uint32_t i, int dim) {
     return __ldg(reinterpret_cast<const double*>(r) + 4 * size_t(i) + dim);
+}
+
+// the double of an order key (the inverse of orderKey; -0 was mapped to the key of +0)
+__device__ __forceinline__ double keyValue(unsigned long long k) {
+    return doubleUnflip(k);
 }
 
 // ---------------------------------------------------------------------------------------------------------
@@ -335,17 +343,93 @@ __global__ void boundsKernel(const dbl4* __restrict__ r, uint32_t n, unsigned lo
     }
 }
 
-// idx = identity, the keys of the particles, and the root segment (box = bounding box of all points, as
-// KdTree::buildImpl) in the phase-1 list or, for a small set, in the phase-2 queue
-__global__ void rootKernel(const dbl4* __restrict__ r, uint32_t n, uint32_t* idx, unsigned long long* keys,
-    BhSegment* seg0, BhSegment* queue, BhNodeGeom* geom, uint32_t* counters, const unsigned long long* bounds) {
+__device__ __forceinline__ TreeElem makeElem(const dbl4* __restrict__ r, uint32_t i) {
+    const dbl4 p = r[i];
+    TreeElem e;
+    e.key[0] = orderKey(p.x);
+    e.key[1] = orderKey(p.y);
+    e.key[2] = orderKey(p.z);
+    e.idx = i;
+    e.pad = 0;
+    return e;
+}
+
+__device__ __forceinline__ void swapElements(TreeElem* elems, uint32_t a, uint32_t b) {
+    const TreeElem x = elems[a], y = elems[b];
+    elems[a] = y;
+    elems[b] = x;
+}
+
+// std::nth_element of the segment [from, to) by coordinate d (KdTree::buildTree's fallback), on the particle
+// indices copied to scratch; the elements are then rebuilt from the positions
+__device__ void nthElementSegment(const dbl4* __restrict__ r, TreeElem* elems, uint32_t* scratch, uint32_t from,
+    uint32_t to, uint32_t nth, int d) {
+    for (uint32_t k = from; k < to; ++k) {
+        scratch[k] = elems[k].idx;
+    }
+    NthCtx ctx{ scratch, r, d };
+    nthElement(ctx, long(from), long(nth), long(to));
+    for (uint32_t k = from; k < to; ++k) {
+        elems[k] = makeElem(r, scratch[k]);
+    }
+}
+
+// Phase-1 arrays of one level parity (segments, their chunks and the per-chunk results); the level after next
+// reuses them.
+struct LevelBufs {
+    BhSegment* seg;        // segments of the level
+    BhChunk* chunks;       // chunks of the level, contiguous per segment
+    BhChunkStats* stats;   // per chunk
+    uint32_t* offB;        // per chunk: elements above the split before the chunk, within its segment
+    uint32_t* offS;
+    uint32_t* done;        // per segment's first chunk: chunks done in the statistics [0] and rank [cap] passes
+};
+
+// queues a phase-1 segment (more than SUBTREE_MAX elements) with its chunks into the level buffers `b` of
+// parity q, or a smaller one into the phase-2 queue
+__device__ void pushSegment(const BhSegment& sg, LevelBufs b, int q, uint32_t* counters, uint32_t chunkCapacity,
+    uint32_t segCapacity, BhSegment* queue, uint32_t* devError) {
+    const uint32_t len = sg.to - sg.from;
+    if (len <= SUBTREE_MAX) {
+        const uint32_t slot = atomicAdd(&counters[C_QUEUE], 1u);
+        if (slot < segCapacity) {
+            queue[slot] = sg;
+        } else {
+            atomicOr(devError, uint32_t(DEV_ERR_SEGMENT_CAPACITY));
+        }
+        return;
+    }
+    const uint32_t slot = atomicAdd(&counters[C_SEGS + q], 1u);
+    const uint32_t nc = (len + R1_CHUNK - 1) / R1_CHUNK;
+    const uint32_t c0 = atomicAdd(&counters[C_CHUNKS + q], nc);
+    if (slot >= segCapacity || c0 + nc > chunkCapacity) {
+        atomicOr(devError, uint32_t(DEV_ERR_SEGMENT_CAPACITY));
+        // the segment still gets its leaves, by one warp in phase 2
+        const uint32_t qs = atomicAdd(&counters[C_QUEUE], 1u);
+        if (qs < segCapacity) {
+            queue[qs] = sg;
+        }
+        return;
+    }
+    b.seg[slot] = sg;
+    for (uint32_t k = 0; k < nc; ++k) {
+        b.chunks[c0 + k].seg = slot;
+        b.chunks[c0 + k].index = k;
+        b.chunks[c0 + k].first = c0;
+        b.chunks[c0 + k].count = nc;
+    }
+    b.done[c0] = 0;
+    b.done[chunkCapacity + c0] = 0;
+}
+
+// the elements of the particles in index order, and the root segment (box = bounding box of all points, as
+// KdTree::buildImpl) in the phase-1 buffers or, for a small set, in the phase-2 queue
+__global__ void rootKernel(const dbl4* __restrict__ r, uint32_t n, TreeElem* elems, LevelBufs b0, BhSegment* queue,
+    BhNodeGeom* geom, uint32_t* counters, uint32_t chunkCapacity, uint32_t segCapacity,
+    const unsigned long long* bounds, uint32_t* devError) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
-        idx[i] = i;
-        const dbl4 p = r[i];
-        keys[i] = orderKey(p.x);
-        keys[size_t(n) + i] = orderKey(p.y);
-        keys[2 * size_t(n) + i] = orderKey(p.z);
+        elems[i] = makeElem(r, i);
     }
     if (i == 0) {
         BhSegment s;
@@ -364,59 +448,74 @@ __global__ void rootKernel(const dbl4* __restrict__ r, uint32_t n, uint32_t* idx
         }
         counters[C_NODES] = 1;
         counters[C_DEPTH] = 1;
-        if (n > SUBTREE_MAX) {
-            seg0[0] = s;
-            counters[C_SEGS] = 1;
-        } else {
-            queue[0] = s;
-            counters[C_QUEUE] = 1;
-        }
+        pushSegment(s, b0, 0, counters, chunkCapacity, segCapacity, queue, devError);
     }
 }
 
 // ---------------------------------------------------------------------------------------------------------
-// phase 1: segments of more than SUBTREE_MAX elements, one level per launch sequence
+// phase 1: segments of more than SUBTREE_MAX elements, three launches per level. The CTA that completes the
+// last chunk of a segment in a pass (an atomic count per segment after a memory fence; nothing waits) does that
+// segment's per-segment step: the split decision after the statistics, the partition count K, the sliding
+// midpoint or nth_element and the children after the ranks.
 // ---------------------------------------------------------------------------------------------------------
 
-// the chunks of every segment of the level (contiguous per segment); also clears the next level's counters
-__global__ void chunkListKernel(const BhSegment* __restrict__ segIn, uint32_t* counters, int parity, BhChunk* chunks,
-    uint32_t chunkCapacity, uint32_t segCapacity, uint32_t* devError) {
-    const uint32_t nIn = min(counters[C_SEGS + parity], segCapacity);
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        counters[C_SEGS + 1 - parity] = 0;
-        if (nIn > 0) {
-            counters[C_R1_LEVELS]++;
+// exclusive prefix sum over the R1_THREADS threads of a block
+__device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t* sh) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
+        if (lane >= off) {
+            x += y;
         }
     }
-    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < nIn; s += gridDim.x * blockDim.x) {
-        const uint32_t len = segIn[s].to - segIn[s].from;
-        const uint32_t nc = (len + R1_CHUNK - 1) / R1_CHUNK;
-        const uint32_t c0 = atomicAdd(&counters[C_CHUNKS + parity], nc);
-        if (c0 + nc > chunkCapacity) {
-            atomicOr(devError, uint32_t(DEV_ERR_SEGMENT_CAPACITY));
-            continue;
-        }
-        for (uint32_t k = 0; k < nc; ++k) {
-            chunks[c0 + k].seg = s;
-            chunks[c0 + k].index = k;
-            chunks[c0 + k].first = c0;
-            chunks[c0 + k].count = nc;
-        }
+    if (lane == 31) {
+        sh[warp] = x;
     }
+    __syncthreads();
+    uint32_t before = 0;
+    for (int w = 0; w < warp; ++w) {
+        before += sh[w];
+    }
+    __syncthreads();
+    return before + x - v;
 }
 
-// per chunk and candidate dimension: elements above / below the box centre and the extremes (first position)
-__global__ void __launch_bounds__(R1_THREADS) chunkStatsKernel(const unsigned long long* __restrict__ keys,
-    uint32_t n, const BhSegment* __restrict__ segIn, const BhChunk* __restrict__ chunks,
-    const uint32_t* __restrict__ counters, int parity, uint32_t chunkCapacity, BhChunkStats* stats) {
+// true in every thread of the CTA that completed the last chunk of segment `first` in pass `pass`
+__device__ __forceinline__ bool lastChunkOfSegment(uint32_t* done, uint32_t first, uint32_t count, bool* flag) {
+    __threadfence(); // this thread's results of the pass before the count
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        *flag = atomicAdd(&done[first], 1u) == count - 1;
+        if (*flag) {
+            __threadfence();
+        }
+    }
+    __syncthreads();
+    return *flag;
+}
+
+// Pass 1: per chunk and candidate dimension, the elements above / below the box centre and the extremes (first
+// position); the segment's last CTA decides the split dimension and mode and the chunk offsets. Also clears the
+// counters of the level after this one's successor (same parity as the level before).
+__global__ void __launch_bounds__(R1_THREADS) statsDecideKernel(const TreeElem* __restrict__ elems, LevelBufs b,
+    uint32_t* counters, int parity, uint32_t chunkCapacity, BhSegWork* work) {
     __shared__ uint32_t shCnt[R1_THREADS / 32][6];
     __shared__ unsigned long long shV[R1_THREADS / 32][6];
     __shared__ uint32_t shP[R1_THREADS / 32][6];
+    __shared__ bool shLast;
     const uint32_t nChunks = min(counters[C_CHUNKS + parity], chunkCapacity);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        counters[C_SEGS + 1 - parity] = 0;
+        counters[C_CHUNKS + 1 - parity] = 0;
+        if (nChunks > 0) {
+            counters[C_R1_LEVELS]++;
+        }
+    }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (uint32_t c = blockIdx.x; c < nChunks; c += gridDim.x) {
-        const BhChunk ch = chunks[c];
-        const BhSegment sg = segIn[ch.seg];
+        const BhChunk ch = b.chunks[c];
+        const BhSegment sg = b.seg[ch.seg];
         const uint32_t from = sg.from + ch.index * R1_CHUNK;
         const uint32_t to = min(sg.to, from + R1_CHUNK);
         unsigned long long center[3];
@@ -426,13 +525,15 @@ __global__ void __launch_bounds__(R1_THREADS) chunkStatsKernel(const unsigned lo
         uint32_t nb[3] = { 0, 0, 0 }, ns[3] = { 0, 0, 0 };
         unsigned long long mnv[3] = { ~0ull, ~0ull, ~0ull }, mxv[3] = { 0ull, 0ull, 0ull };
         uint32_t mnp[3] = { 0xffffffffu, 0xffffffffu, 0xffffffffu }, mxp[3] = { 0xffffffffu, 0xffffffffu, 0xffffffffu };
-#pragma unroll
+#pragma unroll 4
         for (int j = 0; j < R1_PER_THREAD; ++j) {
             const uint32_t k = from + uint32_t(j * R1_THREADS) + threadIdx.x;
             if (k < to) {
+                const ulonglong2 k01 = *reinterpret_cast<const ulonglong2*>(&elems[k].key[0]);
+                const unsigned long long xs[3] = { k01.x, k01.y, elems[k].key[2] };
 #pragma unroll
                 for (int d = 0; d < 3; ++d) {
-                    const unsigned long long x = keys[size_t(d) * n + k];
+                    const unsigned long long x = xs[d];
                     nb[d] += x > center[d] ? 1u : 0u;
                     ns[d] += x < center[d] ? 1u : 0u;
                     if (betterArg(x, k, mnv[d], mnp[d], false)) {
@@ -467,15 +568,15 @@ __global__ void __launch_bounds__(R1_THREADS) chunkStatsKernel(const unsigned lo
             constexpr int W = R1_THREADS / 32;
             BhChunkStats out;
             for (int d = 0; d < 3; ++d) {
-                uint32_t b = lane < W ? shCnt[lane][d] : 0u, s = lane < W ? shCnt[lane][3 + d] : 0u;
+                uint32_t cb = lane < W ? shCnt[lane][d] : 0u, cs = lane < W ? shCnt[lane][3 + d] : 0u;
                 unsigned long long v0 = lane < W ? shV[lane][d] : ~0ull, v1 = lane < W ? shV[lane][3 + d] : 0ull;
                 uint32_t p0 = lane < W ? shP[lane][d] : 0xffffffffu, p1 = lane < W ? shP[lane][3 + d] : 0xffffffffu;
-                b = __reduce_add_sync(0xffffffffu, b);
-                s = __reduce_add_sync(0xffffffffu, s);
+                cb = __reduce_add_sync(0xffffffffu, cb);
+                cs = __reduce_add_sync(0xffffffffu, cs);
                 warpArgExtreme(v0, p0, false);
                 warpArgExtreme(v1, p1, true);
-                out.nb[d] = b;
-                out.ns[d] = s;
+                out.nb[d] = cb;
+                out.ns[d] = cs;
                 out.diff[d] = 0;
                 out.minv[d] = v0;
                 out.minp[d] = p0;
@@ -484,40 +585,28 @@ __global__ void __launch_bounds__(R1_THREADS) chunkStatsKernel(const unsigned lo
             }
             out.pad = 0;
             if (lane == 0) {
-                stats[c] = out;
+                b.stats[c] = out;
             }
         }
-        __syncthreads();
-    }
-}
-
-// one warp per segment (the warp of its first chunk): split dimension and mode, chunk offsets of the elements
-// above / below the box centre, the extremes of the split coordinate
-__global__ void segDecideKernel(const BhSegment* __restrict__ segIn, const BhChunk* __restrict__ chunks,
-    const uint32_t* __restrict__ counters, int parity, uint32_t chunkCapacity, const BhChunkStats* __restrict__ stats,
-    uint32_t* chunkOffB, uint32_t* chunkOffS, BhSegWork* work) {
-    const uint32_t nChunks = min(counters[C_CHUNKS + parity], chunkCapacity);
-    const int lane = threadIdx.x & 31;
-    const uint32_t nWarps = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < nChunks; c += nWarps) {
-        const BhChunk ch = chunks[c];
-        if (ch.index != 0) {
+        if (!lastChunkOfSegment(b.done, ch.first, ch.count, &shLast) || warp != 0) {
             continue;
         }
-        const BhSegment sg = segIn[ch.seg];
-        // extremes of every dimension over the segment: a dimension is singular when they are equal
-        unsigned long long mnv[3] = { ~0ull, ~0ull, ~0ull }, mxv[3] = { 0ull, 0ull, 0ull };
-        uint32_t mnp[3] = { 0xffffffffu, 0xffffffffu, 0xffffffffu }, mxp[3] = { 0xffffffffu, 0xffffffffu, 0xffffffffu };
+        // the segment's decision (warp 0 of the last CTA; the other chunks' statistics are read through L2)
+        mnv[0] = mnv[1] = mnv[2] = ~0ull;
+        mxv[0] = mxv[1] = mxv[2] = 0ull;
+        mnp[0] = mnp[1] = mnp[2] = mxp[0] = mxp[1] = mxp[2] = 0xffffffffu;
         for (uint32_t k = lane; k < ch.count; k += 32) {
-            const BhChunkStats& st = stats[ch.first + k];
+            const BhChunkStats* st = &b.stats[ch.first + k];
             for (int d = 0; d < 3; ++d) {
-                if (betterArg(st.minv[d], st.minp[d], mnv[d], mnp[d], false)) {
-                    mnv[d] = st.minv[d];
-                    mnp[d] = st.minp[d];
+                const unsigned long long v0 = __ldcg(&st->minv[d]), v1 = __ldcg(&st->maxv[d]);
+                const uint32_t p0 = __ldcg(&st->minp[d]), p1 = __ldcg(&st->maxp[d]);
+                if (betterArg(v0, p0, mnv[d], mnp[d], false)) {
+                    mnv[d] = v0;
+                    mnp[d] = p0;
                 }
-                if (betterArg(st.maxv[d], st.maxp[d], mxv[d], mxp[d], true)) {
-                    mxv[d] = st.maxv[d];
-                    mxp[d] = st.maxp[d];
+                if (betterArg(v1, p1, mxv[d], mxp[d], true)) {
+                    mxv[d] = v1;
+                    mxp[d] = p1;
                 }
             }
         }
@@ -532,12 +621,12 @@ __global__ void segDecideKernel(const BhSegment* __restrict__ segIn, const BhChu
         uint32_t ob = 0, os = 0;
         for (uint32_t k0 = 0; k0 < ch.count; k0 += 32) {
             const uint32_t k = k0 + lane;
-            uint32_t nb = 0, ns = 0;
+            uint32_t cb = 0, cs = 0;
             if (k < ch.count) {
-                nb = stats[ch.first + k].nb[splitIdx];
-                ns = stats[ch.first + k].ns[splitIdx];
+                cb = __ldcg(&b.stats[ch.first + k].nb[splitIdx]);
+                cs = __ldcg(&b.stats[ch.first + k].ns[splitIdx]);
             }
-            uint32_t xb = nb, xs = ns;
+            uint32_t xb = cb, xs = cs;
             for (int off = 1; off < 32; off <<= 1) {
                 const uint32_t yb = __shfl_up_sync(0xffffffffu, xb, off), ys = __shfl_up_sync(0xffffffffu, xs, off);
                 if (lane >= off) {
@@ -546,8 +635,8 @@ __global__ void segDecideKernel(const BhSegment* __restrict__ segIn, const BhChu
                 }
             }
             if (k < ch.count) {
-                chunkOffB[ch.first + k] = ob + xb - nb;
-                chunkOffS[ch.first + k] = os + xs - ns;
+                b.offB[ch.first + k] = ob + xb - cb;
+                b.offS[ch.first + k] = os + xs - cs;
             }
             ob += __shfl_sync(0xffffffffu, xb, 31);
             os += __shfl_sync(0xffffffffu, xs, 31);
@@ -569,211 +658,166 @@ __global__ void segDecideKernel(const BhSegment* __restrict__ segIn, const BhChu
     }
 }
 
-// exclusive prefix sum over the R1_THREADS threads of a block
-__device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t* sh) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t x = v;
-    for (int off = 1; off < 32; off <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
-        if (lane >= off) {
-            x += y;
+// The segment's pair count K of the two-pointer partition (one warp: a 32-ary search of the monotone predicate
+// posB[k] >= posS[nS - 1 - k], one probe per lane and round), then, in lane 0, the sliding midpoint or
+// nth_element and the children: those of more than SUBTREE_MAX elements, with their chunks, into the next
+// level's buffers, the others into the phase-2 queue.
+__device__ void finishSegment(const dbl4* __restrict__ r, TreeElem* elems, const uint32_t* __restrict__ posB,
+    uint32_t* posScratch, const BhSegment& sg, uint32_t segSlot, BhSegWork* work, LevelBufs next, int nextParity,
+    uint32_t* counters, uint32_t chunkCapacity, uint32_t segCapacity, BhSegment* queue, BhNodeGeom* geom,
+    uint32_t nodeCapacity, uint32_t* devError, const uint32_t* __restrict__ posS) {
+    const int lane = threadIdx.x & 31;
+    BhSegWork w = work[segSlot];
+    const uint32_t from = sg.from, to = sg.to;
+    uint32_t K = 0;
+    if (w.mode == 0) {
+        const uint32_t nS = w.nS;
+        uint32_t lo = 0, hi = min(w.nB, nS);
+        while (hi > lo) {
+            const uint32_t span = hi - lo;
+            if (span <= 32u) {
+                const uint32_t k = lo + uint32_t(lane);
+                const bool pred = uint32_t(lane) < span && __ldcg(&posB[from + k]) >= __ldcg(&posS[from + nS - 1 - k]);
+                const unsigned m = __ballot_sync(0xffffffffu, pred);
+                lo = m ? lo + uint32_t(__ffs(m) - 1) : hi;
+                break;
+            }
+            // lanes probe lo + j span / 32; the first true probe bounds the answer from above, the last false one
+            // from below
+            const uint32_t k = lo + uint32_t((unsigned long long)span * uint32_t(lane) / 32u);
+            const bool pred = __ldcg(&posB[from + k]) >= __ldcg(&posS[from + nS - 1 - k]);
+            const unsigned m = __ballot_sync(0xffffffffu, pred);
+            const int j = m ? __ffs(m) - 1 : 32;
+            if (j == 0) {
+                hi = lo;
+                break;
+            }
+            const uint32_t newLo = lo + uint32_t((unsigned long long)span * uint32_t(j - 1) / 32u) + 1u;
+            const uint32_t newHi = j < 32 ? lo + uint32_t((unsigned long long)span * uint32_t(j) / 32u) : hi;
+            lo = newLo;
+            hi = newHi;
         }
+        K = lo;
     }
-    if (lane == 31) {
-        sh[warp] = x;
+    if (lane != 0) {
+        return;
     }
-    __syncthreads();
-    uint32_t before = 0;
-    for (int w = 0; w < warp; ++w) {
-        before += sh[w];
+    const int d = w.splitIdx;
+    double splitPosition = 0.5 * (sg.lo[d] + sg.hi[d]);
+    uint32_t n1;
+    bool sliding = false;
+    double cut;
+    if (w.mode == 0) {
+        const uint32_t nB = w.nB, nS = w.nS;
+        n1 = K < nB ? __ldcg(&posB[from + K]) : to;
+        if (K >= 1) {
+            n1 = min(n1, __ldcg(&posS[from + nS - K]));
+        }
+        if (n1 == from || n1 == to) {
+            // sliding midpoint (then K = 0): the extreme element to the empty side
+            const bool isMax = (n1 == to);
+            const uint32_t dst = isMax ? to - 1 : from;
+            const uint32_t src = isMax ? w.maxp : w.minp;
+            splitPosition = coord(r, elems[src].idx, d);
+            swapElements(elems, dst, src);
+            n1 = isMax ? to - 1 : from + 1;
+            sliding = true;
+        }
+        cut = splitPosition;
+    } else {
+        n1 = (from + to) >> 1;
+        if (w.mode == 1) {
+            // the rank scratch of this segment is not used in this mode
+            nthElementSegment(r, elems, posScratch, from, to, n1, d);
+        }
+        cut = coord(r, elems[n1].idx, d);
     }
-    __syncthreads();
-    return before + x - v;
+    work[segSlot].K = K;
+    BhSegment left, right;
+    if (!makeChildren(geom, counters, nodeCapacity, devError, sg, n1, d, cut, sliding, left, right)) {
+        return;
+    }
+    pushSegment(left, next, nextParity, counters, chunkCapacity, segCapacity, queue, devError);
+    pushSegment(right, next, nextParity, counters, chunkCapacity, segCapacity, queue, devError);
 }
 
-// positions of the elements above (posB) and below (posS) the split position, in segment order: R1_PER_THREAD
-// consecutive elements per thread, one block scan of their packed counts per chunk
-__global__ void __launch_bounds__(R1_THREADS) chunkRanksKernel(const unsigned long long* __restrict__ keys,
-    uint32_t n, const BhSegment* __restrict__ segIn, const BhChunk* __restrict__ chunks,
-    const uint32_t* __restrict__ counters, int parity, uint32_t chunkCapacity, const uint32_t* __restrict__ chunkOffB,
-    const uint32_t* __restrict__ chunkOffS, const BhSegWork* __restrict__ work, uint32_t* posB, uint32_t* posS) {
-    __shared__ uint32_t shScan[R1_THREADS / 32];
-    const uint32_t nChunks = min(counters[C_CHUNKS + parity], chunkCapacity);
-    for (uint32_t c = blockIdx.x; c < nChunks; c += gridDim.x) {
-        const BhChunk ch = chunks[c];
-        const BhSegWork w = work[ch.seg];
-        if (w.mode != 0) {
-            continue;
-        }
-        const BhSegment sg = segIn[ch.seg];
-        const int d = w.splitIdx;
-        const unsigned long long split = orderKey(0.5 * (sg.lo[d] + sg.hi[d]));
-        const uint32_t from = sg.from + ch.index * R1_CHUNK;
-        const uint32_t to = min(sg.to, from + R1_CHUNK);
-        const uint32_t k0 = from + threadIdx.x * R1_PER_THREAD;
-        const unsigned long long* kd = keys + size_t(d) * n;
-        uint32_t flagsB = 0, flagsS = 0;
-#pragma unroll
-        for (int j = 0; j < R1_PER_THREAD; ++j) {
-            const uint32_t k = k0 + j;
-            if (k < to) {
-                const unsigned long long x = kd[k];
-                flagsB |= (x > split ? 1u : 0u) << j;
-                flagsS |= (x < split ? 1u : 0u) << j;
-            }
-        }
-        // counts of at most R1_CHUNK fit 16 bits each
-        const uint32_t packed = (uint32_t(__popc(flagsB)) << 16) | uint32_t(__popc(flagsS));
-        const uint32_t pre = blockExclusiveScan(packed, shScan);
-        uint32_t rb = sg.from + chunkOffB[c] + (pre >> 16), rs = sg.from + chunkOffS[c] + (pre & 0xffffu);
-#pragma unroll
-        for (int j = 0; j < R1_PER_THREAD; ++j) {
-            if (flagsB & (1u << j)) {
-                posB[rb++] = k0 + j;
-            }
-            if (flagsS & (1u << j)) {
-                posS[rs++] = k0 + j;
-            }
-        }
-    }
-}
-
-__device__ __forceinline__ void swapElements(uint32_t* idx, unsigned long long* keys, size_t n, uint32_t a,
-    uint32_t b) {
-    const uint32_t t = idx[a];
-    idx[a] = idx[b];
-    idx[b] = t;
-    for (int d = 0; d < 3; ++d) {
-        const unsigned long long x = keys[d * n + a];
-        keys[d * n + a] = keys[d * n + b];
-        keys[d * n + b] = x;
-    }
-}
-
-// one thread per segment: the pair count K of the two-pointer partition, the sliding midpoint or nth_element,
-// the children; children of more than SUBTREE_MAX elements go to the next level's list, the others to the
-// phase-2 queue
-__global__ void segFinishKernel(const dbl4* __restrict__ r, uint32_t n, uint32_t* idx, unsigned long long* keys,
-    const uint32_t* __restrict__ posB, const uint32_t* __restrict__ posS, const BhSegment* __restrict__ segIn,
-    const BhChunk* __restrict__ chunks, uint32_t* counters, int parity, uint32_t chunkCapacity, BhSegWork* work,
-    BhSegment* segOut, BhSegment* queue, BhNodeGeom* geom, uint32_t nodeCapacity, uint32_t segCapacity,
+// Pass 2: positions of the elements above (posB) and below (posS) the split position, in segment order
+// (R1_PER_THREAD consecutive elements per thread, one block scan of their packed counts per chunk); the
+// segment's last CTA finishes the segment.
+__global__ void __launch_bounds__(R1_THREADS) ranksFinishKernel(const dbl4* __restrict__ r, TreeElem* elems,
+    LevelBufs b, LevelBufs next, uint32_t* counters, int parity, uint32_t chunkCapacity, uint32_t segCapacity,
+    BhSegWork* work, uint32_t* posB, uint32_t* posS, BhSegment* queue, BhNodeGeom* geom, uint32_t nodeCapacity,
     uint32_t* devError) {
+    __shared__ uint32_t shScan[R1_THREADS / 32];
+    __shared__ bool shLast;
     const uint32_t nChunks = min(counters[C_CHUNKS + parity], chunkCapacity);
-    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < nChunks; c += gridDim.x * blockDim.x) {
-        if (chunks[c].index != 0) {
-            continue;
-        }
-        const uint32_t s = chunks[c].seg;
-        const BhSegment sg = segIn[s];
-        BhSegWork w = work[s];
-        const uint32_t from = sg.from, to = sg.to;
-        const int d = w.splitIdx;
-        double splitPosition = 0.5 * (sg.lo[d] + sg.hi[d]);
-        uint32_t n1;
-        bool sliding = false;
-        double cut;
-        if (w.mode == 0) {
-            const uint32_t nB = w.nB, nS = w.nS;
-            // first k with posB[k] >= posS[nS - 1 - k] (the predicate is monotone in k)
-            uint32_t lo = 0, hi = min(nB, nS);
-            while (lo < hi) {
-                const uint32_t mid = (lo + hi) >> 1;
-                if (posB[from + mid] < posS[from + nS - 1 - mid]) {
-                    lo = mid + 1;
-                } else {
-                    hi = mid;
+    for (uint32_t c = blockIdx.x; c < nChunks; c += gridDim.x) {
+        const BhChunk ch = b.chunks[c];
+        const BhSegment sg = b.seg[ch.seg];
+        const int mode = work[ch.seg].mode;
+        if (mode == 0) {
+            const int d = work[ch.seg].splitIdx;
+            const unsigned long long split = orderKey(0.5 * (sg.lo[d] + sg.hi[d]));
+            const uint32_t from = sg.from + ch.index * R1_CHUNK;
+            const uint32_t to = min(sg.to, from + R1_CHUNK);
+            const uint32_t k0 = from + threadIdx.x * R1_PER_THREAD;
+            uint32_t flagsB = 0, flagsS = 0;
+#pragma unroll
+            for (int j = 0; j < R1_PER_THREAD; ++j) {
+                const uint32_t k = k0 + j;
+                if (k < to) {
+                    const unsigned long long x = elems[k].key[d];
+                    flagsB |= (x > split ? 1u : 0u) << j;
+                    flagsS |= (x < split ? 1u : 0u) << j;
                 }
             }
-            const uint32_t K = lo;
-            w.K = K;
-            n1 = K < nB ? posB[from + K] : to;
-            if (K >= 1) {
-                n1 = min(n1, posS[from + nS - K]);
-            }
-            if (n1 == from || n1 == to) {
-                // sliding midpoint (then K = 0): the extreme element to the empty side
-                const bool isMax = (n1 == to);
-                const uint32_t dst = isMax ? to - 1 : from;
-                const uint32_t src = isMax ? w.maxp : w.minp;
-                splitPosition = coord(r, idx[src], d);
-                swapElements(idx, keys, n, dst, src);
-                n1 = isMax ? to - 1 : from + 1;
-                sliding = true;
-            }
-            cut = splitPosition;
-        } else {
-            w.K = 0;
-            n1 = (from + to) >> 1;
-            if (w.mode == 1) {
-                NthCtx ctx{ idx, r, d };
-                nthElement(ctx, long(from), long(n1), long(to));
-                for (uint32_t k = from; k < to; ++k) {
-                    const dbl4 p = r[idx[k]];
-                    keys[k] = orderKey(p.x);
-                    keys[size_t(n) + k] = orderKey(p.y);
-                    keys[2 * size_t(n) + k] = orderKey(p.z);
+            // counts of at most R1_CHUNK fit 16 bits each
+            const uint32_t packed = (uint32_t(__popc(flagsB)) << 16) | uint32_t(__popc(flagsS));
+            const uint32_t pre = blockExclusiveScan(packed, shScan);
+            uint32_t rb = sg.from + b.offB[c] + (pre >> 16), rs = sg.from + b.offS[c] + (pre & 0xffffu);
+#pragma unroll
+            for (int j = 0; j < R1_PER_THREAD; ++j) {
+                if (flagsB & (1u << j)) {
+                    posB[rb++] = k0 + j;
                 }
-            }
-            cut = coord(r, idx[n1], d);
-        }
-        work[s] = w;
-        BhSegment left, right;
-        if (!makeChildren(geom, counters, nodeCapacity, devError, sg, n1, d, cut, sliding, left, right)) {
-            continue;
-        }
-        const BhSegment* kids[2] = { &left, &right };
-        for (int k = 0; k < 2; ++k) {
-            const BhSegment& ks = *kids[k];
-            if (ks.to - ks.from > SUBTREE_MAX) {
-                const uint32_t slot = atomicAdd(&counters[C_SEGS + 1 - parity], 1u);
-                if (slot < segCapacity) {
-                    segOut[slot] = ks;
-                } else {
-                    atomicOr(devError, uint32_t(DEV_ERR_SEGMENT_CAPACITY));
-                }
-            } else {
-                const uint32_t slot = atomicAdd(&counters[C_QUEUE], 1u);
-                if (slot < segCapacity) {
-                    queue[slot] = ks;
-                } else {
-                    atomicOr(devError, uint32_t(DEV_ERR_SEGMENT_CAPACITY));
+                if (flagsS & (1u << j)) {
+                    posS[rs++] = k0 + j;
                 }
             }
         }
+        if (lastChunkOfSegment(b.done + chunkCapacity, ch.first, ch.count, &shLast) && threadIdx.x < 32) {
+            finishSegment(r, elems, posB, posB, sg, ch.seg, work, next, 1 - parity, counters, chunkCapacity,
+                segCapacity, queue, geom, nodeCapacity, devError, posS);
+        }
+        __syncthreads();
     }
 }
 
-// the K swaps of each segment's two-pointer partition
-__global__ void __launch_bounds__(R1_THREADS) chunkSwapKernel(uint32_t* idx, unsigned long long* keys, uint32_t n,
-    const uint32_t* __restrict__ posB, const uint32_t* __restrict__ posS, const BhSegment* __restrict__ segIn,
-    const BhChunk* __restrict__ chunks, uint32_t* counters, int parity, uint32_t chunkCapacity,
-    const BhSegWork* __restrict__ work) {
+// Pass 3: the K swaps of each segment's two-pointer partition, four per thread
+__global__ void __launch_bounds__(SWAP_THREADS) chunkSwapKernel(TreeElem* elems, const uint32_t* __restrict__ posB,
+    const uint32_t* __restrict__ posS, LevelBufs b, const uint32_t* __restrict__ counters, int parity,
+    uint32_t chunkCapacity, const BhSegWork* __restrict__ work) {
     const uint32_t nChunks = min(counters[C_CHUNKS + parity], chunkCapacity);
     for (uint32_t c = blockIdx.x; c < nChunks; c += gridDim.x) {
-        const BhChunk ch = chunks[c];
+        const BhChunk ch = b.chunks[c];
         const BhSegWork w = work[ch.seg];
-        const uint32_t from = segIn[ch.seg].from;
+        const uint32_t from = b.seg[ch.seg].from;
         const uint32_t k0 = ch.index * R1_CHUNK;
         const uint32_t k1 = min(w.K, k0 + R1_CHUNK);
         for (uint32_t k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
-            swapElements(idx, keys, n, posB[from + k], posS[from + w.nS - 1 - k]);
+            swapElements(elems, posB[from + k], posS[from + w.nS - 1 - k]);
         }
     }
 }
 
-// end of a level: its chunk count is cleared for the level after next (same parity)
-__global__ void levelEndKernel(uint32_t* counters, int parity) {
-    counters[C_CHUNKS + parity] = 0;
-}
-
-// segments still in the phase-1 list after the last launched level go to the phase-2 queue
-__global__ void flushKernel(const BhSegment* __restrict__ segIn, uint32_t* counters, int parity, BhSegment* queue,
-    uint32_t segCapacity, uint32_t* devError) {
+// segments still in the phase-1 buffers after the last launched level go to the phase-2 queue
+__global__ void flushKernel(LevelBufs b, uint32_t* counters, int parity, BhSegment* queue, uint32_t segCapacity,
+    uint32_t* devError) {
     const uint32_t nIn = min(counters[C_SEGS + parity], segCapacity);
     for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < nIn; s += gridDim.x * blockDim.x) {
         const uint32_t slot = atomicAdd(&counters[C_QUEUE], 1u);
         if (slot < segCapacity) {
-            queue[slot] = segIn[s];
+            queue[slot] = b.seg[s];
         } else {
             atomicOr(devError, uint32_t(DEV_ERR_SEGMENT_CAPACITY));
         }
@@ -786,15 +830,17 @@ __global__ void flushKernel(const BhSegment* __restrict__ segIn, uint32_t* count
 
 // the elements [base, base + len) of a subtree: idx, keys of the three dimensions and the rank scratch, indexed
 // from 0 (shared-memory copies, or the global arrays offset by base)
+template <typename Pos>
 struct SubView {
     uint32_t* idx;
     unsigned long long* key[3];
-    uint32_t* posB;
-    uint32_t* posS;
+    Pos* posB;
+    Pos* posS;
     uint32_t base;
 };
 
-__device__ __forceinline__ void swapSub(const SubView& a, uint32_t x, uint32_t y) {
+template <typename Pos>
+__device__ __forceinline__ void swapSub(const SubView<Pos>& a, uint32_t x, uint32_t y) {
     const uint32_t t = a.idx[x];
     a.idx[x] = a.idx[y];
     a.idx[y] = t;
@@ -805,9 +851,10 @@ __device__ __forceinline__ void swapSub(const SubView& a, uint32_t x, uint32_t y
     }
 }
 
-// One split (or the leaf) of segment sg by the calling warp. Returns true, with the children in l and r (valid
-// in every lane), when the segment was split.
-__device__ bool warpSplit(const dbl4* __restrict__ r, const SubView& a, const BhSegment& sg, BhNodeGeom* geom,
+// One split (or the leaf) of segment sg by the calling warp. Returns true, with the children in l and rr (valid in
+// lane 0 only), when the segment was split.
+template <typename Pos>
+__device__ bool warpSplit(const dbl4* __restrict__ r, const SubView<Pos>& a, const BhSegment& sg, BhNodeGeom* geom,
     uint32_t* counters, uint32_t* leaves, uint32_t leafSize, uint32_t nodeCapacity, uint32_t* devError, BhSegment& l,
     BhSegment& rr) {
     const int lane = threadIdx.x & 31;
@@ -815,27 +862,27 @@ __device__ bool warpSplit(const dbl4* __restrict__ r, const SubView& a, const Bh
     const uint32_t from = sg.from - a.base, to = sg.to - a.base;
     const int node = sg.node;
     if (sg.to - sg.from <= leafSize) {
-        // KdTree::addLeaf: tight box of the leaf's points (min / max are exact in any order)
-        double lo[3] = { DBL_MAX, DBL_MAX, DBL_MAX }, hi[3] = { -DBL_MAX, -DBL_MAX, -DBL_MAX };
+        // KdTree::addLeaf: tight box of the leaf's points, as the extreme order keys (integer minima, exact in any
+        // order; a coordinate of -0 is returned as +0, which no difference or comparison of the box tells apart)
+        unsigned long long lo[3] = { ~0ull, ~0ull, ~0ull }, hi[3] = { 0ull, 0ull, 0ull };
         for (uint32_t k = from + lane; k < to; k += 32) {
-            const dbl4 p = r[a.idx[k]];
-            const double x[3] = { p.x, p.y, p.z };
             for (int d = 0; d < 3; ++d) {
-                lo[d] = fmin(lo[d], x[d]);
-                hi[d] = fmax(hi[d], x[d]);
+                const unsigned long long x = a.key[d][k];
+                lo[d] = min(lo[d], x);
+                hi[d] = max(hi[d], x);
             }
         }
-        for (int off = 16; off > 0; off >>= 1) {
-            for (int d = 0; d < 3; ++d) {
-                lo[d] = fmin(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], off));
-                hi[d] = fmax(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], off));
+        for (int d = 0; d < 3; ++d) {
+            for (int off = 16; off > 0; off >>= 1) {
+                lo[d] = min(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], off));
+                hi[d] = max(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], off));
             }
         }
         if (lane == 0) {
             BhNodeGeom& g = geom[node];
             for (int d = 0; d < 3; ++d) {
-                g.lo[d] = lo[d];
-                g.hi[d] = hi[d];
+                g.lo[d] = keyValue(lo[d]);
+                g.hi[d] = keyValue(hi[d]);
             }
             g.left = -1;
             g.right = -1;
@@ -880,10 +927,10 @@ __device__ bool warpSplit(const dbl4* __restrict__ r, const SubView& a, const Bh
             }
             const unsigned mB = __ballot_sync(0xffffffffu, isB), mS = __ballot_sync(0xffffffffu, isS);
             if (isB) {
-                a.posB[from + nB + __popc(mB & below)] = k;
+                a.posB[from + nB + __popc(mB & below)] = Pos(k);
             }
             if (isS) {
-                a.posS[from + nS + __popc(mS & below)] = k;
+                a.posS[from + nS + __popc(mS & below)] = Pos(k);
             }
             nB += __popc(mB);
             nS += __popc(mS);
@@ -950,41 +997,57 @@ __device__ bool warpSplit(const dbl4* __restrict__ r, const SubView& a, const Bh
         ok = makeChildren(geom, counters, nodeCapacity, devError, sg, n1 + a.base, splitIdx, cut, sliding, l, rr) ? 1
                                                                                                                   : 0;
     }
-    ok = __shfl_sync(0xffffffffu, ok, 0);
-    if (!ok) {
-        return false;
-    }
-    // the children to every lane (lane 0 formed them)
-    l.from = __shfl_sync(0xffffffffu, l.from, 0);
-    l.to = __shfl_sync(0xffffffffu, l.to, 0);
-    l.node = __shfl_sync(0xffffffffu, l.node, 0);
-    l.sliding = __shfl_sync(0xffffffffu, l.sliding, 0);
-    rr.from = __shfl_sync(0xffffffffu, rr.from, 0);
-    rr.to = __shfl_sync(0xffffffffu, rr.to, 0);
-    rr.node = __shfl_sync(0xffffffffu, rr.node, 0);
-    rr.sliding = __shfl_sync(0xffffffffu, rr.sliding, 0);
-    for (int d = 0; d < 3; ++d) {
-        l.lo[d] = __shfl_sync(0xffffffffu, l.lo[d], 0);
-        l.hi[d] = __shfl_sync(0xffffffffu, l.hi[d], 0);
-        rr.lo[d] = __shfl_sync(0xffffffffu, rr.lo[d], 0);
-        rr.hi[d] = __shfl_sync(0xffffffffu, rr.hi[d], 0);
-    }
-    return true;
+    return __shfl_sync(0xffffffffu, ok, 0) != 0;
 }
 
 // shared memory of one warp of subtreeKernel
+// (18.7 KB: three CTAs of four warps fit the shared memory of an SM)
 struct SubtreeShared {
     uint32_t idx[SUBTREE_MAX];
     unsigned long long key[3][SUBTREE_MAX];
-    uint32_t posB[SUBTREE_MAX];
-    uint32_t posS[SUBTREE_MAX];
+    uint16_t posB[SUBTREE_MAX];
+    uint16_t posS[SUBTREE_MAX];
     BhSegment stack[R2_STACK];
 };
+static_assert(SUBTREE_MAX <= 65536, "subtree positions are 16-bit");
 
-__global__ void __launch_bounds__(R2_WARPS * 32) subtreeKernel(const dbl4* __restrict__ r, uint32_t n, uint32_t* idx,
-    unsigned long long* keys, uint32_t* posBg, uint32_t* posSg, const BhSegment* __restrict__ queue,
-    uint32_t* counters, BhNodeGeom* geom, uint32_t* leaves, uint32_t leafSize, uint32_t nodeCapacity,
-    uint32_t segCapacity, uint32_t* devError) {
+// the segment `top` split down to its leaves, depth first, by the calling warp (stack in shared memory)
+template <typename Pos>
+__device__ void splitSubtree(const dbl4* __restrict__ r, const SubView<Pos>& a, const BhSegment& top,
+    BhSegment* stack, BhNodeGeom* geom, uint32_t* counters, uint32_t* leaves, uint32_t leafSize,
+    uint32_t nodeCapacity, uint32_t* devError) {
+    const int lane = threadIdx.x & 31;
+    if (lane == 0) {
+        stack[0] = top;
+    }
+    int sp = 1;
+    __syncwarp();
+    while (sp > 0) {
+        const BhSegment sg = stack[--sp];
+        __syncwarp();
+        // with the stack full, the segment becomes a leaf (flagged as an error): every node keeps a valid state
+        const bool full = sp + 2 > R2_STACK;
+        if (full && lane == 0) {
+            atomicOr(devError, uint32_t(DEV_ERR_SEGMENT_CAPACITY));
+        }
+        BhSegment l, rr;
+        if (warpSplit(r, a, sg, geom, counters, leaves, full ? 0xffffffffu : leafSize, nodeCapacity, devError, l,
+                rr)) {
+            if (lane == 0) {
+                stack[sp] = rr;
+                stack[sp + 1] = l;
+            }
+            sp += 2;
+        }
+        __syncwarp();
+    }
+}
+
+// idx receives the final permutation; keys (3 x n) is the scratch of segments too large for shared memory
+__global__ void __launch_bounds__(R2_WARPS * 32) subtreeKernel(const dbl4* __restrict__ r, uint32_t n,
+    const TreeElem* __restrict__ elems, uint32_t* idx, unsigned long long* keys, uint32_t* posBg, uint32_t* posSg,
+    const BhSegment* __restrict__ queue, uint32_t* counters, BhNodeGeom* geom, uint32_t* leaves, uint32_t leafSize,
+    uint32_t nodeCapacity, uint32_t segCapacity, uint32_t* devError) {
     extern __shared__ __align__(16) unsigned char smem[];
     SubtreeShared& sh = reinterpret_cast<SubtreeShared*>(smem)[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
@@ -1000,61 +1063,46 @@ __global__ void __launch_bounds__(R2_WARPS * 32) subtreeKernel(const dbl4* __res
         }
         const BhSegment top = queue[q];
         const uint32_t len = top.to - top.from;
-        const bool staged = len <= SUBTREE_MAX;
-        SubView a;
-        a.base = top.from;
-        if (staged) {
+        if (len <= SUBTREE_MAX) {
             for (uint32_t k = lane; k < len; k += 32) {
-                sh.idx[k] = idx[top.from + k];
+                const TreeElem e = elems[top.from + k];
+                sh.idx[k] = e.idx;
                 for (int d = 0; d < 3; ++d) {
-                    sh.key[d][k] = keys[size_t(d) * n + top.from + k];
+                    sh.key[d][k] = e.key[d];
                 }
             }
+            SubView<uint16_t> a;
+            a.base = top.from;
             a.idx = sh.idx;
             for (int d = 0; d < 3; ++d) {
                 a.key[d] = sh.key[d];
             }
             a.posB = sh.posB;
             a.posS = sh.posS;
+            __syncwarp();
+            splitSubtree(r, a, top, sh.stack, geom, counters, leaves, leafSize, nodeCapacity, devError);
+            for (uint32_t k = lane; k < len; k += 32) {
+                idx[top.from + k] = sh.idx[k];
+            }
         } else {
-            // a segment that phase 1 left over: the same splits on the global arrays
+            // a segment that phase 1 left over: the same splits on global copies
+            for (uint32_t k = lane; k < len; k += 32) {
+                const TreeElem e = elems[top.from + k];
+                idx[top.from + k] = e.idx;
+                for (int d = 0; d < 3; ++d) {
+                    keys[size_t(d) * n + top.from + k] = e.key[d];
+                }
+            }
+            SubView<uint32_t> a;
+            a.base = top.from;
             a.idx = idx + top.from;
             for (int d = 0; d < 3; ++d) {
                 a.key[d] = keys + size_t(d) * n + top.from;
             }
             a.posB = posBg + top.from;
             a.posS = posSg + top.from;
-        }
-        __syncwarp();
-        int sp = 0;
-        if (lane == 0) {
-            sh.stack[0] = top;
-        }
-        sp = 1;
-        __syncwarp();
-        while (sp > 0) {
-            const BhSegment sg = sh.stack[--sp];
             __syncwarp();
-            if (sp + 2 > R2_STACK && lane == 0) {
-                atomicOr(devError, uint32_t(DEV_ERR_SEGMENT_CAPACITY));
-            }
-            BhSegment l, rr;
-            // with the stack full, the segment becomes a leaf (flagged as an error): every node keeps a valid state
-            const bool full = sp + 2 > R2_STACK;
-            if (warpSplit(r, a, sg, geom, counters, leaves, full ? 0xffffffffu : leafSize, nodeCapacity, devError, l,
-                    rr)) {
-                if (lane == 0) {
-                    sh.stack[sp] = rr;
-                    sh.stack[sp + 1] = l;
-                }
-                sp += 2;
-            }
-            __syncwarp();
-        }
-        if (staged) {
-            for (uint32_t k = lane; k < len; k += 32) {
-                idx[top.from + k] = sh.idx[k];
-            }
+            splitSubtree(r, a, top, sh.stack, geom, counters, leaves, leafSize, nodeCapacity, devError);
         }
         __syncwarp();
     }
@@ -1064,16 +1112,33 @@ __global__ void __launch_bounds__(R2_WARPS * 32) subtreeKernel(const dbl4* __res
 // nodes by level (counting sort) for the level-by-level list phase of the mixed walk
 // ---------------------------------------------------------------------------------------------------------
 
+// nodes per level: a shared-memory histogram per tile of blockDim nodes, one global atomic per level and tile
 __global__ void levelCountKernel(const BhNodeGeom* __restrict__ geom, const uint32_t* __restrict__ counters,
     uint32_t nodeCapacity, uint32_t* levelCount, uint32_t* devError) {
+    __shared__ uint32_t hist[TREE_MAX_LEVELS];
     const uint32_t nn = min(counters[C_NODES], nodeCapacity);
-    for (uint32_t id = blockIdx.x * blockDim.x + threadIdx.x; id < nn; id += gridDim.x * blockDim.x) {
-        const int lvl = geom[id].level;
-        if (lvl < 0 || lvl >= int(TREE_MAX_LEVELS)) {
-            atomicOr(devError, uint32_t(DEV_ERR_NODE_CAPACITY));
-            continue;
+    const uint32_t depth = min(counters[C_DEPTH], TREE_MAX_LEVELS);
+    for (uint32_t t0 = blockIdx.x * blockDim.x; t0 < nn; t0 += gridDim.x * blockDim.x) {
+        for (uint32_t l = threadIdx.x; l < depth; l += blockDim.x) {
+            hist[l] = 0;
         }
-        atomicAdd(&levelCount[lvl], 1u);
+        __syncthreads();
+        const uint32_t id = t0 + threadIdx.x;
+        if (id < nn) {
+            const int lvl = geom[id].level;
+            if (lvl < 0 || uint32_t(lvl) >= depth) {
+                atomicOr(devError, uint32_t(DEV_ERR_NODE_CAPACITY));
+            } else {
+                atomicAdd(&hist[lvl], 1u);
+            }
+        }
+        __syncthreads();
+        for (uint32_t l = threadIdx.x; l < depth; l += blockDim.x) {
+            if (hist[l]) {
+                atomicAdd(&levelCount[l], hist[l]);
+            }
+        }
+        __syncthreads();
     }
 }
 
@@ -1100,15 +1165,41 @@ __global__ void levelScanKernel(const uint32_t* __restrict__ levelCount, uint32_
     }
 }
 
+// node ids by level: per tile, ranks within the tile's level bins in shared memory and one global cursor
+// advance per level and tile
 __global__ void levelScatterKernel(const BhNodeGeom* __restrict__ geom, const uint32_t* __restrict__ counters,
     uint32_t nodeCapacity, const uint32_t* __restrict__ levelFirst, uint32_t* cursor, uint32_t* levelNodes) {
+    __shared__ uint32_t hist[TREE_MAX_LEVELS];
+    __shared__ uint32_t base[TREE_MAX_LEVELS];
     const uint32_t nn = min(counters[C_NODES], nodeCapacity);
-    for (uint32_t id = blockIdx.x * blockDim.x + threadIdx.x; id < nn; id += gridDim.x * blockDim.x) {
-        const int lvl = geom[id].level;
-        if (lvl < 0 || lvl >= int(TREE_MAX_LEVELS)) {
-            continue;
+    const uint32_t depth = min(counters[C_DEPTH], TREE_MAX_LEVELS);
+    for (uint32_t t0 = blockIdx.x * blockDim.x; t0 < nn; t0 += gridDim.x * blockDim.x) {
+        for (uint32_t l = threadIdx.x; l < depth; l += blockDim.x) {
+            hist[l] = 0;
         }
-        levelNodes[levelFirst[lvl] + atomicAdd(&cursor[lvl], 1u)] = id;
+        __syncthreads();
+        const uint32_t id = t0 + threadIdx.x;
+        int lvl = -1;
+        uint32_t local = 0;
+        if (id < nn) {
+            lvl = geom[id].level;
+            if (lvl >= 0 && uint32_t(lvl) < depth) {
+                local = atomicAdd(&hist[lvl], 1u);
+            } else {
+                lvl = -1;
+            }
+        }
+        __syncthreads();
+        for (uint32_t l = threadIdx.x; l < depth; l += blockDim.x) {
+            if (hist[l]) {
+                base[l] = levelFirst[l] + atomicAdd(&cursor[l], hist[l]);
+            }
+        }
+        __syncthreads();
+        if (lvl >= 0) {
+            levelNodes[base[lvl] + local] = id;
+        }
+        __syncthreads();
     }
 }
 
@@ -1130,21 +1221,31 @@ cudaError_t treeBuildAllocate(Tree& t, uint32_t n) {
             e = cudaMalloc(p, bytes > 0 ? bytes : 16);
         }
     };
-    alloc((void**)&t.keys, 3 * size_t(nn) * sizeof(unsigned long long));
+    alloc((void**)&t.elems, size_t(nn) * sizeof(TreeElem));
+    alloc((void**)&t.subtree_keys, 3 * size_t(nn) * sizeof(unsigned long long));
     alloc((void**)&t.queue, size_t(t.seg_capacity) * sizeof(BhSegment));
     alloc((void**)&t.level_count, TREE_MAX_LEVELS * sizeof(uint32_t));
     alloc((void**)&t.level_first_dev, TREE_MAX_LEVELS * sizeof(uint32_t));
     alloc((void**)&t.level_cursor, TREE_MAX_LEVELS * sizeof(uint32_t));
     alloc((void**)&t.level_nodes, size_t(t.node_capacity) * sizeof(uint32_t));
+    // phase-1 buffers of two level parities
+    t.chunk_capacity = treeChunkCapacity(nn);
+    const size_t cc2 = 2 * size_t(t.chunk_capacity);
+    alloc((void**)&t.chunks, cc2 * sizeof(BhChunk));
+    alloc((void**)&t.chunk_stats, cc2 * sizeof(BhChunkStats));
+    alloc((void**)&t.chunk_off_b, cc2 * sizeof(uint32_t));
+    alloc((void**)&t.chunk_off_s, cc2 * sizeof(uint32_t));
+    alloc((void**)&t.chunk_done, 2 * cc2 * sizeof(uint32_t));
+    alloc((void**)&t.work, size_t(t.seg_capacity) * sizeof(BhSegWork));
     if (e == cudaSuccess) {
         e = cudaMallocHost((void**)&t.info_host, (C_WORDS + TREE_MAX_LEVELS) * sizeof(uint32_t));
     }
-    t.chunk_capacity = 2 * nn / R1_CHUNK + nn / SUBTREE_MAX + 64;
     return e;
 }
 
 void treeBuildFree(Tree& t) {
-    void* ptrs[] = { t.keys, t.queue, t.level_count, t.level_first_dev, t.level_cursor, t.level_nodes };
+    void* ptrs[] = { t.elems, t.subtree_keys, t.queue, t.level_count, t.level_first_dev, t.level_cursor, t.level_nodes,
+        t.chunks, t.chunk_stats, t.chunk_off_b, t.chunk_off_s, t.chunk_done, t.work };
     for (void* p : ptrs) {
         if (p) {
             cudaFree(p);
@@ -1155,10 +1256,28 @@ void treeBuildFree(Tree& t) {
     }
 }
 
+// chunks of one phase-1 level: each segment has more than SUBTREE_MAX elements, so a level holds fewer than
+// n / SUBTREE_MAX segments and at most n / R1_CHUNK + (segments) chunks
 uint32_t treeChunkCapacity(uint32_t n) {
     const uint32_t nn = n > 0 ? n : 1;
-    return 2 * nn / R1_CHUNK + nn / SUBTREE_MAX + 64;
+    return nn / R1_CHUNK + nn / SUBTREE_MAX + 64;
 }
+
+namespace {
+
+LevelBufs levelBufs(const Tree& t, int parity) {
+    const size_t off = size_t(parity) * t.chunk_capacity;
+    LevelBufs b;
+    b.seg = t.seg[parity];
+    b.chunks = t.chunks + off;
+    b.stats = t.chunk_stats + off;
+    b.offB = t.chunk_off_b + off;
+    b.offS = t.chunk_off_s + off;
+    b.done = t.chunk_done + 2 * off;
+    return b;
+}
+
+} // namespace
 
 cudaError_t treeBuild(const DState& s, Tree& t, const Physics& ph, uint32_t* devError, cudaStream_t st) {
     const uint32_t n = s.n;
@@ -1170,18 +1289,22 @@ cudaError_t treeBuild(const DState& s, Tree& t, const Physics& ph, uint32_t* dev
         t.built = true;
         return cudaSuccess;
     }
-    static int gridC = 0, gridR2 = 0;
+    static int gridC = 0, gridR2 = 0, gridSwap = 0;
     const size_t r2Shared = R2_WARPS * sizeof(SubtreeShared);
     if (gridC == 0) {
-        gridC = residentGrid(reinterpret_cast<const void*>(chunkStatsKernel), R1_THREADS, 0);
+        gridC = std::min(residentGrid(reinterpret_cast<const void*>(statsDecideKernel), R1_THREADS, 0),
+            residentGrid(reinterpret_cast<const void*>(ranksFinishKernel), R1_THREADS, 0));
+        gridSwap = residentGrid(reinterpret_cast<const void*>(chunkSwapKernel), SWAP_THREADS, 0);
         cudaFuncSetAttribute(subtreeKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(r2Shared));
         gridR2 = residentGrid(reinterpret_cast<const void*>(subtreeKernel), R2_WARPS * 32, r2Shared);
     }
     t.launches = 0;
     auto launched = [&](uint32_t k) { t.launches += k; };
+    const uint32_t cc = t.chunk_capacity;
     resetBoundsKernel<<<1, 32, 0, st>>>(t.bbox);
     boundsKernel<<<std::min(ceilDiv(n, 256), 152 * 8), 256, 0, st>>>(s.r, n, t.bbox);
-    rootKernel<<<ceilDiv(n, 256), 256, 0, st>>>(s.r, n, t.idx, t.keys, t.seg[0], t.queue, t.geom, t.counters, t.bbox);
+    rootKernel<<<ceilDiv(n, 256), 256, 0, st>>>(s.r, n, t.elems, levelBufs(t, 0), t.queue, t.geom, t.counters, cc,
+        t.seg_capacity, t.bbox, devError);
     cudaMemsetAsync(t.level_count, 0, TREE_MAX_LEVELS * sizeof(uint32_t), st);
     launched(3);
     // phase 1: the previous build's level count plus two (a first build: from the size)
@@ -1195,31 +1318,22 @@ cudaError_t treeBuild(const DState& s, Tree& t, const Physics& ph, uint32_t* dev
     if (n <= SUBTREE_MAX) {
         levels = 0;
     }
-    const uint32_t maxSegs = n / SUBTREE_MAX + 1;
-    const int gridSeg = std::max(1, std::min(ceilDiv(maxSegs, 256), 152 * 8));
-    const int gridWarpSeg = std::max(1, std::min(ceilDiv(std::min(t.chunk_capacity, n), 4), 152 * 16));
     for (uint32_t level = 0; level < levels; ++level) {
         const int p = int(level & 1u);
-        BhSegment* segIn = t.seg[p];
-        BhSegment* segOut = t.seg[1 - p];
-        const uint32_t cc = t.chunk_capacity;
-        chunkListKernel<<<gridSeg, 256, 0, st>>>(segIn, t.counters, p, t.chunks, cc, t.seg_capacity, devError);
-        chunkStatsKernel<<<gridC, R1_THREADS, 0, st>>>(t.keys, n, segIn, t.chunks, t.counters, p, cc, t.chunk_stats);
-        segDecideKernel<<<gridWarpSeg, 128, 0, st>>>(segIn, t.chunks, t.counters, p, cc, t.chunk_stats,
-            t.chunk_off_b, t.chunk_off_s, t.work);
-        chunkRanksKernel<<<gridC, R1_THREADS, 0, st>>>(t.keys, n, segIn, t.chunks, t.counters, p, cc, t.chunk_off_b,
-            t.chunk_off_s, t.work, t.scratch_b, t.scratch_s);
-        segFinishKernel<<<gridWarpSeg, 128, 0, st>>>(s.r, n, t.idx, t.keys, t.scratch_b, t.scratch_s, segIn,
-            t.chunks, t.counters, p, cc, t.work, segOut, t.queue, t.geom, t.node_capacity, t.seg_capacity, devError);
-        chunkSwapKernel<<<gridC, R1_THREADS, 0, st>>>(t.idx, t.keys, n, t.scratch_b, t.scratch_s, segIn, t.chunks,
-            t.counters, p, cc, t.work);
-        levelEndKernel<<<1, 1, 0, st>>>(t.counters, p);
-        launched(7);
+        const LevelBufs b = levelBufs(t, p), next = levelBufs(t, 1 - p);
+        statsDecideKernel<<<gridC, R1_THREADS, 0, st>>>(t.elems, b, t.counters, p, cc, t.work);
+        ranksFinishKernel<<<gridC, R1_THREADS, 0, st>>>(s.r, t.elems, b, next, t.counters, p, cc, t.seg_capacity,
+            t.work, t.scratch_b, t.scratch_s, t.queue, t.geom, t.node_capacity, devError);
+        chunkSwapKernel<<<gridSwap, SWAP_THREADS, 0, st>>>(t.elems, t.scratch_b, t.scratch_s, b, t.counters, p, cc,
+            t.work);
+        launched(3);
     }
-    flushKernel<<<gridSeg, 256, 0, st>>>(t.seg[levels & 1u], t.counters, int(levels & 1u), t.queue, t.seg_capacity,
-        devError);
+    const uint32_t gridSeg = std::max(1, std::min(ceilDiv(n / SUBTREE_MAX + 1, 256), 152 * 8));
+    flushKernel<<<gridSeg, 256, 0, st>>>(levelBufs(t, int(levels & 1u)), t.counters, int(levels & 1u), t.queue,
+        t.seg_capacity, devError);
     // phase 2
-    subtreeKernel<<<gridR2, R2_WARPS * 32, r2Shared, st>>>(s.r, n, t.idx, t.keys, t.scratch_b, t.scratch_s, t.queue,
+    subtreeKernel<<<gridR2, R2_WARPS * 32, r2Shared, st>>>(s.r, n, t.elems, t.idx, t.subtree_keys, t.scratch_b,
+        t.scratch_s, t.queue,
         t.counters, t.geom, t.leaves, ph.leaf_size, t.node_capacity, t.seg_capacity, devError);
     // nodes by level
     const int gridNodes = std::min(ceilDiv(t.node_capacity, 256), 152 * 8);

@@ -11,8 +11,13 @@ particle set. The state (~300 B per particle) exceeds the 129 MB L2, so no flush
 Prints one JSON line (rank 0). `value` is the mixed-precision path with the state resident in HBM; `e2e`
 is the same metric through the public API with host buffers (positions and velocities uploaded from pinned
 host memory and positions, velocities, density and energy read back every step); `fp64` reports the plain
-FP64 GPU path on the same workload and the mixed path's error against it. `--impl reference` times the CPU
-implementation of the path (the oracle restatement of the reference, all host threads) on the same workload.
+FP64 GPU path on the same workload, the mixed path's error against it after 100 steps (fields and conserved
+totals) and both paths' error against the CPU oracle after the first steps; `nbody_plummer` the 4,194,304-
+particle Plummer walk at theta 0.3 / 0.5 / 0.7 against the FP64 direct sum on 65,536 particles; `fp64_configs`
+the FP64 GPU path against the CPU oracle on the 10,648-particle sphere and the 217,823-particle impact;
+`adjoint` and `nbody_reaccumulation` the adjoint and N-body workloads. `roofline` divides by the FP32 rate
+measured on the device in the same run. `--impl reference` times the CPU implementation of the path (the
+oracle restatement of the reference, all host threads) on the same workload.
 """
 import argparse
 import json
@@ -45,13 +50,17 @@ def parse():
     ap.add_argument("--cpu-steps", type=int, default=1)
     ap.add_argument("--error-steps", type=int, default=100,
                     help="steps after which the mixed path is compared with the FP64 GPU path")
+    ap.add_argument("--port-error-steps", type=int, default=5,
+                    help="steps after which both GPU paths are compared with the CPU oracle (0: skip)")
+    ap.add_argument("--no-fp64-configs", action="store_true",
+                    help="skip the FP64 GPU vs CPU lines of the 10,648- and 217,823-particle configurations")
     ap.add_argument("--profile-only", action="store_true", help="warm-up + timed steps only (for ncu)")
     ap.add_argument("--no-nbody", action="store_true", help="skip the gravity-only Plummer measurement")
     ap.add_argument("--nbody-n", type=int, default=4_194_304)
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurement")
     ap.add_argument("--no-reaccumulation", action="store_true", help="skip the N-body collision measurement")
     ap.add_argument("--reacc-n", type=int, default=1_000_000)
-    ap.add_argument("--only", choices=["nbody", "adjoint", "reaccumulation"], default=None,
+    ap.add_argument("--only", choices=["nbody", "adjoint", "reaccumulation", "fp64_configs"], default=None,
                     help="run only one of the secondary measurements and print its JSON (for profiling)")
     ap.add_argument("--adjoint-target", type=int, default=100_000)
     ap.add_argument("--adjoint-impactor", type=int, default=2_000)
@@ -235,6 +244,12 @@ def run_gpu(args, rank, world):
         result["adjoint"] = adjoint(args, dev)
     if rank == 0 and not args.no_reaccumulation:
         result["reaccumulation"] = reaccumulation(args, dev)
+    if rank == 0 and not args.no_fp64_configs:
+        result["fp64_configs"] = fp64_configs(args, dev)
+    if rank == 0:
+        from opensph_gb300.solver import measure_fp32_peak
+
+        result["fp32_peak_tflops"] = measure_fp32_peak(200.0)
     return result
 
 
@@ -245,15 +260,21 @@ def compare_fp64(args, st, mats, n, mixed_cfg, dev):
     from opensph_gb300 import abi
     from opensph_gb300.solver import GpuSolver
 
+    from oracle import oracle
+
     steps = max(args.error_steps, args.warmup + args.steps)
+    port_steps = args.port_error_steps
     out = {}
-    states = {}
+    states, totals, early = {}, {}, {}
     for name, prec in (("fp64", abi.PRECISION_FP64), ("mixed", abi.PRECISION_MIXED)):
         cfg, keep = make_config(n, mats, prec)
         cfg.device = dev
         with GpuSolver(cfg, keep) as g:
             g.set_state({k: v.copy() for k, v in st.items()})
             stream = torch.cuda.ExternalStream(g.stream)
+            if port_steps > 0:
+                g.step(port_steps)
+                early[name] = g.get_state(["r", "v", "rho", "u"])
             if name == "fp64":
                 g.step(args.warmup)
                 s0 = torch.cuda.Event(enable_timing=True)
@@ -264,10 +285,11 @@ def compare_fp64(args, st, mats, n, mixed_cfg, dev):
                 s1.synchronize()
                 out["value"] = n * args.steps / (s0.elapsed_time(s1) * 1e-3)
                 out["ms_per_step"] = s0.elapsed_time(s1) / args.steps
-                g.step(steps - args.warmup - args.steps)
+                g.step(steps - port_steps - args.warmup - args.steps)
             else:
-                g.step(steps)
+                g.step(steps - port_steps)
             states[name] = g.get_state(["r", "v", "rho", "u", "D"])
+            totals[name] = g.totals()
             out[f"{name}_final_timestep"] = g.timestep
     ref, mix = states["fp64"], states["mixed"]
 
@@ -281,13 +303,39 @@ def compare_fp64(args, st, mats, n, mixed_cfg, dev):
     out["rel_err_velocity"] = rel(vmix, vref)
     out["rel_err_energy"] = rel(mix["u"], ref["u"])
     out["max_abs_err_damage"] = float(np.max(np.abs(mix["D"] - ref["D"])))
+    # conserved totals (core/physics/Integrals.cpp:24-91) after the same steps: total energy relative to itself,
+    # momentum and angular momentum relative to their largest component
+    tm, tf = totals["mixed"], totals["fp64"]
+    out["totals_after_steps"] = {
+        "rel_err_total_energy": abs((tm[6] + tm[7]) - (tf[6] + tf[7])) / abs(tf[6] + tf[7]),
+        "rel_err_momentum": float(np.max(np.abs(tm[0:3] - tf[0:3])) / np.max(np.abs(tf[0:3]))),
+        "rel_err_angular_momentum": float(np.max(np.abs(tm[3:6] - tf[3:6])) / np.max(np.abs(tf[3:6]))),
+        "fp64_total_energy": float(tf[6] + tf[7]), "fp64_momentum": [float(x) for x in tf[0:3]]}
+    if port_steps > 0:
+        # both GPU paths against the CPU implementation of the reference's algorithms (the oracle, all host
+        # threads) after the first port_steps steps from the same state
+        work = {k: v.copy() for k, v in st.items()}
+        cfg64, _ = make_config(n, mats, abi.PRECISION_FP64)
+        oracle.set_threads(0)
+        oracle.run(cfg64, work, port_steps, float(cfg64.initial_timestep))
+        vport = work["v"].reshape(-1, 4)[:, :3]
+        port = {"steps": port_steps}
+        for name in ("fp64", "mixed"):
+            e = early[name]
+            port[name] = {"rel_err_density": rel(e["rho"], work["rho"]),
+                          "rel_err_velocity": rel(e["v"].reshape(-1, 4)[:, :3], vport),
+                          "rel_err_energy": rel(e["u"], work["u"]),
+                          "rel_err_position": rel(e["r"].reshape(-1, 4)[:, :3], work["r"].reshape(-1, 4)[:, :3])}
+        out["vs_cpu_port"] = port
     return out
 
 
 # DRAM bytes (read + write) of one mixed walk of the default workload (the evaluation launch plus the launches
-# that build the interaction lists), from the ncu capture summarised in profiles/evalListsKernel_impact1M.md
+# that build the interaction lists): a constant from a separate ncu capture of the same workload and command
+# (dram__bytes_read.sum + dram__bytes_write.sum), not measured in this run
 WALK_TRAFFIC_BYTES = (277.7 + 35.1 + 175.4 + 76.1 + 15.2) * 1e6
-WALK_TRAFFIC_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, profiles/evalListsKernel_impact1M.md"
+WALK_TRAFFIC_SOURCE = ("constant from an earlier ncu capture of one walk of this workload (dram__bytes_read.sum + "
+                       "dram__bytes_write.sum); not measured in this run")
 
 # FP32 operations of one particle-multipole evaluation (accMultipoleF, csrc/gravity32.cu: octupole) and the
 # N-body convention for one softened particle-particle interaction
@@ -297,8 +345,10 @@ FP32_PEAK_NOMINAL = 152 * 128 * 2 * 2.07e9 / 1e12  # TFLOP/s at the maximum SM c
 
 
 def nbody(args, dev):
-    """Gravity-only workload: Plummer sphere (scale radius 1, M = 1, G = 1, softening 1e-3 as h), Barnes-Hut
-    theta = 0.5 octupole; tree build + walk timed for the mixed (FP32 evaluation) and the FP64 walk."""
+    """Gravity-only workload: Plummer sphere (scale radius 1, M = 1, G = 1, softening 1e-3 as h), 4,194,304
+    particles, Barnes-Hut octupole at theta 0.3, 0.5 and 0.7: tree build + walk timed for the mixed (FP32
+    evaluation) and the FP64 walk; both checked against the FP64 direct sum (BruteForceGravity,
+    sphgpu_gravity_direct) on 65,536 seeded particles."""
     import torch
 
     from opensph_gb300 import abi, initial
@@ -307,35 +357,118 @@ def nbody(args, dev):
     n = args.nbody_n
     r, m = initial.plummer(n, seed=7, softening=1e-3)
     r = r.ravel()
-    out = {"particles": n, "theta": 0.5, "workload": "Plummer sphere, G = 1, softening 1e-3, octupole"}
-    accs = {}
-    for name, prec in (("mixed", abi.PRECISION_MIXED), ("fp64", abi.PRECISION_FP64)):
+    targets = np.sort(np.random.default_rng(11).choice(n, size=min(65536, n), replace=False)).astype("u4")
+    out = {"particles": n, "workload": "Plummer sphere, G = 1, softening 1e-3, octupole",
+           "direct_check_targets": int(targets.size)}
+
+    def solver(theta, prec):
         cfg, keep = abi.make_config(n, [abi.ideal_gas()], forces=abi.FORCE_PRESSURE | abi.FORCE_SELF_GRAVITY,
-                                    gravity_constant=1.0, gravity_opening_angle=0.5, precision=prec)
+                                    gravity_constant=1.0, gravity_opening_angle=theta, precision=prec)
         cfg.device = dev
-        with GpuSolver(cfg, keep) as g:
-            g.set_quantity(abi.Q_POSITION, 0, r)
-            g.set_quantity(abi.Q_MASS, 0, m)
-            g.gravity()
-            g.set_profiling(True)
-            g.phase_times()
-            reps = 3 if name == "mixed" else 1
-            for _ in range(reps):
-                accs[name] = g.gravity()
-            phases, _ = g.phase_times()
-            inter = g.gravity_interactions()
-        walk_ms = phases["gravity_eval"] / reps
-        build_ms = phases["gravity_build"] / reps
-        total = inter[0] + inter[1]
-        flops = inter[0] * FLOP_PN + inter[1] * FLOP_PP
-        out[name] = {"walk_ms": walk_ms, "build_ms": build_ms, "interactions": total,
-                     "particle_node": inter[0], "particle_particle": inter[1],
-                     "interactions_per_s": total / (walk_ms * 1e-3), "walk_tflops": flops / (walk_ms * 1e-3) / 1e12}
-    out["mixed"]["fp32_frac_of_nominal_peak"] = out["mixed"]["walk_tflops"] / FP32_PEAK_NOMINAL
-    out["walk_speedup_mixed_vs_fp64"] = out["fp64"]["walk_ms"] / out["mixed"]["walk_ms"]
-    a, b = accs["mixed"].reshape(-1, 4)[:, :3], accs["fp64"].reshape(-1, 4)[:, :3]
-    out["mixed_vs_fp64_rel_err"] = float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+        g = GpuSolver(cfg, keep)
+        g.set_quantity(abi.Q_POSITION, 0, r)
+        g.set_quantity(abi.Q_MASS, 0, m)
+        return g
+
+    t0 = time.perf_counter()
+    with solver(0.5, abi.PRECISION_FP64) as g:
+        direct = g.gravity_direct(targets).reshape(-1, 4)[:, :3]
+    out["direct_sum_s"] = time.perf_counter() - t0
+    dnorm = np.linalg.norm(direct, axis=1)
+
+    def errors(acc):
+        e = np.linalg.norm(acc.reshape(-1, 4)[targets, :3] - direct, axis=1) / dnorm
+        return {"median": float(np.median(e)), "p99": float(np.percentile(e, 99)), "max": float(np.max(e))}
+
+    for theta in (0.3, 0.5, 0.7):
+        res = {}
+        accs = {}
+        for name, prec in (("mixed", abi.PRECISION_MIXED), ("fp64", abi.PRECISION_FP64)):
+            with solver(theta, prec) as g:
+                g.gravity()
+                g.set_profiling(True)
+                g.phase_times()
+                reps = 3 if name == "mixed" else 1
+                for _ in range(reps):
+                    accs[name] = g.gravity()
+                phases, _ = g.phase_times()
+                inter = g.gravity_interactions()
+            walk_ms = phases["gravity_eval"] / reps
+            build_ms = phases["gravity_build"] / reps
+            total = inter[0] + inter[1]
+            flops = inter[0] * FLOP_PN + inter[1] * FLOP_PP
+            res[name] = {"walk_ms": walk_ms, "build_ms": build_ms, "interactions": total,
+                         "particle_node": inter[0], "particle_particle": inter[1],
+                         "interactions_per_s": total / (walk_ms * 1e-3),
+                         "walk_tflops": flops / (walk_ms * 1e-3) / 1e12,
+                         "rel_err_vs_direct": errors(accs[name])}
+        res["walk_speedup_mixed_vs_fp64"] = res["fp64"]["walk_ms"] / res["mixed"]["walk_ms"]
+        a, b = accs["mixed"].reshape(-1, 4)[:, :3], accs["fp64"].reshape(-1, 4)[:, :3]
+        res["mixed_vs_fp64_rel_err"] = float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+        out[f"theta_{theta}"] = res
     torch.cuda.synchronize()
+    return out
+
+
+def fp64_configs(args, dev):
+    """The plain FP64 path on the two CPU-runnable configurations, GPU against the CPU implementation of the
+    reference's algorithms (the oracle, all host threads), same inputs:
+    config 1, the basalt sphere of 10,000 requested particles (HCP, R = 10 km, h = 1.3 x the lattice spacing,
+    rho 2700, u 1e3, velocities N(0, 1 m/s) per component), Tillotson, continuity + pressure + standard AV,
+    Barnes-Hut theta 0.5 octupole, predictor-corrector with the Courant criterion, 100 steps;
+    config 2, the solid impact of 200,000 + 5,000 requested particles (R 50 km and 5 km, 5 km/s at 45 degrees),
+    von Mises + Grady-Kipp, adaptive h."""
+    import torch
+
+    from opensph_gb300 import abi, initial
+    from opensph_gb300.solver import GpuSolver
+    from oracle import oracle
+
+    out = {}
+    # config 1
+    rr = initial.hcp_sphere(10000, 1.0e4, eta=1.43)
+    n1 = len(rr)
+    volume = 4.0 / 3.0 * np.pi * 1.0e12
+    vel = np.zeros((n1, 4))
+    vel[:, :3] = np.random.default_rng(1).standard_normal((n1, 3))
+    st1 = {"r": rr.ravel(), "v": vel.ravel(), "dv": np.zeros(4 * n1), "m": np.full(n1, 2700.0 * volume / n1),
+           "rho": np.full(n1, 2700.0), "drho": np.zeros(n1), "u": np.full(n1, 1.0e3), "du": np.zeros(n1),
+           "p": np.zeros(n1), "cs": np.zeros(n1), "divv": np.zeros(n1), "ncnt": np.zeros(n1, "u4"),
+           "flag": np.zeros(n1, "u4"), "mat": np.zeros(n1, "u4")}
+    mat1 = abi.basalt(yielding=abi.YIELDING_NONE, damage=abi.DAMAGE_NONE)
+    cfg1, keep1 = abi.make_config(n1, [mat1], forces=abi.FORCE_PRESSURE | abi.FORCE_SELF_GRAVITY)
+    # config 2
+    st2, mats2 = initial.impact_state(200000, 5.0e4, 5000, 5.0e3, speed=5.0e3, angle_deg=45.0, seed=1234)
+    n2 = len(st2["m"])
+    cfg2, keep2 = make_config(n2, mats2, abi.PRECISION_FP64)
+    for name, st, cfg, gpu_steps, cpu_steps in (("config1_sphere", st1, cfg1, 100, 100),
+                                                ("config2_impact", st2, cfg2, 20, 2)):
+        cfg.device = dev
+        with GpuSolver(cfg, [keep1, keep2]) as g:
+            g.set_state({k: v.copy() for k, v in st.items()})
+            g.step(3)
+            g.synchronize()
+            stream = torch.cuda.ExternalStream(g.stream)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            g.step(gpu_steps)
+            e1.record(stream)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1)
+        work = {k: v.copy() for k, v in st.items()}
+        oracle.set_threads(0)
+        t0 = time.perf_counter()
+        oracle.run(cfg, work, cpu_steps, float(cfg.initial_timestep))
+        secs = time.perf_counter() - t0
+        n = len(st["m"])
+        gpu = n * gpu_steps / (ms * 1e-3)
+        cpu = n * cpu_steps / secs
+        out[name] = {"particles": n, "fp64_gpu": {"value": gpu, "unit": UNIT, "ms_per_step": ms / gpu_steps,
+                                                 "steps": gpu_steps},
+                     "cpu": {"value": cpu, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+                             "steps": cpu_steps, "seconds": secs},
+                     "gpu_over_cpu": gpu / cpu}
     return out
 
 
@@ -528,7 +661,8 @@ def main():
     if args.only is not None:
         dev = int(os.environ.get("LOCAL_RANK", "0"))
         torch.cuda.set_device(dev)
-        out = {"nbody": nbody, "adjoint": adjoint, "reaccumulation": reaccumulation}[args.only](args, dev)
+        out = {"nbody": nbody, "adjoint": adjoint, "reaccumulation": reaccumulation,
+               "fp64_configs": fp64_configs}[args.only](args, dev)
         print(json.dumps({args.only: out}))
         return
 
@@ -550,17 +684,19 @@ def main():
     pn, pp = res["interactions"]
     walk_flops = pn * FLOP_PN + pp * FLOP_PP
     walk_tf = walk_flops / (walk_ms * 1e-3) / 1e12 if walk_ms > 0 else None
+    fp32_peak = res.get("fp32_peak_tflops") or FP32_PEAK_NOMINAL
+    fp32_source = ("measured: FMA-chain kernel on every SM, CUDA events (sphgpu_measure_fp32_peak)"
+                   if res.get("fp32_peak_tflops") else "nominal (152 SMs x 128 lanes x 2 x 2.07 GHz)")
     line = {
         "metric": METRIC, "value": res["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32/f64", "data": "synthetic", "config": config_json(args, n),
         "e2e": res["e2e"], "gpu_launches": res["launches"], "clocks": res["clocks"],
         "phases_ms_per_step": {k: v / args.steps for k, v in res["phases"].items()},
-        "roofline": {"kernel": "evalListsKernel + listLevelKernel (mixed walk)", "bound": "fp32", "achieved": walk_tf, "peak": FP32_PEAK_NOMINAL,
-                     "unit": "TFLOP/s", "frac": walk_tf / FP32_PEAK_NOMINAL if walk_tf else None,
+        "roofline": {"kernel": "evalListsKernel + listLevelKernel (mixed walk)", "bound": "fp32", "achieved": walk_tf,
+                     "peak": fp32_peak, "unit": "TFLOP/s", "frac": walk_tf / fp32_peak if walk_tf else None,
                      "traffic": WALK_TRAFFIC_BYTES, "traffic_source": WALK_TRAFFIC_SOURCE,
-                     "peak_source": "nominal FP32 (152 SMs x 128 lanes x 2 x 2.07 GHz); MEASURED_PEAKS.json has no "
-                                    "FP32 figure",
+                     "peak_source": fp32_source, "fp32_nominal_tflops": FP32_PEAK_NOMINAL,
                      "flops_per_launch": walk_flops, "particle_node": pn, "particle_particle": pp,
                      "flop_per_particle_node": FLOP_PN, "flop_per_particle_particle": FLOP_PP,
                      "launch_ms": walk_ms},
@@ -578,6 +714,8 @@ def main():
         line["adjoint"] = res["adjoint"]
     if "reaccumulation" in res:
         line["nbody_reaccumulation"] = res["reaccumulation"]
+    if "fp64_configs" in res:
+        line["fp64_configs"] = res["fp64_configs"]
     if not args.no_cpu:
         st, mats, n2 = workload(args)
         value, secs = cpu_sample(args, st, mats, n2, args.cpu_steps)

@@ -2,7 +2,7 @@
  *
  * One handle owns the particle state of one simulation, resident in HBM, and one CUDA stream. The entry
  * points below replace the reference's per-step C++ interfaces; the reference-side adaptor classes that
- * forward to them are shown in INTEGRATION.md. Every function returns an sphgpu_status (0 = success); no
+ * forward to them are in opensph_gb300/adaptor/GpuSph.h. Every function returns an sphgpu_status (0 = success); no
  * C++ exception crosses this boundary. Handles are not re-entrant: one host thread per handle at a time,
  * as the reference calls ISolver/ITimeStepping from one thread (core/timestepping/ISolver.h:22-31).
  *
@@ -191,7 +191,8 @@ typedef struct {
     double bounce_merge_limit;         /* COLLISION_BOUNCE_MERGE_LIMIT */
     double rotation_merge_limit;       /* COLLISION_ROTATION_MERGE_LIMIT */
     uint32_t max_bounces;              /* COLLISION_MAX_BOUNCES */
-    uint32_t reserved2;
+    uint32_t collision_records;        /* collision records beyond one per particle that a collide call may create
+                                        * (the work space of its time-ordered loop); 0 = max(n, 65,536) */
     /* GRAVITY_RECOMPUTATION_PERIOD (CachedGravity, core/gravity/CachedGravity.h): with a positive value the
      * self-gravity accelerations are reused while the run time is less than this period after their last
      * evaluation and the particle count is unchanged; 0 = every evaluation */
@@ -224,6 +225,20 @@ sphgpu_status sphgpu_build_neighbors(sphgpu_handle* h);
  * If *npairs on return exceeds capacity, nothing beyond capacity was written (SPHGPU_ERR_CAPACITY). */
 sphgpu_status sphgpu_get_pairs(sphgpu_handle* h, uint32_t* pair_i, uint32_t* pair_j, uint64_t capacity,
     uint64_t* npairs);
+/* The answer of ISymmetricFinder::findAll(i, 2 h_i) (core/objects/finders/NeighborFinder.h:106-111, the query
+ * radius of SymmetricSolver::loop) for every particle at once: the directed pairs (i, j), j != i, with
+ * |r_j - r_i|^2 < (2 h_i)^2 (FP64), sorted by i then j; capacity semantics of sphgpu_get_pairs. */
+sphgpu_status sphgpu_get_radius_pairs(sphgpu_handle* h, uint32_t* pair_i, uint32_t* pair_j, uint64_t capacity,
+    uint64_t* npairs);
+
+/* ISymmetricFinder::findAll(const Vector& pos, Float radius, Array<NeighborRecord>&)
+ * (core/objects/finders/NeighborFinder.h:112-117) on the neighbour grid of the last sphgpu_build_neighbors (or
+ * sphgpu_get_pairs) of the current positions: the particles j with |r_j - pos|^2 < radius^2 (x, y, z; FP64),
+ * ascending in j, with those squared distances. If *count on return exceeds capacity, nothing was written
+ * (SPHGPU_ERR_CAPACITY; call again with a larger capacity). SPHGPU_ERR_STATE when the positions changed since
+ * the last grid build. */
+sphgpu_status sphgpu_find_neighbors(sphgpu_handle* h, const double pos[3], double radius, uint32_t* indices,
+    double* dist_sqr, uint64_t capacity, uint64_t* count);
 
 /* IGravity::build + evalSelfGravity (core/gravity/IGravity.h:16-62, core/gravity/BarnesHut.cpp:50-99):
  * builds the k-d tree and multipole moments, then adds the self-gravity acceleration of every particle to
@@ -233,6 +248,19 @@ sphgpu_status sphgpu_gravity_build(sphgpu_handle* h);
 sphgpu_status sphgpu_gravity_eval(sphgpu_handle* h, double* dv, uint64_t count);
 /* IGravity::evalAcceleration (core/gravity/BarnesHut.cpp:118-160) at npoints host points (4 doubles each). */
 sphgpu_status sphgpu_gravity_eval_points(sphgpu_handle* h, const double* points, uint64_t npoints, double* acc);
+/* IGravity::evalAttractors as BarnesHut implements it (core/gravity/BarnesHut.cpp:100-125), for the particles'
+ * current positions and masses: attractors holds count x 5 doubles (position x, y, z, radius, mass). For each
+ * attractor in order, every particle's dv (host, 4 doubles per particle, dv_count = particle count; may be NULL)
+ * loses (G M_a) grad W(r_i - x_a, (h_i + R_a) / 2), all four components as the reference's Vector arithmetic,
+ * and attractor_acc (host, 3 doubles per attractor, accumulated into) gains the sum over the particles of
+ * (G m_i) grad W; then the attractor-attractor terms of each pair. At most 65,535 attractors per call. */
+sphgpu_status sphgpu_gravity_attractors(sphgpu_handle* h, const double* attractors, uint64_t count,
+    double* attractor_acc, double* dv, uint64_t dv_count);
+/* BruteForceGravity::evalSelfGravity (core/gravity/BruteForceGravity.h:38-58, evalImpl :110-129) for the
+ * particles listed in targets (host array of indices): a_i = G sum_{j != i} m_j grad W(r_j - r_i, (h_i + h_j)/2),
+ * summed in FP64 over all other particles in index order; acc receives 4 doubles per target (h component 0).
+ * The direct sum the Barnes-Hut walk approximates; O(targets x N). */
+sphgpu_status sphgpu_gravity_direct(sphgpu_handle* h, const uint32_t* targets, uint64_t ntargets, double* acc);
 /* StatisticsId::GRAVITY_NODES_APPROX / GRAVITY_NODES_EXACT / GRAVITY_NODE_COUNT of the last evaluation. */
 sphgpu_status sphgpu_gravity_stats(sphgpu_handle* h, uint64_t out[3]);
 /* Interactions evaluated by the last walk: out[0] particle-multipole evaluations (sum over leaves of
@@ -261,7 +289,10 @@ sphgpu_status sphgpu_set_time(sphgpu_handle* h, double t);
 /* HardSphereSolver::collide (core/gravity/NBodySolver.cpp:329-484) over the interval [0, dt): finds every
  * particle's earliest collision or overlap, resolves them in time order (re-searching the particles whose
  * pending collisions were invalidated), and removes merged particles, keeping the order of the others
- * (Storage::remove). N-body solver only; sphgpu_step calls it twice per leap-frog step. */
+ * (Storage::remove). N-body solver only; sphgpu_step calls it twice per leap-frog step. When the collision
+ * work space (pool_capacity records) runs out, SPHGPU_ERR_CAPACITY is returned with the collisions processed
+ * until then applied and their merged particles removed (mass and momentum conserved); the interval's remaining
+ * collisions are not processed. */
 sphgpu_status sphgpu_collide(sphgpu_handle* h, double dt);
 /* Current particle count (changes when collisions merge particles). */
 sphgpu_status sphgpu_particle_count(sphgpu_handle* h, uint64_t* n);
@@ -290,14 +321,20 @@ sphgpu_status sphgpu_totals_frame(sphgpu_handle* h, double omega, double out[9])
 /* Device NaN/Inf scan of the integrated state; SPHGPU_ERR_NONFINITE with the first bad particle index. */
 sphgpu_status sphgpu_check_finite(sphgpu_handle* h, uint64_t* first_bad);
 
+/* Measured FP32 FMA rate of the current device in TFLOP/s (independent FMA chains on every SM, one launch of about
+ * ms_target milliseconds timed with CUDA events): the denominator of FP32 roofline reports. No counterpart in the
+ * reference. */
+sphgpu_status sphgpu_measure_fp32_peak(double ms_target, double* tflops);
+
 /* Conserved totals without any allocation (no counterpart in the reference). For callers that cannot call
  * cudaMalloc: an application that owns the device memory budget and passes only its own buffers, or a
  * per-step hook that must not risk the implicit synchronisation of an allocation. r, v (4 doubles per
  * particle), m, u (1 double per particle) and totals (9 doubles, layout of sphgpu_totals) are DEVICE
  * pointers of the current device; the work is queued on `stream` (a cudaStream_t, NULL for the default
  * stream) and the call returns without synchronising. The scratch is a fixed 72 KiB array inside the
- * library, shared by all calls: calls whose kernels overlap on the GPU race, so serialise them. The first
- * call on a device looks up that array's device address (make it before any stream capture).
+ * library, shared by all calls: calls whose kernels overlap on the GPU race, so serialise them. Each call
+ * looks up that array's device address for the current device (a host-side query); the first call on a device
+ * may load the library's device code, so make it before any stream capture.
  * n above SPHGPU_TOTALS_NOALLOC_MAX_PARTICLES returns SPHGPU_ERR_CAPACITY (use sphgpu_totals). */
 #define SPHGPU_TOTALS_NOALLOC_MAX_PARTICLES 4194304u
 sphgpu_status sphgpu_totals_noalloc(const double* r, const double* v, const double* m, const double* u, uint64_t n,

@@ -170,7 +170,7 @@ class Config(ctypes.Structure):
         ("bounce_merge_limit", ctypes.c_double),
         ("rotation_merge_limit", ctypes.c_double),
         ("max_bounces", ctypes.c_uint32),
-        ("reserved2", ctypes.c_uint32),
+        ("collision_records", ctypes.c_uint32),
         ("gravity_recomputation_period", ctypes.c_double),
     ]
 

@@ -6,6 +6,7 @@
 
 #include "objects/Exceptions.h"
 #include "sph/solvers/StandardSets.h"
+#include "quantities/Attractor.h"
 #include "quantities/IMaterial.h"
 #include "quantities/Quantity.h"
 #include "system/Statistics.h"
@@ -434,6 +435,8 @@ void GpuBarnesHut::build(IScheduler& UNUSED(scheduler), const Storage& storage) 
         device = std::make_unique<DeviceState>(settings, storage, SPHGPU_PRECISION_FP64);
     }
     const Size n = storage.getParticleCnt();
+    positions = storage.getValue<Vector>(QuantityId::POSITION);
+    finderCurrent = false;
     device->check(
         sphgpu_set_quantity(device->get(), SPHGPU_Q_POSITION, 0, &storage.getValue<Vector>(QuantityId::POSITION)[0][0], n));
     device->check(sphgpu_set_quantity(device->get(), SPHGPU_Q_MASS, 0, &storage.getValue<Float>(QuantityId::MASS)[0], n));
@@ -451,9 +454,21 @@ void GpuBarnesHut::evalSelfGravity(IScheduler& UNUSED(scheduler), ArrayView<Vect
 
 void GpuBarnesHut::evalAttractors(IScheduler& UNUSED(scheduler),
     ArrayView<Attractor> attractors,
-    ArrayView<Vector> UNUSED(dv)) const {
-    if (!attractors.empty()) {
-        raise(true, "GpuBarnesHut does not evaluate attractors");
+    ArrayView<Vector> dv) const {
+    if (attractors.empty()) {
+        return;
+    }
+    // BarnesHut::evalAttractors (core/gravity/BarnesHut.cpp:100-125) on the device
+    std::vector<double> att, acc;
+    for (const Attractor& a : attractors) {
+        att.insert(att.end(), { a.position[X], a.position[Y], a.position[Z], a.radius, a.mass });
+        acc.insert(acc.end(), { a.acceleration[X], a.acceleration[Y], a.acceleration[Z] });
+    }
+    device->check(sphgpu_gravity_attractors(device->get(), att.data(), attractors.size(), acc.data(),
+        dv.empty() ? nullptr : &dv[0][0], dv.size()));
+    for (Size k = 0; k < attractors.size(); ++k) {
+        Vector& out = attractors[k].acceleration;
+        out = Vector(acc[3 * k], acc[3 * k + 1], acc[3 * k + 2], out[H]);
     }
 }
 
@@ -468,71 +483,84 @@ Float GpuBarnesHut::evalEnergy(IScheduler& UNUSED(scheduler), Statistics& UNUSED
 }
 
 RawPtr<const IBasicFinder> GpuBarnesHut::getFinder() const {
-    return nullptr;
+    if (!finderCurrent) {
+        if (!finder) {
+            finder = std::make_unique<GpuFinder>(settings);
+        }
+        finder->build(SEQUENTIAL, positions);
+        finderCurrent = true;
+    }
+    return finder.get();
 }
 
 // ---------------------------------------------------------------------------------------------------------
 
-GpuFinder::GpuFinder(const RunSettings& settings)
-    : settings(settings) {}
+GpuFinder::GpuFinder(const RunSettings& UNUSED(settings)) {}
+
+GpuFinder::~GpuFinder() {
+    sphgpu_destroy(handle);
+}
 
 void GpuFinder::buildImpl(IScheduler& UNUSED(scheduler), ArrayView<const Vector> points) {
     const Size n = points.size();
-    std::vector<sphgpu_material> mats(1);
-    mats[0].eos = SPHGPU_EOS_IDEAL_GAS;
-    mats[0].density = 1.;
-    mats[0].adiabatic_index = 1.4;
-    sphgpu_config cfg{};
-    cfg.particle_count = n;
-    cfg.material_count = 1;
-    cfg.materials = mats.data();
-    cfg.forces = SPHGPU_FORCE_PRESSURE;
-    cfg.gravity_leaf_size = 25;
-    cfg.gravity_multipole_order = 3;
-    sphgpu_handle* h = nullptr;
-    if (sphgpu_create(&cfg, &h) != SPHGPU_OK) {
-        raise(false, std::string("sphgpu: ") + sphgpu_last_error(nullptr));
+    if (!handle || handleCount != n) {
+        sphgpu_destroy(handle);
+        handle = nullptr;
+        sphgpu_material mat{};
+        mat.eos = SPHGPU_EOS_IDEAL_GAS;
+        mat.density = 1.;
+        mat.adiabatic_index = 1.4;
+        sphgpu_config cfg{};
+        cfg.particle_count = n;
+        cfg.material_count = 1;
+        cfg.materials = &mat;
+        cfg.forces = SPHGPU_FORCE_PRESSURE;
+        cfg.gravity_leaf_size = 25;
+        cfg.gravity_multipole_order = 3;
+        if (sphgpu_create(&cfg, &handle) != SPHGPU_OK) {
+            handle = nullptr;
+            raise(false, std::string("sphgpu: ") + sphgpu_last_error(nullptr));
+        }
+        handleCount = n;
     }
-    uint64_t npairs = 0;
-    std::vector<uint32_t> pi, pj;
-    int rc = sphgpu_set_quantity(h, SPHGPU_Q_POSITION, 0, &points[0][0], n);
-    if (rc == SPHGPU_OK) {
-        rc = sphgpu_get_pairs(h, nullptr, nullptr, 0, &npairs);
-        pi.resize(npairs);
-        pj.resize(npairs);
-        rc = sphgpu_get_pairs(h, pi.data(), pj.data(), npairs, &npairs);
-    }
-    const std::string err = sphgpu_last_error(h);
-    sphgpu_destroy(h);
-    if (rc != SPHGPU_OK) {
-        raise(false, "sphgpu: " + err);
-    }
+    auto check = [&](int rc) {
+        if (rc != SPHGPU_OK) {
+            raise(false, std::string("sphgpu: ") + sphgpu_last_error(handle));
+        }
+    };
     start.assign(n + 1, 0);
+    neighbours.clear();
+    if (n == 0) {
+        return;
+    }
+    check(sphgpu_set_quantity(handle, SPHGPU_Q_POSITION, 0, &points[0][0], n));
+    // the ball of radius 2 h_i of every particle, directed pairs sorted by i then j
+    uint64_t npairs = 0;
+    const int rc = sphgpu_get_radius_pairs(handle, nullptr, nullptr, 0, &npairs);
+    if (rc != SPHGPU_OK && rc != SPHGPU_ERR_CAPACITY) {
+        check(rc);
+    }
+    std::vector<uint32_t> pi(npairs), pj(npairs);
+    if (npairs) {
+        check(sphgpu_get_radius_pairs(handle, pi.data(), pj.data(), npairs, &npairs));
+    }
     for (uint64_t k = 0; k < npairs; ++k) {
         start[pi[k] + 1]++;
-        start[pj[k] + 1]++;
     }
     for (Size i = 0; i < n; ++i) {
         start[i + 1] += start[i];
     }
-    neighbours.resize(start[n]);
-    std::vector<Size> fill(start.begin(), start.end() - 1);
-    for (uint64_t k = 0; k < npairs; ++k) {
-        neighbours[fill[pi[k]]++] = pj[k];
-        neighbours[fill[pj[k]]++] = pi[k];
-    }
+    neighbours.assign(pj.begin(), pj.end());
 }
 
 template <bool FindAll>
 Size GpuFinder::find(const Vector& pos, const Size index, const Float radius, Array<NeighborRecord>& neighs) const {
-    // queries of particles are answered from the GPU pair set (radius 2 h_i of SymmetricSolver::loop);
-    // arbitrary points fall back to a scan of the stored values
-    if (index < values.size() && almostEqual(radius, 2._f * values[index][H])) {
+    if (index < values.size() && radius == 2._f * values[index][H]) {
+        // the query of the SPH loops, from the lists of the build
         for (Size k = start[index]; k < start[index + 1]; ++k) {
             const Size j = neighbours[k];
-            const Float distSqr = getSqrLength(values[j] - pos);
-            if (distSqr < sqr(radius) && (FindAll || rank[j] < rank[index])) {
-                neighs.push(NeighborRecord{ j, distSqr });
+            if (FindAll || rank[j] < rank[index]) {
+                neighs.push(NeighborRecord{ j, getSqrLength(values[j] - pos) });
             }
         }
         if (FindAll) {
@@ -540,10 +568,26 @@ Size GpuFinder::find(const Vector& pos, const Size index, const Float radius, Ar
         }
         return neighs.size();
     }
-    for (Size j = 0; j < values.size(); ++j) {
-        const Float distSqr = getSqrLength(values[j] - pos);
-        if (distSqr < sqr(radius) && (FindAll || rank[j] < rank[index])) {
-            neighs.push(NeighborRecord{ j, distSqr });
+    // any other ball on the device
+    const double p[3] = { pos[X], pos[Y], pos[Z] };
+    uint64_t count = 0;
+    if (queryIdx.empty()) {
+        queryIdx.resize(256);
+        queryDistSqr.resize(256);
+    }
+    int rc = sphgpu_find_neighbors(handle, p, radius, queryIdx.data(), queryDistSqr.data(), queryIdx.size(), &count);
+    if (rc == SPHGPU_ERR_CAPACITY) {
+        queryIdx.resize(count);
+        queryDistSqr.resize(count);
+        rc = sphgpu_find_neighbors(handle, p, radius, queryIdx.data(), queryDistSqr.data(), queryIdx.size(), &count);
+    }
+    if (rc != SPHGPU_OK) {
+        raise(false, std::string("sphgpu: ") + sphgpu_last_error(handle));
+    }
+    for (uint64_t k = 0; k < count; ++k) {
+        const Size j = queryIdx[k];
+        if (FindAll || index >= values.size() || rank[j] < rank[index]) {
+            neighs.push(NeighborRecord{ j, queryDistSqr[k] });
         }
     }
     return neighs.size();

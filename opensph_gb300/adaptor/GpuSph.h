@@ -158,10 +158,17 @@ public:
     virtual Expected<Path> dump(const Storage& storage, const Statistics& stats) override;
 };
 
-/// IGravity drop-in: k-d tree, moments and tree walk on the device.
+class GpuFinder;
+
+/// IGravity drop-in: k-d tree, moments and tree walk on the device. getFinder returns a GpuFinder over the
+/// positions of the last build (built on first use after each build), as BarnesHut returns its k-d tree
+/// (core/gravity/BarnesHut.cpp:496-499).
 class GpuBarnesHut : public IGravity {
     RunSettings settings;
     mutable std::unique_ptr<DeviceState> device;
+    ArrayView<const Vector> positions;
+    mutable std::unique_ptr<GpuFinder> finder;
+    mutable bool finderCurrent = false;
 
 public:
     explicit GpuBarnesHut(const RunSettings& settings);
@@ -177,17 +184,26 @@ public:
     virtual RawPtr<const IBasicFinder> getFinder() const override;
 };
 
-/// ISymmetricFinder drop-in: the pair set of the GPU grid, answered per particle from CSR lists.
+/// ISymmetricFinder drop-in on the library's cell grid. One device handle is kept across builds (created again
+/// only when the particle count changes). The query of SymmetricSolver::loop, findAll / findLowerRank(i, 2 h_i),
+/// is answered from the per-particle lists of sphgpu_get_radius_pairs fetched at build; every other query (another
+/// radius, an arbitrary point) runs on the device (sphgpu_find_neighbors). The sets are those of KdTree::find.
 class GpuFinder : public FinderTemplate<GpuFinder> {
+    sphgpu_handle* handle = nullptr;
+    Size handleCount = 0;
     std::vector<Size> start;
     std::vector<Size> neighbours;
-    RunSettings settings;
+    mutable std::vector<uint32_t> queryIdx;
+    mutable std::vector<double> queryDistSqr;
 
 protected:
     virtual void buildImpl(IScheduler& scheduler, ArrayView<const Vector> points) override;
 
 public:
     explicit GpuFinder(const RunSettings& settings);
+    ~GpuFinder() override;
+    GpuFinder(const GpuFinder&) = delete;
+    GpuFinder& operator=(const GpuFinder&) = delete;
 
     template <bool FindAll>
     Size find(const Vector& pos, const Size index, const Float radius, Array<NeighborRecord>& neighs) const;

@@ -31,6 +31,7 @@ UNITS = {
     "sph32.cu": [],
     "gravity32.cu": [],
     "noalloc.cu": [],
+    "peak.cu": [],
     "adjoint.cu": ["-fmad=false"],
     "nbody.cu": ["-fmad=false"],
 }

@@ -45,6 +45,8 @@ struct sphgpu_handle {
     std::vector<void*> allocations;
     std::string error;
     bool gravity_current = false;
+    // the neighbour grid of sphgpu_build_neighbors is that of the current positions (point queries use it)
+    bool grid_current = false;
     // profiling: device time per phase (CUDA events on the handle's stream) and own kernel launches
     bool profiling = false;
     std::vector<cudaEvent_t> event_pool;
@@ -472,6 +474,8 @@ sphgpu_status collideNbody(sphgpu_handle* h, const double* dt, double factor) {
     const int st = nbodyCollide(h->s, h->grid, h->coll, h->cp, dt, factor, &capacityError, h->stream);
     h->launches += h->coll.launches;
     if (st == SPHGPU_ERR_CAPACITY) {
+        // the collisions processed before the work space ran out are applied and their mergers removed
+        h->gravity_current = false;
         return fail(h, SPHGPU_ERR_CAPACITY, "collision work space exhausted (bits 0x%x: 1 records, 2 heap, "
                                             "4 invalidated particles, 8 moved-particle lists)", capacityError);
     }
@@ -819,7 +823,7 @@ sphgpu_status sphgpu_create(const sphgpu_config* config, sphgpu_handle** out) {
         e = treeAllocate(h->tree, n, ph.leaf_size);
     }
     if (e == cudaSuccess && ph.nbody) {
-        e = collideAllocate(h->coll, n, h->grid.cell_capacity);
+        e = collideAllocate(h->coll, n, h->grid.cell_capacity, config->collision_records);
     }
     if (e != cudaSuccess) {
         const std::string msg = std::string("device allocation failed: ") + cudaGetErrorString(e);
@@ -963,6 +967,9 @@ sphgpu_status sphgpu_set_quantity(sphgpu_handle* h, int32_t id, int32_t order, c
         return fail(h, SPHGPU_ERR_ARGUMENT, "quantity %d: %llu values given for %u particles", id,
             (unsigned long long)count, h->s.n);
     }
+    if (id == SPHGPU_Q_POSITION && order == 0) {
+        h->grid_current = false;
+    }
     const size_t n = count;
     if (q.soa) {
         const double* a = static_cast<const double*>(src);
@@ -1028,10 +1035,91 @@ sphgpu_status sphgpu_build_neighbors(sphgpu_handle* h) {
     launchGridBuild(h->s, h->grid, h->ph, h->stream);
     launchGatherSorted(h->s, h->grid, h->ph, h->stream);
     CUDA_TRY(h, cudaGetLastError());
+    h->grid_current = true;
     return SPHGPU_OK;
 }
 
+sphgpu_status sphgpu_find_neighbors(sphgpu_handle* h, const double pos[3], double radius, uint32_t* indices,
+    double* dist_sqr, uint64_t capacity, uint64_t* count) {
+    if (!h || !pos || !count || (capacity && (!indices || !dist_sqr)) || !(radius >= 0.)) {
+        return h ? fail(h, SPHGPU_ERR_ARGUMENT, "invalid query arguments") : SPHGPU_ERR_ARGUMENT;
+    }
+    if (!h->grid_current) {
+        return fail(h, SPHGPU_ERR_STATE, "find_neighbors needs sphgpu_build_neighbors of the current positions");
+    }
+    const uint64_t cap = std::min<uint64_t>(capacity, h->s.n);
+    uint32_t* di = nullptr;
+    double* dd = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (cap) {
+        e = cudaMalloc(&di, cap * sizeof(uint32_t));
+        if (e == cudaSuccess) {
+            e = cudaMalloc(&dd, cap * sizeof(double));
+        }
+    }
+    const dbl4 p = mkd4(pos[0], pos[1], pos[2], 0.);
+    if (e == cudaSuccess) {
+        launchFindBall(h->grid, h->s.n, p, radius, di, dd, h->d_count, cap, h->stream);
+        h->launches += 1;
+        e = cudaMemcpyAsync(h->h_pinned, h->d_count, sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->stream);
+    }
+    if (e == cudaSuccess) {
+        e = cudaStreamSynchronize(h->stream);
+    }
+    const uint64_t total = e == cudaSuccess ? h->h_pinned[0] : 0;
+    std::vector<uint32_t> idx;
+    std::vector<double> d2;
+    if (e == cudaSuccess && total <= capacity && total > 0) {
+        idx.resize(total);
+        d2.resize(total);
+        e = cudaMemcpy(idx.data(), di, total * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) {
+            e = cudaMemcpy(d2.data(), dd, total * sizeof(double), cudaMemcpyDeviceToHost);
+        }
+    }
+    cudaFree(di);
+    cudaFree(dd);
+    if (e != cudaSuccess) {
+        return cudaFail(h, e, "find neighbors");
+    }
+    *count = total;
+    if (total > capacity) {
+        return fail(h, SPHGPU_ERR_CAPACITY, "%llu neighbours, capacity %llu", (unsigned long long)total,
+            (unsigned long long)capacity);
+    }
+    // ascending particle index (the device emits them unordered)
+    std::vector<uint64_t> order(total);
+    for (uint64_t k = 0; k < total; ++k) {
+        order[k] = k;
+    }
+    std::sort(order.begin(), order.end(), [&](uint64_t a, uint64_t b) { return idx[a] < idx[b]; });
+    for (uint64_t k = 0; k < total; ++k) {
+        indices[k] = idx[order[k]];
+        dist_sqr[k] = d2[order[k]];
+    }
+    return SPHGPU_OK;
+}
+
+namespace {
+
+sphgpu_status listPairs(sphgpu_handle* h, bool directed, uint32_t* pair_i, uint32_t* pair_j, uint64_t capacity,
+    uint64_t* npairs);
+
+} // namespace
+
 sphgpu_status sphgpu_get_pairs(sphgpu_handle* h, uint32_t* pair_i, uint32_t* pair_j, uint64_t capacity,
+    uint64_t* npairs) {
+    return listPairs(h, false, pair_i, pair_j, capacity, npairs);
+}
+
+sphgpu_status sphgpu_get_radius_pairs(sphgpu_handle* h, uint32_t* pair_i, uint32_t* pair_j, uint64_t capacity,
+    uint64_t* npairs) {
+    return listPairs(h, true, pair_i, pair_j, capacity, npairs);
+}
+
+namespace {
+
+sphgpu_status listPairs(sphgpu_handle* h, bool directed, uint32_t* pair_i, uint32_t* pair_j, uint64_t capacity,
     uint64_t* npairs) {
     if (!h || !npairs || (capacity && (!pair_i || !pair_j))) {
         return h ? fail(h, SPHGPU_ERR_ARGUMENT, "invalid pair buffers") : SPHGPU_ERR_ARGUMENT;
@@ -1040,7 +1128,11 @@ sphgpu_status sphgpu_get_pairs(sphgpu_handle* h, uint32_t* pair_i, uint32_t* pai
     if (st != SPHGPU_OK) {
         return st;
     }
-    launchCountPairs(h->s, h->grid, h->d_count, h->stream);
+    if (directed) {
+        launchRadiusPairs(h->s, h->grid, nullptr, nullptr, h->d_count, 0, h->stream);
+    } else {
+        launchCountPairs(h->s, h->grid, h->d_count, h->stream);
+    }
     CUDA_TRY(h, cudaMemcpyAsync(h->h_pinned, h->d_count, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
         h->stream));
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
@@ -1060,7 +1152,11 @@ sphgpu_status sphgpu_get_pairs(sphgpu_handle* h, uint32_t* pair_i, uint32_t* pai
         cudaFree(dpi);
         return cudaFail(h, e, "pair buffer");
     }
-    launchListPairs(h->s, h->grid, dpi, dpj, h->d_count, total, h->stream);
+    if (directed) {
+        launchRadiusPairs(h->s, h->grid, dpi, dpj, h->d_count, total, h->stream);
+    } else {
+        launchListPairs(h->s, h->grid, dpi, dpj, h->d_count, total, h->stream);
+    }
     std::vector<uint32_t> a(total), b(total);
     e = cudaMemcpyAsync(a.data(), dpi, total * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream);
     if (e == cudaSuccess) {
@@ -1085,6 +1181,8 @@ sphgpu_status sphgpu_get_pairs(sphgpu_handle* h, uint32_t* pair_i, uint32_t* pai
     }
     return SPHGPU_OK;
 }
+
+} // namespace
 
 sphgpu_status sphgpu_gravity_build(sphgpu_handle* h) {
     if (!h) {
@@ -1115,17 +1213,29 @@ sphgpu_status sphgpu_gravity_eval(sphgpu_handle* h, double* dv, uint64_t count) 
         return fail(h, SPHGPU_ERR_ARGUMENT, "dv holds %llu particles, state has %u", (unsigned long long)count,
             h->s.n);
     }
-    {
-        Phase ph(h, SPHGPU_PHASE_GRAVITY_EVAL);
-        if (h->ph.precision == SPHGPU_PRECISION_MIXED) {
-            launchGravityWalkMixed(h->s, h->tree, h->ph, h->d_lut_grav_f, h->d_err, h->stream);
-            h->launches += h->tree.walk_launches;
-        } else {
-            launchGravityWalk(h->s, h->tree, h->ph, h->d_lut_grav, h->d_err, h->stream);
-            h->launches += 1;
+    // the walk, again with check lists four times as long when one outgrew them (small opening angles)
+    for (int attempt = 0;; ++attempt) {
+        {
+            Phase ph(h, SPHGPU_PHASE_GRAVITY_EVAL);
+            if (h->ph.precision == SPHGPU_PRECISION_MIXED) {
+                launchGravityWalkMixed(h->s, h->tree, h->ph, h->d_lut_grav_f, h->d_err, h->stream);
+                h->launches += h->tree.walk_launches;
+            } else {
+                launchGravityWalk(h->s, h->tree, h->ph, h->d_lut_grav, h->d_err, h->stream);
+                h->launches += 1;
+            }
         }
+        CUDA_TRY(h, cudaGetLastError());
+        CUDA_TRY(h, cudaMemcpyAsync(h->h_pinned, h->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        const uint32_t bits = *reinterpret_cast<uint32_t*>(h->h_pinned);
+        if (bits == uint32_t(DEV_ERR_WALK_CAPACITY) && attempt < 3) {
+            CUDA_TRY(h, cudaMemsetAsync(h->d_err, 0, sizeof(uint32_t), h->stream));
+            CUDA_TRY(h, treeGrowWalkScratch(h->tree, 4 * h->tree.walk_capacity));
+            continue;
+        }
+        break;
     }
-    CUDA_TRY(h, cudaGetLastError());
     const sphgpu_status st = checkDeviceError(h);
     if (st != SPHGPU_OK) {
         return st;
@@ -1140,6 +1250,104 @@ sphgpu_status sphgpu_gravity_eval(sphgpu_handle* h, double* dv, uint64_t count) 
                 dv[4 * i + c] += a[4 * i + c];
             }
         }
+    }
+    return SPHGPU_OK;
+}
+
+sphgpu_status sphgpu_gravity_attractors(sphgpu_handle* h, const double* attractors, uint64_t count,
+    double* attractor_acc, double* dv, uint64_t dv_count) {
+    if (!h || (count && (!attractors || !attractor_acc)) || (dv && dv_count != h->s.n) || count > 0xffffull) {
+        return h ? fail(h, SPHGPU_ERR_ARGUMENT, "invalid attractor or acceleration buffers") : SPHGPU_ERR_ARGUMENT;
+    }
+    if (!h->ph.gravity) {
+        return fail(h, SPHGPU_ERR_STATE, "gravity_attractors without self-gravity");
+    }
+    if (count == 0) {
+        return SPHGPU_OK;
+    }
+    const uint32_t n = h->s.n;
+    const size_t partials = gravityAttractorPartials(n, uint32_t(count));
+    double* dAtt = nullptr;
+    double* dAcc = nullptr;
+    double* dPart = nullptr;
+    dbl4* dDv = nullptr;
+    cudaError_t e = cudaMalloc(&dAtt, 5 * count * sizeof(double));
+    if (e == cudaSuccess) {
+        e = cudaMalloc(&dAcc, 3 * count * sizeof(double));
+    }
+    if (e == cudaSuccess && partials) {
+        e = cudaMalloc(&dPart, partials * sizeof(double));
+    }
+    if (e == cudaSuccess && n) {
+        e = cudaMalloc(&dDv, size_t(n) * sizeof(dbl4));
+    }
+    if (e == cudaSuccess) {
+        e = cudaMemcpyAsync(dAtt, attractors, 5 * count * sizeof(double), cudaMemcpyHostToDevice, h->stream);
+    }
+    if (e == cudaSuccess) {
+        e = cudaMemcpyAsync(dAcc, attractor_acc, 3 * count * sizeof(double), cudaMemcpyHostToDevice, h->stream);
+    }
+    if (e == cudaSuccess && n) {
+        e = dv ? cudaMemcpyAsync(dDv, dv, size_t(n) * sizeof(dbl4), cudaMemcpyHostToDevice, h->stream)
+               : cudaMemsetAsync(dDv, 0, size_t(n) * sizeof(dbl4), h->stream);
+    }
+    if (e == cudaSuccess) {
+        launchGravityAttractors(h->s, h->ph, h->d_lut_grav, dAtt, uint32_t(count), dDv, dPart, dAcc, h->stream);
+        h->launches += 2;
+        e = cudaMemcpyAsync(attractor_acc, dAcc, 3 * count * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+    }
+    if (e == cudaSuccess && dv && n) {
+        e = cudaMemcpyAsync(dv, dDv, size_t(n) * sizeof(dbl4), cudaMemcpyDeviceToHost, h->stream);
+    }
+    if (e == cudaSuccess) {
+        e = cudaStreamSynchronize(h->stream);
+    }
+    for (void* p : { (void*)dAtt, (void*)dAcc, (void*)dPart, (void*)dDv }) {
+        if (p) {
+            cudaFree(p);
+        }
+    }
+    if (e != cudaSuccess) {
+        return cudaFail(h, e, "gravity attractors");
+    }
+    return SPHGPU_OK;
+}
+
+sphgpu_status sphgpu_gravity_direct(sphgpu_handle* h, const uint32_t* targets, uint64_t ntargets, double* acc) {
+    if (!h || (ntargets && (!targets || !acc)) || ntargets > 0xffffffffull) {
+        return h ? fail(h, SPHGPU_ERR_ARGUMENT, "invalid target buffers") : SPHGPU_ERR_ARGUMENT;
+    }
+    if (!h->ph.gravity) {
+        return fail(h, SPHGPU_ERR_STATE, "gravity_direct without self-gravity");
+    }
+    for (uint64_t k = 0; k < ntargets; ++k) {
+        if (targets[k] >= h->s.n) {
+            return fail(h, SPHGPU_ERR_ARGUMENT, "target %llu out of range", (unsigned long long)targets[k]);
+        }
+    }
+    if (ntargets == 0) {
+        return SPHGPU_OK;
+    }
+    uint32_t* dt = nullptr;
+    dbl4* da = nullptr;
+    CUDA_TRY(h, cudaMalloc(&dt, ntargets * sizeof(uint32_t)));
+    cudaError_t e = cudaMalloc(&da, ntargets * sizeof(dbl4));
+    if (e == cudaSuccess) {
+        e = cudaMemcpyAsync(dt, targets, ntargets * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream);
+    }
+    if (e == cudaSuccess) {
+        launchGravityDirect(h->s, h->ph, h->d_lut_grav, dt, uint32_t(ntargets), da, h->stream);
+        e = cudaMemcpyAsync(acc, da, ntargets * sizeof(dbl4), cudaMemcpyDeviceToHost, h->stream);
+    }
+    if (e == cudaSuccess) {
+        e = cudaStreamSynchronize(h->stream);
+    }
+    cudaFree(dt);
+    if (da) {
+        cudaFree(da);
+    }
+    if (e != cudaSuccess) {
+        return cudaFail(h, e, "gravity direct");
     }
     return SPHGPU_OK;
 }
@@ -1214,6 +1422,7 @@ sphgpu_status sphgpu_integrate(sphgpu_handle* h) {
     if (!h) {
         return SPHGPU_ERR_ARGUMENT;
     }
+    h->grid_current = false;
     const sphgpu_status cst = decideGravityCache(h);
     if (cst != SPHGPU_OK) {
         return cst;
@@ -1244,6 +1453,7 @@ sphgpu_status sphgpu_step(sphgpu_handle* h, uint32_t nsteps) {
     if (!h) {
         return SPHGPU_ERR_ARGUMENT;
     }
+    h->grid_current = false;
     for (uint32_t k = 0; k < nsteps; ++k) {
         if (h->ph.nbody) {
             const sphgpu_status st = stepNbody(h);

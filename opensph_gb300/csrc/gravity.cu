@@ -538,7 +538,176 @@ __global__ void pointsKernel(const dbl4* __restrict__ r, const double* __restric
     acc[k] = mkd4(ax, ay, az, 0.);
 }
 
+// BruteForceGravity::evalSelfGravity for listed particles (core/gravity/BruteForceGravity.h:38-58, evalImpl
+// :110-129): a_i = G sum_{j != i} m_j grad(r_j - r_i) with the symmetrised smoothing length, in FP64 and in index
+// order, as the reference sums it. One thread per target; the sources in tiles staged in shared memory.
+constexpr int DIRECT_THREADS = 128;
+
+__global__ void __launch_bounds__(DIRECT_THREADS) directKernel(const dbl4* __restrict__ r,
+    const double* __restrict__ m, double G, uint32_t n, const uint32_t* __restrict__ targets, uint32_t nt,
+    const double* __restrict__ lut, int kernelRadius, dbl4* acc) {
+    __shared__ dbl4 shR[DIRECT_THREADS];
+    __shared__ double shM[DIRECT_THREADS];
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = k < nt;
+    const uint32_t i = valid ? targets[k] : 0u;
+    const dbl4 ri = valid && i < n ? r[i] : mkd4(0., 0., 0., 0.);
+    double ax = 0., ay = 0., az = 0.;
+    for (uint32_t base = 0; base < n; base += DIRECT_THREADS) {
+        const uint32_t j = base + threadIdx.x;
+        if (j < n) {
+            shR[threadIdx.x] = r[j];
+            shM[threadIdx.x] = m[j];
+        }
+        __syncthreads();
+        const uint32_t cnt = min(uint32_t(DIRECT_THREADS), n - base);
+        if (valid) {
+            for (uint32_t t = 0; t < cnt; ++t) {
+                if (base + t == i) {
+                    continue;
+                }
+                const dbl4 rj = shR[t];
+                double gx, gy, gz;
+                gravGrad(rj.x - ri.x, rj.y - ri.y, rj.z - ri.z, 0.5 * (rj.w + ri.w), lut, kernelRadius, gx, gy, gz);
+                const double mj = shM[t];
+                ax += mj * gx;
+                ay += mj * gy;
+                az += mj * gz;
+            }
+        }
+        __syncthreads();
+    }
+    if (valid) {
+        acc[k] = mkd4(G * ax, G * ay, G * az, 0.);
+    }
+}
+
+// BarnesHut::evalAttractors (core/gravity/BarnesHut.cpp:100-125), attractor-particle part: thread i subtracts
+// (G M_a) grad W(r_i - x_a, (h_i + R_a) / 2) of each attractor in order from dv_i (all four components: the
+// reference scales the whole separation Vector); each block sums (G m_i) grad W per attractor in thread order
+// into partial[block][a][3].
+constexpr int ATT_THREADS = 256;
+
+__device__ __forceinline__ void gravGrad4(const double r[4], double h, const double* __restrict__ lut,
+    int kernelRadius, double g[4]) {
+    const double hInv = 1. / h;
+    const double sx = r[0] * hInv, sy = r[1] * hInv, sz = r[2] * hInv;
+    const double qSqr = sx * sx + sy * sy + sz * sz;
+    const double rad = double(kernelRadius);
+    if (qSqr + SPH_EPS >= rad * rad) {
+        const double len = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+        const double l3 = len * len * len;
+        for (int c = 0; c < 4; ++c) {
+            g[c] = r[c] / l3;
+        }
+        return;
+    }
+    const double floatIdx = (double(LUT_ENTRIES) * (1. / (2. * 2.))) * qSqr;
+    const int idx1 = int(floatIdx);
+    const double ratio = floatIdx - double(idx1);
+    const double gr = __ldg(lut + idx1) * (1. - ratio) + __ldg(lut + idx1 + 1) * ratio;
+    const double h3 = hInv * hInv * hInv;
+    for (int c = 0; c < 4; ++c) {
+        g[c] = (h3 * r[c]) * gr;
+    }
+}
+
+__global__ void __launch_bounds__(ATT_THREADS) attractorParticlesKernel(const dbl4* __restrict__ r,
+    const double* __restrict__ m, double G, uint32_t n, const double* __restrict__ att, uint32_t count,
+    const double* __restrict__ lut, int kernelRadius, dbl4* dv, double* partial) {
+    __shared__ double sh[3][ATT_THREADS];
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = i < n;
+    dbl4 ri = mkd4(0., 0., 0., 0.), d = mkd4(0., 0., 0., 0.);
+    double mi = 0.;
+    if (valid) {
+        ri = r[i];
+        d = dv[i];
+        mi = G * m[i];
+    }
+    for (uint32_t a = 0; a < count; ++a) {
+        const double* xa = att + 5 * a;
+        double f[4] = { 0., 0., 0., 0. };
+        if (valid) {
+            const double sep[4] = { ri.x - xa[0], ri.y - xa[1], ri.z - xa[2], ri.w - xa[3] };
+            gravGrad4(sep, 0.5 * (ri.w + xa[3]), lut, kernelRadius, f);
+            const double gm = G * xa[4];
+            d.x -= gm * f[0];
+            d.y -= gm * f[1];
+            d.z -= gm * f[2];
+            d.w -= gm * f[3];
+        }
+        for (int c = 0; c < 3; ++c) {
+            sh[c][threadIdx.x] = mi * f[c];
+        }
+        __syncthreads();
+        if (threadIdx.x < 3) {
+            double acc = 0.;
+            for (int t = 0; t < ATT_THREADS; ++t) {
+                acc += sh[threadIdx.x][t];
+            }
+            partial[(size_t(blockIdx.x) * count + a) * 3 + threadIdx.x] = acc;
+        }
+        __syncthreads();
+    }
+    if (valid) {
+        dv[i] = d;
+    }
+}
+
+// the attractors' accelerations: block partial sums in block order, then the attractor-attractor terms of each
+// pair i < j in order (f = G grad W(x_i - x_j, (R_i + R_j) / 2), acc_i -= M_j f, acc_j += M_i f). One thread.
+__global__ void attractorFinishKernel(const double* __restrict__ partial, uint32_t blocks, const double* __restrict__ att,
+    uint32_t count, double G, const double* __restrict__ lut, int kernelRadius, double* acc) {
+    for (uint32_t a = 0; a < count; ++a) {
+        for (int c = 0; c < 3; ++c) {
+            double s = acc[3 * a + c];
+            for (uint32_t b = 0; b < blocks; ++b) {
+                s += partial[(size_t(b) * count + a) * 3 + c];
+            }
+            acc[3 * a + c] = s;
+        }
+    }
+    for (uint32_t i = 0; i < count; ++i) {
+        for (uint32_t j = i + 1; j < count; ++j) {
+            const double* xi = att + 5 * i;
+            const double* xj = att + 5 * j;
+            const double sep[4] = { xi[0] - xj[0], xi[1] - xj[1], xi[2] - xj[2], xi[3] - xj[3] };
+            double g[4];
+            gravGrad4(sep, 0.5 * (xi[3] + xj[3]), lut, kernelRadius, g);
+            for (int c = 0; c < 3; ++c) {
+                const double f = G * g[c];
+                acc[3 * i + c] -= xj[4] * f;
+                acc[3 * j + c] += xi[4] * f;
+            }
+        }
+    }
+}
+
 } // namespace
+
+void launchGravityAttractors(const DState& s, const Physics& ph, const double* lut, const double* att, uint32_t count,
+    dbl4* dv, double* partial, double* acc, cudaStream_t st) {
+    const uint32_t blocks = s.n ? uint32_t(ceilDiv(s.n, ATT_THREADS)) : 0u;
+    if (blocks && count) {
+        attractorParticlesKernel<<<blocks, ATT_THREADS, 0, st>>>(s.r, s.m, ph.G, s.n, att, count, lut,
+            ph.kernel_radius, dv, partial);
+    }
+    attractorFinishKernel<<<1, 1, 0, st>>>(partial, blocks, att, count, ph.G, lut, ph.kernel_radius, acc);
+}
+
+uint32_t gravityAttractorPartials(uint32_t n, uint32_t count) {
+    return (n ? uint32_t(ceilDiv(n, ATT_THREADS)) : 0u) * count * 3u;
+}
+
+void launchGravityDirect(const DState& s, const Physics& ph, const double* lut, const uint32_t* targets, uint32_t nt,
+    dbl4* acc, cudaStream_t st) {
+    if (nt == 0) {
+        return;
+    }
+    directKernel<<<ceilDiv(nt, DIRECT_THREADS), DIRECT_THREADS, 0, st>>>(s.r, s.m, ph.G, s.n, targets, nt, lut,
+        ph.kernel_radius, acc);
+}
 
 cudaError_t treeAllocate(Tree& t, uint32_t n, uint32_t leafSize) {
     const uint32_t nn = n > 0 ? n : 1;
@@ -575,6 +744,16 @@ cudaError_t treeAllocate(Tree& t, uint32_t n, uint32_t leafSize) {
         e = treeBuildAllocate(t, nn);
     }
     return e;
+}
+
+cudaError_t treeGrowWalkScratch(Tree& t, uint32_t capacity) {
+    if (capacity <= t.walk_capacity) {
+        return cudaSuccess;
+    }
+    cudaFree(t.walk_scratch);
+    t.walk_scratch = nullptr;
+    t.walk_capacity = capacity;
+    return cudaMalloc((void**)&t.walk_scratch, size_t(t.walk_warps) * 2 * t.walk_capacity * sizeof(int32_t));
 }
 
 void treeFree(Tree& t) {

@@ -715,7 +715,9 @@ void launchGravityWalkMixed(const DState& s, Tree& t, const Physics& ph, const f
     }
     // per-warp staging of one node's lists in the walk scratch: 4 lists of NL_STAGE entries in the first pass
     // of a level, of NL_STAGE_DEFER entries in the pass over the nodes deferred by the first
-    constexpr uint32_t NL_STAGE = 4096, NL_STAGE_DEFER = 16384;
+    // (the staging grows with the walk scratch: sphgpu_gravity_eval enlarges it and walks again when a list
+    // outgrew it)
+    const uint32_t NL_STAGE = t.walk_capacity, NL_STAGE_DEFER = 4 * t.walk_capacity;
     const size_t scratchEntries = size_t(t.walk_warps) * 2 * t.walk_capacity;
     const uint32_t listWarps = std::max(1u, uint32_t(scratchEntries / (4 * size_t(NL_STAGE))));
     const uint32_t deferWarps = std::max(1u, uint32_t(scratchEntries / (4 * size_t(NL_STAGE_DEFER))));

@@ -229,7 +229,18 @@ __device__ __forceinline__ bool interacts(const dbl4& a, const dbl4& b) {
     return d2 < __dmul_rn(rad, rad);
 }
 
-template <bool List>
+// the query of findAll(i, 2 h_i) (KdTree::find, core/objects/finders/KdTree.inl.h:316-391): |r_j - r_i|^2 <
+// (2 h_i)^2 in FP64
+__device__ __forceinline__ bool withinTwoH(const dbl4& a, const dbl4& b) {
+    const double dx = __dsub_rn(b.x, a.x), dy = __dsub_rn(b.y, a.y), dz = __dsub_rn(b.z, a.z);
+    const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+    const double rad = __dmul_rn(2., a.w);
+    return d2 < __dmul_rn(rad, rad);
+}
+
+// Directed = false: the unordered interacting pairs (i < j, 2 h_bar); true: the directed pairs (i, j), j != i, of
+// every particle's ball of radius 2 h_i (the cell edge is at least 2 max h, so 27 cells hold either set)
+template <bool List, bool Directed = false>
 __global__ void pairsKernel(uint32_t n, const dbl4* __restrict__ rs, const uint32_t* __restrict__ perm,
     const uint32_t* __restrict__ keys, const uint32_t* __restrict__ cstart, const uint32_t* __restrict__ cend,
     const GridInfo* __restrict__ g, uint32_t* pi, uint32_t* pj, unsigned long long* count,
@@ -251,7 +262,7 @@ __global__ void pairsKernel(uint32_t n, const dbl4* __restrict__ rs, const uint3
                 const uint32_t e = cend[c];
                 for (uint32_t t = cstart[c]; t < e; ++t) {
                     const uint32_t j = perm[t];
-                    if (j <= i || !interacts(ri, rs[t])) {
+                    if (Directed ? (j == i || !withinTwoH(ri, rs[t])) : (j <= i || !interacts(ri, rs[t]))) {
                         continue;
                     }
                     const unsigned long long slot = atomicAdd(count, 1ull);
@@ -369,6 +380,68 @@ void launchGatherSorted(const DState& s, Grid& g, const Physics& ph, cudaStream_
     }
     gatherSorted<<<ceilDiv(s.n, 256), 256, 0, st>>>(s, g.perm, g.rs, g.vs, g.ms, g.rhos, g.ps, g.css, g.Ss,
         g.reduces, g.flags, ph.solid);
+}
+
+// ISymmetricFinder::findAll(const Vector& pos, radius) (core/objects/finders/NeighborFinder.h:112-117) on the grid:
+// every particle j with |r_j - pos|^2 < radius^2 (xyz, FP64, the test of KdTree::find), from the cells that the
+// ball's bounding box overlaps. Output slots are taken atomically (unordered); count keeps counting past capacity.
+__global__ void findBallKernel(const dbl4* __restrict__ rs, const uint32_t* __restrict__ perm,
+    const uint32_t* __restrict__ cellStart, const uint32_t* __restrict__ cellEnd, const GridInfo* __restrict__ info,
+    dbl4 pos, double radius, uint32_t* outIdx, double* outD2, unsigned long long* count, unsigned long long capacity) {
+    const GridInfo gi = *info;
+    int c0[3], c1[3];
+    const double p[3] = { pos.x, pos.y, pos.z };
+    for (int d = 0; d < 3; ++d) {
+        const double a = floor((p[d] - radius - gi.lo[d]) * gi.inv_cell);
+        const double b = floor((p[d] + radius - gi.lo[d]) * gi.inv_cell);
+        c0[d] = int(fmax(0., fmin(a, double(gi.dims[d] - 1))));
+        c1[d] = int(fmax(0., fmin(b, double(gi.dims[d] - 1))));
+    }
+    const uint32_t nx = uint32_t(c1[0] - c0[0] + 1), ny = uint32_t(c1[1] - c0[1] + 1), nz = uint32_t(c1[2] - c0[2] + 1);
+    const unsigned long long total = (unsigned long long)nx * ny * nz;
+    const double r2 = radius * radius;
+    for (unsigned long long t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        const uint32_t x = c0[0] + uint32_t(t % nx), y = c0[1] + uint32_t((t / nx) % ny),
+                       z = c0[2] + uint32_t(t / (unsigned long long)(nx * ny));
+        const uint32_t c = (z * uint32_t(gi.dims[1]) + y) * uint32_t(gi.dims[0]) + x;
+        for (uint32_t k = cellStart[c]; k < cellEnd[c]; ++k) {
+            const dbl4 q = rs[k];
+            const double dx = q.x - pos.x, dy = q.y - pos.y, dz = q.z - pos.z;
+            const double d2 = dx * dx + dy * dy + dz * dz;
+            if (d2 < r2) {
+                const unsigned long long slot = atomicAdd(count, 1ull);
+                if (slot < capacity) {
+                    outIdx[slot] = perm[k];
+                    outD2[slot] = d2;
+                }
+            }
+        }
+    }
+}
+
+void launchFindBall(const Grid& g, uint32_t n, const dbl4& pos, double radius, uint32_t* idx, double* d2,
+    unsigned long long* count, unsigned long long capacity, cudaStream_t st) {
+    cudaMemsetAsync(count, 0, sizeof(unsigned long long), st);
+    if (n == 0) {
+        return;
+    }
+    findBallKernel<<<152, 128, 0, st>>>(g.rs, g.perm, g.cell_start, g.cell_end, g.info, pos, radius, idx, d2, count,
+        capacity);
+}
+
+void launchRadiusPairs(const DState& s, const Grid& g, uint32_t* pi, uint32_t* pj, unsigned long long* count,
+    unsigned long long capacity, cudaStream_t st) {
+    cudaMemsetAsync(count, 0, sizeof(unsigned long long), st);
+    if (s.n == 0) {
+        return;
+    }
+    if (pi) {
+        pairsKernel<true, true><<<ceilDiv(s.n, 128), 128, 0, st>>>(s.n, g.rs, g.perm, g.keys_sorted, g.cell_start,
+            g.cell_end, g.info, pi, pj, count, capacity);
+    } else {
+        pairsKernel<false, true><<<ceilDiv(s.n, 128), 128, 0, st>>>(s.n, g.rs, g.perm, g.keys_sorted, g.cell_start,
+            g.cell_end, g.info, nullptr, nullptr, count, 0);
+    }
 }
 
 void launchCountPairs(const DState& s, const Grid& g, unsigned long long* count, cudaStream_t st) {

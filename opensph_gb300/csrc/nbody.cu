@@ -1116,10 +1116,10 @@ __global__ void scatterValidKernel(uint32_t n, const uint32_t* __restrict__ vali
 
 } // namespace
 
-cudaError_t collideAllocate(Collide& c, uint32_t n, uint32_t cellCapacity) {
+cudaError_t collideAllocate(Collide& c, uint32_t n, uint32_t cellCapacity, uint32_t records) {
     const size_t nn = n > 0 ? n : 1;
     c.capacity = uint32_t(nn);
-    c.pool_capacity = uint32_t(nn + std::max<size_t>(nn, size_t(1) << 16));
+    c.pool_capacity = uint32_t(nn + (records > 0 ? size_t(records) : std::max<size_t>(nn, size_t(1) << 16)));
     c.extra_capacity = uint32_t(std::max<size_t>(2 * nn, size_t(1) << 16));
     cudaError_t e = cudaSuccess;
     auto A = [&](auto** p, size_t count) {
@@ -1273,10 +1273,12 @@ int nbodyCollide(DState& s, Grid& g, Collide& c, const CollideParams& p, const d
         return SPHGPU_ERR_CUDA;
     }
     const unsigned long long* cnt = c.counters_host;
-    if (cnt[CNT_ERROR]) {
+    // When a work list ran out, the loop stopped after the collisions it had processed: those stay applied and
+    // are counted, and the particles they merged away are removed below, so the state stays consistent (mass and
+    // momentum conserved); the collisions left in the interval are not processed.
+    const bool overflow = cnt[CNT_ERROR] != 0;
+    if (overflow) {
         *capacityError = uint32_t(cnt[CNT_ERROR]);
-        std::swap(c.removed, c.prev_removed);
-        return SPHGPU_ERR_CAPACITY;
     }
     for (int k = 0; k < 4; ++k) {
         c.totals[k] += cnt[k];
@@ -1304,7 +1306,7 @@ int nbodyCollide(DState& s, Grid& g, Collide& c, const CollideParams& p, const d
         s.n = n - removed;
     }
     std::swap(c.removed, c.prev_removed);
-    return SPHGPU_OK;
+    return overflow ? SPHGPU_ERR_CAPACITY : SPHGPU_OK;
 }
 
 void launchIota(uint32_t* a, uint32_t n, cudaStream_t st) {

@@ -12,10 +12,10 @@
 // the caller. Each call writes every row it later reads, so nothing carries over from the previous call.
 //
 // Set-up: host code cannot use the array's name as a device address (on the host it names a stand-in
-// object). The first call on each device, with that device current, looks the address up with
-// cudaGetSymbolAddress and caches it; make that first call before any stream capture begins.
-
-#include <mutex>
+// object). Every call looks the address up with cudaGetSymbolAddress for the current device and context: a
+// host-side query that queues no work, so the address is never stale (a cudaDeviceReset or another context
+// loads the library image at a different address). The first call on a device may load the library's
+// device code; make it before any stream capture begins.
 
 #include "state.h"
 
@@ -25,7 +25,6 @@ namespace {
 constexpr uint32_t kTotalsChunk = 4096;     // particles per block
 constexpr uint32_t kTotalsMaxBlocks = 1024; // rows of the scratch array
 constexpr uint32_t kTotalsThreads = 256;
-constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) double gTotalsScratch[kTotalsMaxBlocks * 9];
 
@@ -89,9 +88,6 @@ __global__ void totalsFinalKernel(const double* __restrict__ scratch, uint32_t r
     }
 }
 
-std::mutex gSetupMutex;
-double* gScratchAddress[kMaxDevices] = { nullptr };
-
 } // namespace
 } // namespace sphgpu
 
@@ -105,22 +101,11 @@ extern "C" sphgpu_status sphgpu_totals_noalloc(const double* r, const double* v,
         // the scratch array holds one row per kTotalsChunk particles: larger sets need sphgpu_totals
         return SPHGPU_ERR_CAPACITY;
     }
-    int device = 0;
-    if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= kMaxDevices) {
+    void* address = nullptr;
+    if (cudaGetSymbolAddress(&address, gTotalsScratch) != cudaSuccess || !address) {
         return SPHGPU_ERR_CUDA;
     }
-    double* scratch = nullptr;
-    {
-        std::lock_guard<std::mutex> lock(gSetupMutex);
-        if (!gScratchAddress[device]) {
-            void* address = nullptr;
-            if (cudaGetSymbolAddress(&address, gTotalsScratch) != cudaSuccess || !address) {
-                return SPHGPU_ERR_CUDA;
-            }
-            gScratchAddress[device] = static_cast<double*>(address);
-        }
-        scratch = gScratchAddress[device];
-    }
+    double* scratch = static_cast<double*>(address);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const uint32_t rows = uint32_t((n + kTotalsChunk - 1) / kTotalsChunk);
     if (rows > 0) {

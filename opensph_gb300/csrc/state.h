@@ -310,6 +310,12 @@ void launchGatherSorted(const DState& s, Grid& g, const Physics& ph, cudaStream_
 cudaError_t gridAllocate(Grid& g, uint32_t n, bool solid, bool correction = false, bool copies = true);
 void gridFree(Grid& g);
 void launchCountPairs(const DState& s, const Grid& g, unsigned long long* count, cudaStream_t st);
+// the directed pairs (i, j), j != i, |r_j - r_i| < 2 h_i (pi NULL: count only)
+void launchRadiusPairs(const DState& s, const Grid& g, uint32_t* pi, uint32_t* pj, unsigned long long* count,
+    unsigned long long capacity, cudaStream_t st);
+// particles within radius of pos on the grid of the last build (unordered; count may exceed capacity)
+void launchFindBall(const Grid& g, uint32_t n, const dbl4& pos, double radius, uint32_t* idx, double* d2,
+    unsigned long long* count, unsigned long long capacity, cudaStream_t st);
 void launchListPairs(const DState& s, const Grid& g, uint32_t* pi, uint32_t* pj, unsigned long long* count,
     unsigned long long capacity, cudaStream_t st);
 
@@ -346,6 +352,8 @@ void launchCorrectionMixed(const DState& s, const Grid& g, const Physics& ph, co
 // ---- launchers (gravity.cu) ----
 cudaError_t treeAllocate(Tree& t, uint32_t n, uint32_t leaf_size);
 void treeFree(Tree& t);
+// reallocates the per-warp check lists of the walks with `capacity` entries per list (no-op when not larger)
+cudaError_t treeGrowWalkScratch(Tree& t, uint32_t capacity);
 cudaError_t treeBuild(const DState& s, Tree& t, const Physics& ph, uint32_t* dev_error, cudaStream_t st);
 // (treebuild.cu) the build's own buffers, and the chunk capacity of the multi-CTA phase for n particles
 cudaError_t treeBuildAllocate(Tree& t, uint32_t n);
@@ -360,11 +368,20 @@ void launchGravityWalk(const DState& s, Tree& t, const Physics& ph, const double
     cudaStream_t st);
 void launchGravityWalkMixed(const DState& s, Tree& t, const Physics& ph, const float* lut_grad_f,
     uint32_t* dev_error, cudaStream_t st);
+// BarnesHut::evalAttractors on the device: att (5 doubles per attractor), dv (particles, in/out), acc (3 doubles per
+// attractor, in/out), partial (gravityAttractorPartials(n, count) doubles of scratch)
+void launchGravityAttractors(const DState& s, const Physics& ph, const double* lut, const double* att, uint32_t count,
+    dbl4* dv, double* partial, double* acc, cudaStream_t st);
+uint32_t gravityAttractorPartials(uint32_t n, uint32_t count);
+// BruteForceGravity for the listed particles (device arrays), FP64
+void launchGravityDirect(const DState& s, const Physics& ph, const double* lut, const uint32_t* targets, uint32_t nt,
+    dbl4* acc, cudaStream_t st);
 void launchGravityPoints(const DState& s, const Tree& t, const Physics& ph, const double* lut_grad,
     const dbl4* points, dbl4* acc, uint32_t npoints, cudaStream_t st);
 
 // ---- HardSphereSolver (nbody.cu) ----
-cudaError_t collideAllocate(Collide& c, uint32_t n, uint32_t cell_capacity);
+// records: collision records beyond one per particle (0 = max(n, 65,536))
+cudaError_t collideAllocate(Collide& c, uint32_t n, uint32_t cell_capacity, uint32_t records);
 void collideFree(Collide& c);
 // HardSphereSolver::collide over [0, factor * (*dt)); compacts the state when particles merged (s.n shrinks).
 // Synchronises the stream. Returns SPHGPU_OK or an error status (capacity bits in *capacity_error).

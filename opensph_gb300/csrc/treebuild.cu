@@ -22,8 +22,9 @@
 //      R1_CHUNK elements per CTA: statistics of the three candidate dimensions -> per segment the split
 //      dimension and the chunk offsets -> ranks of the elements above / below the split -> K, sliding
 //      midpoint, nth_element and the children -> the K swaps. The host launches as many levels as the
-//      previous build used plus two; the kernels read the segment and chunk counts from device memory, so
-//      levels without work end at once.
+//      previous build used plus two (then, only if large segments remain, four more at a time after reading
+//      their count); the kernels read the segment and chunk counts from device memory, so levels without work
+//      end at once.
 //   2. every other segment (the children of at most SUBTREE_MAX elements, and whatever phase 1 left over) is
 //      split down to its leaves by one warp, depth first, on a copy of its idx and keys in shared memory.
 // A counting sort by level then lists the nodes level by level for the mixed walk; the moments are formed
@@ -1318,7 +1319,7 @@ cudaError_t treeBuild(const DState& s, Tree& t, const Physics& ph, uint32_t* dev
     if (n <= SUBTREE_MAX) {
         levels = 0;
     }
-    for (uint32_t level = 0; level < levels; ++level) {
+    auto launchLevel = [&](uint32_t level) {
         const int p = int(level & 1u);
         const LevelBufs b = levelBufs(t, p), next = levelBufs(t, 1 - p);
         statsDecideKernel<<<gridC, R1_THREADS, 0, st>>>(t.elems, b, t.counters, p, cc, t.work);
@@ -1327,6 +1328,21 @@ cudaError_t treeBuild(const DState& s, Tree& t, const Physics& ph, uint32_t* dev
         chunkSwapKernel<<<gridSwap, SWAP_THREADS, 0, st>>>(t.elems, t.scratch_b, t.scratch_s, b, t.counters, p, cc,
             t.work);
         launched(3);
+    };
+    for (uint32_t level = 0; level < levels; ++level) {
+        launchLevel(level);
+    }
+    // a deeper tree than the last one (a first build, a more concentrated distribution): more levels while large
+    // segments remain (one host read per batch; the one-warp splits of the queue would take them otherwise)
+    for (int batch = 0; levels > 0 && batch < 64; ++batch) {
+        cudaMemcpyAsync(t.info_host, t.counters + C_SEGS + (levels & 1u), sizeof(uint32_t), cudaMemcpyDeviceToHost,
+            st);
+        if (cudaStreamSynchronize(st) != cudaSuccess || t.info_host[0] == 0) {
+            break;
+        }
+        for (uint32_t k = 0; k < 4; ++k) {
+            launchLevel(levels++);
+        }
     }
     const uint32_t gridSeg = std::max(1, std::min(ceilDiv(n / SUBTREE_MAX + 1, 256), 152 * 8));
     flushKernel<<<gridSeg, 256, 0, st>>>(levelBufs(t, int(levels & 1u)), t.counters, int(levels & 1u), t.queue,

@@ -26,6 +26,15 @@ class SphGpuError(RuntimeError):
         self.code = code
 
 
+def measure_fp32_peak(ms_target=200.0):
+    """The device's FP32 FMA rate in TFLOP/s (an FMA-chain kernel on every SM timed with CUDA events)."""
+    out = np.zeros(1)
+    rc = library().sphgpu_measure_fp32_peak(float(ms_target), out.ctypes.data_as(_F8P))
+    if rc != abi.OK:
+        raise SphGpuError(rc, "sphgpu_measure_fp32_peak failed")
+    return float(out[0])
+
+
 def library():
     """Loads libsphgpu.so (built in-tree by opensph_gb300.build); raises if it is missing."""
     global _LIB
@@ -50,6 +59,12 @@ def library():
     lib.sphgpu_gravity_build.argtypes = [h]
     lib.sphgpu_gravity_eval.argtypes = [h, _F8P, ctypes.c_uint64]
     lib.sphgpu_gravity_eval_points.argtypes = [h, _F8P, ctypes.c_uint64, _F8P]
+    lib.sphgpu_gravity_direct.argtypes = [h, _U4P, ctypes.c_uint64, _F8P]
+    lib.sphgpu_get_radius_pairs.argtypes = [h, _U4P, _U4P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]
+    lib.sphgpu_find_neighbors.argtypes = [h, _F8P, ctypes.c_double, _U4P, _F8P, ctypes.c_uint64,
+                                          ctypes.POINTER(ctypes.c_uint64)]
+    lib.sphgpu_gravity_attractors.argtypes = [h, _F8P, ctypes.c_uint64, _F8P, _F8P, ctypes.c_uint64]
+    lib.sphgpu_measure_fp32_peak.argtypes = [ctypes.c_double, _F8P]
     lib.sphgpu_gravity_stats.argtypes = [h, ctypes.POINTER(ctypes.c_uint64)]
     lib.sphgpu_gravity_interactions.argtypes = [h, ctypes.POINTER(ctypes.c_uint64)]
     lib.sphgpu_integrate.argtypes = [h]
@@ -271,6 +286,56 @@ class GpuSolver:
         self._check(self._lib.sphgpu_gravity_eval_points(self._h, pts.ctypes.data_as(_F8P), pts.size // 4,
                                                          acc.ctypes.data_as(_F8P)))
         return acc
+
+    def radius_pairs(self):
+        """The directed pairs (i, j), j != i, |r_j - r_i| < 2 h_i of every particle, sorted by i then j."""
+        cnt = ctypes.c_uint64(0)
+        rc = self._lib.sphgpu_get_radius_pairs(self._h, None, None, 0, ctypes.byref(cnt))
+        if rc not in (abi.OK, abi.ERR_CAPACITY):
+            self._check(rc)
+        pi = np.zeros(cnt.value, dtype="u4")
+        pj = np.zeros(cnt.value, dtype="u4")
+        if cnt.value:
+            self._check(self._lib.sphgpu_get_radius_pairs(self._h, pi.ctypes.data_as(_U4P), pj.ctypes.data_as(_U4P),
+                                                          cnt.value, ctypes.byref(cnt)))
+        return pi, pj
+
+    def find_neighbors(self, pos, radius):
+        """Particles within radius of pos (ascending index) and their squared distances, on the grid of the last
+        neighbour build."""
+        p = np.ascontiguousarray(pos[:3], dtype="f8")
+        cap = 1024
+        while True:
+            idx = np.zeros(cap, dtype="u4")
+            d2 = np.zeros(cap)
+            cnt = ctypes.c_uint64(0)
+            rc = self._lib.sphgpu_find_neighbors(self._h, p.ctypes.data_as(_F8P), float(radius),
+                                                 idx.ctypes.data_as(_U4P), d2.ctypes.data_as(_F8P), cap,
+                                                 ctypes.byref(cnt))
+            if rc == abi.ERR_CAPACITY:
+                cap = int(cnt.value)
+                continue
+            self._check(rc)
+            return idx[:cnt.value], d2[:cnt.value]
+
+    def gravity_direct(self, targets):
+        """BruteForceGravity's FP64 direct sum for the particles listed in targets (4 doubles per target)."""
+        t = np.ascontiguousarray(targets, dtype="u4")
+        acc = np.zeros(4 * t.size)
+        self._check(self._lib.sphgpu_gravity_direct(self._h, t.ctypes.data_as(_U4P), t.size,
+                                                    acc.ctypes.data_as(_F8P)))
+        return acc
+
+    def gravity_attractors(self, attractors, dv, attractor_acc):
+        """IGravity::evalAttractors: attractors (count x 5: x, y, z, radius, mass); dv (4 per particle) and
+        attractor_acc (3 per attractor) are updated in place and returned."""
+        att = np.ascontiguousarray(attractors, dtype="f8").ravel()
+        dv = np.ascontiguousarray(dv, dtype="f8")
+        acc = np.ascontiguousarray(attractor_acc, dtype="f8")
+        self._check(self._lib.sphgpu_gravity_attractors(self._h, att.ctypes.data_as(_F8P), att.size // 5,
+                                                        acc.ctypes.data_as(_F8P), dv.ctypes.data_as(_F8P),
+                                                        dv.size // 4))
+        return dv, acc
 
     def gravity_stats(self):
         out = (ctypes.c_uint64 * 3)()

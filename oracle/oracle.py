@@ -194,6 +194,22 @@ def gravity_direct(r, m, G=1.0, kernel_radius=2, targets=None):
     return acc
 
 
+def gravity_attractors(r, m, attractors, dv, acc, G=1.0, kernel_radius=2):
+    """BarnesHut::evalAttractors: attractors (count x 5: x, y, z, radius, mass); dv (4 per particle) and acc
+    (3 per attractor) are updated in place and returned."""
+    r = np.ascontiguousarray(r, dtype="f8")
+    m = np.ascontiguousarray(m, dtype="f8")
+    att = np.ascontiguousarray(attractors, dtype="f8").ravel()
+    dv = np.ascontiguousarray(dv, dtype="f8")
+    acc = np.ascontiguousarray(acc, dtype="f8")
+    rc = _lib().ora_gravity_attractors(ctypes.c_uint64(m.size), r.ctypes.data_as(_F8), m.ctypes.data_as(_F8),
+                                       ctypes.c_double(G), ctypes.c_int(kernel_radius), ctypes.c_uint64(att.size // 5),
+                                       att.ctypes.data_as(_F8), dv.ctypes.data_as(_F8), acc.ctypes.data_as(_F8))
+    if rc:
+        raise RuntimeError(f"ora_gravity_attractors failed: {rc}")
+    return dv, acc
+
+
 def kernel_values(qsqr):
     lib = _lib()
     return (np.array([lib.ora_sph_kernel_value(float(q)) for q in qsqr]),

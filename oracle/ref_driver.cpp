@@ -16,6 +16,7 @@
 #include "gravity/Moments.h"
 #include "gravity/NBodySolver.h"
 #include "physics/Integrals.h"
+#include "quantities/Attractor.h"
 #include "objects/finders/KdTree.h"
 #include "sph/kernel/GravityKernel.h"
 
@@ -573,6 +574,104 @@ int modeGravity(Writer& w, int n, double theta, uint64_t seed, double soft) {
     return 0;
 }
 
+// BarnesHut::evalAttractors (core/gravity/BarnesHut.cpp:100-125) on a Plummer sphere with two attractors (one
+// inside the particle cloud, one outside): the particles' accelerations (self-gravity, then the attractor terms
+// added) and the attractors' accelerations
+int modeAttractors(Writer& w, int n, uint64_t seed, double soft) {
+    SplitMix rng{ seed };
+    Array<Vector> r(n);
+    Array<Float> m(n);
+    for (int i = 0; i < n; ++i) {
+        double rad;
+        do {
+            const double x = rng.uniform();
+            rad = 1.0 / std::sqrt(std::pow(x, -2.0 / 3.0) - 1.0);
+        } while (rad > 10.0);
+        const double ct = 2.0 * rng.uniform() - 1.0;
+        const double ph = 2.0 * 3.14159265358979323846 * rng.uniform();
+        const double st = std::sqrt(1.0 - ct * ct);
+        r[i] = Vector(rad * st * std::cos(ph), rad * st * std::sin(ph), rad * ct, soft);
+        m[i] = 1.0 / n;
+    }
+    Storage storage;
+    storage.insert<Vector>(QuantityId::POSITION, OrderEnum::SECOND, r.clone());
+    storage.insert<Float>(QuantityId::MASS, OrderEnum::ZERO, m.clone());
+    w.f64("r", vec4(r));
+    w.f64("m", flt(m));
+    const double G = 0.7;
+    BarnesHut bh(0.5, MultipoleOrder::OCTUPOLE, GravityKernel<CubicSpline<3>>{}, 25, 50, G);
+    bh.build(SEQUENTIAL, storage);
+    Array<Vector> dv(n);
+    dv.fill(Vector(0._f));
+    Statistics stats;
+    bh.evalSelfGravity(SEQUENTIAL, dv, stats);
+    w.f64("a_self", vec4(dv));
+    Array<Attractor> attractors;
+    attractors.push(Attractor(Vector(0.1, -0.2, 0.05), Vector(0._f), 0.3, 0.25));
+    attractors.push(Attractor(Vector(4.0, 3.0, -2.0), Vector(0._f), 0.5, 2.0));
+    std::vector<double> att;
+    for (const Attractor& a : attractors) {
+        att.insert(att.end(), { a.position[X], a.position[Y], a.position[Z], a.radius, a.mass });
+    }
+    bh.evalAttractors(SEQUENTIAL, attractors, dv);
+    std::vector<double> aacc;
+    for (const Attractor& a : attractors) {
+        aacc.insert(aacc.end(), { a.acceleration[X], a.acceleration[Y], a.acceleration[Z] });
+    }
+    w.scalar("G", G);
+    w.f64("attractors", att);
+    w.f64("a_total", vec4(dv));
+    w.f64("attractor_acc", aacc);
+    return 0;
+}
+
+// BruteForceGravity (core/gravity/BruteForceGravity.h:38-58, 110-129) on n seeded points whose coordinates use only
+// exactly rounded arithmetic, so that any machine regenerates them bit for bit: per coordinate x = s (2u - 1) with
+// s = u'^2 (u, u' uniform from the splitmix64 sequence, one u' per point), h = soft, m = 1 / n, G = 1; writes the
+// accelerations of nSample seeded particles and checksums of the points.
+int modeDirect(Writer& w, int n, uint64_t seed, double soft, int nSample) {
+    SplitMix rng{ seed };
+    Array<Vector> r(n);
+    Array<Float> m(n);
+    double sx = 0., sy = 0., sz = 0.;
+    for (int i = 0; i < n; ++i) {
+        const double u = rng.uniform();
+        const double s = u * u;
+        const double x = s * (2. * rng.uniform() - 1.);
+        const double y = s * (2. * rng.uniform() - 1.);
+        const double z = s * (2. * rng.uniform() - 1.);
+        r[i] = Vector(x, y, z, soft);
+        m[i] = 1. / n;
+        sx += x;
+        sy += y;
+        sz += z;
+    }
+    Storage storage;
+    storage.insert<Vector>(QuantityId::POSITION, OrderEnum::SECOND, r.clone());
+    storage.insert<Float>(QuantityId::MASS, OrderEnum::ZERO, m.clone());
+    BruteForceGravity bf(GravityKernel<CubicSpline<3>>{}, 1._f);
+    bf.build(SEQUENTIAL, storage);
+    Array<Vector> dv(n);
+    dv.fill(Vector(0._f));
+    Statistics stats;
+    bf.evalSelfGravity(SEQUENTIAL, dv, stats);
+    SplitMix pick{ seed + 1 };
+    std::vector<uint32_t> idx;
+    std::vector<double> acc;
+    for (int k = 0; k < nSample; ++k) {
+        const uint32_t i = uint32_t(pick.next() % uint64_t(n));
+        idx.push_back(i);
+        for (int c = 0; c < 4; ++c) {
+            acc.push_back(dv[i][c]);
+        }
+    }
+    w.f64("params", { double(n), double(seed), soft });
+    w.f64("checksum", { sx, sy, sz });
+    w.u32("sample_idx", idx);
+    w.f64("a_direct", acc);
+    return 0;
+}
+
 // symmetric-finder pair set (KdTree.findLowerRank + the SymmetricSolver radius filter) on a solver state
 int modePairs(Writer& w, int n, uint64_t seed) {
     SplitMix rng{ seed };
@@ -825,6 +924,10 @@ int main(int argc, char** argv) {
             return modeGas(w, int(arg(3, 2000)), int(arg(4, 100)), int(arg(5, 5)));
         } else if (mode == "gravity") {
             return modeGravity(w, int(arg(3, 2000)), arg(4, 0.5), uint64_t(arg(5, 7)), arg(6, 1.e-3));
+        } else if (mode == "attractors") {
+            return modeAttractors(w, int(arg(3, 2000)), uint64_t(arg(4, 7)), arg(5, 1.e-2));
+        } else if (mode == "direct") {
+            return modeDirect(w, int(arg(3, 65536)), uint64_t(arg(4, 17)), arg(5, 1.e-3), int(arg(6, 1024)));
         } else if (mode == "pairs") {
             return modePairs(w, int(arg(3, 1000)), uint64_t(arg(4, 3)));
         } else if (mode == "eos") {

@@ -1696,6 +1696,63 @@ int ora_gravity_direct(uint64_t n, const double* r, const double* m, double G, i
     return SPHGPU_OK;
 }
 
+// BarnesHut::evalAttractors (core/gravity/BarnesHut.cpp:100-125): for each attractor a (in order) and particle i
+// (in index order), f = grad W(r_i - x_a, (h_i + R_a) / 2), dv_i -= (G M_a) f and acc_a += (G m_i) f; then for
+// each attractor pair i < j, f = G grad W(x_i - x_j, (R_i + R_j) / 2), acc_i -= M_j f and acc_j += M_i f.
+// att: 5 doubles per attractor (x, y, z, radius, mass); dv: 4 per particle and acc: 3 per attractor, in/out.
+// GravityLutKernel::grad keeping the fourth component of the separation (the reference scales the whole Vector,
+// so a difference of smoothing lengths or radii yields a non-zero h component)
+V4 gravGradV4(const V4& r, double h, int kernelRadius) {
+    const double hInv = 1. / h;
+    const V4 rh{ r.x * hInv, r.y * hInv, r.z * hInv, 0. };
+    const double qSqr = sqrLen(rh);
+    const double rad = double(kernelRadius < 0 ? -kernelRadius : kernelRadius);
+    if (qSqr + EPS >= rad * rad) {
+        const double len = std::sqrt(sqrLen(r));
+        const double l3 = len * len * len;
+        return V4{ r.x / l3, r.y / l3, r.z / l3, r.h / l3 };
+    }
+    const double g = (kernelRadius < 0 ? solidLut() : gravLut()).grad(qSqr);
+    const double h3 = hInv * hInv * hInv;
+    return V4{ (h3 * r.x) * g, (h3 * r.y) * g, (h3 * r.z) * g, (h3 * r.h) * g };
+}
+
+int ora_gravity_attractors(uint64_t n, const double* r, const double* m, double G, int kernel_radius,
+    uint64_t count, const double* att, double* dv, double* acc) {
+    if ((n && (!r || !m || !dv)) || (count && (!att || !acc))) {
+        return SPHGPU_ERR_ARGUMENT;
+    }
+    for (uint64_t a = 0; a < count; ++a) {
+        const V4 xa{ att[5 * a], att[5 * a + 1], att[5 * a + 2], att[5 * a + 3] };
+        const double gm = G * att[5 * a + 4];
+        for (uint64_t i = 0; i < n; ++i) {
+            const V4 ri = load4(r, i);
+            const V4 f = gravGradV4(sub(ri, xa), 0.5 * (ri.h + xa.h), kernel_radius);
+            dv[4 * i] -= gm * f.x;
+            dv[4 * i + 1] -= gm * f.y;
+            dv[4 * i + 2] -= gm * f.z;
+            dv[4 * i + 3] -= gm * f.h;
+            const double mi = G * m[i];
+            acc[3 * a] += mi * f.x;
+            acc[3 * a + 1] += mi * f.y;
+            acc[3 * a + 2] += mi * f.z;
+        }
+    }
+    for (uint64_t i = 0; i < count; ++i) {
+        for (uint64_t j = i + 1; j < count; ++j) {
+            const V4 xi{ att[5 * i], att[5 * i + 1], att[5 * i + 2], att[5 * i + 3] };
+            const V4 xj{ att[5 * j], att[5 * j + 1], att[5 * j + 2], att[5 * j + 3] };
+            const V4 g = gravGradV(sub(xi, xj), 0.5 * (xi.h + xj.h), kernel_radius);
+            const double f[3] = { G * g.x, G * g.y, G * g.z };
+            for (int c = 0; c < 3; ++c) {
+                acc[3 * i + c] -= att[5 * j + 4] * f[c];
+                acc[3 * j + c] += att[5 * i + 4] * f[c];
+            }
+        }
+    }
+    return SPHGPU_OK;
+}
+
 int ora_integrate(const sphgpu_config* cfg, ora_state* s) {
     if (!validConfig(cfg, s)) {
         return SPHGPU_ERR_ARGUMENT;

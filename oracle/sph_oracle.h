@@ -68,6 +68,10 @@ int ora_gravity_bh(uint64_t n, const double* r, const double* m, double G, doubl
 int ora_gravity_points(uint64_t n, const double* r, const double* m, double G, double theta, int order,
     uint32_t leaf_size, int kernel_radius, uint64_t npoints, const double* points, double* acc);
 /* BruteForceGravity::evalSelfGravity restricted to the targets listed in idx (all if idx is NULL). */
+/* BarnesHut::evalAttractors (core/gravity/BarnesHut.cpp:100-125): att 5 doubles per attractor (x, y, z, radius,
+ * mass); dv (4 per particle) and acc (3 per attractor) are updated in place. */
+int ora_gravity_attractors(uint64_t n, const double* r, const double* m, double G, int kernel_radius,
+    uint64_t count, const double* att, double* dv, double* acc);
 int ora_gravity_direct(uint64_t n, const double* r, const double* m, double G, int kernel_radius,
     uint64_t ntargets, const uint32_t* idx, double* acc);
 

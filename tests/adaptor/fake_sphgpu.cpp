@@ -177,6 +177,21 @@ sphgpu_status sphgpu_gravity_eval_points(sphgpu_handle*, const double*, uint64_t
     return SPHGPU_ERR_UNSUPPORTED;
 }
 
+sphgpu_status sphgpu_gravity_attractors(sphgpu_handle*, const double*, uint64_t, double*, double*, uint64_t) {
+    return SPHGPU_ERR_UNSUPPORTED;
+}
+
+sphgpu_status sphgpu_get_radius_pairs(sphgpu_handle*, uint32_t*, uint32_t*, uint64_t, uint64_t* npairs) {
+    *npairs = 0;
+    return SPHGPU_OK;
+}
+
+sphgpu_status sphgpu_find_neighbors(sphgpu_handle*, const double*, double, uint32_t*, double*, uint64_t,
+    uint64_t* count) {
+    *count = 0;
+    return SPHGPU_OK;
+}
+
 } // extern "C"
 
 extern "C" {

@@ -119,3 +119,28 @@ def scale_err(a, b):
 
 def vec3(a):
     return np.asarray(a).reshape(-1, 4)[:, :3]
+
+
+def splitmix_uniform(seed, count):
+    """The first `count` uniforms (0, 1) of the splitmix64 sequence of oracle/ref_driver.cpp (SplitMix::uniform):
+    integer arithmetic and exactly rounded scaling, identical on every machine."""
+    with np.errstate(over="ignore"):
+        k = np.arange(1, count + 1, dtype=np.uint64)
+        z = np.uint64(seed) + k * np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return ((z >> np.uint64(11)).astype(np.float64) + 0.5) * (1.0 / 9007199254740992.0)
+
+
+def direct_points(fx):
+    """The points of a BruteForceGravity fixture (ref_driver's modeDirect): r (n x 4) and m, regenerated exactly."""
+    n, seed, soft = int(fx["params"][0]), int(fx["params"][1]), float(fx["params"][2])
+    u = splitmix_uniform(seed, 4 * n).reshape(n, 4)
+    s = u[:, 0] * u[:, 0]
+    r = np.empty((n, 4))
+    for c in range(3):
+        r[:, c] = s * (2.0 * u[:, c + 1] - 1.0)
+    r[:, 3] = soft
+    m = np.full(n, 1.0 / n)
+    return r, m

@@ -1,10 +1,11 @@
 """Regenerates the golden fixtures of tests/golden/ from the REFERENCE implementation.
 
 Builds oracle/_ref/refdriver from the reference's own core/*.cpp sources (oracle/Makefile, target `ref`;
-needs the reference tree, by default /root/reference) and runs it in each mode below. Every fixture stores
+needs the reference tree: oracle/Makefile's REF, or the OPENSPH_REFERENCE environment variable, or --ref) and
+runs it in each mode below. Every fixture stores
 the reference's inputs and outputs, so the tests never need the reference itself.
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py [--ref REFERENCE_TREE]
 """
 import argparse
 import os
@@ -43,6 +44,10 @@ FIXTURES = {
     # gravity only: Plummer sphere, BH theta 0.5 octupole vs brute force
     "gravity_n3000": ["gravity", "3000", "0.5", "7", "1e-3"],
     "gravity_n3000_t07": ["gravity", "3000", "0.7", "11", "1e-2"],
+    # Barnes-Hut with two attractors (BarnesHut::evalAttractors): particle and attractor accelerations
+    "attractors_n2000": ["attractors", "2000", "7", "1e-2"],
+    # BruteForceGravity at N = 65,536 on portably generated points (accelerations of 1,024 seeded particles)
+    "direct_n65536": ["direct", "65536", "17", "1e-3", "1024"],
     # symmetric finder pair set (KdTree findLowerRank + SymmetricSolver filter), variable h
     "pairs_n1500": ["pairs", "1500", "3"],
     # Tillotson EOS values on a (rho, u) grid
@@ -67,11 +72,12 @@ FIXTURES = {
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=None, help="reference tree (default: oracle/Makefile's REF)")
     ap.add_argument("--only", nargs="*")
     args = ap.parse_args()
-    subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref", f"REF={args.ref}",
-                    f"-j{os.cpu_count() or 4}"], check=True)
+    ref = [f"REF={args.ref}"] if args.ref else []
+    subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref"] + ref + [f"-j{os.cpu_count() or 4}"],
+                   check=True)
     driver = os.path.join(REPO, "oracle", "_ref", "refdriver")
     for name, argv in FIXTURES.items():
         if args.only and name not in args.only:

@@ -9,7 +9,9 @@ import pytest
 from opensph_gb300 import abi
 
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference"
+# the reference tree: oracle/Makefile's REF (OPENSPH_REFERENCE when set)
+REF = subprocess.run(["make", "-s", "--no-print-directory", "-C", os.path.join(REPO, "oracle"), "print-ref"],
+                     capture_output=True, text=True).stdout.strip()
 LIBCORE = os.path.join(REPO, "oracle", "_ref", "libcore.a")
 
 

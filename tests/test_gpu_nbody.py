@@ -231,3 +231,30 @@ def test_gpu_no_handler_ignores_collisions_and_sph_calls_are_refused():
         with pytest.raises(SphGpuError) as e:
             g.pairs()
         assert e.value.code == abi.ERR_UNSUPPORTED
+
+
+def test_gpu_collision_work_space_overflow_keeps_a_consistent_state():
+    # a collide call whose loop runs out of collision records returns SPHGPU_ERR_CAPACITY with the collisions it
+    # processed applied and the particles they merged away removed: mass and momentum are conserved and the
+    # particle count drops by the mergers counted
+    st = nc.cloud()
+    n0 = len(st["m"])
+    cfg, keep = nc.kat_config(n0, abi.COLLISION_PERFECT_MERGING, abi.OVERLAP_FORCE_MERGE, bounce_merge_limit=0.0,
+                              rotation_merge_limit=0.0, collision_records=4)
+    m0 = float(np.sum(st["m"]))
+    v0 = st["v"].reshape(-1, 4)[:, :3]
+    p0 = np.sum(st["m"][:, None] * v0, 0)
+    pscale = float(np.sum(st["m"] * np.linalg.norm(v0, axis=1)))
+    with GpuSolver(cfg, keep) as g:
+        g.set_state(nc.cloud())
+        with pytest.raises(SphGpuError) as e:
+            g.collide(0.3)  # every sphere meets the others at the centre at t = 0.25
+        assert e.value.code == abi.ERR_CAPACITY
+        g._refresh_count()
+        stats = g.collision_stats()
+        got = g.get_state(nc.FIELDS)
+        n = g.n
+    assert stats[1] > 0 and n == n0 - stats[1]
+    assert abs(float(np.sum(got["m"])) - m0) <= 1e-12 * m0
+    p = np.sum(got["m"][:, None] * got["v"].reshape(-1, 4)[:, :3], 0)
+    assert np.max(np.abs(p - p0)) <= 1e-12 * pscale

@@ -390,3 +390,104 @@ def test_plummer_walks_against_direct_sum(theta):
         rel = np.linalg.norm(a[targets] - direct, axis=1) / np.linalg.norm(direct, axis=1)
         assert np.median(rel) < bound / 5
         assert np.percentile(rel, 99) < bound
+
+
+@pytest.mark.parametrize("name", ["gravity_n3000", "direct_n65536"])
+def test_gpu_direct_sum_matches_reference_bruteforce(name):
+    # sphgpu_gravity_direct against the reference's BruteForceGravity: the same FP64 terms summed in the same
+    # (index) order
+    fx = cases.load(name)
+    if name == "direct_n65536":
+        r, m = cases.direct_points(fx)
+        r = r.ravel()
+        targets = fx["sample_idx"]
+        ref = fx["a_direct"].reshape(-1, 4)[:, :3]
+    else:
+        r, m = fx["r"], fx["m"]
+        targets = np.arange(len(m), dtype="u4")
+        ref = fx["a_direct"].reshape(-1, 4)[:, :3]
+    with grav_solver(r, m, 0.5) as g:  # G = 1, as both fixtures
+        got = g.gravity_direct(targets).reshape(-1, 4)[:, :3]
+    assert cases.scale_err(got, ref) < 1e-14
+
+
+def test_gpu_attractors_match_reference():
+    # IGravity::evalAttractors (core/gravity/BarnesHut.cpp:100-125) on the device against the reference: the
+    # particles' accelerations (the reference's self-gravity plus the attractor terms, all four components) and
+    # the attractors' accelerations (sums over the particles in another order: 1e-13)
+    fx = cases.load("attractors_n2000")
+    n = len(fx["m"])
+    cfg, keep = abi.make_config(n, [abi.ideal_gas()], forces=abi.FORCE_PRESSURE | abi.FORCE_SELF_GRAVITY,
+                                gravity_constant=float(fx["G"][0]), gravity_opening_angle=0.5)
+    with GpuSolver(cfg, keep) as g:
+        g.set_quantity(abi.Q_POSITION, 0, fx["r"])
+        g.set_quantity(abi.Q_MASS, 0, fx["m"])
+        dv, acc = g.gravity_attractors(fx["attractors"].reshape(-1, 5), fx["a_self"].copy(), np.zeros(6))
+    np.testing.assert_allclose(dv, fx["a_total"], rtol=0, atol=1e-14 * np.max(np.abs(fx["a_total"])))
+    assert cases.scale_err(acc, fx["attractor_acc"]) < 1e-13
+
+
+def _ball_sets(r, centres, radii):
+    """Brute force in the device's FP64 expression: |r_j - c|^2 = (dx dx + dy dy) + dz dz < radius^2."""
+    out = []
+    for c, rad in zip(centres, radii):
+        d = r[:, :3] - c[:3]
+        d2 = (d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2]
+        sel = np.nonzero(d2 < rad * rad)[0]
+        out.append((sel, d2[sel]))
+    return out
+
+
+def test_radius_pairs_are_the_balls_of_two_h():
+    # findAll(i, 2 h_i) of every particle (variable h): the directed pairs of sphgpu_get_radius_pairs
+    fx = cases.load("pairs_n1500")
+    r = fx["r"].reshape(-1, 4)
+    with gas_solver(fx["r"]) as g:
+        pi, pj = g.radius_pairs()
+    want = _ball_sets(r, r, 2.0 * r[:, 3])
+    got_i, got_j = [], []
+    for i, (sel, _) in enumerate(want):
+        sel = sel[sel != i]
+        got_i.append(np.full(len(sel), i))
+        got_j.append(sel)
+    np.testing.assert_array_equal(pi, np.concatenate(got_i))
+    np.testing.assert_array_equal(pj, np.concatenate(got_j))
+
+
+def test_point_queries_on_the_device():
+    # findAll(pos, radius) at arbitrary points and radii (smaller and larger than the grid cells, outside the set)
+    fx = cases.load("pairs_n1500")
+    r = fx["r"].reshape(-1, 4)
+    rng = np.random.default_rng(3)
+    centres = np.concatenate([rng.random((6, 4)), r[:2], np.array([[3.0, 3.0, 3.0, 0.0]])])
+    radii = [0.01, 0.05, 0.2, 0.5, 1.0, 2.0, 0.1, 0.3, 4.0]
+    with gas_solver(fx["r"]) as g:
+        g.pairs()  # the grid of the current positions
+        for c, rad, (sel, d2) in zip(centres, radii, _ball_sets(r, centres, radii)):
+            idx, dd = g.find_neighbors(c, rad)
+            np.testing.assert_array_equal(idx, sel)
+            np.testing.assert_array_equal(dd, d2)
+        # a query after the positions changed needs a new neighbour build
+        g.set_quantity(abi.Q_POSITION, 0, fx["r"])
+        with pytest.raises(SphGpuError) as e:
+            g.find_neighbors(centres[0], 0.1)
+        assert e.value.code == abi.ERR_STATE
+
+
+def test_on_demand_device_state_is_authoritative():
+    # the state stays on the device between outputs (GpuTimeStepping ON_DEMAND, GpuOutput): K steps with no
+    # download give bit for bit the state of K steps each followed by a full download
+    fx = cases.load("impact_n1200")
+    cfg, keep = cases.config_of(fx)
+    out = []
+    for download in (False, True):
+        with GpuSolver(cfg, keep) as g:
+            g.set_state(cases.state_of(fx, "s0_"))
+            g.timestep = float(fx["dts"][0])
+            for _ in range(4):
+                g.step(1)
+                if download:
+                    g.get_state()
+            out.append(g.get_state())
+    for f in out[0]:
+        np.testing.assert_array_equal(out[0][f], out[1][f])

@@ -139,3 +139,26 @@ def test_cached_gravity_differs_from_recomputed_gravity():
     st = cases.state_of(fx, "s0_")
     oracle.run(cfg, st, len(fx["dts"]) - 1, float(fx["dts"][0]))
     assert cases.scale_err(st["v"], fx["sN_v"]) > 100 * TOL_STEPS
+
+
+def test_direct_sum_matches_reference_bruteforce_at_65536():
+    # BruteForceGravity (core/gravity/BruteForceGravity.h:38-58, 110-129) at N = 65,536: the points regenerate bit
+    # for bit from the fixture's seed (sequential sums of the coordinates equal the reference driver's), and the
+    # oracle's FP64 direct sum equals the reference's accelerations exactly at 1,024 seeded particles
+    fx = cases.load("direct_n65536")
+    r, m = cases.direct_points(fx)
+    for c in range(3):
+        assert np.add.accumulate(r[:, c])[-1] == fx["checksum"][c]
+    got = oracle.gravity_direct(r.ravel(), m, G=1.0, targets=fx["sample_idx"]).reshape(-1, 4)
+    np.testing.assert_array_equal(got[:, :3], fx["a_direct"].reshape(-1, 4)[:, :3])
+
+
+def test_attractors_match_reference():
+    # BarnesHut::evalAttractors (core/gravity/BarnesHut.cpp:100-125) with two attractors: the particles'
+    # accelerations (all four components, as the reference scales the whole separation Vector) and the
+    # attractors' accelerations, bit for bit
+    fx = cases.load("attractors_n2000")
+    dv, acc = oracle.gravity_attractors(fx["r"], fx["m"], fx["attractors"].reshape(-1, 5), fx["a_self"].copy(),
+                                        np.zeros(6), G=float(fx["G"][0]))
+    np.testing.assert_array_equal(dv, fx["a_total"])
+    np.testing.assert_array_equal(acc, fx["attractor_acc"])

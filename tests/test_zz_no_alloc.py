@@ -2,9 +2,11 @@
 
 Callers that cannot call cudaMalloc (an application that owns the device memory budget, a per-step hook that
 must not allocate) pass their own device buffers; the entry point keeps its scratch in a fixed array inside
-the library. The test runs two calls in a row on the same output buffer (the shared scratch must not carry
-state between calls), on a state that fills several scratch rows, and checks the size limit. This file is
-collected last so that a failure here does not hide the other GPU tests.
+the library. The tests run two calls in a row on the same output buffer (the shared scratch must not carry
+state between calls) on states that fill one and several scratch rows, an empty set (zeros), the largest
+accepted set (every row; compared with numpy's pairwise sums, and with no change of the device's free memory
+across the call), and check the size limit. This file is collected last so that a failure here does not hide
+the other GPU tests.
 """
 import ctypes
 
@@ -71,6 +73,47 @@ def test_totals_noalloc_matches_totals_twice():
             assert rc == abi.OK
             got = out.cpu().numpy()
             assert np.all(np.abs(got - ref) <= 1e-13 * scale + 1e-300), (got, ref)
+
+
+def test_totals_noalloc_empty_input_gives_zeros():
+    torch = pytest.importorskip("torch")
+    f = _entry()
+    buf = torch.zeros(16, dtype=torch.float64, device="cuda")
+    out = torch.full((9,), float("nan"), dtype=torch.float64, device="cuda")
+    p = buf.data_ptr()
+    assert f(p, p, p, p, 0, out.data_ptr(), None) == abi.OK
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(out.cpu().numpy(), np.zeros(9))
+
+
+def test_totals_noalloc_at_its_limit_allocates_nothing():
+    # the largest accepted set fills every row of the scratch array; the call changes no device memory
+    # reservation (a first call may load device code, so the comparison brackets the second)
+    torch = pytest.importorskip("torch")
+    f = _entry()
+    n = MAX_PARTICLES
+    rng = np.random.default_rng(21)
+    st = {"r": rng.normal(size=4 * n), "v": rng.normal(size=4 * n), "m": rng.random(n) + 0.5, "u": rng.random(n)}
+    r = st["r"].reshape(-1, 4)[:, :3]
+    v = st["v"].reshape(-1, 4)[:, :3]
+    terms = np.concatenate([st["m"][:, None] * v, st["m"][:, None] * np.cross(r, v),
+                            (0.5 * st["m"] * np.sum(v * v, 1))[:, None], (st["m"] * st["u"])[:, None],
+                            st["m"][:, None]], 1)
+    # numpy's pairwise summation along contiguous rows (a reduction along axis 0 would add row after row)
+    ref = np.sum(np.ascontiguousarray(terms.T), axis=1)
+    scale = np.sum(np.abs(terms), 0)
+    dev = {k: torch.tensor(st[k], dtype=torch.float64, device="cuda") for k in ("r", "v", "m", "u")}
+    out = torch.empty(9, dtype=torch.float64, device="cuda")
+    args = (dev["r"].data_ptr(), dev["v"].data_ptr(), dev["m"].data_ptr(), dev["u"].data_ptr(), n, out.data_ptr(),
+            None)
+    assert f(*args) == abi.OK
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
+    assert f(*args) == abi.OK
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free_before
+    got = out.cpu().numpy()
+    assert np.all(np.abs(got - ref) <= 1e-13 * scale), (got, ref)
 
 
 def test_totals_noalloc_rejects_oversized_input():

@@ -4,11 +4,11 @@
 // 212-489) with the moments of core/gravity/Moments.h over the k-d tree of treebuild.cu. Moments are formed
 // bottom-up in one launch (momentsUpKernel).
 //
-// Walk: one warp per leaf replays the reference's dual walk along the leaf's root path: at each ancestor
-// the pending check-list entries are classified against that ancestor's box with the reference's
-// sphere-box test (core/objects/geometry/Sphere.h:70-116), so every leaf receives exactly the reference's
-// particle list and node list. Each lane owns one particle of the leaf (leaf size <= 32) and evaluates the
-// exact softened pair terms and octupole expansions as soon as the warp classifies them.
+// Walk: the interaction lists of every node come from the list phase shared with the mixed walk (gravity32.cu:
+// the reference's dual-walk classification, core/gravity/BarnesHut.cpp:212-312 with Sphere::intersectsBox,
+// core/objects/geometry/Sphere.h:70-116, done once per node level by level, FP32-guarded with FP64 decisions at
+// the margin), so every leaf receives exactly the reference's particle list and node list; evalLists64Kernel
+// evaluates them in FP64, a warp per leaf and a lane per particle.
 
 #include <algorithm>
 
@@ -18,7 +18,6 @@ namespace sphgpu {
 
 namespace {
 
-constexpr int MAX_PATH = 512;
 
 // BarnesHut::buildLeaf (core/gravity/BarnesHut.cpp:376-437), geometry part: mass, centre of mass and opening
 // radius of the leaf in FP64, summed in the leaf's particle order (the walk's decisions depend on these bits).
@@ -299,200 +298,6 @@ __global__ void momentsUpKernel(const dbl4* __restrict__ r, const double* __rest
     }
 }
 
-// ---------------------------------------------------------------------------------------------------------
-// walk: one warp per leaf
-// ---------------------------------------------------------------------------------------------------------
-
-constexpr int WALK_THREADS = 128;
-
-__global__ void __launch_bounds__(WALK_THREADS) walkKernel(const dbl4* __restrict__ r,
-    const double* __restrict__ m, double G, const uint32_t* __restrict__ idx, const BhNodeGeom* __restrict__ geom,
-    const BhNodeMoments* __restrict__ mom, const float* __restrict__ nodef, const uint32_t* __restrict__ leaves,
-    uint32_t nLeaves, const double* __restrict__ lut, int kernelRadius, int order, int32_t* scratch,
-    uint32_t listCap, dbl4* agrav, unsigned long long* stats, uint32_t* devError) {
-    __shared__ int32_t pathSh[WALK_THREADS / 32][MAX_PATH];
-    const int lane = threadIdx.x & 31;
-    const int wib = threadIdx.x >> 5;
-    const uint32_t warpGlobal = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nWarps = (gridDim.x * blockDim.x) >> 5;
-    int32_t* listA = scratch + size_t(warpGlobal) * 2 * listCap;
-    int32_t* listB = listA + listCap;
-    int32_t* path = pathSh[wib];
-    unsigned long long nApprox = 0, nExact = 0, nPn = 0, nPp = 0;
-    (void)nWarps;
-
-    // leaves are taken from a shared counter (stats[4]) so that warps that drew cheap leaves take more
-    for (;;) {
-        uint32_t li = 0;
-        if (lane == 0) {
-            li = uint32_t(atomicAdd(&stats[4], 1ull));
-        }
-        li = __shfl_sync(0xffffffffu, li, 0);
-        if (li >= nLeaves) {
-            break;
-        }
-        const int leaf = int(leaves[li]);
-        const BhNodeGeom lg = geom[leaf];
-        const uint32_t cnt = lg.to - lg.from;
-        // root path (path[0] = root ... path[depth] = leaf)
-        int depth = 0;
-        if (lane == 0) {
-            int d = 0, nd = leaf;
-            while (geom[nd].parent >= 0 && d < MAX_PATH - 1) {
-                nd = geom[nd].parent;
-                ++d;
-            }
-            depth = d;
-            nd = leaf;
-            for (int k = d; k >= 0; --k) {
-                path[k] = nd;
-                nd = geom[nd].parent;
-            }
-            if (d >= MAX_PATH - 1) {
-                atomicOr(devError, uint32_t(DEV_ERR_WALK_CAPACITY));
-            }
-        }
-        depth = __shfl_sync(0xffffffffu, depth, 0);
-        __syncwarp();
-        const bool active = uint32_t(lane) < cnt;
-        const float4* nf = reinterpret_cast<const float4*>(nodef);
-        float lh[3], ll[3];
-        {
-            const float4 a = nodeGroup(nf, leaf, NF_COM_HI), b = nodeGroup(nf, leaf, NF_COM_LO);
-            lh[0] = a.x, lh[1] = a.y, lh[2] = a.z;
-            ll[0] = b.x, ll[1] = b.y, ll[2] = b.z;
-        }
-        uint32_t pi = 0;
-        dbl4 ri = mkd4(0., 0., 0., 1.);
-        if (active) {
-            pi = idx[lg.from + lane];
-            ri = r[pi];
-        }
-        double ax = 0., ay = 0., az = 0.;
-        int32_t* cur = listA;
-        int32_t* nxt = listB;
-        uint32_t ncur = 0, nnxt = 0;
-        bool overflow = false;
-        for (int k = 1; k <= depth && !overflow; ++k) {
-            const int ev = path[k];
-            const int par = path[k - 1];
-            const BhNodeGeom& pg = geom[par];
-            const int sib = pg.left == ev ? pg.right : pg.left;
-            WalkFrame fr;
-            setFrame(fr, nf, ev, k == depth, lh, ll);
-            if (lane == 0) {
-                cur[ncur] = sib;
-            }
-            ncur += 1;
-            __syncwarp();
-            uint32_t pos = 0;
-            while (pos < ncur) {
-                const uint32_t batch = min(32u, ncur - pos);
-                const uint32_t e = pos + lane;
-                int node = -1, cls = CL_KEEP;
-                if (uint32_t(lane) < batch) {
-                    node = cur[e];
-                    cls = classifyEntry(node, geom, nf, fr, lh, ll);
-                }
-                const unsigned mKeep = __ballot_sync(0xffffffffu, uint32_t(lane) < batch && cls == CL_KEEP);
-                const unsigned mOpen = __ballot_sync(0xffffffffu, cls == CL_OPEN);
-                const unsigned mPart = __ballot_sync(0xffffffffu, cls == CL_PARTICLES);
-                const unsigned mNode = __ballot_sync(0xffffffffu, cls == CL_NODE);
-                const unsigned below = (1u << lane) - 1u;
-                const uint32_t nOpen = __popc(mOpen), nKeep = __popc(mKeep);
-                if (ncur + 2 * nOpen > listCap || nnxt + nKeep > listCap) {
-                    overflow = true;
-                    break;
-                }
-                if (cls == CL_KEEP && uint32_t(lane) < batch) {
-                    nxt[nnxt + __popc(mKeep & below)] = node;
-                }
-                if (cls == CL_OPEN) {
-                    const uint32_t slot = ncur + 2 * __popc(mOpen & below);
-                    cur[slot] = geom[node].left;
-                    cur[slot + 1] = geom[node].right;
-                }
-                pos += batch;
-                ncur += 2 * nOpen;
-                nnxt += nKeep;
-                __syncwarp();
-                // exact pair terms with every particle of the listed leaves
-                unsigned mp = mPart;
-                while (mp) {
-                    const int src = __ffs(mp) - 1;
-                    mp &= mp - 1;
-                    const int pn = __shfl_sync(0xffffffffu, node, src);
-                    const uint32_t f0 = geom[pn].from, f1 = geom[pn].to;
-                    nExact += 1;
-                    nPp += uint64_t(cnt) * (f1 - f0);
-                    for (uint32_t t = f0; t < f1; ++t) {
-                        const uint32_t j = idx[t];
-                        const dbl4 rj = r[j];
-                        const double mj = G * m[j];
-                        if (active) {
-                            double gx, gy, gz;
-                            gravGrad(rj.x - ri.x, rj.y - ri.y, rj.z - ri.z, 0.5 * (rj.w + ri.w), lut, kernelRadius,
-                                gx, gy, gz);
-                            ax += mj * gx;
-                            ay += mj * gy;
-                            az += mj * gz;
-                        }
-                    }
-                }
-                // multipole expansions
-                unsigned mn = mNode;
-                while (mn) {
-                    const int src = __ffs(mn) - 1;
-                    mn &= mn - 1;
-                    const int nn = __shfl_sync(0xffffffffu, node, src);
-                    nApprox += 1;
-                    nPn += cnt;
-                    if (active) {
-                        const BhNodeGeom& ng = geom[nn];
-                        evalMultipole(ri.x - ng.com[0], ri.y - ng.com[1], ri.z - ng.com[2], mom[nn], order, ax, ay, az);
-                    }
-                }
-            }
-            // the kept entries are the check list of the next ancestor
-            int32_t* t = cur;
-            cur = nxt;
-            nxt = t;
-            ncur = nnxt;
-            nnxt = 0;
-        }
-        if (overflow) {
-            if (lane == 0) {
-                atomicOr(devError, uint32_t(DEV_ERR_WALK_CAPACITY));
-            }
-            continue;
-        }
-        // intra-leaf pairs
-        nPp += uint64_t(cnt) * (cnt - 1);
-        for (uint32_t t = lg.from; t < lg.to; ++t) {
-            const uint32_t j = idx[t];
-            const dbl4 rj = r[j];
-            const double mj = G * m[j];
-            if (active && j != pi) {
-                double gx, gy, gz;
-                gravGrad(rj.x - ri.x, rj.y - ri.y, rj.z - ri.z, 0.5 * (rj.w + ri.w), lut, kernelRadius, gx, gy, gz);
-                ax += mj * gx;
-                ay += mj * gy;
-                az += mj * gz;
-            }
-        }
-        if (active) {
-            agrav[pi] = mkd4(ax, ay, az, 0.);
-        }
-    }
-    if (lane == 0) {
-        atomicAdd(&stats[0], nApprox);
-        atomicAdd(&stats[1], nExact);
-        atomicAdd(&stats[2], nPn);
-        atomicAdd(&stats[3], nPp);
-    }
-}
-
-// BarnesHut::evalImpl / evalExact (core/gravity/BarnesHut.cpp:118-175, 364-374): one thread per point
 __global__ void pointsKernel(const dbl4* __restrict__ r, const double* __restrict__ m, double G,
     const uint32_t* __restrict__ idx, const BhNodeGeom* __restrict__ geom, const BhNodeMoments* __restrict__ mom,
     const double* __restrict__ lut, int kernelRadius, int order, double thetaInv, const dbl4* pts, dbl4* acc,
@@ -800,30 +605,220 @@ void treeEnsureFp64Moments(const DState& s, Tree& t, const Physics& ph, cudaStre
     }
 }
 
+namespace {
+
+constexpr int WALK_THREADS_D = 128;
+
+// Walk phase 2 in FP64 (the plain FP64 path): for each leaf, the lists of its ancestors (built once per node by
+// phase 1, the reference's lists) and the pairs inside the leaf, one warp per leaf, a lane per particle.
+// Multipoles: evaluateGravity (core/gravity/Moments.h:336-360) on the FP64 reduced moments; pairs:
+// GravityLutKernel::grad (core/sph/kernel/GravityKernel.h:69-80). The reciprocal powers come from one FP64
+// reciprocal square root instead of a division and a square root (a last-bit difference), the rest is the
+// reference's arithmetic; sums in FP64 in list order.
+__device__ __forceinline__ void multipole64(double drx, double dry, double drz, const BhNodeMoments& mo, int order,
+    double& ax, double& ay, double& az) {
+    const double invDist = rsqrt(drx * drx + dry * dry + drz * drz);
+    const double invDistSqr = invDist * invDist;
+    double gamma[5];
+    gamma[0] = -invDist;
+    for (int i = 1; i < 5; ++i) {
+        gamma[i] = -(2. * i - 1.) * invDistSqr * gamma[i - 1];
+    }
+    const double x[3] = { -drx, -dry, -drz };
+    double a[3] = { 0., 0., 0. };
+    if (order >= 3) {
+        double Q1[3], Q0 = 0.;
+        for (int i = 0; i < 3; ++i) {
+            double sum = 0.;
+            for (int j = 0; j < 3; ++j) {
+                for (int k = 0; k < 3; ++k) {
+                    sum += mo.q3[i3(i, j, k)] * x[j] * x[k];
+                }
+            }
+            Q1[i] = sum * 0.5;
+            Q0 += sum * x[i];
+        }
+        Q0 *= 1. / 6.;
+        for (int i = 0; i < 3; ++i) {
+            a[i] += gamma[4] * x[i] * Q0 + gamma[3] * Q1[i];
+        }
+    }
+    if (order >= 2) {
+        double Q1[3], Q0 = 0.;
+        for (int i = 0; i < 3; ++i) {
+            Q1[i] = mo.q2[i2(i, 0)] * x[0] + mo.q2[i2(i, 1)] * x[1] + mo.q2[i2(i, 2)] * x[2];
+            Q0 += Q1[i] * x[i];
+        }
+        Q0 *= 0.5;
+        for (int i = 0; i < 3; ++i) {
+            a[i] += gamma[3] * x[i] * Q0 + gamma[2] * Q1[i];
+        }
+    }
+    for (int i = 0; i < 3; ++i) {
+        a[i] += gamma[1] * x[i] * mo.m0;
+    }
+    ax += a[0];
+    ay += a[1];
+    az += a[2];
+}
+
+__device__ __forceinline__ void pair64(double rx, double ry, double rz, double h, double m, const double* __restrict__ lut,
+    int kernelRadius, double& ax, double& ay, double& az) {
+    const double hInv = 1. / h;
+    const double sx = rx * hInv, sy = ry * hInv, sz = rz * hInv;
+    const double qSqr = sx * sx + sy * sy + sz * sz;
+    const double rad = double(kernelRadius);
+    double gx, gy, gz;
+    if (qSqr + SPH_EPS >= rad * rad) {
+        const double inv = rsqrt(rx * rx + ry * ry + rz * rz);
+        const double inv3 = inv * inv * inv;
+        gx = rx * inv3;
+        gy = ry * inv3;
+        gz = rz * inv3;
+    } else {
+        const double floatIdx = (double(LUT_ENTRIES) * (1. / (2. * 2.))) * qSqr;
+        const int idx1 = int(floatIdx);
+        const double ratio = floatIdx - double(idx1);
+        const double g = __ldg(lut + idx1) * (1. - ratio) + __ldg(lut + idx1 + 1) * ratio;
+        const double h3 = hInv * hInv * hInv;
+        gx = (h3 * rx) * g;
+        gy = (h3 * ry) * g;
+        gz = (h3 * rz) * g;
+    }
+    ax += m * gx;
+    ay += m * gy;
+    az += m * gz;
+}
+
+__global__ void __launch_bounds__(WALK_THREADS_D) evalLists64Kernel(const dbl4* __restrict__ r,
+    const double* __restrict__ m, double G, const uint32_t* __restrict__ idx, const BhNodeGeom* __restrict__ geom,
+    const BhNodeMoments* __restrict__ mom, const uint32_t* __restrict__ leaves, uint32_t nLeaves,
+    const double* __restrict__ lut, int kernelRadius, int order, const int32_t* __restrict__ pool,
+    const uint32_t* __restrict__ meta, dbl4* agrav, unsigned long long* stats) {
+    constexpr int W = WALK_THREADS_D / 32;
+    __shared__ int32_t pathSh[W][MAX_PATH_F];
+    __shared__ unsigned long long countSh[W][4];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    int32_t* path = pathSh[wib];
+    unsigned long long* wc = countSh[wib];
+    if (lane < 4) {
+        wc[lane] = 0;
+    }
+    __syncwarp();
+    for (;;) {
+        uint32_t li = 0;
+        if (lane == 0) {
+            li = uint32_t(atomicAdd(&stats[4], 1ull));
+        }
+        li = __shfl_sync(0xffffffffu, li, 0);
+        if (li >= nLeaves) {
+            break;
+        }
+        const int leaf = int(leaves[li]);
+        const uint32_t from = geom[leaf].from, to = geom[leaf].to;
+        const uint32_t cnt = to - from;
+        int depth = 0;
+        if (lane == 0) {
+            depth = min(geom[leaf].level, MAX_PATH_F - 1);
+            int nd = leaf;
+            for (int k = depth; k >= 0; --k) {
+                path[k] = nd;
+                nd = geom[nd].parent;
+            }
+        }
+        depth = __shfl_sync(0xffffffffu, depth, 0);
+        __syncwarp();
+        const bool active = uint32_t(lane) < cnt;
+        uint32_t pi = 0;
+        dbl4 ri = mkd4(0., 0., 0., 1.);
+        if (active) {
+            pi = idx[from + lane];
+            ri = r[pi];
+        }
+        double ax = 0., ay = 0., az = 0.;
+        uint32_t leafN = 0, leafP = 0, leafSrc = 0;
+        for (int k = 1; k <= depth; ++k) {
+            const uint32_t* mt = meta + size_t(path[k]) * NL_META;
+            const uint32_t nOff = mt[0], nLen = mt[1], pOff = mt[2], pLen = mt[3];
+            leafN += nLen;
+            leafP += pLen;
+            for (uint32_t c = 0; c < pLen; ++c) {
+                const int pn = pool[pOff + c];
+                const uint32_t f0 = geom[pn].from, f1 = geom[pn].to;
+                leafSrc += f1 - f0;
+                for (uint32_t t = f0; t < f1; ++t) {
+                    const uint32_t j = idx[t];
+                    const dbl4 rj = r[j];
+                    const double mj = G * m[j];
+                    if (active) {
+                        pair64(rj.x - ri.x, rj.y - ri.y, rj.z - ri.z, 0.5 * (rj.w + ri.w), mj, lut, kernelRadius, ax,
+                            ay, az);
+                    }
+                }
+            }
+            for (uint32_t c = 0; c < nLen; ++c) {
+                const int nn = pool[nOff + c];
+                if (active) {
+                    const BhNodeGeom& ng = geom[nn];
+                    multipole64(ri.x - ng.com[0], ri.y - ng.com[1], ri.z - ng.com[2], mom[nn], order, ax, ay, az);
+                }
+            }
+        }
+        // pairs inside the leaf
+        for (uint32_t t = from; t < to; ++t) {
+            const uint32_t j = idx[t];
+            const dbl4 rj = r[j];
+            const double mj = G * m[j];
+            if (active && t != from + uint32_t(lane)) {
+                pair64(rj.x - ri.x, rj.y - ri.y, rj.z - ri.z, 0.5 * (rj.w + ri.w), mj, lut, kernelRadius, ax, ay, az);
+            }
+        }
+        if (lane == 0) {
+            wc[0] += leafN;
+            wc[1] += leafP;
+            wc[2] += uint64_t(cnt) * leafN;
+            wc[3] += uint64_t(cnt) * (leafSrc + cnt - 1);
+        }
+        if (active) {
+            agrav[pi] = mkd4(ax, ay, az, 0.);
+        }
+        __syncwarp();
+    }
+    __syncwarp();
+    if (lane < 4) {
+        atomicAdd(&stats[lane], wc[lane]);
+    }
+}
+
+} // namespace
+
 void launchGravityWalk(const DState& s, Tree& t, const Physics& ph, const double* lut, uint32_t* devError,
     cudaStream_t st) {
     cudaMemsetAsync(t.stats, 0, 5 * sizeof(unsigned long long), st);
-    if (s.n == 0) {
+    t.walk_launches = 0;
+    if (s.n == 0 || t.node_count == 0) {
         return;
     }
     cudaMemsetAsync(s.agrav, 0, size_t(s.n) * sizeof(dbl4), st);
     if (ph.leaf_size > 32) {
-        // one warp owns a leaf: larger leaves are not supported by this walk
         return;
     }
+    launchWalkLists(s, t, devError, st);
     static int residentBlocks = 0;
     if (residentBlocks == 0) {
-        int perSm = 0, sms = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, walkKernel, WALK_THREADS, 0);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+        int perSm = 0, sms = 0, dev = 0;
+        cudaGetDevice(&dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, evalLists64Kernel, WALK_THREADS_D, 0);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         residentBlocks = std::max(1, perSm * sms);
     }
-    const int blocks = std::max(1, std::min(residentBlocks, int(t.walk_warps / (WALK_THREADS / 32))));
-    walkKernel<<<blocks, WALK_THREADS, 0, st>>>(s.r, s.m, ph.G, t.idx, t.geom, t.mom, t.nodef, t.leaves,
-        t.leaf_count, lut,
-        ph.kernel_radius,
-        ph.multipole_order, t.walk_scratch, t.walk_capacity, s.agrav, t.stats, devError);
+    const int blocks = std::max(1, std::min(residentBlocks, int(t.walk_warps / (WALK_THREADS_D / 32))));
+    evalLists64Kernel<<<blocks, WALK_THREADS_D, 0, st>>>(s.r, s.m, ph.G, t.idx, t.geom, t.mom, t.leaves, t.leaf_count,
+        lut, ph.kernel_radius, ph.multipole_order, t.nl_pool, t.nl_meta, s.agrav, t.stats);
+    t.walk_launches++;
 }
+
 
 void launchGravityPoints(const DState& s, const Tree& t, const Physics& ph, const double* lut, const dbl4* points,
     dbl4* acc, uint32_t npoints, cudaStream_t st) {

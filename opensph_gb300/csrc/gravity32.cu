@@ -17,7 +17,6 @@ namespace sphgpu {
 namespace {
 
 constexpr int WALK_THREADS_F = 128;
-constexpr int MAX_PATH_F = 512;
 
 __device__ __forceinline__ void splitF(double x, float& hi, float& lo) {
     hi = float(x);
@@ -184,7 +183,6 @@ constexpr uint32_t MAX_GROUPS = 4;
 // phase 2 (evalListsKernel, a warp per leaf) evaluates, for the particles of a leaf, the N and P lists of all
 // its ancestors and the pairs inside the leaf. The interaction lists are those of the per-leaf walk.
 
-constexpr int NL_META = 6; // per node: N offset, N length, P offset, P length, kept offset, kept length
 
 __global__ void flagErrorKernel(uint32_t* devError, uint32_t bit) {
     atomicOr(devError, bit);
@@ -196,7 +194,7 @@ __global__ void flagErrorKernel(uint32_t* devError, uint32_t bit) {
 // that outgrows those too is a capacity error.
 __global__ void __launch_bounds__(128, 8) listLevelKernel(const BhNodeGeom* __restrict__ geom,
     const float* __restrict__ nodef, const uint32_t* __restrict__ levelNodes, uint32_t first, uint32_t last,
-    int deferPass, uint32_t* __restrict__ defer,
+    int deferPass, uint32_t* __restrict__ defer, uint32_t scratchWarps,
     int32_t* scratch, uint32_t cap, int32_t* __restrict__ pool, uint32_t poolCap,
     const int32_t* __restrict__ keptIn, int32_t* __restrict__ keptOut, uint32_t keptCap, uint32_t* __restrict__ meta,
     uint32_t* __restrict__ counters, int parity, uint32_t* devError) {
@@ -204,7 +202,11 @@ __global__ void __launch_bounds__(128, 8) listLevelKernel(const BhNodeGeom* __re
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const uint32_t warpGlobal = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nWarps = (gridDim.x * blockDim.x) >> 5;
+    // the warps that have staging lists in the scratch (the grid is rounded up to whole blocks)
+    const uint32_t nWarps = min((gridDim.x * blockDim.x) >> 5, scratchWarps);
+    if (warpGlobal >= nWarps) {
+        return;
+    }
     int32_t* cur = scratch + size_t(warpGlobal) * 4 * cap;
     int32_t* kept = cur + cap;
     int32_t* lN = kept + cap;
@@ -701,13 +703,8 @@ void launchPrepareWalkDev(const DState& s, Tree& t, const Physics& ph, cudaStrea
         t.nodef, t.pf, t.mf, !t.mixed_moments);
 }
 
-void launchGravityWalkMixed(const DState& s, Tree& t, const Physics& ph, const float* lutF, uint32_t* devError,
-    cudaStream_t st) {
-    cudaMemsetAsync(t.stats, 0, 5 * sizeof(unsigned long long), st);
-    t.walk_launches = 0;
-    if (s.n == 0 || t.node_count == 0) {
-        return;
-    }
+// walk phase 1 for both precisions: the node, particle-list and kept lists of every node, level by level
+void launchWalkLists(const DState& s, Tree& t, uint32_t* devError, cudaStream_t st) {
     if (!t.nl_meta) {
         cudaMalloc(&t.nl_meta, size_t(t.node_capacity) * NL_META * sizeof(uint32_t));
         cudaMalloc(&t.nl_counters, 8 * sizeof(uint32_t));
@@ -766,12 +763,12 @@ void launchGravityWalkMixed(const DState& s, Tree& t, const Physics& ph, const f
             cudaMemsetAsync(t.nl_counters + 4, 0, sizeof(uint32_t), st);
             const uint32_t warps = std::min(last - first, listWarps);
             listLevelKernel<<<ceilDiv(warps, 4), 128, 0, st>>>(t.geom, t.nodef, t.level_nodes, first, last, 0,
-                t.nl_defer,
+                t.nl_defer, warps,
                 t.walk_scratch, NL_STAGE, t.nl_pool, t.nl_capacity, t.nl_kept[1 - parity], t.nl_kept[parity],
                 t.nl_kept_capacity, t.nl_meta, t.nl_counters, parity, devError);
             const uint32_t dWarps = std::min(last - first, deferWarps);
             listLevelKernel<<<ceilDiv(dWarps, 4), 128, 0, st>>>(t.geom, t.nodef, t.level_nodes, first, last, 1,
-                t.nl_defer,
+                t.nl_defer, dWarps,
                 t.walk_scratch, NL_STAGE_DEFER, t.nl_pool, t.nl_capacity, t.nl_kept[1 - parity], t.nl_kept[parity],
                 t.nl_kept_capacity, t.nl_meta, t.nl_counters, parity, devError);
             t.walk_launches += 2;
@@ -788,6 +785,17 @@ void launchGravityWalkMixed(const DState& s, Tree& t, const Physics& ph, const f
     if (!fits) {
         flagErrorKernel<<<1, 1, 0, st>>>(devError, uint32_t(DEV_ERR_WALK_CAPACITY));
     }
+    (void)s;
+}
+
+void launchGravityWalkMixed(const DState& s, Tree& t, const Physics& ph, const float* lutF, uint32_t* devError,
+    cudaStream_t st) {
+    cudaMemsetAsync(t.stats, 0, 5 * sizeof(unsigned long long), st);
+    t.walk_launches = 0;
+    if (s.n == 0 || t.node_count == 0) {
+        return;
+    }
+    launchWalkLists(s, t, devError, st);
     static int residentBlocks = 0;
     if (residentBlocks == 0) {
         int perSm = 0, sms = 0;

@@ -366,6 +366,8 @@ void launchPrepareWalkDev(const DState& s, Tree& t, const Physics& ph, cudaStrea
 void treeEnsureFp64Moments(const DState& s, Tree& t, const Physics& ph, cudaStream_t st);
 void launchGravityWalk(const DState& s, Tree& t, const Physics& ph, const double* lut_grad, uint32_t* dev_error,
     cudaStream_t st);
+// (gravity32.cu) walk phase 1, shared by both walks: the interaction lists of every node, level by level
+void launchWalkLists(const DState& s, Tree& t, uint32_t* dev_error, cudaStream_t st);
 void launchGravityWalkMixed(const DState& s, Tree& t, const Physics& ph, const float* lut_grad_f,
     uint32_t* dev_error, cudaStream_t st);
 // BarnesHut::evalAttractors on the device: att (5 doubles per attractor), dv (particles, in/out), acc (3 doubles per

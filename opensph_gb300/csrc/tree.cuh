@@ -116,27 +116,33 @@ __device__ __forceinline__ void evalMultipole(double drx, double dry, double drz
     az += a[2];
 }
 
-// Sphere::intersectsBox: 0 box outside, 1 intersection, 2 box inside the sphere
+// Sphere::intersectsBox (core/objects/geometry/Sphere.h:70-116): 0 box outside, 1 intersection, 2 box inside the
+// sphere. Every product and sum is an explicitly rounded intrinsic, never contracted into a fused multiply-add
+// whatever the translation unit's flags, so that the decisions at the margin are the reference's (its squared
+// lengths sum x, y, z left to right).
+__device__ __forceinline__ double sqrLength3(double x, double y, double z) {
+    return __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
+}
+
 __device__ int intersectsBox(const double p[3], double rad, const double lo[3], const double hi[3]) {
-    double l2 = 0., r2 = 0.;
+    double lft[3], rgt[3];
     for (int d = 0; d < 3; ++d) {
-        const double lft = fmax(lo[d] - p[d], 0.);
-        const double rgt = fmax(p[d] - hi[d], 0.);
-        l2 = d == 0 ? lft * lft : l2 + lft * lft;
-        r2 = d == 0 ? rgt * rgt : r2 + rgt * rgt;
+        lft[d] = fmax(__dsub_rn(lo[d], p[d]), 0.);
+        rgt[d] = fmax(__dsub_rn(p[d], hi[d]), 0.);
     }
-    const double rSqr = rad * rad;
-    const double distSqr = rSqr - l2 - r2;
+    const double rSqr = __dmul_rn(rad, rad);
+    const double distSqr = __dsub_rn(__dsub_rn(rSqr, sqrLength3(lft[0], lft[1], lft[2])),
+        sqrLength3(rgt[0], rgt[1], rgt[2]));
     if (!(distSqr > 0.)) {
         return 0;
     }
-    const double sx = hi[0] - lo[0], sy = hi[1] - lo[1], sz = hi[2] - lo[2];
-    const double vx[8] = { lo[0], lo[0] + sx, lo[0] + 0., lo[0] + 0., hi[0], hi[0] - sx, hi[0] - 0., hi[0] - 0. };
-    const double vy[8] = { lo[1], lo[1] + 0., lo[1] + sy, lo[1] + 0., hi[1], hi[1] - 0., hi[1] - sy, hi[1] - 0. };
-    const double vz[8] = { lo[2], lo[2] + 0., lo[2] + 0., lo[2] + sz, hi[2], hi[2] - 0., hi[2] - 0., hi[2] - sz };
+    const double sx = __dsub_rn(hi[0], lo[0]), sy = __dsub_rn(hi[1], lo[1]), sz = __dsub_rn(hi[2], lo[2]);
+    const double vx[8] = { lo[0], __dadd_rn(lo[0], sx), lo[0], lo[0], hi[0], __dsub_rn(hi[0], sx), hi[0], hi[0] };
+    const double vy[8] = { lo[1], lo[1], __dadd_rn(lo[1], sy), lo[1], hi[1], hi[1], __dsub_rn(hi[1], sy), hi[1] };
+    const double vz[8] = { lo[2], lo[2], lo[2], __dadd_rn(lo[2], sz), hi[2], hi[2], hi[2], __dsub_rn(hi[2], sz) };
     for (int k = 0; k < 8; ++k) {
-        const double dx = vx[k] - p[0], dy = vy[k] - p[1], dz = vz[k] - p[2];
-        if (!(dx * dx + dy * dy + dz * dz < rSqr)) {
+        const double d2 = sqrLength3(__dsub_rn(vx[k], p[0]), __dsub_rn(vy[k], p[1]), __dsub_rn(vz[k], p[2]));
+        if (!(d2 < rSqr)) {
             return 1;
         }
     }
@@ -153,6 +159,10 @@ enum : int { CL_KEEP = 0, CL_PARTICLES = 1, CL_NODE = 2, CL_OPEN = 3 };
 // Centres and corners are unevaluated float pairs (hi + lo) of the FP64 values. The signed r_open is
 // -r_open for leaves and +r_open for inner nodes; it is (either signed) zero exactly when the FP64 r_open is
 // zero (a tiny positive r_open is stored as the smallest normal float).
+// walk lists, per node: N offset, N length, P offset, P length, kept offset, kept length
+constexpr int NL_META = 6;
+constexpr int MAX_PATH_F = 512;
+
 constexpr int NODEF = 40;
 constexpr int NODEF4 = NODEF / 4;
 constexpr int NF_COM_HI = 0;

@@ -4,7 +4,8 @@
 
 Each translation unit is compiled in parallel; the FP64 units are compiled without FMA contraction
 (-fmad=false) so that their per-pair terms are the IEEE-identical expressions of the reference, the
-mixed-precision unit with contraction. Host code is compiled with -ffp-contract=off for the same reason
+mixed-precision units and the FP64 gravity evaluation (walk64.cu, whose terms differ from the reference's in
+the last bits only) with contraction. Host code is compiled with -ffp-contract=off for the same reason
 (the LUT tables built on the host must match the reference's bit for bit on both x86 and Arm hosts).
 """
 import argparse
@@ -30,6 +31,7 @@ UNITS = {
     "treebuild.cu": ["-fmad=false"],
     "sph32.cu": [],
     "gravity32.cu": [],
+    "walk64.cu": [],
     "noalloc.cu": [],
     "peak.cu": [],
     "adjoint.cu": ["-fmad=false"],

@@ -7,8 +7,8 @@
 // Walk: the interaction lists of every node come from the list phase shared with the mixed walk (gravity32.cu:
 // the reference's dual-walk classification, core/gravity/BarnesHut.cpp:212-312 with Sphere::intersectsBox,
 // core/objects/geometry/Sphere.h:70-116, done once per node level by level, FP32-guarded with FP64 decisions at
-// the margin), so every leaf receives exactly the reference's particle list and node list; evalLists64Kernel
-// evaluates them in FP64, a warp per leaf and a lane per particle.
+// the margin), so every leaf receives exactly the reference's particle list and node list; walk64.cu evaluates
+// them in FP64, a warp per leaf and a lane per particle.
 
 #include <algorithm>
 
@@ -604,221 +604,6 @@ void treeEnsureFp64Moments(const DState& s, Tree& t, const Physics& ph, cudaStre
         t.mixed_moments = false;
     }
 }
-
-namespace {
-
-constexpr int WALK_THREADS_D = 128;
-
-// Walk phase 2 in FP64 (the plain FP64 path): for each leaf, the lists of its ancestors (built once per node by
-// phase 1, the reference's lists) and the pairs inside the leaf, one warp per leaf, a lane per particle.
-// Multipoles: evaluateGravity (core/gravity/Moments.h:336-360) on the FP64 reduced moments; pairs:
-// GravityLutKernel::grad (core/sph/kernel/GravityKernel.h:69-80). The reciprocal powers come from one FP64
-// reciprocal square root instead of a division and a square root (a last-bit difference), the rest is the
-// reference's arithmetic; sums in FP64 in list order.
-__device__ __forceinline__ void multipole64(double drx, double dry, double drz, const BhNodeMoments& mo, int order,
-    double& ax, double& ay, double& az) {
-    const double invDist = rsqrt(drx * drx + dry * dry + drz * drz);
-    const double invDistSqr = invDist * invDist;
-    double gamma[5];
-    gamma[0] = -invDist;
-    for (int i = 1; i < 5; ++i) {
-        gamma[i] = -(2. * i - 1.) * invDistSqr * gamma[i - 1];
-    }
-    const double x[3] = { -drx, -dry, -drz };
-    double a[3] = { 0., 0., 0. };
-    if (order >= 3) {
-        double Q1[3], Q0 = 0.;
-        for (int i = 0; i < 3; ++i) {
-            double sum = 0.;
-            for (int j = 0; j < 3; ++j) {
-                for (int k = 0; k < 3; ++k) {
-                    sum += mo.q3[i3(i, j, k)] * x[j] * x[k];
-                }
-            }
-            Q1[i] = sum * 0.5;
-            Q0 += sum * x[i];
-        }
-        Q0 *= 1. / 6.;
-        for (int i = 0; i < 3; ++i) {
-            a[i] += gamma[4] * x[i] * Q0 + gamma[3] * Q1[i];
-        }
-    }
-    if (order >= 2) {
-        double Q1[3], Q0 = 0.;
-        for (int i = 0; i < 3; ++i) {
-            Q1[i] = mo.q2[i2(i, 0)] * x[0] + mo.q2[i2(i, 1)] * x[1] + mo.q2[i2(i, 2)] * x[2];
-            Q0 += Q1[i] * x[i];
-        }
-        Q0 *= 0.5;
-        for (int i = 0; i < 3; ++i) {
-            a[i] += gamma[3] * x[i] * Q0 + gamma[2] * Q1[i];
-        }
-    }
-    for (int i = 0; i < 3; ++i) {
-        a[i] += gamma[1] * x[i] * mo.m0;
-    }
-    ax += a[0];
-    ay += a[1];
-    az += a[2];
-}
-
-__device__ __forceinline__ void pair64(double rx, double ry, double rz, double h, double m, const double* __restrict__ lut,
-    int kernelRadius, double& ax, double& ay, double& az) {
-    const double hInv = 1. / h;
-    const double sx = rx * hInv, sy = ry * hInv, sz = rz * hInv;
-    const double qSqr = sx * sx + sy * sy + sz * sz;
-    const double rad = double(kernelRadius);
-    double gx, gy, gz;
-    if (qSqr + SPH_EPS >= rad * rad) {
-        const double inv = rsqrt(rx * rx + ry * ry + rz * rz);
-        const double inv3 = inv * inv * inv;
-        gx = rx * inv3;
-        gy = ry * inv3;
-        gz = rz * inv3;
-    } else {
-        const double floatIdx = (double(LUT_ENTRIES) * (1. / (2. * 2.))) * qSqr;
-        const int idx1 = int(floatIdx);
-        const double ratio = floatIdx - double(idx1);
-        const double g = __ldg(lut + idx1) * (1. - ratio) + __ldg(lut + idx1 + 1) * ratio;
-        const double h3 = hInv * hInv * hInv;
-        gx = (h3 * rx) * g;
-        gy = (h3 * ry) * g;
-        gz = (h3 * rz) * g;
-    }
-    ax += m * gx;
-    ay += m * gy;
-    az += m * gz;
-}
-
-__global__ void __launch_bounds__(WALK_THREADS_D) evalLists64Kernel(const dbl4* __restrict__ r,
-    const double* __restrict__ m, double G, const uint32_t* __restrict__ idx, const BhNodeGeom* __restrict__ geom,
-    const BhNodeMoments* __restrict__ mom, const uint32_t* __restrict__ leaves, uint32_t nLeaves,
-    const double* __restrict__ lut, int kernelRadius, int order, const int32_t* __restrict__ pool,
-    const uint32_t* __restrict__ meta, dbl4* agrav, unsigned long long* stats) {
-    constexpr int W = WALK_THREADS_D / 32;
-    __shared__ int32_t pathSh[W][MAX_PATH_F];
-    __shared__ unsigned long long countSh[W][4];
-    const int lane = threadIdx.x & 31;
-    const int wib = threadIdx.x >> 5;
-    int32_t* path = pathSh[wib];
-    unsigned long long* wc = countSh[wib];
-    if (lane < 4) {
-        wc[lane] = 0;
-    }
-    __syncwarp();
-    for (;;) {
-        uint32_t li = 0;
-        if (lane == 0) {
-            li = uint32_t(atomicAdd(&stats[4], 1ull));
-        }
-        li = __shfl_sync(0xffffffffu, li, 0);
-        if (li >= nLeaves) {
-            break;
-        }
-        const int leaf = int(leaves[li]);
-        const uint32_t from = geom[leaf].from, to = geom[leaf].to;
-        const uint32_t cnt = to - from;
-        int depth = 0;
-        if (lane == 0) {
-            depth = min(geom[leaf].level, MAX_PATH_F - 1);
-            int nd = leaf;
-            for (int k = depth; k >= 0; --k) {
-                path[k] = nd;
-                nd = geom[nd].parent;
-            }
-        }
-        depth = __shfl_sync(0xffffffffu, depth, 0);
-        __syncwarp();
-        const bool active = uint32_t(lane) < cnt;
-        uint32_t pi = 0;
-        dbl4 ri = mkd4(0., 0., 0., 1.);
-        if (active) {
-            pi = idx[from + lane];
-            ri = r[pi];
-        }
-        double ax = 0., ay = 0., az = 0.;
-        uint32_t leafN = 0, leafP = 0, leafSrc = 0;
-        for (int k = 1; k <= depth; ++k) {
-            const uint32_t* mt = meta + size_t(path[k]) * NL_META;
-            const uint32_t nOff = mt[0], nLen = mt[1], pOff = mt[2], pLen = mt[3];
-            leafN += nLen;
-            leafP += pLen;
-            for (uint32_t c = 0; c < pLen; ++c) {
-                const int pn = pool[pOff + c];
-                const uint32_t f0 = geom[pn].from, f1 = geom[pn].to;
-                leafSrc += f1 - f0;
-                for (uint32_t t = f0; t < f1; ++t) {
-                    const uint32_t j = idx[t];
-                    const dbl4 rj = r[j];
-                    const double mj = G * m[j];
-                    if (active) {
-                        pair64(rj.x - ri.x, rj.y - ri.y, rj.z - ri.z, 0.5 * (rj.w + ri.w), mj, lut, kernelRadius, ax,
-                            ay, az);
-                    }
-                }
-            }
-            for (uint32_t c = 0; c < nLen; ++c) {
-                const int nn = pool[nOff + c];
-                if (active) {
-                    const BhNodeGeom& ng = geom[nn];
-                    multipole64(ri.x - ng.com[0], ri.y - ng.com[1], ri.z - ng.com[2], mom[nn], order, ax, ay, az);
-                }
-            }
-        }
-        // pairs inside the leaf
-        for (uint32_t t = from; t < to; ++t) {
-            const uint32_t j = idx[t];
-            const dbl4 rj = r[j];
-            const double mj = G * m[j];
-            if (active && t != from + uint32_t(lane)) {
-                pair64(rj.x - ri.x, rj.y - ri.y, rj.z - ri.z, 0.5 * (rj.w + ri.w), mj, lut, kernelRadius, ax, ay, az);
-            }
-        }
-        if (lane == 0) {
-            wc[0] += leafN;
-            wc[1] += leafP;
-            wc[2] += uint64_t(cnt) * leafN;
-            wc[3] += uint64_t(cnt) * (leafSrc + cnt - 1);
-        }
-        if (active) {
-            agrav[pi] = mkd4(ax, ay, az, 0.);
-        }
-        __syncwarp();
-    }
-    __syncwarp();
-    if (lane < 4) {
-        atomicAdd(&stats[lane], wc[lane]);
-    }
-}
-
-} // namespace
-
-void launchGravityWalk(const DState& s, Tree& t, const Physics& ph, const double* lut, uint32_t* devError,
-    cudaStream_t st) {
-    cudaMemsetAsync(t.stats, 0, 5 * sizeof(unsigned long long), st);
-    t.walk_launches = 0;
-    if (s.n == 0 || t.node_count == 0) {
-        return;
-    }
-    cudaMemsetAsync(s.agrav, 0, size_t(s.n) * sizeof(dbl4), st);
-    if (ph.leaf_size > 32) {
-        return;
-    }
-    launchWalkLists(s, t, devError, st);
-    static int residentBlocks = 0;
-    if (residentBlocks == 0) {
-        int perSm = 0, sms = 0, dev = 0;
-        cudaGetDevice(&dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, evalLists64Kernel, WALK_THREADS_D, 0);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        residentBlocks = std::max(1, perSm * sms);
-    }
-    const int blocks = std::max(1, std::min(residentBlocks, int(t.walk_warps / (WALK_THREADS_D / 32))));
-    evalLists64Kernel<<<blocks, WALK_THREADS_D, 0, st>>>(s.r, s.m, ph.G, t.idx, t.geom, t.mom, t.leaves, t.leaf_count,
-        lut, ph.kernel_radius, ph.multipole_order, t.nl_pool, t.nl_meta, s.agrav, t.stats);
-    t.walk_launches++;
-}
-
 
 void launchGravityPoints(const DState& s, const Tree& t, const Physics& ph, const double* lut, const dbl4* points,
     dbl4* acc, uint32_t npoints, cudaStream_t st) {

@@ -121,6 +121,27 @@ def test_sph_pair_terms_are_antisymmetric(stirred, precision, tol):
     assert np.abs(mdv.sum(axis=0)).max() < tol * np.abs(mdv).sum(axis=0).max()
 
 
+def test_gravity_full_size_matches_oracle(impact):
+    # self-gravity alone on the 1,083,803-particle impact: the FP64 walk within 1e-13 of the oracle's Barnes-Hut
+    # (core/gravity/BarnesHut.cpp) with the same interaction counts, and the mixed walk within 1e-6 of the FP64
+    # walk (it takes the same interaction lists, so a single node approximated instead of opened, a change of
+    # about 1e-5, shows)
+    st, mats = impact
+    n = len(st["m"])
+    oracle.set_threads(0)
+    ref, ref_stats = oracle.gravity_bh(st["r"], st["m"], G=abi.GRAVITY_CONSTANT)
+    ref = ref.reshape(-1, 4)[:, :3]
+    acc = {}
+    for prec in (abi.PRECISION_FP64, abi.PRECISION_MIXED):
+        cfg, keep = config(n, mats, prec)
+        with GpuSolver(cfg, keep) as g:
+            g.set_state(fresh(st))
+            acc[prec] = g.gravity().reshape(-1, 4)[:, :3]
+            assert g.gravity_stats() == list(ref_stats)
+    assert scale_err(acc[abi.PRECISION_FP64], ref) < 1e-13
+    assert scale_err(acc[abi.PRECISION_MIXED], acc[abi.PRECISION_FP64]) < 1e-6
+
+
 def test_plummer_full_size_against_direct_sum():
     # gravity-only N-body at 4,194,304 particles (Plummer sphere, G = 1, softening 1e-3, theta 0.5, octupole):
     # the FP64 and mixed walks take the same interactions, agree within 2e-6, and both are within the opening

@@ -580,6 +580,10 @@ sphgpu_status validate(const sphgpu_config* c) {
     if (c->precision != SPHGPU_PRECISION_FP64 && c->precision != SPHGPU_PRECISION_MIXED) {
         return fail(nullptr, SPHGPU_ERR_UNSUPPORTED, "unknown precision %d", c->precision);
     }
+    if (c->precision == SPHGPU_PRECISION_MIXED && !nbody && c->particle_count >= NB_MAX_PARTICLES) {
+        return fail(nullptr, SPHGPU_ERR_UNSUPPORTED, "the mixed-precision SPH path takes fewer than %u particles",
+            NB_MAX_PARTICLES);
+    }
     if (c->solver_type != SPHGPU_SOLVER_SYMMETRIC && c->solver_type != SPHGPU_SOLVER_ASYMMETRIC && !nbody) {
         return fail(nullptr, SPHGPU_ERR_UNSUPPORTED, "unknown solver type %d", c->solver_type);
     }
@@ -818,7 +822,8 @@ sphgpu_status sphgpu_create(const sphgpu_config* config, sphgpu_handle** out) {
         e = cudaMallocHost((void**)&h->h_pinned, 64 * sizeof(unsigned long long));
     }
     if (e == cudaSuccess) {
-        e = gridAllocate(h->grid, n, ph.solid != 0, ph.correction != 0, !ph.nbody);
+        e = gridAllocate(h->grid, n, ph.solid != 0, ph.correction != 0, !ph.nbody,
+            !ph.nbody && ph.precision == SPHGPU_PRECISION_MIXED);
     }
     if (e == cudaSuccess && ph.gravity) {
         e = treeAllocate(h->tree, n, ph.leaf_size);

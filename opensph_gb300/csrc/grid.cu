@@ -278,7 +278,7 @@ __global__ void pairsKernel(uint32_t n, const dbl4* __restrict__ rs, const uint3
 
 } // namespace
 
-cudaError_t gridAllocate(Grid& g, uint32_t n, bool solid, bool correction, bool copies) {
+cudaError_t gridAllocate(Grid& g, uint32_t n, bool solid, bool correction, bool copies, bool neighbourLists) {
     const uint32_t nn = n > 0 ? n : 1;
     g.cell_capacity = max(1u << 12, min(4u * nn, 1u << 26));
     cudaError_t e = cudaSuccess;
@@ -316,6 +316,12 @@ cudaError_t gridAllocate(Grid& g, uint32_t n, bool solid, bool correction, bool 
     if (correction) {
         alloc((void**)&g.mxC, 6 * size_t(nn) * sizeof(float));
     }
+    if (neighbourLists) {
+        alloc((void**)&g.nb, size_t(NB_CAP) * nn * sizeof(uint32_t));
+        alloc((void**)&g.nb_count, nn * sizeof(uint32_t));
+        alloc((void**)&g.nb_over, nn * sizeof(uint32_t));
+        alloc((void**)&g.nb_over_count, sizeof(uint32_t));
+    }
     if (e != cudaSuccess) {
         return e;
     }
@@ -331,7 +337,7 @@ cudaError_t gridAllocate(Grid& g, uint32_t n, bool solid, bool correction, bool 
 void gridFree(Grid& g) {
     void* ptrs[] = { g.info, g.bounds, g.keys, g.keys_sorted, g.perm_in, g.perm, g.cell_start, g.cell_end,
         g.sort_temp, g.rs, g.vs, g.ms, g.rhos, g.ps, g.css, g.Ss, g.reduces, g.flags, g.mx0, g.mx1, g.mx2, g.mx3,
-        g.mxS, g.mxC };
+        g.mxS, g.mxC, g.nb, g.nb_count, g.nb_over, g.nb_over_count };
     for (void* p : ptrs) {
         if (p) {
             cudaFree(p);

@@ -9,6 +9,8 @@
 // Sterbenz lemma, so the FP32 difference keeps ~1e-14 relative accuracy of the FP64 inputs). Sums over
 // neighbours use Kahan compensation. Material updates, finalize and integrator stay FP64.
 
+#include <algorithm>
+
 #include "physics.cuh"
 
 namespace sphgpu {
@@ -120,132 +122,31 @@ __global__ void __launch_bounds__(128) correctionMixedKernel(DState s, Grid g, P
     }
 }
 
-// Candidates of the 27 cells are first tested (cheap: one float4 load and a distance test per candidate,
-// every lane busy) and the interacting ones queued per lane in shared memory; the pair terms are then
-// evaluated from the queues, when any lane's queue is full and at the end. The pair terms thus run with
-// nearly all lanes active instead of only the ~15 % of lanes whose candidate interacts. Each lane still
-// visits its neighbours in cell order, so the sums are the same as a direct loop's.
+// The pair loop runs in three kernels. neighboursMixedKernel tests the candidates of the 27 cells (one float4 load
+// and a distance test each) and writes the interacting ones, in cell order, to a per-particle neighbour list
+// (sorted index | cell offset << 27, laid out [slot][particle] so that a warp's writes and reads of one slot are
+// contiguous); it holds few registers and runs at full occupancy. pairSumMixedKernel then evaluates the pair terms
+// from the lists and finalizes the particle. A particle with more than NB_CAP neighbours is left to
+// pairSumMixedOverflowKernel, which scans its cells again (rare: a queue of such particles is filled by the first
+// kernel). Each particle visits its neighbours in cell order, so the sums are those of a direct loop over the cells.
 constexpr int PAIR_THREADS = 128;
-constexpr int PAIR_QUEUE = 32;
+constexpr uint32_t NB_INDEX_BITS = 27;
+constexpr uint32_t NB_INDEX_MASK = (1u << NB_INDEX_BITS) - 1u;
 
-template <bool Solid>
-__global__ void __launch_bounds__(PAIR_THREADS) pairSumMixedKernel(DState s, Grid g, Physics ph,
-    const MaterialD* __restrict__ mats, const float* __restrict__ lut) {
-    __shared__ uint32_t queueT[PAIR_QUEUE][PAIR_THREADS];
-    __shared__ uint8_t queueOff[PAIR_QUEUE][PAIR_THREADS];
-    const uint32_t n = s.n;
-    const uint32_t si = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid = si < n;
-    const uint32_t sv = valid ? si : n - 1;
+// the 27 neighbour cells of a particle in cell order, calling f(t, off) for every candidate t != si of cell off
+// (the next cell's range is loaded while the current cell's candidates are visited)
+template <typename F>
+__device__ __forceinline__ void forEachCandidate(const Grid& g, uint32_t si, F&& f) {
     const GridInfo* gi = g.info;
-    const float4 pi0 = g.mx0[sv], pi1 = g.mx1[sv], pi2 = g.mx2[sv], pi3 = g.mx3[sv];
-    const float cellf = float(gi->cell);
-    float Sif[5] = { 0, 0, 0, 0, 0 };
-    if (Solid) {
-        for (int c = 0; c < 5; ++c) {
-            Sif[c] = g.mxS[c * n + sv];
-        }
-    }
-    const float rhoiInv = 1.f / pi2.w;
-    const float alpha = float(ph.av_alpha), beta = float(ph.av_beta);
-    Kahan ax, ay, az, du, divv;
-    Kahan gv[6];
-    // strain-rate correction tensor of the velocity gradient (identity without it)
-    float Ci[6] = { 1.f, 1.f, 1.f, 0.f, 0.f, 0.f };
-    if (Solid && ph.correction) {
-        for (int k = 0; k < 6; ++k) {
-            Ci[k] = g.mxC[k * n + sv];
-        }
-    }
-    uint32_t cnt = 0;
     const int dxc = gi->dims[0], dyc = gi->dims[1], dzc = gi->dims[2];
-    const uint32_t key = g.keys_sorted[sv];
+    const uint32_t key = g.keys_sorted[si];
     const int cx = int(key % uint32_t(dxc)), cy = int((key / uint32_t(dxc)) % uint32_t(dyc)),
               cz = int(key / (uint32_t(dxc) * uint32_t(dyc)));
-
-    // pair terms of the queued neighbours (the loop is warp-uniform; each lane stops at its own count)
-    auto flush = [&](uint32_t nq) {
-        const uint32_t nmax = __reduce_max_sync(0xffffffffu, nq);
-        for (uint32_t q = 0; q < nmax; ++q) {
-            if (q >= nq) {
-                continue;
-            }
-            const uint32_t t = queueT[q][threadIdx.x];
-            const int off = queueOff[q][threadIdx.x];
-            const float sx = float(off % 3 - 1) * cellf, sy = float((off / 3) % 3 - 1) * cellf,
-                        sz = float(off / 9 - 1) * cellf;
-            const float4 pj0 = g.mx0[t];
-            const float drx = (pi0.x - pj0.x) - sx, dry = (pi0.y - pj0.y) - sy, drz = (pi0.z - pj0.z) - sz;
-            const float d2 = drx * drx + dry * dry + drz * drz;
-            const float hbar = 0.5f * (pi0.w + pj0.w);
-            const float4 pj1 = g.mx1[t], pj2 = g.mx2[t], pj3 = g.mx3[t];
-            const float hInv = 1.f / hbar;
-            const float h2 = hInv * hInv;
-            const float gl = lutGradF(lut, d2 * h2) * (h2 * h2 * hInv);
-            const float gx = drx * gl, gy = dry * gl, gz = drz * gl;
-            cnt++;
-            const float mj = pj1.w, rhoj = pj2.w;
-            const float dvx = (pj1.x - pi1.x) + (pj2.x - pi2.x);
-            const float dvy = (pj1.y - pi1.y) + (pj2.y - pi2.y);
-            const float dvz = (pj1.z - pi1.z) + (pj2.z - pi2.z);
-            const float mr = mj * rhoiInv;
-            divv.add(mr * (dvx * gx + dvy * gy + dvz * gz));
-            float fx = -(pi3.x + pj3.x), fy = fx, fz = fx;
-            fx *= gx;
-            fy *= gy;
-            fz *= gz;
-            const float dvdr = -(dvx * drx + dvy * dry + dvz * drz);
-            if (dvdr < 0.f) {
-                const float rhobar = 0.5f * (pi2.w + rhoj);
-                const float csbar = 0.5f * (pi3.y + pj3.y);
-                const float mu = hbar * dvdr / (d2 + 1.e-2f * (hbar * hbar));
-                const float av = (-alpha * csbar * mu + beta * (mu * mu)) / rhobar;
-                fx -= av * gx;
-                fy -= av * gy;
-                fz -= av * gz;
-                du.add(mj * (0.5f * av * -(dvx * gx + dvy * gy + dvz * gz)));
-            }
-            if (Solid) {
-                const bool undamaged = !ph.sum_only_undamaged ||
-                                       (__float_as_uint(pi3.w) == __float_as_uint(pj3.w) && pi3.z != 0.f &&
-                                           pj3.z != 0.f);
-                if (undamaged) {
-                    float hx = gx, hy = gy, hz = gz;
-                    if (ph.correction) {
-                        hx = Ci[0] * gx + Ci[3] * gy + Ci[4] * gz;
-                        hy = Ci[3] * gx + Ci[1] * gy + Ci[5] * gz;
-                        hz = Ci[4] * gx + Ci[5] * gy + Ci[2] * gz;
-                    }
-                    gv[0].add(mr * (dvx * hx));
-                    gv[1].add(mr * (dvy * hy));
-                    gv[2].add(mr * (dvz * hz));
-                    gv[3].add(mr * (0.5f * (dvx * hy + dvy * hx)));
-                    gv[4].add(mr * (0.5f * (dvx * hz + dvz * hx)));
-                    gv[5].add(mr * (0.5f * (dvy * hz + dvz * hy)));
-                    float tt[5];
-                    for (int k = 0; k < 5; ++k) {
-                        tt[k] = Sif[k] + g.mxS[k * n + t];
-                    }
-                    const float tzz = -tt[0] - tt[1];
-                    fx += tt[0] * gx + tt[2] * gy + tt[3] * gz;
-                    fy += tt[2] * gx + tt[1] * gy + tt[4] * gz;
-                    fz += tt[3] * gx + tt[4] * gy + tzz * gz;
-                }
-            }
-            ax.add(mj * fx);
-            ay.add(mj * fy);
-            az.add(mj * fz);
-        }
-    };
-
-    uint32_t nq = 0;
-    // the particle range of neighbour cell off (empty outside the grid); the next cell's range is loaded while the
-    // current cell's candidates are tested
     auto cellRange = [&](int off, uint32_t& tb, uint32_t& te) {
         const int x = cx + off % 3 - 1, y = cy + (off / 3) % 3 - 1, z = cz + off / 9 - 1;
         tb = 0;
         te = 0;
-        if (valid && x >= 0 && x < dxc && y >= 0 && y < dyc && z >= 0 && z < dzc) {
+        if (x >= 0 && x < dxc && y >= 0 && y < dyc && z >= 0 && z < dzc) {
             const uint32_t c = (uint32_t(z) * uint32_t(dyc) + uint32_t(y)) * uint32_t(dxc) + uint32_t(x);
             tb = g.cell_start[c];
             te = g.cell_end[c];
@@ -254,61 +155,268 @@ __global__ void __launch_bounds__(PAIR_THREADS) pairSumMixedKernel(DState s, Gri
     uint32_t nextB, nextE;
     cellRange(0, nextB, nextE);
     for (int off = 0; off < 27; ++off) {
-        const int ox = off % 3 - 1, oy = (off / 3) % 3 - 1, oz = off / 9 - 1;
         const uint32_t tb = nextB, te = nextE;
         if (off + 1 < 27) {
             cellRange(off + 1, nextB, nextE);
         }
-        const uint32_t len = te - tb;
-        const uint32_t lmax = __reduce_max_sync(0xffffffffu, len);
-        const float sx = float(ox) * cellf, sy = float(oy) * cellf, sz = float(oz) * cellf;
-        for (uint32_t k = 0; k < lmax; ++k) {
-            const uint32_t t = tb + k;
-            bool pass = false;
-            if (k < len && t != si) {
-                const float4 pj0 = g.mx0[t];
-                const float drx = (pi0.x - pj0.x) - sx, dry = (pi0.y - pj0.y) - sy, drz = (pi0.z - pj0.z) - sz;
-                const float d2 = drx * drx + dry * dry + drz * drz;
-                const float rad = 2.f * (0.5f * (pi0.w + pj0.w));
-                pass = d2 < rad * rad;
-            }
-            if (pass) {
-                queueT[nq][threadIdx.x] = t;
-                queueOff[nq][threadIdx.x] = uint8_t(off);
-                ++nq;
-            }
-            if (__any_sync(0xffffffffu, nq == PAIR_QUEUE)) {
-                flush(nq);
-                nq = 0;
+        for (uint32_t t = tb; t < te; ++t) {
+            if (t != si) {
+                f(t, off);
             }
         }
     }
-    flush(nq);
-    if (!valid) {
+}
+
+// the pair test of candidate t in cell offset off against particle i (pi0: cell-relative position and h)
+__device__ __forceinline__ bool interactsMixed(const Grid& g, const float4& pi0, float cellf, uint32_t t, int off) {
+    const float sx = float(off % 3 - 1) * cellf, sy = float((off / 3) % 3 - 1) * cellf, sz = float(off / 9 - 1) * cellf;
+    const float4 pj0 = g.mx0[t];
+    const float drx = (pi0.x - pj0.x) - sx, dry = (pi0.y - pj0.y) - sy, drz = (pi0.z - pj0.z) - sz;
+    const float d2 = drx * drx + dry * dry + drz * drz;
+    const float rad = 2.f * (0.5f * (pi0.w + pj0.w));
+    return d2 < rad * rad;
+}
+
+// The candidates are visited as 9 rows of 3 cells: a row's cells have consecutive keys, so their particles form one
+// contiguous range, and a candidate's x offset follows from its position against the row's two inner cell
+// boundaries. Candidates are loaded four at a time ahead of their tests. The neighbours come out in the cell
+// order of the 27-cell stencil (x fastest, then y, then z).
+__global__ void __launch_bounds__(PAIR_THREADS) neighboursMixedKernel(Grid g, uint32_t n) {
+    const uint32_t si = blockIdx.x * blockDim.x + threadIdx.x;
+    if (si >= n) {
         return;
     }
+    const GridInfo* gi = g.info;
+    const float4 pi0 = g.mx0[si];
+    const float cellf = float(gi->cell);
+    const int dxc = gi->dims[0], dyc = gi->dims[1], dzc = gi->dims[2];
+    const uint32_t key = g.keys_sorted[si];
+    const int cx = int(key % uint32_t(dxc)), cy = int((key / uint32_t(dxc)) % uint32_t(dyc)),
+              cz = int(key / (uint32_t(dxc) * uint32_t(dyc)));
+    uint32_t c = 0;
+    for (int row = 0; row < 9; ++row) {
+        const int oy = row % 3 - 1, oz = row / 3 - 1;
+        const int y = cy + oy, z = cz + oz;
+        if (y < 0 || y >= dyc || z < 0 || z >= dzc) {
+            continue;
+        }
+        const uint32_t rowBase = (uint32_t(z) * uint32_t(dyc) + uint32_t(y)) * uint32_t(dxc);
+        uint32_t cs[3], ce[3];
+        for (int k = 0; k < 3; ++k) {
+            const int x = cx + k - 1;
+            const bool in = x >= 0 && x < dxc;
+            cs[k] = in ? g.cell_start[rowBase + uint32_t(x)] : 0u;
+            ce[k] = in ? g.cell_end[rowBase + uint32_t(x)] : 0u;
+        }
+        // the row's range and the first positions of its middle and right cells (empty cells: start = end = 0)
+        const bool ne0 = ce[0] > cs[0], ne1 = ce[1] > cs[1], ne2 = ce[2] > cs[2];
+        const uint32_t lo = ne0 ? cs[0] : (ne1 ? cs[1] : (ne2 ? cs[2] : 0u));
+        const uint32_t hi = ne2 ? ce[2] : (ne1 ? ce[1] : (ne0 ? ce[0] : 0u));
+        const uint32_t b1 = ne0 ? ce[0] : lo;
+        const uint32_t b2 = ne1 ? ce[1] : b1;
+        const float sy = float(oy) * cellf, sz = float(oz) * cellf;
+        const uint32_t offYZ = uint32_t(3 * (oy + 1) + 9 * (oz + 1));
+        // (the separation and the radius 2 h_bar = h_i + h_j, rounded as in the pair terms)
+        auto test = [&](const float4& pj0, uint32_t t) {
+            const float sx = t < b1 ? -cellf : (t < b2 ? 0.f : cellf);
+            const float drx = (pi0.x - pj0.x) - sx, dry = (pi0.y - pj0.y) - sy, drz = (pi0.z - pj0.z) - sz;
+            const float d2 = drx * drx + dry * dry + drz * drz;
+            const float rad = pi0.w + pj0.w;
+            if (d2 < rad * rad && t != si) {
+                if (c < uint32_t(NB_CAP)) {
+                    const uint32_t off = offYZ + uint32_t(t >= b1) + uint32_t(t >= b2);
+                    g.nb[size_t(c) * n + si] = t | (off << NB_INDEX_BITS);
+                }
+                ++c;
+            }
+        };
+        uint32_t t = lo;
+        for (; t + 4 <= hi; t += 4) {
+            const float4 q0 = g.mx0[t], q1 = g.mx0[t + 1], q2 = g.mx0[t + 2], q3 = g.mx0[t + 3];
+            test(q0, t);
+            test(q1, t + 1);
+            test(q2, t + 2);
+            test(q3, t + 3);
+        }
+        for (; t < hi; ++t) {
+            test(g.mx0[t], t);
+        }
+    }
+    g.nb_count[si] = c;
+    if (c > uint32_t(NB_CAP)) {
+        g.nb_over[atomicAdd(g.nb_over_count, 1u)] = si;
+    }
+}
+
+// particle i's side of the pair terms, and its sums
+struct MixedSelf {
+    float4 p0, p1, p2, p3;
+    float S[5];
+    float C[6];
+    float rhoInv;
+};
+
+struct MixedSums {
+    Kahan ax, ay, az, du, divv;
+    Kahan gv[6];
+    uint32_t cnt = 0;
+};
+
+template <bool Solid>
+__device__ __forceinline__ void loadSelfMixed(const Grid& g, const Physics& ph, uint32_t n, uint32_t si, MixedSelf& me) {
+    me.p0 = g.mx0[si];
+    me.p1 = g.mx1[si];
+    me.p2 = g.mx2[si];
+    me.p3 = g.mx3[si];
+    for (int c = 0; c < 5; ++c) {
+        me.S[c] = Solid ? g.mxS[c * n + si] : 0.f;
+    }
+    // strain-rate correction tensor of the velocity gradient (identity without it)
+    const bool corr = Solid && ph.correction;
+    for (int k = 0; k < 6; ++k) {
+        me.C[k] = corr ? g.mxC[k * n + si] : (k < 3 ? 1.f : 0.f);
+    }
+    me.rhoInv = 1.f / me.p2.w;
+}
+
+// the pair terms of neighbour t (cell offset off) of particle i, added into the sums
+template <bool Solid>
+__device__ __forceinline__ void pairTermMixed(const Grid& g, const Physics& ph, const float* __restrict__ lut,
+    uint32_t n, float cellf, const MixedSelf& me, uint32_t t, int off, MixedSums& a) {
+    const float4 &pi0 = me.p0, &pi1 = me.p1, &pi2 = me.p2, &pi3 = me.p3;
+    const float sx = float(off % 3 - 1) * cellf, sy = float((off / 3) % 3 - 1) * cellf, sz = float(off / 9 - 1) * cellf;
+    const float4 pj0 = g.mx0[t];
+    const float drx = (pi0.x - pj0.x) - sx, dry = (pi0.y - pj0.y) - sy, drz = (pi0.z - pj0.z) - sz;
+    const float d2 = drx * drx + dry * dry + drz * drz;
+    const float hbar = 0.5f * (pi0.w + pj0.w);
+    const float4 pj1 = g.mx1[t], pj2 = g.mx2[t], pj3 = g.mx3[t];
+    const float hInv = 1.f / hbar;
+    const float h2 = hInv * hInv;
+    const float gl = lutGradF(lut, d2 * h2) * (h2 * h2 * hInv);
+    const float gx = drx * gl, gy = dry * gl, gz = drz * gl;
+    a.cnt++;
+    const float mj = pj1.w, rhoj = pj2.w;
+    const float dvx = (pj1.x - pi1.x) + (pj2.x - pi2.x);
+    const float dvy = (pj1.y - pi1.y) + (pj2.y - pi2.y);
+    const float dvz = (pj1.z - pi1.z) + (pj2.z - pi2.z);
+    const float mr = mj * me.rhoInv;
+    a.divv.add(mr * (dvx * gx + dvy * gy + dvz * gz));
+    float fx = -(pi3.x + pj3.x), fy = fx, fz = fx;
+    fx *= gx;
+    fy *= gy;
+    fz *= gz;
+    const float dvdr = -(dvx * drx + dvy * dry + dvz * drz);
+    if (dvdr < 0.f) {
+        const float rhobar = 0.5f * (pi2.w + rhoj);
+        const float csbar = 0.5f * (pi3.y + pj3.y);
+        const float mu = hbar * dvdr / (d2 + 1.e-2f * (hbar * hbar));
+        const float av = (-float(ph.av_alpha) * csbar * mu + float(ph.av_beta) * (mu * mu)) / rhobar;
+        fx -= av * gx;
+        fy -= av * gy;
+        fz -= av * gz;
+        a.du.add(mj * (0.5f * av * -(dvx * gx + dvy * gy + dvz * gz)));
+    }
+    if (Solid) {
+        const bool undamaged = !ph.sum_only_undamaged ||
+                               (__float_as_uint(pi3.w) == __float_as_uint(pj3.w) && pi3.z != 0.f && pj3.z != 0.f);
+        if (undamaged) {
+            float hx = gx, hy = gy, hz = gz;
+            if (ph.correction) {
+                hx = me.C[0] * gx + me.C[3] * gy + me.C[4] * gz;
+                hy = me.C[3] * gx + me.C[1] * gy + me.C[5] * gz;
+                hz = me.C[4] * gx + me.C[5] * gy + me.C[2] * gz;
+            }
+            a.gv[0].add(mr * (dvx * hx));
+            a.gv[1].add(mr * (dvy * hy));
+            a.gv[2].add(mr * (dvz * hz));
+            a.gv[3].add(mr * (0.5f * (dvx * hy + dvy * hx)));
+            a.gv[4].add(mr * (0.5f * (dvx * hz + dvz * hx)));
+            a.gv[5].add(mr * (0.5f * (dvy * hz + dvz * hy)));
+            float tt[5];
+            for (int k = 0; k < 5; ++k) {
+                tt[k] = me.S[k] + g.mxS[k * n + t];
+            }
+            const float tzz = -tt[0] - tt[1];
+            fx += tt[0] * gx + tt[2] * gy + tt[3] * gz;
+            fy += tt[2] * gx + tt[1] * gy + tt[4] * gz;
+            fz += tt[3] * gx + tt[4] * gy + tzz * gz;
+        }
+    }
+    a.ax.add(mj * fx);
+    a.ay.add(mj * fy);
+    a.az.add(mj * fz);
+}
+
+// FP64 finalize of particle i (sorted position si) with its sums and the gravity acceleration
+template <bool Solid>
+__device__ __forceinline__ void finishMixed(const DState& s, const Grid& g, const Physics& ph,
+    const MaterialD* __restrict__ mats, uint32_t si, const MixedSums& a) {
+    const uint32_t n = s.n;
     const uint32_t i = g.perm[si];
     double gax = 0., gay = 0., gaz = 0.;
     if (ph.gravity) {
-        const dbl4 a = s.agrav[i];
-        gax = a.x;
-        gay = a.y;
-        gaz = a.z;
+        const dbl4 ag = s.agrav[i];
+        gax = ag.x;
+        gay = ag.y;
+        gaz = ag.z;
     }
     const dbl4 ri = g.rs[si];
     const double rhoi = g.rhos[si], pri = g.ps[si];
     double Si[5] = { 0, 0, 0, 0, 0 };
     double gvd[6];
     for (int c = 0; c < 6; ++c) {
-        gvd[c] = gv[c].value();
+        gvd[c] = a.gv[c].value();
     }
     if (Solid) {
         for (int c = 0; c < 5; ++c) {
             Si[c] = g.Ss[c * n + si];
         }
     }
-    finalizeParticle<Solid>(s, ph, mats, i, ri, rhoi, pri, Si, gax + ax.value(), gay + ay.value(), gaz + az.value(),
-        du.value(), divv.value(), gvd, cnt);
+    finalizeParticle<Solid>(s, ph, mats, i, ri, rhoi, pri, Si, gax + a.ax.value(), gay + a.ay.value(),
+        gaz + a.az.value(), a.du.value(), a.divv.value(), gvd, a.cnt);
+}
+
+template <bool Solid>
+__global__ void __launch_bounds__(PAIR_THREADS, 6) pairSumMixedKernel(DState s, Grid g, Physics ph,
+    const MaterialD* __restrict__ mats, const float* __restrict__ lut) {
+    const uint32_t n = s.n;
+    const uint32_t si = blockIdx.x * blockDim.x + threadIdx.x;
+    if (si >= n) {
+        return;
+    }
+    const uint32_t total = g.nb_count[si];
+    if (total > uint32_t(NB_CAP)) {
+        return; // pairSumMixedOverflowKernel
+    }
+    const float cellf = float(g.info->cell);
+    MixedSelf me;
+    loadSelfMixed<Solid>(g, ph, n, si, me);
+    MixedSums a;
+    for (uint32_t q = 0; q < total; ++q) {
+        const uint32_t e = g.nb[size_t(q) * n + si];
+        pairTermMixed<Solid>(g, ph, lut, n, cellf, me, e & NB_INDEX_MASK, int(e >> NB_INDEX_BITS), a);
+    }
+    finishMixed<Solid>(s, g, ph, mats, si, a);
+}
+
+template <bool Solid>
+__global__ void __launch_bounds__(PAIR_THREADS) pairSumMixedOverflowKernel(DState s, Grid g, Physics ph,
+    const MaterialD* __restrict__ mats, const float* __restrict__ lut) {
+    const uint32_t n = s.n;
+    const uint32_t count = min(*g.nb_over_count, n);
+    const float cellf = float(g.info->cell);
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+        const uint32_t si = g.nb_over[k];
+        MixedSelf me;
+        loadSelfMixed<Solid>(g, ph, n, si, me);
+        MixedSums a;
+        forEachCandidate(g, si, [&](uint32_t t, int off) {
+            if (interactsMixed(g, me.p0, cellf, t, off)) {
+                pairTermMixed<Solid>(g, ph, lut, n, cellf, me, t, off, a);
+            }
+        });
+        finishMixed<Solid>(s, g, ph, mats, si, a);
+    }
 }
 
 } // namespace
@@ -324,10 +432,16 @@ void launchPairSumMixed(const DState& s, const Grid& g, const Physics& ph, const
     if (!s.n) {
         return;
     }
+    cudaMemsetAsync(g.nb_over_count, 0, sizeof(uint32_t), st);
+    neighboursMixedKernel<<<ceilDiv(s.n, PAIR_THREADS), PAIR_THREADS, 0, st>>>(g, s.n);
+    // the overflow pass runs on a small fixed grid over the particles queued by the first kernel (usually none)
+    const int overBlocks = std::min(ceilDiv(s.n, PAIR_THREADS), 152);
     if (ph.solid) {
         pairSumMixedKernel<true><<<ceilDiv(s.n, PAIR_THREADS), PAIR_THREADS, 0, st>>>(s, g, ph, mats, lut);
+        pairSumMixedOverflowKernel<true><<<overBlocks, PAIR_THREADS, 0, st>>>(s, g, ph, mats, lut);
     } else {
         pairSumMixedKernel<false><<<ceilDiv(s.n, PAIR_THREADS), PAIR_THREADS, 0, st>>>(s, g, ph, mats, lut);
+        pairSumMixedOverflowKernel<false><<<overBlocks, PAIR_THREADS, 0, st>>>(s, g, ph, mats, lut);
     }
 }
 

@@ -141,6 +141,11 @@ struct Collide {
 };
 
 // Neighbour grid buffers (cell-sorted copies of the pair-loop inputs)
+// neighbour-list slots per particle of the mixed pair loop (a particle with more evaluates the rest by a second
+// scan of its cells), and the particle count up to which the lists' 27-bit indices reach
+constexpr int NB_CAP = 128;
+constexpr uint32_t NB_MAX_PARTICLES = 1u << 27;
+
 struct Grid {
     uint32_t cell_capacity = 0;
     GridInfo* info = nullptr;          // device
@@ -171,6 +176,12 @@ struct Grid {
     float4* mx3 = nullptr;     // p / rho^2, cs, stress reducing, flag (bit pattern)
     float* mxS = nullptr;      // 5 x n: S / rho^2
     float* mxC = nullptr;      // 6 x n: correction tensor (mixed path, cell-sorted)
+    // mixed pair loop: the interacting neighbours of each particle (NB_CAP x n, [slot][particle], sorted index |
+    // cell offset << 27) and their number (which may exceed NB_CAP)
+    uint32_t* nb = nullptr;
+    uint32_t* nb_count = nullptr;
+    uint32_t* nb_over = nullptr;       // particles (sorted positions) with more than NB_CAP neighbours
+    uint32_t* nb_over_count = nullptr; // device: their number
     uint32_t launches = 0;     // own kernels launched by the last build / gather (library sort excluded)
 };
 
@@ -307,7 +318,8 @@ struct Tree {
 void launchGridBuild(const DState& s, Grid& g, const Physics& ph, cudaStream_t st);
 void launchGatherSorted(const DState& s, Grid& g, const Physics& ph, cudaStream_t st);
 // copies: the cell-sorted copies of the SPH pair loops (not needed by the collision search)
-cudaError_t gridAllocate(Grid& g, uint32_t n, bool solid, bool correction = false, bool copies = true);
+cudaError_t gridAllocate(Grid& g, uint32_t n, bool solid, bool correction = false, bool copies = true,
+    bool neighbourLists = false);
 void gridFree(Grid& g);
 void launchCountPairs(const DState& s, const Grid& g, unsigned long long* count, cudaStream_t st);
 // the directed pairs (i, j), j != i, |r_j - r_i| < 2 h_i (pi NULL: count only)

@@ -306,6 +306,30 @@ def test_mixed_integrate_error_bound(name):
     np.testing.assert_array_equal(got["p"], fx["d0_p"])
 
 
+@pytest.mark.parametrize("name", ["impact_n1200", "gas_n1500"])
+def test_mixed_neighbour_list_overflow(name):
+    # smoothing lengths scaled by 1.8: most particles have several hundred neighbours, more than the 128 slots of the
+    # mixed pair loop's neighbour lists (those are evaluated by its overflow pass), the ones near the surface fewer;
+    # the mixed derivatives stay within their bound of the FP64 path's, with the same neighbour counts
+    fx = cases.load(name)
+    st0 = cases.state_of(fx, "s0_")
+    r = st0["r"].reshape(-1, 4)
+    r[:, 3] *= 1.8
+    out = {}
+    for prec in (abi.PRECISION_FP64, abi.PRECISION_MIXED):
+        cfg, keep = cases.config_of(fx, precision=prec)
+        with GpuSolver(cfg, keep) as g:
+            g.set_state({k: v.copy() for k, v in st0.items()})
+            g.integrate()
+            out[prec] = g.get_state()
+    ref, got = out[abi.PRECISION_FP64], out[abi.PRECISION_MIXED]
+    assert ref["ncnt"].max() > 128 and ref["ncnt"].min() < 128
+    np.testing.assert_array_equal(got["ncnt"], ref["ncnt"])
+    for f in ["dv", "drho", "du", "divv", "gradv", "dS"]:
+        if f in ref:
+            assert cases.scale_err(got[f], ref[f]) < 1e-5, f
+
+
 @pytest.mark.parametrize("name", ["sphere_n1000", "impact_n1200", "gas_n1500", "impact_asym_n1200"])
 def test_mixed_steps_error_bound(name):
     fx = cases.load(name)

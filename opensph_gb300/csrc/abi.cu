@@ -373,7 +373,8 @@ void evalSphPrepare(sphgpu_handle* h) {
         h->launches += 1;
     }
     Phase ph(h, SPHGPU_PHASE_NEIGHBORS);
-    launchGridBuild(h->s, h->grid, h->ph, h->stream);
+    // the mixed pair loop searches a grid of h_max cells
+    launchGridBuild(h->s, h->grid, h->ph, h->stream, h->ph.precision == SPHGPU_PRECISION_MIXED);
     h->launches += h->grid.launches;
     launchGatherSorted(h->s, h->grid, h->ph, h->stream);
     h->launches += h->grid.launches;
@@ -420,17 +421,17 @@ sphgpu_status evalDerivatives(sphgpu_handle* h) {
     }
     CUDA_TRY(h, cudaEventRecord(h->ev_fork, h->stream));
     CUDA_TRY(h, cudaStreamWaitEvent(h->gstream, h->ev_fork, 0));
-    // The material update, the neighbour grid and the pair loop are queued before the tree build, so that they run
-    // beside the build and the walk (the build returns to the host once, at its end, and the walk's list phase
-    // once, to check its pools). Queued after the build instead (beside the walk alone) the 1M-particle impact step
-    // measured 4 % slower; a pair loop on a persistent grid of 3 or 4 blocks per SM, leaving room for the build,
-    // measured 1-7 % slower.
+    // The material update and the neighbour grid are queued before the tree build and run beside it; the pair loop
+    // is queued once the build has returned to the host (it reads the level counts once at its end), so that it
+    // runs beside the walk. The build is a chain of short dependent launches that the pair loop's blocks would
+    // hold off the SMs. Measured on the 1.08M impact (ms per step): pair loop queued after the build 8.97, before
+    // the build 9.50, after the walk's list phase (beside its evaluation alone) 9.36.
     evalSphPrepare(h);
-    evalSphPairs(h, false);
     sphgpu_status st = evalGravityBuild(h, h->gstream);
     if (st != SPHGPU_OK) {
         return st;
     }
+    evalSphPairs(h, false);
     st = evalGravityWalk(h, h->gstream);
     if (st != SPHGPU_OK) {
         return st;

@@ -43,15 +43,21 @@ struct MaterialD {
 };
 
 // Uniform grid of the neighbour search (computed on the device each step)
+// A fine grid (the mixed SPH step) has cells of about h_max: the pairs of a particle lie within span = 2 cells in each
+// direction, and the mixed path's FP32 positions are relative to the origin of the coarse cell of 2 x 2 x 2 fine
+// cells (fine coordinate >> shift). Otherwise the cells are at least 2 h_max, span = 1 and shift = 0.
 struct GridInfo {
     double lo[3];      // grid origin
-    double cell;       // cell edge (>= kernel radius * max h)
+    double cell;       // cell edge
     double inv_cell;
     double hmax;
     int dims[3];
     uint32_t ncells;
     float lo_f[3];     // FP32 copy of the origin (mixed path)
     float pad;
+    double ccell;      // coarse cell edge, cell << shift (origin of the mixed path's relative positions)
+    int span;          // cells of the pair stencil on each side
+    int shift;         // coarse coordinate = cell coordinate >> shift
 };
 
 struct Vec3 {

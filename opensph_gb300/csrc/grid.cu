@@ -10,6 +10,8 @@
 
 #include <cub/device/device_radix_sort.cuh>
 
+#include <algorithm>
+
 #include "state.h"
 
 namespace sphgpu {
@@ -67,8 +69,9 @@ __global__ void boundsKernel(const dbl4* __restrict__ r, const double* __restric
 }
 
 // meanCell: cell edge 2 max(mean radius, max radius / 8) (the collision search scans the cells of each
-// particle's own search box), else 2 max radius (the 27-cell stencil of the SPH pair loops)
-__global__ void gridSetupKernel(const unsigned long long* b, uint32_t capacity, uint32_t n, int meanCell,
+// particle's own search box); fine: cell edge h_max (the 5 x 5 x 5 stencil of the mixed pair loop, coarse cells of
+// 2 x 2 x 2 fine cells); else 2 h_max (the 27-cell stencil of the SPH pair loops)
+__global__ void gridSetupKernel(const unsigned long long* b, uint32_t capacity, uint32_t n, int meanCell, int fine,
     GridInfo* g) {
     if (threadIdx.x != 0 || blockIdx.x != 0) {
         return;
@@ -82,7 +85,8 @@ __global__ void gridSetupKernel(const unsigned long long* b, uint32_t capacity, 
     const double hmax = n ? doubleUnflip(b[6]) : 0.;
     // cell edge: kernel support 2 h_max, widened by 1e-4 so that rounding in the cell index can never
     // separate two interacting particles by more than one cell
-    double cell = 2. * hmax * 1.0001;
+    const double support = 2. * hmax * 1.0001;
+    double cell = fine ? 0.5 * support : support;
     if (meanCell && n) {
         const double mean = __longlong_as_double(static_cast<long long>(b[7])) / double(n);
         cell = 2. * fmax(mean, 0.125 * hmax) * 1.0001;
@@ -112,6 +116,11 @@ __global__ void gridSetupKernel(const unsigned long long* b, uint32_t capacity, 
     g->cell = cell;
     g->inv_cell = 1. / cell;
     g->hmax = hmax;
+    // a fine grid that had to be coarsened to fit the cell capacity to 2 h_max or more is an ordinary grid
+    const bool isFine = fine && !meanCell && cell < support;
+    g->span = isFine ? 2 : 1;
+    g->shift = isFine ? 1 : 0;
+    g->ccell = isFine ? 2. * cell : cell;
     g->ncells = uint32_t(dims[0]) * uint32_t(dims[1]) * uint32_t(dims[2]);
 }
 
@@ -157,6 +166,25 @@ __global__ void cellRanges(const uint32_t* __restrict__ keys, uint32_t n, uint32
     }
 }
 
+// first[c] = the first sorted position whose cell key is at least c, for c = 0 .. ncells (first[ncells] = n): the
+// particles of the consecutive cells c0 .. c1 are the positions first[c0] .. first[c1 + 1]
+__global__ void cellFirstKernel(const uint32_t* __restrict__ keys, uint32_t n, const GridInfo* __restrict__ g,
+    uint32_t capacity, uint32_t* first) {
+    const uint32_t nc = min(g->ncells, capacity);
+    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c <= nc; c += gridDim.x * blockDim.x) {
+        uint32_t lo = 0, hi = n;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (keys[mid] < c) {
+                lo = mid + 1;
+            } else {
+                hi = mid;
+            }
+        }
+        first[c] = lo;
+    }
+}
+
 __global__ void gatherSorted(DState st, const uint32_t* __restrict__ perm, dbl4* rs, dbl4* vs, double* ms,
     double* rhos, double* ps, double* css, double* Ss, double* reduces, uint32_t* flags, int solid) {
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -196,12 +224,15 @@ __global__ void gatherSortedMixed(DState st, const uint32_t* __restrict__ perm, 
     const uint32_t i = perm[s];
     const uint32_t key = keys[s];
     const uint32_t dx = uint32_t(g->dims[0]), dy = uint32_t(g->dims[1]);
-    const double cx = double(key % dx), cy = double((key / dx) % dy), cz = double(key / (dx * dy));
+    const int sh = g->shift;
+    // the origin of the particle's coarse cell
+    const double cx = double((key % dx) >> sh), cy = double(((key / dx) % dy) >> sh),
+                 cz = double((key / (dx * dy)) >> sh);
     const dbl4 p = st.r[i];
     const dbl4 v = st.v[i];
     const double rho = st.rho[i];
-    mx0[s] = make_float4(float(p.x - (g->lo[0] + cx * g->cell)), float(p.y - (g->lo[1] + cy * g->cell)),
-        float(p.z - (g->lo[2] + cz * g->cell)), float(p.w));
+    mx0[s] = make_float4(float(p.x - (g->lo[0] + cx * g->ccell)), float(p.y - (g->lo[1] + cy * g->ccell)),
+        float(p.z - (g->lo[2] + cz * g->ccell)), float(p.w));
     float hx, lx, hy, ly, hz, lz;
     splitFloat(v.x, hx, lx);
     splitFloat(v.y, hy, ly);
@@ -321,6 +352,7 @@ cudaError_t gridAllocate(Grid& g, uint32_t n, bool solid, bool correction, bool 
         alloc((void**)&g.nb_count, nn * sizeof(uint32_t));
         alloc((void**)&g.nb_over, nn * sizeof(uint32_t));
         alloc((void**)&g.nb_over_count, sizeof(uint32_t));
+        alloc((void**)&g.cell_first, (size_t(g.cell_capacity) + 1) * sizeof(uint32_t));
     }
     if (e != cudaSuccess) {
         return e;
@@ -337,7 +369,7 @@ cudaError_t gridAllocate(Grid& g, uint32_t n, bool solid, bool correction, bool 
 void gridFree(Grid& g) {
     void* ptrs[] = { g.info, g.bounds, g.keys, g.keys_sorted, g.perm_in, g.perm, g.cell_start, g.cell_end,
         g.sort_temp, g.rs, g.vs, g.ms, g.rhos, g.ps, g.css, g.Ss, g.reduces, g.flags, g.mx0, g.mx1, g.mx2, g.mx3,
-        g.mxS, g.mxC, g.nb, g.nb_count, g.nb_over, g.nb_over_count };
+        g.mxS, g.mxC, g.nb, g.nb_count, g.nb_over, g.nb_over_count, g.cell_first };
     for (void* p : ptrs) {
         if (p) {
             cudaFree(p);
@@ -346,12 +378,12 @@ void gridFree(Grid& g) {
     g = Grid();
 }
 
-void launchGridBuild(const DState& s, Grid& g, const Physics& ph, cudaStream_t st) {
+void launchGridBuild(const DState& s, Grid& g, const Physics& ph, cudaStream_t st, bool fine) {
     (void)ph;
-    launchGridBuildRadius(s.r, nullptr, s.n, g, st);
+    launchGridBuildRadius(s.r, nullptr, s.n, g, st, fine && g.cell_first != nullptr);
 }
 
-void launchGridBuildRadius(const dbl4* r, const double* radius, uint32_t n, Grid& g, cudaStream_t st) {
+void launchGridBuildRadius(const dbl4* r, const double* radius, uint32_t n, Grid& g, cudaStream_t st, bool fine) {
     const int meanCell = radius ? 1 : 0;
     g.launches = n > 0 ? 6 : 2;
     resetBounds<<<1, 32, 0, st>>>(g.bounds);
@@ -359,7 +391,7 @@ void launchGridBuildRadius(const dbl4* r, const double* radius, uint32_t n, Grid
         const int blocks = min(ceilDiv(n, 256), 152 * 8);
         boundsKernel<<<blocks, 256, 0, st>>>(r, radius, n, g.bounds);
     }
-    gridSetupKernel<<<1, 1, 0, st>>>(g.bounds, g.cell_capacity, n, meanCell, g.info);
+    gridSetupKernel<<<1, 1, 0, st>>>(g.bounds, g.cell_capacity, n, meanCell, fine ? 1 : 0, g.info);
     if (n == 0) {
         return;
     }
@@ -373,6 +405,11 @@ void launchGridBuildRadius(const dbl4* r, const double* radius, uint32_t n, Grid
         st);
     clearCells<<<152 * 4, 256, 0, st>>>(g.cell_start, g.cell_end, g.info);
     cellRanges<<<ceilDiv(n, 256), 256, 0, st>>>(g.keys_sorted, n, g.cell_start, g.cell_end);
+    if (fine) {
+        cellFirstKernel<<<std::min(ceilDiv(g.cell_capacity + 1, 256), 152 * 16), 256, 0, st>>>(g.keys_sorted, n,
+            g.info, g.cell_capacity, g.cell_first);
+        g.launches += 1;
+    }
 }
 
 void launchGatherSorted(const DState& s, Grid& g, const Physics& ph, cudaStream_t st) {

@@ -41,6 +41,57 @@ __device__ __forceinline__ float lutGradF(const float* __restrict__ lut, float q
     return g0 + (g1 - g0) * ratio;
 }
 
+// The pair loop runs in three kernels. neighboursMixedKernel tests the candidates of the 27 cells (one float4 load
+// and a distance test each) and writes the interacting ones, in cell order, to a per-particle neighbour list
+// (sorted index | cell offset << 27, laid out [slot][particle] so that a warp's writes and reads of one slot are
+// contiguous); it holds few registers and runs at full occupancy. pairSumMixedKernel then evaluates the pair terms
+// from the lists and finalizes the particle. A particle with more than NB_CAP neighbours is left to
+// pairSumMixedOverflowKernel, which scans its cells again (rare: a queue of such particles is filled by the first
+// kernel). Each particle visits its neighbours in cell order, so the sums are those of a direct loop over the cells.
+constexpr int PAIR_THREADS = 128;
+constexpr uint32_t NB_INDEX_BITS = 27;
+constexpr uint32_t NB_INDEX_MASK = (1u << NB_INDEX_BITS) - 1u;
+
+// the cells of a particle's pair stencil (span cells on each side) in key order (x fastest, then y, then z),
+// calling f(t, off) for every candidate t != si, off = the coarse-cell offset (ox + 1) + 3 (oy + 1) + 9 (oz + 1)
+// of t's cell against si's
+template <typename F>
+__device__ __forceinline__ void forEachCandidate(const Grid& g, uint32_t si, F&& f) {
+    const GridInfo* gi = g.info;
+    const int dxc = gi->dims[0], dyc = gi->dims[1], dzc = gi->dims[2];
+    const int span = gi->span, shift = gi->shift;
+    const uint32_t key = g.keys_sorted[si];
+    const int cx = int(key % uint32_t(dxc)), cy = int((key / uint32_t(dxc)) % uint32_t(dyc)),
+              cz = int(key / (uint32_t(dxc) * uint32_t(dyc)));
+    for (int z = max(cz - span, 0); z <= min(cz + span, dzc - 1); ++z) {
+        const int oz = (z >> shift) - (cz >> shift);
+        for (int y = max(cy - span, 0); y <= min(cy + span, dyc - 1); ++y) {
+            const int oy = (y >> shift) - (cy >> shift);
+            for (int x = max(cx - span, 0); x <= min(cx + span, dxc - 1); ++x) {
+                const int ox = (x >> shift) - (cx >> shift);
+                const int off = (ox + 1) + 3 * (oy + 1) + 9 * (oz + 1);
+                const uint32_t c = (uint32_t(z) * uint32_t(dyc) + uint32_t(y)) * uint32_t(dxc) + uint32_t(x);
+                const uint32_t te = g.cell_end[c];
+                for (uint32_t t = g.cell_start[c]; t < te; ++t) {
+                    if (t != si) {
+                        f(t, off);
+                    }
+                }
+            }
+        }
+    }
+}
+
+// the pair test of candidate t in cell offset off against particle i (pi0: cell-relative position and h)
+__device__ __forceinline__ bool interactsMixed(const Grid& g, const float4& pi0, float cellf, uint32_t t, int off) {
+    const float sx = float(off % 3 - 1) * cellf, sy = float((off / 3) % 3 - 1) * cellf, sz = float(off / 9 - 1) * cellf;
+    const float4 pj0 = g.mx0[t];
+    const float drx = (pi0.x - pj0.x) - sx, dry = (pi0.y - pj0.y) - sy, drz = (pi0.z - pj0.z) - sz;
+    const float d2 = drx * drx + dry * dry + drz * drz;
+    const float rad = 2.f * (0.5f * (pi0.w + pj0.w));
+    return d2 < rad * rad;
+}
+
 // CorrectionTensor::evalNeighs (core/sph/equations/Derivative.cpp:36-74) in mixed precision: the sum of
 // m_j / rho_j sym((r_j - r_i) x grad W_ij) in FP32 with compensation, its determinant and inverse in FP64; the
 // result is written in FP64 (particle order, the quantity) and FP32 (cell order, for the pair loop).
@@ -53,52 +104,37 @@ __global__ void __launch_bounds__(128) correctionMixedKernel(DState s, Grid g, P
     }
     const GridInfo* gi = g.info;
     const float4 pi0 = g.mx0[si], pi3 = g.mx3[si];
-    const float cellf = float(gi->cell);
+    const float cellf = float(gi->ccell);
     Kahan c[6];
-    const int dxc = gi->dims[0], dyc = gi->dims[1], dzc = gi->dims[2];
-    const uint32_t key = g.keys_sorted[si];
-    const int cx = int(key % uint32_t(dxc)), cy = int((key / uint32_t(dxc)) % uint32_t(dyc)),
-              cz = int(key / (uint32_t(dxc) * uint32_t(dyc)));
-    for (int off = 0; off < 27; ++off) {
-        const int ox = off % 3 - 1, oy = (off / 3) % 3 - 1, oz = off / 9 - 1;
-        const int x = cx + ox, y = cy + oy, z = cz + oz;
-        if (x < 0 || x >= dxc || y < 0 || y >= dyc || z < 0 || z >= dzc) {
-            continue;
+    forEachCandidate(g, si, [&](uint32_t t, int off) {
+        const float sx = float(off % 3 - 1) * cellf, sy = float((off / 3) % 3 - 1) * cellf,
+                    sz = float(off / 9 - 1) * cellf;
+        const float4 pj0 = g.mx0[t];
+        const float drx = (pi0.x - pj0.x) - sx, dry = (pi0.y - pj0.y) - sy, drz = (pi0.z - pj0.z) - sz;
+        const float d2 = drx * drx + dry * dry + drz * drz;
+        const float hbar = 0.5f * (pi0.w + pj0.w);
+        const float rad = 2.f * hbar;
+        if (!(d2 < rad * rad)) {
+            return;
         }
-        const uint32_t cell = (uint32_t(z) * uint32_t(dyc) + uint32_t(y)) * uint32_t(dxc) + uint32_t(x);
-        const uint32_t te = g.cell_end[cell];
-        const float sx = float(ox) * cellf, sy = float(oy) * cellf, sz = float(oz) * cellf;
-        for (uint32_t t = g.cell_start[cell]; t < te; ++t) {
-            if (t == si) {
-                continue;
-            }
-            const float4 pj0 = g.mx0[t];
-            const float drx = (pi0.x - pj0.x) - sx, dry = (pi0.y - pj0.y) - sy, drz = (pi0.z - pj0.z) - sz;
-            const float d2 = drx * drx + dry * dry + drz * drz;
-            const float hbar = 0.5f * (pi0.w + pj0.w);
-            const float rad = 2.f * hbar;
-            if (!(d2 < rad * rad)) {
-                continue;
-            }
-            const float4 pj3 = g.mx3[t];
-            if (ph.sum_only_undamaged &&
-                !(__float_as_uint(pi3.w) == __float_as_uint(pj3.w) && pi3.z != 0.f && pj3.z != 0.f)) {
-                continue;
-            }
-            const float4 pj1 = g.mx1[t], pj2 = g.mx2[t];
-            const float hInv = 1.f / hbar;
-            const float h2 = hInv * hInv;
-            const float gl = lutGradF(lut, d2 * h2) * (h2 * h2 * hInv);
-            const float gx = drx * gl, gy = dry * gl, gz = drz * gl;
-            const float f = pj1.w / pj2.w;
-            c[0].add(f * (-drx * gx));
-            c[1].add(f * (-dry * gy));
-            c[2].add(f * (-drz * gz));
-            c[3].add(f * (-0.5f * (drx * gy + dry * gx)));
-            c[4].add(f * (-0.5f * (drx * gz + drz * gx)));
-            c[5].add(f * (-0.5f * (dry * gz + drz * gy)));
+        const float4 pj3 = g.mx3[t];
+        if (ph.sum_only_undamaged &&
+            !(__float_as_uint(pi3.w) == __float_as_uint(pj3.w) && pi3.z != 0.f && pj3.z != 0.f)) {
+            return;
         }
-    }
+        const float4 pj1 = g.mx1[t], pj2 = g.mx2[t];
+        const float hInv = 1.f / hbar;
+        const float h2 = hInv * hInv;
+        const float gl = lutGradF(lut, d2 * h2) * (h2 * h2 * hInv);
+        const float gx = drx * gl, gy = dry * gl, gz = drz * gl;
+        const float f = pj1.w / pj2.w;
+        c[0].add(f * (-drx * gx));
+        c[1].add(f * (-dry * gy));
+        c[2].add(f * (-drz * gz));
+        c[3].add(f * (-0.5f * (drx * gy + dry * gx)));
+        c[4].add(f * (-0.5f * (drx * gz + drz * gx)));
+        c[5].add(f * (-0.5f * (dry * gz + drz * gy)));
+    });
     double cd[6];
     for (int k = 0; k < 6; ++k) {
         cd[k] = c[k].value();
@@ -122,65 +158,12 @@ __global__ void __launch_bounds__(128) correctionMixedKernel(DState s, Grid g, P
     }
 }
 
-// The pair loop runs in three kernels. neighboursMixedKernel tests the candidates of the 27 cells (one float4 load
-// and a distance test each) and writes the interacting ones, in cell order, to a per-particle neighbour list
-// (sorted index | cell offset << 27, laid out [slot][particle] so that a warp's writes and reads of one slot are
-// contiguous); it holds few registers and runs at full occupancy. pairSumMixedKernel then evaluates the pair terms
-// from the lists and finalizes the particle. A particle with more than NB_CAP neighbours is left to
-// pairSumMixedOverflowKernel, which scans its cells again (rare: a queue of such particles is filled by the first
-// kernel). Each particle visits its neighbours in cell order, so the sums are those of a direct loop over the cells.
-constexpr int PAIR_THREADS = 128;
-constexpr uint32_t NB_INDEX_BITS = 27;
-constexpr uint32_t NB_INDEX_MASK = (1u << NB_INDEX_BITS) - 1u;
-
-// the 27 neighbour cells of a particle in cell order, calling f(t, off) for every candidate t != si of cell off
-// (the next cell's range is loaded while the current cell's candidates are visited)
-template <typename F>
-__device__ __forceinline__ void forEachCandidate(const Grid& g, uint32_t si, F&& f) {
-    const GridInfo* gi = g.info;
-    const int dxc = gi->dims[0], dyc = gi->dims[1], dzc = gi->dims[2];
-    const uint32_t key = g.keys_sorted[si];
-    const int cx = int(key % uint32_t(dxc)), cy = int((key / uint32_t(dxc)) % uint32_t(dyc)),
-              cz = int(key / (uint32_t(dxc) * uint32_t(dyc)));
-    auto cellRange = [&](int off, uint32_t& tb, uint32_t& te) {
-        const int x = cx + off % 3 - 1, y = cy + (off / 3) % 3 - 1, z = cz + off / 9 - 1;
-        tb = 0;
-        te = 0;
-        if (x >= 0 && x < dxc && y >= 0 && y < dyc && z >= 0 && z < dzc) {
-            const uint32_t c = (uint32_t(z) * uint32_t(dyc) + uint32_t(y)) * uint32_t(dxc) + uint32_t(x);
-            tb = g.cell_start[c];
-            te = g.cell_end[c];
-        }
-    };
-    uint32_t nextB, nextE;
-    cellRange(0, nextB, nextE);
-    for (int off = 0; off < 27; ++off) {
-        const uint32_t tb = nextB, te = nextE;
-        if (off + 1 < 27) {
-            cellRange(off + 1, nextB, nextE);
-        }
-        for (uint32_t t = tb; t < te; ++t) {
-            if (t != si) {
-                f(t, off);
-            }
-        }
-    }
-}
-
-// the pair test of candidate t in cell offset off against particle i (pi0: cell-relative position and h)
-__device__ __forceinline__ bool interactsMixed(const Grid& g, const float4& pi0, float cellf, uint32_t t, int off) {
-    const float sx = float(off % 3 - 1) * cellf, sy = float((off / 3) % 3 - 1) * cellf, sz = float(off / 9 - 1) * cellf;
-    const float4 pj0 = g.mx0[t];
-    const float drx = (pi0.x - pj0.x) - sx, dry = (pi0.y - pj0.y) - sy, drz = (pi0.z - pj0.z) - sz;
-    const float d2 = drx * drx + dry * dry + drz * drz;
-    const float rad = 2.f * (0.5f * (pi0.w + pj0.w));
-    return d2 < rad * rad;
-}
-
-// The candidates are visited as 9 rows of 3 cells: a row's cells have consecutive keys, so their particles form one
-// contiguous range, and a candidate's x offset follows from its position against the row's two inner cell
-// boundaries. Candidates are loaded four at a time ahead of their tests. The neighbours come out in the cell
-// order of the 27-cell stencil (x fastest, then y, then z).
+// The candidates are visited row by row: a row's cells have consecutive keys, so the particles of any run of
+// them are one contiguous range (first[] of the fine grid), and a candidate's coarse x offset follows from its
+// position against the first positions of the coarse cell's fine cells. Rows and cells farther from the particle
+// than h_i + h_max (with a 1e-4 margin over the FP32 rounding) are skipped: on the fine grid of h_max cells this
+// leaves about a third of the candidates of the 27 coarse cells. Candidates are loaded four at a time ahead of
+// their tests. The neighbours come out in key order (x fastest, then y, then z), the order of forEachCandidate.
 __global__ void __launch_bounds__(PAIR_THREADS) neighboursMixedKernel(Grid g, uint32_t n) {
     const uint32_t si = blockIdx.x * blockDim.x + threadIdx.x;
     if (si >= n) {
@@ -188,58 +171,76 @@ __global__ void __launch_bounds__(PAIR_THREADS) neighboursMixedKernel(Grid g, ui
     }
     const GridInfo* gi = g.info;
     const float4 pi0 = g.mx0[si];
-    const float cellf = float(gi->cell);
+    const float cellf = float(gi->cell), ccellf = float(gi->ccell);
     const int dxc = gi->dims[0], dyc = gi->dims[1], dzc = gi->dims[2];
+    const int span = gi->span, shift = gi->shift;
     const uint32_t key = g.keys_sorted[si];
     const int cx = int(key % uint32_t(dxc)), cy = int((key / uint32_t(dxc)) % uint32_t(dyc)),
               cz = int(key / (uint32_t(dxc) * uint32_t(dyc)));
+    const int ccx = cx >> shift, ccy = cy >> shift, ccz = cz >> shift;
+    // the particle's position in its own cell
+    const float fx = pi0.x - float(cx - (ccx << shift)) * cellf;
+    const float fy = pi0.y - float(cy - (ccy << shift)) * cellf;
+    const float fz = pi0.z - float(cz - (ccz << shift)) * cellf;
+    const float reach = (pi0.w + float(gi->hmax)) * 1.0001f;
+    const float reach2 = reach * reach;
+    // distance from the particle to the slab of the cell at offset d along one axis
+    auto gap = [&](int d, float f) {
+        return d > 0 ? float(d) * cellf - f : (d < 0 ? f - float(d + 1) * cellf : 0.f);
+    };
     uint32_t c = 0;
-    for (int row = 0; row < 9; ++row) {
-        const int oy = row % 3 - 1, oz = row / 3 - 1;
-        const int y = cy + oy, z = cz + oz;
-        if (y < 0 || y >= dyc || z < 0 || z >= dzc) {
+    for (int dz = -span; dz <= span; ++dz) {
+        const int z = cz + dz;
+        const float gz = gap(dz, fz);
+        if (z < 0 || z >= dzc || gz > reach) {
             continue;
         }
-        const uint32_t rowBase = (uint32_t(z) * uint32_t(dyc) + uint32_t(y)) * uint32_t(dxc);
-        uint32_t cs[3], ce[3];
-        for (int k = 0; k < 3; ++k) {
-            const int x = cx + k - 1;
-            const bool in = x >= 0 && x < dxc;
-            cs[k] = in ? g.cell_start[rowBase + uint32_t(x)] : 0u;
-            ce[k] = in ? g.cell_end[rowBase + uint32_t(x)] : 0u;
-        }
-        // the row's range and the first positions of its middle and right cells (empty cells: start = end = 0)
-        const bool ne0 = ce[0] > cs[0], ne1 = ce[1] > cs[1], ne2 = ce[2] > cs[2];
-        const uint32_t lo = ne0 ? cs[0] : (ne1 ? cs[1] : (ne2 ? cs[2] : 0u));
-        const uint32_t hi = ne2 ? ce[2] : (ne1 ? ce[1] : (ne0 ? ce[0] : 0u));
-        const uint32_t b1 = ne0 ? ce[0] : lo;
-        const uint32_t b2 = ne1 ? ce[1] : b1;
-        const float sy = float(oy) * cellf, sz = float(oz) * cellf;
-        const uint32_t offYZ = uint32_t(3 * (oy + 1) + 9 * (oz + 1));
-        // (the separation and the radius 2 h_bar = h_i + h_j, rounded as in the pair terms)
-        auto test = [&](const float4& pj0, uint32_t t) {
-            const float sx = t < b1 ? -cellf : (t < b2 ? 0.f : cellf);
-            const float drx = (pi0.x - pj0.x) - sx, dry = (pi0.y - pj0.y) - sy, drz = (pi0.z - pj0.z) - sz;
-            const float d2 = drx * drx + dry * dry + drz * drz;
-            const float rad = pi0.w + pj0.w;
-            if (d2 < rad * rad && t != si) {
-                if (c < uint32_t(NB_CAP)) {
-                    const uint32_t off = offYZ + uint32_t(t >= b1) + uint32_t(t >= b2);
-                    g.nb[size_t(c) * n + si] = t | (off << NB_INDEX_BITS);
-                }
-                ++c;
+        const int ocz = (z >> shift) - ccz;
+        for (int dy = -span; dy <= span; ++dy) {
+            const int y = cy + dy;
+            const float gy = gap(dy, fy);
+            const float gyz = gy * gy + gz * gz;
+            if (y < 0 || y >= dyc || gyz > reach2) {
+                continue;
             }
-        };
-        uint32_t t = lo;
-        for (; t + 4 <= hi; t += 4) {
-            const float4 q0 = g.mx0[t], q1 = g.mx0[t + 1], q2 = g.mx0[t + 2], q3 = g.mx0[t + 3];
-            test(q0, t);
-            test(q1, t + 1);
-            test(q2, t + 2);
-            test(q3, t + 3);
-        }
-        for (; t < hi; ++t) {
-            test(g.mx0[t], t);
+            // the cells of the row within reach
+            const float xr = sqrtf(reach2 - gyz);
+            const int left = xr >= fx ? min(span, int((xr - fx) / cellf) + 1) : 0;
+            const int right = min(span, int((xr + fx) / cellf));
+            const int xlo = max(cx - left, 0), xhi = min(cx + right, dxc - 1);
+            const uint32_t rowBase = (uint32_t(z) * uint32_t(dyc) + uint32_t(y)) * uint32_t(dxc);
+            const uint32_t lo = g.cell_first[rowBase + uint32_t(xlo)], hi = g.cell_first[rowBase + uint32_t(xhi) + 1];
+            // positions below b1 are in the coarse cell to the left, from b2 in the one to the right
+            const int cb0 = min(max(ccx << shift, xlo), xhi + 1), cb1 = min(max((ccx + 1) << shift, xlo), xhi + 1);
+            const uint32_t b1 = g.cell_first[rowBase + uint32_t(cb0)], b2 = g.cell_first[rowBase + uint32_t(cb1)];
+            const int ocy = (y >> shift) - ccy;
+            const float sy = float(ocy) * ccellf, sz = float(ocz) * ccellf;
+            const uint32_t offYZ = uint32_t(3 * (ocy + 1) + 9 * (ocz + 1));
+            // (the separation and the radius 2 h_bar = h_i + h_j, rounded as in the pair terms)
+            auto test = [&](const float4& pj0, uint32_t t) {
+                const float sx = t < b1 ? -ccellf : (t < b2 ? 0.f : ccellf);
+                const float drx = (pi0.x - pj0.x) - sx, dry = (pi0.y - pj0.y) - sy, drz = (pi0.z - pj0.z) - sz;
+                const float d2 = drx * drx + dry * dry + drz * drz;
+                const float rad = pi0.w + pj0.w;
+                if (d2 < rad * rad && t != si) {
+                    if (c < uint32_t(NB_CAP)) {
+                        const uint32_t off = offYZ + uint32_t(t >= b1) + uint32_t(t >= b2);
+                        g.nb[size_t(c) * n + si] = t | (off << NB_INDEX_BITS);
+                    }
+                    ++c;
+                }
+            };
+            uint32_t t = lo;
+            for (; t + 4 <= hi; t += 4) {
+                const float4 q0 = g.mx0[t], q1 = g.mx0[t + 1], q2 = g.mx0[t + 2], q3 = g.mx0[t + 3];
+                test(q0, t);
+                test(q1, t + 1);
+                test(q2, t + 2);
+                test(q3, t + 3);
+            }
+            for (; t < hi; ++t) {
+                test(g.mx0[t], t);
+            }
         }
     }
     g.nb_count[si] = c;
@@ -388,7 +389,7 @@ __global__ void __launch_bounds__(PAIR_THREADS, 6) pairSumMixedKernel(DState s, 
     if (total > uint32_t(NB_CAP)) {
         return; // pairSumMixedOverflowKernel
     }
-    const float cellf = float(g.info->cell);
+    const float cellf = float(g.info->ccell);
     MixedSelf me;
     loadSelfMixed<Solid>(g, ph, n, si, me);
     MixedSums a;
@@ -404,7 +405,7 @@ __global__ void __launch_bounds__(PAIR_THREADS) pairSumMixedOverflowKernel(DStat
     const MaterialD* __restrict__ mats, const float* __restrict__ lut) {
     const uint32_t n = s.n;
     const uint32_t count = min(*g.nb_over_count, n);
-    const float cellf = float(g.info->cell);
+    const float cellf = float(g.info->ccell);
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
         const uint32_t si = g.nb_over[k];
         MixedSelf me;

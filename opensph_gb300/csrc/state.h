@@ -182,6 +182,7 @@ struct Grid {
     uint32_t* nb_count = nullptr;
     uint32_t* nb_over = nullptr;       // particles (sorted positions) with more than NB_CAP neighbours
     uint32_t* nb_over_count = nullptr; // device: their number
+    uint32_t* cell_first = nullptr;    // fine grids: first sorted position of each cell key (cell_capacity + 1)
     uint32_t launches = 0;     // own kernels launched by the last build / gather (library sort excluded)
 };
 
@@ -315,7 +316,8 @@ struct Tree {
 };
 
 // ---- launchers (grid.cu) ----
-void launchGridBuild(const DState& s, Grid& g, const Physics& ph, cudaStream_t st);
+// fine: cells of h_max for the mixed pair loop (needs the grid's cell_first array)
+void launchGridBuild(const DState& s, Grid& g, const Physics& ph, cudaStream_t st, bool fine = false);
 void launchGatherSorted(const DState& s, Grid& g, const Physics& ph, cudaStream_t st);
 // copies: the cell-sorted copies of the SPH pair loops (not needed by the collision search)
 cudaError_t gridAllocate(Grid& g, uint32_t n, bool solid, bool correction = false, bool copies = true,
@@ -333,7 +335,8 @@ void launchListPairs(const DState& s, const Grid& g, uint32_t* pi, uint32_t* pj,
 
 // grid over the positions r: radius NULL -> cell edge >= 2 max h (27-cell stencil of the pair loops); else the
 // collision grid, cell edge 2 max(mean radius, max radius / 8), searched over each particle's own cell box
-void launchGridBuildRadius(const dbl4* r, const double* radius, uint32_t n, Grid& g, cudaStream_t st);
+void launchGridBuildRadius(const dbl4* r, const double* radius, uint32_t n, Grid& g, cudaStream_t st,
+    bool fine = false);
 
 // ---- launchers (sph64.cu) ----
 void launchMaterialsInit(const DState& s, const Physics& ph, const MaterialD* mats, cudaStream_t st);

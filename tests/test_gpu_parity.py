@@ -330,6 +330,41 @@ def test_mixed_neighbour_list_overflow(name):
             assert cases.scale_err(got[f], ref[f]) < 1e-5, f
 
 
+def _gas_lattice(shape, spacing, h, offset=(0.0, 0.0, 0.0), seed=0):
+    rng = np.random.default_rng(seed)
+    idx = np.stack(np.meshgrid(*[np.arange(k) for k in shape], indexing="ij"), -1).reshape(-1, 3)
+    pos = idx * spacing + np.asarray(offset) + 0.05 * spacing * rng.standard_normal(idx.shape)
+    return np.concatenate([pos, np.full((len(pos), 1), h)], axis=1)
+
+
+@pytest.mark.parametrize("layout", ["enlarged_fine_cells", "coarse_cells"])
+def test_mixed_pair_loop_on_coarsened_grids(layout):
+    # the mixed pair loop searches cells of h_max; when those would exceed the grid's cell capacity the cells are
+    # enlarged, to between h_max and 2 h_max (the stencil of 5 x 5 x 5 cells stays) or to 2 h_max and more (a
+    # stencil of 3 x 3 x 3 cells): the mixed derivatives within their bound of the FP64 path's, the same neighbours
+    if layout == "enlarged_fine_cells":
+        r = _gas_lattice((10, 10, 10), 1.0, 0.55)
+    else:
+        r = np.concatenate([_gas_lattice((8, 8, 8), 1.0, 0.8), _gas_lattice((8, 8, 8), 1.0, 0.8, (1000.0, 0.0, 0.0))])
+    n = len(r)
+    rng = np.random.default_rng(3)
+    st = {"r": r.ravel(), "v": np.concatenate([rng.standard_normal((n, 3)), np.zeros((n, 1))], 1).ravel(),
+          "dv": np.zeros(4 * n), "m": np.ones(n), "rho": 1.0 + 0.1 * rng.random(n), "drho": np.zeros(n),
+          "u": 1.0 + rng.random(n), "du": np.zeros(n), "flag": np.zeros(n, "u4"), "mat": np.zeros(n, "u4")}
+    out = {}
+    for prec in (abi.PRECISION_FP64, abi.PRECISION_MIXED):
+        cfg, keep = abi.make_config(n, [abi.ideal_gas()], forces=abi.FORCE_PRESSURE, precision=prec)
+        with GpuSolver(cfg, keep) as g:
+            g.set_state({k: v.copy() for k, v in st.items()})
+            g.integrate()
+            out[prec] = g.get_state(["dv", "drho", "du", "ncnt"])
+    ref, got = out[abi.PRECISION_FP64], out[abi.PRECISION_MIXED]
+    assert ref["ncnt"].min() > 0
+    np.testing.assert_array_equal(got["ncnt"], ref["ncnt"])
+    for f in ["dv", "drho", "du"]:
+        assert cases.scale_err(got[f], ref[f]) < 1e-5, f
+
+
 @pytest.mark.parametrize("name", ["sphere_n1000", "impact_n1200", "gas_n1500", "impact_asym_n1200"])
 def test_mixed_steps_error_bound(name):
     fx = cases.load(name)

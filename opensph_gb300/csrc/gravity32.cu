@@ -105,7 +105,7 @@ __device__ __forceinline__ void gravAccF(float rx, float ry, float rz, float h, 
         const float inv = rsqrtf(d2);
         g = inv * inv * inv;
     } else {
-        const float hInv = __frcp_rn(h);
+        const float hInv = __fdividef(1.f, h); // (the fast reciprocal: 2 ulp, far below the interpolation error)
         const float hInv2 = hInv * hInv;
         const float floatIdx = float(LUT_ENTRIES / 4) * (d2 * hInv2);
         const int idx1 = min(int(floatIdx), LUT_ENTRIES - 1);

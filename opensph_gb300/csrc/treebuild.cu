@@ -27,8 +27,8 @@
 //      end at once.
 //   2. every other segment (the children of at most SUBTREE_MAX elements, and whatever phase 1 left over) is
 //      split down to its leaves by one warp, depth first, on a copy of its idx and keys in shared memory.
-// A counting sort by level then lists the nodes level by level for the mixed walk; the moments are formed
-// bottom-up (gravity.cu) before one copy to the host returns the node, leaf and level counts.
+// A counting sort by level then lists the nodes level by level for the walks; one copy to the host returns the
+// node, leaf and level counts, and the moments are formed bottom-up (gravity.cu) after it, while the host goes on.
 
 #include <algorithm>
 #include <cfloat>
@@ -1358,12 +1358,8 @@ cudaError_t treeBuild(const DState& s, Tree& t, const Physics& ph, uint32_t* dev
     levelScatterKernel<<<gridNodes, 256, 0, st>>>(t.geom, t.counters, t.node_capacity, t.level_first_dev,
         t.level_cursor, t.level_nodes);
     launched(5);
-    // moments, bottom-up, and the walks' FP32 node records, sized on the device
-    t.mixed_moments = ph.precision == SPHGPU_PRECISION_MIXED;
-    launchMomentsDev(s, t, ph, t.mixed_moments, st);
-    launchPrepareWalkDev(s, t, ph, st);
-    launched(3);
-    // the counts to the host: the walk launches its level passes from them
+    // the counts to the host (the walk launches its level passes from them), before the moments: the host returns
+    // while the moments are formed, so that work queued on other streams next (the SPH pair loop) overlaps them
     cudaMemcpyAsync(t.info_host, t.counters, C_WORDS * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(t.info_host + C_WORDS, t.level_count, TREE_MAX_LEVELS * sizeof(uint32_t), cudaMemcpyDeviceToHost,
         st);
@@ -1371,6 +1367,11 @@ cudaError_t treeBuild(const DState& s, Tree& t, const Physics& ph, uint32_t* dev
     if (e != cudaSuccess) {
         return e;
     }
+    // moments, bottom-up, and the walks' FP32 node records, sized on the device
+    t.mixed_moments = ph.precision == SPHGPU_PRECISION_MIXED;
+    launchMomentsDev(s, t, ph, t.mixed_moments, st);
+    launchPrepareWalkDev(s, t, ph, st);
+    launched(3);
     const uint32_t* info = t.info_host;
     t.node_count = std::min(info[C_NODES], t.node_capacity);
     t.leaf_count = std::min(info[C_LEAVES], n);

@@ -115,7 +115,9 @@ enum {
 };
 enum {
     SPHGPU_PRECISION_FP64 = 0, /* every operation in FP64; pair terms IEEE-identical to the reference */
-    SPHGPU_PRECISION_MIXED = 1 /* FP32 cell-relative pair sums and walk, FP64 state/integrator/totals */
+    SPHGPU_PRECISION_MIXED = 1 /* FP32 cell-relative pair sums and walk, FP64 state/integrator/totals; SPH
+                                  handles of fewer than 2^27 particles (the pair loop's neighbour lists hold
+                                  27-bit indices; sphgpu_create refuses more with SPHGPU_ERR_UNSUPPORTED) */
 };
 
 /* One material (the reference's BodySettings entries read by EosMaterial/SolidMaterial, core/sph/Materials.cpp,

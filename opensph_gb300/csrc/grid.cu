@@ -2,8 +2,10 @@
 // core/objects/finders/KdTree.inl.h:316-391, NeighborFinder.cpp:11-25).
 //
 // Each step: device reduction of the bounding box and max h -> grid of cells of edge >= 2 h_max (the
-// kernel support) -> cell key per particle -> radix sort of (key, index) -> per-cell [start, end) ranges ->
-// cell-sorted copies of the pair-loop inputs. The pair loops then scan the 27 cells around each particle.
+// kernel support; h_max for the mixed pair loop's fine grid) -> cell key per particle -> radix sort of (key,
+// index) -> per-cell [start, end) ranges (and, for the fine grid, the first position of every cell key) ->
+// cell-sorted copies of the pair-loop inputs. The pair loops then scan the 27 cells around each particle (the
+// cells within two of it on the fine grid).
 // The interacting pair set is decided by the exact FP64 test of SymmetricSolver::loop
 // (core/sph/solvers/SymmetricSolver.cpp:126-130): |r_i - r_j|^2 < (2 * 0.5 (h_i + h_j))^2, evaluated
 // with round-to-nearest multiplies and adds (no FMA), i.e. bit-identically to the reference.

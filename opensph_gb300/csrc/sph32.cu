@@ -41,10 +41,10 @@ __device__ __forceinline__ float lutGradF(const float* __restrict__ lut, float q
     return g0 + (g1 - g0) * ratio;
 }
 
-// The pair loop runs in three kernels. neighboursMixedKernel tests the candidates of the 27 cells (one float4 load
-// and a distance test each) and writes the interacting ones, in cell order, to a per-particle neighbour list
-// (sorted index | cell offset << 27, laid out [slot][particle] so that a warp's writes and reads of one slot are
-// contiguous); it holds few registers and runs at full occupancy. pairSumMixedKernel then evaluates the pair terms
+// The pair loop runs in three kernels. neighboursMixedKernel tests the candidates of the cells around a particle
+// (one float4 load and a distance test each) and writes the interacting ones, in cell order, to a per-particle
+// neighbour list (sorted index | coarse-cell offset << 27, laid out [slot][particle] so that a warp's writes and
+// reads of one slot are contiguous); it holds few registers and runs at high occupancy. pairSumMixedKernel then evaluates the pair terms
 // from the lists and finalizes the particle. A particle with more than NB_CAP neighbours is left to
 // pairSumMixedOverflowKernel, which scans its cells again (rare: a queue of such particles is filled by the first
 // kernel). Each particle visits its neighbours in cell order, so the sums are those of a direct loop over the cells.

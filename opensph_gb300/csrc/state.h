@@ -333,8 +333,9 @@ void launchFindBall(const Grid& g, uint32_t n, const dbl4& pos, double radius, u
 void launchListPairs(const DState& s, const Grid& g, uint32_t* pi, uint32_t* pj, unsigned long long* count,
     unsigned long long capacity, cudaStream_t st);
 
-// grid over the positions r: radius NULL -> cell edge >= 2 max h (27-cell stencil of the pair loops); else the
-// collision grid, cell edge 2 max(mean radius, max radius / 8), searched over each particle's own cell box
+// grid over the positions r: radius NULL -> cell edge >= 2 max h (27-cell stencil of the pair loops), or max h
+// with fine (the mixed pair loop); else the collision grid, cell edge 2 max(mean radius, max radius / 8),
+// searched over each particle's own cell box
 void launchGridBuildRadius(const dbl4* r, const double* radius, uint32_t n, Grid& g, cudaStream_t st,
     bool fine = false);
 

@@ -246,15 +246,31 @@ def test_quantity_size_mismatch_is_rejected():
             g.get_quantity(abi.Q_DEVIATORIC_STRESS, 0)
 
 
-def test_single_particle_and_pairless():
+@pytest.mark.parametrize("precision", [abi.PRECISION_FP64, abi.PRECISION_MIXED])
+def test_single_particle_and_pairless(precision):
     r = np.array([0.0, 0.0, 0.0, 1.0])
-    with gas_solver(r) as g:
+    with gas_solver(r, precision=precision) as g:
         pi, pj = g.pairs()
         g.integrate()
         st = g.get_state(["dv", "ncnt"])
     assert pi.size == 0
     assert st["ncnt"][0] == 0
     np.testing.assert_array_equal(st["dv"], 0.0)
+
+
+@pytest.mark.parametrize("precision", [abi.PRECISION_FP64, abi.PRECISION_MIXED])
+def test_two_particles_and_far_apart_pairs(precision):
+    # two particles within each other's support, and a third one far from both: the pair's accelerations are
+    # equal and opposite, the lone particle has no neighbour
+    r = np.array([0.0, 0.0, 0.0, 1.0, 1.0, 0.0, 0.0, 1.0, 50.0, 0.0, 0.0, 1.0])
+    with gas_solver(r, precision=precision) as g:
+        g.integrate()
+        st = g.get_state(["dv", "ncnt"])
+    np.testing.assert_array_equal(st["ncnt"], [1, 1, 0])
+    dv = st["dv"].reshape(-1, 4)
+    assert dv[0, 0] != 0.0
+    np.testing.assert_allclose(dv[0, :3], -dv[1, :3], rtol=1e-6 if precision == abi.PRECISION_MIXED else 1e-15)
+    np.testing.assert_array_equal(dv[2, :3], 0.0)
 
 
 # ---- mixed precision: FP32 pair sums and FP32 tree-walk evaluation against the FP64 path -----------------

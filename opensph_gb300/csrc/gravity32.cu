@@ -197,7 +197,7 @@ __global__ void __launch_bounds__(128, 8) listLevelKernel(const BhNodeGeom* __re
     int deferPass, uint32_t* __restrict__ defer, uint32_t scratchWarps,
     int32_t* scratch, uint32_t cap, int32_t* __restrict__ pool, uint32_t poolCap,
     const int32_t* __restrict__ keptIn, int32_t* __restrict__ keptOut, uint32_t keptCap, uint32_t* __restrict__ meta,
-    uint32_t* __restrict__ counters, int parity, uint32_t* devError) {
+    uint32_t* __restrict__ counters, int parity) {
     __shared__ WalkFrame frameSh[4];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
@@ -307,7 +307,7 @@ __global__ void __launch_bounds__(128, 8) listLevelKernel(const BhNodeGeom* __re
         if (overflow || base + nN + nP > poolCap || kbase + nK > keptCap) {
             if (lane == 0) {
                 if (overflow) {
-                    atomicOr(devError, uint32_t(DEV_ERR_WALK_CAPACITY));
+                    atomicOr(&counters[5], 1u); // the staging lists were too short
                 }
                 uint32_t* m = meta + size_t(ev) * NL_META;
                 m[0] = m[1] = m[2] = m[3] = m[4] = m[5] = 0;
@@ -348,8 +348,7 @@ __global__ void __launch_bounds__(LB_THREADS, 4) listBlockKernel(const BhNodeGeo
     const float* __restrict__ nodef, const uint32_t* __restrict__ levelNodes, uint32_t first, uint32_t last,
     int32_t* scratch, uint32_t cap,
     int32_t* __restrict__ pool, uint32_t poolCap, const int32_t* __restrict__ keptIn, int32_t* __restrict__ keptOut,
-    uint32_t keptCap, uint32_t* __restrict__ meta, uint32_t* __restrict__ counters, int parity,
-    uint32_t* devError) {
+    uint32_t keptCap, uint32_t* __restrict__ meta, uint32_t* __restrict__ counters, int parity) {
     __shared__ WalkFrame fr;
     __shared__ uint32_t warpCnt[LB_WARPS][4]; // per warp of a round: kept, opened, particle lists, nodes
     __shared__ uint32_t baseSh[2];
@@ -461,7 +460,7 @@ __global__ void __launch_bounds__(LB_THREADS, 4) listBlockKernel(const BhNodeGeo
         if (overflow || base + nN + nP > poolCap || kbase + nK > keptCap) {
             if (tid == 0) {
                 if (overflow) {
-                    atomicOr(devError, uint32_t(DEV_ERR_WALK_CAPACITY));
+                    atomicOr(&counters[5], 1u); // the staging lists were too short
                 }
                 uint32_t* m = meta + size_t(ev) * NL_META;
                 m[0] = m[1] = m[2] = m[3] = m[4] = m[5] = 0;
@@ -710,14 +709,6 @@ void launchWalkLists(const DState& s, Tree& t, uint32_t* devError, cudaStream_t 
         cudaMalloc(&t.nl_counters, 8 * sizeof(uint32_t));
         cudaMallocHost(&t.nl_host, 8 * sizeof(uint32_t));
     }
-    // per-warp staging of one node's lists in the walk scratch: 4 lists of NL_STAGE entries in the first pass
-    // of a level, of NL_STAGE_DEFER entries in the pass over the nodes deferred by the first
-    // (the staging grows with the walk scratch: sphgpu_gravity_eval enlarges it and walks again when a list
-    // outgrew it)
-    const uint32_t NL_STAGE = t.walk_capacity, NL_STAGE_DEFER = 4 * t.walk_capacity;
-    const size_t scratchEntries = size_t(t.walk_warps) * 2 * t.walk_capacity;
-    const uint32_t listWarps = std::max(1u, uint32_t(scratchEntries / (4 * size_t(NL_STAGE))));
-    const uint32_t deferWarps = std::max(1u, uint32_t(scratchEntries / (4 * size_t(NL_STAGE_DEFER))));
     if (!t.nl_defer) {
         cudaMalloc(&t.nl_defer, size_t(t.node_capacity) * sizeof(uint32_t));
     }
@@ -726,9 +717,19 @@ void launchWalkLists(const DState& s, Tree& t, uint32_t* devError, cudaStream_t 
     // level l holds the nodes level_nodes[level_first[l] .. level_first[l + 1])
     const uint32_t levels = t.level_first.empty() ? 0u : uint32_t(t.level_first.size() - 1);
     // the lists of all levels; when a pool overflowed, grow it to twice the counted need (the count misses what
-    // the children of the nodes that did not fit would have added) and build them again
+    // the children of the nodes that did not fit would have added), and when a node's lists outgrew the staging,
+    // the staging four times, and build them again
     bool fits = false;
-    for (int attempt = 0; attempt < 4 && !fits; ++attempt) {
+    for (int attempt = 0; attempt < 8 && !fits; ++attempt) {
+        // per-warp staging of one node's lists in the walk scratch: 4 lists of NL_STAGE entries in the first pass
+        // of a level, of NL_STAGE_DEFER entries (the scratch of walk_defer_factor warps) in the pass over the nodes
+        // deferred by the first and on the levels of few nodes
+        const size_t scratchEntries = size_t(t.walk_warps) * 2 * t.walk_capacity;
+        const uint32_t NL_STAGE = t.walk_capacity;
+        const uint32_t NL_STAGE_DEFER = uint32_t(std::min<size_t>(size_t(t.walk_defer_factor) * t.walk_capacity,
+            scratchEntries / 4));
+        const uint32_t listWarps = std::max(1u, uint32_t(scratchEntries / (4 * size_t(NL_STAGE))));
+        const uint32_t deferWarps = std::max(1u, uint32_t(scratchEntries / (4 * size_t(NL_STAGE_DEFER))));
         if (t.nl_capacity < poolNeed) {
             cudaFree(t.nl_pool);
             cudaMalloc(&t.nl_pool, size_t(poolNeed) * sizeof(int32_t));
@@ -756,7 +757,7 @@ void launchWalkLists(const DState& s, Tree& t, uint32_t* devError, cudaStream_t 
                 listBlockKernel<<<last - first, LB_THREADS, 0, st>>>(t.geom, t.nodef, t.level_nodes, first, last,
                     t.walk_scratch,
                     NL_STAGE_DEFER, t.nl_pool, t.nl_capacity, t.nl_kept[1 - parity], t.nl_kept[parity],
-                    t.nl_kept_capacity, t.nl_meta, t.nl_counters, parity, devError);
+                    t.nl_kept_capacity, t.nl_meta, t.nl_counters, parity);
                 t.walk_launches++;
                 continue;
             }
@@ -765,12 +766,12 @@ void launchWalkLists(const DState& s, Tree& t, uint32_t* devError, cudaStream_t 
             listLevelKernel<<<ceilDiv(warps, 4), 128, 0, st>>>(t.geom, t.nodef, t.level_nodes, first, last, 0,
                 t.nl_defer, warps,
                 t.walk_scratch, NL_STAGE, t.nl_pool, t.nl_capacity, t.nl_kept[1 - parity], t.nl_kept[parity],
-                t.nl_kept_capacity, t.nl_meta, t.nl_counters, parity, devError);
+                t.nl_kept_capacity, t.nl_meta, t.nl_counters, parity);
             const uint32_t dWarps = std::min(last - first, deferWarps);
             listLevelKernel<<<ceilDiv(dWarps, 4), 128, 0, st>>>(t.geom, t.nodef, t.level_nodes, first, last, 1,
                 t.nl_defer, dWarps,
                 t.walk_scratch, NL_STAGE_DEFER, t.nl_pool, t.nl_capacity, t.nl_kept[1 - parity], t.nl_kept[parity],
-                t.nl_kept_capacity, t.nl_meta, t.nl_counters, parity, devError);
+                t.nl_kept_capacity, t.nl_meta, t.nl_counters, parity);
             t.walk_launches += 2;
         }
         cudaMemcpyAsync(t.nl_host, t.nl_counters, 8 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
@@ -778,9 +779,19 @@ void launchWalkLists(const DState& s, Tree& t, uint32_t* devError, cudaStream_t 
             return;
         }
         const uint32_t usedPool = t.nl_host[0], usedKept = t.nl_host[3];
-        fits = usedPool <= t.nl_capacity && usedKept <= t.nl_kept_capacity;
+        const bool staged = t.nl_host[5] == 0;
+        fits = staged && usedPool <= t.nl_capacity && usedKept <= t.nl_kept_capacity;
         poolNeed = std::max(poolNeed, 2 * usedPool);
         keptNeed = std::max(keptNeed, 2 * usedKept);
+        if (!staged) {
+            // longer staging for the few nodes whose lists outgrew it: fewer warps share the scratch, and only when
+            // one warp holds all of it, a larger scratch
+            if (size_t(t.walk_defer_factor) * 4 * t.walk_capacity <= scratchEntries / 4) {
+                t.walk_defer_factor *= 4;
+            } else if (treeGrowWalkScratch(t, 4 * t.walk_capacity) != cudaSuccess) {
+                break;
+            }
+        }
     }
     if (!fits) {
         flagErrorKernel<<<1, 1, 0, st>>>(devError, uint32_t(DEV_ERR_WALK_CAPACITY));

@@ -290,12 +290,13 @@ struct Tree {
     uint32_t nl_kept_capacity = 0;
     uint32_t* nl_meta = nullptr;      // per node: N offset, N length, P offset, P length, kept offset, kept length
     uint32_t* nl_counters = nullptr;  // device: pool entries used, kept entries used (two levels), max kept,
-                                      // deferred nodes of the level
+                                      // deferred nodes of the level, a node's lists outgrew the staging
     uint32_t* nl_host = nullptr;      // pinned mirror of nl_counters
     uint32_t* nl_defer = nullptr;     // nodes of a level whose lists outgrew the first pass's staging
     uint32_t walk_launches = 0;       // kernels launched by the last mixed walk
     uint32_t walk_warps = 0;
     uint32_t walk_capacity = 0;       // entries per list per warp
+    uint32_t walk_defer_factor = 4;   // staging of a deferred node: the scratch of this many warps
     unsigned long long* stats = nullptr; // device: approx, exact
     unsigned long long* bbox = nullptr;  // device: flipped bounding box of the root
     float* nodef = nullptr;           // mixed walk: FP32 evaluation record per node (28 floats)

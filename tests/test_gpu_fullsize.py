@@ -170,6 +170,34 @@ def test_plummer_full_size_against_direct_sum():
         assert np.percentile(rel, 99) < 1e-3
 
 
+def test_walk_lists_outgrowing_their_staging():
+    # Plummer sphere of 1,048,576 particles at an opening angle of 0.2: the interaction lists of some nodes outgrow
+    # the list phase's first staging, which grows inside the walk (no capacity error on the step path); both
+    # walks take the same interactions (about 45,000 per particle), the mixed one within 5e-6 of the FP64 one (the
+    # FP32 rounding of that many terms; 2e-6 at the opening angles of 0.3 and above), and the accelerations are
+    # within the octupole's error of the FP64 direct sum on 256 seeded particles
+    n = 1 << 20
+    r, m = initial.plummer(n, seed=3, softening=1e-3)
+    targets = np.random.default_rng(9).choice(n, 256, replace=False).astype("u4")
+    acc, inter = {}, {}
+    for prec in (abi.PRECISION_MIXED, abi.PRECISION_FP64):
+        cfg, keep = abi.make_config(n, [abi.ideal_gas()], forces=abi.FORCE_PRESSURE | abi.FORCE_SELF_GRAVITY,
+                                    gravity_constant=1.0, gravity_opening_angle=0.2, precision=prec)
+        with GpuSolver(cfg, keep) as g:
+            g.set_quantity(abi.Q_POSITION, 0, r.ravel())
+            g.set_quantity(abi.Q_MASS, 0, m)
+            g.set_state({"rho": np.ones(n), "u": np.zeros(n)})
+            g.integrate()
+            acc[prec] = g.get_quantity(abi.Q_POSITION, 2).reshape(-1, 4)[:, :3]
+            inter[prec] = g.gravity_interactions()
+            if prec == abi.PRECISION_FP64:
+                direct = g.gravity_direct(targets).reshape(-1, 4)[:, :3]
+    assert list(inter[abi.PRECISION_MIXED]) == list(inter[abi.PRECISION_FP64])
+    assert scale_err(acc[abi.PRECISION_MIXED], acc[abi.PRECISION_FP64]) < 5e-6
+    rel = np.linalg.norm(acc[abi.PRECISION_FP64][targets] - direct, axis=1) / np.linalg.norm(direct, axis=1)
+    assert np.median(rel) < 2e-5
+
+
 @pytest.mark.parametrize("h,sigma,steps", [(400.0, 0.1, 3), (600.0, 0.02, 2)])
 def test_nbody_cloud_full_size_matches_oracle(h, sigma, steps):
     # HardSphereSolver on 1,000,000 spheres (the rubble cloud of the N-body benchmark; with h = 600 m and a cold

@@ -333,9 +333,10 @@ def compare_fp64(args, st, mats, n, mixed_cfg, dev):
 # DRAM bytes (read + write) of one mixed walk of the default workload (the evaluation launch plus the launches
 # that build the interaction lists): a constant from a separate ncu capture of the same workload and command
 # (dram__bytes_read.sum + dram__bytes_write.sum), not measured in this run
-WALK_TRAFFIC_BYTES = (277.7 + 35.1 + 175.4 + 76.1 + 15.2) * 1e6
-WALK_TRAFFIC_SOURCE = ("constant from an earlier ncu capture of one walk of this workload (dram__bytes_read.sum + "
-                       "dram__bytes_write.sum); not measured in this run")
+WALK_TRAFFIC_BYTES = (240.2 + 27.7) * 1e6
+WALK_TRAFFIC_SOURCE = ("constant from an ncu capture of the evaluation kernel of one walk of this workload "
+                       "(dram__bytes_read.sum + dram__bytes_write.sum, profiles/evalListsKernel_impact1M.md); not "
+                       "measured in this run")
 
 # FP32 operations of one particle-multipole evaluation (accMultipoleF, csrc/gravity32.cu: octupole) and the
 # N-body convention for one softened particle-particle interaction
@@ -678,12 +679,15 @@ def main():
     pair_ms = res["phases"]["sph_eval"] / args.steps
     peak, peak_kind = peaks()
     achieved = PAIR_BYTES_PER_PARTICLE * n / (pair_ms * 1e-3) / 1e9 if pair_ms > 0 else None
-    # dominant kernel: the mixed tree walk, FP32-pipe bound; algorithmic FLOPs of the last step's walk
-    # (interaction counts of the walk itself) over its CUDA-event time on the gravity stream
+    # dominant kernel: the mixed tree walk's evaluation kernel, FP32-pipe bound; algorithmic FLOPs of the last
+    # step's walk (interaction counts of the walk itself) over the kernel's CUDA-event time on the gravity stream
+    # (the whole walk, with its interaction-list phase, beside it)
+    eval_ms = res["phases"]["walk_evaluation"] / args.steps
     walk_ms = res["phases"]["gravity_eval"] / args.steps
     pn, pp = res["interactions"]
     walk_flops = pn * FLOP_PN + pp * FLOP_PP
-    walk_tf = walk_flops / (walk_ms * 1e-3) / 1e12 if walk_ms > 0 else None
+    walk_tf = walk_flops / (eval_ms * 1e-3) / 1e12 if eval_ms > 0 else None
+    whole_tf = walk_flops / (walk_ms * 1e-3) / 1e12 if walk_ms > 0 else None
     fp32_peak = res.get("fp32_peak_tflops") or FP32_PEAK_NOMINAL
     fp32_source = ("measured: FMA-chain kernel on every SM, CUDA events (sphgpu_measure_fp32_peak)"
                    if res.get("fp32_peak_tflops") else "nominal (152 SMs x 128 lanes x 2 x 2.07 GHz)")
@@ -693,18 +697,20 @@ def main():
         "vs_baseline": None, "dtype": "f32/f64", "data": "synthetic", "config": config_json(args, n),
         "e2e": res["e2e"], "gpu_launches": res["launches"], "clocks": res["clocks"],
         "phases_ms_per_step": {k: v / args.steps for k, v in res["phases"].items()},
-        "roofline": {"kernel": "evalListsKernel + listLevelKernel (mixed walk)", "bound": "fp32", "achieved": walk_tf,
+        "roofline": {"kernel": "evalListsKernel (mixed walk evaluation)", "bound": "fp32", "achieved": walk_tf,
                      "peak": fp32_peak, "unit": "TFLOP/s", "frac": walk_tf / fp32_peak if walk_tf else None,
                      "traffic": WALK_TRAFFIC_BYTES, "traffic_source": WALK_TRAFFIC_SOURCE,
                      "peak_source": fp32_source, "fp32_nominal_tflops": FP32_PEAK_NOMINAL,
                      "flops_per_launch": walk_flops, "particle_node": pn, "particle_particle": pp,
                      "flop_per_particle_node": FLOP_PN, "flop_per_particle_particle": FLOP_PP,
-                     "launch_ms": walk_ms},
+                     "launch_ms": eval_ms, "whole_walk_ms": walk_ms, "whole_walk_achieved": whole_tf,
+                     "whole_walk_frac": whole_tf / fp32_peak if whole_tf else None},
         "roofline_pair": {"kernel": "pairSumMixedKernel", "bound": "hbm", "achieved": achieved, "peak": peak,
                           "unit": "GB/s", "frac": achieved / peak if achieved else None,
                           "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                           "algorithmic_bytes_per_particle": PAIR_BYTES_PER_PARTICLE,
-                          "note": "timed while the tree build runs concurrently on the gravity stream"},
+                          "note": "timed from its queueing to its end, beside the tree's moments and walk on the "
+                                  "gravity stream"},
     }
     if "fp64" in res:
         line["fp64"] = res["fp64"]

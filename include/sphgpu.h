@@ -383,7 +383,9 @@ enum {
     SPHGPU_PHASE_SPH_EVAL = 4,      /* pair loop + finalize + fracture model */
     SPHGPU_PHASE_CORRECT = 5,       /* corrector (or leap-frog kick) + Courant criterion */
     SPHGPU_PHASE_COLLIDE = 6,       /* N-body collision search and resolution (COLLISION_EVAL_TIME) */
-    SPHGPU_PHASE_COUNT = 7
+    SPHGPU_PHASE_WALK_EVALUATION = 7, /* the tree walk's evaluation kernel alone (inside GRAVITY_EVAL, which also
+                                         holds the walk's interaction-list phase) */
+    SPHGPU_PHASE_COUNT = 8
 };
 sphgpu_status sphgpu_set_profiling(sphgpu_handle* h, int32_t enabled);
 /* Device milliseconds per phase and the number of this library's kernel launches since the last call

@@ -347,12 +347,23 @@ sphgpu_status evalGravityWalk(sphgpu_handle* h, cudaStream_t st) {
     }
     {
         Phase ph(h, SPHGPU_PHASE_GRAVITY_EVAL, st);
+        // the evaluation kernel alone, timed inside the phase
+        cudaEvent_t e0 = h->profiling ? takeEvent(h) : nullptr, e1 = h->profiling ? takeEvent(h) : nullptr;
         if (h->ph.precision == SPHGPU_PRECISION_MIXED) {
-            launchGravityWalkMixed(h->s, h->tree, h->ph, h->d_lut_grav_f, h->d_err, st);
+            launchGravityWalkMixed(h->s, h->tree, h->ph, h->d_lut_grav_f, h->d_err, st, e0, e1);
             h->launches += h->tree.walk_launches;
         } else {
-            launchGravityWalk(h->s, h->tree, h->ph, h->d_lut_grav, h->d_err, st);
-            h->launches += 1;
+            launchGravityWalk(h->s, h->tree, h->ph, h->d_lut_grav, h->d_err, st, e0, e1);
+            h->launches += h->tree.walk_launches;
+        }
+        if (e0) {
+            // (no walk was launched for an empty state: the events go back unrecorded)
+            if (h->tree.walk_launches > 0) {
+                h->marks.push_back({ SPHGPU_PHASE_WALK_EVALUATION, { e0, e1 } });
+            } else {
+                h->event_pool.push_back(e0);
+                h->event_pool.push_back(e1);
+            }
         }
     }
     h->gravity_current = true;
@@ -1229,7 +1240,7 @@ sphgpu_status sphgpu_gravity_eval(sphgpu_handle* h, double* dv, uint64_t count) 
                 h->launches += h->tree.walk_launches;
             } else {
                 launchGravityWalk(h->s, h->tree, h->ph, h->d_lut_grav, h->d_err, h->stream);
-                h->launches += 1;
+                h->launches += h->tree.walk_launches;
             }
         }
         CUDA_TRY(h, cudaGetLastError());

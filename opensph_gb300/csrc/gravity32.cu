@@ -800,7 +800,7 @@ void launchWalkLists(const DState& s, Tree& t, uint32_t* devError, cudaStream_t 
 }
 
 void launchGravityWalkMixed(const DState& s, Tree& t, const Physics& ph, const float* lutF, uint32_t* devError,
-    cudaStream_t st) {
+    cudaStream_t st, cudaEvent_t evalStart, cudaEvent_t evalEnd) {
     cudaMemsetAsync(t.stats, 0, 5 * sizeof(unsigned long long), st);
     t.walk_launches = 0;
     if (s.n == 0 || t.node_count == 0) {
@@ -818,8 +818,14 @@ void launchGravityWalkMixed(const DState& s, Tree& t, const Physics& ph, const f
         residentBlocks = std::max(1, perSm * sms);
     }
     const int blocks = std::max(1, std::min(residentBlocks, int(t.walk_warps / (WALK_THREADS_F / 32))));
+    if (evalStart) {
+        cudaEventRecord(evalStart, st);
+    }
     evalListsKernel<<<blocks, WALK_THREADS_F, 0, st>>>(t.idx, t.geom, t.nodef, t.pf, t.mf, t.leaves, t.leaf_count,
         lutF, ph.kernel_radius, ph.multipole_order, t.nl_pool, t.nl_meta, s.agrav, t.stats);
+    if (evalEnd) {
+        cudaEventRecord(evalEnd, st);
+    }
     t.walk_launches++;
 }
 

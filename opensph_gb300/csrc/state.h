@@ -381,12 +381,13 @@ void launchMomentsDev(const DState& s, Tree& t, const Physics& ph, bool mixed, c
 void launchPrepareWalkDev(const DState& s, Tree& t, const Physics& ph, cudaStream_t st);
 // forms the FP64 moments of a tree built with FP32 moments (for the FP64 point evaluation)
 void treeEnsureFp64Moments(const DState& s, Tree& t, const Physics& ph, cudaStream_t st);
+// evalStart / evalEnd (or null): events recorded around the walk's evaluation kernel
 void launchGravityWalk(const DState& s, Tree& t, const Physics& ph, const double* lut_grad, uint32_t* dev_error,
-    cudaStream_t st);
+    cudaStream_t st, cudaEvent_t evalStart = nullptr, cudaEvent_t evalEnd = nullptr);
 // (gravity32.cu) walk phase 1, shared by both walks: the interaction lists of every node, level by level
 void launchWalkLists(const DState& s, Tree& t, uint32_t* dev_error, cudaStream_t st);
 void launchGravityWalkMixed(const DState& s, Tree& t, const Physics& ph, const float* lut_grad_f,
-    uint32_t* dev_error, cudaStream_t st);
+    uint32_t* dev_error, cudaStream_t st, cudaEvent_t evalStart = nullptr, cudaEvent_t evalEnd = nullptr);
 // BarnesHut::evalAttractors on the device: att (5 doubles per attractor), dv (particles, in/out), acc (3 doubles per
 // attractor, in/out), partial (gravityAttractorPartials(n, count) doubles of scratch)
 void launchGravityAttractors(const DState& s, const Physics& ph, const double* lut, const double* att, uint32_t count,

@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(WALK64_THREADS, 6) evalLists64Kernel(const dbl
 } // namespace
 
 void launchGravityWalk(const DState& s, Tree& t, const Physics& ph, const double* lut, uint32_t* devError,
-    cudaStream_t st) {
+    cudaStream_t st, cudaEvent_t evalStart, cudaEvent_t evalEnd) {
     cudaMemsetAsync(t.stats, 0, 5 * sizeof(unsigned long long), st);
     t.walk_launches = 0;
     if (s.n == 0 || t.node_count == 0) {
@@ -237,8 +237,14 @@ void launchGravityWalk(const DState& s, Tree& t, const Physics& ph, const double
         residentBlocks = std::max(1, perSm * sms);
     }
     const int blocks = std::max(1, std::min(residentBlocks, ceilDiv(t.leaf_count, WALK64_THREADS / 32)));
+    if (evalStart) {
+        cudaEventRecord(evalStart, st);
+    }
     evalLists64Kernel<<<blocks, WALK64_THREADS, 0, st>>>(s.r, s.m, ph.G, t.idx, t.geom, t.mom, t.leaves,
         t.leaf_count, lut, ph.kernel_radius, ph.multipole_order, t.nl_pool, t.nl_meta, s.agrav, t.stats);
+    if (evalEnd) {
+        cudaEventRecord(evalEnd, st);
+    }
     t.walk_launches++;
 }
 

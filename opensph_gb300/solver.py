@@ -357,7 +357,8 @@ class GpuSolver:
             self._check(self._lib.sphgpu_totals_frame(self._h, float(frame_frequency), out.ctypes.data_as(_F8P)))
         return out
 
-    PHASES = ["predict", "gravity_build", "gravity_eval", "neighbors", "sph_eval", "correct", "collide"]
+    PHASES = ["predict", "gravity_build", "gravity_eval", "neighbors", "sph_eval", "correct", "collide",
+              "walk_evaluation"]
 
     def set_profiling(self, enabled=True):
         self._check(self._lib.sphgpu_set_profiling(self._h, 1 if enabled else 0))

@@ -564,7 +564,7 @@ cudaError_t treeGrowWalkScratch(Tree& t, uint32_t capacity) {
 void treeFree(Tree& t) {
     void* ptrs[] = { t.idx, t.scratch_b, t.scratch_s, t.geom, t.mom, t.seg[0], t.seg[1], t.counters, t.leaves, t.visits,
         t.walk_scratch, t.nl_pool, t.nl_kept[0], t.nl_kept[1], t.nl_meta, t.nl_counters, t.nl_defer, t.stats, t.bbox,
-        t.nodef, t.pf, t.mf };
+        t.nodef, t.pf, t.mf, t.slice_part };
     for (void* p : ptrs) {
         if (p) {
             cudaFree(p);

@@ -145,11 +145,20 @@ __global__ void __launch_bounds__(128) correction64Kernel(DState s, Grid g, Phys
     }
 }
 
+// Gather form: a thread per particle sums its terms over the candidates of the 27 cells around it, then
+// finalizes the particle. With few particles (fewer than about a thread per SM thread slot at S = 1), 2^shift = S
+// consecutive lanes of a warp share a particle: lane s of the group takes the candidates s, s + S, ... of every
+// row range, and the groups' partial sums are added by a fixed pairwise tree of shuffles (deterministic; the
+// order of the sums differs from the single-thread order in the last bits only) before lane 0 finalizes.
 template <bool Solid>
 __global__ void __launch_bounds__(128) pairSum64Kernel(DState s, Grid g, Physics ph,
-    const MaterialD* __restrict__ mats, const double* __restrict__ lut) {
+    const MaterialD* __restrict__ mats, const double* __restrict__ lut, uint32_t shift) {
     const uint32_t n = s.n;
-    const uint32_t si = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t slices = 1u << shift;
+    const uint32_t si = gt >> shift;
+    const uint32_t sl = gt & (slices - 1u);
+    // (the lanes of a group share si: a group returns as a whole)
     if (si >= n) {
         return;
     }
@@ -169,7 +178,7 @@ __global__ void __launch_bounds__(128) pairSum64Kernel(DState s, Grid g, Physics
         flagi = g.flags[si];
     }
     double ax = 0., ay = 0., az = 0.;
-    if (ph.gravity) {
+    if (ph.gravity && sl == 0) {
         const dbl4 a = s.agrav[i];
         ax = a.x;
         ay = a.y;
@@ -206,7 +215,7 @@ __global__ void __launch_bounds__(128) pairSum64Kernel(DState s, Grid g, Physics
                     tEnd = max(tEnd, ce0);
                 }
             }
-            for (uint32_t t = tb; t < tEnd; ++t) {
+            for (uint32_t t = tb + sl; t < tEnd; t += slices) {
                 if (t == si) {
                     continue;
                 }
@@ -281,6 +290,26 @@ __global__ void __launch_bounds__(128) pairSum64Kernel(DState s, Grid g, Physics
                     }
                 }
             }
+        }
+    }
+    if (slices > 1) {
+        const uint32_t lane = threadIdx.x & 31u;
+        const unsigned mask = ((slices == 32u ? 0u : (1u << slices)) - 1u) << (lane & ~(slices - 1u));
+        for (uint32_t off = slices >> 1; off > 0; off >>= 1) {
+            ax += __shfl_down_sync(mask, ax, off, int(slices));
+            ay += __shfl_down_sync(mask, ay, off, int(slices));
+            az += __shfl_down_sync(mask, az, off, int(slices));
+            du += __shfl_down_sync(mask, du, off, int(slices));
+            divv += __shfl_down_sync(mask, divv, off, int(slices));
+            cnt += __shfl_down_sync(mask, cnt, off, int(slices));
+            if (Solid) {
+                for (int c = 0; c < 6; ++c) {
+                    gv[c] += __shfl_down_sync(mask, gv[c], off, int(slices));
+                }
+            }
+        }
+        if (sl != 0) {
+            return;
         }
     }
     finalizeParticle<Solid>(s, ph, mats, i, ri, rhoi, pri, Si, ax, ay, az, du, divv, gv, cnt);
@@ -672,10 +701,23 @@ void launchPairSum64(const DState& s, const Grid& g, const Physics& ph, const Ma
     if (!s.n) {
         return;
     }
+    // lanes per particle: a power of two up to 8, while the threads stay within about 1,024 per SM
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        sms = std::max(sms, 1);
+    }
+    uint32_t shift = 0;
+    while (shift < 3 && (size_t(s.n) << (shift + 1)) <= size_t(sms) * 1024) {
+        ++shift;
+    }
+    const int blocks = int((((size_t(s.n) << shift) + 127) / 128));
     if (ph.solid) {
-        pairSum64Kernel<true><<<ceilDiv(s.n, 128), 128, 0, st>>>(s, g, ph, mats, lut);
+        pairSum64Kernel<true><<<blocks, 128, 0, st>>>(s, g, ph, mats, lut, shift);
     } else {
-        pairSum64Kernel<false><<<ceilDiv(s.n, 128), 128, 0, st>>>(s, g, ph, mats, lut);
+        pairSum64Kernel<false><<<blocks, 128, 0, st>>>(s, g, ph, mats, lut, shift);
     }
 }
 

@@ -302,6 +302,8 @@ struct Tree {
     float* nodef = nullptr;           // mixed walk: FP32 evaluation record per node (28 floats)
     float4* pf = nullptr;             // mixed walk: particle position relative to its leaf's centre of mass, h
     float* mf = nullptr;              // mixed walk: G * m in tree order
+    dbl4* slice_part = nullptr;       // FP64 walk of few leaves: partial sums per slice (slices x n, tree order)
+    size_t slice_capacity = 0;
     uint32_t chunk_capacity = 0;
     BhChunk* chunks = nullptr;
     BhChunkStats* chunk_stats = nullptr;

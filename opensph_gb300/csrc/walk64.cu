@@ -22,6 +22,13 @@
 // would run about 1.3x faster but reorders the sums, and a last-bit change in the accelerations is enough to
 // change which hard-sphere collisions the N-body solver finds within a step: the collision sequences of the
 // reference's N-body runs are reproduced with the fixed order and not without it.
+//
+// A tree of few leaves (fewer than the resident warps) leaves most of the FP64 units idle with a warp per leaf:
+// there, outside the N-body solver, each leaf is taken by S <= 8 warps ("slices"): slice s evaluates the source
+// particles s, s + S, s + 2 S, ... of every source leaf and of the leaf itself, and the nodes at positions s,
+// s + S, ... of the node lists in the fixed order above, into its own partial sums, which a second kernel adds
+// in slice order. The result is deterministic for a given tree; it differs from the single-slice order in the
+// last bits.
 #include <algorithm>
 
 #include "tree.cuh"
@@ -115,7 +122,8 @@ __global__ void __launch_bounds__(WALK64_THREADS, 6) evalLists64Kernel(const dbl
     const double* __restrict__ m, double G, const uint32_t* __restrict__ idx, const BhNodeGeom* __restrict__ geom,
     const BhNodeMoments* __restrict__ mom, const uint32_t* __restrict__ leaves, uint32_t nLeaves,
     const double* __restrict__ lut, int kernelRadius, int order, const int32_t* __restrict__ pool,
-    const uint32_t* __restrict__ meta, dbl4* agrav, unsigned long long* stats) {
+    const uint32_t* __restrict__ meta, dbl4* agrav, unsigned long long* stats, uint32_t slices, dbl4* part,
+    uint32_t n) {
     constexpr int W = WALK64_THREADS / 32;
     __shared__ int32_t pathSh[W][MAX_PATH_F];
     __shared__ unsigned long long countSh[W][4];
@@ -129,14 +137,15 @@ __global__ void __launch_bounds__(WALK64_THREADS, 6) evalLists64Kernel(const dbl
     }
     __syncwarp();
     for (;;) {
-        uint32_t li = 0;
+        uint32_t item = 0;
         if (lane == 0) {
-            li = uint32_t(atomicAdd(&stats[4], 1ull));
+            item = uint32_t(atomicAdd(&stats[4], 1ull));
         }
-        li = __shfl_sync(0xffffffffu, li, 0);
-        if (li >= nLeaves) {
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= nLeaves * slices) {
             break;
         }
+        const uint32_t li = item / slices, sl = item - li * slices;
         const int leaf = int(leaves[li]);
         const uint32_t from = geom[leaf].from, to = geom[leaf].to;
         const uint32_t cnt = to - from;
@@ -160,6 +169,8 @@ __global__ void __launch_bounds__(WALK64_THREADS, 6) evalLists64Kernel(const dbl
         }
         double ax = 0., ay = 0., az = 0.;
         uint32_t leafN = 0, leafP = 0, leafSrc = 0;
+        // the slice whose turn the next node is
+        uint32_t turn = 0;
         for (int k = 1; k <= depth; ++k) {
             const uint32_t* mt = meta + size_t(path[k]) * NL_META;
             const uint32_t nOff = mt[0], nLen = mt[1], pOff = mt[2], pLen = mt[3];
@@ -170,7 +181,7 @@ __global__ void __launch_bounds__(WALK64_THREADS, 6) evalLists64Kernel(const dbl
                 const uint32_t f0 = geom[pn].from, f1 = geom[pn].to;
                 leafSrc += f1 - f0;
                 if (active) {
-                    for (uint32_t t = f0; t < f1; ++t) {
+                    for (uint32_t t = f0 + sl; t < f1; t += slices) {
                         const uint32_t j = idx[t];
                         const dbl4 rj = r[j];
                         pairAcc64(rj.x - ri.x, rj.y - ri.y, rj.z - ri.z, 0.5 * (rj.w + ri.w), G * m[j], lut, rad, ax,
@@ -178,8 +189,10 @@ __global__ void __launch_bounds__(WALK64_THREADS, 6) evalLists64Kernel(const dbl
                     }
                 }
             }
-            if (active) {
-                for (uint32_t c = 0; c < nLen; ++c) {
+            for (uint32_t c = 0; c < nLen; ++c) {
+                const bool mine = turn == sl;
+                turn = turn + 1 == slices ? 0u : turn + 1;
+                if (active && mine) {
                     const int nn = pool[nOff + c];
                     const BhNodeGeom& ng = geom[nn];
                     multipoleAcc64(ng.com[0] - ri.x, ng.com[1] - ri.y, ng.com[2] - ri.z, mom[nn], order, ax, ay, az);
@@ -188,7 +201,7 @@ __global__ void __launch_bounds__(WALK64_THREADS, 6) evalLists64Kernel(const dbl
         }
         // pairs inside the leaf
         if (active) {
-            for (uint32_t t = from; t < to; ++t) {
+            for (uint32_t t = from + sl; t < to; t += slices) {
                 if (t != from + uint32_t(lane)) {
                     const uint32_t j = idx[t];
                     const dbl4 rj = r[j];
@@ -197,14 +210,18 @@ __global__ void __launch_bounds__(WALK64_THREADS, 6) evalLists64Kernel(const dbl
                 }
             }
         }
-        if (lane == 0) {
+        if (lane == 0 && sl == 0) {
             wc[0] += leafN;
             wc[1] += leafP;
             wc[2] += uint64_t(cnt) * leafN;
             wc[3] += uint64_t(cnt) * (leafSrc + cnt - 1);
         }
         if (active) {
-            agrav[idx[from + lane]] = mkd4(ax, ay, az, 0.);
+            if (slices == 1) {
+                agrav[idx[from + lane]] = mkd4(ax, ay, az, 0.);
+            } else {
+                part[size_t(sl) * n + from + lane] = mkd4(ax, ay, az, 0.);
+            }
         }
         __syncwarp();
     }
@@ -212,6 +229,23 @@ __global__ void __launch_bounds__(WALK64_THREADS, 6) evalLists64Kernel(const dbl
     if (lane < 4) {
         atomicAdd(&stats[lane], wc[lane]);
     }
+}
+
+// the partial sums of the slices, added in slice order, into the accelerations (tree slot k = particle idx[k])
+__global__ void addSlicesKernel(const dbl4* __restrict__ part, uint32_t n, uint32_t slices,
+    const uint32_t* __restrict__ idx, dbl4* agrav) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) {
+        return;
+    }
+    dbl4 a = part[k];
+    for (uint32_t sl = 1; sl < slices; ++sl) {
+        const dbl4 b = part[size_t(sl) * n + k];
+        a.x += b.x;
+        a.y += b.y;
+        a.z += b.z;
+    }
+    agrav[idx[k]] = mkd4(a.x, a.y, a.z, 0.);
 }
 
 } // namespace
@@ -236,16 +270,42 @@ void launchGravityWalk(const DState& s, Tree& t, const Physics& ph, const double
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         residentBlocks = std::max(1, perSm * sms);
     }
-    const int blocks = std::max(1, std::min(residentBlocks, ceilDiv(t.leaf_count, WALK64_THREADS / 32)));
+    // slices per leaf: enough warps to fill the resident ones (never for the N-body solver, whose collision
+    // sequences need the single fixed order)
+    uint32_t slices = 1;
+    if (!ph.nbody && t.leaf_count > 0) {
+        const uint32_t residentWarps = uint32_t(residentBlocks) * (WALK64_THREADS / 32);
+        slices = std::min(8u, std::max(1u, residentWarps / t.leaf_count));
+        if (slices > 1 && t.slice_capacity < size_t(slices) * s.n) {
+            if (t.slice_part) {
+                cudaFree(t.slice_part);
+            }
+            t.slice_capacity = 0;
+            if (cudaMalloc(&t.slice_part, size_t(slices) * s.n * sizeof(dbl4)) == cudaSuccess) {
+                t.slice_capacity = size_t(slices) * s.n;
+            } else {
+                t.slice_part = nullptr;
+                cudaGetLastError();
+                slices = 1;
+            }
+        }
+    }
+    const int blocks =
+        std::max(1, std::min(residentBlocks, ceilDiv(t.leaf_count * slices, WALK64_THREADS / 32)));
     if (evalStart) {
         cudaEventRecord(evalStart, st);
     }
     evalLists64Kernel<<<blocks, WALK64_THREADS, 0, st>>>(s.r, s.m, ph.G, t.idx, t.geom, t.mom, t.leaves,
-        t.leaf_count, lut, ph.kernel_radius, ph.multipole_order, t.nl_pool, t.nl_meta, s.agrav, t.stats);
+        t.leaf_count, lut, ph.kernel_radius, ph.multipole_order, t.nl_pool, t.nl_meta, s.agrav, t.stats, slices,
+        t.slice_part, s.n);
+    t.walk_launches++;
+    if (slices > 1) {
+        addSlicesKernel<<<ceilDiv(s.n, 256), 256, 0, st>>>(t.slice_part, s.n, slices, t.idx, s.agrav);
+        t.walk_launches++;
+    }
     if (evalEnd) {
         cudaEventRecord(evalEnd, st);
     }
-    t.walk_launches++;
 }
 
 } // namespace sphgpu

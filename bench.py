@@ -330,12 +330,12 @@ def compare_fp64(args, st, mats, n, mixed_cfg, dev):
     return out
 
 
-# DRAM bytes (read + write) of one mixed walk of the default workload (the evaluation launch plus the launches
-# that build the interaction lists): a constant from a separate ncu capture of the same workload and command
-# (dram__bytes_read.sum + dram__bytes_write.sum), not measured in this run
+# DRAM bytes (read + write) of one launch of the walk's evaluation kernel on the default workload: a constant from
+# a separate ncu capture of the same workload and command (dram__bytes_read.sum + dram__bytes_write.sum, caches
+# flushed before the launch), not measured in this run
 WALK_TRAFFIC_BYTES = (240.2 + 27.7) * 1e6
 WALK_TRAFFIC_SOURCE = ("constant from an ncu capture of the evaluation kernel of one walk of this workload "
-                       "(dram__bytes_read.sum + dram__bytes_write.sum, profiles/evalListsKernel_impact1M.md); not "
+                       "(dram__bytes_read.sum + dram__bytes_write.sum, caches flushed before the launch); not "
                        "measured in this run")
 
 # FP32 operations of one particle-multipole evaluation (accMultipoleF, csrc/gravity32.cu: octupole) and the

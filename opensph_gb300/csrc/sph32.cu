@@ -257,9 +257,11 @@ struct MixedSelf {
     float rhoInv;
 };
 
+// compensated: the acceleration, energy and density (velocity divergence) rates; the velocity gradient, which
+// enters only the stress and damage rates, is summed plainly
 struct MixedSums {
     Kahan ax, ay, az, du, divv;
-    Kahan gv[6];
+    float gv[6] = { 0.f, 0.f, 0.f, 0.f, 0.f, 0.f };
     uint32_t cnt = 0;
 };
 
@@ -327,12 +329,12 @@ __device__ __forceinline__ void pairTermMixed(const Grid& g, const Physics& ph, 
                 hy = me.C[3] * gx + me.C[1] * gy + me.C[5] * gz;
                 hz = me.C[4] * gx + me.C[5] * gy + me.C[2] * gz;
             }
-            a.gv[0].add(mr * (dvx * hx));
-            a.gv[1].add(mr * (dvy * hy));
-            a.gv[2].add(mr * (dvz * hz));
-            a.gv[3].add(mr * (0.5f * (dvx * hy + dvy * hx)));
-            a.gv[4].add(mr * (0.5f * (dvx * hz + dvz * hx)));
-            a.gv[5].add(mr * (0.5f * (dvy * hz + dvz * hy)));
+            a.gv[0] += mr * (dvx * hx);
+            a.gv[1] += mr * (dvy * hy);
+            a.gv[2] += mr * (dvz * hz);
+            a.gv[3] += mr * (0.5f * (dvx * hy + dvy * hx));
+            a.gv[4] += mr * (0.5f * (dvx * hz + dvz * hx));
+            a.gv[5] += mr * (0.5f * (dvy * hz + dvz * hy));
             float tt[5];
             for (int k = 0; k < 5; ++k) {
                 tt[k] = me.S[k] + g.mxS[k * n + t];
@@ -366,7 +368,7 @@ __device__ __forceinline__ void finishMixed(const DState& s, const Grid& g, cons
     double Si[5] = { 0, 0, 0, 0, 0 };
     double gvd[6];
     for (int c = 0; c < 6; ++c) {
-        gvd[c] = a.gv[c].value();
+        gvd[c] = double(a.gv[c]);
     }
     if (Solid) {
         for (int c = 0; c < 5; ++c) {

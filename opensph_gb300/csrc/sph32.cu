@@ -293,7 +293,8 @@ __device__ __forceinline__ void pairTermMixed(const Grid& g, const Physics& ph, 
     const float d2 = drx * drx + dry * dry + drz * drz;
     const float hbar = 0.5f * (pi0.w + pj0.w);
     const float4 pj1 = g.mx1[t], pj2 = g.mx2[t], pj3 = g.mx3[t];
-    const float hInv = 1.f / hbar;
+    // (fast divisions: an error of about 2 ulp, below the rounding of the FP32 pair terms themselves)
+    const float hInv = __fdividef(1.f, hbar);
     const float h2 = hInv * hInv;
     const float gl = lutGradF(lut, d2 * h2) * (h2 * h2 * hInv);
     const float gx = drx * gl, gy = dry * gl, gz = drz * gl;
@@ -312,8 +313,8 @@ __device__ __forceinline__ void pairTermMixed(const Grid& g, const Physics& ph, 
     if (dvdr < 0.f) {
         const float rhobar = 0.5f * (pi2.w + rhoj);
         const float csbar = 0.5f * (pi3.y + pj3.y);
-        const float mu = hbar * dvdr / (d2 + 1.e-2f * (hbar * hbar));
-        const float av = (-float(ph.av_alpha) * csbar * mu + float(ph.av_beta) * (mu * mu)) / rhobar;
+        const float mu = __fdividef(hbar * dvdr, d2 + 1.e-2f * (hbar * hbar));
+        const float av = __fdividef(-float(ph.av_alpha) * csbar * mu + float(ph.av_beta) * (mu * mu), rhobar);
         fx -= av * gx;
         fy -= av * gy;
         fz -= av * gz;
@@ -380,7 +381,7 @@ __device__ __forceinline__ void finishMixed(const DState& s, const Grid& g, cons
 }
 
 template <bool Solid>
-__global__ void __launch_bounds__(PAIR_THREADS, 6) pairSumMixedKernel(DState s, Grid g, Physics ph,
+__global__ void __launch_bounds__(PAIR_THREADS, 8) pairSumMixedKernel(DState s, Grid g, Physics ph,
     const MaterialD* __restrict__ mats, const float* __restrict__ lut) {
     const uint32_t n = s.n;
     const uint32_t si = blockIdx.x * blockDim.x + threadIdx.x;

@@ -109,6 +109,35 @@ __device__ void eigenvalues(const double t[6], double sig[3]) {
     sig[2] = (t1 * cos((phi + 4. * SPH_PI) / 3.) - p3) * n;
 }
 
+// The largest eigenvalue of findEigenvalues' result for the mixed-precision path: the same characteristic
+// polynomial in FP64 with the divisions by constants and by the norm turned into products, and only the root
+// of cos(phi / 3), which is the largest for phi in [0, pi] (the reference forms all three roots and takes the
+// largest: the same value up to the last bits). The acos argument is clamped to [-1, 1] against rounding.
+__device__ double maxEigenvalueFast(const double t[6]) {
+    const double dx = t[0], dy = t[1], dz = t[2], ox = t[3], oy = t[4], oz = t[5];
+    const double mx = fmax(dx, ox), my = fmax(dy, oy), mz = fmax(dz, oz);
+    const double n = sqrtApproxRef(mx * mx + my * my + mz * mz);
+    if (n < 1.e-12) {
+        return 0.;
+    }
+    const double invN = 1. / n;
+    const double inv1 = dx + dy + dz;
+    const double inv2 = (ox * ox + oy * oy + oz * oz) - (dy * dz + dz * dx + dx * dy);
+    const double inv3 = dx * dy * dz + 2. * ox * oy * oz - ((ox * ox) * dz + (oy * oy) * dy + (oz * oz) * dx);
+    const double p = -inv1 * invN;
+    const double q = -inv2 * (invN * invN);
+    const double r = -inv3 * (invN * invN * invN);
+    const double a = q - p * p * (1. / 3.);
+    const double b = (2. * (p * p * p) - 9. * p * q + 27. * r) * (1. / 27.);
+    const double aCub = (a * a * a) * (1. / 27.);
+    if (0.25 * b * b + aCub >= 0.) {
+        return 0.;
+    }
+    const double t1 = 2. * sqrt(-a * (1. / 3.));
+    const double phi = acos(fmin(fmax(-0.5 * b * rsqrt(-aCub), -1.), 1.));
+    return (t1 * cos(phi * (1. / 3.)) - p * (1. / 3.)) * n;
+}
+
 // AdaptiveSmoothingLength::initialize (core/sph/equations/EquationTerm.cpp:356-364): h clamped to its range.
 // Applied with the position update, before the tree build reads h as the gravitational softening.
 __device__ __forceinline__ void clampSmoothingLength(const DState& s, const Physics& ph, uint32_t i) {
@@ -172,16 +201,20 @@ __device__ __forceinline__ void clampDeriv(double& x, double& dx, double lo, dou
 // AdaptiveSmoothingLength / ConstSmoothingLength (EquationTerm.cpp:366-391, 427-434), ContinuityEquation
 // (:289-316), SolidStressForce (:177-203), PressureForce (:90-99); then the fracture model of the material
 // (ScalarGradyKippModel::integrate, core/physics/Damage.cpp:128-170). Writes every highest derivative of
-// particle i from the pair sums (the reference zeroes them before the loop).
-template <bool Solid>
+// particle i from the pair sums (the reference zeroes them before the loop). Fast (the mixed-precision path):
+// the same terms with the divisions by constants and the repeated reciprocals of the density turned into
+// products and the largest principal stress from maxEigenvalueFast (results that differ in the last FP64 bits);
+// the FP64 path keeps the reference's operations.
+template <bool Solid, bool Fast = false>
 __device__ __forceinline__ void finalizeParticle(const DState& s, const Physics& ph, const MaterialD* __restrict__ mats,
     uint32_t i, const dbl4& ri, double rhoi, double pri, const double Si[5], double ax, double ay, double az,
     double du, double divv, const double gv[6], uint32_t cnt) {
     const uint32_t n = s.n;
     const MaterialD mt = mats[ph.nmat > 1 ? s.mat[i] : 0];
+    const double invRho = Fast ? 1. / rhoi : 0.;
     dbl4 vout = s.v[i];
     if (ph.adaptive_h) {
-        vout.w = ri.w > 2. * ph.h_lo ? ri.w / 3. * divv : 0.;
+        vout.w = ri.w > 2. * ph.h_lo ? (Fast ? ri.w * (1. / 3.) * divv : ri.w / 3. * divv) : 0.;
     } else {
         vout.w = 0.;
     }
@@ -197,9 +230,9 @@ __device__ __forceinline__ void finalizeParticle(const DState& s, const Physics&
         double dS[5] = { 0, 0, 0, 0, 0 };
         if (mt.yielding != SPHGPU_YIELDING_NONE) {
             const double szz = -Si[0] - Si[1];
-            du += 1. / rhoi * ((Si[0] * gv[0] + Si[1] * gv[1] + szz * gv[2]) +
-                                  2. * (Si[2] * gv[3] + Si[3] * gv[4] + Si[4] * gv[5]));
-            const double tr3 = (gv[0] * 1. + gv[1] * 1. + gv[2] * 1.) / 3.;
+            du += (Fast ? invRho : 1. / rhoi) * ((Si[0] * gv[0] + Si[1] * gv[1] + szz * gv[2]) +
+                                                    2. * (Si[2] * gv[3] + Si[3] * gv[4] + Si[4] * gv[5]));
+            const double tr3 = Fast ? (gv[0] + gv[1] + gv[2]) * (1. / 3.) : (gv[0] * 1. + gv[1] * 1. + gv[2] * 1.) / 3.;
             const double twoMu = 2. * mt.mu;
             dS[0] = 0. + twoMu * (gv[0] - tr3);
             dS[1] = 0. + twoMu * (gv[1] - tr3);
@@ -211,7 +244,7 @@ __device__ __forceinline__ void finalizeParticle(const DState& s, const Physics&
             s.dS[c * n + i] = dS[c];
         }
     }
-    du -= pri / rhoi * divv;
+    du -= (Fast ? pri * invRho : pri / rhoi) * divv;
     s.du[i] = du;
     if (Solid && ph.damage) {
         double dD = 0.;
@@ -221,12 +254,16 @@ __device__ __forceinline__ void finalizeParticle(const DState& s, const Physics&
                 dD = SPH_LARGE;
             } else {
                 const double sigma[6] = { Si[0] - pri, Si[1] - pri, (-Si[0] - Si[1]) - pri, Si[2], Si[3], Si[4] };
-                double sig[3];
-                eigenvalues(sigma, sig);
-                const double sigMax = fmax(fmax(sig[0], sig[1]), sig[2]);
+                double sigMax;
+                if (Fast) {
+                    sigMax = maxEigenvalueFast(sigma);
+                } else {
+                    double sig[3];
+                    eigenvalues(sigma, sig);
+                    sigMax = fmax(fmax(sig[0], sig[1]), sig[2]);
+                }
                 const double youngRed = fmax((1. - D * D * D) * mt.young, 1.e-20);
-                const double strain = sigMax / youngRed;
-                const double ratio = strain / s.eps_min[i];
+                const double ratio = Fast ? sigMax / (youngRed * s.eps_min[i]) : (sigMax / youngRed) / s.eps_min[i];
                 if (ratio > 1.) {
                     dD = s.growth[i] * cbrt(fmin(pow(ratio, s.m_zero[i]), double(s.n_flaws[i])));
                 }

@@ -376,7 +376,7 @@ __device__ __forceinline__ void finishMixed(const DState& s, const Grid& g, cons
             Si[c] = g.Ss[c * n + si];
         }
     }
-    finalizeParticle<Solid>(s, ph, mats, i, ri, rhoi, pri, Si, gax + a.ax.value(), gay + a.ay.value(),
+    finalizeParticle<Solid, true>(s, ph, mats, i, ri, rhoi, pri, Si, gax + a.ax.value(), gay + a.ay.value(),
         gaz + a.az.value(), a.du.value(), a.divv.value(), gvd, a.cnt);
 }
 

@@ -205,6 +205,9 @@ MaterialD toDevice(const sphgpu_material& m) {
     d.u_min = m.energy_min;
     d.s_min = m.stress_min;
     d.d_min = m.damage_min;
+    d.inv_rho0 = d.rho0 != 0. ? 1. / d.rho0 : 0.;
+    d.inv_u0 = d.u0 != 0. ? 1. / d.u0 : 0.;
+    d.inv_u_melt = d.u_melt != 0. ? 1. / d.u_melt : 0.;
     return d;
 }
 

@@ -40,6 +40,7 @@ struct MaterialD {
     double mu, limit, u_melt, young;
     double rho_lo, rho_hi, u_lo, u_hi, d_lo, d_hi;
     double rho_min, u_min, s_min, d_min; // IMaterial::minimal (derivative time-step criterion)
+    double inv_rho0, inv_u0, inv_u_melt;   // reciprocals (0 for a zero constant), for the mixed path's material update
 };
 
 // Uniform grid of the neighbour search (computed on the device each step)

@@ -14,7 +14,11 @@
 namespace sphgpu {
 namespace {
 
-__device__ void eosEval(const MaterialD& mt, double rho, double u, double& p, double& cs) {
+// Fast (the mixed-precision path): the same expressions with the reciprocals of the material constants, of the
+// density and of the denominator formed once and the divisions turned into products (FP64 results that differ in
+// the last bits); the FP64 path keeps the reference's divisions.
+template <bool Fast>
+__device__ void eosEvalT(const MaterialD& mt, double rho, double u, double& p, double& cs) {
     if (mt.eos == SPHGPU_EOS_IDEAL_GAS) {
         const double gamma = mt.gamma;
         p = (gamma - 1.) * u * rho;
@@ -23,28 +27,43 @@ __device__ void eosEval(const MaterialD& mt, double rho, double u, double& p, do
     }
     const double rho0 = mt.rho0, A = mt.A, B = mt.B, a = mt.a, b = mt.b, alpha = mt.alpha, beta = mt.beta;
     const double u0 = mt.u0, uiv = mt.uiv, ucv = mt.ucv;
-    const double eta = rho / rho0;
+    const double eta = Fast ? rho * mt.inv_rho0 : rho / rho0;
     const double mu = eta - 1.;
-    const double denom = u / (u0 * eta * eta) + 1.;
-    const double pc = (a + b / denom) * rho * u + A * mu + B * mu * mu;
-    double dpdu = a * rho + b * rho / (denom * denom);
-    double dpdrho = a * u + b * u * (3. * denom - 2.) / (denom * denom) + A / rho0 + 2. * B * mu / rho0;
-    const double csc = dpdrho + dpdu * pc / (rho * rho);
+    const double denom = Fast ? u * mt.inv_u0 * (1. / (eta * eta)) + 1. : u / (u0 * eta * eta) + 1.;
+    const double invDen = Fast ? 1. / denom : 0.;
+    const double invDen2 = invDen * invDen;
+    const double invRho = Fast ? 1. / rho : 0.;
+    const double invRho2 = invRho * invRho;
+    const double pc = (Fast ? a + b * invDen : a + b / denom) * rho * u + A * mu + B * mu * mu;
+    double dpdu = Fast ? a * rho + b * rho * invDen2 : a * rho + b * rho / (denom * denom);
+    double dpdrho = Fast ? a * u + b * u * (3. * denom - 2.) * invDen2 + A * mt.inv_rho0 + 2. * B * mu * mt.inv_rho0
+                         : a * u + b * u * (3. * denom - 2.) / (denom * denom) + A / rho0 + 2. * B * mu / rho0;
+    const double csc = Fast ? dpdrho + dpdu * pc * invRho2 : dpdrho + dpdu * pc / (rho * rho);
     double pp = pc, cc = csc;
     // the expanded phase enters only for rho <= rho0 above the incipient / complete vaporisation energies; it is
     // formed only then (the reference forms it always and uses it only then: the same values)
     const bool vapor = rho <= rho0 && u > ucv;
     const bool blend = rho <= rho0 && u > uiv && u <= ucv;
     if (vapor || blend) {
-        const double rhoExp = rho0 / rho - 1.;
+        const double rhoExp = Fast ? rho0 * invRho - 1. : rho0 / rho - 1.;
         const double betaExp = exp(-fmin(beta * rhoExp, 70.));
         const double alphaExp = exp(-fmin(alpha * (rhoExp * rhoExp), 70.));
-        const double pe = a * rho * u + (b * rho * u / denom + A * mu * betaExp) * alphaExp;
-        dpdu = a * rho + alphaExp * b * rho / (denom * denom);
-        dpdrho = a * u + alphaExp * (b * u * (3. * denom - 2.) / (denom * denom)) +
-                 alphaExp * (b * u * rho / denom) * rho0 * (2. * alpha * rhoExp) / (rho * rho) +
-                 alphaExp * A * betaExp * (1. / rho0 + rho0 * mu / (rho * rho) * (2. * alpha * rhoExp + beta));
-        double cse = dpdrho + dpdu * pe / (rho * rho);
+        double pe, cse;
+        if (Fast) {
+            pe = a * rho * u + (b * rho * u * invDen + A * mu * betaExp) * alphaExp;
+            dpdu = a * rho + alphaExp * b * rho * invDen2;
+            dpdrho = a * u + alphaExp * (b * u * (3. * denom - 2.) * invDen2) +
+                     alphaExp * (b * u * rho * invDen) * rho0 * (2. * alpha * rhoExp) * invRho2 +
+                     alphaExp * A * betaExp * (mt.inv_rho0 + rho0 * mu * invRho2 * (2. * alpha * rhoExp + beta));
+            cse = dpdrho + dpdu * pe * invRho2;
+        } else {
+            pe = a * rho * u + (b * rho * u / denom + A * mu * betaExp) * alphaExp;
+            dpdu = a * rho + alphaExp * b * rho / (denom * denom);
+            dpdrho = a * u + alphaExp * (b * u * (3. * denom - 2.) / (denom * denom)) +
+                     alphaExp * (b * u * rho / denom) * rho0 * (2. * alpha * rhoExp) / (rho * rho) +
+                     alphaExp * A * betaExp * (1. / rho0 + rho0 * mu / (rho * rho) * (2. * alpha * rhoExp + beta));
+            cse = dpdrho + dpdu * pe / (rho * rho);
+        }
         cse = fmax(cse, 0.);
         if (vapor) {
             pp = pe;
@@ -54,7 +73,7 @@ __device__ void eosEval(const MaterialD& mt, double rho, double u, double& p, do
             cc = ((u - uiv) * cse + (ucv - u) * csc) / (ucv - uiv);
         }
     }
-    cc = fmax(cc, 0.25 * A / rho0);
+    cc = fmax(cc, Fast ? 0.25 * A * mt.inv_rho0 : 0.25 * A / rho0);
     p = pp;
     cs = sqrt(cc);
 }
@@ -148,18 +167,20 @@ __device__ __forceinline__ void clampSmoothingLength(const DState& s, const Phys
     }
 }
 
-// materials initialize (EOS, von Mises) for particle i; does not read h
+// materials initialize (EOS, von Mises) for particle i; does not read h. Fast: the mixed path (eosEvalT<true>,
+// products by the reciprocals of u_melt and of sqrt(3 J2))
+template <bool Fast>
 __device__ void materialInit(const DState& s, const Physics& ph, const MaterialD* __restrict__ mats, uint32_t i) {
     const MaterialD mt = mats[ph.nmat > 1 ? s.mat[i] : 0];
     double p, cs;
-    eosEval(mt, s.rho[i], s.u[i], p, cs);
+    eosEvalT<Fast>(mt, s.rho[i], s.u[i], p, cs);
     if (ph.solid && mt.yielding != SPHGPU_YIELDING_NONE) {
         const uint32_t n = s.n;
         const double d = (s.D && mt.damage != SPHGPU_DAMAGE_NONE) ? s.D[i] * s.D[i] * s.D[i] : 0.;
         if (p < 0.) {
             p = (1. - d) * p;
         }
-        const double unorm = s.u[i] / mt.u_melt;
+        const double unorm = Fast ? s.u[i] * mt.inv_u_melt : s.u[i] / mt.u_melt;
         double Y = unorm < 1.e-5 ? mt.limit : mt.limit * fmax(1. - unorm, 0.);
         Y = (1. - d) * Y;
         double S[5];
@@ -173,7 +194,7 @@ __device__ void materialInit(const DState& s, const Physics& ph, const MaterialD
             }
         } else {
             const double J2 = 0.5 * ddotTT(S, S) + 1.e-15;
-            const double red = fmin(Y / sqrt(3. * J2), 1.);
+            const double red = fmin(Fast ? Y * rsqrt(3. * J2) : Y / sqrt(3. * J2), 1.);
             s.reduce[i] = red;
             for (int c = 0; c < 5; ++c) {
                 s.S[c * n + i] = S[c] * red;

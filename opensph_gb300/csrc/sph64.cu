@@ -30,7 +30,11 @@ namespace {
 __global__ void materialsInitKernel(DState s, Physics ph, const MaterialD* __restrict__ mats) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < s.n) {
-        materialInit(s, ph, mats, i);
+        if (ph.precision == SPHGPU_PRECISION_MIXED) {
+            materialInit<true>(s, ph, mats, i);
+        } else {
+            materialInit<false>(s, ph, mats, i);
+        }
     }
 }
 
@@ -315,6 +319,14 @@ __global__ void __launch_bounds__(128) pairSum64Kernel(DState s, Grid g, Physics
     finalizeParticle<Solid>(s, ph, mats, i, ri, rhoi, pri, Si, ax, ay, az, du, divv, gv, cnt);
 }
 
+// The mixed-precision path's integrator keeps its state and arithmetic in FP64 but forms the updates with fused
+// multiply-adds (this unit is otherwise compiled without contraction, so that the FP64 path's updates are the
+// reference's products and sums): fewer FP64 operations on a part whose FP64 rate is 1/64 of its FP32 rate,
+// results that differ from the FP64 path's in the last bits.
+__device__ __forceinline__ double updFma(double x, double dx, double k) {
+    return __fma_rn(dx, k, x);
+}
+
 // PredictorCorrector::makePredictions (TimeStepping.cpp:286-300) + materials initialize at the prediction
 __global__ void predictKernel(DState s, Physics ph, const MaterialD* __restrict__ mats, const double* __restrict__ dtp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -322,38 +334,51 @@ __global__ void predictKernel(DState s, Physics ph, const MaterialD* __restrict_
     if (i >= n) {
         return;
     }
+    const bool fast = ph.precision == SPHGPU_PRECISION_MIXED;
     const double dt = *dtp;
     const double dt2 = 0.5 * (dt * dt);
     dbl4 r = s.r[i], v = s.v[i];
     const dbl4 a = s.dv[i];
-    r.x += v.x * dt + a.x * dt2;
-    r.y += v.y * dt + a.y * dt2;
-    r.z += v.z * dt + a.z * dt2;
-    r.w += v.w * dt + a.w * dt2;
-    v.x += a.x * dt;
-    v.y += a.y * dt;
-    v.z += a.z * dt;
-    v.w += a.w * dt;
+    if (fast) {
+        r.x = updFma(updFma(r.x, v.x, dt), a.x, dt2);
+        r.y = updFma(updFma(r.y, v.y, dt), a.y, dt2);
+        r.z = updFma(updFma(r.z, v.z, dt), a.z, dt2);
+        r.w = updFma(updFma(r.w, v.w, dt), a.w, dt2);
+        v.x = updFma(v.x, a.x, dt);
+        v.y = updFma(v.y, a.y, dt);
+        v.z = updFma(v.z, a.z, dt);
+        v.w = updFma(v.w, a.w, dt);
+    } else {
+        r.x += v.x * dt + a.x * dt2;
+        r.y += v.y * dt + a.y * dt2;
+        r.z += v.z * dt + a.z * dt2;
+        r.w += v.w * dt + a.w * dt2;
+        v.x += a.x * dt;
+        v.y += a.y * dt;
+        v.z += a.z * dt;
+        v.w += a.w * dt;
+    }
     s.r[i] = r;
     s.v[i] = v;
     const MaterialD& mt = mats[ph.nmat > 1 ? s.mat[i] : 0];
     double rho = s.rho[i], drho = s.drho[i];
-    rho += drho * dt;
+    rho = fast ? updFma(rho, drho, dt) : rho + drho * dt;
     clampDeriv(rho, drho, mt.rho_lo, mt.rho_hi);
     s.rho[i] = rho;
     s.drho[i] = drho;
     double u = s.u[i], du = s.du[i];
-    u += du * dt;
+    u = fast ? updFma(u, du, dt) : u + du * dt;
     clampDeriv(u, du, mt.u_lo, mt.u_hi);
     s.u[i] = u;
     s.du[i] = du;
     if (ph.solid) {
         for (int c = 0; c < 5; ++c) {
-            s.S[c * n + i] += s.dS[c * n + i] * dt;
+            const double S = s.S[c * n + i], dS = s.dS[c * n + i];
+            s.S[c * n + i] = fast ? updFma(S, dS, dt) : S + dS * dt;
         }
         if (ph.damage) {
             double D = s.D[i], dD = s.dD[i];
-            D += dD * dt;
+            D = fast ? updFma(D, dD, dt) : D + dD * dt;
             clampDeriv(D, dD, mt.d_lo, mt.d_hi);
             s.D[i] = D;
             s.dD[i] = dD;
@@ -445,29 +470,44 @@ __global__ void correctKernel(DState s, Physics ph, const MaterialD* __restrict_
     const uint32_t n = s.n;
     double local = DBL_MAX;
     if (i < n) {
+        const bool fast = ph.precision == SPHGPU_PRECISION_MIXED;
         const double dt = *dtp;
         const double dt2 = 0.5 * (dt * dt);
         const double ca = 1. / 3., cb = 0.5;
+        // (mixed path) x - c (px - dx) dt as fma(px - dx, -c dt, x)
+        const double kr = -(ca * dt2), kv = -(cb * dt), kh = -(0.5 * dt);
         dbl4 r = s.r[i], v = s.v[i];
         const dbl4 pa = s.pdv[i], a = s.dv[i];
-        r.x -= ca * (pa.x - a.x) * dt2;
-        r.y -= ca * (pa.y - a.y) * dt2;
-        r.z -= ca * (pa.z - a.z) * dt2;
-        r.w -= ca * (pa.w - a.w) * dt2;
-        v.x -= cb * (pa.x - a.x) * dt;
-        v.y -= cb * (pa.y - a.y) * dt;
-        v.z -= cb * (pa.z - a.z) * dt;
-        v.w -= cb * (pa.w - a.w) * dt;
+        if (fast) {
+            const double ex = pa.x - a.x, ey = pa.y - a.y, ez = pa.z - a.z, ew = pa.w - a.w;
+            r.x = updFma(r.x, ex, kr);
+            r.y = updFma(r.y, ey, kr);
+            r.z = updFma(r.z, ez, kr);
+            r.w = updFma(r.w, ew, kr);
+            v.x = updFma(v.x, ex, kv);
+            v.y = updFma(v.y, ey, kv);
+            v.z = updFma(v.z, ez, kv);
+            v.w = updFma(v.w, ew, kv);
+        } else {
+            r.x -= ca * (pa.x - a.x) * dt2;
+            r.y -= ca * (pa.y - a.y) * dt2;
+            r.z -= ca * (pa.z - a.z) * dt2;
+            r.w -= ca * (pa.w - a.w) * dt2;
+            v.x -= cb * (pa.x - a.x) * dt;
+            v.y -= cb * (pa.y - a.y) * dt;
+            v.z -= cb * (pa.z - a.z) * dt;
+            v.w -= cb * (pa.w - a.w) * dt;
+        }
         s.r[i] = r;
         s.v[i] = v;
         const MaterialD& mt = mats[ph.nmat > 1 ? s.mat[i] : 0];
         double rho = s.rho[i], drho = s.drho[i];
-        rho -= 0.5 * (s.pdrho[i] - drho) * dt;
+        rho = fast ? updFma(rho, s.pdrho[i] - drho, kh) : rho - 0.5 * (s.pdrho[i] - drho) * dt;
         clampDeriv(rho, drho, mt.rho_lo, mt.rho_hi);
         s.rho[i] = rho;
         s.drho[i] = drho;
         double u = s.u[i], du = s.du[i];
-        u -= 0.5 * (s.pdu[i] - du) * dt;
+        u = fast ? updFma(u, s.pdu[i] - du, kh) : u - 0.5 * (s.pdu[i] - du) * dt;
         clampDeriv(u, du, mt.u_lo, mt.u_hi);
         s.u[i] = u;
         s.du[i] = du;
@@ -475,13 +515,14 @@ __global__ void correctKernel(DState s, Physics ph, const MaterialD* __restrict_
         if (ph.solid) {
             for (int c = 0; c < 5; ++c) {
                 dS[c] = s.dS[c * n + i];
-                S[c] = s.S[c * n + i] - 0.5 * (s.pdS[c * n + i] - dS[c]) * dt;
+                const double Sc = s.S[c * n + i], pdS = s.pdS[c * n + i];
+                S[c] = fast ? updFma(Sc, pdS - dS[c], kh) : Sc - 0.5 * (pdS - dS[c]) * dt;
                 s.S[c * n + i] = S[c];
             }
             if (ph.damage) {
                 D = s.D[i];
                 dD = s.dD[i];
-                D -= 0.5 * (s.pdD[i] - dD) * dt;
+                D = fast ? updFma(D, s.pdD[i] - dD, kh) : D - 0.5 * (s.pdD[i] - dD) * dt;
                 clampDeriv(D, dD, mt.d_lo, mt.d_hi);
                 s.D[i] = D;
                 s.dD[i] = dD;

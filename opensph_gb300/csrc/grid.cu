@@ -241,16 +241,18 @@ __global__ void gatherSortedMixed(DState st, const uint32_t* __restrict__ perm, 
     splitFloat(v.z, hz, lz);
     mx1[s] = make_float4(hx, hy, hz, float(st.m[i]));
     mx2[s] = make_float4(lx, ly, lz, float(rho));
-    const double rho2 = rho * rho;
+    // (the FP32 records take S / rho^2 and p / rho^2 from one FP64 reciprocal: the FP64 pipe runs at 1/64 of the
+    // FP32 rate on this part; the products round to the quotients' floats or to a neighbouring one)
+    const double invRho2 = 1. / (rho * rho);
     float red = 0.f, flg = 0.f;
     if (solid) {
         red = float(st.reduce[i]);
         flg = __uint_as_float(st.flag[i]);
         for (int c = 0; c < 5; ++c) {
-            mxS[c * n + s] = float(st.S[c * n + i] / rho2);
+            mxS[c * n + s] = float(st.S[c * n + i] * invRho2);
         }
     }
-    mx3[s] = make_float4(float(st.p[i] / rho2), float(st.cs[i]), red, flg);
+    mx3[s] = make_float4(float(st.p[i] * invRho2), float(st.cs[i]), red, flg);
 }
 
 // exact FP64 interaction test of SymmetricSolver::loop, no FMA contraction

@@ -105,6 +105,36 @@ __device__ void leafMoments(const dbl4* __restrict__ r, const double* __restrict
     reduceMoments(M2, M3, q2, q3);
 }
 
+// the mixed walk's leaf: FP32 moments about the centre of mass (as leafMoments<float>, only for a leaf with mass)
+// and, for every particle of the leaf, the evaluation inputs of the mixed walk: the position relative to the
+// centre of mass with half the smoothing length (pf) and G m (mf), from the same FP64 differences
+__device__ void leafMomentsMixed(const dbl4* __restrict__ r, const double* __restrict__ m, double G,
+    const uint32_t* __restrict__ idx, const BhNodeGeom& g, bool massive, float q2[6], float q3[10], float4* pf,
+    float* mf) {
+    float M2[6] = { 0, 0, 0, 0, 0, 0 }, M3[10] = { 0, 0, 0, 0, 0, 0, 0, 0, 0, 0 };
+    for (uint32_t k = g.from; k < g.to; ++k) {
+        const uint32_t i = idx[k];
+        const dbl4 p = r[i];
+        const float mi = float(G * m[i]);
+        const float d[3] = { float(p.x - g.com[0]), float(p.y - g.com[1]), float(p.z - g.com[2]) };
+        pf[k] = make_float4(d[0], d[1], d[2], 0.5f * float(p.w));
+        mf[k] = mi;
+        if (massive) {
+            for (int a = 0; a < 3; ++a) {
+                for (int b = a; b < 3; ++b) {
+                    M2[i2(a, b)] += (d[a] * d[b]) * mi;
+                    for (int c = b; c < 3; ++c) {
+                        M3[i3(a, b, c)] += (d[a] * d[b] * d[c]) * mi;
+                    }
+                }
+            }
+        }
+    }
+    if (massive) {
+        reduceMoments(M2, M3, q2, q3);
+    }
+}
+
 // BarnesHut::buildLeaf with FP64 moments, one thread per leaf
 __device__ void buildLeaf(const dbl4* __restrict__ r, const double* __restrict__ m, double G,
     const uint32_t* __restrict__ idx, double thetaInv, BhNodeGeom& g, BhNodeMoments& mo) {
@@ -229,16 +259,15 @@ __device__ __forceinline__ void readMomentsF(const float* nodef, int node, float
 template <bool Mixed>
 __device__ void momentsUpLeaf(const dbl4* __restrict__ r, const double* __restrict__ m, double G,
     const uint32_t* __restrict__ idx, double thetaInv, BhNodeGeom* geom, BhNodeMoments* mom, float* nodef, int node,
-    uint32_t* visits) {
+    uint32_t* visits, float4* pf, float* mf) {
     int parent;
     {
         BhNodeGeom g = geom[node];
         if (Mixed) {
             double m0;
             float q2[6] = { 0, 0, 0, 0, 0, 0 }, q3[10] = { 0, 0, 0, 0, 0, 0, 0, 0, 0, 0 };
-            if (buildLeafGeom(r, m, G, idx, thetaInv, g, m0)) {
-                leafMoments(r, m, G, idx, g, q2, q3);
-            }
+            const bool massive = buildLeafGeom(r, m, G, idx, thetaInv, g, m0);
+            leafMomentsMixed(r, m, G, idx, g, massive, q2, q3, pf, mf);
             mom[node].m0 = m0;
             writeMomentsF(nodef, node, q2, q3);
         } else {
@@ -291,10 +320,10 @@ template <bool Mixed>
 __global__ void momentsUpKernel(const dbl4* __restrict__ r, const double* __restrict__ m, double G,
     const uint32_t* __restrict__ idx, double thetaInv, BhNodeGeom* geom, BhNodeMoments* mom, float* nodef,
     const uint32_t* __restrict__ leaves, const uint32_t* __restrict__ leafCount, uint32_t maxLeaves,
-    uint32_t* visits) {
+    uint32_t* visits, float4* pf, float* mf) {
     const uint32_t nLeaves = min(*leafCount, maxLeaves);
     for (uint32_t li = blockIdx.x * blockDim.x + threadIdx.x; li < nLeaves; li += gridDim.x * blockDim.x) {
-        momentsUpLeaf<Mixed>(r, m, G, idx, thetaInv, geom, mom, nodef, int(leaves[li]), visits);
+        momentsUpLeaf<Mixed>(r, m, G, idx, thetaInv, geom, mom, nodef, int(leaves[li]), visits, pf, mf);
     }
 }
 
@@ -591,10 +620,10 @@ void launchMomentsDev(const DState& s, Tree& t, const Physics& ph, bool mixed, c
     const int blocks = std::max(1, std::min(grid, ceilDiv(s.n, 128)));
     if (mixed) {
         momentsUpKernel<true><<<blocks, 128, 0, st>>>(s.r, s.m, ph.G, t.idx, ph.theta_inv, t.geom, t.mom, t.nodef,
-            t.leaves, t.counters + C_LEAVES, s.n, t.visits);
+            t.leaves, t.counters + C_LEAVES, s.n, t.visits, t.pf, t.mf);
     } else {
         momentsUpKernel<false><<<blocks, 128, 0, st>>>(s.r, s.m, ph.G, t.idx, ph.theta_inv, t.geom, t.mom, t.nodef,
-            t.leaves, t.counters + C_LEAVES, s.n, t.visits);
+            t.leaves, t.counters + C_LEAVES, s.n, t.visits, t.pf, t.mf);
     }
 }
 

@@ -23,9 +23,8 @@ __device__ __forceinline__ void splitF(double x, float& hi, float& lo) {
     lo = float(x - double(hi));
 }
 
-__device__ void prepareNode(const dbl4* __restrict__ r, const double* __restrict__ m, double G,
-    const uint32_t* __restrict__ idx, const BhNodeGeom* __restrict__ geom, const BhNodeMoments* __restrict__ mom,
-    uint32_t id, float* __restrict__ nodef, float4* __restrict__ pf, float* __restrict__ mf, bool moments) {
+__device__ void prepareNode(const BhNodeGeom* __restrict__ geom, const BhNodeMoments* __restrict__ mom, uint32_t id,
+    float* __restrict__ nodef, bool moments) {
     const BhNodeGeom& g = geom[id];
     const BhNodeMoments& mo = mom[id];
     float4* o = reinterpret_cast<float4*>(nodef) + size_t(id) * NODEF4;
@@ -61,24 +60,14 @@ __device__ void prepareNode(const dbl4* __restrict__ r, const double* __restrict
     o[NF_BOX + 1] = make_float4(bl[0][0], bl[0][1], bl[0][2], 0.f);
     o[NF_BOX + 2] = make_float4(bh[1][0], bh[1][1], bh[1][2], 0.f);
     o[NF_BOX + 3] = make_float4(bl[1][0], bl[1][1], bl[1][2], 0.f);
-    if (g.left < 0) {
-        for (uint32_t k = g.from; k < g.to; ++k) {
-            const uint32_t i = idx[k];
-            const dbl4 p = r[i];
-            // w: half the smoothing length, so that a pair's symmetrised length is one addition
-            pf[k] = make_float4(float(p.x - g.com[0]), float(p.y - g.com[1]), float(p.z - g.com[2]), 0.5f * float(p.w));
-            mf[k] = float(G * m[i]);
-        }
-    }
+    // (the leaves' particle inputs of the mixed walk, pf and mf, are written by the mixed moments' leaf pass)
 }
 
-__global__ void prepareMixedKernel(const dbl4* __restrict__ r, const double* __restrict__ m, double G,
-    const uint32_t* __restrict__ idx, const BhNodeGeom* __restrict__ geom, const BhNodeMoments* __restrict__ mom,
-    const uint32_t* __restrict__ nodeCountDev, uint32_t nodeCapacity, float* __restrict__ nodef,
-    float4* __restrict__ pf, float* __restrict__ mf, bool moments) {
+__global__ void prepareMixedKernel(const BhNodeGeom* __restrict__ geom, const BhNodeMoments* __restrict__ mom,
+    const uint32_t* __restrict__ nodeCountDev, uint32_t nodeCapacity, float* __restrict__ nodef, bool moments) {
     const uint32_t nodeCount = min(*nodeCountDev, nodeCapacity);
     for (uint32_t id = blockIdx.x * blockDim.x + threadIdx.x; id < nodeCount; id += gridDim.x * blockDim.x) {
-        prepareNode(r, m, G, idx, geom, mom, id, nodef, pf, mf, moments);
+        prepareNode(geom, mom, id, nodef, moments);
     }
 }
 
@@ -698,8 +687,9 @@ void launchPrepareWalkDev(const DState& s, Tree& t, const Physics& ph, cudaStrea
     }
     // the node count is read on the device (counters[C_NODES]); at most 2 n nodes
     const int blocks = std::max(1, std::min(ceilDiv(t.node_capacity, 128), 152 * 16));
-    prepareMixedKernel<<<blocks, 128, 0, st>>>(s.r, s.m, ph.G, t.idx, t.geom, t.mom, t.counters + C_NODES, t.node_capacity,
-        t.nodef, t.pf, t.mf, !t.mixed_moments);
+    prepareMixedKernel<<<blocks, 128, 0, st>>>(t.geom, t.mom, t.counters + C_NODES, t.node_capacity, t.nodef,
+        !t.mixed_moments);
+    (void)ph;
 }
 
 // walk phase 1 for both precisions: the node, particle-list and kept lists of every node, level by level

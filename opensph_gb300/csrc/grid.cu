@@ -58,14 +58,39 @@ __global__ void boundsKernel(const dbl4* __restrict__ r, const double* __restric
         hm = max(hm, __shfl_xor_sync(0xffffffffu, hm, off));
         sum += __shfl_xor_sync(0xffffffffu, sum, off);
     }
+    // the warps' values combined in the block, one atomic per block and word (a few hundred blocks: the atomics
+    // on these words were the kernel's time with one per warp)
+    __shared__ unsigned long long sMn[32][3], sMx[32][3], sHm[32];
+    __shared__ double sSum[32];
+    const int w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
     if ((threadIdx.x & 31) == 0) {
         for (int k = 0; k < 3; ++k) {
-            atomicMin(&b[k], mn[k]);
-            atomicMax(&b[3 + k], mx[k]);
+            sMn[w][k] = mn[k];
+            sMx[w][k] = mx[k];
         }
-        atomicMax(&b[6], hm);
+        sHm[w] = hm;
+        sSum[w] = sum;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        const int k = threadIdx.x;
+        unsigned long long a = sMn[0][k], c = sMx[0][k];
+        for (int q = 1; q < nw; ++q) {
+            a = min(a, sMn[q][k]);
+            c = max(c, sMx[q][k]);
+        }
+        atomicMin(&b[k], a);
+        atomicMax(&b[3 + k], c);
+    } else if (threadIdx.x == 3) {
+        unsigned long long a = sHm[0];
+        double t = sSum[0];
+        for (int q = 1; q < nw; ++q) {
+            a = max(a, sHm[q]);
+            t += sSum[q];
+        }
+        atomicMax(&b[6], a);
         if (rad) {
-            atomicAdd(reinterpret_cast<double*>(&b[7]), sum);
+            atomicAdd(reinterpret_cast<double*>(&b[7]), t);
         }
     }
 }
@@ -392,7 +417,7 @@ void launchGridBuildRadius(const dbl4* r, const double* radius, uint32_t n, Grid
     g.launches = n > 0 ? 6 : 2;
     resetBounds<<<1, 32, 0, st>>>(g.bounds);
     if (n > 0) {
-        const int blocks = min(ceilDiv(n, 256), 152 * 8);
+        const int blocks = min(ceilDiv(n, 256), 152 * 2);
         boundsKernel<<<blocks, 256, 0, st>>>(r, radius, n, g.bounds);
     }
     gridSetupKernel<<<1, 1, 0, st>>>(g.bounds, g.cell_capacity, n, meanCell, fine ? 1 : 0, g.info);

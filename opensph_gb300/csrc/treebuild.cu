@@ -336,11 +336,26 @@ __global__ void boundsKernel(const dbl4* __restrict__ r, uint32_t n, unsigned lo
             mx[k] = max(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], off));
         }
     }
+    // the warps' extremes combined in the block, one atomic per block and coordinate (a few hundred blocks: the
+    // atomics on six words were the kernel's time with one per warp)
+    __shared__ unsigned long long sMn[32][3], sMx[32][3];
+    const int w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
     if ((threadIdx.x & 31) == 0) {
         for (int k = 0; k < 3; ++k) {
-            atomicMin(&b[k], mn[k]);
-            atomicMax(&b[3 + k], mx[k]);
+            sMn[w][k] = mn[k];
+            sMx[w][k] = mx[k];
         }
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        const int k = threadIdx.x;
+        unsigned long long a = sMn[0][k], c = sMx[0][k];
+        for (int q = 1; q < nw; ++q) {
+            a = min(a, sMn[q][k]);
+            c = max(c, sMx[q][k]);
+        }
+        atomicMin(&b[k], a);
+        atomicMax(&b[3 + k], c);
     }
 }
 
@@ -1303,7 +1318,7 @@ cudaError_t treeBuild(const DState& s, Tree& t, const Physics& ph, uint32_t* dev
     auto launched = [&](uint32_t k) { t.launches += k; };
     const uint32_t cc = t.chunk_capacity;
     resetBoundsKernel<<<1, 32, 0, st>>>(t.bbox);
-    boundsKernel<<<std::min(ceilDiv(n, 256), 152 * 8), 256, 0, st>>>(s.r, n, t.bbox);
+    boundsKernel<<<std::min(ceilDiv(n, 256), 152 * 2), 256, 0, st>>>(s.r, n, t.bbox);
     rootKernel<<<ceilDiv(n, 256), 256, 0, st>>>(s.r, n, t.elems, levelBufs(t, 0), t.queue, t.geom, t.counters, cc,
         t.seg_capacity, t.bbox, devError);
     cudaMemsetAsync(t.level_count, 0, TREE_MAX_LEVELS * sizeof(uint32_t), st);

@@ -181,6 +181,9 @@ __global__ void flagErrorKernel(uint32_t* devError, uint32_t bit) {
 // small per-warp staging lists and many warps; a node whose lists outgrow them is appended to the defer list and
 // left to the second pass (deferPass == 1), which runs only the deferred nodes with large staging lists. A node
 // that outgrows those too is a capacity error.
+constexpr uint32_t LIST_POOL_CHUNK = 512;
+constexpr uint32_t LIST_KEPT_CHUNK = 256;
+
 __global__ void __launch_bounds__(128, 8) listLevelKernel(const BhNodeGeom* __restrict__ geom,
     const float* __restrict__ nodef, const uint32_t* __restrict__ levelNodes, uint32_t first, uint32_t last,
     int deferPass, uint32_t* __restrict__ defer, uint32_t scratchWarps,
@@ -203,6 +206,16 @@ __global__ void __launch_bounds__(128, 8) listLevelKernel(const BhNodeGeom* __re
     const float4* nf = reinterpret_cast<const float4*>(nodef);
     // counters[4]: the number of deferred nodes of this level
     const uint32_t total = deferPass ? min(counters[4], last - first) : last - first;
+    // the warp's current chunks of the list pool and of the kept pool: a node's lists take their space
+    // from them, and a chunk is reserved with one atomic when the next node's lists do not fit (one returning
+    // atomic per node was about 0.1 ms of the list phase); the counters add up the reserved chunks
+    // (kept in shared memory: position and end of the pool chunk, of the kept chunk)
+    __shared__ uint32_t chunkSh[4][4];
+    uint32_t* ch = chunkSh[wib];
+    if (lane < 4) {
+        ch[lane] = 0;
+    }
+    __syncwarp();
     for (uint32_t k = warpGlobal; k < total; k += nWarps) {
         const uint32_t ev = deferPass ? defer[k] : levelNodes[first + k];
         const BhNodeGeom& eg = geom[ev];
@@ -287,9 +300,24 @@ __global__ void __launch_bounds__(128, 8) listLevelKernel(const BhNodeGeom* __re
         // pools to the need and build the lists again
         uint32_t base = 0, kbase = 0;
         if (lane == 0 && !overflow) {
-            base = atomicAdd(&counters[0], nN + nP);
-            kbase = nK ? atomicAdd(&counters[1 + parity], nK) : 0u;
-            atomicMax(&counters[3], kbase + nK);
+            const uint32_t need = nN + nP;
+            if (ch[0] + need > ch[1]) {
+                const uint32_t size = max(need, LIST_POOL_CHUNK);
+                ch[0] = atomicAdd(&counters[0], size);
+                ch[1] = ch[0] + size;
+            }
+            base = ch[0];
+            ch[0] += need;
+            if (nK) {
+                if (ch[2] + nK > ch[3]) {
+                    const uint32_t size = max(nK, LIST_KEPT_CHUNK);
+                    ch[2] = atomicAdd(&counters[1 + parity], size);
+                    ch[3] = ch[2] + size;
+                    atomicMax(&counters[3], ch[3]);
+                }
+                kbase = ch[2];
+                ch[2] += nK;
+            }
         }
         base = __shfl_sync(0xffffffffu, base, 0);
         kbase = __shfl_sync(0xffffffffu, kbase, 0);

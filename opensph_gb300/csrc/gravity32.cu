@@ -194,6 +194,12 @@ __global__ void __launch_bounds__(128, 8) listLevelKernel(const BhNodeGeom* __re
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const uint32_t warpGlobal = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    // the first launch of a level clears the kept-pool and deferred-node counters of the next level (the other
+    // parity), which no launch of this level uses
+    if (!deferPass && blockIdx.x == 0 && threadIdx.x == 0) {
+        counters[1 + (1 - parity)] = 0;
+        counters[6 + (1 - parity)] = 0;
+    }
     // the warps that have staging lists in the scratch (the grid is rounded up to whole blocks)
     const uint32_t nWarps = min((gridDim.x * blockDim.x) >> 5, scratchWarps);
     if (warpGlobal >= nWarps) {
@@ -204,8 +210,8 @@ __global__ void __launch_bounds__(128, 8) listLevelKernel(const BhNodeGeom* __re
     int32_t* lN = kept + cap;
     int32_t* lP = lN + cap;
     const float4* nf = reinterpret_cast<const float4*>(nodef);
-    // counters[4]: the number of deferred nodes of this level
-    const uint32_t total = deferPass ? min(counters[4], last - first) : last - first;
+    // counters[6 + parity]: the number of deferred nodes of this level
+    const uint32_t total = deferPass ? min(counters[6 + parity], last - first) : last - first;
     // the warp's current chunks of the list pool and of the kept pool: a node's lists take their space
     // from them, and a chunk is reserved with one atomic when the next node's lists do not fit (one returning
     // atomic per node was about 0.1 ms of the list phase); the counters add up the reserved chunks
@@ -291,7 +297,7 @@ __global__ void __launch_bounds__(128, 8) listLevelKernel(const BhNodeGeom* __re
         }
         if (overflow && !deferPass) {
             if (lane == 0) {
-                defer[atomicAdd(&counters[4], 1u)] = ev;
+                defer[atomicAdd(&counters[6 + parity], 1u)] = ev;
             }
             __syncwarp();
             continue;
@@ -372,6 +378,11 @@ __global__ void __launch_bounds__(LB_THREADS, 4) listBlockKernel(const BhNodeGeo
     const int tid = threadIdx.x;
     const int lane = tid & 31;
     const int w = tid >> 5;
+    // (as listLevelKernel's first launch: the next level's kept-pool and deferred-node counters)
+    if (blockIdx.x == 0 && tid == 0) {
+        counters[1 + (1 - parity)] = 0;
+        counters[6 + (1 - parity)] = 0;
+    }
     int32_t* cur = scratch + size_t(blockIdx.x) * 4 * cap;
     int32_t* kept = cur + cap;
     int32_t* lN = kept + cap;
@@ -766,10 +777,14 @@ void launchWalkLists(const DState& s, Tree& t, uint32_t* devError, cudaStream_t 
             const uint32_t first = t.level_first[level];
             const uint32_t last = t.level_first[level + 1];
             if (last <= first) {
+                // (no launch to clear the next level's counters: both parities' are cleared here)
+                cudaMemsetAsync(t.nl_counters + 1, 0, 2 * sizeof(uint32_t), st);
+                cudaMemsetAsync(t.nl_counters + 6, 0, 2 * sizeof(uint32_t), st);
                 continue;
             }
+            // (this level's kept-pool and deferred-node counters, counters[1 + parity] and counters[6 + parity],
+            // were cleared by the previous level's first launch, or by the clearing of all counters above)
             const int parity = int(level & 1u);
-            cudaMemsetAsync(t.nl_counters + 1 + parity, 0, sizeof(uint32_t), st);
             if (last - first <= deferWarps) {
                 // few nodes: a CTA per node with the large staging lists
                 listBlockKernel<<<last - first, LB_THREADS, 0, st>>>(t.geom, t.nodef, t.level_nodes, first, last,
@@ -779,7 +794,6 @@ void launchWalkLists(const DState& s, Tree& t, uint32_t* devError, cudaStream_t 
                 t.walk_launches++;
                 continue;
             }
-            cudaMemsetAsync(t.nl_counters + 4, 0, sizeof(uint32_t), st);
             const uint32_t warps = std::min(last - first, listWarps);
             listLevelKernel<<<ceilDiv(warps, 4), 128, 0, st>>>(t.geom, t.nodef, t.level_nodes, first, last, 0,
                 t.nl_defer, warps,

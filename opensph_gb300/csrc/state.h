@@ -289,8 +289,9 @@ struct Tree {
     int32_t* nl_kept[2] = { nullptr, nullptr }; // kept (undecided) lists of two consecutive levels
     uint32_t nl_kept_capacity = 0;
     uint32_t* nl_meta = nullptr;      // per node: N offset, N length, P offset, P length, kept offset, kept length
-    uint32_t* nl_counters = nullptr;  // device: pool entries used, kept entries used (two levels), max kept,
-                                      // deferred nodes of the level, a node's lists outgrew the staging
+    uint32_t* nl_counters = nullptr;  // device: [0] pool entries reserved, [1], [2] kept entries reserved (by level
+                                      // parity), [3] end of the kept entries, [5] a node's lists outgrew the
+                                      // staging, [6], [7] deferred nodes (by level parity)
     uint32_t* nl_host = nullptr;      // pinned mirror of nl_counters
     uint32_t* nl_defer = nullptr;     // nodes of a level whose lists outgrew the first pass's staging
     uint32_t walk_launches = 0;       // kernels launched by the last mixed walk
